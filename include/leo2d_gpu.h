@@ -1,0 +1,205 @@
+/*
+ * leo2d_gpu.h - C ABI of the GB300 implementation of LEO2D's Chebyshev
+ * kernel-polynomial-method (KPM) path.
+ *
+ * The reference (LEO2D) has no plugin interface for this path. Its worker runs,
+ * per job, three C++ calls (src/locality.cpp:3041-3148):
+ *   Locality::generateRealH      (src/locality.h:157, src/locality.cpp:3900)
+ *   Locality::computeDosKPM / computeDosTraceKPM
+ *                                (src/locality.h:173-176, src/locality.cpp:5945, 6138)
+ *   Locality::computeCondKPM     (src/locality.h:179, src/locality.cpp:6348)
+ * followed by Param_tools::densityTransform / densityTransformTrace /
+ * conductivityTransform (src/params/param_tools.h:16-81). The entry points
+ * below replace those calls one for one; each names the reference interface
+ * it stands in for.
+ *
+ * Rules (all entry points):
+ *  - Every function returns a leo2d_status; no C++ exception crosses the ABI.
+ *    The text of the last failure is leo2d_last_error(ctx).
+ *  - Host buffers are owned by the caller and are complete when the call
+ *    returns (calls synchronise the context's stream before returning).
+ *  - One context = one CUDA device + one stream. A context may be used by one
+ *    host thread at a time; use one context per thread.
+ *  - Sizes and indices that can exceed 2^31 are 64-bit.
+ *  - There is no CPU fallback: without a usable CUDA device every compute call
+ *    fails with LEO2D_ERR_CUDA.
+ */
+#ifndef LEO2D_GPU_H
+#define LEO2D_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LEO2D_ABI_VERSION 1
+#define LEO2D_MAX_SHEETS 8
+
+typedef enum {
+  LEO2D_OK = 0,
+  LEO2D_ERR_BAD_ARG = 1,     /* invalid argument (null pointer, size, poly_order % 4 != 0, ...) */
+  LEO2D_ERR_OOM = 2,         /* device or host allocation failed */
+  LEO2D_ERR_CUDA = 3,        /* CUDA runtime error or no device */
+  LEO2D_ERR_TIMEOUT = 4,     /* a bounded device-side wait ran out */
+  LEO2D_ERR_NONFINITE = 5,   /* NaN or Inf met in an input or a result */
+  LEO2D_ERR_UNSUPPORTED = 6, /* a reference option this build does not implement */
+  LEO2D_ERR_IO = 7           /* file could not be read or written */
+} leo2d_status;
+
+/* Tight-binding models. LEO2D_MODEL_REF is the reference's graphene
+ * (src/materials/graphene.h:77-95, graphene.cpp:13-222). LEO2D_MODEL_SIMPLE is
+ * nearest-neighbour graphene, a = 2.46 A, t = -2.7 eV, with interlayer
+ * t(r) = 0.33 exp(-(r - 3.35)/0.45) eV for 3-D distance r < 8 A. */
+typedef enum { LEO2D_MODEL_REF = 0, LEO2D_MODEL_SIMPLE = 1 } leo2d_model;
+
+/* Geometry of one job: what main.cpp:75-911 collects into Sdata/Job_params and
+ * Locality::setupSupercell (src/locality.cpp:130-293) completes. Fields marked
+ * "derived" are filled by leo2d_geom_prepare(). */
+typedef struct {
+  int32_t num_sheets;          /* NUM_SHEETS, 1..LEO2D_MAX_SHEETS */
+  int32_t model;               /* leo2d_model (MATERIAL = Graphene -> REF) */
+  int32_t boundary_condition;  /* BOUNDARY_CONDITION: 0 = disk flake, 1 = periodic supercell */
+  int32_t sc_search_size;      /* supercell images searched, default 1 (job_params.cpp:57) */
+  int32_t supercell_m;         /* SUPERCELL_M_N (periodic only) */
+  int32_t supercell_n;
+  int32_t min_shape[LEO2D_MAX_SHEETS][2]; /* MINSIZE per sheet (grid cells) */
+  int32_t max_shape[LEO2D_MAX_SHEETS][2]; /* MAXSIZE per sheet */
+  double max_R[LEO2D_MAX_SHEETS];         /* disk radius, A (MAXSIZE or MAX_R) */
+  double heights[LEO2D_MAX_SHEETS];       /* HEIGHT, A */
+  double angles[LEO2D_MAX_SHEETS];        /* ANGLE in radians (derived for periodic) */
+  double energy_rescale;                  /* H~ = (H + shift*I) / rescale, as generateRealH */
+  double energy_shift;
+  /* derived */
+  double lattice[LEO2D_MAX_SHEETS][2][2];       /* unrotated lattice vectors a1, a2 */
+  double sheet_supercell[LEO2D_MAX_SHEETS][2][2];
+  int32_t sheet_sc_stride[LEO2D_MAX_SHEETS][2][2];
+  double supercell[2][2];                       /* sheet 0's supercell (Job_params "supercell") */
+  int32_t prepared;
+} leo2d_geom;
+
+typedef struct leo2d_ctx leo2d_ctx;
+typedef struct leo2d_csr leo2d_csr;
+
+/* ---------------------------------------------------------------- context */
+
+/* Creates a context on CUDA device `device` with its own stream. */
+leo2d_status leo2d_ctx_create(leo2d_ctx** out, int device);
+leo2d_status leo2d_ctx_destroy(leo2d_ctx* ctx);
+/* Message of the last failure on this context ("" if none). */
+const char* leo2d_last_error(const leo2d_ctx* ctx);
+const char* leo2d_status_string(leo2d_status s);
+int leo2d_abi_version(void);
+/* The context's cudaStream_t, for callers that enqueue their own work. */
+void* leo2d_ctx_stream(leo2d_ctx* ctx);
+/* Iteration limit of every device-side spin wait (0 = library default).
+ * A wait that runs out makes the call return LEO2D_ERR_TIMEOUT. */
+leo2d_status leo2d_ctx_set_spin_limit(leo2d_ctx* ctx, uint64_t iterations);
+/* When enabled, kernels are bracketed by CUDA events on the context stream and
+ * per-kernel launch counts and device times are kept. */
+leo2d_status leo2d_ctx_set_profiling(leo2d_ctx* ctx, int enable);
+leo2d_status leo2d_ctx_kernel_stats(leo2d_ctx* ctx, const char* kernel,
+                                    int64_t* launches, double* total_ms);
+leo2d_status leo2d_ctx_reset_stats(leo2d_ctx* ctx);
+/* Total kernel launches made through this context since creation. */
+int64_t leo2d_ctx_launch_count(const leo2d_ctx* ctx);
+
+/* ---------------------------------------------------------------- geometry */
+
+/* Fills the derived fields of `g`: lattices, and for periodic jobs the
+ * supercell vectors, strides and sheet angles of Locality::setupSupercell
+ * type 1 (src/locality.cpp:153-293). Host-only. */
+leo2d_status leo2d_geom_prepare(leo2d_geom* g);
+
+/* ---------------------------------------------------------------- (a) assembly */
+
+#define LEO2D_CSR_KEEP_ZEROS 0x1u /* keep every stored entry of generateRealH (bit-exact layout) */
+#define LEO2D_CSR_WITH_DX 0x2u    /* also build dxH = (x_i - x_j) H_ij and dyH (locality.cpp:4182-4183) */
+
+/* Builds H~ on the device from the geometry: site enumeration
+ * (Sheet::setIndex, src/geom/sheet.cpp:217), intra- and interlayer pair
+ * search (Sheet::getIntraPairs sheet.cpp:624, Hstruct::getInterPairs
+ * src/geom/hstruct.cpp:298) and CSR assembly (Locality::generateRealH,
+ * src/locality.cpp:3900-4321). With LEO2D_CSR_KEEP_ZEROS the row pointers and
+ * column indices equal the reference's; without it entries whose value is
+ * exactly 0 are dropped (the layout the KPM kernels stream). */
+leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uint32_t flags,
+                             leo2d_csr** out);
+leo2d_status leo2d_csr_destroy(leo2d_csr* csr);
+/* n = orbitals, nnz = stored entries, pair counts as the reference's
+ * max_intra_pairs / max_inter_pairs (src/locality.cpp:946-947). */
+leo2d_status leo2d_csr_info(const leo2d_csr* csr, int64_t* n, int64_t* nnz,
+                            int64_t* n_intra_pairs, int64_t* n_inter_pairs);
+/* Copies the CSR to host arrays (any pointer may be NULL to skip it). */
+leo2d_status leo2d_csr_download(leo2d_ctx* ctx, const leo2d_csr* csr, int64_t* rowptr,
+                                int32_t* col, double* val, double* val_dx, double* val_dy);
+/* index_to_grid [n][4] = (i, j, orbital, sheet) as Hstruct::getIndexArray
+ * (hstruct.cpp:69-110); pos [n][3] = i2pos of setConfigPositions
+ * (locality.cpp:3618-3642, zero shifts). Either pointer may be NULL. */
+leo2d_status leo2d_csr_geometry(leo2d_ctx* ctx, const leo2d_csr* csr, int32_t* index_to_grid,
+                                double* pos);
+/* Uploads a host CSR (e.g. one generateRealH built) for the KPM calls. val_dx and
+ * pos may be NULL. Replaces SpMatrix::setup (src/matrix/spmatrix.cpp:154-175). */
+leo2d_status leo2d_csr_upload(leo2d_ctx* ctx, int64_t n, int64_t nnz, const int64_t* rowptr,
+                              const int32_t* col, const double* val, const double* val_dx,
+                              const double* pos, leo2d_csr** out);
+/* Gershgorin bounds of the stored matrix, FP64: emin = min_i (H_ii - sum_{j!=i}|H_ij|),
+ * emax = max_i (H_ii + sum_{j!=i}|H_ij|). */
+leo2d_status leo2d_csr_bounds(leo2d_ctx* ctx, const leo2d_csr* csr, double* emin, double* emax);
+/* In place: H <- (H + shift*I) / rescale (FP64, then the FP32 copy is refreshed). */
+leo2d_status leo2d_csr_rescale(leo2d_ctx* ctx, leo2d_csr* csr, double rescale, double shift);
+
+/* ---------------------------------------------------------------- (b) KPM DOS */
+
+typedef enum {
+  LEO2D_VEC_PHASE = 0,    /* complex random-phase vectors e^{i phi}, phi ~ U[0,2pi) from Philox4x32-10 */
+  LEO2D_VEC_HOST = 1,     /* real vectors supplied by the caller ([num_vectors][n], FP64) */
+  LEO2D_VEC_GAUSSIAN = 2  /* real N(0,1) vectors, Box-Muller on Philox4x32-10 */
+} leo2d_vec_kind;
+
+typedef enum { LEO2D_FP32 = 0, LEO2D_FP64 = 1 } leo2d_precision;
+
+typedef struct {
+  int32_t poly_order;    /* P (POLY_ORDER); a multiple of 4 (main.cpp:914-917) */
+  int32_t num_vectors;   /* R random vectors (KPM_TRACE_SAMPS) */
+  int32_t vector_kind;   /* leo2d_vec_kind */
+  int32_t precision;     /* leo2d_precision of the recursion; moments always sum in FP64 */
+  int32_t block;         /* vector-block width in columns per SpMM pass; 0 = autotuned */
+  int32_t rows_per_warp; /* 0 = autotuned */
+  uint64_t seed;         /* Philox key; vector v uses counter (v, row) */
+  uint64_t first_vector; /* index of the first vector (lets callers extend a run) */
+} leo2d_kpm_cfg;
+
+/* Stochastic-trace moments: mu_out[v][n] = <r_v| T_n(H~) |r_v> for v < R, n < P.
+ * Same recursion and moment doubling as Locality::computeDosTraceKPM
+ * (src/locality.cpp:6138-6346): T_{n+1} = 2 H~ T_n - T_{n-1},
+ * mu_{2n} = 2<T_n|T_n> - mu_0, mu_{2n+1} = 2<T_{n+1}|T_n> - mu_1.
+ * For LEO2D_VEC_HOST, host_vectors is [R][n] (the reference's kpm_trace_vectors). */
+leo2d_status leo2d_kpm_dos(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg,
+                           const double* host_vectors, double* mu_out);
+/* Site-resolved moments mu_out[t][n] = <e_t| T_n(H~) |e_t>, as
+ * Locality::computeDosKPM (src/locality.cpp:5945-6136). */
+leo2d_status leo2d_kpm_ldos(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg,
+                            const int64_t* targets, int64_t num_targets, double* mu_out);
+
+/* Param_tools::densityTransform (param_tools.cpp:661-705) for one moment set, or
+ * densityTransformTrace (707-768) when num_sets > 1 (mean over sets first):
+ * Jackson kernel, DCT-III, division by pi*sqrt(a^2 - (E_k - b)^2) at the P
+ * Chebyshev nodes E_k = shift + rescale*cos((k+1/2)pi/P), times `scale`.
+ * energies_out (may be NULL) receives E_k. FP64, on the device. */
+leo2d_status leo2d_dos_transform(leo2d_ctx* ctx, const double* mu, int32_t poly_order,
+                                 int32_t num_sets, double rescale, double shift, double scale,
+                                 double* dos_out, double* energies_out);
+/* Jackson-damped DOS on an arbitrary energy grid (FP64):
+ * dos(E) = scale * [g_0 mu_0 + 2 sum_n g_n mu_n T_n(x)] / (pi rescale sqrt(1-x^2)),
+ * x = (E - center) / rescale; zero outside |x| < 1. mu is the mean moment set. */
+leo2d_status leo2d_dos_reconstruct(leo2d_ctx* ctx, const double* mu, int32_t poly_order,
+                                   const double* energies, int64_t num_energies, double rescale,
+                                   double center, double scale, double* dos_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LEO2D_GPU_H */

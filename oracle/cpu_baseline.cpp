@@ -1,0 +1,69 @@
+/*
+ * cpu_baseline.cpp - the reference's CPU recursion, timed on host cores.
+ *
+ * TEST INFRASTRUCTURE ONLY (bench.py's cpu_baseline leg and its reference arm).
+ * The work per Chebyshev step is what Locality::computeDosTraceKPM does per
+ * vector (src/locality.cpp:6195-6234): one FP64 SpMV with the in-tree loop
+ * (src/matrix/spmatrix.cpp:346-360), the three-term update and the two
+ * doubling dot products. The reference runs one vector per MPI job and gets no
+ * threads of its own (no OpenMP, MKL absent); here disjoint vector sets run on
+ * `threads` host threads, standing in for one MPI worker per core.
+ */
+#include <chrono>
+#include <cstdint>
+#include <thread>
+#include <vector>
+
+extern "C" {
+
+/* Runs `steps` Chebyshev steps on `nvec` real vectors of length n and returns
+ * the wall time in seconds. Vectors are split across `threads` threads. The
+ * checksum of the last moments is written to *checksum so the work cannot be
+ * optimised away. */
+double oracle_cpu_kpm_steps(int64_t n, const int64_t* rp, const int32_t* col, const double* val,
+                            int32_t nvec, int32_t steps, int32_t threads, double* checksum) {
+  if (threads < 1) threads = 1;
+  std::vector<double> sums(nvec, 0.0);
+  auto work = [&](int v0, int v1) {
+    std::vector<double> Tp(n), Tj(n), Tn(n);
+    for (int v = v0; v < v1; ++v) {
+      for (int64_t i = 0; i < n; ++i) {
+        Tj[i] = (double)((i * 2654435761u + v) % 1000) / 1000.0 - 0.5;
+        Tp[i] = 0.0;
+      }
+      double acc = 0.0;
+      for (int s = 0; s < steps; ++s) {
+        for (int64_t r = 0; r < n; ++r) {
+          double temp_sum = 0;
+          for (int64_t i = rp[r]; i < rp[r + 1]; ++i) temp_sum += Tj[col[i]] * val[i];
+          Tn[r] = 2 * temp_sum + 0 * Tn[r];
+        }
+        double an_an = 0, anp_an = 0;
+        for (int64_t c = 0; c < n; ++c) {
+          Tn[c] = Tn[c] - Tp[c];
+          an_an += Tj[c] * Tj[c];
+          anp_an += Tn[c] * Tj[c];
+        }
+        acc += an_an + anp_an;
+        Tp.swap(Tj);
+        Tj.swap(Tn);
+      }
+      sums[v] = acc;
+    }
+  };
+  auto t0 = std::chrono::steady_clock::now();
+  std::vector<std::thread> th;
+  const int nt = threads < nvec ? threads : nvec;
+  for (int t = 0; t < nt; ++t) {
+    int v0 = (int)((int64_t)nvec * t / nt), v1 = (int)((int64_t)nvec * (t + 1) / nt);
+    th.emplace_back(work, v0, v1);
+  }
+  for (auto& x : th) x.join();
+  auto t1 = std::chrono::steady_clock::now();
+  double cs = 0;
+  for (double s : sums) cs += s;
+  if (checksum) *checksum = cs;
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
+}  // extern "C"

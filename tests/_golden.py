@@ -1,0 +1,80 @@
+"""Shared helpers: load golden fixtures and rebuild their geometry specs."""
+import gzip
+import math
+import os
+
+import numpy as np
+
+from leo2d_gb300._abi import Geom, MODEL_REF
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    with np.load(os.path.join(GOLDEN, name + ".npz")) as z:
+        return {k: z[k] for k in z.files}
+
+
+def e2e_text(name, suffix):
+    with gzip.open(os.path.join(GOLDEN, "e2e", name + suffix + ".gz"), "rt") as f:
+        return f.read()
+
+
+def parse_in(name):
+    """Reads a fixture's .in with the token rules of main.cpp:75-911 (subset).
+
+    Test helper only: the product parser is C++ (leo2d_gb300/host/input.cpp)
+    and is checked against the same files.
+    """
+    path = os.path.join(GOLDEN, "inputs", name + ".in")
+    g = Geom()
+    g.sc_search_size = 1
+    g.model = MODEL_REF
+    mn = mx = None
+    max_R = 0.0
+    height = angle = 0.0
+    cur = -1
+    kv = {"target_sheets": []}
+    for line in open(path):
+        tk = line.rstrip("\n").split(" ")
+        for p, key in enumerate(tk):
+            v = lambda k: tk[p + k] if p + k < len(tk) else ""
+            if key == "MAXSIZE":
+                mx = int(v(2)); max_R = float(mx)
+            elif key == "MINSIZE":
+                mn = int(v(2))
+            elif key == "MAX_R":
+                max_R = float(v(2))
+            elif key == "BOUNDARY_CONDITION":
+                g.boundary_condition = int(v(2))
+            elif key == "NUM_SHEETS":
+                g.num_sheets = int(v(2))
+            elif key == "SUPERCELL_M_N":
+                g.supercell_m, g.supercell_n = int(v(2)), int(v(3))
+            elif key == "START_SHEET":
+                cur = int(v(1)) - 1
+            elif key == "END_SHEET":
+                if cur == int(v(1)) - 1:
+                    g.heights[cur] = height
+                    g.angles[cur] = angle
+                    cur = -1
+            elif key == "MATERIAL":
+                g.min_shape[cur][0] = g.min_shape[cur][1] = mn
+                g.max_shape[cur][0] = g.max_shape[cur][1] = mx
+                g.max_R[cur] = max_R
+            elif key == "HEIGHT":
+                height = float(v(2))
+            elif key == "ANGLE":
+                angle = (2 * math.pi * float(v(2))) / (360.0)
+            elif key == "ENERGY_RESCALE":
+                g.energy_rescale = float(v(2))
+            elif key == "ENERGY_SHIFT":
+                g.energy_shift = float(v(2))
+            elif key == "POLY_ORDER":
+                kv["P"] = int(v(2))
+            elif key == "TARGET_SHEETS":
+                kv["target_sheets"] = [int(v(2)) - 1]
+    return g, kv
+
+
+CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
