@@ -1,0 +1,13 @@
+"""GB300 implementation of LEO2D's Chebyshev kernel-polynomial-method path.
+
+The product is libleo2d_gb300.so (C ABI in include/leo2d_gpu.h, CUDA kernels
+for sm_103a in csrc/, C++ host code in host/) and the `leo2d` driver built
+beside it. This package only builds and binds them.
+"""
+from ._abi import (CSR_KEEP_ZEROS, CSR_WITH_DX, FP32, FP64, MODEL_REF, MODEL_SIMPLE, VEC_GAUSSIAN,
+                   VEC_HOST, VEC_PHASE, Geom, KpmCfg, make_geom)
+from .api import Context, Csr, Leo2dError, kpm_cfg
+
+__all__ = ["Context", "Csr", "Leo2dError", "kpm_cfg", "Geom", "KpmCfg", "make_geom", "MODEL_REF",
+           "MODEL_SIMPLE", "VEC_PHASE", "VEC_HOST", "VEC_GAUSSIAN", "FP32", "FP64", "CSR_KEEP_ZEROS",
+           "CSR_WITH_DX"]

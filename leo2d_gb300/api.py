@@ -1,0 +1,187 @@
+"""Python view of the C ABI (include/leo2d_gpu.h) used by the tests and bench.
+
+Every call goes straight to libleo2d_gb300.so; failures raise Leo2dError with
+the library's status and message. There is no computation in Python and no
+fallback: without the library or a CUDA device the calls raise.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _abi
+from ._abi import Geom, KpmCfg
+
+
+class Leo2dError(RuntimeError):
+    def __init__(self, status, msg):
+        name = _abi.STATUS_NAMES[status] if 0 <= status < len(_abi.STATUS_NAMES) else str(status)
+        super().__init__(f"LEO2D_ERR_{name}: {msg}")
+        self.status = status
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Context:
+    def __init__(self, device=0):
+        self.lib = _abi.load()
+        h = ctypes.c_void_p()
+        st = self.lib.leo2d_ctx_create(ctypes.byref(h), device)
+        if st != _abi.OK:
+            raise Leo2dError(st, "leo2d_ctx_create failed (see stderr)")
+        self.h = h
+
+    def check(self, st):
+        if st != _abi.OK:
+            msg = self.lib.leo2d_last_error(self.h)
+            raise Leo2dError(st, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.leo2d_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- profiling -------------------------------------------------------
+    def set_profiling(self, on):
+        self.check(self.lib.leo2d_ctx_set_profiling(self.h, 1 if on else 0))
+
+    def kernel_stats(self, name):
+        n = ctypes.c_int64()
+        ms = ctypes.c_double()
+        self.check(self.lib.leo2d_ctx_kernel_stats(self.h, name.encode(), ctypes.byref(n),
+                                                   ctypes.byref(ms)))
+        return n.value, ms.value
+
+    def reset_stats(self):
+        self.check(self.lib.leo2d_ctx_reset_stats(self.h))
+
+    def launch_count(self):
+        return self.lib.leo2d_ctx_launch_count(self.h)
+
+    def set_spin_limit(self, n):
+        self.check(self.lib.leo2d_ctx_set_spin_limit(self.h, n))
+
+    # -- assembly --------------------------------------------------------
+    def prepare(self, geom):
+        g = Geom()
+        ctypes.memmove(ctypes.byref(g), ctypes.byref(geom), ctypes.sizeof(Geom))
+        self.check(self.lib.leo2d_geom_prepare(ctypes.byref(g)))
+        return g
+
+    def build_csr(self, geom, keep_zeros=False, with_dx=False):
+        g = geom if geom.prepared else self.prepare(geom)
+        flags = (_abi.CSR_KEEP_ZEROS if keep_zeros else 0) | (_abi.CSR_WITH_DX if with_dx else 0)
+        h = ctypes.c_void_p()
+        self.check(self.lib.leo2d_build_csr(self.h, ctypes.byref(g), flags, ctypes.byref(h)))
+        return Csr(self, h)
+
+    def upload_csr(self, rowptr, col, val, val_dx=None, pos=None):
+        rowptr = np.ascontiguousarray(rowptr, np.int64)
+        col = np.ascontiguousarray(col, np.int32)
+        val = np.ascontiguousarray(val, np.float64)
+        if val_dx is not None:
+            val_dx = np.ascontiguousarray(val_dx, np.float64)
+        if pos is not None:
+            pos = np.ascontiguousarray(pos, np.float64)
+        h = ctypes.c_void_p()
+        self.check(self.lib.leo2d_csr_upload(self.h, len(rowptr) - 1, len(col), _p(rowptr), _p(col),
+                                             _p(val), _p(val_dx), _p(pos), ctypes.byref(h)))
+        return Csr(self, h)
+
+    # -- transforms ------------------------------------------------------
+    def dos_transform(self, mu, P, rescale, shift, scale=1.0):
+        mu = np.ascontiguousarray(mu, np.float64).reshape(-1, P)
+        dos = np.zeros(P)
+        E = np.zeros(P)
+        self.check(self.lib.leo2d_dos_transform(self.h, _p(mu), P, mu.shape[0], rescale, shift,
+                                                scale, _p(dos), _p(E)))
+        return dos, E
+
+    def dos_reconstruct(self, mu, energies, rescale, center, scale=1.0):
+        mu = np.ascontiguousarray(mu, np.float64)
+        E = np.ascontiguousarray(energies, np.float64)
+        out = np.zeros(len(E))
+        self.check(self.lib.leo2d_dos_reconstruct(self.h, _p(mu), len(mu), _p(E), len(E), rescale,
+                                                  center, scale, _p(out)))
+        return out
+
+
+def kpm_cfg(P, R=1, kind=_abi.VEC_PHASE, precision=_abi.FP32, block=0, rows_per_warp=0, seed=0,
+            first_vector=0):
+    c = KpmCfg()
+    c.poly_order, c.num_vectors, c.vector_kind, c.precision = P, R, kind, precision
+    c.block, c.rows_per_warp, c.seed, c.first_vector = block, rows_per_warp, seed, first_vector
+    return c
+
+
+class Csr:
+    def __init__(self, ctx, h):
+        self.ctx = ctx
+        self.h = h
+        n, nnz, ni, ne = (ctypes.c_int64() for _ in range(4))
+        ctx.check(ctx.lib.leo2d_csr_info(h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(ni),
+                                         ctypes.byref(ne)))
+        self.n, self.nnz, self.n_intra, self.n_inter = n.value, nnz.value, ni.value, ne.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.leo2d_csr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def download(self, dx=False):
+        rp = np.zeros(self.n + 1, np.int64)
+        col = np.zeros(self.nnz, np.int32)
+        val = np.zeros(self.nnz)
+        vdx = np.zeros(self.nnz) if dx else None
+        vdy = np.zeros(self.nnz) if dx else None
+        self.ctx.check(self.ctx.lib.leo2d_csr_download(self.ctx.h, self.h, _p(rp), _p(col), _p(val),
+                                                       _p(vdx), _p(vdy)))
+        return (rp, col, val, vdx, vdy) if dx else (rp, col, val)
+
+    def geometry(self):
+        grid = np.zeros(4 * self.n, np.int32)
+        pos = np.zeros(3 * self.n)
+        self.ctx.check(self.ctx.lib.leo2d_csr_geometry(self.ctx.h, self.h, _p(grid), _p(pos)))
+        return grid, pos
+
+    def bounds(self):
+        lo, hi = ctypes.c_double(), ctypes.c_double()
+        self.ctx.check(self.ctx.lib.leo2d_csr_bounds(self.ctx.h, self.h, ctypes.byref(lo),
+                                                     ctypes.byref(hi)))
+        return lo.value, hi.value
+
+    def rescale(self, rescale, shift):
+        self.ctx.check(self.ctx.lib.leo2d_csr_rescale(self.ctx.h, self.h, rescale, shift))
+
+    def kpm_dos(self, cfg, host_vectors=None):
+        mu = np.zeros((cfg.num_vectors, cfg.poly_order))
+        hv = None if host_vectors is None else np.ascontiguousarray(host_vectors, np.float64)
+        self.ctx.check(self.ctx.lib.leo2d_kpm_dos(self.ctx.h, self.h, ctypes.byref(cfg), _p(hv),
+                                                  _p(mu)))
+        return mu
+
+    def kpm_ldos(self, cfg, targets):
+        t = np.ascontiguousarray(targets, np.int64)
+        mu = np.zeros((len(t), cfg.poly_order))
+        self.ctx.check(self.ctx.lib.leo2d_kpm_ldos(self.ctx.h, self.h, ctypes.byref(cfg), _p(t), len(t),
+                                                   _p(mu)))
+        return mu

@@ -1,0 +1,179 @@
+// common.cuh - context, errors, device buffers and launch helpers shared by
+// every translation unit of libleo2d_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <map>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/leo2d_gpu.h"
+
+namespace leo2d {
+
+struct Error : std::exception {
+  leo2d_status status;
+  std::string msg;
+  Error(leo2d_status s, std::string m) : status(s), msg(std::move(m)) {}
+  const char* what() const noexcept override { return msg.c_str(); }
+};
+
+[[noreturn]] inline void fail(leo2d_status s, const std::string& m) { throw Error(s, m); }
+
+#define LEO_CUDA(call)                                                                  \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      if (e_ == cudaErrorMemoryAllocation)                                              \
+        ::leo2d::fail(LEO2D_ERR_OOM, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+      ::leo2d::fail(LEO2D_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));  \
+    }                                                                                   \
+  } while (0)
+
+#define LEO_REQUIRE(cond, msg)                          \
+  do {                                                  \
+    if (!(cond)) ::leo2d::fail(LEO2D_ERR_BAD_ARG, msg); \
+  } while (0)
+
+// Owning device allocation (move-only).
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  explicit DevBuf(size_t count) { alloc(count); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void alloc(size_t count) {
+    release();
+    if (count == 0) return;
+    LEO_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    n = count;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+struct KStat {
+  int64_t launches = 0;
+  double ms = 0.0;
+};
+
+struct PendingTimer {
+  std::string name;
+  cudaEvent_t start, stop;
+};
+
+// Device-side status word written by bounded waits (see kStatus*).
+enum : int { kStatusOk = 0, kStatusTimeout = 1, kStatusNonfinite = 2, kStatusBadIndex = 3 };
+
+}  // namespace leo2d
+
+struct leo2d_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  uint64_t spin_limit = 1ull << 26;
+  bool profiling = false;
+  int sm_count = 0;
+  size_t l2_bytes = 0;
+  size_t smem_optin = 0;
+  std::map<std::string, leo2d::KStat> stats;
+  std::vector<leo2d::PendingTimer> pending;
+  std::vector<cudaEvent_t> free_events;
+  int64_t launches = 0;
+  leo2d::DevBuf<int> status;  // one int, reset before kernels that may set it
+};
+
+namespace leo2d {
+
+// Runs f, converting exceptions into a status and the context's last error.
+template <class F>
+leo2d_status guard(leo2d_ctx* ctx, F&& f) {
+  try {
+    f();
+    if (ctx) ctx->last_error.clear();
+    return LEO2D_OK;
+  } catch (const Error& e) {
+    if (ctx) ctx->last_error = e.msg;
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    if (ctx) ctx->last_error = "host allocation failed";
+    return LEO2D_ERR_OOM;
+  } catch (const std::exception& e) {
+    if (ctx) ctx->last_error = e.what();
+    return LEO2D_ERR_CUDA;
+  } catch (...) {
+    if (ctx) ctx->last_error = "unknown error";
+    return LEO2D_ERR_CUDA;
+  }
+}
+
+cudaEvent_t ctx_event(leo2d_ctx* ctx);
+// Synchronises the context stream and folds finished timers into the stats.
+void ctx_sync(leo2d_ctx* ctx);
+// Reads and clears the device status word; throws on a non-zero code.
+void ctx_check_status(leo2d_ctx* ctx, const char* where);
+
+// Launches `f` (which enqueues exactly one kernel on ctx->stream), counts it and,
+// when profiling is on, brackets it with CUDA events on the same stream.
+template <class F>
+void launch(leo2d_ctx* ctx, const char* name, F&& f) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (ctx->profiling) {
+    a = ctx_event(ctx);
+    b = ctx_event(ctx);
+    LEO_CUDA(cudaEventRecord(a, ctx->stream));
+  }
+  f();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) fail(LEO2D_ERR_CUDA, std::string("launch of ") + name + ": " + cudaGetErrorString(e));
+  ctx->launches += 1;
+  if (ctx->profiling) {
+    LEO_CUDA(cudaEventRecord(b, ctx->stream));
+    ctx->pending.push_back(PendingTimer{name, a, b});
+  } else {
+    ctx->stats[name].launches += 1;
+  }
+}
+
+inline unsigned grid_for(int64_t work, int per_block, int64_t cap = (1ll << 31) - 1) {
+  int64_t g = (work + per_block - 1) / per_block;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return (unsigned)g;
+}
+
+template <class T>
+void h2d(leo2d_ctx* ctx, T* dst, const T* src, size_t count) {
+  if (count) LEO_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+}
+template <class T>
+void d2h(leo2d_ctx* ctx, T* dst, const T* src, size_t count) {
+  if (count) LEO_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+}
+
+// Exclusive prefix sum of n int64 values: out[0..n] with out[n] = total.
+// `out` may alias `in` only if it is a distinct buffer of n+1 elements.
+void exclusive_scan_i64(leo2d_ctx* ctx, const int64_t* in, int64_t* out, int64_t n);
+
+// Sum of n int64 values (device), returned to the host.
+int64_t reduce_sum_i64(leo2d_ctx* ctx, const int64_t* in, int64_t n);
+
+}  // namespace leo2d

@@ -1,0 +1,844 @@
+// geom.cu - GPU assembly of the tight-binding Hamiltonian.
+//
+// Replaces, for one job with zero sheet shifts:
+//   Sheet::setIndex / posAtomGrid / checkShape   src/geom/sheet.cpp:217-285, 482-559
+//   Hstruct::setIndex / posAtomIndex / findNearest src/geom/hstruct.cpp:69-288
+//   Hstruct::getInterPairs (+ orderPairs)         src/geom/hstruct.cpp:298-666
+//   Sheet::getIntraPairs (+ orderPairs)           src/geom/sheet.cpp:624-849
+//   Locality::setConfigPositions (real space)     src/locality.cpp:3618-3642
+//   Locality::generateRealH                       src/locality.cpp:3900-4321
+// The CSR row pointers and column indices equal the reference's; values agree
+// to within rounding of the FP64 transcendental functions.
+//
+// This file is compiled with -fmad=false: the reference's x86-64 build never
+// fuses a multiply into an add, and site membership, search windows and the
+// 12.5 A pair cutoff depend on those roundings. Products of integers and
+// lattice constants, window arithmetic and squared distances are therefore
+// evaluated here in the same order and rounding as the reference.
+//
+// Work layout
+//   sites: one thread per grid cell (mask), device scan, one thread per site.
+//   flake rows (no periodic images, no duplicate pairs): one warp per row;
+//     candidates of the reference's search windows are evaluated 32 at a time
+//     and compacted with a ballot, so the row comes out in the reference's
+//     order without any sort. Two passes: count -> scan -> fill.
+//   periodic rows: one CTA per row; candidates of every supercell image are
+//     keyed (intra/inter, column, image), bitonic-sorted in shared memory -
+//     equal to the reference's stable bubble sort by column, because the
+//     image index is the generation order - and consecutive duplicates are
+//     merged in that order, as generateRealH does.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "csr.cuh"
+
+using namespace leo2d;
+
+namespace {
+
+constexpr int kMaxSheets = LEO2D_MAX_SHEETS;
+constexpr int kIntraSearch = 4;    // (int) Graphene::intra_search_radius (graphene.h:94)
+constexpr int kInterSearch = 6;    // (int) Graphene::inter_search_radius (graphene.h:95)
+constexpr double kInterCutoff = 12.5;  // hstruct.cpp:310
+
+struct SheetDev {
+  int min0, min1, max0, max1, H, W, n_orb;
+  int stride[2][2];
+  double max_R;
+  double a[2][2], atom[2][3], a_inv[2][2];
+  double sc[2][2], sc_inv[2][2];
+  double cos_t, sin_t;    // cos/sin(angle)   (host libm, as the reference)
+  double cos_mt, sin_mt;  // cos/sin(-angle)
+  double s1a[2][2];       // rotated lattice of setConfigPositions
+  double angle, height;
+  int64_t base;           // first global index of the sheet
+  const int32_t* grid;    // [H][W][n_orb] local index or -1
+};
+
+struct GeomDev {
+  int S, model, bc, sc_search, keep_zeros, with_dx;
+  double supercell[2][2];
+  double rescale, shift;
+  SheetDev sh[kMaxSheets];
+};
+
+__device__ __forceinline__ void pos_grid(const SheetDev& s, int i, int j, int l, double p[3]) {
+  const int ii = i + s.min0, jj = j + s.min1;
+  p[0] = ii * s.a[0][0] + jj * s.a[1][0] + s.atom[l][0];
+  p[1] = ii * s.a[0][1] + jj * s.a[1][1] + s.atom[l][1];
+  p[2] = s.atom[l][2];
+}
+
+// Sheet::checkShape; pow(x, 2) is x*x exactly in glibc.
+__device__ __forceinline__ bool check_shape(const SheetDev& s, int bc, const double p[3]) {
+  if (bc == 1) {
+    const double delta = 0.0, grid_delta = 0.000001;
+    double i = (p[0] + delta) * s.sc_inv[0][0] + (p[1] + delta) * s.sc_inv[0][1];
+    double j = (p[0] + delta) * s.sc_inv[1][0] + (p[1] + delta) * s.sc_inv[1][1];
+    return i >= 0.0 - grid_delta && i < 1.0 - grid_delta && j >= 0.0 - grid_delta &&
+           j < 1.0 - grid_delta;
+  }
+  return p[0] * p[0] + p[1] * p[1] < s.max_R * s.max_R;
+}
+
+__device__ __forceinline__ int grid_to_index(const SheetDev& s, int i, int j, int l) {
+  if (i >= 0 && i < s.H && j >= 0 && j < s.W && l >= 0 && l < s.n_orb)
+    return s.grid[((int64_t)i * s.W + j) * s.n_orb + l];
+  return -1;
+}
+
+// Sheet::findNearest (sheet frame)
+__device__ __forceinline__ int find_nearest_sheet(const SheetDev& s, const double p[3], int dim) {
+  if (dim == 0) {
+    double i_new = s.a_inv[0][0] * p[0] + s.a_inv[0][1] * p[1];
+    return min(max(int(floor(i_new)), s.min0), s.max0) - s.min0;
+  }
+  double j_new = s.a_inv[1][0] * p[0] + s.a_inv[1][1] * p[1];
+  return min(max(int(floor(j_new)), s.min1), s.max1) - s.min1;
+}
+
+// Hstruct::findNearest (global frame, rotated by -angle, zero shifts)
+__device__ __forceinline__ int find_nearest_h(const SheetDev& s, const double p[3], int dim) {
+  const double z0 = 0.0;
+  double x_new = p[0] * s.cos_mt - p[1] * s.sin_mt + z0 * s.a[0][0] + z0 * s.a[1][0];
+  double y_new = p[0] * s.sin_mt + p[1] * s.cos_mt + z0 * s.a[0][1] + z0 * s.a[1][1];
+  if (dim == 0) {
+    double i_new = s.a_inv[0][0] * x_new + s.a_inv[0][1] * y_new;
+    return min(max(int(floor(i_new)), s.min0), s.max0) - s.min0;
+  }
+  double j_new = s.a_inv[1][0] * x_new + s.a_inv[1][1] * y_new;
+  return min(max(int(floor(j_new)), s.min1), s.max1) - s.min1;
+}
+
+// Coupling::Intralayer::graphene (graphene.cpp:13-89) and the simple model.
+__device__ __forceinline__ double intralayer(int model, int orow, int ocol, int d0, int d1) {
+  int h0 = 2 * d0 + d1;
+  const int h1 = -1 * d0 + d1;
+  if (ocol == 0 && orow == 1) h0 -= 1;
+  else if (ocol == 1 && orow == 0) h0 += 1;
+  const int r = h0 * (h0 + h1) + h1 * h1;
+  if (model == LEO2D_MODEL_SIMPLE) return r == 1 ? -2.7 : 0.0;
+  switch (r) {
+    case 0: return 0.3504;
+    case 1: return -2.8922;
+    case 3: return 0.2425;
+    case 4: return -0.2656;
+    case 7: return 0.0235;
+    case 9: return 0.0524;
+    case 12: return -0.0209;
+    case 13: return -0.0148;
+    case 16: return -0.0211;
+    default: return 0.;
+  }
+}
+
+// Coupling::Interlayer::C_to_C (graphene.cpp:91-222). abs() at graphene.cpp:117
+// binds to the int overload in the reference, hence the truncation. The
+// fitted coefficients and the order of operations are the reference's.
+__device__ double c_to_c(int orow, int ocol, double v0, double v1, double v2, double theta_row,
+                         double theta_col) {
+  const double kPi = 3.14159265358979323846, kPi_6 = 0.523598775598298873077;
+  if (abs((int)v2) > 5) return 0;
+  double r = sqrt(v0 * v0 + v1 * v1);
+  if (r < 8.0) {
+    double ac = atan2(v1, v0);
+    double theta21 = ac - theta_row;
+    if (orow == 1) theta21 += kPi_6; else theta21 -= kPi_6;
+    double theta12 = ac - theta_col + kPi;
+    if (ocol == 1) theta12 += kPi_6; else theta12 -= kPi_6;
+    double rs = r / 2.4768;
+    double z_eq = 3.35;
+    double z_eps = (fabs(v2) - z_eq) / z_eq;
+    double lambda_0 = 0.310 - 1.882 * z_eps + 7.741 * z_eps * z_eps;
+    double xi_0 = 1.750 - 1.618 * z_eps + 1.848 * z_eps * z_eps;
+    double kappa_0 = 1.990 + 1.007 * z_eps + 2.427 * z_eps * z_eps;
+    double lambda_3 = -0.068 + 0.399 * z_eps - 1.739 * z_eps * z_eps;
+    double xi_3 = 3.286 - 0.914 * z_eps + 12.011 * z_eps * z_eps;
+    double x_3 = 0.500 + 0.322 * z_eps + 0.908 * z_eps * z_eps;
+    double lambda_6 = -0.008 + 0.046 * z_eps - 0.183 * z_eps * z_eps;
+    double xi_6 = 2.272 - 0.721 * z_eps - 4.414 * z_eps * z_eps;
+    double x_6 = 1.217 + 0.027 * z_eps - 0.658 * z_eps * z_eps;
+    double kappa_6 = 1.562 - 0.371 * z_eps - 0.134 * z_eps * z_eps;
+    double V0 = lambda_0 * exp(-xi_0 * (rs) * (rs)) * cos(kappa_0 * rs);
+    double V3 = lambda_3 * rs * rs * exp(-xi_3 * (rs - x_3) * (rs - x_3));
+    double V6 = lambda_6 * exp(-xi_6 * (rs - x_6) * (rs - x_6)) * sin(kappa_6 * rs);
+    double t = V0 + V3 * (cos(3 * theta12) + cos(3 * theta21)) + V6 * (cos(6 * theta12) + cos(6 * theta21));
+    double d = 8.0 - r;
+    if (d < 1. && d > 0.) t *= exp(1. - 1. / (d * d));
+    return t;
+  }
+  return 0.;
+}
+
+__device__ __forceinline__ double interlayer(int model, int orow, int ocol, double v0, double v1,
+                                             double v2, double th_row, double th_col) {
+  if (model == LEO2D_MODEL_SIMPLE) {
+    double r = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
+    return r < 8.0 ? 0.33 * exp(-(r - 3.35) / 0.45) : 0.0;
+  }
+  return c_to_c(orow, ocol, v0, v1, v2, th_row, th_col);
+}
+
+__device__ __forceinline__ int sheet_of(const GeomDev& G, int64_t k) {
+  int s = 0;
+  for (int t = 1; t < G.S; ++t)
+    if (k >= G.sh[t].base) s = t;
+  return s;
+}
+
+// ---------------------------------------------------------------- sites
+
+__global__ void k_site_mask(const __grid_constant__ GeomDev G, int s, int64_t* __restrict__ mask) {
+  const SheetDev& sh = G.sh[s];
+  const int64_t cells = (int64_t)sh.H * sh.W * sh.n_orb;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int l = (int)(c % sh.n_orb);
+    const int64_t ij = c / sh.n_orb;
+    const int j = (int)(ij % sh.W), i = (int)(ij / sh.W);
+    double p[3];
+    pos_grid(sh, i, j, l, p);
+    mask[c] = check_shape(sh, G.bc, p) ? 1 : 0;
+  }
+}
+
+__global__ void k_site_fill(int64_t cells, const int64_t* __restrict__ mask,
+                            const int64_t* __restrict__ scan, int32_t* __restrict__ grid,
+                            int32_t* __restrict__ site_cell) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    if (mask[c]) {
+      grid[c] = (int32_t)scan[c];
+      site_cell[scan[c]] = (int32_t)c;
+    } else {
+      grid[c] = -1;
+    }
+  }
+}
+
+// grid4 and i2pos of every orbital (Hstruct::setIndex, posAtomIndex, setConfigPositions).
+__global__ void k_sites(const __grid_constant__ GeomDev G, int64_t n,
+                        const int32_t* const* __restrict__ site_cells, int32_t* __restrict__ grid4,
+                        double* __restrict__ pos) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int s = sheet_of(G, k);
+    const SheetDev& sh = G.sh[s];
+    const int64_t c = site_cells[s][k - sh.base];
+    const int l = (int)(c % sh.n_orb);
+    const int64_t ij = c / sh.n_orb;
+    const int j = (int)(ij % sh.W), i = (int)(ij / sh.W);
+    grid4[4 * k + 0] = i;
+    grid4[4 * k + 1] = j;
+    grid4[4 * k + 2] = l;
+    grid4[4 * k + 3] = s;
+    double lp[3];
+    pos_grid(sh, i, j, l, lp);
+    const double z0 = 0.0;
+    // index_to_pos (Hstruct::posAtomIndex with zero sheet shifts)
+    double x = lp[0] * sh.cos_t - lp[1] * sh.sin_t + z0 * sh.a[0][0] + z0 * sh.a[1][0];
+    double y = lp[0] * sh.sin_t + lp[1] * sh.cos_t + z0 * sh.a[0][1] + z0 * sh.a[1][1];
+    double z = lp[2] + sh.height;
+    // i2pos (setConfigPositions with zero job shifts)
+    pos[3 * k + 0] = x + z0 * sh.s1a[0][0] + z0 * sh.s1a[1][0];
+    pos[3 * k + 1] = y + z0 * sh.s1a[0][1] + z0 * sh.s1a[1][1];
+    pos[3 * k + 2] = z;
+  }
+}
+
+// ---------------------------------------------------------------- flake rows
+
+struct RowOut {
+  int64_t* cnt_ent;
+  int64_t* cnt_intra;
+  int64_t* cnt_inter;
+  const int64_t* rowptr;
+  int32_t* col;
+  double* val;
+  double* dx;
+  double* dy;
+};
+
+template <bool kFill>
+__global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ GeomDev G, int64_t n,
+                                                    const int32_t* __restrict__ grid4,
+                                                    const double* __restrict__ pos, RowOut out) {
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n; row += warps) {
+    const int ih = grid4[4 * row], jh = grid4[4 * row + 1], l0 = grid4[4 * row + 2],
+              s = grid4[4 * row + 3];
+    const SheetDev& sh = G.sh[s];
+    const double x1 = pos[3 * row] + 0.0, y1 = pos[3 * row + 1] + 0.0, z1 = pos[3 * row + 2];
+    int64_t o = kFill ? out.rowptr[row] : 0;
+    int64_t n_ent = 0, n_intra = 0, n_inter = 0;
+
+    // intralayer: window [i0-4, i0+4) x [j0-4, j0+4) x orbitals, every candidate kept
+    {
+      double lp[3];
+      pos_grid(sh, ih, jh, l0, lp);
+      double ph[3] = {lp[0] + 0.0, lp[1] + 0.0, lp[2]};
+      const int i0 = find_nearest_sheet(sh, ph, 0), j0 = find_nearest_sheet(sh, ph, 1);
+      const int side = 2 * kIntraSearch;
+      const int nc = side * side * sh.n_orb;
+      for (int c0 = 0; c0 < nc; c0 += 32) {
+        const int c = c0 + (int)lane;
+        int64_t k2g = -1;
+        double t = 0.0;
+        if (c < nc) {
+          const int l = c % sh.n_orb;
+          const int j = j0 - kIntraSearch + (c / sh.n_orb) % side;
+          const int i = i0 - kIntraSearch + c / (sh.n_orb * side);
+          const int k2 = grid_to_index(sh, i, j, l);
+          if (k2 != -1) {
+            k2g = k2 + sh.base;
+            const double raw = intralayer(G.model, l0, l, i - ih, j - jh);
+            t = k2g == row ? (raw + G.shift) / G.rescale : raw / G.rescale;
+          }
+        }
+        const bool keep = k2g >= 0;
+        // without KEEP_ZEROS the diagonal stays so a later rescale can shift it
+        const bool store = keep && (G.keep_zeros || t != 0 || k2g == row);
+        const unsigned m = __ballot_sync(0xffffffffu, store);
+        n_intra += __popc(__ballot_sync(0xffffffffu, keep));
+        if (kFill && store) {
+          const int64_t e = o + __popc(m & lt_mask);
+          out.col[e] = (int32_t)k2g;
+          out.val[e] = t != 0 ? 0.0 + t : 0.0;
+          if (G.with_dx) {
+            const double x2 = pos[3 * k2g], y2 = pos[3 * k2g + 1];
+            out.dx[e] = t != 0 ? 0.0 + (x1 - x2) * t : 0.0;
+            out.dy[e] = t != 0 ? 0.0 + (y1 - y2) * t : 0.0;
+          }
+        }
+        o += __popc(m);
+        n_ent += __popc(m);
+      }
+    }
+
+    // interlayer: sheet below, then sheet above; window +-6 clipped; d_xy < 12.5 A
+    {
+      const double ph[3] = {x1, y1, z1};
+      for (int side_k = 0; side_k < 2; ++side_k) {
+        const int s0 = side_k == 0 ? s - 1 : s + 1;
+        if (s0 < 0 || s0 >= G.S) continue;
+        const SheetDev& o0 = G.sh[s0];
+        const int i0 = find_nearest_h(o0, ph, 0), j0 = find_nearest_h(o0, ph, 1);
+        const int ilo = max(0, i0 - kInterSearch), ihi = min(o0.H, i0 + kInterSearch);
+        const int jlo = max(0, j0 - kInterSearch), jhi = min(o0.W, j0 + kInterSearch);
+        if (ihi <= ilo || jhi <= jlo) continue;
+        const int wj = jhi - jlo;
+        const int nc = (ihi - ilo) * wj * o0.n_orb;
+        for (int c0 = 0; c0 < nc; c0 += 32) {
+          const int c = c0 + (int)lane;
+          int64_t k2g = -1;
+          double t = 0.0;
+          if (c < nc) {
+            const int l = c % o0.n_orb;
+            const int j = jlo + (c / o0.n_orb) % wj;
+            const int i = ilo + c / (o0.n_orb * wj);
+            const int k2 = grid_to_index(o0, i, j, l);
+            if (k2 != -1) {
+              const int64_t kk = k2 + o0.base;
+              const double x2 = pos[3 * kk], y2 = pos[3 * kk + 1];
+              if ((x2 - ph[0]) * (x2 - ph[0]) + (y2 - ph[1]) * (y2 - ph[1]) <
+                  kInterCutoff * kInterCutoff) {
+                k2g = kk;
+                if (kFill || !G.keep_zeros) {
+                  const double z2 = pos[3 * kk + 2];
+                  t = interlayer(G.model, l0, l, x2 - x1, y2 - y1, z2 - z1, sh.angle, o0.angle) /
+                      G.rescale;
+                }
+              }
+            }
+          }
+          const bool keep = k2g >= 0;
+          const bool store = keep && (G.keep_zeros || t != 0);
+          const unsigned m = __ballot_sync(0xffffffffu, store);
+          n_inter += __popc(__ballot_sync(0xffffffffu, keep));
+          if (kFill && store) {
+            const int64_t e = o + __popc(m & lt_mask);
+            out.col[e] = (int32_t)k2g;
+            out.val[e] = t != 0 ? 0.0 + t : 0.0;
+            if (G.with_dx) {
+              const double x2 = pos[3 * k2g], y2 = pos[3 * k2g + 1];
+              out.dx[e] = t != 0 ? 0.0 + (x1 - x2) * t : 0.0;
+              out.dy[e] = t != 0 ? 0.0 + (y1 - y2) * t : 0.0;
+            }
+          }
+          o += __popc(m);
+          n_ent += __popc(m);
+        }
+      }
+    }
+    if (!kFill && lane == 0) {
+      out.cnt_ent[row] = n_ent;
+      out.cnt_intra[row] = n_intra;
+      out.cnt_inter[row] = n_inter;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- periodic rows
+
+constexpr uint64_t kKeyInter = 1ull << 48;
+constexpr uint64_t kKeyPad = ~0ull;
+
+__device__ __forceinline__ void image_of(int img, int ss, int& dxs, int& dys) {
+  const int side = 2 * ss + 1;
+  dxs = img / side - ss;
+  dys = img % side - ss;
+}
+
+// Value of one candidate (row, k2, image), generateRealH's rescaling included.
+__device__ double periodic_value(const GeomDev& G, int64_t row, const int32_t* grid4,
+                                 const double* pos, bool inter, int64_t k2, int img,
+                                 double& x1, double& y1) {
+  int dxs, dys;
+  image_of(img, G.sc_search, dxs, dys);
+  const int ih = grid4[4 * row], jh = grid4[4 * row + 1], l0 = grid4[4 * row + 2],
+            s = grid4[4 * row + 3];
+  const double shx = dxs * G.supercell[0][0] + dys * G.supercell[1][0];
+  const double shy = dxs * G.supercell[0][1] + dys * G.supercell[1][1];
+  x1 = pos[3 * row] + shx;
+  y1 = pos[3 * row + 1] + shy;
+  const int i2 = grid4[4 * k2], j2 = grid4[4 * k2 + 1], l2 = grid4[4 * k2 + 2], s2 = grid4[4 * k2 + 3];
+  if (!inter) {
+    const SheetDev& sh = G.sh[s];
+    int gd0 = i2 - ih, gd1 = j2 - jh;
+    gd0 = gd0 - dxs * sh.stride[0][0] - dys * sh.stride[1][0];
+    gd1 = gd1 - dxs * sh.stride[0][1] - dys * sh.stride[1][1];
+    const double raw = intralayer(G.model, l0, l2, gd0, gd1);
+    return k2 == row ? (raw + G.shift) / G.rescale : raw / G.rescale;
+  }
+  const double z1 = pos[3 * row + 2];
+  const double x2 = pos[3 * k2], y2 = pos[3 * k2 + 1], z2 = pos[3 * k2 + 2];
+  return interlayer(G.model, l0, l2, x2 - x1, y2 - y1, z2 - z1, G.sh[s].angle, G.sh[s2].angle) /
+         G.rescale;
+}
+
+__device__ void block_bitonic_sort(uint64_t* keys, int n2) {
+  for (int k = 2; k <= n2; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const uint64_t a = keys[i], b = keys[ixj];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            keys[i] = b;
+            keys[ixj] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+template <bool kFill>
+__global__ void __launch_bounds__(256) k_periodic_rows(const __grid_constant__ GeomDev G, int64_t n,
+                                                       const int32_t* __restrict__ grid4,
+                                                       const double* __restrict__ pos, int cap,
+                                                       RowOut out, int* status) {
+  extern __shared__ uint64_t keys[];
+  __shared__ int cnt, n_intra_s, n_inter_s, n_run;
+  __shared__ int warp_sums[8];
+  const int ss = G.sc_search;
+  const int n_img = (2 * ss + 1) * (2 * ss + 1);
+  for (int64_t row = blockIdx.x; row < n; row += gridDim.x) {
+    if (threadIdx.x == 0) { cnt = 0; n_intra_s = 0; n_inter_s = 0; }
+    __syncthreads();
+    const int ih = grid4[4 * row], jh = grid4[4 * row + 1], l0 = grid4[4 * row + 2],
+              s = grid4[4 * row + 3];
+    const SheetDev& sh = G.sh[s];
+    double lp[3];
+    pos_grid(sh, ih, jh, l0, lp);
+    const double khx = pos[3 * row], khy = pos[3 * row + 1], khz = pos[3 * row + 2];
+
+    // intralayer candidates of every image (Sheet::getIntraPairs)
+    const int side = 2 * kIntraSearch;
+    const int per_img = side * side * sh.n_orb;
+    for (int c = threadIdx.x; c < n_img * per_img; c += blockDim.x) {
+      const int img = c / per_img, cc = c % per_img;
+      int dxs, dys;
+      image_of(img, ss, dxs, dys);
+      const double scx = dxs * sh.sc[0][0] + dys * sh.sc[1][0];
+      const double scy = dxs * sh.sc[0][1] + dys * sh.sc[1][1];
+      double ph[3] = {lp[0] + scx, lp[1] + scy, lp[2]};
+      const int i0 = find_nearest_sheet(sh, ph, 0), j0 = find_nearest_sheet(sh, ph, 1);
+      const int l = cc % sh.n_orb;
+      const int j = j0 - kIntraSearch + (cc / sh.n_orb) % side;
+      const int i = i0 - kIntraSearch + cc / (sh.n_orb * side);
+      const int k2 = grid_to_index(sh, i, j, l);
+      if (k2 == -1) continue;
+      int gd0 = i - ih, gd1 = j - jh;
+      gd0 = gd0 - dxs * sh.stride[0][0] - dys * sh.stride[1][0];
+      gd1 = gd1 - dxs * sh.stride[0][1] - dys * sh.stride[1][1];
+      const double raw = intralayer(G.model, l0, l, gd0, gd1);
+      const bool keep = raw != 0 || (dxs == 0 && dys == 0);
+      if (!keep) continue;
+      atomicAdd(&n_intra_s, 1);
+      const int64_t k2g = k2 + sh.base;
+      if (!G.keep_zeros) {
+        const double t = k2g == row ? (raw + G.shift) / G.rescale : raw / G.rescale;
+        if (t == 0 && k2g != row) continue;
+      }
+      const int slot = atomicAdd(&cnt, 1);
+      if (slot < cap) keys[slot] = ((uint64_t)k2g << 16) | (uint64_t)img;
+    }
+    // interlayer candidates of every image (Hstruct::getInterPairs)
+    for (int img = 0; img < n_img; ++img) {
+      int dxs, dys;
+      image_of(img, ss, dxs, dys);
+      const double scx = dxs * G.supercell[0][0] + dys * G.supercell[1][0];
+      const double scy = dxs * G.supercell[0][1] + dys * G.supercell[1][1];
+      const double ph[3] = {khx + scx, khy + scy, khz};
+      for (int side_k = 0; side_k < 2; ++side_k) {
+        const int s0 = side_k == 0 ? s - 1 : s + 1;
+        if (s0 < 0 || s0 >= G.S) continue;
+        const SheetDev& o0 = G.sh[s0];
+        const int i0 = find_nearest_h(o0, ph, 0), j0 = find_nearest_h(o0, ph, 1);
+        const int ilo = max(0, i0 - kInterSearch), ihi = min(o0.H, i0 + kInterSearch);
+        const int jlo = max(0, j0 - kInterSearch), jhi = min(o0.W, j0 + kInterSearch);
+        if (ihi <= ilo || jhi <= jlo) continue;
+        const int wj = jhi - jlo;
+        const int nc = (ihi - ilo) * wj * o0.n_orb;
+        for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+          const int l = c % o0.n_orb;
+          const int j = jlo + (c / o0.n_orb) % wj;
+          const int i = ilo + c / (o0.n_orb * wj);
+          const int k2 = grid_to_index(o0, i, j, l);
+          if (k2 == -1) continue;
+          const int64_t kk = k2 + o0.base;
+          const double x2 = pos[3 * kk], y2 = pos[3 * kk + 1];
+          if (!((x2 - ph[0]) * (x2 - ph[0]) + (y2 - ph[1]) * (y2 - ph[1]) <
+                kInterCutoff * kInterCutoff))
+            continue;
+          atomicAdd(&n_inter_s, 1);
+          if (!G.keep_zeros) {
+            double xx, yy;
+            const double t = periodic_value(G, row, grid4, pos, true, kk, img, xx, yy);
+            if (t == 0) continue;
+          }
+          const int slot = atomicAdd(&cnt, 1);
+          if (slot < cap) keys[slot] = kKeyInter | ((uint64_t)kk << 16) | (uint64_t)img;
+        }
+      }
+    }
+    __syncthreads();
+    const int m = cnt;
+    if (m > cap) {
+      if (threadIdx.x == 0) atomicExch(status, kStatusBadIndex);
+      __syncthreads();
+      continue;
+    }
+    int n2 = 1;
+    while (n2 < m) n2 <<= 1;
+    for (int i = m + threadIdx.x; i < n2; i += blockDim.x) keys[i] = kKeyPad;
+    __syncthreads();
+    block_bitonic_sort(keys, n2);
+
+    // one output entry per run of equal (intra/inter, column)
+    if (!kFill) {
+      int local = 0;
+      for (int p = threadIdx.x; p < m; p += blockDim.x)
+        if (p == m - 1 || (keys[p] >> 16) != (keys[p + 1] >> 16)) ++local;
+      if (threadIdx.x == 0) n_run = 0;
+      __syncthreads();
+      atomicAdd(&n_run, local);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        out.cnt_ent[row] = n_run;
+        out.cnt_intra[row] = n_intra_s;
+        out.cnt_inter[row] = n_inter_s;
+      }
+      __syncthreads();
+      continue;
+    }
+    // fill: ordered slots by a block-wide scan of run-end flags, chunk by chunk
+    int64_t base_out = out.rowptr[row];
+    for (int p0 = 0; p0 < m; p0 += blockDim.x) {
+      const int p = p0 + threadIdx.x;
+      const bool end = p < m && (p == m - 1 || (keys[p] >> 16) != (keys[p + 1] >> 16));
+      const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      const unsigned bal = __ballot_sync(0xffffffffu, end);
+      if (lane == 0) warp_sums[warp] = __popc(bal);
+      __syncthreads();
+      int before = 0, total = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        if (w < (int)warp) before += warp_sums[w];
+        total += warp_sums[w];
+      }
+      before += __popc(bal & ((1u << lane) - 1u));
+      if (end) {
+        int q = p;
+        while (q > 0 && (keys[q - 1] >> 16) == (keys[p] >> 16)) --q;
+        const bool inter = (keys[p] & kKeyInter) != 0;
+        const int64_t k2 = (int64_t)((keys[p] >> 16) & 0xffffffffull);
+        double v = 0.0, vdx = 0.0, vdy = 0.0;
+        for (int e = q; e <= p; ++e) {
+          const int img = (int)(keys[e] & 0xffffull);
+          double x1, y1;
+          const double t = periodic_value(G, row, grid4, pos, inter, k2, img, x1, y1);
+          if (t != 0) {
+            v += t;
+            vdx += (x1 - pos[3 * k2]) * t;
+            vdy += (y1 - pos[3 * k2 + 1]) * t;
+          }
+        }
+        const int64_t e = base_out + before;
+        out.col[e] = (int32_t)k2;
+        out.val[e] = v;
+        if (G.with_dx) {
+          out.dx[e] = vdx;
+          out.dy[e] = vdy;
+        }
+      }
+      base_out += total;
+      __syncthreads();
+    }
+  }
+}
+
+__global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+// ---------------------------------------------------------------- host
+
+void fill_sheet(const leo2d_geom& g, int s, SheetDev& d) {
+  d.min0 = g.min_shape[s][0];
+  d.min1 = g.min_shape[s][1];
+  d.max0 = g.max_shape[s][0];
+  d.max1 = g.max_shape[s][1];
+  d.H = d.max0 - d.min0;
+  d.W = d.max1 - d.min1;
+  d.n_orb = 2;
+  d.max_R = g.max_R[s];
+  const double a = g.model == LEO2D_MODEL_SIMPLE ? 2.46 : 2.4768;
+  for (int x = 0; x < 2; ++x)
+    for (int y = 0; y < 2; ++y) d.a[x][y] = g.lattice[s][x][y];
+  // Graphene::atom_pos (graphene.h:82-85)
+  d.atom[0][0] = 0.; d.atom[0][1] = 0.; d.atom[0][2] = 0.;
+  d.atom[1][0] = 0.5 * a; d.atom[1][1] = 0.288675134594812882255 * a; d.atom[1][2] = 0;
+  const double a11 = d.a[0][0], a12 = d.a[0][1], a21 = d.a[1][0], a22 = d.a[1][1];
+  const double det_a = a11 * a22 - a12 * a21;
+  d.a_inv[0][0] = a22 / det_a;
+  d.a_inv[0][1] = -a21 / det_a;
+  d.a_inv[1][0] = -a12 / det_a;
+  d.a_inv[1][1] = a11 / det_a;
+  std::memset(d.sc, 0, sizeof(d.sc));
+  std::memset(d.sc_inv, 0, sizeof(d.sc_inv));
+  std::memset(d.stride, 0, sizeof(d.stride));
+  if (g.boundary_condition == 1) {
+    for (int x = 0; x < 2; ++x)
+      for (int y = 0; y < 2; ++y) {
+        d.sc[x][y] = g.sheet_supercell[s][x][y];
+        d.stride[x][y] = g.sheet_sc_stride[s][x][y];
+      }
+    const double det = d.sc[0][0] * d.sc[1][1] - d.sc[0][1] * d.sc[1][0];
+    d.sc_inv[0][0] = d.sc[1][1] / det;
+    d.sc_inv[0][1] = -d.sc[1][0] / det;
+    d.sc_inv[1][0] = -d.sc[0][1] / det;
+    d.sc_inv[1][1] = d.sc[0][0] / det;
+  }
+  d.angle = g.angles[s];
+  d.height = g.heights[s];
+  d.cos_t = std::cos(d.angle);
+  d.sin_t = std::sin(d.angle);
+  const double mt = -d.angle;
+  d.cos_mt = std::cos(mt);
+  d.sin_mt = std::sin(mt);
+  for (int x = 0; x < 2; ++x) {
+    d.s1a[x][0] = std::cos(d.angle) * d.a[x][0] - std::sin(d.angle) * d.a[x][1];
+    d.s1a[x][1] = std::sin(d.angle) * d.a[x][0] + std::cos(d.angle) * d.a[x][1];
+  }
+  d.base = 0;
+  d.grid = nullptr;
+}
+
+void validate_geom(const leo2d_geom* g) {
+  LEO_REQUIRE(g, "geometry is NULL");
+  LEO_REQUIRE(g->prepared, "geometry not prepared: call leo2d_geom_prepare first");
+  LEO_REQUIRE(g->num_sheets >= 1 && g->num_sheets <= kMaxSheets, "num_sheets must be 1..8");
+  LEO_REQUIRE(g->model == LEO2D_MODEL_REF || g->model == LEO2D_MODEL_SIMPLE, "unknown model");
+  LEO_REQUIRE(g->boundary_condition == 0 || g->boundary_condition == 1,
+              "boundary_condition must be 0 or 1");
+  LEO_REQUIRE(g->energy_rescale != 0.0 && std::isfinite(g->energy_rescale),
+              "energy_rescale must be finite and non-zero");
+  LEO_REQUIRE(std::isfinite(g->energy_shift), "energy_shift must be finite");
+  for (int s = 0; s < g->num_sheets; ++s) {
+    LEO_REQUIRE(g->max_shape[s][0] > g->min_shape[s][0] && g->max_shape[s][1] > g->min_shape[s][1],
+                "MAXSIZE must exceed MINSIZE");
+    const int64_t cells = (int64_t)(g->max_shape[s][0] - g->min_shape[s][0]) *
+                          (g->max_shape[s][1] - g->min_shape[s][1]) * 2;
+    LEO_REQUIRE(cells < (1ll << 31), "grid too large");
+    LEO_REQUIRE(std::isfinite(g->angles[s]) && std::isfinite(g->heights[s]),
+                "angles and heights must be finite");
+  }
+  if (g->boundary_condition == 1)
+    LEO_REQUIRE(g->sc_search_size >= 0 && g->sc_search_size <= 3, "sc_search_size must be 0..3");
+}
+
+}  // namespace
+
+namespace leo2d {
+void csr_refresh_fp32(leo2d_ctx* ctx, leo2d_csr* csr) {
+  if (csr->nnz == 0) return;
+  csr->val32.alloc(csr->nnz);
+  launch(ctx, "to_f32", [&] {
+    k_to_f32<<<grid_for(csr->nnz, 256, (int64_t)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
+        csr->val64.p, csr->val32.p, csr->nnz);
+  });
+  if (csr->dx64.p) {
+    csr->dx32.alloc(csr->nnz);
+    launch(ctx, "to_f32", [&] {
+      k_to_f32<<<grid_for(csr->nnz, 256, (int64_t)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
+          csr->dx64.p, csr->dx32.p, csr->nnz);
+    });
+  }
+}
+}  // namespace leo2d
+
+extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uint32_t flags,
+                                        leo2d_csr** out) {
+  if (!ctx || !out) return LEO2D_ERR_BAD_ARG;
+  *out = nullptr;
+  leo2d_csr* csr = nullptr;
+  leo2d_status st = guard(ctx, [&] {
+    validate_geom(g);
+    LEO_CUDA(cudaSetDevice(ctx->device));
+    csr = new leo2d_csr();
+    csr->device = ctx->device;
+    csr->flags = flags;
+    csr->geom = *g;
+    csr->has_geom = true;
+    GeomDev G;
+    std::memset(&G, 0, sizeof(G));
+    G.S = g->num_sheets;
+    G.model = g->model;
+    G.bc = g->boundary_condition;
+    G.sc_search = g->boundary_condition == 1 ? g->sc_search_size : 0;
+    G.keep_zeros = (flags & LEO2D_CSR_KEEP_ZEROS) ? 1 : 0;
+    G.with_dx = (flags & LEO2D_CSR_WITH_DX) ? 1 : 0;
+    std::memcpy(G.supercell, g->supercell, sizeof(G.supercell));
+    G.rescale = g->energy_rescale;
+    G.shift = g->energy_shift;
+    for (int s = 0; s < G.S; ++s) fill_sheet(*g, s, G.sh[s]);
+
+    // sites of every sheet
+    std::vector<DevBuf<int32_t>> grids(G.S), site_cells(G.S);
+    int64_t n = 0;
+    for (int s = 0; s < G.S; ++s) {
+      SheetDev& d = G.sh[s];
+      const int64_t cells = (int64_t)d.H * d.W * d.n_orb;
+      DevBuf<int64_t> mask(cells), scan(cells + 1);
+      launch(ctx, "site_mask", [&] {
+        k_site_mask<<<grid_for(cells, 256, (int64_t)ctx->sm_count * 32), 256, 0, ctx->stream>>>(G, s, mask.p);
+      });
+      exclusive_scan_i64(ctx, mask.p, scan.p, cells);
+      int64_t count = 0;
+      d2h(ctx, &count, scan.p + cells, 1);
+      ctx_sync(ctx);
+      grids[s].alloc(cells);
+      site_cells[s].alloc(count > 0 ? count : 1);
+      launch(ctx, "site_fill", [&] {
+        k_site_fill<<<grid_for(cells, 256, (int64_t)ctx->sm_count * 32), 256, 0, ctx->stream>>>(
+            cells, mask.p, scan.p, grids[s].p, site_cells[s].p);
+      });
+      d.grid = grids[s].p;
+      d.base = n;
+      n += count;
+      ctx_sync(ctx);
+    }
+    LEO_REQUIRE(n < (1ll << 31) - 1, "more than 2^31-1 orbitals: column indices are 32-bit");
+    csr->n = n;
+    csr->grid4.alloc(4 * (size_t)std::max<int64_t>(n, 1));
+    csr->pos.alloc(3 * (size_t)std::max<int64_t>(n, 1));
+    DevBuf<const int32_t*> cell_ptrs(G.S);
+    std::vector<const int32_t*> hp(G.S);
+    for (int s = 0; s < G.S; ++s) hp[s] = site_cells[s].p;
+    h2d(ctx, cell_ptrs.p, hp.data(), G.S);
+    if (n > 0)
+      launch(ctx, "sites", [&] {
+        k_sites<<<grid_for(n, 256, (int64_t)ctx->sm_count * 32), 256, 0, ctx->stream>>>(
+            G, n, cell_ptrs.p, csr->grid4.p, csr->pos.p);
+      });
+
+    // count -> scan -> fill
+    DevBuf<int64_t> cnt_ent(std::max<int64_t>(n, 1)), cnt_intra(std::max<int64_t>(n, 1)),
+        cnt_inter(std::max<int64_t>(n, 1));
+    csr->rowptr.alloc(n + 1);
+    RowOut ro{cnt_ent.p, cnt_intra.p, cnt_inter.p, csr->rowptr.p, nullptr, nullptr, nullptr, nullptr};
+    int cap = 0;
+    size_t smem = 0;
+    if (G.bc == 1) {
+      const int n_img = (2 * G.sc_search + 1) * (2 * G.sc_search + 1);
+      int neigh = (G.S > 1) ? (G.S > 2 ? 2 : 1) : 0;
+      int need = n_img * ((2 * kIntraSearch) * (2 * kIntraSearch) * 2 +
+                          neigh * (2 * kInterSearch) * (2 * kInterSearch) * 2);
+      cap = 1;
+      while (cap < need) cap <<= 1;
+      smem = (size_t)cap * sizeof(uint64_t);
+      LEO_REQUIRE(smem <= ctx->smem_optin, "periodic search too large for shared memory");
+      LEO_CUDA(cudaFuncSetAttribute(k_periodic_rows<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      LEO_CUDA(cudaFuncSetAttribute(k_periodic_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    const unsigned rows_grid = grid_for(n, 8, (int64_t)ctx->sm_count * 64);
+    const unsigned cta_grid = grid_for(n, 1, (int64_t)ctx->sm_count * 8);
+    if (n > 0) {
+      if (G.bc == 0)
+        launch(ctx, "flake_rows_count", [&] {
+          k_flake_rows<false><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, ro);
+        });
+      else
+        launch(ctx, "periodic_rows_count", [&] {
+          k_periodic_rows<false><<<cta_grid, 256, smem, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p,
+                                                                       cap, ro, ctx->status.p);
+        });
+    }
+    ctx_check_status(ctx, "leo2d_build_csr (count)");
+    exclusive_scan_i64(ctx, cnt_ent.p, csr->rowptr.p, n);
+    int64_t nnz = 0;
+    d2h(ctx, &nnz, csr->rowptr.p + n, 1);
+    ctx_sync(ctx);
+    csr->nnz = nnz;
+    csr->n_intra = reduce_sum_i64(ctx, cnt_intra.p, n);
+    csr->n_inter = reduce_sum_i64(ctx, cnt_inter.p, n);
+    csr->col.alloc(std::max<int64_t>(nnz, 1));
+    csr->val64.alloc(std::max<int64_t>(nnz, 1));
+    if (G.with_dx) {
+      csr->dx64.alloc(std::max<int64_t>(nnz, 1));
+      csr->dy64.alloc(std::max<int64_t>(nnz, 1));
+    }
+    ro.col = csr->col.p;
+    ro.val = csr->val64.p;
+    ro.dx = csr->dx64.p;
+    ro.dy = csr->dy64.p;
+    if (n > 0) {
+      if (G.bc == 0)
+        launch(ctx, "flake_rows_fill", [&] {
+          k_flake_rows<true><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, ro);
+        });
+      else
+        launch(ctx, "periodic_rows_fill", [&] {
+          k_periodic_rows<true><<<cta_grid, 256, smem, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p,
+                                                                      cap, ro, ctx->status.p);
+        });
+    }
+    ctx_check_status(ctx, "leo2d_build_csr (fill)");
+    csr_refresh_fp32(ctx, csr);
+    ctx_sync(ctx);
+  });
+  if (st != LEO2D_OK) {
+    delete csr;
+    return st;
+  }
+  *out = csr;
+  return LEO2D_OK;
+}

@@ -1,0 +1,665 @@
+// kpm.cu - the fused Chebyshev step: CSR SpMM over a block of vectors with the
+// three-term update and the moment dot products in one pass.
+//
+// Replaces the inner loop of Locality::computeDosTraceKPM / computeDosKPM
+// (src/locality.cpp:6195-6234, 5997-6033): SpMatrix::vectorMultiply
+// (src/matrix/spmatrix.cpp:346-360), the T_{n+1} = 2 H~ T_n - T_{n-1} loop and the
+// dots <T_n|T_n>, <T_{n+1}|T_n> of the moment doubling.
+//
+// Layout in HBM
+//   H~   CSR: rowptr int64[n+1], col int32[nnz], val fp32[nnz] (fp64 in FP64 mode)
+//   T    two row-major blocks n x C (C real columns: a complex random-phase
+//        vector is two columns, re and im). One row of a block is C*4 bytes
+//        contiguous, so a gather of row `col` by the lanes of a group is one
+//        coalesced 128..512-byte read.
+// Kernel
+//   A warp owns 32/LPR row slots; the LPR lanes of a slot own V consecutive
+//   columns each (C = LPR*V). Column indices and values of a row are loaded
+//   LPR at a time (coalesced, streaming cache hint: the matrix is read once per
+//   step and must not evict the vector block from L2), broadcast with shuffles
+//   and used to gather T_n rows with 16/8/4-byte vector loads.
+//   Epilogue: T_{n+1} = a H~T_n - T_{n-1} is written over T_{n-1} (each row is
+//   read and written by its own slot only), and <T_n|T_n>, <T_{n+1}|T_n> are
+//   accumulated per column: FP32 within a work item (<= 16 rows), FP64 across
+//   items, warps and blocks.
+//   The grid is persistent (a multiple of the SM count); work items of
+//   `rows_per_item` consecutive row slots are taken in grid-stride order so the
+//   rows in flight form one band and their gathered neighbours stay in L2.
+//   Block partials of step k are reduced, in fixed order, by the first 2C blocks
+//   of step k+1 (deterministic, no extra launch per step).
+// The step launches of a whole recursion are captured in one CUDA graph.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <tuple>
+
+#include "kpm.cuh"
+
+using namespace leo2d;
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+
+template <typename T, int V>
+struct VT;
+template <> struct VT<float, 1> { using t = float; };
+template <> struct VT<float, 2> { using t = float2; };
+template <> struct VT<float, 4> { using t = float4; };
+template <> struct VT<double, 1> { using t = double; };
+template <> struct VT<double, 2> { using t = double2; };
+
+template <typename T, int V>
+struct Pack {
+  T v[V];
+};
+
+template <typename T, int V>
+__device__ __forceinline__ Pack<T, V> ld_gather(const T* p) {
+  using vt = typename VT<T, V>::t;
+  vt x = __ldg(reinterpret_cast<const vt*>(p));
+  Pack<T, V> r;
+  memcpy(&r, &x, sizeof(r));
+  return r;
+}
+
+template <typename T, int V>
+__device__ __forceinline__ Pack<T, V> ld_plain(const T* p) {
+  using vt = typename VT<T, V>::t;
+  vt x = *reinterpret_cast<const vt*>(p);
+  Pack<T, V> r;
+  memcpy(&r, &x, sizeof(r));
+  return r;
+}
+
+template <typename T, int V>
+__device__ __forceinline__ void st_plain(T* p, const Pack<T, V>& r) {
+  using vt = typename VT<T, V>::t;
+  vt x;
+  memcpy(&x, &r, sizeof(r));
+  *reinterpret_cast<vt*>(p) = x;
+}
+
+template <typename T>
+struct StepArgs {
+  int64_t n;
+  const int64_t* __restrict__ rowptr;
+  const int32_t* __restrict__ col;
+  const T* __restrict__ val;
+  const T* __restrict__ tn;  // T_n (gathered)
+  T* __restrict__ tp;        // T_{n-1} in, T_{n+1} out
+  int first;                 // step 0: T_1 = H~ T_0
+  int rows_per_item;
+  double* __restrict__ partials;             // this step: [grid][C][2]
+  const double* __restrict__ prev_partials;  // previous step's partials, or null
+  double* __restrict__ prev_dots;            // where the previous step's dots go
+};
+
+// Fixed-order tree reduction of partials[b][t] over b < nb into out[t], for the
+// values t assigned to this block.
+template <int C>
+__device__ __forceinline__ void reduce_prev(const double* __restrict__ partials,
+                                            double* __restrict__ out, int nb) {
+  __shared__ double red[kThreads];
+  for (int t = blockIdx.x; t < 2 * C; t += gridDim.x) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nb; b += kThreads) s += __ldcg(partials + (size_t)b * 2 * C + t);
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kThreads / 2; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[t] = red[0];
+    __syncthreads();
+  }
+}
+
+template <typename T, int V, int LPR>
+__global__ void __launch_bounds__(kThreads, 3) k_cheb_step(const StepArgs<T> a) {
+  constexpr int C = V * LPR;
+  constexpr int RPW = 32 / LPR;
+  using Acc = T;  // FP32 recursion accumulates rows in FP32, FP64 mode in FP64
+  if (a.prev_partials) reduce_prev<C>(a.prev_partials, a.prev_dots, gridDim.x);
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int slot = lane / LPR, sub = lane % LPR;
+  const unsigned gmask = LPR == 32 ? 0xffffffffu : (((1u << LPR) - 1u) << (slot * LPR));
+  const int64_t item_rows = (int64_t)a.rows_per_item * RPW;
+  const int64_t n_items = (a.n + item_rows - 1) / item_rows;
+  const int64_t warps_total = (int64_t)gridDim.x * kWarps;
+  const T alpha = a.first ? T(1) : T(2);
+
+  double d0[V], d1[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) d0[v] = d1[v] = 0.0;
+
+  for (int64_t item = (int64_t)blockIdx.x * kWarps + warp; item < n_items; item += warps_total) {
+    Acc f0[V], f1[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) f0[v] = f1[v] = Acc(0);
+    for (int r = 0; r < a.rows_per_item; ++r) {
+      const int64_t row = item * item_rows + (int64_t)r * RPW + slot;
+      const bool valid = row < a.n;
+      const int64_t beg = valid ? a.rowptr[row] : 0;
+      const int64_t end = valid ? a.rowptr[row + 1] : 0;
+      T acc[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) acc[v] = T(0);
+      for (int64_t p = beg; p < end; p += LPR) {
+        const int cnt = (end - p) < (int64_t)LPR ? (int)(end - p) : LPR;
+        int c_mine = 0;
+        T v_mine = T(0);
+        if (sub < cnt) {
+          c_mine = __ldcs(a.col + p + sub);
+          v_mine = __ldcs(a.val + p + sub);
+        }
+        int k = 0;
+        for (; k + 4 <= cnt; k += 4) {
+          int c[4];
+          T w[4];
+          Pack<T, V> x[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            c[u] = __shfl_sync(gmask, c_mine, k + u, LPR);
+            w[u] = __shfl_sync(gmask, v_mine, k + u, LPR);
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) x[u] = ld_gather<T, V>(a.tn + (int64_t)c[u] * C + sub * V);
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[v] += w[u] * x[u].v[v];
+        }
+        for (; k < cnt; ++k) {
+          const int c = __shfl_sync(gmask, c_mine, k, LPR);
+          const T w = __shfl_sync(gmask, v_mine, k, LPR);
+          const Pack<T, V> x = ld_gather<T, V>(a.tn + (int64_t)c * C + sub * V);
+#pragma unroll
+          for (int v = 0; v < V; ++v) acc[v] += w * x.v[v];
+        }
+      }
+      if (valid) {
+        const int64_t off = row * C + sub * V;
+        const Pack<T, V> xn = ld_gather<T, V>(a.tn + off);
+        Pack<T, V> y;
+        if (a.first) {
+#pragma unroll
+          for (int v = 0; v < V; ++v) y.v[v] = alpha * acc[v];
+        } else {
+          const Pack<T, V> xp = ld_plain<T, V>(a.tp + off);
+#pragma unroll
+          for (int v = 0; v < V; ++v) y.v[v] = alpha * acc[v] - xp.v[v];
+        }
+        st_plain<T, V>(a.tp + off, y);
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          f0[v] += xn.v[v] * xn.v[v];
+          f1[v] += y.v[v] * xn.v[v];
+        }
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      d0[v] += (double)f0[v];
+      d1[v] += (double)f1[v];
+    }
+  }
+
+  // combine the row slots of the warp (lanes with equal `sub`)
+#pragma unroll
+  for (int o = LPR; o < 32; o <<= 1)
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      d0[v] += __shfl_xor_sync(0xffffffffu, d0[v], o);
+      d1[v] += __shfl_xor_sync(0xffffffffu, d1[v], o);
+    }
+  __shared__ double wsum[kWarps][2 * C];
+  if (slot == 0) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      wsum[warp][2 * (sub * V + v)] = d0[v];
+      wsum[warp][2 * (sub * V + v) + 1] = d1[v];
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < 2 * C; t += kThreads) {
+    double s = 0.0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) s += wsum[w][t];
+    a.partials[(size_t)blockIdx.x * 2 * C + t] = s;
+  }
+}
+
+template <int C>
+__global__ void __launch_bounds__(kThreads) k_reduce_partials(const double* __restrict__ partials,
+                                                              double* __restrict__ out, int nb) {
+  reduce_prev<C>(partials, out, nb);
+}
+
+// ---------------------------------------------------------------- start vectors
+
+__device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+    const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+// Random-phase columns: complex vector j of the block -> columns 2j (cos), 2j+1 (sin).
+template <typename T>
+__global__ void k_fill_phase(int64_t n, int C, T* __restrict__ x, uint64_t seed, uint64_t first,
+                             int n_complex) {
+  const int64_t total = n * C;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = e / C;
+    const int c = (int)(e % C);
+    const int j = c >> 1;
+    T out = T(0);
+    if (j < n_complex) {
+      const uint64_t vv = first + (uint64_t)j;
+      uint32_t ctr[4] = {(uint32_t)row, (uint32_t)((uint64_t)row >> 32), (uint32_t)vv, (uint32_t)(vv >> 32)};
+      philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32));
+      const double u = (double)(ctr[0] >> 8) * (1.0 / 16777216.0);
+      const double phi = 6.283185307179586 * u;
+      const double s = (c & 1) ? sin(phi) : cos(phi);
+      out = (T)(float)s;
+    }
+    x[e] = out;
+  }
+}
+
+// Gaussian columns (Box-Muller on Philox).
+template <typename T>
+__global__ void k_fill_gauss(int64_t n, int C, T* __restrict__ x, uint64_t seed, uint64_t first,
+                             int n_vec) {
+  const int64_t total = n * C;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = e / C;
+    const int c = (int)(e % C);
+    T out = T(0);
+    if (c < n_vec) {
+      const uint64_t vv = first + (uint64_t)c;
+      uint32_t ctr[4] = {(uint32_t)row, (uint32_t)((uint64_t)row >> 32), (uint32_t)vv, (uint32_t)(vv >> 32)};
+      philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32));
+      const double u1 = ((double)(ctr[0] >> 8) + 1.0) * (1.0 / 16777216.0);
+      const double u2 = (double)(ctr[1] >> 8) * (1.0 / 16777216.0);
+      const double z = sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+      out = sizeof(T) == 4 ? (T)(float)z : (T)z;
+    }
+    x[e] = out;
+  }
+}
+
+// Host vectors [R][n] (FP64) -> block columns.
+template <typename T>
+__global__ void k_fill_from(int64_t n, int C, T* __restrict__ x, const double* __restrict__ src,
+                            int n_vec) {
+  const int64_t total = n * C;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = e / C;
+    const int c = (int)(e % C);
+    x[e] = c < n_vec ? (T)src[(int64_t)c * n + row] : T(0);
+  }
+}
+
+template <typename T>
+__global__ void k_fill_unit(int64_t n, int C, T* __restrict__ x, const int64_t* __restrict__ targets,
+                            int n_t) {
+  const int64_t total = n * C;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = e / C;
+    const int c = (int)(e % C);
+    x[e] = (c < n_t && targets[c] == row) ? T(1) : T(0);
+  }
+}
+
+// ---------------------------------------------------------------- dispatch
+
+template <typename T, int V, int LPR>
+void launch_step_t(leo2d_ctx* ctx, unsigned grid, const StepArgs<T>& a) {
+  launch(ctx, "cheb_step", [&] { k_cheb_step<T, V, LPR><<<grid, kThreads, 0, ctx->stream>>>(a); });
+}
+
+template <typename T>
+void launch_step(leo2d_ctx* ctx, int cols, unsigned grid, const StepArgs<T>& a);
+
+template <>
+void launch_step<float>(leo2d_ctx* ctx, int cols, unsigned grid, const StepArgs<float>& a) {
+  switch (cols) {
+    case 8: return launch_step_t<float, 1, 8>(ctx, grid, a);
+    case 16: return launch_step_t<float, 1, 16>(ctx, grid, a);
+    case 32: return launch_step_t<float, 1, 32>(ctx, grid, a);
+    case 64: return launch_step_t<float, 2, 32>(ctx, grid, a);
+    case 128: return launch_step_t<float, 4, 32>(ctx, grid, a);
+  }
+  fail(LEO2D_ERR_BAD_ARG, "FP32 block width must be 8, 16, 32, 64 or 128 columns");
+}
+
+template <>
+void launch_step<double>(leo2d_ctx* ctx, int cols, unsigned grid, const StepArgs<double>& a) {
+  switch (cols) {
+    case 8: return launch_step_t<double, 1, 8>(ctx, grid, a);
+    case 16: return launch_step_t<double, 1, 16>(ctx, grid, a);
+    case 32: return launch_step_t<double, 1, 32>(ctx, grid, a);
+    case 64: return launch_step_t<double, 2, 32>(ctx, grid, a);
+  }
+  fail(LEO2D_ERR_BAD_ARG, "FP64 block width must be 8, 16, 32 or 64 columns");
+}
+
+void launch_reduce(leo2d_ctx* ctx, int cols, const double* partials, double* out, int nb) {
+  const unsigned g = (unsigned)std::min(2 * cols, 1024);
+  auto go = [&](auto kern) {
+    launch(ctx, "reduce_partials", [&] { kern<<<g, kThreads, 0, ctx->stream>>>(partials, out, nb); });
+  };
+  switch (cols) {
+    case 8: return go(k_reduce_partials<8>);
+    case 16: return go(k_reduce_partials<16>);
+    case 32: return go(k_reduce_partials<32>);
+    case 64: return go(k_reduce_partials<64>);
+    case 128: return go(k_reduce_partials<128>);
+  }
+  fail(LEO2D_ERR_BAD_ARG, "unsupported block width");
+}
+
+template <typename T, int V, int LPR>
+int occupancy_t() {
+  int b = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_cheb_step<T, V, LPR>, kThreads, 0);
+  return b;
+}
+
+int occupancy(int cols, bool fp64) {
+  if (!fp64) {
+    switch (cols) {
+      case 8: return occupancy_t<float, 1, 8>();
+      case 16: return occupancy_t<float, 1, 16>();
+      case 32: return occupancy_t<float, 1, 32>();
+      case 64: return occupancy_t<float, 2, 32>();
+      case 128: return occupancy_t<float, 4, 32>();
+    }
+  } else {
+    switch (cols) {
+      case 8: return occupancy_t<double, 1, 8>();
+      case 16: return occupancy_t<double, 1, 16>();
+      case 32: return occupancy_t<double, 1, 32>();
+      case 64: return occupancy_t<double, 2, 32>();
+    }
+  }
+  return 1;
+}
+
+template <typename T>
+void enqueue_steps(Recursion& r) {
+  leo2d_ctx* ctx = r.ctx;
+  const int C = r.shape.cols;
+  for (int k = 0; k < r.steps; ++k) {
+    StepArgs<T> a;
+    a.n = r.n;
+    a.rowptr = r.csr->rowptr.p;
+    a.col = r.csr->col.p;
+    a.val = r.shape.fp64 ? reinterpret_cast<const T*>(r.csr->val64.p)
+                         : reinterpret_cast<const T*>(r.csr->val32.p);
+    a.tn = reinterpret_cast<const T*>(r.buf(k % 2));
+    a.tp = reinterpret_cast<T*>(r.buf((k + 1) % 2));
+    a.first = k == 0;
+    a.rows_per_item = r.shape.rows_per_item;
+    a.partials = r.partials.p + (size_t)(k % 2) * r.grid * 2 * C;
+    a.prev_partials = k == 0 ? nullptr : r.partials.p + (size_t)((k + 1) % 2) * r.grid * 2 * C;
+    a.prev_dots = k == 0 ? nullptr : r.dots.p + (size_t)(k - 1) * 2 * C;
+    launch_step<T>(ctx, C, r.grid, a);
+  }
+  launch_reduce(ctx, C, r.partials.p + (size_t)((r.steps - 1) % 2) * r.grid * 2 * C,
+                r.dots.p + (size_t)(r.steps - 1) * 2 * C, (int)r.grid);
+}
+
+struct ShapeKey {
+  const leo2d_csr* csr;
+  int64_t n, nnz;
+  bool fp64;
+  int cols;
+  bool operator<(const ShapeKey& o) const {
+    return std::tie(csr, n, nnz, fp64, cols) < std::tie(o.csr, o.n, o.nnz, o.fp64, o.cols);
+  }
+};
+std::map<std::pair<leo2d_ctx*, ShapeKey>, int> g_rows_cache;
+
+}  // namespace
+
+namespace leo2d {
+
+void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_) {
+  ctx = c;
+  csr = m;
+  shape = s;
+  n = m->n;
+  steps = steps_;
+  LEO_REQUIRE(m->nnz == 0 || (s.fp64 ? m->val64.p != nullptr : m->val32.p != nullptr),
+              "matrix has no values");
+  const int occ = std::max(1, occupancy(s.cols, s.fp64));
+  const int lpr = s.cols <= 32 ? s.cols : 32;  // lanes per row slot
+  const int64_t item_rows = (int64_t)s.rows_per_item * (32 / lpr);
+  const int64_t items = (n + item_rows - 1) / item_rows;
+  int64_t g = (int64_t)ctx->sm_count * occ;
+  const int64_t need = (items + kWarps - 1) / kWarps;
+  if (g > need) g = std::max<int64_t>(need, 1);
+  grid = (unsigned)g;
+  const size_t esz = s.fp64 ? sizeof(double) : sizeof(float);
+  x0.alloc((size_t)n * s.cols * esz);
+  x1.alloc((size_t)n * s.cols * esz);
+  partials.alloc((size_t)2 * grid * 2 * s.cols);
+  dots.alloc((size_t)steps * 2 * s.cols);
+}
+
+void Recursion::run() {
+  if (shape.fp64) enqueue_steps<double>(*this);
+  else enqueue_steps<float>(*this);
+}
+
+Recursion::~Recursion() {
+  if (graph) cudaGraphExecDestroy(graph);
+}
+
+StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols_needed,
+                       int requested_cols, int requested_rows) {
+  StepShape s;
+  s.fp64 = fp64;
+  if (requested_cols > 0) {
+    s.cols = requested_cols;
+  } else {
+    // smallest supported width that holds the request, capped at the widest
+    const int maxc = fp64 ? 64 : 128;
+    int c = 8;
+    while (c < cols_needed && c < maxc) c <<= 1;
+    s.cols = c;
+  }
+  if (requested_rows > 0) {
+    s.rows_per_item = requested_rows;
+  } else {
+    auto it = g_rows_cache.find({ctx, ShapeKey{csr, csr->n, csr->nnz, fp64, s.cols}});
+    s.rows_per_item = it != g_rows_cache.end() ? it->second : 4;
+  }
+  LEO_REQUIRE(s.rows_per_item >= 1 && s.rows_per_item <= 64, "rows_per_warp must be 1..64");
+  return s;
+}
+
+void fill_phase(leo2d_ctx* ctx, Recursion& r, uint64_t seed, uint64_t first, int n_complex) {
+  const int64_t total = r.n * r.shape.cols;
+  const unsigned g = grid_for(total, 256, (int64_t)ctx->sm_count * 32);
+  if (r.shape.fp64)
+    launch(ctx, "fill_phase", [&] {
+      k_fill_phase<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, seed, first, n_complex);
+    });
+  else
+    launch(ctx, "fill_phase", [&] {
+      k_fill_phase<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, seed, first, n_complex);
+    });
+}
+
+void fill_gaussian(leo2d_ctx* ctx, Recursion& r, uint64_t seed, uint64_t first, int n_vec) {
+  const int64_t total = r.n * r.shape.cols;
+  const unsigned g = grid_for(total, 256, (int64_t)ctx->sm_count * 32);
+  if (r.shape.fp64)
+    launch(ctx, "fill_gauss", [&] {
+      k_fill_gauss<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, seed, first, n_vec);
+    });
+  else
+    launch(ctx, "fill_gauss", [&] {
+      k_fill_gauss<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, seed, first, n_vec);
+    });
+}
+
+void fill_host(leo2d_ctx* ctx, Recursion& r, const double* host_vectors, int first_vec, int n_vec) {
+  DevBuf<double> src((size_t)n_vec * r.n);
+  h2d(ctx, src.p, host_vectors + (size_t)first_vec * r.n, (size_t)n_vec * r.n);
+  const int64_t total = r.n * r.shape.cols;
+  const unsigned g = grid_for(total, 256, (int64_t)ctx->sm_count * 32);
+  if (r.shape.fp64)
+    launch(ctx, "fill_host", [&] {
+      k_fill_from<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, src.p, n_vec);
+    });
+  else
+    launch(ctx, "fill_host", [&] {
+      k_fill_from<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, src.p, n_vec);
+    });
+  LEO_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+void fill_unit(leo2d_ctx* ctx, Recursion& r, const int64_t* targets, int n_t) {
+  DevBuf<int64_t> t(std::max(n_t, 1));
+  h2d(ctx, t.p, targets, n_t);
+  const int64_t total = r.n * r.shape.cols;
+  const unsigned g = grid_for(total, 256, (int64_t)ctx->sm_count * 32);
+  if (r.shape.fp64)
+    launch(ctx, "fill_unit", [&] {
+      k_fill_unit<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, t.p, n_t);
+    });
+  else
+    launch(ctx, "fill_unit", [&] {
+      k_fill_unit<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, t.p, n_t);
+    });
+  LEO_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+void dots_to_moments(const std::vector<double>& dots, int cols, int steps, int group, int n_vec,
+                     double* mu_out, int P) {
+  for (int v = 0; v < n_vec; ++v) {
+    double* mu = mu_out + (size_t)v * P;
+    for (int k = 0; k < steps; ++k) {
+      double D0 = 0, D1 = 0;
+      for (int gidx = 0; gidx < group; ++gidx) {
+        const int c = v * group + gidx;
+        D0 += dots[((size_t)k * cols + c) * 2];
+        D1 += dots[((size_t)k * cols + c) * 2 + 1];
+      }
+      if (k == 0) {
+        mu[0] = D0;
+        mu[1] = D1;
+      } else {
+        mu[2 * k] = 2 * D0 - mu[0];
+        mu[2 * k + 1] = 2 * D1 - mu[1];
+      }
+    }
+  }
+}
+
+}  // namespace leo2d
+
+// ---------------------------------------------------------------- C ABI
+
+namespace {
+
+void validate_cfg(const leo2d_kpm_cfg* cfg) {
+  LEO_REQUIRE(cfg, "cfg is NULL");
+  LEO_REQUIRE(cfg->poly_order >= 4 && cfg->poly_order % 4 == 0,
+              "poly_order must be a positive multiple of 4 (main.cpp:914-917)");
+  LEO_REQUIRE(cfg->precision == LEO2D_FP32 || cfg->precision == LEO2D_FP64, "unknown precision");
+  LEO_REQUIRE(cfg->block >= 0 && cfg->rows_per_warp >= 0, "block and rows_per_warp must be >= 0");
+}
+
+// Runs the recursion over the vector blocks of a trace estimate and writes moments.
+void run_trace(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg, const double* host_vectors,
+               double* mu_out) {
+  const int P = cfg->poly_order;
+  const int steps = P / 2;
+  const bool fp64 = cfg->precision == LEO2D_FP64;
+  const int group = cfg->vector_kind == LEO2D_VEC_PHASE ? 2 : 1;
+  const int total_cols = cfg->num_vectors * group;
+  StepShape shape = choose_shape(ctx, csr, fp64, total_cols, cfg->block, cfg->rows_per_warp);
+  LEO_REQUIRE(shape.cols % group == 0, "block width must hold whole complex vectors");
+  const int vec_per_block = shape.cols / group;
+  Recursion r;
+  r.setup(ctx, csr, shape, steps);
+  std::vector<double> dots((size_t)steps * 2 * shape.cols);
+  for (int v0 = 0; v0 < cfg->num_vectors; v0 += vec_per_block) {
+    const int nv = std::min(vec_per_block, cfg->num_vectors - v0);
+    switch (cfg->vector_kind) {
+      case LEO2D_VEC_PHASE: fill_phase(ctx, r, cfg->seed, cfg->first_vector + v0, nv); break;
+      case LEO2D_VEC_GAUSSIAN: fill_gaussian(ctx, r, cfg->seed, cfg->first_vector + v0, nv); break;
+      case LEO2D_VEC_HOST: fill_host(ctx, r, host_vectors, v0, nv); break;
+      default: fail(LEO2D_ERR_BAD_ARG, "unknown vector_kind");
+    }
+    r.run();
+    d2h(ctx, dots.data(), r.dots.p, dots.size());
+    ctx_sync(ctx);
+    dots_to_moments(dots, shape.cols, steps, group, nv, mu_out + (size_t)v0 * P, P);
+  }
+  for (size_t i = 0; i < (size_t)cfg->num_vectors * P; ++i)
+    if (!std::isfinite(mu_out[i])) fail(LEO2D_ERR_NONFINITE, "non-finite moment (check the spectral bounds)");
+}
+
+}  // namespace
+
+extern "C" {
+
+leo2d_status leo2d_kpm_dos(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg,
+                           const double* host_vectors, double* mu_out) {
+  if (!ctx || !csr || !mu_out) return LEO2D_ERR_BAD_ARG;
+  return guard(ctx, [&] {
+    validate_cfg(cfg);
+    LEO_REQUIRE(cfg->num_vectors >= 1, "num_vectors must be >= 1");
+    LEO_REQUIRE(cfg->vector_kind != LEO2D_VEC_HOST || host_vectors,
+                "LEO2D_VEC_HOST needs host_vectors");
+    LEO_CUDA(cudaSetDevice(ctx->device));
+    run_trace(ctx, csr, cfg, host_vectors, mu_out);
+  });
+}
+
+leo2d_status leo2d_kpm_ldos(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg,
+                            const int64_t* targets, int64_t num_targets, double* mu_out) {
+  if (!ctx || !csr || !mu_out || (num_targets > 0 && !targets)) return LEO2D_ERR_BAD_ARG;
+  return guard(ctx, [&] {
+    validate_cfg(cfg);
+    for (int64_t t = 0; t < num_targets; ++t)
+      LEO_REQUIRE(targets[t] >= 0 && targets[t] < csr->n, "target index out of range");
+    LEO_CUDA(cudaSetDevice(ctx->device));
+    const int P = cfg->poly_order, steps = P / 2;
+    const bool fp64 = cfg->precision == LEO2D_FP64;
+    StepShape shape = choose_shape(ctx, csr, fp64, (int)std::min<int64_t>(num_targets, 128),
+                                   cfg->block, cfg->rows_per_warp);
+    Recursion r;
+    r.setup(ctx, csr, shape, steps);
+    std::vector<double> dots((size_t)steps * 2 * shape.cols);
+    for (int64_t t0 = 0; t0 < num_targets; t0 += shape.cols) {
+      const int nt = (int)std::min<int64_t>(shape.cols, num_targets - t0);
+      fill_unit(ctx, r, targets + t0, nt);
+      r.run();
+      d2h(ctx, dots.data(), r.dots.p, dots.size());
+      ctx_sync(ctx);
+      dots_to_moments(dots, shape.cols, steps, 1, nt, mu_out + (size_t)t0 * P, P);
+    }
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,54 @@
+// kpm.cuh - the fused Chebyshev-step SpMM and its drivers, shared by the DOS,
+// LDOS, batched and conductivity entry points.
+#pragma once
+
+#include "csr.cuh"
+
+namespace leo2d {
+
+// One launch configuration of the step kernel.
+struct StepShape {
+  int cols = 32;           // real columns per vector block (C)
+  int rows_per_item = 4;   // consecutive row slots a warp takes per work item
+  bool fp64 = false;
+};
+
+// Vector block resident on the device: two buffers of n x cols (T_k, T_{k-1}).
+struct Recursion {
+  leo2d_ctx* ctx = nullptr;
+  const leo2d_csr* csr = nullptr;
+  StepShape shape;
+  int64_t n = 0;
+  unsigned grid = 0;
+  DevBuf<char> x0, x1;          // T buffers (float or double)
+  DevBuf<double> partials;      // [grid][cols][2]
+  DevBuf<unsigned> counter;     // last-block ticket
+  DevBuf<double> dots;          // [steps][cols][2]: <T_k|T_k>, <T_{k+1}|T_k>
+  int steps = 0;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = -1;
+
+  void setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_);
+  void* buf(int i) { return i == 0 ? (void*)x0.p : (void*)x1.p; }
+  // Enqueues steps [0, steps) on T_0 already in x0; dots land in `dots`.
+  void run();
+  ~Recursion();
+};
+
+// Chooses the shape for a matrix; cached per context and matrix.
+StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols_needed,
+                       int requested_cols, int requested_rows);
+
+// Fills x0 with the start vectors of one block.
+void fill_phase(leo2d_ctx* ctx, Recursion& r, uint64_t seed, uint64_t first_complex, int n_complex);
+void fill_gaussian(leo2d_ctx* ctx, Recursion& r, uint64_t seed, uint64_t first_vec, int n_vec);
+void fill_host(leo2d_ctx* ctx, Recursion& r, const double* host_vectors, int first_vec, int n_vec);
+void fill_unit(leo2d_ctx* ctx, Recursion& r, const int64_t* targets, int n_targets);
+
+// Converts per-column dots of a finished recursion into moments:
+// mu[v][2k] = 2 D0_k - mu_0, mu[v][2k+1] = 2 D1_k - mu_1 (mu_0 = D0_0, mu_1 = D1_0),
+// with D the sum over the `group` columns of vector v (2 for complex vectors).
+void dots_to_moments(const std::vector<double>& dots, int cols, int steps, int group, int n_vec,
+                     double* mu_out, int P);
+
+}  // namespace leo2d

@@ -1,0 +1,117 @@
+"""GPU assembly against the reference's CSR (golden fixtures) and the oracle.
+
+Row pointers, column indices, pair counts and the index/position arrays must be
+identical; values agree within 1e-12 (FP64 transcendental functions differ in
+the last bits between CUDA and glibc).
+"""
+import numpy as np
+import pytest
+
+import leo2d_gb300 as L
+from oracle import oracle
+from tests._golden import CASES, load, parse_in
+
+pytestmark = pytest.mark.gpu
+VAL_TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    with L.Context(0) as c:
+        yield c
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_golden_csr_bit_exact(ctx, name):
+    gold = load(name)
+    g, kv = parse_in(name)
+    csr = ctx.build_csr(ctx.prepare(g), keep_zeros=True, with_dx=True)
+    meta = gold["meta"]
+    assert (csr.n, csr.nnz, csr.n_intra, csr.n_inter) == tuple(int(x) for x in meta[:4])
+    rp, col, val, dx, dy = csr.download(dx=True)
+    assert np.array_equal(rp, gold["rowptr"].astype(np.int64))
+    assert np.array_equal(col, gold["col"])
+    np.testing.assert_allclose(val, gold["val"], rtol=0, atol=VAL_TOL)
+    if "val_dx" in gold:
+        np.testing.assert_allclose(dx, gold["val_dx"], rtol=0, atol=VAL_TOL * 100)
+        np.testing.assert_allclose(dy, gold["val_dy"], rtol=0, atol=VAL_TOL * 100)
+    grid, pos = csr.geometry()
+    assert np.array_equal(grid, gold["index_to_grid"])
+    assert np.array_equal(pos, gold["i2pos"])
+
+
+@pytest.mark.parametrize("model", [L.MODEL_REF, L.MODEL_SIMPLE])
+@pytest.mark.parametrize("angle,size", [(5.09, 24), (1.05, 30), (-2.2, 17)])
+def test_flake_vs_oracle(ctx, model, angle, size):
+    g = L.make_geom(model=model, size=size, angles_deg=(0.0, angle), energy_rescale=11.0,
+                    energy_shift=0.25)
+    gp = ctx.prepare(g)
+    ref = oracle.Built(gp)
+    csr = ctx.build_csr(gp, keep_zeros=True, with_dx=True)
+    rp, col, val, dx, dy = csr.download(dx=True)
+    assert np.array_equal(rp, ref.rowptr) and np.array_equal(col, ref.col)
+    assert (csr.n_intra, csr.n_inter) == (ref.n_intra, ref.n_inter)
+    np.testing.assert_allclose(val, ref.val, rtol=0, atol=VAL_TOL)
+    np.testing.assert_allclose(dx, ref.val_dx, rtol=0, atol=1e-10)
+    # compact layout: the reference's entries with non-zero value, diagonal always kept
+    c = ctx.build_csr(gp)
+    crp, ccol, cval = c.download()
+    keep = (ref.val != 0) | (ref.col == np.repeat(np.arange(ref.n), np.diff(ref.rowptr)))
+    exp_rp = np.concatenate([[0], np.cumsum(np.add.reduceat(keep.astype(np.int64), ref.rowptr[:-1]))])
+    assert np.array_equal(crp, exp_rp)
+    assert np.array_equal(ccol, ref.col[keep])
+    np.testing.assert_allclose(cval, ref.val[keep], rtol=0, atol=VAL_TOL)
+
+
+@pytest.mark.parametrize("mn", [(5, 4), (4, 5), (7, 6)])
+def test_periodic_vs_oracle(ctx, mn):
+    g = L.make_geom(boundary_condition=1, supercell_mn=mn, size=16, energy_rescale=13.0)
+    gp = ctx.prepare(g)
+    ref = oracle.Built(gp)
+    csr = ctx.build_csr(gp, keep_zeros=True)
+    rp, col, val = csr.download()
+    assert np.array_equal(rp, ref.rowptr) and np.array_equal(col, ref.col)
+    np.testing.assert_allclose(val, ref.val, rtol=0, atol=VAL_TOL)
+
+
+def test_trilayer_simple_model(ctx):
+    g = L.make_geom(num_sheets=3, model=L.MODEL_SIMPLE, size=14, heights=(0, 3.35, 6.7),
+                    angles_deg=(0, 3.0, -1.5), energy_rescale=10.0)
+    gp = ctx.prepare(g)
+    ref = oracle.Built(gp)
+    csr = ctx.build_csr(gp, keep_zeros=True)
+    rp, col, val = csr.download()
+    assert np.array_equal(rp, ref.rowptr) and np.array_equal(col, ref.col)
+    np.testing.assert_allclose(val, ref.val, rtol=0, atol=VAL_TOL)
+
+
+def test_bounds_and_rescale(ctx):
+    g = L.make_geom(model=L.MODEL_SIMPLE, size=20, angles_deg=(0, 2.0), energy_rescale=1.0)
+    gp = ctx.prepare(g)
+    csr = ctx.build_csr(gp)
+    rp, col, val = csr.download()
+    lo, hi = csr.bounds()
+    elo, ehi = oracle.gershgorin(rp, col, val)
+    assert abs(lo - elo) < 1e-12 and abs(hi - ehi) < 1e-12
+    a, b = 1.01 * (hi - lo) / 2, (hi + lo) / 2
+    csr.rescale(a, -b)
+    g2 = L.make_geom(model=L.MODEL_SIMPLE, size=20, angles_deg=(0, 2.0), energy_rescale=a,
+                     energy_shift=-b)
+    rp2, col2, val2 = ctx.build_csr(ctx.prepare(g2)).download()
+    assert np.array_equal(rp2, csr.download()[0])
+    np.testing.assert_allclose(csr.download()[2], val2, rtol=1e-14, atol=1e-15)
+    lo2, hi2 = csr.bounds()
+    assert -1.0 < lo2 and hi2 < 1.0
+
+
+def test_bad_geometry_is_rejected(ctx):
+    import ctypes
+    g = L.make_geom(size=5)
+    h = ctypes.c_void_p()
+    st = ctx.lib.leo2d_build_csr(ctx.h, ctypes.byref(g), 0, ctypes.byref(h))
+    assert st == 1 and not h.value  # LEO2D_ERR_BAD_ARG: geometry not prepared
+    assert b"prepared" in ctx.lib.leo2d_last_error(ctx.h)
+    g = ctx.prepare(L.make_geom(size=5))
+    g.energy_rescale = 0.0
+    with pytest.raises(L.Leo2dError, match="energy_rescale"):
+        ctx.build_csr(g)
