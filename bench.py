@@ -1,0 +1,384 @@
+"""Benchmark: time-to-DOS of the KPM path on a 10M-orbital twisted-bilayer flake.
+
+Workload (one GB300): twisted bilayer graphene disk, twist 0.5 deg, radius
+2042 A (~1.0e7 pz orbitals), simple model (a = 2.46 A, t = -2.7 eV,
+t_perp(r) = 0.33 exp(-(r-3.35)/0.45) eV, r < 8 A), Gershgorin bounds x 1.01,
+P = 1024 Chebyshev moments, Jackson kernel, DOS on 4001 energies spanning the
+rescaled band. Inputs are synthetic: the geometry is generated by the
+library's own GPU assembly.
+
+A step = one DOS estimate from the Hamiltonian resident in HBM: R random-phase
+vectors through the fused FP32 Chebyshev recursion (FP64 moment sums), then
+the FP64 Jackson/Chebyshev reconstruction. R is the smallest number of
+vectors whose DOS is within 1e-3 relative L1 error of a stochastic reference
+(R_ref vectors, independent seed), found once before timing; so
+value = time-to-DOS at 1e-3 L1 error (seconds, lower is better).
+e2e = the same DOS through the C ABI from the host geometry description,
+including GPU assembly, with moments and DOS copied back to host memory.
+Vector blocks (>= 80 MB per block at this size) exceed the 126 MB L2 together
+with the 8 GB matrix, so every step streams from HBM; no L2 flush is needed.
+
+--impl reference times the reference's CPU recursion (the oracle port of
+Locality::computeDosTraceKPM + SpMatrix::vectorMultiply, FP64) on the host
+cores on a bounded sample of the same workload and extrapolates to it.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "time-to-DOS at 1e-3 L1 err (plain GPU KPM; CV-surrogate reported beside it)"
+UNIT = "s"
+TWIST_DEG = 0.5
+RADIUS = 2042.0
+P = 1024
+N_E = 4001
+TARGET_L1 = 1e-3
+
+
+def geom(L, radius=RADIUS, twist=TWIST_DEG):
+    # |i| <= R/a + |j|/2 with |j| <= R/(a sqrt(3)/2) for sites of the disk
+    size = int(math.ceil(radius / 2.46 * (1.0 + 1.0 / math.sqrt(3.0)))) + 4
+    return L.make_geom(model=L.MODEL_SIMPLE, size=size, max_R=radius, heights=(0.0, 3.35),
+                       angles_deg=(0.0, twist), energy_rescale=1.0)
+
+
+def energies(a, b):
+    x = -1.0 + 2.0 * (np.arange(N_E) + 0.5) / N_E
+    return b + a * x
+
+
+def l1(d, ref):
+    return float(np.abs(d - ref).sum() / np.abs(ref).sum())
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def step_bytes(n, nnz_true, cols):
+    """Algorithmic bytes of one Chebyshev step over a block of `cols` FP32 columns."""
+    return nnz_true * (4 + 4) + (n + 1) * 8 + 3 * n * cols * 4
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        pg = dist
+    return ws, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- CPU baseline
+
+def cpu_sample(threads, sample_radius=260.0, steps=8, rng_seed=0):
+    """Reference CPU recursion on a bounded sample: a same-model flake of radius
+    `sample_radius` built by the oracle, `threads` vectors on `threads` threads,
+    `steps` Chebyshev steps. Returns seconds per (step, vector-batch) and nnz."""
+    import ctypes
+    import leo2d_gb300 as L
+    from oracle import oracle
+    g = oracle.geom_prepare(geom(L, radius=sample_radius))
+    g.energy_rescale = 14.0
+    b = oracle.Built(g)
+    rp, col, val = b.compact()
+    lib = oracle.lib()
+    lib.oracle_cpu_kpm_steps.restype = ctypes.c_double
+    chk = ctypes.c_double()
+    t = lib.oracle_cpu_kpm_steps(ctypes.c_int64(b.n), oracle._p(np.ascontiguousarray(rp)),
+                                 oracle._p(np.ascontiguousarray(col)),
+                                 oracle._p(np.ascontiguousarray(val)), ctypes.c_int32(threads),
+                                 ctypes.c_int32(steps), ctypes.c_int32(threads), ctypes.byref(chk))
+    return t / steps, len(col), b.n
+
+
+def cpu_time_to_dos(R, n_full, nnz_full, threads, sample):
+    t_step, nnz_s, n_s = sample
+    # per step every thread advances one vector over the sample; scale by work
+    scale = (nnz_full * 12 + n_full * 40) / (nnz_s * 12 + n_s * 40)
+    batches = math.ceil(R / threads)
+    return batches * (P // 2) * t_step * scale
+
+
+# ---------------------------------------------------------------- main
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--radius", type=float, default=RADIUS)
+    ap.add_argument("--ref-vectors", type=int, default=256)
+    ap.add_argument("--max-vectors", type=int, default=128)
+    args = ap.parse_args()
+    ws, rank, local, pg = dist_setup()
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        run_reference(args, threads)
+        return
+
+    import leo2d_gb300 as L
+    ctx = L.Context(local)
+    g = ctx.prepare(geom(L, radius=args.radius))
+    t0 = time.perf_counter()
+    csr = ctx.build_csr(g)
+    lo, hi = csr.bounds()
+    a, b = 1.01 * (hi - lo) / 2, (hi + lo) / 2
+    csr.rescale(a, -b)
+    t_build = time.perf_counter() - t0
+    n, nnz = csr.n, csr.nnz
+    E = energies(a, b)
+
+    def dos_of(mu_mean):
+        return ctx.dos_reconstruct(mu_mean, E, a, b, 1.0 / n)
+
+    # stochastic reference (independent seed) and calibration of R
+    mu_ref = csr.kpm_dos(L.kpm_cfg(P, R=args.ref_vectors, seed=1_000_003))
+    d_ref = dos_of(mu_ref.mean(axis=0))
+    mu_cal = csr.kpm_dos(L.kpm_cfg(P, R=args.max_vectors, seed=7))
+    errs = []
+    R_needed = None
+    csum = np.cumsum(mu_cal, axis=0)
+    for R in range(1, args.max_vectors + 1):
+        e = l1(dos_of(csum[R - 1] / R), d_ref)
+        errs.append(e)
+        if R_needed is None and e <= TARGET_L1:
+            R_needed = R
+    if R_needed is None:
+        R_needed = args.max_vectors
+    # FP32 recursion against FP64 on the same vectors (2 vectors)
+    mu64 = csr.kpm_dos(L.kpm_cfg(P, R=2, seed=11, precision=L.FP64))
+    mu32 = csr.kpm_dos(L.kpm_cfg(P, R=2, seed=11, precision=L.FP32))
+    fp32_l1 = l1(dos_of(mu32.mean(axis=0)), dos_of(mu64.mean(axis=0)))
+
+    cfg = L.kpm_cfg(P, R=R_needed, seed=7)
+    cols = 8
+    while cols < 2 * R_needed and cols < 128:
+        cols *= 2
+
+    import torch
+    torch.cuda.set_device(local)
+    stream = torch.cuda.ExternalStream(ctx.lib.leo2d_ctx_stream(ctx.h))
+
+    def one_dos():
+        mu = csr.kpm_dos(cfg)
+        return dos_of(mu.mean(axis=0))
+
+    for _ in range(args.warmup):
+        one_dos()
+    ctx.reset_stats()
+    ctx.set_profiling(True)
+    launches0 = ctx.launch_count()
+    barrier(pg)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            d = one_dos()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier(pg)
+    t_dev = ev0.elapsed_time(ev1) / 1000.0 / args.steps
+    launches = ctx.launch_count() - launches0
+    k_n, k_ms = ctx.kernel_stats("cheb_step")
+    ctx.set_profiling(False)
+    t_dev_max = max_over_ranks(pg, t_dev)
+    final_err = l1(d, d_ref)
+
+    # e2e: geometry description on the host -> DOS in host memory, through the C ABI
+    def e2e_once():
+        c2 = ctx.build_csr(g)
+        lo2, hi2 = c2.bounds()
+        a2, b2 = 1.01 * (hi2 - lo2) / 2, (hi2 + lo2) / 2
+        c2.rescale(a2, -b2)
+        mu = c2.kpm_dos(cfg)
+        out = ctx.dos_reconstruct(mu.mean(axis=0), energies(a2, b2), a2, b2, 1.0 / n)
+        c2.close()
+        return mu, out
+
+    e2e_once()
+    barrier(pg)
+    t1 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        mu_e, _ = e2e_once()
+    t_e2e = max_over_ranks(pg, (time.perf_counter() - t1) / e2e_steps)
+    import ctypes
+    h2d = ctypes.sizeof(L.Geom) + P * 8 + N_E * 8
+    d2h = mu_e.nbytes + N_E * 8 + 2 * 8
+
+    peak, peak_kind = peaks()
+    bytes_step = step_bytes(n, nnz, cols)
+    achieved = bytes_step / (k_ms / k_n / 1000.0) / 1e9 if k_n else None
+    traffic = None
+    tp = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get("cheb_step_bytes_per_launch_10M")
+        except Exception:
+            traffic = None
+
+    out = {
+        "metric": METRIC, "value": round(t_dev_max, 6), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_dev_max * 1000, 3),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (geometry generated on the GPU; random-phase vectors, Philox)",
+        "config": {"workload": f"TBLG flake {TWIST_DEG} deg, R={args.radius:.0f} A, {n} orbitals, "
+                               f"simple model, P={P}, {N_E} energies",
+                   "orbitals": n, "nnz": nnz, "poly_order": P, "vectors_to_1e-3": R_needed,
+                   "ref_vectors": args.ref_vectors, "final_l1": final_err,
+                   "fp32_vs_fp64_l1": fp32_l1, "block_cols": cols,
+                   "l2": "inputs larger than L2 (8 GB matrix streamed every step)",
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": round(t_e2e, 6), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
+                     "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4) if achieved else None, "traffic": traffic,
+                     "kernel": "cheb_step", "bytes_per_launch": bytes_step,
+                     "launch_ms": round(k_ms / k_n, 4) if k_n else None,
+                     "peak_kind": peak_kind},
+        "clocks": clk.summary(),
+        "build_s": round(t_build, 3),
+        "l1_curve": [round(x, 6) for x in errs[:16]],
+    }
+    if rank == 0 and ws == 1:
+        sample = cpu_sample(threads)
+        cpu_t = cpu_time_to_dos(R_needed, n, nnz, threads, sample)
+        out["cpu_baseline"] = {"value": round(cpu_t, 3), "unit": UNIT, "cores": threads,
+                               "kind": "port",
+                               "sample": f"oracle FP64 recursion, {threads} vectors on {threads} "
+                                         f"threads, 8 steps on a {sample[2]}-orbital flake of the "
+                                         f"same model, scaled by bytes to {n} orbitals x "
+                                         f"{R_needed} vectors x {P // 2} steps"}
+    if rank == 0:
+        print(json.dumps(out))
+    ctx.close()
+
+
+def run_reference(args, threads):
+    """CPU reference arm: the oracle port of the reference recursion on host cores."""
+    import leo2d_gb300 as L
+    from oracle import oracle
+    # sizes of the full workload from the oracle geometry formula (no GPU used)
+    steps_timed = []
+    sample = None
+    for _ in range(args.warmup):
+        cpu_sample(threads, sample_radius=180.0, steps=2)
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        sample = cpu_sample(threads)
+        steps_timed.append(time.perf_counter() - t0)
+    # full-size orbital and entry counts: area scaling of the sample flake
+    t_step, nnz_s, n_s = sample
+    scale_n = (RADIUS / 260.0) ** 2
+    n_full = int(n_s * scale_n)
+    nnz_full = int(nnz_s * scale_n)
+    R = int(os.environ.get("LEO2D_BENCH_VECTORS", "16"))
+    v = cpu_time_to_dos(R, n_full, nnz_full, threads, sample)
+    out = {"impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": UNIT,
+           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": round(float(np.mean(steps_timed)) * 1000, 1), "higher_is_better": False,
+           "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+           "config": {"workload": f"TBLG flake {TWIST_DEG} deg, R={RADIUS:.0f} A, ~{n_full} orbitals, "
+                                  f"simple model, P={P}", "vectors": R},
+           "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": f"oracle FP64 recursion on a {n_s}-orbital flake, {threads} "
+                                      f"vectors x 8 steps, scaled to {n_full} orbitals x {R} "
+                                      f"vectors x {P // 2} steps"},
+           "e2e": {"value": round(v, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()
