@@ -198,6 +198,34 @@ leo2d_status leo2d_dos_reconstruct(leo2d_ctx* ctx, const double* mu, int32_t pol
                                    const double* energies, int64_t num_energies, double rescale,
                                    double center, double scale, double* dos_out);
 
+/* ---------------------------------------------------------------- no device allocation */
+
+/* Allocation-free variant of leo2d_kpm_dos (random-phase vectors, FP32
+ * recursion). No counterpart in the reference: it exists for callers that may
+ * not allocate device memory - code that runs while a stream is being captured
+ * into a CUDA graph, or a host application whose device memory is entirely
+ * owned by its own allocator and budget - so it calls no cudaMalloc, cudaFree
+ * or allocating library routine and needs no context.
+ * Inputs and output are device pointers owned by the caller: the H~ CSR
+ * (rowptr[n+1], col[nnz], FP32 val[nnz]) and mu_out[num_vectors][poly_order]
+ * (FP64), written as leo2d_kpm_dos writes its host buffer. Work is enqueued on
+ * `stream` (a cudaStream_t, NULL for the legacy stream) and the call returns
+ * without waiting; synchronise the stream before reading mu_out.
+ * Scratch: one file-scope 32 MiB device array (held by every device that loads
+ * the library until the process exits). The two vector blocks, block partials
+ * and moment dots must fit in it: n * 64 bytes plus a few hundred KB, i.e. up to
+ * about 5e5 orbitals. Larger problems return LEO2D_ERR_BAD_ARG.
+ * The first call on a device looks up the array's device address with that
+ * device current (set-up, once per device); make that first call before any
+ * stream capture. All calls share the array: calls that overlap on the GPU
+ * (other streams, other host threads) race and corrupt each other's results.
+ * Status codes: LEO2D_ERR_BAD_ARG (null pointer, size, poly_order % 4 != 0,
+ * problem too large), LEO2D_ERR_CUDA (no device, failed launch). */
+leo2d_status leo2d_kpm_dos_noalloc(const int64_t* rowptr, const int32_t* col, const float* val,
+                                   int64_t n, int32_t poly_order, int32_t num_vectors,
+                                   uint64_t seed, uint64_t first_vector, double* mu_out,
+                                   void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -136,7 +136,9 @@ def _declare(lib):
 
 
 # entry points declared when present (added alongside their kernels)
-_EXTRA = []
+_EXTRA = [
+    ("leo2d_kpm_dos_noalloc", c_i32, (P, P, P, c_i64, c_i32, c_i32, c_u64, c_u64, P, c_void_p)),
+]
 
 
 def exported_symbols_from_header(header_path=None):

@@ -32,6 +32,8 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
+#include <string>
 #include <tuple>
 
 #include "kpm.cuh"
@@ -663,3 +665,148 @@ leo2d_status leo2d_kpm_ldos(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kp
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- allocation-free entry point
+//
+// leo2d_kpm_dos_noalloc: the trace recursion of leo2d_kpm_dos for callers that
+// cannot allocate device memory. Its working set (the two vector blocks, the
+// block partials and the per-step dots) lives in one file-scope device array.
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;  // 32 MiB, held by every device that loads the library
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of g_noalloc_scratch per device (a host-side use of the symbol
+// itself would name host memory, not the device array).
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {nullptr};
+
+__global__ void k_dots_to_moments(const double* __restrict__ dots, int cols, int steps, int n_vec,
+                                  double* __restrict__ mu_out, int P) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n_vec) return;
+  double* mu = mu_out + (size_t)v * P;
+  double mu0 = 0.0, mu1 = 0.0;
+  for (int k = 0; k < steps; ++k) {
+    const double* d = dots + (size_t)k * cols * 2;
+    const double D0 = d[2 * (2 * v)] + d[2 * (2 * v + 1)];
+    const double D1 = d[2 * (2 * v) + 1] + d[2 * (2 * v + 1) + 1];
+    if (k == 0) {
+      mu0 = D0;
+      mu1 = D1;
+      mu[0] = D0;
+      mu[1] = D1;
+    } else {
+      mu[2 * k] = 2 * D0 - mu0;
+      mu[2 * k + 1] = 2 * D1 - mu1;
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" leo2d_status leo2d_kpm_dos_noalloc(const int64_t* rowptr, const int32_t* col,
+                                              const float* val, int64_t n, int32_t poly_order,
+                                              int32_t num_vectors, uint64_t seed,
+                                              uint64_t first_vector, double* mu_out, void* stream) {
+  auto bad = [](leo2d_status s, const char*) { return s; };
+  if (!rowptr || !col || !val || !mu_out) return bad(LEO2D_ERR_BAD_ARG, "null pointer argument");
+  if (n <= 0 || n >= (1ll << 31) - 1) return bad(LEO2D_ERR_BAD_ARG, "n must be in 1..2^31-2");
+  if (poly_order < 4 || poly_order % 4 != 0)
+    return bad(LEO2D_ERR_BAD_ARG, "poly_order must be a positive multiple of 4");
+  if (num_vectors < 1) return bad(LEO2D_ERR_BAD_ARG, "num_vectors must be >= 1");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    return bad(LEO2D_ERR_CUDA, "no current CUDA device");
+  void* base = nullptr;
+  {
+    // once per device, with that device current
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      cudaError_t e = cudaGetSymbolAddress(&g_noalloc_ptr[dev], g_noalloc_scratch);
+      if (e != cudaSuccess || !g_noalloc_ptr[dev]) {
+        g_noalloc_ptr[dev] = nullptr;
+        return bad(LEO2D_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed");
+      }
+    }
+    base = g_noalloc_ptr[dev];
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return bad(LEO2D_ERR_CUDA, "cannot query the device");
+  const int steps = poly_order / 2;
+  // widest block (8, 16 or 32 columns) whose working set fits the scratch array
+  int cols = 0;
+  unsigned grid = 0;
+  size_t off_x1 = 0, off_part = 0, off_dots = 0;
+  for (int c = 32; c >= 8; c /= 2) {
+    StepShape s;
+    s.cols = c;
+    s.rows_per_item = 4;
+    const int occ = std::max(1, occupancy(c, false));
+    const int64_t item_rows = (int64_t)s.rows_per_item * (32 / c);
+    const int64_t need = ((n + item_rows - 1) / item_rows + kWarps - 1) / kWarps;
+    const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * occ, need));
+    auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t xb = up((size_t)n * c * sizeof(float));
+    const size_t pb = up((size_t)2 * g * 2 * c * sizeof(double));
+    const size_t db = up((size_t)steps * 2 * c * sizeof(double));
+    if (2 * xb + pb + db <= kNoAllocScratchBytes) {
+      cols = c;
+      grid = g;
+      off_x1 = xb;
+      off_part = 2 * xb;
+      off_dots = 2 * xb + pb;
+      break;
+    }
+  }
+  if (cols == 0)
+    return bad(LEO2D_ERR_BAD_ARG,
+               "problem too large for the 32 MiB scratch array: n * 64 bytes plus moments must fit");
+  unsigned char* sc = static_cast<unsigned char*>(base);
+  float* x0 = reinterpret_cast<float*>(sc);
+  float* x1 = reinterpret_cast<float*>(sc + off_x1);
+  double* partials = reinterpret_cast<double*>(sc + off_part);
+  double* dots = reinterpret_cast<double*>(sc + off_dots);
+  const int vec_per_block = cols / 2;
+  for (int v0 = 0; v0 < num_vectors; v0 += vec_per_block) {
+    const int nv = std::min(vec_per_block, num_vectors - v0);
+    const int64_t total = n * cols;
+    k_fill_phase<float><<<(unsigned)std::min<int64_t>((total + 255) / 256, (int64_t)sms * 32), 256, 0, st>>>(
+        n, cols, x0, seed, first_vector + v0, nv);
+    for (int k = 0; k < steps; ++k) {
+      StepArgs<float> a;
+      a.n = n;
+      a.rowptr = rowptr;
+      a.col = col;
+      a.val = val;
+      a.tn = k % 2 == 0 ? x0 : x1;
+      a.tp = k % 2 == 0 ? x1 : x0;
+      a.first = k == 0;
+      a.rows_per_item = 4;
+      a.partials = partials + (size_t)(k % 2) * grid * 2 * cols;
+      a.prev_partials = k == 0 ? nullptr : partials + (size_t)((k + 1) % 2) * grid * 2 * cols;
+      a.prev_dots = k == 0 ? nullptr : dots + (size_t)(k - 1) * 2 * cols;
+      switch (cols) {
+        case 8: k_cheb_step<float, 1, 8><<<grid, kThreads, 0, st>>>(a); break;
+        case 16: k_cheb_step<float, 1, 16><<<grid, kThreads, 0, st>>>(a); break;
+        default: k_cheb_step<float, 1, 32><<<grid, kThreads, 0, st>>>(a); break;
+      }
+    }
+    const double* last = partials + (size_t)((steps - 1) % 2) * grid * 2 * cols;
+    double* last_dots = dots + (size_t)(steps - 1) * 2 * cols;
+    const unsigned rg = (unsigned)std::min(2 * cols, 1024);
+    switch (cols) {
+      case 8: k_reduce_partials<8><<<rg, kThreads, 0, st>>>(last, last_dots, (int)grid); break;
+      case 16: k_reduce_partials<16><<<rg, kThreads, 0, st>>>(last, last_dots, (int)grid); break;
+      default: k_reduce_partials<32><<<rg, kThreads, 0, st>>>(last, last_dots, (int)grid); break;
+    }
+    k_dots_to_moments<<<(nv + 63) / 64, 64, 0, st>>>(dots, cols, steps, nv, mu_out + (size_t)v0 * poly_order,
+                                                     poly_order);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return LEO2D_ERR_CUDA;
+  }
+  return LEO2D_OK;
+}
