@@ -240,9 +240,9 @@ def main():
     fp32_l1 = l1(dos_of(mu32.mean(axis=0)), dos_of(mu64.mean(axis=0)))
 
     cfg = L.kpm_cfg(P, R=R_needed, seed=7)
-    cols = 8
-    while cols < 2 * R_needed and cols < 128:
-        cols *= 2
+    t_tune = time.perf_counter()
+    cols, rows = csr.autotune(cfg)  # untimed: picks block width, rows per slot, warps
+    t_tune = time.perf_counter() - t_tune
 
     import torch
     torch.cuda.set_device(local)
@@ -297,7 +297,7 @@ def main():
     d2h = mu_e.nbytes + N_E * 8 + 2 * 8
 
     peak, peak_kind = peaks()
-    bytes_step = step_bytes(n, nnz, cols)
+    bytes_step = step_bytes(n, nnz, cols)  # per launch: one pass over one vector block
     achieved = bytes_step / (k_ms / k_n / 1000.0) / 1e9 if k_n else None
     traffic = None
     tp = os.path.join(REPO, "profiles", "traffic.json")
@@ -316,7 +316,8 @@ def main():
                                f"simple model, P={P}, {N_E} energies",
                    "orbitals": n, "nnz": nnz, "poly_order": P, "vectors_to_1e-3": R_needed,
                    "ref_vectors": args.ref_vectors, "final_l1": final_err,
-                   "fp32_vs_fp64_l1": fp32_l1, "block_cols": cols,
+                   "fp32_vs_fp64_l1": fp32_l1, "block_cols": cols, "rows_per_slot": rows,
+                   "passes_per_step": -(-2 * R_needed // cols), "autotune_s": round(t_tune, 2),
                    "l2": "inputs larger than L2 (8 GB matrix streamed every step)",
                    "parallelism": f"replicas x{ws}"},
         "e2e": {"value": round(t_e2e, 6), "unit": UNIT, "h2d_bytes_per_step": h2d,

@@ -104,6 +104,15 @@ leo2d_status leo2d_ctx_kernel_stats(leo2d_ctx* ctx, const char* kernel,
 leo2d_status leo2d_ctx_reset_stats(leo2d_ctx* ctx);
 /* Total kernel launches made through this context since creation. */
 int64_t leo2d_ctx_launch_count(const leo2d_ctx* ctx);
+/* Tuning switches of a context. Keys: "step_kernel" (0 = shared-memory tiles
+ * filled by bulk copies, the default; 1 = register streaming of the matrix),
+ * "tile_stages" (2..4 shared-memory stages of the tiled kernel, default 2),
+ * "tile_chunk" (1..64 consecutive row tiles per block between grid-wide
+ * jumps, default 4), "tile_warps" (8 or 24 warps per block of the tiled
+ * kernel; 0 = chosen per block width, the default), "reorder" (locality ordering of the streamed matrix:
+ * -1 = automatic for >= 1e5 orbitals with positions, 0 = off, 1 = on),
+ * "reorder_patch_dA" (patch edge of that ordering in tenths of A, default 160). */
+leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value);
 
 /* ---------------------------------------------------------------- geometry */
 
@@ -182,6 +191,13 @@ leo2d_status leo2d_kpm_dos(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm
  * Locality::computeDosKPM (src/locality.cpp:5945-6136). */
 leo2d_status leo2d_kpm_ldos(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg,
                             const int64_t* targets, int64_t num_targets, double* mu_out);
+/* Times the step kernel on this matrix for every vector-block width (8..128
+ * columns), rows per warp slot and warps per block, and keeps the fastest
+ * choice per width and the width that minimises the time of a run of
+ * cfg->num_vectors vectors; later calls with block = 0 / rows_per_warp = 0 use
+ * them. No counterpart in the reference (its SpMV has no tunable shape). */
+leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg,
+                                int32_t* block_out, int32_t* rows_out);
 
 /* Param_tools::densityTransform (param_tools.cpp:661-705) for one moment set, or
  * densityTransformTrace (707-768) when num_sets > 1 (mean over sets first):

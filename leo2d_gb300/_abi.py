@@ -117,6 +117,7 @@ def _declare(lib):
     fn("leo2d_ctx_kernel_stats", c_i32, c_void_p, ctypes.c_char_p, P, P)
     fn("leo2d_ctx_reset_stats", c_i32, c_void_p)
     fn("leo2d_ctx_launch_count", c_i64, c_void_p)
+    fn("leo2d_ctx_set_option", c_i32, c_void_p, ctypes.c_char_p, c_i64)
     fn("leo2d_geom_prepare", c_i32, gp)
     fn("leo2d_build_csr", c_i32, c_void_p, gp, c_u32, pp)
     fn("leo2d_csr_destroy", c_i32, c_void_p)
@@ -128,6 +129,7 @@ def _declare(lib):
     fn("leo2d_csr_rescale", c_i32, c_void_p, c_void_p, c_dbl, c_dbl)
     fn("leo2d_kpm_dos", c_i32, c_void_p, c_void_p, cp, P, P)
     fn("leo2d_kpm_ldos", c_i32, c_void_p, c_void_p, cp, P, c_i64, P)
+    fn("leo2d_kpm_autotune", c_i32, c_void_p, c_void_p, cp, P, P)
     fn("leo2d_dos_transform", c_i32, c_void_p, P, c_i32, c_i32, c_dbl, c_dbl, c_dbl, P, P)
     fn("leo2d_dos_reconstruct", c_i32, c_void_p, P, c_i32, P, c_i64, c_dbl, c_dbl, c_dbl, P)
     for name, res, args in _EXTRA:

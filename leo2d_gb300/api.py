@@ -71,6 +71,9 @@ class Context:
     def launch_count(self):
         return self.lib.leo2d_ctx_launch_count(self.h)
 
+    def set_option(self, key, value):
+        self.check(self.lib.leo2d_ctx_set_option(self.h, key.encode(), int(value)))
+
     def set_spin_limit(self, n):
         self.check(self.lib.leo2d_ctx_set_spin_limit(self.h, n))
 
@@ -178,6 +181,12 @@ class Csr:
         self.ctx.check(self.ctx.lib.leo2d_kpm_dos(self.ctx.h, self.h, ctypes.byref(cfg), _p(hv),
                                                   _p(mu)))
         return mu
+
+    def autotune(self, cfg):
+        b, r = ctypes.c_int32(), ctypes.c_int32()
+        self.ctx.check(self.ctx.lib.leo2d_kpm_autotune(self.ctx.h, self.h, ctypes.byref(cfg),
+                                                       ctypes.byref(b), ctypes.byref(r)))
+        return b.value, r.value
 
     def kpm_ldos(self, cfg, targets):
         t = np.ascontiguousarray(targets, np.int64)

@@ -98,6 +98,12 @@ struct leo2d_ctx {
   std::vector<leo2d::PendingTimer> pending;
   std::vector<cudaEvent_t> free_events;
   int64_t launches = 0;
+  int kernel_variant = 0;     // 0 = tiled (bulk copies), 1 = register streaming
+  int tile_stages = 2;        // shared-memory stages of the tiled kernel
+  int tile_chunk = 4;         // consecutive tiles per block between grid-wide jumps
+  int tile_warps = 0;         // warps per block of the tiled kernel (0 = per shape, 8 or 24)
+  int reorder = -1;           // locality ordering: -1 auto, 0 off, 1 on
+  double reorder_patch = 16.0;  // patch edge (A)
   leo2d::DevBuf<int> status;  // one int, reset before kernels that may set it
 };
 

@@ -278,4 +278,32 @@ leo2d_status leo2d_ctx_reset_stats(leo2d_ctx* ctx) {
 
 int64_t leo2d_ctx_launch_count(const leo2d_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
+leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value) {
+  if (!ctx || !key) return LEO2D_ERR_BAD_ARG;
+  return guard(ctx, [&] {
+    const std::string k(key);
+    if (k == "step_kernel") {
+      LEO_REQUIRE(value == 0 || value == 1, "step_kernel must be 0 or 1");
+      ctx->kernel_variant = (int)value;
+    } else if (k == "tile_stages") {
+      LEO_REQUIRE(value >= 2 && value <= 4, "tile_stages must be 2..4");
+      ctx->tile_stages = (int)value;
+    } else if (k == "tile_chunk") {
+      LEO_REQUIRE(value >= 1 && value <= 64, "tile_chunk must be 1..64");
+      ctx->tile_chunk = (int)value;
+    } else if (k == "tile_warps") {
+      LEO_REQUIRE(value == 0 || value == 8 || value == 24, "tile_warps must be 0, 8 or 24");
+      ctx->tile_warps = (int)value;
+    } else if (k == "reorder") {
+      LEO_REQUIRE(value >= -1 && value <= 1, "reorder must be -1, 0 or 1");
+      ctx->reorder = (int)value;
+    } else if (k == "reorder_patch_dA") {
+      LEO_REQUIRE(value >= 5 && value <= 2000, "reorder_patch_dA must be 5..2000 (tenths of A)");
+      ctx->reorder_patch = value / 10.0;
+    } else {
+      fail(LEO2D_ERR_BAD_ARG, "unknown option " + k);
+    }
+  });
+}
+
 }  // extern "C"

@@ -3,6 +3,13 @@
 
 #include "common.cuh"
 
+namespace leo2d {
+// Elements allocated past the end of rowptr / col / val so that bulk copies of
+// a tile may round their range up to 16-byte multiples without leaving the
+// allocation. The padding is zero-filled.
+constexpr int64_t kCsrPad = 16;
+}  // namespace leo2d
+
 struct leo2d_csr {
   int device = 0;
   int64_t n = 0;        // orbitals (rows)
@@ -13,16 +20,38 @@ struct leo2d_csr {
   leo2d::DevBuf<int64_t> rowptr;  // n + 1
   leo2d::DevBuf<int32_t> col;     // nnz
   leo2d::DevBuf<double> val64;    // nnz, FP64 values (assembly, bounds, FP64 recursion)
-  leo2d::DevBuf<float> val32;     // nnz, FP32 copy streamed by the FP32 recursion
+  leo2d::DevBuf<float> val32;     // nnz, FP32 copy of the values
+  leo2d::DevBuf<uint2> ent;       // nnz, (column, FP32 value bits) streamed by the FP32 recursion
   leo2d::DevBuf<double> dx64, dy64;
   leo2d::DevBuf<float> dx32;
   leo2d::DevBuf<int32_t> grid4;   // n x 4 (i, j, orbital, sheet)
   leo2d::DevBuf<double> pos;      // n x 3
   bool has_geom = false;
   leo2d_geom geom{};
+  // largest stored-entry count of any tile of `tile_rows` consecutive rows (cached)
+  int tile_rows_cached = 0;
+  int64_t tile_max_nnz = 0;
+  // locality-ordered copy streamed by the recursion (reorder.cu)
+  bool reordered = false;
+  bool reorder_fp64 = false;
+  double reorder_patch = 0.0;
+  leo2d::DevBuf<int32_t> new2old, old2new;
+  leo2d::DevBuf<int64_t> prow;
+  leo2d::DevBuf<int32_t> pcol;
+  leo2d::DevBuf<float> pval32;
+  leo2d::DevBuf<uint2> pent;
+  leo2d::DevBuf<double> pval64;
+  int perm_tile_rows = 0;
+  int64_t perm_tile_max_nnz = 0;
 };
 
 namespace leo2d {
 // Refreshes the FP32 copies of the values from the FP64 arrays.
 void csr_refresh_fp32(leo2d_ctx* ctx, leo2d_csr* csr);
+// Allocates rowptr (n+1), col and val64 (nnz) with zeroed kCsrPad padding.
+void csr_alloc_rowptr(leo2d_ctx* ctx, leo2d_csr* csr, int64_t n);
+void csr_alloc_entries(leo2d_ctx* ctx, leo2d_csr* csr, int64_t nnz, bool with_dx);
+// Builds / drops the locality-ordered copy (patch = real-space patch edge, A).
+void csr_build_reordered(leo2d_ctx* ctx, leo2d_csr* csr, double patch, bool with_fp64);
+void csr_drop_reordered(leo2d_csr* csr);
 }  // namespace leo2d

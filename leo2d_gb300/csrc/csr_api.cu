@@ -134,14 +134,14 @@ leo2d_status leo2d_csr_upload(leo2d_ctx* ctx, int64_t n, int64_t nnz, const int6
     csr->device = ctx->device;
     csr->n = n;
     csr->nnz = nnz;
-    csr->rowptr.alloc(n + 1);
-    csr->col.alloc(std::max<int64_t>(nnz, 1));
-    csr->val64.alloc(std::max<int64_t>(nnz, 1));
+    csr_alloc_rowptr(ctx, csr, n);
+    csr_alloc_entries(ctx, csr, nnz, false);
     h2d(ctx, csr->rowptr.p, rowptr, n + 1);
     h2d(ctx, csr->col.p, col, nnz);
     h2d(ctx, csr->val64.p, val, nnz);
     if (val_dx) {
-      csr->dx64.alloc(std::max<int64_t>(nnz, 1));
+      csr->dx64.alloc(nnz + kCsrPad);
+      LEO_CUDA(cudaMemsetAsync(csr->dx64.p + nnz, 0, kCsrPad * sizeof(double), ctx->stream));
       h2d(ctx, csr->dx64.p, val_dx, nnz);
     }
     if (pos) {

@@ -603,6 +603,13 @@ __global__ void __launch_bounds__(256) k_periodic_rows(const __grid_constant__ G
   }
 }
 
+__global__ void k_pack_ent(const int32_t* __restrict__ col, const float* __restrict__ v, uint2* __restrict__ e,
+                           int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    e[i] = make_uint2((unsigned)col[i], __float_as_uint(v[i]));
+}
+
 __global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -688,15 +695,43 @@ void validate_geom(const leo2d_geom* g) {
 }  // namespace
 
 namespace leo2d {
+void csr_alloc_rowptr(leo2d_ctx* ctx, leo2d_csr* csr, int64_t n) {
+  csr->rowptr.alloc(n + 1 + kCsrPad);
+  LEO_CUDA(cudaMemsetAsync(csr->rowptr.p + n + 1, 0, kCsrPad * sizeof(int64_t), ctx->stream));
+}
+
+void csr_alloc_entries(leo2d_ctx* ctx, leo2d_csr* csr, int64_t nnz, bool with_dx) {
+  csr->col.alloc(nnz + kCsrPad);
+  csr->val64.alloc(nnz + kCsrPad);
+  LEO_CUDA(cudaMemsetAsync(csr->col.p + nnz, 0, kCsrPad * sizeof(int32_t), ctx->stream));
+  LEO_CUDA(cudaMemsetAsync(csr->val64.p + nnz, 0, kCsrPad * sizeof(double), ctx->stream));
+  if (with_dx) {
+    csr->dx64.alloc(nnz + kCsrPad);
+    csr->dy64.alloc(nnz + kCsrPad);
+    LEO_CUDA(cudaMemsetAsync(csr->dx64.p + nnz, 0, kCsrPad * sizeof(double), ctx->stream));
+    LEO_CUDA(cudaMemsetAsync(csr->dy64.p + nnz, 0, kCsrPad * sizeof(double), ctx->stream));
+  }
+}
+
 void csr_refresh_fp32(leo2d_ctx* ctx, leo2d_csr* csr) {
+  csr->tile_rows_cached = 0;
+  csr_drop_reordered(csr);
   if (csr->nnz == 0) return;
-  csr->val32.alloc(csr->nnz);
+  csr->val32.alloc(csr->nnz + kCsrPad);
+  LEO_CUDA(cudaMemsetAsync(csr->val32.p + csr->nnz, 0, kCsrPad * sizeof(float), ctx->stream));
+  csr->ent.alloc(csr->nnz + kCsrPad);
+  LEO_CUDA(cudaMemsetAsync(csr->ent.p + csr->nnz, 0, kCsrPad * sizeof(uint2), ctx->stream));
   launch(ctx, "to_f32", [&] {
     k_to_f32<<<grid_for(csr->nnz, 256, (int64_t)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
         csr->val64.p, csr->val32.p, csr->nnz);
   });
+  launch(ctx, "pack_ent", [&] {
+    k_pack_ent<<<grid_for(csr->nnz, 256, (int64_t)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
+        csr->col.p, csr->val32.p, csr->ent.p, csr->nnz);
+  });
   if (csr->dx64.p) {
-    csr->dx32.alloc(csr->nnz);
+    csr->dx32.alloc(csr->nnz + kCsrPad);
+    LEO_CUDA(cudaMemsetAsync(csr->dx32.p + csr->nnz, 0, kCsrPad * sizeof(float), ctx->stream));
     launch(ctx, "to_f32", [&] {
       k_to_f32<<<grid_for(csr->nnz, 256, (int64_t)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
           csr->dx64.p, csr->dx32.p, csr->nnz);
@@ -773,7 +808,7 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     // count -> scan -> fill
     DevBuf<int64_t> cnt_ent(std::max<int64_t>(n, 1)), cnt_intra(std::max<int64_t>(n, 1)),
         cnt_inter(std::max<int64_t>(n, 1));
-    csr->rowptr.alloc(n + 1);
+    csr_alloc_rowptr(ctx, csr, n);
     RowOut ro{cnt_ent.p, cnt_intra.p, cnt_inter.p, csr->rowptr.p, nullptr, nullptr, nullptr, nullptr};
     int cap = 0;
     size_t smem = 0;
@@ -810,12 +845,7 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     csr->nnz = nnz;
     csr->n_intra = reduce_sum_i64(ctx, cnt_intra.p, n);
     csr->n_inter = reduce_sum_i64(ctx, cnt_inter.p, n);
-    csr->col.alloc(std::max<int64_t>(nnz, 1));
-    csr->val64.alloc(std::max<int64_t>(nnz, 1));
-    if (G.with_dx) {
-      csr->dx64.alloc(std::max<int64_t>(nnz, 1));
-      csr->dy64.alloc(std::max<int64_t>(nnz, 1));
-    }
+    csr_alloc_entries(ctx, csr, nnz, G.with_dx != 0);
     ro.col = csr->col.p;
     ro.val = csr->val64.p;
     ro.dx = csr->dx64.p;

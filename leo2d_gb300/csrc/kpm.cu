@@ -33,6 +33,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <type_traits>
 #include <string>
 #include <tuple>
 
@@ -77,6 +78,15 @@ __device__ __forceinline__ Pack<T, V> ld_plain(const T* p) {
 }
 
 template <typename T, int V>
+__device__ __forceinline__ Pack<T, V> ld_stream(const T* p) {
+  using vt = typename VT<T, V>::t;
+  vt x = __ldcs(reinterpret_cast<const vt*>(p));
+  Pack<T, V> r;
+  memcpy(&r, &x, sizeof(r));
+  return r;
+}
+
+template <typename T, int V>
 __device__ __forceinline__ void st_plain(T* p, const Pack<T, V>& r) {
   using vt = typename VT<T, V>::t;
   vt x;
@@ -90,6 +100,7 @@ struct StepArgs {
   const int64_t* __restrict__ rowptr;
   const int32_t* __restrict__ col;
   const T* __restrict__ val;
+  const uint2* __restrict__ ent;  // FP32 entries as (column, value bits) pairs
   const T* __restrict__ tn;  // T_n (gathered)
   T* __restrict__ tp;        // T_{n-1} in, T_{n+1} out
   int first;                 // step 0: T_1 = H~ T_0
@@ -101,16 +112,22 @@ struct StepArgs {
 
 // Fixed-order tree reduction of partials[b][t] over b < nb into out[t], for the
 // values t assigned to this block.
-template <int C>
+template <int C, int NT = kThreads>
 __device__ __forceinline__ void reduce_prev(const double* __restrict__ partials,
                                             double* __restrict__ out, int nb) {
-  __shared__ double red[kThreads];
+  constexpr int kPow = NT >= 512 ? 512 : 256;  // tree over the first kPow lanes
+  __shared__ double red[kPow];
   for (int t = blockIdx.x; t < 2 * C; t += gridDim.x) {
     double s = 0.0;
-    for (int b = threadIdx.x; b < nb; b += kThreads) s += __ldcg(partials + (size_t)b * 2 * C + t);
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int w = kThreads / 2; w > 0; w >>= 1) {
+    for (int b = threadIdx.x; b < nb; b += NT) s += __ldcg(partials + (size_t)b * 2 * C + t);
+    for (int base = 0; base < NT; base += kPow) {  // fold lanes >= kPow in, in order
+      if ((int)threadIdx.x >= base && (int)threadIdx.x < base + kPow) {
+        if (base == 0) red[threadIdx.x] = s;
+        else red[threadIdx.x - base] += s;
+      }
+      __syncthreads();
+    }
+    for (int w = kPow / 2; w > 0; w >>= 1) {
       if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
       __syncthreads();
     }
@@ -241,6 +258,298 @@ __global__ void __launch_bounds__(kThreads) k_reduce_partials(const double* __re
   reduce_prev<C>(partials, out, nb);
 }
 
+// ---------------------------------------------------------------- tiled step (bulk copies)
+//
+// Same step, with the matrix stream decoupled from the gathers: a block takes
+// tiles of TR consecutive rows; an elected thread copies each tile's row
+// pointers, column indices and values into shared memory with
+// cp.async.bulk (completion counted on an mbarrier), double-buffered so the
+// copy of tile i+2 runs while tile i is computed. Lanes then read (col, val)
+// from shared memory (broadcast within a row slot) and spend their memory
+// parallelism on the gathers of T_n only. Ranges are rounded outward to 16-byte
+// multiples; the CSR arrays carry kCsrPad elements of padding for this.
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+// Waits for the phase of `bar` with the given parity; gives up after `limit`
+// polls or two seconds, whichever comes first, and returns whether it completed.
+__device__ __forceinline__ bool bounded_wait(uint64_t* bar, uint32_t parity, uint64_t limit) {
+  const uint64_t t0 = global_ns();
+  for (uint64_t k = 0; k < limit; ++k) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((k & 255) == 255 && global_ns() - t0 > 2000000000ull) return false;
+  }
+  return false;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+struct TileLayout {
+  int stages;        // shared-memory stages (2..4)
+  int chunk;         // consecutive tiles a block takes before jumping by the grid
+  int tile_rows;     // TR
+  int cap;           // entries per stage (multiple of 4)
+  int rp_bytes;      // (TR + 4) * 8 rounded to 128
+  int col_bytes;     // cap * 4 rounded to 128
+  int stage_bytes;   // rp + col + val, rounded to 128
+};
+
+template <typename T>
+struct TileArgs {
+  StepArgs<T> s;
+  TileLayout lay;
+  uint64_t spin_limit;
+  int* status;
+};
+
+template <typename T, int V, int LPR, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? 3 : 1) k_cheb_tile(const TileArgs<T> ta) {
+  constexpr int C = V * LPR;
+  constexpr int RPW = 32 / LPR;
+  constexpr int NS = WARPS * RPW;
+  constexpr int NT = WARPS * 32;
+  // FP32: (column, value) pairs, one 8-byte shared load per entry
+  constexpr bool kAoS = std::is_same<T, float>::value;
+  constexpr int kMaxStages = 4;
+  const StepArgs<T>& a = ta.s;
+  const TileLayout& L = ta.lay;
+  const int nst = L.stages;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t full[kMaxStages];
+  __shared__ int released[kMaxStages];  // warps done with the stage's current tile
+  __shared__ int issued[kMaxStages];    // copies issued into the stage so far
+  if (a.prev_partials) reduce_prev<C, NT>(a.prev_partials, a.prev_dots, gridDim.x);
+
+  const int TR = L.tile_rows;
+  const int64_t n_tiles = (a.n + TR - 1) / TR;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < nst; ++i) {
+      mbar_init(&full[i], 1);
+      released[i] = 0;
+      issued[i] = 0;
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+
+  // copies of `tile` into `stage` (one lane)
+  auto issue = [&](int64_t tile, int stage) {
+    const int64_t r0 = tile * TR;
+    const int64_t tr = min((int64_t)TR, a.n - r0);
+    const int64_t q0 = a.rowptr[r0], q1 = a.rowptr[r0 + tr];
+    const int64_t ra = r0 & ~1ll;
+    const int64_t rcount = ((r0 + tr + 1 - ra) + 1) & ~1ll;
+    const int64_t qa = q0 & ~3ll;
+    const int64_t qcount = ((q1 - qa) + 3) & ~3ll;
+    unsigned char* st = smem + (size_t)stage * L.stage_bytes;
+    issued[stage] += 1;
+    if constexpr (kAoS) {
+      const uint32_t bytes = (uint32_t)(rcount * 8 + qcount * 8);
+      mbar_expect_tx(&full[stage], bytes);
+      bulk_g2s(st, a.rowptr + ra, (uint32_t)(rcount * 8), &full[stage]);
+      if (qcount > 0) bulk_g2s(st + L.rp_bytes, a.ent + qa, (uint32_t)(qcount * 8), &full[stage]);
+    } else {
+      const uint32_t bytes = (uint32_t)(rcount * 8 + qcount * (4 + (int64_t)sizeof(T)));
+      mbar_expect_tx(&full[stage], bytes);
+      bulk_g2s(st, a.rowptr + ra, (uint32_t)(rcount * 8), &full[stage]);
+      if (qcount > 0) {
+        bulk_g2s(st + L.rp_bytes, a.col + qa, (uint32_t)(qcount * 4), &full[stage]);
+        bulk_g2s(st + L.rp_bytes + L.col_bytes, a.val + qa, (uint32_t)(qcount * sizeof(T)), &full[stage]);
+      }
+    }
+  };
+
+  // Runs of `chunk` consecutive tiles are dealt round-robin: consecutive tiles
+  // of a block share most of their gathered T_n rows (L1 reuse) while the grid
+  // still sweeps the matrix as one band (the rows in flight stay L2-resident).
+  const int64_t chunk = L.chunk;
+  auto tile_of = [&](int64_t i) -> int64_t {
+    return ((int64_t)blockIdx.x + (i / chunk) * (int64_t)gridDim.x) * chunk + i % chunk;
+  };
+  if (threadIdx.x == 0)
+    for (int i = 0; i < nst; ++i)
+      if (tile_of(i) < n_tiles) issue(tile_of(i), i);
+  __syncthreads();
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int slot = lane / LPR, sub = lane % LPR;
+  const int gslot = warp * RPW + slot;
+  const T alpha = a.first ? T(1) : T(2);
+  double d0[V], d1[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) d0[v] = d1[v] = 0.0;
+
+  // Warps advance independently: no block barrier per tile. The last warp to
+  // release a stage refills it with the tile nst steps ahead.
+  int it = 0;
+  for (int64_t tile = tile_of(0); tile < n_tiles; tile = tile_of(++it)) {
+    const int stage = it % nst;
+    const uint32_t parity = (uint32_t)(it / nst) & 1u;
+    if (!bounded_wait(&full[stage], parity, ta.spin_limit)) {
+      if (lane == 0) atomicExch(ta.status, kStatusTimeout);
+      break;
+    }
+    const unsigned char* st = smem + (size_t)stage * L.stage_bytes;
+    const int64_t* rp_s = reinterpret_cast<const int64_t*>(st);
+    const int32_t* col_s = reinterpret_cast<const int32_t*>(st + L.rp_bytes);
+    const T* val_s = reinterpret_cast<const T*>(st + L.rp_bytes + L.col_bytes);
+    const uint2* ent_s = reinterpret_cast<const uint2*>(st + L.rp_bytes);
+    const int64_t r0 = tile * TR;
+    const int tr = (int)min((int64_t)TR, a.n - r0);
+    const int64_t ra = r0 & ~1ll;
+    const int64_t qa = rp_s[r0 - ra] & ~3ll;
+    T f0[V], f1[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) f0[v] = f1[v] = T(0);
+    for (int lr = gslot; lr < tr; lr += NS) {
+      const int64_t row = r0 + lr;
+      const int beg = (int)(rp_s[row - ra] - qa), end = (int)(rp_s[row + 1 - ra] - qa);
+      const int64_t off = row * C + sub * V;
+      // epilogue operands first: their latency overlaps the gathers
+      const Pack<T, V> xn = ld_gather<T, V>(a.tn + off);
+      Pack<T, V> xp;
+      if (!a.first) xp = ld_stream<T, V>(a.tp + off);
+      T acc[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) acc[v] = T(0);
+      for (int k = beg; k < end; k += 8) {
+        int c[8];
+        T w[8];
+        Pack<T, V> x[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const bool in = k + u < end;
+          if constexpr (kAoS) {
+            const uint2 e = in ? ent_s[k + u] : make_uint2(0u, 0u);
+            c[u] = (int)e.x;
+            w[u] = __uint_as_float(e.y);
+          } else {
+            c[u] = in ? col_s[k + u] : 0;
+            w[u] = in ? val_s[k + u] : T(0);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          if (k + u < end) {
+            x[u] = ld_gather<T, V>(a.tn + (int64_t)c[u] * C + sub * V);
+          } else {
+#pragma unroll
+            for (int v = 0; v < V; ++v) x[u].v[v] = T(0);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+#pragma unroll
+          for (int v = 0; v < V; ++v) acc[v] += w[u] * x[u].v[v];
+      }
+      Pack<T, V> y;
+#pragma unroll
+      for (int v = 0; v < V; ++v) y.v[v] = a.first ? alpha * acc[v] : alpha * acc[v] - xp.v[v];
+      st_plain<T, V>(a.tp + off, y);
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        f0[v] += xn.v[v] * xn.v[v];
+        f1[v] += y.v[v] * xn.v[v];
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      d0[v] += (double)f0[v];
+      d1[v] += (double)f1[v];
+    }
+    // release the stage; the last warp refills it
+    __syncwarp();
+    if (lane == 0) {
+      __threadfence_block();
+      if (atomicAdd(&released[stage], 1) == WARPS - 1) {
+        released[stage] = 0;
+        const int64_t nt = tile_of(it + nst);
+        if (nt < n_tiles) issue(nt, stage);
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  // after a timeout a copy may still be in flight: it must land before exit
+  if (threadIdx.x == 0)
+    for (int i = 0; i < nst; ++i)
+      if (issued[i] > 0) bounded_wait(&full[i], (uint32_t)(issued[i] - 1) & 1u, ta.spin_limit);
+
+#pragma unroll
+  for (int o = LPR; o < 32; o <<= 1)
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      d0[v] += __shfl_xor_sync(0xffffffffu, d0[v], o);
+      d1[v] += __shfl_xor_sync(0xffffffffu, d1[v], o);
+    }
+  // warps add their column sums in warp order (deterministic)
+  __shared__ double bsum[2 * C];
+  for (int t = threadIdx.x; t < 2 * C; t += NT) bsum[t] = 0.0;
+  __syncthreads();
+  for (int w = 0; w < WARPS; ++w) {
+    if (warp == w && slot == 0) {
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        bsum[2 * (sub * V + v)] += d0[v];
+        bsum[2 * (sub * V + v) + 1] += d1[v];
+      }
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < 2 * C; t += NT) a.partials[(size_t)blockIdx.x * 2 * C + t] = bsum[t];
+}
+
+// Largest entry count over tiles of `tr` consecutive rows.
+__global__ void k_tile_max_nnz(const int64_t* __restrict__ rp, int64_t n, int tr,
+                               unsigned long long* out) {
+  const int64_t tiles = (n + tr - 1) / tr;
+  unsigned long long m = 0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tiles;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r0 = t * tr, r1 = min(n, r0 + tr);
+    const unsigned long long v = (unsigned long long)(rp[r1] - (rp[r0] & ~3ll));
+    m = v > m ? v : m;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long y = __shfl_down_sync(0xffffffffu, m, o);
+    m = y > m ? y : m;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
 // ---------------------------------------------------------------- start vectors
 
 __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
@@ -258,11 +567,11 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32
 // Random-phase columns: complex vector j of the block -> columns 2j (cos), 2j+1 (sin).
 template <typename T>
 __global__ void k_fill_phase(int64_t n, int C, T* __restrict__ x, uint64_t seed, uint64_t first,
-                             int n_complex) {
+                             int n_complex, const int32_t* __restrict__ new2old) {
   const int64_t total = n * C;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t row = e / C;
+    const int64_t row = new2old ? (int64_t)new2old[e / C] : e / C;
     const int c = (int)(e % C);
     const int j = c >> 1;
     T out = T(0);
@@ -282,11 +591,11 @@ __global__ void k_fill_phase(int64_t n, int C, T* __restrict__ x, uint64_t seed,
 // Gaussian columns (Box-Muller on Philox).
 template <typename T>
 __global__ void k_fill_gauss(int64_t n, int C, T* __restrict__ x, uint64_t seed, uint64_t first,
-                             int n_vec) {
+                             int n_vec, const int32_t* __restrict__ new2old) {
   const int64_t total = n * C;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t row = e / C;
+    const int64_t row = new2old ? (int64_t)new2old[e / C] : e / C;
     const int c = (int)(e % C);
     T out = T(0);
     if (c < n_vec) {
@@ -305,11 +614,11 @@ __global__ void k_fill_gauss(int64_t n, int C, T* __restrict__ x, uint64_t seed,
 // Host vectors [R][n] (FP64) -> block columns.
 template <typename T>
 __global__ void k_fill_from(int64_t n, int C, T* __restrict__ x, const double* __restrict__ src,
-                            int n_vec) {
+                            int n_vec, const int32_t* __restrict__ new2old) {
   const int64_t total = n * C;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t row = e / C;
+    const int64_t row = new2old ? (int64_t)new2old[e / C] : e / C;
     const int c = (int)(e % C);
     x[e] = c < n_vec ? (T)src[(int64_t)c * n + row] : T(0);
   }
@@ -317,11 +626,11 @@ __global__ void k_fill_from(int64_t n, int C, T* __restrict__ x, const double* _
 
 template <typename T>
 __global__ void k_fill_unit(int64_t n, int C, T* __restrict__ x, const int64_t* __restrict__ targets,
-                            int n_t) {
+                            int n_t, const int32_t* __restrict__ new2old) {
   const int64_t total = n * C;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t row = e / C;
+    const int64_t row = new2old ? (int64_t)new2old[e / C] : e / C;
     const int c = (int)(e % C);
     x[e] = (c < n_t && targets[c] == row) ? T(1) : T(0);
   }
@@ -332,6 +641,64 @@ __global__ void k_fill_unit(int64_t n, int C, T* __restrict__ x, const int64_t* 
 template <typename T, int V, int LPR>
 void launch_step_t(leo2d_ctx* ctx, unsigned grid, const StepArgs<T>& a) {
   launch(ctx, "cheb_step", [&] { k_cheb_step<T, V, LPR><<<grid, kThreads, 0, ctx->stream>>>(a); });
+}
+
+// (V, LPR) of the tiled kernel for a block width: 16-byte gathers per lane (FP32
+// V=4, FP64 V=2), except 8 FP32 columns (V=2).
+template <typename T, int V, int LPR, int WARPS>
+void tile_kernel_w(leo2d_ctx* ctx, unsigned grid, size_t smem, const TileArgs<T>* a, int* occ,
+                   size_t set_smem) {
+  if (occ) {
+    LEO_CUDA(cudaFuncSetAttribute(k_cheb_tile<T, V, LPR, WARPS>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)set_smem));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k_cheb_tile<T, V, LPR, WARPS>, WARPS * 32, set_smem);
+    return;
+  }
+  launch(ctx, "cheb_step",
+         [&] { k_cheb_tile<T, V, LPR, WARPS><<<grid, WARPS * 32, smem, ctx->stream>>>(*a); });
+}
+
+template <typename T, int V, int LPR>
+void tile_kernel_t(leo2d_ctx* ctx, unsigned grid, size_t smem, const TileArgs<T>* a, int* occ,
+                   size_t set_smem, int warps) {
+  if (warps == 24) return tile_kernel_w<T, V, LPR, 24>(ctx, grid, smem, a, occ, set_smem);
+  return tile_kernel_w<T, V, LPR, 8>(ctx, grid, smem, a, occ, set_smem);
+}
+
+template <typename T>
+void tile_dispatch(leo2d_ctx* ctx, int cols, unsigned grid, size_t smem, const TileArgs<T>* a, int* occ,
+                   size_t set_smem, int warps);
+
+template <>
+void tile_dispatch<float>(leo2d_ctx* ctx, int cols, unsigned grid, size_t smem, const TileArgs<float>* a,
+                          int* occ, size_t set_smem, int warps) {
+  switch (cols) {
+    case 8: return tile_kernel_t<float, 2, 4>(ctx, grid, smem, a, occ, set_smem, warps);
+    case 16: return tile_kernel_t<float, 4, 4>(ctx, grid, smem, a, occ, set_smem, warps);
+    case 32: return tile_kernel_t<float, 4, 8>(ctx, grid, smem, a, occ, set_smem, warps);
+    case 64: return tile_kernel_t<float, 4, 16>(ctx, grid, smem, a, occ, set_smem, warps);
+    case 128: return tile_kernel_t<float, 4, 32>(ctx, grid, smem, a, occ, set_smem, warps);
+  }
+  fail(LEO2D_ERR_BAD_ARG, "FP32 block width must be 8, 16, 32, 64 or 128 columns");
+}
+
+template <>
+void tile_dispatch<double>(leo2d_ctx* ctx, int cols, unsigned grid, size_t smem, const TileArgs<double>* a,
+                           int* occ, size_t set_smem, int warps) {
+  switch (cols) {
+    case 8: return tile_kernel_t<double, 2, 4>(ctx, grid, smem, a, occ, set_smem, warps);
+    case 16: return tile_kernel_t<double, 2, 8>(ctx, grid, smem, a, occ, set_smem, warps);
+    case 32: return tile_kernel_t<double, 2, 16>(ctx, grid, smem, a, occ, set_smem, warps);
+    case 64: return tile_kernel_t<double, 2, 32>(ctx, grid, smem, a, occ, set_smem, warps);
+  }
+  fail(LEO2D_ERR_BAD_ARG, "FP64 block width must be 8, 16, 32 or 64 columns");
+}
+
+// Row slots of a block (warps x slots per warp) in the tiled kernel.
+int tile_slots(int cols, bool fp64, int warps) {
+  const int v = fp64 ? 2 : (cols == 8 ? 2 : 4);
+  const int lpr = cols / v;
+  return warps * (32 / lpr);
 }
 
 template <typename T>
@@ -409,10 +776,18 @@ void enqueue_steps(Recursion& r) {
   for (int k = 0; k < r.steps; ++k) {
     StepArgs<T> a;
     a.n = r.n;
-    a.rowptr = r.csr->rowptr.p;
-    a.col = r.csr->col.p;
-    a.val = r.shape.fp64 ? reinterpret_cast<const T*>(r.csr->val64.p)
-                         : reinterpret_cast<const T*>(r.csr->val32.p);
+    a.ent = r.use_perm ? r.csr->pent.p : r.csr->ent.p;
+    if (r.use_perm) {
+      a.rowptr = r.csr->prow.p;
+      a.col = r.csr->pcol.p;
+      a.val = r.shape.fp64 ? reinterpret_cast<const T*>(r.csr->pval64.p)
+                           : reinterpret_cast<const T*>(r.csr->pval32.p);
+    } else {
+      a.rowptr = r.csr->rowptr.p;
+      a.col = r.csr->col.p;
+      a.val = r.shape.fp64 ? reinterpret_cast<const T*>(r.csr->val64.p)
+                           : reinterpret_cast<const T*>(r.csr->val32.p);
+    }
     a.tn = reinterpret_cast<const T*>(r.buf(k % 2));
     a.tp = reinterpret_cast<T*>(r.buf((k + 1) % 2));
     a.first = k == 0;
@@ -420,7 +795,17 @@ void enqueue_steps(Recursion& r) {
     a.partials = r.partials.p + (size_t)(k % 2) * r.grid * 2 * C;
     a.prev_partials = k == 0 ? nullptr : r.partials.p + (size_t)((k + 1) % 2) * r.grid * 2 * C;
     a.prev_dots = k == 0 ? nullptr : r.dots.p + (size_t)(k - 1) * 2 * C;
-    launch_step<T>(ctx, C, r.grid, a);
+    if (r.shape.tiled) {
+      TileArgs<T> ta;
+      ta.s = a;
+      ta.lay = TileLayout{r.tile_stages, r.tile_chunk, r.tile_rows, r.tile_cap, r.tile_rp_bytes, r.tile_col_bytes,
+                          r.tile_stage_bytes};
+      ta.spin_limit = ctx->spin_limit;
+      ta.status = ctx->status.p;
+      tile_dispatch<T>(ctx, C, r.grid, r.dyn_smem, &ta, nullptr, 0, r.shape.warps);
+    } else {
+      launch_step<T>(ctx, C, r.grid, a);
+    }
   }
   launch_reduce(ctx, C, r.partials.p + (size_t)((r.steps - 1) % 2) * r.grid * 2 * C,
                 r.dots.p + (size_t)(r.steps - 1) * 2 * C, (int)r.grid);
@@ -435,7 +820,12 @@ struct ShapeKey {
     return std::tie(csr, n, nnz, fp64, cols) < std::tie(o.csr, o.n, o.nnz, o.fp64, o.cols);
   }
 };
-std::map<std::pair<leo2d_ctx*, ShapeKey>, int> g_rows_cache;
+struct Tuned {
+  int rows = 0, warps = 0;
+};
+std::map<std::pair<leo2d_ctx*, ShapeKey>, Tuned> g_shape_cache;
+// best block width per (context, matrix, precision, columns requested)
+std::map<std::pair<leo2d_ctx*, ShapeKey>, int> g_block_cache;
 
 }  // namespace
 
@@ -449,14 +839,72 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
   steps = steps_;
   LEO_REQUIRE(m->nnz == 0 || (s.fp64 ? m->val64.p != nullptr : m->val32.p != nullptr),
               "matrix has no values");
-  const int occ = std::max(1, occupancy(s.cols, s.fp64));
-  const int lpr = s.cols <= 32 ? s.cols : 32;  // lanes per row slot
-  const int64_t item_rows = (int64_t)s.rows_per_item * (32 / lpr);
-  const int64_t items = (n + item_rows - 1) / item_rows;
-  int64_t g = (int64_t)ctx->sm_count * occ;
-  const int64_t need = (items + kWarps - 1) / kWarps;
-  if (g > need) g = std::max<int64_t>(need, 1);
-  grid = (unsigned)g;
+  leo2d_csr* mm = const_cast<leo2d_csr*>(m);
+  const bool want_perm = m->pos.p != nullptr && m->nnz > 0 &&
+                         (ctx->reorder == 1 || (ctx->reorder == -1 && n >= 100000));
+  if (want_perm && (!m->reordered || (s.fp64 && !m->reorder_fp64) ||
+                    m->reorder_patch != ctx->reorder_patch))
+    csr_build_reordered(ctx, mm, ctx->reorder_patch, s.fp64 || m->reorder_fp64);
+  use_perm = want_perm;
+  if (shape.tiled) {
+    const int ns = tile_slots(s.cols, s.fp64, s.warps);
+    const int ri = s.rows_per_item > 0 ? s.rows_per_item : std::max(1, 32 / ns);
+    tile_rows = ns * ri;
+    int& cached_rows = use_perm ? mm->perm_tile_rows : mm->tile_rows_cached;
+    int64_t& cached_max = use_perm ? mm->perm_tile_max_nnz : mm->tile_max_nnz;
+    if (cached_rows != tile_rows) {
+      DevBuf<unsigned long long> mx(1);
+      LEO_CUDA(cudaMemsetAsync(mx.p, 0, sizeof(unsigned long long), ctx->stream));
+      const int64_t tiles = (n + tile_rows - 1) / tile_rows;
+      const int64_t* rp = use_perm ? m->prow.p : m->rowptr.p;
+      launch(ctx, "tile_max_nnz", [&] {
+        k_tile_max_nnz<<<grid_for(tiles, 256, (int64_t)ctx->sm_count * 8), 256, 0, ctx->stream>>>(
+            rp, n, tile_rows, mx.p);
+      });
+      unsigned long long h = 0;
+      d2h(ctx, &h, mx.p, 1);
+      ctx_sync(ctx);
+      cached_max = (int64_t)h;
+      cached_rows = tile_rows;
+    }
+    auto up = [](int64_t x, int64_t a_) { return (x + a_ - 1) / a_ * a_; };
+    tile_cap = (int)up(cached_max + 4, 4);
+    const size_t esz = s.fp64 ? sizeof(double) : sizeof(float);
+    tile_rp_bytes = (int)up((int64_t)(tile_rows + 4) * 8, 128);
+    if (s.fp64) {
+      tile_col_bytes = (int)up((int64_t)tile_cap * 4, 128);
+      tile_stage_bytes = (int)up(tile_rp_bytes + tile_col_bytes + (int64_t)tile_cap * esz, 128);
+    } else {  // (column, value) pairs
+      tile_col_bytes = (int)up((int64_t)tile_cap * 8, 128);
+      tile_stage_bytes = (int)up(tile_rp_bytes + tile_col_bytes, 128);
+    }
+    tile_stages = ctx->tile_stages;
+    tile_chunk = ctx->tile_chunk;
+    dyn_smem = (size_t)tile_stages * tile_stage_bytes;
+    if (dyn_smem + 24 * 1024 > ctx->smem_optin) {
+      shape.tiled = false;  // rows too heavy for a staged tile: stream from registers
+    } else {
+      int occ = 0;
+      if (s.fp64) tile_dispatch<double>(ctx, s.cols, 0, 0, nullptr, &occ, dyn_smem, s.warps);
+      else tile_dispatch<float>(ctx, s.cols, 0, 0, nullptr, &occ, dyn_smem, s.warps);
+      const int64_t tiles = (n + tile_rows - 1) / tile_rows;
+      const int64_t chunks = (tiles + tile_chunk - 1) / tile_chunk;
+      int64_t g = (int64_t)ctx->sm_count * std::max(occ, 1);
+      if (g > chunks) g = std::max<int64_t>(chunks, 1);
+      grid = (unsigned)g;
+    }
+  }
+  if (!shape.tiled) {
+    if (shape.rows_per_item <= 0) shape.rows_per_item = 4;
+    const int occ = std::max(1, occupancy(s.cols, s.fp64));
+    const int lpr = s.cols <= 32 ? s.cols : 32;  // lanes per row slot
+    const int64_t item_rows = (int64_t)shape.rows_per_item * (32 / lpr);
+    const int64_t items = (n + item_rows - 1) / item_rows;
+    int64_t g = (int64_t)ctx->sm_count * occ;
+    const int64_t need = (items + kWarps - 1) / kWarps;
+    if (g > need) g = std::max<int64_t>(need, 1);
+    grid = (unsigned)g;
+  }
   const size_t esz = s.fp64 ? sizeof(double) : sizeof(float);
   x0.alloc((size_t)n * s.cols * esz);
   x1.alloc((size_t)n * s.cols * esz);
@@ -467,6 +915,7 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
 void Recursion::run() {
   if (shape.fp64) enqueue_steps<double>(*this);
   else enqueue_steps<float>(*this);
+  if (shape.tiled) ctx_check_status(ctx, "Chebyshev recursion");
 }
 
 Recursion::~Recursion() {
@@ -480,19 +929,24 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
   if (requested_cols > 0) {
     s.cols = requested_cols;
   } else {
-    // smallest supported width that holds the request, capped at the widest
-    const int maxc = fp64 ? 64 : 128;
-    int c = 8;
-    while (c < cols_needed && c < maxc) c <<= 1;
-    s.cols = c;
+    auto bt = g_block_cache.find({ctx, ShapeKey{csr, csr->n, csr->nnz, fp64, cols_needed}});
+    if (bt != g_block_cache.end()) {
+      s.cols = bt->second;
+    } else {
+      // smallest supported width that holds the request, capped at the widest
+      const int maxc = fp64 ? 64 : 128;
+      int c = 8;
+      while (c < cols_needed && c < maxc) c <<= 1;
+      s.cols = c;
+    }
   }
-  if (requested_rows > 0) {
-    s.rows_per_item = requested_rows;
-  } else {
-    auto it = g_rows_cache.find({ctx, ShapeKey{csr, csr->n, csr->nnz, fp64, s.cols}});
-    s.rows_per_item = it != g_rows_cache.end() ? it->second : 4;
-  }
-  LEO_REQUIRE(s.rows_per_item >= 1 && s.rows_per_item <= 64, "rows_per_warp must be 1..64");
+  auto it = g_shape_cache.find({ctx, ShapeKey{csr, csr->n, csr->nnz, fp64, s.cols}});
+  s.rows_per_item = requested_rows > 0 ? requested_rows : (it != g_shape_cache.end() ? it->second.rows : 0);
+  if (ctx->tile_warps > 0) s.warps = ctx->tile_warps;
+  else if (it != g_shape_cache.end() && it->second.warps > 0) s.warps = it->second.warps;
+  else s.warps = (!fp64 && (s.cols == 32 || s.cols == 64)) ? 24 : 8;
+  s.tiled = ctx->kernel_variant != 1;
+  LEO_REQUIRE(s.rows_per_item >= 0 && s.rows_per_item <= 64, "rows_per_warp must be 0..64");
   return s;
 }
 
@@ -501,11 +955,11 @@ void fill_phase(leo2d_ctx* ctx, Recursion& r, uint64_t seed, uint64_t first, int
   const unsigned g = grid_for(total, 256, (int64_t)ctx->sm_count * 32);
   if (r.shape.fp64)
     launch(ctx, "fill_phase", [&] {
-      k_fill_phase<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, seed, first, n_complex);
+      k_fill_phase<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, seed, first, n_complex, r.perm());
     });
   else
     launch(ctx, "fill_phase", [&] {
-      k_fill_phase<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, seed, first, n_complex);
+      k_fill_phase<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, seed, first, n_complex, r.perm());
     });
 }
 
@@ -514,11 +968,11 @@ void fill_gaussian(leo2d_ctx* ctx, Recursion& r, uint64_t seed, uint64_t first, 
   const unsigned g = grid_for(total, 256, (int64_t)ctx->sm_count * 32);
   if (r.shape.fp64)
     launch(ctx, "fill_gauss", [&] {
-      k_fill_gauss<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, seed, first, n_vec);
+      k_fill_gauss<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, seed, first, n_vec, r.perm());
     });
   else
     launch(ctx, "fill_gauss", [&] {
-      k_fill_gauss<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, seed, first, n_vec);
+      k_fill_gauss<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, seed, first, n_vec, r.perm());
     });
 }
 
@@ -529,11 +983,11 @@ void fill_host(leo2d_ctx* ctx, Recursion& r, const double* host_vectors, int fir
   const unsigned g = grid_for(total, 256, (int64_t)ctx->sm_count * 32);
   if (r.shape.fp64)
     launch(ctx, "fill_host", [&] {
-      k_fill_from<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, src.p, n_vec);
+      k_fill_from<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, src.p, n_vec, r.perm());
     });
   else
     launch(ctx, "fill_host", [&] {
-      k_fill_from<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, src.p, n_vec);
+      k_fill_from<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, src.p, n_vec, r.perm());
     });
   LEO_CUDA(cudaStreamSynchronize(ctx->stream));
 }
@@ -545,11 +999,11 @@ void fill_unit(leo2d_ctx* ctx, Recursion& r, const int64_t* targets, int n_t) {
   const unsigned g = grid_for(total, 256, (int64_t)ctx->sm_count * 32);
   if (r.shape.fp64)
     launch(ctx, "fill_unit", [&] {
-      k_fill_unit<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, t.p, n_t);
+      k_fill_unit<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, t.p, n_t, r.perm());
     });
   else
     launch(ctx, "fill_unit", [&] {
-      k_fill_unit<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, t.p, n_t);
+      k_fill_unit<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, t.p, n_t, r.perm());
     });
   LEO_CUDA(cudaStreamSynchronize(ctx->stream));
 }
@@ -666,6 +1120,69 @@ leo2d_status leo2d_kpm_ldos(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kp
 
 }  // extern "C"
 
+// ---------------------------------------------------------------- autotuner
+
+extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg,
+                                           int32_t* block_out, int32_t* rows_out) {
+  if (!ctx || !csr || !cfg) return LEO2D_ERR_BAD_ARG;
+  return guard(ctx, [&] {
+    validate_cfg(cfg);
+    LEO_REQUIRE(cfg->num_vectors >= 1, "num_vectors must be >= 1");
+    LEO_CUDA(cudaSetDevice(ctx->device));
+    const bool fp64 = cfg->precision == LEO2D_FP64;
+    const int group = cfg->vector_kind == LEO2D_VEC_PHASE ? 2 : 1;
+    const int total_cols = cfg->num_vectors * group;
+    const int steps = 8;
+    const bool was_profiling = ctx->profiling;
+    if (!was_profiling) { ctx_sync(ctx); ctx->profiling = true; }
+    double best_cost = INFINITY;
+    int best_cols = 0, best_rows = 0, best_warps = 8;
+    const int maxc = fp64 ? 64 : 128;
+    for (int cols = 8; cols <= maxc; cols <<= 1) {
+      if (cols % group) continue;
+      const int passes = (total_cols + cols - 1) / cols;
+      double best_c = INFINITY;
+      Tuned best_t;
+      for (int warps : {8, 24}) {
+        if (ctx->tile_warps > 0 && warps != ctx->tile_warps) continue;
+        for (int rows : {0, 2}) {
+          StepShape sh = choose_shape(ctx, csr, fp64, cols, cols, rows > 0 ? rows : 0);
+          sh.rows_per_item = rows;
+          sh.warps = warps;
+          Recursion r;
+          r.setup(ctx, csr, sh, steps);
+          fill_phase(ctx, r, 1, 0, cols / 2);
+          r.run();  // warm
+          ctx_sync(ctx);
+          const auto before = ctx->stats["cheb_step"];
+          r.run();
+          ctx_sync(ctx);
+          const auto after = ctx->stats["cheb_step"];
+          const double per = (after.ms - before.ms) / std::max<int64_t>(1, after.launches - before.launches);
+          if (per < best_c) {
+            best_c = per;
+            best_t.rows = rows;
+            best_t.warps = warps;
+          }
+        }
+      }
+      g_shape_cache[{ctx, ShapeKey{csr, csr->n, csr->nnz, fp64, cols}}] = best_t;
+      const double cost = passes * best_c;
+      if (cost < best_cost) {
+        best_cost = cost;
+        best_cols = cols;
+        best_rows = best_t.rows;
+        best_warps = best_t.warps;
+      }
+    }
+    if (!was_profiling) { ctx_sync(ctx); ctx->profiling = false; }
+    g_block_cache[{ctx, ShapeKey{csr, csr->n, csr->nnz, fp64, total_cols}}] = best_cols;
+    (void)best_warps;
+    if (block_out) *block_out = best_cols;
+    if (rows_out) *rows_out = best_rows;
+  });
+}
+
 // ---------------------------------------------------------------- allocation-free entry point
 //
 // leo2d_kpm_dos_noalloc: the trace recursion of leo2d_kpm_dos for callers that
@@ -775,7 +1292,7 @@ extern "C" leo2d_status leo2d_kpm_dos_noalloc(const int64_t* rowptr, const int32
     const int nv = std::min(vec_per_block, num_vectors - v0);
     const int64_t total = n * cols;
     k_fill_phase<float><<<(unsigned)std::min<int64_t>((total + 255) / 256, (int64_t)sms * 32), 256, 0, st>>>(
-        n, cols, x0, seed, first_vector + v0, nv);
+        n, cols, x0, seed, first_vector + v0, nv, nullptr);
     for (int k = 0; k < steps; ++k) {
       StepArgs<float> a;
       a.n = n;

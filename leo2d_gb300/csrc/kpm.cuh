@@ -9,8 +9,10 @@ namespace leo2d {
 // One launch configuration of the step kernel.
 struct StepShape {
   int cols = 32;           // real columns per vector block (C)
-  int rows_per_item = 4;   // consecutive row slots a warp takes per work item
+  int rows_per_item = 0;   // rows per row slot per work item / tile (0 = default)
   bool fp64 = false;
+  bool tiled = true;       // bulk-copy tiled kernel (else the register-streaming kernel)
+  int warps = 8;           // warps per block of the tiled kernel (8 or 24)
 };
 
 // Vector block resident on the device: two buffers of n x cols (T_k, T_{k-1}).
@@ -25,8 +27,12 @@ struct Recursion {
   DevBuf<unsigned> counter;     // last-block ticket
   DevBuf<double> dots;          // [steps][cols][2]: <T_k|T_k>, <T_{k+1}|T_k>
   int steps = 0;
+  int tile_stages = 2, tile_chunk = 1, tile_rows = 0, tile_cap = 0, tile_rp_bytes = 0, tile_col_bytes = 0, tile_stage_bytes = 0;
+  size_t dyn_smem = 0;
   cudaGraphExec_t graph = nullptr;
   int graph_steps = -1;
+  bool use_perm = false;  // stream the locality-ordered copy of the matrix
+  const int32_t* perm() const { return use_perm ? csr->new2old.p : nullptr; }
 
   void setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_);
   void* buf(int i) { return i == 0 ? (void*)x0.p : (void*)x1.p; }

@@ -68,25 +68,60 @@ def flake(ctx):
     return csr, rp, col, val
 
 
+def _with_options(ctx, opts, fn):
+    for k, v in opts.items():
+        ctx.set_option(k, v)
+    try:
+        return fn()
+    finally:
+        for k, v in {"step_kernel": 0, "reorder": -1, "tile_warps": 0, "tile_chunk": 4,
+                     "tile_stages": 2}.items():
+            ctx.set_option(k, v)
+
+
+@pytest.mark.parametrize("opts", [{"step_kernel": 0}, {"step_kernel": 1},
+                                  {"step_kernel": 0, "reorder": 1},
+                                  {"step_kernel": 0, "reorder": 1, "tile_warps": 24},
+                                  {"step_kernel": 1, "reorder": 1},
+                                  {"step_kernel": 0, "tile_stages": 4, "tile_chunk": 1}])
 @pytest.mark.parametrize("cols", [8, 16, 32, 64, 128])
 @pytest.mark.parametrize("rows", [1, 3, 8])
-def test_block_shapes_fp32(flake, cols, rows):
+def test_block_shapes_fp32(ctx, flake, opts, cols, rows):
     csr, rp, col, val = flake
     P, R = 128, 6
     vec = np.random.default_rng(cols * 10 + rows).standard_normal((R, csr.n))
     ref = oracle.kpm_trace(rp, col, val, vec, P, literal=False)
-    mu = csr.kpm_dos(L.kpm_cfg(P, R=R, kind=L.VEC_HOST, block=cols, rows_per_warp=rows), vec)
+    mu = _with_options(ctx, opts, lambda: csr.kpm_dos(
+        L.kpm_cfg(P, R=R, kind=L.VEC_HOST, block=cols, rows_per_warp=rows), vec))
     assert _rel(mu, ref) < FP32_RTOL
 
 
-@pytest.mark.parametrize("cols", [8, 32, 64])
-def test_block_shapes_fp64(flake, cols):
+@pytest.mark.parametrize("opts", [{"step_kernel": 0}, {"step_kernel": 1},
+                                  {"step_kernel": 0, "reorder": 1, "tile_warps": 24}])
+@pytest.mark.parametrize("cols", [8, 16, 32, 64])
+def test_block_shapes_fp64(ctx, flake, opts, cols):
     csr, rp, col, val = flake
     P, R = 96, 5
     vec = np.random.default_rng(cols).standard_normal((R, csr.n))
     ref = oracle.kpm_trace(rp, col, val, vec, P, literal=False)
-    mu = csr.kpm_dos(L.kpm_cfg(P, R=R, kind=L.VEC_HOST, precision=L.FP64, block=cols), vec)
+    mu = _with_options(ctx, opts, lambda: csr.kpm_dos(
+        L.kpm_cfg(P, R=R, kind=L.VEC_HOST, precision=L.FP64, block=cols), vec))
     assert _rel(mu, ref) < 1e-12
+
+
+@pytest.mark.parametrize("patch_dA", [60, 160, 400])
+def test_reordered_phase_and_ldos(ctx, flake, patch_dA):
+    csr, rp, col, val = flake
+    P, R, seed = 64, 3, 77
+    ref = csr.kpm_dos(L.kpm_cfg(P, R=R, kind=L.VEC_PHASE, precision=L.FP64, seed=seed))
+    opts = {"reorder": 1, "reorder_patch_dA": patch_dA}
+    mu = _with_options(ctx, opts, lambda: csr.kpm_dos(
+        L.kpm_cfg(P, R=R, kind=L.VEC_PHASE, precision=L.FP64, seed=seed)))
+    assert _rel(mu, ref) < 1e-12
+    tg = [0, 5, csr.n // 2, csr.n - 1]
+    lref = oracle.kpm_ldos(rp, col, val, tg, P)
+    ld = _with_options(ctx, opts, lambda: csr.kpm_ldos(L.kpm_cfg(P, precision=L.FP64), tg))
+    np.testing.assert_allclose(ld, lref, rtol=0, atol=1e-11)
 
 
 def test_phase_vectors_match_oracle_generator(flake):
@@ -138,3 +173,13 @@ def test_bad_arguments(flake):
         csr.kpm_ldos(L.kpm_cfg(32), [csr.n])
     with pytest.raises(L.Leo2dError, match="block width"):
         csr.kpm_dos(L.kpm_cfg(32, R=1, block=48))
+
+
+def test_autotune_picks_a_supported_shape(ctx, flake):
+    csr, rp, col, val = flake
+    cfg = L.kpm_cfg(64, R=10, kind=L.VEC_PHASE, seed=2)
+    block, rows = csr.autotune(cfg)
+    assert block in (8, 16, 32, 64, 128) and rows in (0, 2)
+    ref = csr.kpm_dos(L.kpm_cfg(64, R=10, kind=L.VEC_PHASE, precision=L.FP64, seed=2))
+    mu = csr.kpm_dos(cfg)  # block = 0 -> the tuned width
+    assert _rel(mu, ref) < FP32_RTOL
