@@ -214,6 +214,49 @@ leo2d_status leo2d_dos_reconstruct(leo2d_ctx* ctx, const double* mu, int32_t pol
                                    const double* energies, int64_t num_energies, double rescale,
                                    double center, double scale, double* dos_out);
 
+/* ---------------------------------------------------------------- (c) Kubo conductivity */
+
+/* Two-index Chebyshev moments of the current-current correlation.
+ * With targets (num_targets >= 1): Locality::computeCondKPM
+ * (src/locality.cpp:6348-6727) for each target t, mu_out[t][n][m] =
+ * < dxH T_n(H~) a_0 , T_m(H~) e_t >, a_0 = -dxH e_t (start_p1 = 0,
+ * cond_poly_par = 0); column m = P-1, which the reference never writes, is 0.
+ * Without targets (NULL): the stochastic trace mu_out[n][m] =
+ * (1/R) sum_r Re <T_n J r | J T_m r> = Tr[J T_n J T_m] estimate, J = i dxH, over
+ * cfg->num_vectors random-phase or Gaussian vectors. The recursion runs in
+ * FP32; the moment GEMM accumulates in FP64 across K chunks. The matrix must
+ * be built with LEO2D_CSR_WITH_DX. */
+leo2d_status leo2d_kpm_cond(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg,
+                            const int64_t* targets, int64_t num_targets, double* mu_out);
+/* Param_tools::matrixResponseTransform (param_tools.cpp:838-905), real case:
+ * 2-D DCT-III of 2 g_i g_j M_ij with Jackson g_i / sqrt(2); P x P in and out. */
+leo2d_status leo2d_cond_transform(leo2d_ctx* ctx, const double* M, int32_t poly_order, double* out);
+/* sigma_xx(E) on an energy grid from trace moments (Kubo-Greenwood, Jackson
+ * kernel): scale * sum_nm h_n h_m g_n g_m mu_nm T_n(x) T_m(x) / (pi^2 (1-x^2)),
+ * x = (E - center)/rescale, h_0 = 1, h_n = 2. No counterpart in the reference,
+ * which stops at the transformed matrix. */
+leo2d_status leo2d_cond_sigma(leo2d_ctx* ctx, const double* mu, int32_t poly_order,
+                              const double* energies, int64_t num_energies, double rescale,
+                              double center, double scale, double* sigma_out);
+
+/* ---------------------------------------------------------------- driver */
+
+/* `LEO2D file.in` for the KPM path (app/src/main.cpp:23): parses the input with
+ * main.cpp's keyword rules, builds and solves the SQ job on `device` and writes
+ * <JOB_NAME>.cheb (Param_tools::save, param_tools.cpp:19-316) and, when asked,
+ * <JOB_NAME>_matrix.dat / _pos.dat (locality.cpp:4366-4448) into out_dir.
+ * Options of other reference paths make it return LEO2D_ERR_UNSUPPORTED; the
+ * reason is copied into msg. */
+leo2d_status leo2d_run_input(const char* in_path, const char* out_dir, int device, char* msg,
+                             size_t msg_len);
+/* Host only: the geometry and job switches leo2d_run_input reads from a .in
+ * file (main.cpp:75-911 rules). ints_out (may be NULL) receives 10 values:
+ * solver_type, observable_type, poly_order, kpm_trace, kpm_trace_samps,
+ * verbose_save, matrix_save, number of unsupported options, first target sheet
+ * (0-based), NSHIFTS. Unsupported options are listed in msg. */
+leo2d_status leo2d_parse_input(const char* in_path, leo2d_geom* geom_out, int32_t* ints_out, char* msg,
+                               size_t msg_len);
+
 /* ---------------------------------------------------------------- no device allocation */
 
 /* Allocation-free variant of leo2d_kpm_dos (random-phase vectors, FP32

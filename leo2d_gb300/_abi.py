@@ -132,6 +132,12 @@ def _declare(lib):
     fn("leo2d_kpm_autotune", c_i32, c_void_p, c_void_p, cp, P, P)
     fn("leo2d_dos_transform", c_i32, c_void_p, P, c_i32, c_i32, c_dbl, c_dbl, c_dbl, P, P)
     fn("leo2d_dos_reconstruct", c_i32, c_void_p, P, c_i32, P, c_i64, c_dbl, c_dbl, c_dbl, P)
+    fn("leo2d_kpm_cond", c_i32, c_void_p, c_void_p, cp, P, c_i64, P)
+    fn("leo2d_cond_transform", c_i32, c_void_p, P, c_i32, P)
+    fn("leo2d_cond_sigma", c_i32, c_void_p, P, c_i32, P, c_i64, c_dbl, c_dbl, c_dbl, P)
+    fn("leo2d_run_input", c_i32, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p,
+       ctypes.c_size_t)
+    fn("leo2d_parse_input", c_i32, ctypes.c_char_p, gp, P, ctypes.c_char_p, ctypes.c_size_t)
     for name, res, args in _EXTRA:
         if hasattr(lib, name):
             fn(name, res, *args)

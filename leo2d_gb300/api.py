@@ -113,6 +113,20 @@ class Context:
                                                 scale, _p(dos), _p(E)))
         return dos, E
 
+    def cond_transform(self, M):
+        M = np.ascontiguousarray(M, np.float64)
+        out = np.zeros_like(M)
+        self.check(self.lib.leo2d_cond_transform(self.h, _p(M), M.shape[0], _p(out)))
+        return out
+
+    def cond_sigma(self, mu, energies, rescale, center, scale=1.0):
+        mu = np.ascontiguousarray(mu, np.float64)
+        E = np.ascontiguousarray(energies, np.float64)
+        out = np.zeros(len(E))
+        self.check(self.lib.leo2d_cond_sigma(self.h, _p(mu), mu.shape[0], _p(E), len(E), rescale,
+                                             center, scale, _p(out)))
+        return out
+
     def dos_reconstruct(self, mu, energies, rescale, center, scale=1.0):
         mu = np.ascontiguousarray(mu, np.float64)
         E = np.ascontiguousarray(energies, np.float64)
@@ -120,6 +134,15 @@ class Context:
         self.check(self.lib.leo2d_dos_reconstruct(self.h, _p(mu), len(mu), _p(E), len(E), rescale,
                                                   center, scale, _p(out)))
         return out
+
+
+def run_input(path, out_dir=".", device=0):
+    """The `leo2d` driver through the C ABI; raises Leo2dError with the reason."""
+    lib = _abi.load()
+    buf = ctypes.create_string_buffer(2048)
+    st = lib.leo2d_run_input(str(path).encode(), str(out_dir).encode(), device, buf, len(buf))
+    if st != _abi.OK:
+        raise Leo2dError(st, buf.value.decode())
 
 
 def kpm_cfg(P, R=1, kind=_abi.VEC_PHASE, precision=_abi.FP32, block=0, rows_per_warp=0, seed=0,
@@ -187,6 +210,19 @@ class Csr:
         self.ctx.check(self.ctx.lib.leo2d_kpm_autotune(self.ctx.h, self.h, ctypes.byref(cfg),
                                                        ctypes.byref(b), ctypes.byref(r)))
         return b.value, r.value
+
+    def kpm_cond(self, cfg, targets=None):
+        P = cfg.poly_order
+        if targets is None:
+            out = np.zeros((P, P))
+            self.ctx.check(self.ctx.lib.leo2d_kpm_cond(self.ctx.h, self.h, ctypes.byref(cfg), None, 0,
+                                                       _p(out)))
+            return out
+        t = np.ascontiguousarray(targets, np.int64)
+        out = np.zeros((len(t), P, P))
+        self.ctx.check(self.ctx.lib.leo2d_kpm_cond(self.ctx.h, self.h, ctypes.byref(cfg), _p(t), len(t),
+                                                   _p(out)))
+        return out
 
     def kpm_ldos(self, cfg, targets):
         t = np.ascontiguousarray(targets, np.int64)

@@ -22,6 +22,7 @@ struct leo2d_csr {
   leo2d::DevBuf<double> val64;    // nnz, FP64 values (assembly, bounds, FP64 recursion)
   leo2d::DevBuf<float> val32;     // nnz, FP32 copy of the values
   leo2d::DevBuf<uint2> ent;       // nnz, (column, FP32 value bits) streamed by the FP32 recursion
+  leo2d::DevBuf<uint2> entd;      // nnz, (column, FP32 dxH bits)
   leo2d::DevBuf<double> dx64, dy64;
   leo2d::DevBuf<float> dx32;
   leo2d::DevBuf<int32_t> grid4;   // n x 4 (i, j, orbital, sheet)

@@ -732,9 +732,15 @@ void csr_refresh_fp32(leo2d_ctx* ctx, leo2d_csr* csr) {
   if (csr->dx64.p) {
     csr->dx32.alloc(csr->nnz + kCsrPad);
     LEO_CUDA(cudaMemsetAsync(csr->dx32.p + csr->nnz, 0, kCsrPad * sizeof(float), ctx->stream));
+    csr->entd.alloc(csr->nnz + kCsrPad);
+    LEO_CUDA(cudaMemsetAsync(csr->entd.p + csr->nnz, 0, kCsrPad * sizeof(uint2), ctx->stream));
     launch(ctx, "to_f32", [&] {
       k_to_f32<<<grid_for(csr->nnz, 256, (int64_t)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
           csr->dx64.p, csr->dx32.p, csr->nnz);
+    });
+    launch(ctx, "pack_ent", [&] {
+      k_pack_ent<<<grid_for(csr->nnz, 256, (int64_t)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
+          csr->col.p, csr->dx32.p, csr->entd.p, csr->nnz);
     });
   }
 }

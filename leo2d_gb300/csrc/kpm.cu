@@ -104,6 +104,8 @@ struct StepArgs {
   const T* __restrict__ tn;  // T_n (gathered)
   T* __restrict__ tp;        // T_{n-1} in, T_{n+1} out
   int first;                 // step 0: T_1 = H~ T_0
+  T alpha;                   // y = alpha H~ x (- T_{n-1} unless first); 0 means the default 1 / 2
+  const T* __restrict__ tprev;  // T_{n-1} when it is not stored at tp (null: read tp)
   int rows_per_item;
   double* __restrict__ partials;             // this step: [grid][C][2]
   const double* __restrict__ prev_partials;  // previous step's partials, or null
@@ -149,7 +151,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_cheb_step(const StepArgs<T> a) 
   const int64_t item_rows = (int64_t)a.rows_per_item * RPW;
   const int64_t n_items = (a.n + item_rows - 1) / item_rows;
   const int64_t warps_total = (int64_t)gridDim.x * kWarps;
-  const T alpha = a.first ? T(1) : T(2);
+  const T alpha = a.alpha != T(0) ? a.alpha : (a.first ? T(1) : T(2));
+  const T* tprev = a.tprev ? a.tprev : a.tp;
 
   double d0[V], d1[V];
 #pragma unroll
@@ -208,7 +211,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_cheb_step(const StepArgs<T> a) 
 #pragma unroll
           for (int v = 0; v < V; ++v) y.v[v] = alpha * acc[v];
         } else {
-          const Pack<T, V> xp = ld_plain<T, V>(a.tp + off);
+          const Pack<T, V> xp = ld_plain<T, V>(tprev + off);
 #pragma unroll
           for (int v = 0; v < V; ++v) y.v[v] = alpha * acc[v] - xp.v[v];
         }
@@ -406,7 +409,8 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? 3 : 1) k_cheb_tile(co
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int slot = lane / LPR, sub = lane % LPR;
   const int gslot = warp * RPW + slot;
-  const T alpha = a.first ? T(1) : T(2);
+  const T alpha = a.alpha != T(0) ? a.alpha : (a.first ? T(1) : T(2));
+  const T* tprev = a.tprev ? a.tprev : a.tp;
   double d0[V], d1[V];
 #pragma unroll
   for (int v = 0; v < V; ++v) d0[v] = d1[v] = 0.0;
@@ -440,7 +444,7 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? 3 : 1) k_cheb_tile(co
       // epilogue operands first: their latency overlaps the gathers
       const Pack<T, V> xn = ld_gather<T, V>(a.tn + off);
       Pack<T, V> xp;
-      if (!a.first) xp = ld_stream<T, V>(a.tp + off);
+      if (!a.first) xp = ld_stream<T, V>(tprev + off);
       T acc[V];
 #pragma unroll
       for (int v = 0; v < V; ++v) acc[v] = T(0);
@@ -776,7 +780,7 @@ void enqueue_steps(Recursion& r) {
   for (int k = 0; k < r.steps; ++k) {
     StepArgs<T> a;
     a.n = r.n;
-    a.ent = r.use_perm ? r.csr->pent.p : r.csr->ent.p;
+    a.ent = r.use_perm ? r.csr->pent.p : r.csr->ent.p;  // (Recursion::step selects dxH itself)
     if (r.use_perm) {
       a.rowptr = r.csr->prow.p;
       a.col = r.csr->pcol.p;
@@ -791,6 +795,8 @@ void enqueue_steps(Recursion& r) {
     a.tn = reinterpret_cast<const T*>(r.buf(k % 2));
     a.tp = reinterpret_cast<T*>(r.buf((k + 1) % 2));
     a.first = k == 0;
+    a.alpha = T(0);
+    a.tprev = nullptr;
     a.rows_per_item = r.shape.rows_per_item;
     a.partials = r.partials.p + (size_t)(k % 2) * r.grid * 2 * C;
     a.prev_partials = k == 0 ? nullptr : r.partials.p + (size_t)((k + 1) % 2) * r.grid * 2 * C;
@@ -840,7 +846,7 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
   LEO_REQUIRE(m->nnz == 0 || (s.fp64 ? m->val64.p != nullptr : m->val32.p != nullptr),
               "matrix has no values");
   leo2d_csr* mm = const_cast<leo2d_csr*>(m);
-  const bool want_perm = m->pos.p != nullptr && m->nnz > 0 &&
+  const bool want_perm = allow_perm && m->pos.p != nullptr && m->nnz > 0 &&
                          (ctx->reorder == 1 || (ctx->reorder == -1 && n >= 100000));
   if (want_perm && (!m->reordered || (s.fp64 && !m->reorder_fp64) ||
                     m->reorder_patch != ctx->reorder_patch))
@@ -910,6 +916,50 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
   x1.alloc((size_t)n * s.cols * esz);
   partials.alloc((size_t)2 * grid * 2 * s.cols);
   dots.alloc((size_t)steps * 2 * s.cols);
+}
+
+template <typename T>
+void one_step(Recursion& r, const void* in, void* out, const void* prev, bool first, double alpha, int matrix) {
+  leo2d_ctx* ctx = r.ctx;
+  const int C = r.shape.cols;
+  LEO_REQUIRE(!r.use_perm, "a recursion over dxH needs the unpermuted matrix");
+  StepArgs<T> a;
+  a.n = r.n;
+  a.rowptr = r.csr->rowptr.p;
+  a.col = r.csr->col.p;
+  if (matrix == 0) {
+    a.val = r.shape.fp64 ? reinterpret_cast<const T*>(r.csr->val64.p) : reinterpret_cast<const T*>(r.csr->val32.p);
+    a.ent = r.csr->ent.p;
+  } else {
+    LEO_REQUIRE(r.csr->dx64.p, "matrix was built without LEO2D_CSR_WITH_DX");
+    a.val = r.shape.fp64 ? reinterpret_cast<const T*>(r.csr->dx64.p) : reinterpret_cast<const T*>(r.csr->dx32.p);
+    a.ent = r.csr->entd.p;
+  }
+  a.tn = reinterpret_cast<const T*>(in);
+  a.tp = reinterpret_cast<T*>(out);
+  a.tprev = reinterpret_cast<const T*>(prev);
+  a.first = first ? 1 : 0;
+  a.alpha = (T)alpha;
+  a.rows_per_item = r.shape.rows_per_item;
+  a.partials = r.partials.p;
+  a.prev_partials = nullptr;
+  a.prev_dots = nullptr;
+  if (r.shape.tiled) {
+    TileArgs<T> ta;
+    ta.s = a;
+    ta.lay = TileLayout{r.tile_stages, r.tile_chunk, r.tile_rows, r.tile_cap, r.tile_rp_bytes, r.tile_col_bytes,
+                        r.tile_stage_bytes};
+    ta.spin_limit = ctx->spin_limit;
+    ta.status = ctx->status.p;
+    tile_dispatch<T>(ctx, C, r.grid, r.dyn_smem, &ta, nullptr, 0, r.shape.warps);
+  } else {
+    launch_step<T>(ctx, C, r.grid, a);
+  }
+}
+
+void Recursion::step(const void* in, void* out, const void* prev, bool first, double alpha, int matrix) {
+  if (shape.fp64) one_step<double>(*this, in, out, prev, first, alpha, matrix);
+  else one_step<float>(*this, in, out, prev, first, alpha, matrix);
 }
 
 void Recursion::run() {
@@ -1136,7 +1186,7 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
     const bool was_profiling = ctx->profiling;
     if (!was_profiling) { ctx_sync(ctx); ctx->profiling = true; }
     double best_cost = INFINITY;
-    int best_cols = 0, best_rows = 0, best_warps = 8;
+    int best_cols = 0, best_rows = 0;
     const int maxc = fp64 ? 64 : 128;
     for (int cols = 8; cols <= maxc; cols <<= 1) {
       if (cols % group) continue;
@@ -1172,12 +1222,10 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
         best_cost = cost;
         best_cols = cols;
         best_rows = best_t.rows;
-        best_warps = best_t.warps;
       }
     }
     if (!was_profiling) { ctx_sync(ctx); ctx->profiling = false; }
     g_block_cache[{ctx, ShapeKey{csr, csr->n, csr->nnz, fp64, total_cols}}] = best_cols;
-    (void)best_warps;
     if (block_out) *block_out = best_cols;
     if (rows_out) *rows_out = best_rows;
   });
@@ -1302,6 +1350,8 @@ extern "C" leo2d_status leo2d_kpm_dos_noalloc(const int64_t* rowptr, const int32
       a.tn = k % 2 == 0 ? x0 : x1;
       a.tp = k % 2 == 0 ? x1 : x0;
       a.first = k == 0;
+      a.alpha = 0.0f;
+      a.tprev = nullptr;
       a.rows_per_item = 4;
       a.partials = partials + (size_t)(k % 2) * grid * 2 * cols;
       a.prev_partials = k == 0 ? nullptr : partials + (size_t)((k + 1) % 2) * grid * 2 * cols;

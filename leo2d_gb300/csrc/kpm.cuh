@@ -32,12 +32,16 @@ struct Recursion {
   cudaGraphExec_t graph = nullptr;
   int graph_steps = -1;
   bool use_perm = false;  // stream the locality-ordered copy of the matrix
+  bool allow_perm = true; // set false before setup() to keep the reference row order
   const int32_t* perm() const { return use_perm ? csr->new2old.p : nullptr; }
 
   void setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_);
   void* buf(int i) { return i == 0 ? (void*)x0.p : (void*)x1.p; }
   // Enqueues steps [0, steps) on T_0 already in x0; dots land in `dots`.
   void run();
+  // Enqueues one step out = alpha M in - prev (no subtraction when first);
+  // M = H~ (matrix 0) or dxH (matrix 1); prev may equal out. Block dots unused.
+  void step(const void* in, void* out, const void* prev, bool first, double alpha, int matrix);
   ~Recursion();
 };
 

@@ -1,0 +1,51 @@
+// job.h - host-side description of a LEO2D KPM job (what app/src/main.cpp
+// collects into Sdata and Job_params for this path) and the driver around the
+// C ABI.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/leo2d_gpu.h"
+
+namespace leo2d_host {
+
+// Parsed input: the .in keywords the KPM path reads (main.cpp:75-911) with
+// the reference's defaults (job_params.cpp:17-225), plus the additive keys of
+// this implementation (MODEL, KPM_VECTORS, KPM_SEED, KPM_PRECISION,
+// KPM_BOUNDS, KPM_ENERGIES, KPM_BLOCK).
+struct JobSpec {
+  std::string job_name = "LEO2D_JOB";
+  leo2d_geom geom{};
+  int solver_type = 0;        // SOLVER_TYPE: 1 = SQ
+  int observable_type = 0;    // 0 = DOS, 1 = COND
+  int poly_order = 20;
+  int kpm_trace = 0;
+  int kpm_trace_samps = -1;
+  int dos_transform = 1;
+  int cond_transform = 1;
+  int matrix_save = 0;
+  int matrix_pos_save = 0;
+  int verbose_save = 1;
+  int nshifts = 1;
+  int num_target_sheets = 1;
+  std::vector<int> target_sheets;  // 0-based
+  // additive keys
+  int vectors = 0;            // 0 = reference Gaussian (std::normal_distribution), 1 = random phase
+  uint64_t seed = 0;
+  int precision = -1;         // -1: the path's default (DOS FP64 as the reference, Kubo FP32)
+  int bounds = 0;             // 0 = ENERGY_RESCALE/SHIFT as given, 1 = Gershgorin x 1.01
+  int energies = 0;           // > 0: also write a DOS on this many equispaced energies
+  int block = 0;
+  std::vector<std::string> unsupported;  // keys that select paths outside this build
+};
+
+// Parses a .in file with main.cpp's token rules. Returns false if unreadable.
+bool parse_input(const std::string& path, JobSpec& spec, std::string& err);
+
+// Runs the job through the C ABI on `device` and writes <job>.cheb (and
+// <job>_matrix.dat / <job>_pos.dat when asked) into `out_dir`.
+leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device, std::string& err);
+
+}  // namespace leo2d_host

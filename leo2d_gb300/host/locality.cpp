@@ -1,0 +1,365 @@
+// locality.cpp - the job driver of the KPM path, host side.
+//
+// Replaces, for one process on one GPU, what the reference spreads over an MPI
+// job farm: Locality::constructGeom (src/locality.cpp:785-1187),
+// rootChebSolve's job and trace-vector set-up (1271-2320) and the worker block
+// of workerChebSolve (3041-3148): geometry and H~ are built on the GPU
+// (leo2d_build_csr), the recursion runs there (leo2d_kpm_dos / _ldos / _cond),
+// the transforms run there (leo2d_dos_transform / leo2d_cond_transform), and
+// the files are written as Param_tools::save (src/params/param_tools.cpp:19-316)
+// and generateRealH (src/locality.cpp:4366-4448) write them.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iomanip>
+#include <random>
+#include <sstream>
+
+#include "job.h"
+
+namespace leo2d_host {
+
+namespace {
+
+struct Ctx {
+  leo2d_ctx* h = nullptr;
+  ~Ctx() {
+    if (h) leo2d_ctx_destroy(h);
+  }
+};
+struct Csr {
+  leo2d_csr* h = nullptr;
+  ~Csr() {
+    if (h) leo2d_csr_destroy(h);
+  }
+};
+
+#define CHECK(call)                                                         \
+  do {                                                                      \
+    leo2d_status st_ = (call);                                              \
+    if (st_ != LEO2D_OK) {                                                  \
+      err = std::string(#call) + ": " + leo2d_last_error(ctx.h);            \
+      return st_;                                                           \
+    }                                                                       \
+  } while (0)
+
+std::string join_path(const std::string& dir, const std::string& name) {
+  if (dir.empty() || dir == ".") return name;
+  return dir.back() == '/' ? dir + name : dir + "/" + name;
+}
+
+// Hstruct::getTargetList, solver type SQ (src/geom/hstruct.cpp:1056-1079):
+// the orbitals of the grid-centre cell of each target sheet.
+bool target_list(const JobSpec& spec, const std::vector<int32_t>& grid4, std::vector<int64_t>& out,
+                 std::string& err) {
+  const leo2d_geom& g = spec.geom;
+  const int64_t n = (int64_t)grid4.size() / 4;
+  for (int ts : spec.target_sheets) {
+    if (ts < 0 || ts >= g.num_sheets) {
+      err = "TARGET_SHEETS names a sheet that does not exist";
+      return false;
+    }
+    const int x_off = (g.max_shape[ts][0] - g.min_shape[ts][0]) / 2;
+    const int y_off = (g.max_shape[ts][1] - g.min_shape[ts][1]) / 2;
+    int64_t center = -1;
+    for (int64_t k = 0; k < n; ++k)
+      if (grid4[4 * k] == x_off && grid4[4 * k + 1] == y_off && grid4[4 * k + 2] == 0 &&
+          grid4[4 * k + 3] == ts) {
+        center = k;
+        break;
+      }
+    if (center < 0) {
+      err = "the centre cell of target sheet " + std::to_string(ts + 1) + " holds no orbital";
+      return false;
+    }
+    for (int orb = 0; orb < 2; ++orb) out.push_back(center + orb);
+  }
+  return true;
+}
+
+void write_energies(std::ofstream& f, const std::vector<double>& E) {
+  for (double e : E) f << e << " ";
+  f << "\n";
+}
+
+}  // namespace
+
+leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device, std::string& err) {
+  if (!spec.unsupported.empty()) {
+    err = "options outside this build's KPM path:";
+    for (const auto& u : spec.unsupported) err += " [" + u + "]";
+    return LEO2D_ERR_UNSUPPORTED;
+  }
+  const int P = spec.poly_order;
+  if (P % 4 != 0 || P < 4) {  // main.cpp:914-917
+    err = "poly_order = " + std::to_string(P) + " is NOT divisible 4 (needed for KPM iterative method)";
+    return LEO2D_ERR_BAD_ARG;
+  }
+  if (spec.solver_type != 1) {
+    err = "SOLVER_TYPE must be SQ (only the uniform-sampling job list is built)";
+    return LEO2D_ERR_UNSUPPORTED;
+  }
+  if (spec.nshifts != 1) {
+    err = "NSHIFTS > 1 (shifted sheet configurations) is not built";
+    return LEO2D_ERR_UNSUPPORTED;
+  }
+  Ctx ctx;
+  {
+    leo2d_status st = leo2d_ctx_create(&ctx.h, device);
+    if (st != LEO2D_OK) {
+      err = "no usable CUDA device";
+      return st;
+    }
+  }
+  leo2d_geom g = spec.geom;
+  CHECK(leo2d_geom_prepare(&g));
+  const bool gersh = spec.bounds == 1;
+  double rescale = g.energy_rescale, shift = g.energy_shift, center = -shift;
+  if (gersh) {
+    g.energy_rescale = 1.0;
+    g.energy_shift = 0.0;
+  }
+  uint32_t flags = 0;
+  if (spec.observable_type == 1 || spec.matrix_save > 1) flags |= LEO2D_CSR_WITH_DX;
+  Csr csr;
+  CHECK(leo2d_build_csr(ctx.h, &g, flags, &csr.h));
+  int64_t n = 0, nnz = 0, ni = 0, ne = 0;
+  CHECK(leo2d_csr_info(csr.h, &n, &nnz, &ni, &ne));
+  std::printf("Heterostructure has %lld orbitals. \n%lld entries expected from intra. \n"
+              "%lld entries expected from inter. \n",
+              (long long)n, (long long)ni, (long long)ne);
+  if (gersh) {
+    double lo = 0, hi = 0;
+    CHECK(leo2d_csr_bounds(ctx.h, csr.h, &lo, &hi));
+    rescale = 1.01 * (hi - lo) / 2;
+    center = (hi + lo) / 2;
+    shift = -center;
+    CHECK(leo2d_csr_rescale(ctx.h, csr.h, rescale, shift));
+  }
+  std::vector<int32_t> grid4(4 * n);
+  std::vector<double> pos(3 * n);
+  CHECK(leo2d_csr_geometry(ctx.h, csr.h, grid4.data(), pos.data()));
+  std::vector<int64_t> targets;
+  if (!target_list(spec, grid4, targets, err)) return LEO2D_ERR_BAD_ARG;
+
+  // Chebyshev nodes of Param_tools::save (param_tools.cpp:57-62); with
+  // Gershgorin bounds the axis is centre + rescale x.
+  std::vector<double> E(P);
+  for (int i = 0; i < P; ++i) {
+    const double x = std::cos((i * 1.0 + 0.5) * M_PI / P);
+    E[i] = gersh ? center + rescale * x : shift + rescale * x;
+  }
+
+  std::ofstream cheb(join_path(out_dir, spec.job_name + ".cheb"));
+  if (!cheb.is_open()) {
+    err = "cannot write " + spec.job_name + ".cheb";
+    return LEO2D_ERR_IO;
+  }
+  cheb << std::fixed;
+  if (spec.verbose_save != 0) {  // Param_tools::saveHeader (param_tools.cpp:467-505)
+    cheb << "JOBID = " << 1 << " \n";
+    cheb << "SHEET: SHIFT_X, SHIFT_Y, SHIFT_Z \n";
+    for (int s = 0; s < g.num_sheets; ++s)
+      cheb << s + 1 << "    : " << 0.0 << ", " << 0.0 << ", " << 0.0 << " \n";
+    cheb << "NUM_TAR = " << targets.size() << "\n";
+    if (!targets.empty()) {
+      cheb << "TAR_LIST: ";
+      for (size_t t = 0; t + 1 < targets.size(); ++t) cheb << targets[t] << ", ";
+      cheb << targets.back() << " \n";
+    } else {
+      cheb << "NO_TAR \n";
+    }
+  }
+
+  leo2d_kpm_cfg cfg{};
+  cfg.poly_order = P;
+  cfg.precision = spec.precision >= 0 ? spec.precision
+                                      : (spec.observable_type == 1 ? LEO2D_FP32 : LEO2D_FP64);
+  cfg.block = spec.block;
+  cfg.seed = spec.seed;
+
+  if (spec.observable_type == 0 && spec.kpm_trace == 1) {
+    // rootChebSolve's trace samples (locality.cpp:2254-2309)
+    int S = spec.kpm_trace_samps;
+    if (S == -1) {
+      S = (int)1.0e6 / ((double)n);
+      if (S < 1) S = 1;
+      if (S > 100) S = 100;
+    }
+    cfg.num_vectors = S;
+    std::vector<double> mu((size_t)S * P);
+    if (spec.vectors == 0) {
+      std::vector<double> vec((size_t)S * n);
+      std::default_random_engine generator;
+      std::normal_distribution<double> distribution(0.0, 1.0);
+      for (int s = 0; s < S; ++s)
+        for (int64_t i = 0; i < n; ++i) vec[(size_t)s * n + i] = distribution(generator);
+      cfg.vector_kind = LEO2D_VEC_HOST;
+      CHECK(leo2d_kpm_dos(ctx.h, csr.h, &cfg, vec.data(), mu.data()));
+    } else {
+      cfg.vector_kind = LEO2D_VEC_PHASE;
+      CHECK(leo2d_kpm_dos(ctx.h, csr.h, &cfg, nullptr, mu.data()));
+    }
+    std::vector<double> dos(P), Ek(P);
+    // densityTransformTrace(results, 1/num_dofs) (locality.cpp:3126-3131)
+    CHECK(leo2d_dos_transform(ctx.h, mu.data(), P, S, rescale, shift, 1.0 / (double)n, dos.data(), Ek.data()));
+    if (spec.verbose_save == 1) {
+      cheb << "E: ";
+      write_energies(cheb, E);
+      cheb << "T: \n";
+      // save() prints cheb_coeffs rows for the job's target list (param_tools.cpp:65-71)
+      for (size_t t = 0; t < targets.size() && t < (size_t)S; ++t) {
+        cheb << targets[t] << ": ";
+        for (int j = 0; j < P - 1; ++j) cheb << mu[t * P + j] << ", ";
+        cheb << mu[t * P + P - 1] << "\n";
+      }
+      cheb << "\n";
+    } else {
+      write_energies(cheb, E);
+      for (int j = 0; j < P - 1; ++j) cheb << dos[j] << " ";
+      cheb << dos[P - 1] << "\n";
+    }
+    if (spec.energies > 0) {
+      std::vector<double> mean(P, 0.0), Eg(spec.energies), d(spec.energies);
+      for (int s = 0; s < S; ++s)
+        for (int j = 0; j < P; ++j) mean[j] += mu[(size_t)s * P + j] / S;
+      for (int k = 0; k < spec.energies; ++k)
+        Eg[k] = center + rescale * (-1.0 + 2.0 * (k + 0.5) / spec.energies);
+      CHECK(leo2d_dos_reconstruct(ctx.h, mean.data(), P, Eg.data(), spec.energies, rescale, center,
+                                  1.0 / (double)n, d.data()));
+      std::ofstream f(join_path(out_dir, spec.job_name + "_dos.dat"));
+      f << std::setprecision(17);
+      for (int k = 0; k < spec.energies; ++k) f << Eg[k] << " " << d[k] << "\n";
+    }
+  } else if (spec.observable_type == 0) {
+    const int64_t T = (int64_t)targets.size();
+    std::vector<double> mu((size_t)T * P);
+    CHECK(leo2d_kpm_ldos(ctx.h, csr.h, &cfg, targets.data(), T, mu.data()));
+    std::vector<double> out = mu;
+    if (spec.dos_transform == 1) {  // Param_tools::densityTransform
+      std::vector<double> Ek(P);
+      for (int64_t t = 0; t < T; ++t)
+        CHECK(leo2d_dos_transform(ctx.h, mu.data() + t * P, P, 1, rescale, shift, 1.0, out.data() + t * P,
+                                  Ek.data()));
+    }
+    if (spec.verbose_save == 1) {
+      cheb << "E: ";
+      write_energies(cheb, E);
+      cheb << "T: \n";
+      for (int64_t t = 0; t < T; ++t) {
+        cheb << targets[t] << ": ";
+        for (int j = 0; j < P - 1; ++j) cheb << out[t * P + j] << ", ";
+        cheb << out[t * P + P - 1] << "\n";
+      }
+      cheb << "\n";
+    } else {
+      write_energies(cheb, E);
+      for (int64_t t = 0; t < T; ++t) {
+        for (int j = 0; j < P - 1; ++j) cheb << out[t * P + j] << " ";
+        cheb << out[t * P + P - 1] << "\n";
+      }
+    }
+  } else {
+    const int64_t T = (int64_t)targets.size();
+    std::vector<double> M((size_t)T * P * P);
+    CHECK(leo2d_kpm_cond(ctx.h, csr.h, &cfg, targets.data(), T, M.data()));
+    std::vector<double> out = M;
+    if (spec.cond_transform == 1)
+      for (int64_t t = 0; t < T; ++t)
+        CHECK(leo2d_cond_transform(ctx.h, M.data() + t * P * P, P, out.data() + t * P * P));
+    if (spec.verbose_save == 0) {  // param_tools.cpp:288-316
+      write_energies(cheb, E);
+      cheb << "\n";
+      for (int64_t t = 0; t < T; ++t) {
+        for (int i = 0; i < P; ++i) {
+          for (int j = 0; j < P; ++j) cheb << out[(size_t)t * P * P + (size_t)i * P + j] << " ";
+          cheb << "\n";
+        }
+        cheb << "\n";
+      }
+    }
+  }
+  cheb.close();
+
+  if (spec.matrix_save > 0) {  // generateRealH's matrix save (locality.cpp:4366-4383)
+    std::vector<int64_t> rp(n + 1);
+    std::vector<int32_t> col(nnz);
+    std::vector<double> val(nnz), dx, dy;
+    if (spec.matrix_save > 1) {
+      dx.resize(nnz);
+      dy.resize(nnz);
+    }
+    CHECK(leo2d_csr_download(ctx.h, csr.h, rp.data(), col.data(), val.data(),
+                             dx.empty() ? nullptr : dx.data(), dy.empty() ? nullptr : dy.data()));
+    auto dump = [&](const std::string& suffix, const std::vector<double>& v) {
+      std::ofstream f(join_path(out_dir, spec.job_name + suffix));
+      for (int64_t i = 0; i < n; ++i)
+        for (int64_t j = rp[i]; j < rp[i + 1]; ++j)
+          if (std::fabs(v[j]) > 1e-12) f << col[j] + 1 << ", " << i + 1 << ", " << v[j] << "\n";
+    };
+    dump("_matrix.dat", val);
+    if (spec.matrix_save > 1) {
+      dump("_dxH_matrix.dat", dx);
+      dump("_dyH_matrix.dat", dy);
+    }
+  }
+  if (spec.matrix_pos_save > 0) {  // locality.cpp:4428-4448
+    std::ofstream f(join_path(out_dir, spec.job_name + "_pos.dat"));
+    f << std::fixed;
+    f.precision(12);
+    for (int64_t i = 0; i < n; ++i)
+      f << pos[3 * i] << "    " << pos[3 * i + 1] << "    " << pos[3 * i + 2] << "    " << grid4[4 * i + 3]
+        << "    " << grid4[4 * i + 2] << "\n";
+  }
+  return LEO2D_OK;
+}
+
+}  // namespace leo2d_host
+
+extern "C" leo2d_status leo2d_run_input(const char* in_path, const char* out_dir, int device, char* msg,
+                                        size_t msg_len) {
+  std::string err;
+  leo2d_status st = LEO2D_OK;
+  try {
+    leo2d_host::JobSpec spec;
+    if (!in_path || !leo2d_host::parse_input(in_path, spec, err)) {
+      st = LEO2D_ERR_IO;
+    } else {
+      st = leo2d_host::run_job(spec, out_dir ? out_dir : ".", device, err);
+    }
+  } catch (const std::exception& e) {
+    err = e.what();
+    st = LEO2D_ERR_CUDA;
+  }
+  if (msg && msg_len) {
+    std::strncpy(msg, err.c_str(), msg_len - 1);
+    msg[msg_len - 1] = 0;
+  }
+  return st;
+}
+
+extern "C" leo2d_status leo2d_parse_input(const char* in_path, leo2d_geom* geom_out, int32_t* ints_out,
+                                          char* msg, size_t msg_len) {
+  std::string err;
+  leo2d_host::JobSpec spec;
+  leo2d_status st = LEO2D_OK;
+  if (!in_path || !leo2d_host::parse_input(in_path, spec, err)) {
+    st = LEO2D_ERR_IO;
+  } else {
+    if (geom_out) *geom_out = spec.geom;
+    if (ints_out) {
+      const int32_t v[10] = {spec.solver_type,    spec.observable_type, spec.poly_order,
+                             spec.kpm_trace,      spec.kpm_trace_samps, spec.verbose_save,
+                             spec.matrix_save,    (int32_t)spec.unsupported.size(),
+                             spec.target_sheets.empty() ? -1 : spec.target_sheets[0], spec.nshifts};
+      for (int i = 0; i < 10; ++i) ints_out[i] = v[i];
+    }
+    for (const auto& u : spec.unsupported) err += "[" + u + "] ";
+  }
+  if (msg && msg_len) {
+    std::strncpy(msg, err.c_str(), msg_len - 1);
+    msg[msg_len - 1] = 0;
+  }
+  return st;
+}

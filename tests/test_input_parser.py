@@ -1,0 +1,60 @@
+"""The C++ .in reader (leo2d_parse_input, host only) against the golden inputs.
+
+The geometry it produces must be identical to the one the golden fixtures
+were generated from, so the GPU job sees the reference's sheets, bounds,
+angles and energy scale bit for bit.
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from leo2d_gb300 import _abi
+from tests._golden import CASES, GOLDEN, parse_in
+
+
+def _parse(path):
+    L = _abi.load()
+    g = _abi.Geom()
+    ints = np.zeros(10, np.int32)
+    msg = ctypes.create_string_buffer(512)
+    st = L.leo2d_parse_input(str(path).encode(), ctypes.byref(g), ints.ctypes.data_as(ctypes.c_void_p),
+                             msg, len(msg))
+    return st, g, ints, msg.value.decode()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_geometry_matches_fixture_spec(name):
+    st, g, ints, msg = _parse(os.path.join(GOLDEN, "inputs", name + ".in"))
+    assert st == 0 and ints[7] == 0, msg
+    ref, kv = parse_in(name)
+    assert bytes(g) == bytes(ref)
+    assert ints[2] == kv["P"] and ints[0] == 1
+    assert ints[8] == kv["target_sheets"][0]
+
+
+def test_unsupported_options_are_reported(tmp_path):
+    p = tmp_path / "x.in"
+    p.write_text("NUM_SHEETS = 1\nSTART_SHEET 1\nMATERIAL = MoS2\nEND_SHEET 1\nUSE_B_FIELD = 1\n"
+                 "STRAIN_TYPE = 2\nPOLY_ORDER = 30\nSOLVER_TYPE = LC\n")
+    st, g, ints, msg = _parse(p)
+    assert st == 0
+    assert ints[7] == 4 and "MoS2" in msg and "USE_B_FIELD" in msg and "STRAIN_TYPE" in msg
+
+
+def test_missing_file():
+    st, g, ints, msg = _parse("/nonexistent/file.in")
+    assert st == _abi.ERR_IO and "not found" in msg
+
+
+def test_model_and_kpm_keys(tmp_path):
+    p = tmp_path / "y.in"
+    p.write_text("MAXSIZE = 30\nMINSIZE = -30\nMAX_R = 25.5\nNUM_SHEETS = 2\nMODEL = SIMPLE\n"
+                 "START_SHEET 1\nMATERIAL = Graphene\nEND_SHEET 1\n"
+                 "START_SHEET 2\nMATERIAL = Graphene\nHEIGHT = 3.35\nANGLE = 1.05\nEND_SHEET 2\n"
+                 "KPM_VECTORS = PHASE\nKPM_SEED = 99\nKPM_BOUNDS = GERSHGORIN\nPOLY_ORDER = 64\n")
+    st, g, ints, msg = _parse(p)
+    assert st == 0 and ints[7] == 0
+    assert g.model == _abi.MODEL_SIMPLE and g.max_R[0] == 25.5 and g.max_R[1] == 25.5
+    assert g.angles[1] == (2 * np.pi * 1.05) / 360.0 and g.heights[1] == 3.35
