@@ -184,6 +184,31 @@ def cpu_time_to_dos(R, n_full, nnz_full, threads, sample):
     return batches * (P // 2) * t_step * scale
 
 
+# ---------------------------------------------------------------- profiling case
+
+def kernel_case(args):
+    """A few Chebyshev-step launches on a mid-size flake, for ncu captures."""
+    import leo2d_gb300 as L
+    radius = args.radius if args.radius != RADIUS else 1000.0
+    with L.Context(0) as ctx:
+        csr = ctx.build_csr(ctx.prepare(geom(L, radius=radius)))
+        lo, hi = csr.bounds()
+        csr.rescale(1.01 * (hi - lo) / 2, -(hi + lo) / 2)
+        cfg = L.kpm_cfg(16, R=max(1, args.kernel_case // 2), block=args.kernel_case, seed=1)
+        for _ in range(2):
+            csr.kpm_dos(cfg)
+        ctx.reset_stats()
+        ctx.set_profiling(True)
+        csr.kpm_dos(cfg)
+        ctx.set_profiling(False)
+        k, ms = ctx.kernel_stats("cheb_step")
+        nnz_true = csr.nnz
+        gbs = step_bytes(csr.n, nnz_true, args.kernel_case) / (ms / k * 1e-3) / 1e9
+        print(json.dumps({"kernel_case": {"n": csr.n, "nnz": csr.nnz, "cols": args.kernel_case,
+                                          "radius_A": radius, "step_ms": round(ms / k, 4),
+                                          "step_gbs": round(gbs, 1)}}))
+
+
 # ---------------------------------------------------------------- main
 
 def main():
@@ -195,7 +220,12 @@ def main():
     ap.add_argument("--radius", type=float, default=RADIUS)
     ap.add_argument("--ref-vectors", type=int, default=256)
     ap.add_argument("--max-vectors", type=int, default=128)
+    ap.add_argument("--kernel-case", type=int, default=0, metavar="COLS",
+                    help="profiling case: two short DOS runs (P=16) of COLS-wide vector blocks on the flake "
+                         "of --radius (1000 A: 2.4M orbitals), then exit; prints no bench line")
     args = ap.parse_args()
+    if args.kernel_case:
+        return kernel_case(args)
     ws, rank, local, pg = dist_setup()
     threads = os.cpu_count() or 1
 
@@ -299,12 +329,16 @@ def main():
     peak, peak_kind = peaks()
     bytes_step = step_bytes(n, nnz, cols)  # per launch: one pass over one vector block
     achieved = bytes_step / (k_ms / k_n / 1000.0) / 1e9 if k_n else None
+    # DRAM bytes per launch from the committed ncu capture of the same kernel on
+    # a 2.4M-orbital flake, scaled to this launch by the algorithmic bytes
+    # (traffic grows with rows and entries; the capture's ratio is 0.995)
     traffic = None
-    tp = os.path.join(REPO, "profiles", "traffic.json")
+    tp = os.path.join(REPO, "profiles", "cheb_step_traffic.json")
     if os.path.exists(tp):
         try:
-            traffic = json.load(open(tp)).get("cheb_step_bytes_per_launch_10M")
-        except Exception:
+            t = json.load(open(tp))
+            traffic = int(bytes_step * t["dram_bytes_per_launch"] / t["algorithmic_bytes_per_launch"])
+        except (OSError, ValueError, KeyError, ZeroDivisionError):
             traffic = None
 
     out = {

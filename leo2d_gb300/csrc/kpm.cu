@@ -448,27 +448,38 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? 3 : 1) k_cheb_tile(co
       T acc[V];
 #pragma unroll
       for (int v = 0; v < V; ++v) acc[v] = T(0);
-      for (int k = beg; k < end; k += 8) {
+      // (AoS) entries are read two per 16-byte shared load from an even index;
+      // the stage holds 8 entries of slack past the last tile's end for this.
+      const int k0 = kAoS ? (beg & ~1) : beg;
+      for (int k = k0; k < end; k += 8) {
         int c[8];
         T w[8];
+        bool in[8];
         Pack<T, V> x[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const bool in = k + u < end;
-          if constexpr (kAoS) {
-            const uint2 e = in ? ent_s[k + u] : make_uint2(0u, 0u);
-            c[u] = (int)e.x;
-            w[u] = __uint_as_float(e.y);
-          } else {
-            c[u] = in ? col_s[k + u] : 0;
-            w[u] = in ? val_s[k + u] : T(0);
+        for (int u = 0; u < 8; ++u) in[u] = (k + u >= beg) && (k + u < end);
+        if constexpr (kAoS) {
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            const uint4 e = reinterpret_cast<const uint4*>(ent_s)[(k >> 1) + h];
+            c[2 * h] = (int)e.x;
+            w[2 * h] = __uint_as_float(e.y);
+            c[2 * h + 1] = (int)e.z;
+            w[2 * h + 1] = __uint_as_float(e.w);
+          }
+        } else {
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            c[u] = in[u] ? col_s[k + u] : 0;
+            w[u] = in[u] ? val_s[k + u] : T(0);
           }
         }
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-          if (k + u < end) {
+          if (in[u]) {
             x[u] = ld_gather<T, V>(a.tn + (int64_t)c[u] * C + sub * V);
           } else {
+            w[u] = T(0);
 #pragma unroll
             for (int v = 0; v < V; ++v) x[u].v[v] = T(0);
           }
@@ -874,7 +885,7 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
       cached_rows = tile_rows;
     }
     auto up = [](int64_t x, int64_t a_) { return (x + a_ - 1) / a_ * a_; };
-    tile_cap = (int)up(cached_max + 4, 4);
+    tile_cap = (int)up(cached_max + 8, 4);  // + slack for the paired entry reads
     const size_t esz = s.fp64 ? sizeof(double) : sizeof(float);
     tile_rp_bytes = (int)up((int64_t)(tile_rows + 4) * 8, 128);
     if (s.fp64) {
