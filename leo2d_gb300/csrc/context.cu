@@ -285,6 +285,11 @@ leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value
     if (k == "step_kernel") {
       LEO_REQUIRE(value == 0 || value == 1, "step_kernel must be 0 or 1");
       ctx->kernel_variant = (int)value;
+    } else if (k == "test_unsatisfied_wait") {
+      // every tiled step waits on an mbarrier that never completes, gives up
+      // after the spin limit and reports LEO2D_ERR_TIMEOUT (tests the bounded
+      // wait without faulting or hanging anything)
+      ctx->test_unsatisfied_wait = value != 0;
     } else if (k == "tile_stages") {
       LEO_REQUIRE(value >= 2 && value <= 4, "tile_stages must be 2..4");
       ctx->tile_stages = (int)value;

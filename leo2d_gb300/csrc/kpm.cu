@@ -335,6 +335,7 @@ struct TileArgs {
   TileLayout lay;
   uint64_t spin_limit;
   int* status;
+  int never_wait;  // test hook: wait on a barrier that nobody completes
 };
 
 template <typename T, int V, int LPR, int WARPS>
@@ -353,6 +354,7 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? 3 : 1) k_cheb_tile(co
   __shared__ __align__(8) uint64_t full[kMaxStages];
   __shared__ int released[kMaxStages];  // warps done with the stage's current tile
   __shared__ int issued[kMaxStages];    // copies issued into the stage so far
+  __shared__ __align__(8) uint64_t never;  // test hook barrier: no arrivals
   if (a.prev_partials) reduce_prev<C, NT>(a.prev_partials, a.prev_dots, gridDim.x);
 
   const int TR = L.tile_rows;
@@ -363,6 +365,7 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? 3 : 1) k_cheb_tile(co
       released[i] = 0;
       issued[i] = 0;
     }
+    mbar_init(&never, 1);
     mbar_fence_init();
   }
   __syncthreads();
@@ -415,10 +418,16 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? 3 : 1) k_cheb_tile(co
 #pragma unroll
   for (int v = 0; v < V; ++v) d0[v] = d1[v] = 0.0;
 
+  bool gave_up = false;
+  if (ta.never_wait && !bounded_wait(&never, 0u, ta.spin_limit)) {
+    if (lane == 0) atomicExch(ta.status, kStatusTimeout);
+    gave_up = true;
+  }
+
   // Warps advance independently: no block barrier per tile. The last warp to
   // release a stage refills it with the tile nst steps ahead.
   int it = 0;
-  for (int64_t tile = tile_of(0); tile < n_tiles; tile = tile_of(++it)) {
+  for (int64_t tile = tile_of(0); !gave_up && tile < n_tiles; tile = tile_of(++it)) {
     const int stage = it % nst;
     const uint32_t parity = (uint32_t)(it / nst) & 1u;
     if (!bounded_wait(&full[stage], parity, ta.spin_limit)) {
@@ -517,10 +526,12 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? 3 : 1) k_cheb_tile(co
     __syncwarp();
   }
   __syncthreads();
-  // after a timeout a copy may still be in flight: it must land before exit
+  // after a timeout a copy may still be in flight: it must land before exit.
+  // Copies finish in microseconds, so this drain is bounded by time only
+  // (two seconds), not by the context's poll limit.
   if (threadIdx.x == 0)
     for (int i = 0; i < nst; ++i)
-      if (issued[i] > 0) bounded_wait(&full[i], (uint32_t)(issued[i] - 1) & 1u, ta.spin_limit);
+      if (issued[i] > 0) bounded_wait(&full[i], (uint32_t)(issued[i] - 1) & 1u, ~0ull);
 
 #pragma unroll
   for (int o = LPR; o < 32; o <<= 1)
@@ -813,12 +824,13 @@ void enqueue_steps(Recursion& r) {
     a.prev_partials = k == 0 ? nullptr : r.partials.p + (size_t)((k + 1) % 2) * r.grid * 2 * C;
     a.prev_dots = k == 0 ? nullptr : r.dots.p + (size_t)(k - 1) * 2 * C;
     if (r.shape.tiled) {
-      TileArgs<T> ta;
+      TileArgs<T> ta{};
       ta.s = a;
       ta.lay = TileLayout{r.tile_stages, r.tile_chunk, r.tile_rows, r.tile_cap, r.tile_rp_bytes, r.tile_col_bytes,
                           r.tile_stage_bytes};
       ta.spin_limit = ctx->spin_limit;
       ta.status = ctx->status.p;
+      ta.never_wait = ctx->test_unsatisfied_wait;
       tile_dispatch<T>(ctx, C, r.grid, r.dyn_smem, &ta, nullptr, 0, r.shape.warps);
     } else {
       launch_step<T>(ctx, C, r.grid, a);
@@ -956,12 +968,13 @@ void one_step(Recursion& r, const void* in, void* out, const void* prev, bool fi
   a.prev_partials = nullptr;
   a.prev_dots = nullptr;
   if (r.shape.tiled) {
-    TileArgs<T> ta;
+    TileArgs<T> ta{};
     ta.s = a;
     ta.lay = TileLayout{r.tile_stages, r.tile_chunk, r.tile_rows, r.tile_cap, r.tile_rp_bytes, r.tile_col_bytes,
                         r.tile_stage_bytes};
     ta.spin_limit = ctx->spin_limit;
     ta.status = ctx->status.p;
+    ta.never_wait = ctx->test_unsatisfied_wait;
     tile_dispatch<T>(ctx, C, r.grid, r.dyn_smem, &ta, nullptr, 0, r.shape.warps);
   } else {
     launch_step<T>(ctx, C, r.grid, a);
