@@ -230,3 +230,42 @@ class Csr:
         self.ctx.check(self.ctx.lib.leo2d_kpm_ldos(self.ctx.h, self.h, ctypes.byref(cfg), _p(t), len(t),
                                                    _p(mu)))
         return mu
+
+
+class Batch:
+    """Several rescaled matrices run together: one launch per Chebyshev step, one
+    CUDA graph per run (leo2d_batch_*). The matrices must outlive the batch."""
+
+    def __init__(self, ctx, csrs, cfg):
+        self.ctx = ctx
+        self.csrs = list(csrs)  # keeps the matrices alive
+        self.cfg = cfg
+        arr = (ctypes.c_void_p * len(self.csrs))(*[c.h for c in self.csrs])
+        h = ctypes.c_void_p()
+        ctx.check(ctx.lib.leo2d_batch_create(ctx.h, arr, len(self.csrs), ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+        cols, warps, rows, grid = (ctypes.c_int32() for _ in range(4))
+        lpr = ctypes.c_int64()
+        ctx.check(ctx.lib.leo2d_batch_info(h, ctypes.byref(cols), ctypes.byref(warps), ctypes.byref(rows),
+                                           ctypes.byref(grid), ctypes.byref(lpr)))
+        self.block_cols, self.warps, self.rows_per_item = cols.value, warps.value, rows.value
+        self.grid, self.launches_per_run = grid.value, lpr.value
+
+    def run(self, seed=None, first_vector=None):
+        """Moments [num matrices][R][P] of one replay."""
+        seed = self.cfg.seed if seed is None else seed
+        first = self.cfg.first_vector if first_vector is None else first_vector
+        mu = np.zeros((len(self.csrs), self.cfg.num_vectors, self.cfg.poly_order))
+        self.ctx.check(self.ctx.lib.leo2d_batch_run(self.h, seed, first, _p(mu)))
+        return mu
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.leo2d_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

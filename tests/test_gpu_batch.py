@@ -1,0 +1,88 @@
+"""Batched flakes: one launch per Chebyshev step over several matrices, replayed
+from a CUDA graph (leo2d_batch_*).
+
+Each flake's moments must equal those of the single-matrix recursion on the
+same Philox vectors. Both are FP32 recursions with FP64 moment sums, but the
+batched grid splits rows into different tiles, so FP32 partial sums round
+differently: tolerance 1e-5 of the largest moment. One flake is also checked
+against the FP64 oracle (1e-4, the FP32 bar). Replays are bit-identical.
+"""
+import numpy as np
+import pytest
+
+import leo2d_gb300 as L
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+FP32_RTOL = 1e-4
+
+
+def _rel(a, b):
+    return np.max(np.abs(a - b)) / np.max(np.abs(b))
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    with L.Context(0) as c:
+        yield c
+
+
+@pytest.fixture(scope="module")
+def flakes(ctx):
+    out = []
+    for size, twist in ((9, 1.2), (14, 2.5), (6, 0.9), (20, 3.0)):
+        g = L.make_geom(model=L.MODEL_SIMPLE, size=size, angles_deg=(0.0, twist), energy_rescale=1.0)
+        csr = ctx.build_csr(ctx.prepare(g))
+        lo, hi = csr.bounds()
+        csr.rescale(1.01 * (hi - lo) / 2, -(hi + lo) / 2)
+        out.append(csr)
+    return out
+
+
+@pytest.mark.parametrize("block", [0, 8, 16, 32, 64])
+def test_batch_matches_single(ctx, flakes, block):
+    P, R, seed = 64, 5, 17
+    cfg = L.kpm_cfg(P, R=R, seed=seed, block=block)
+    b = L.Batch(ctx, flakes, cfg)
+    mu = b.run()
+    assert mu.shape == (len(flakes), R, P)
+    for f, csr in enumerate(flakes):
+        single = csr.kpm_dos(L.kpm_cfg(P, R=R, seed=seed))
+        assert _rel(mu[f], single) < 1e-5, (f, block)
+    again = b.run()
+    np.testing.assert_array_equal(mu, again)
+    if block:
+        assert b.block_cols == block
+    assert b.launches_per_run >= P // 2
+    b.close()
+
+
+def test_batch_seed_and_first_vector(ctx, flakes):
+    P, R = 32, 3
+    b = L.Batch(ctx, flakes[:2], L.kpm_cfg(P, R=R, seed=1, block=16))
+    mu = b.run(seed=99, first_vector=7)
+    for f in range(2):
+        single = flakes[f].kpm_dos(L.kpm_cfg(P, R=R, seed=99, first_vector=7))
+        assert _rel(mu[f], single) < 1e-5
+    b.close()
+
+
+def test_batch_vs_oracle(ctx, flakes):
+    P, R, seed = 48, 4, 3
+    b = L.Batch(ctx, flakes, L.kpm_cfg(P, R=R, seed=seed, block=16))
+    mu = b.run()
+    csr = flakes[1]
+    rp, col, val = csr.download()
+    re, im = oracle.phase_vectors(seed, 0, R, csr.n)
+    ref = oracle.kpm_trace(rp, col, val, re, P, literal=False) + oracle.kpm_trace(rp, col, val, im, P, literal=False)
+    assert _rel(mu[1], ref) < FP32_RTOL
+    b.close()
+
+
+def test_batch_rejects(ctx, flakes):
+    with pytest.raises(L.Leo2dError, match="twice"):
+        L.Batch(ctx, [flakes[0], flakes[0]], L.kpm_cfg(16, R=1))
+    with pytest.raises(L.Leo2dError, match="FP32"):
+        L.Batch(ctx, flakes[:1], L.kpm_cfg(16, R=1, precision=L.FP64))
+    with pytest.raises(L.Leo2dError, match="random-phase"):
+        L.Batch(ctx, flakes[:1], L.kpm_cfg(16, R=1, kind=L.VEC_GAUSSIAN))
