@@ -235,6 +235,17 @@ leo2d_status leo2d_batch_info(const leo2d_batch* b, int32_t* block_cols, int32_t
                               int32_t* rows_per_item, int32_t* grid, int64_t* launches_per_run);
 leo2d_status leo2d_batch_destroy(leo2d_batch* b);
 
+/* ---------------------------------------------------------------- tensor cores */
+
+/* D[M][N] = A[M][K] * B[N][K]^T with BF16 inputs (raw bits, row-major, K
+ * contiguous) and FP32 accumulation, on the tcgen05 tensor cores (TMA-staged
+ * operands, TMEM accumulator). The learned control variate's forward and
+ * backward passes run on this kernel with fused epilogues; this entry point
+ * exposes the plain product (host buffers) so it can be checked on its own.
+ * K must be a multiple of 8. No counterpart in the reference. */
+leo2d_status leo2d_tc_gemm(leo2d_ctx* ctx, const uint16_t* a, const uint16_t* b, int64_t M, int64_t N,
+                           int64_t K, float* d);
+
 /* ---------------------------------------------------------------- (c) Kubo conductivity */
 
 /* Two-index Chebyshev moments of the current-current correlation.

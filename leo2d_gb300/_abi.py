@@ -136,6 +136,7 @@ def _declare(lib):
     fn("leo2d_batch_run", c_i32, c_void_p, c_u64, c_u64, P)
     fn("leo2d_batch_info", c_i32, c_void_p, P, P, P, P, P)
     fn("leo2d_batch_destroy", c_i32, c_void_p)
+    fn("leo2d_tc_gemm", c_i32, c_void_p, P, P, c_i64, c_i64, c_i64, P)
     fn("leo2d_kpm_cond", c_i32, c_void_p, c_void_p, cp, P, c_i64, P)
     fn("leo2d_cond_transform", c_i32, c_void_p, P, c_i32, P)
     fn("leo2d_cond_sigma", c_i32, c_void_p, P, c_i32, P, c_i64, c_dbl, c_dbl, c_dbl, P)

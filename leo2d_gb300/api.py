@@ -127,6 +127,18 @@ class Context:
                                              center, scale, _p(out)))
         return out
 
+    def tc_gemm(self, a_bf16, b_bf16):
+        """D = A B^T on the tensor cores; a [M][K], b [N][K] as uint16 BF16 bits."""
+        a = np.ascontiguousarray(a_bf16, np.uint16)
+        b = np.ascontiguousarray(b_bf16, np.uint16)
+        M, K = a.shape
+        N, K2 = b.shape
+        if K != K2:
+            raise ValueError("inner dimensions differ")
+        d = np.zeros((M, N), np.float32)
+        self.check(self.lib.leo2d_tc_gemm(self.h, _p(a), _p(b), M, N, K, _p(d)))
+        return d
+
     def dos_reconstruct(self, mu, energies, rescale, center, scale=1.0):
         mu = np.ascontiguousarray(mu, np.float64)
         E = np.ascontiguousarray(energies, np.float64)

@@ -1,0 +1,243 @@
+// tc_gemm.cu - tcgen05 / TMA / TMEM GEMM with fused MLP epilogues (see tc_gemm.cuh).
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <mutex>
+
+#include "tc_gemm.cuh"
+
+using namespace leo2d;
+
+namespace {
+
+constexpr int BM = kGemmBM, BK = kGemmBK, ST = kGemmStages, BN = 256;
+constexpr uint32_t kABytes = BM * BK * 2, kBBytes = BN * BK * 2, kStage = kABytes + kBBytes;
+constexpr uint32_t kIdesc = umma::idesc_bf16(BM, BN);
+
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float z) {
+  return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * expf(-0.5f * z * z) * 0.39894228040143268f;
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(128, 1)
+    k_tc_gemm(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const GemmArgs g) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ __align__(8) uint64_t full[ST], empty[ST], done;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  __shared__ double wsum[4][EPI == kEpiBias ? BN : 1];
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < ST; ++s) {
+      umma::bar_init(&full[s], 1);
+      umma::bar_init(&empty[s], 1);
+    }
+    umma::bar_init(&done, 1);
+    umma::bar_fence_init();
+    abort_flag = 0;
+  }
+  if (EPI == kEpiBias)
+    for (int i = threadIdx.x; i < 4 * BN; i += 128) (&wsum[0][0])[i] = 0.0;
+  if (warp == 0) umma::tmem_alloc(&tmem_base, BN);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+
+  const int m_tiles = (g.M + BM - 1) / BM, n_tiles = (g.N + BN - 1) / BN;
+  const int nkb = (g.K + BK - 1) / BK;
+  uint32_t it = 0;
+  int local = 0;
+  for (int t = blockIdx.x; t < m_tiles * n_tiles; t += gridDim.x, ++local) {
+    const int mt = t % m_tiles, nt = t / m_tiles;
+    if (warp == 0 && lane == 0) {
+      // producer: TMA tiles of A and B into the ring
+      for (int kb = 0; kb < nkb && !abort_flag; ++kb) {
+        const uint32_t i = it + kb, s = i % ST, ph = (i / ST) & 1u;
+        if (!umma::bar_wait(&empty[s], ph ^ 1u)) {
+          abort_flag = 1;
+          break;
+        }
+        unsigned char* st = smem + (size_t)s * kStage;
+        umma::bar_expect_tx(&full[s], kStage);
+        umma::tma_load_2d(st, &ta, kb * BK, mt * BM, &full[s]);
+        umma::tma_load_2d(st + kABytes, &tb, kb * BK, nt * BN, &full[s]);
+      }
+    } else if (warp == 1 && lane == 0) {
+      // MMA issuer
+      for (int kb = 0; kb < nkb && !abort_flag; ++kb) {
+        const uint32_t i = it + kb, s = i % ST, ph = (i / ST) & 1u;
+        if (!umma::bar_wait(&full[s], ph)) {
+          abort_flag = 1;
+          break;
+        }
+        umma::fence_after_sync();
+        const uint32_t a0 = umma::saddr(smem + (size_t)s * kStage), b0 = a0 + kABytes;
+#pragma unroll
+        for (int k = 0; k < BK / 16; ++k)
+          umma::mma_bf16(tmem, umma::desc_k128(a0 + 32 * k), umma::desc_k128(b0 + 32 * k), kIdesc,
+                         (kb | k) != 0 ? 1u : 0u);
+        umma::mma_commit(&empty[s]);
+      }
+      umma::mma_commit(&done);  // arrives when every MMA of this tile has finished
+    }
+    it += nkb;
+    __syncwarp();
+    const int late = umma::bar_wait(&done, (uint32_t)local & 1u) ? 0 : 1;
+    if (__syncthreads_or(late | abort_flag)) {  // the whole block leaves together
+      abort_flag = 1;
+      break;
+    }
+    umma::fence_after_sync();
+
+    // epilogue: thread = one row of the tile
+    const int r = mt * BM + warp * 32 + lane;
+    const bool row_ok = r < g.M;
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      const int n0 = nt * BN + c0;
+      if (n0 >= g.N) break;
+      float v[16];
+      umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      const int cnt = min(16, g.N - n0);
+      if (EPI == kEpiBias && g.colsum) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          double x = (row_ok && j < cnt) ? (double)(v[j] + g.bias[n0 + j]) : 0.0;
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+          if (lane == 0 && j < cnt) wsum[warp][c0 + j] += x;
+        }
+        continue;
+      }
+      if (!row_ok) continue;
+      const size_t base = (size_t)r * g.N + n0;
+      if (EPI == kEpiF32) {
+        for (int j = 0; j < cnt; ++j) g.out_f32[base + j] = v[j];
+      } else if (EPI == kEpiBias) {
+        for (int j = 0; j < cnt; ++j) g.out_f32[base + j] = v[j] + g.bias[n0 + j];
+      } else if (EPI == kEpiBiasGelu) {
+        for (int j = 0; j < cnt; ++j) {
+          const float z = v[j] + g.bias[n0 + j];
+          if (g.zout) g.zout[base + j] = z;
+          const __nv_bfloat16 h = __float2bfloat16_rn(gelu(z));
+          if (g.out_bf16) g.out_bf16[base + j] = h;
+          if (g.out_bf16_t) g.out_bf16_t[(size_t)(n0 + j) * g.ld_t + r] = h;
+        }
+      } else {  // kEpiGeluBwd
+        for (int j = 0; j < cnt; ++j) {
+          const float gz = v[j] * gelu_grad(g.zin[base + j]);
+          if (g.out_f32) g.out_f32[base + j] = gz;
+          const __nv_bfloat16 h = __float2bfloat16_rn(gz);
+          if (g.out_bf16) g.out_bf16[base + j] = h;
+          if (g.out_bf16_t) g.out_bf16_t[(size_t)(n0 + j) * g.ld_t + r] = h;
+        }
+      }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (abort_flag && threadIdx.x == 0) atomicExch(g.status, kStatusTimeout);
+  if (EPI == kEpiBias && g.colsum)
+    for (int n = threadIdx.x; n < g.N && n < BN; n += 128)
+      g.colsum[(size_t)blockIdx.x * g.N + n] = ((wsum[0][n] + wsum[1][n]) + wsum[2][n]) + wsum[3][n];
+  if (warp == 0) umma::tmem_dealloc(tmem, BN);
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+}  // namespace
+
+namespace leo2d {
+
+void make_tmap_bf16(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, int box_rows) {
+  make_tmap_bf16_ld(map, base, rows, cols, cols, box_rows);
+}
+
+void make_tmap_bf16_ld(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, int64_t ld, int box_rows) {
+  auto fn = encode_fn();
+  LEO_REQUIRE(fn != nullptr, "cuTensorMapEncodeTiled is not available from the driver");
+  LEO_REQUIRE(((uintptr_t)base & 15) == 0, "tensor base must be 16-byte aligned");
+  LEO_REQUIRE((ld * 2) % 16 == 0, "tensor row stride must be a multiple of 16 bytes");
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
+  cuuint32_t box[2] = {(cuuint32_t)kGemmBK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  LEO_REQUIRE(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled rejected the tensor");
+}
+
+void tc_gemm(leo2d_ctx* ctx, GemmEpi epi, const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g,
+             int grid_cap) {
+  LEO_REQUIRE(g.M > 0 && g.N > 0 && g.K > 0, "empty GEMM");
+  const size_t smem = gemm_smem_bytes(BN);
+  const int tiles = ((g.M + BM - 1) / BM) * ((g.N + BN - 1) / BN);
+  int grid = std::min(tiles, ctx->sm_count);
+  if (grid_cap > 0) grid = std::min(grid, grid_cap);
+  auto go = [&](auto kern) {
+    LEO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    launch(ctx, "tc_gemm", [&] { kern<<<grid, 128, smem, ctx->stream>>>(ta, tb, g); });
+  };
+  switch (epi) {
+    case kEpiF32: return go(k_tc_gemm<kEpiF32>);
+    case kEpiBias: return go(k_tc_gemm<kEpiBias>);
+    case kEpiBiasGelu: return go(k_tc_gemm<kEpiBiasGelu>);
+    case kEpiGeluBwd: return go(k_tc_gemm<kEpiGeluBwd>);
+  }
+  fail(LEO2D_ERR_BAD_ARG, "unknown GEMM epilogue");
+}
+
+int tc_gemm_grid(leo2d_ctx* ctx, int M, int N) {
+  const int tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+  return std::min(tiles, ctx->sm_count);
+}
+
+}  // namespace leo2d
+
+// ---------------------------------------------------------------- C ABI
+
+extern "C" leo2d_status leo2d_tc_gemm(leo2d_ctx* ctx, const uint16_t* a, const uint16_t* b, int64_t M, int64_t N,
+                                      int64_t K, float* d) {
+  if (!ctx || !a || !b || !d) return LEO2D_ERR_BAD_ARG;
+  return guard(ctx, [&] {
+    LEO_REQUIRE(M >= 1 && N >= 1 && K >= 1 && M < (1ll << 31) && N < (1ll << 31) && K < (1ll << 31),
+                "sizes must be in [1, 2^31)");
+    LEO_REQUIRE(K % 8 == 0, "K must be a multiple of 8 (16-byte rows)");
+    LEO_CUDA(cudaSetDevice(ctx->device));
+    DevBuf<__nv_bfloat16> da((size_t)M * K), db((size_t)N * K);
+    DevBuf<float> dd((size_t)M * N);
+    h2d(ctx, reinterpret_cast<uint16_t*>(da.p), a, (size_t)M * K);
+    h2d(ctx, reinterpret_cast<uint16_t*>(db.p), b, (size_t)N * K);
+    CUtensorMap ta, tb;
+    make_tmap_bf16(&ta, da.p, M, K, BM);
+    make_tmap_bf16(&tb, db.p, N, K, BN);
+    GemmArgs g{};
+    g.M = (int)M;
+    g.N = (int)N;
+    g.K = (int)K;
+    g.out_f32 = dd.p;
+    g.status = ctx->status.p;
+    tc_gemm(ctx, kEpiF32, ta, tb, g);
+    d2h(ctx, d, dd.p, (size_t)M * N);
+    ctx_check_status(ctx, "tensor-core GEMM");
+  });
+}
