@@ -159,6 +159,12 @@ leo2d_status leo2d_csr_bounds(leo2d_ctx* ctx, const leo2d_csr* csr, double* emin
 /* In place: H <- (H + shift*I) / rescale (FP64, then the FP32 copy is refreshed). */
 leo2d_status leo2d_csr_rescale(leo2d_ctx* ctx, leo2d_csr* csr, double rescale, double shift);
 
+/* Per-orbital local stacking disregistry of a bilayer, out[n][2] in [0,1)^2:
+ * Hstruct::getShiftConfigs (src/geom/hstruct.cpp:672-820), bit-exact. The
+ * learned control variate's site feature. Needs a matrix built by
+ * leo2d_build_csr with two sheets. */
+leo2d_status leo2d_csr_shift_configs(leo2d_ctx* ctx, const leo2d_csr* csr, double* out);
+
 /* ---------------------------------------------------------------- (b) KPM DOS */
 
 typedef enum {

@@ -127,6 +127,7 @@ def _declare(lib):
     fn("leo2d_csr_upload", c_i32, c_void_p, c_i64, c_i64, P, P, P, P, P, pp)
     fn("leo2d_csr_bounds", c_i32, c_void_p, c_void_p, P, P)
     fn("leo2d_csr_rescale", c_i32, c_void_p, c_void_p, c_dbl, c_dbl)
+    fn("leo2d_csr_shift_configs", c_i32, c_void_p, c_void_p, P)
     fn("leo2d_kpm_dos", c_i32, c_void_p, c_void_p, cp, P, P)
     fn("leo2d_kpm_ldos", c_i32, c_void_p, c_void_p, cp, P, c_i64, P)
     fn("leo2d_kpm_autotune", c_i32, c_void_p, c_void_p, cp, P, P)

@@ -201,6 +201,12 @@ class Csr:
         self.ctx.check(self.ctx.lib.leo2d_csr_geometry(self.ctx.h, self.h, _p(grid), _p(pos)))
         return grid, pos
 
+    def shift_configs(self):
+        """Per-orbital disregistry [n][2] (Hstruct::getShiftConfigs); bilayers."""
+        out = np.zeros((self.n, 2))
+        self.ctx.check(self.ctx.lib.leo2d_csr_shift_configs(self.ctx.h, self.h, _p(out)))
+        return out
+
     def bounds(self):
         lo, hi = ctypes.c_double(), ctypes.c_double()
         self.ctx.check(self.ctx.lib.leo2d_csr_bounds(self.ctx.h, self.h, ctypes.byref(lo),

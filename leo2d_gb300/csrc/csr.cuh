@@ -54,5 +54,7 @@ void csr_alloc_rowptr(leo2d_ctx* ctx, leo2d_csr* csr, int64_t n);
 void csr_alloc_entries(leo2d_ctx* ctx, leo2d_csr* csr, int64_t nnz, bool with_dx);
 // Builds / drops the locality-ordered copy (patch = real-space patch edge, A).
 void csr_build_reordered(leo2d_ctx* ctx, leo2d_csr* csr, double patch, bool with_fp64);
+// Per-orbital disregistry (Hstruct::getShiftConfigs) into device memory out[n][2]; bilayers.
+void csr_shift_configs(leo2d_ctx* ctx, const leo2d_csr* csr, double* out);
 void csr_drop_reordered(leo2d_csr* csr);
 }  // namespace leo2d

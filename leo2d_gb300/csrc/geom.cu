@@ -616,6 +616,49 @@ __global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, in
     b[i] = (float)a[i];
 }
 
+// ---------------------------------------------------------------- disregistry
+
+// Inverse of each sheet's rotated unit cell (computed on the host with the
+// same libm calls as the reference).
+struct CellInv {
+  double inv[2][2][2];
+};
+
+// Hstruct::getShiftConfigs (src/geom/hstruct.cpp:672-820), bilayers: the
+// fractional offset of orbital k's cell site (orbital 0) from the site of the
+// other sheet that Hstruct::findNearest picks, in the other sheet's rotated
+// lattice, wrapped to [0,1) by the reference's loops.
+__global__ void k_shift_configs(const __grid_constant__ GeomDev G, const CellInv ci, int64_t n,
+                                const int32_t* __restrict__ grid4, double* __restrict__ out) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int s_here = grid4[4 * k + 3];
+    const int s = s_here == 0 ? 1 : 0;
+    const SheetDev& a = G.sh[s_here];
+    const SheetDev& b = G.sh[s];
+    double orig[3];
+    pos_grid(a, grid4[4 * k], grid4[4 * k + 1], 0, orig);
+    double here[3];
+    here[0] = a.cos_t * orig[0] - a.sin_t * orig[1];
+    here[1] = a.sin_t * orig[0] + a.cos_t * orig[1];
+    here[2] = 0.0;
+    const int ni = find_nearest_h(b, here, 0), nj = find_nearest_h(b, here, 1);
+    double sp[3];
+    pos_grid(b, ni, nj, 0, sp);
+    const double np0 = b.cos_t * sp[0] - b.sin_t * sp[1];
+    const double np1 = b.sin_t * sp[0] + b.cos_t * sp[1];
+    const double cr0 = here[0] - np0, cr1 = here[1] - np1;
+    double c0 = cr0 * ci.inv[s][0][0] + cr1 * ci.inv[s][0][1];
+    double c1 = cr0 * ci.inv[s][1][0] + cr1 * ci.inv[s][1][1];
+    while (c0 >= 1) c0 += -1;
+    while (c0 < 0) c0 += 1;
+    while (c1 >= 1) c1 += -1;
+    while (c1 < 0) c1 += 1;
+    out[2 * k] = c0;
+    out[2 * k + 1] = c1;
+  }
+}
+
 // ---------------------------------------------------------------- host
 
 void fill_sheet(const leo2d_geom& g, int s, SheetDev& d) {
@@ -877,4 +920,52 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
   }
   *out = csr;
   return LEO2D_OK;
+}
+
+namespace leo2d {
+
+// Disregistry of every orbital into device memory out[n][2].
+void csr_shift_configs(leo2d_ctx* ctx, const leo2d_csr* csr, double* out) {
+  LEO_REQUIRE(csr->has_geom && csr->grid4.p, "matrix has no geometry (uploaded without it)");
+  const leo2d_geom& g = csr->geom;
+  LEO_REQUIRE(g.num_sheets == 2, "disregistry is defined for bilayers (two sheets)");
+  GeomDev G;
+  std::memset(&G, 0, sizeof(G));
+  G.S = g.num_sheets;
+  G.model = g.model;
+  G.bc = g.boundary_condition;
+  for (int s = 0; s < G.S; ++s) fill_sheet(g, s, G.sh[s]);
+  CellInv ci;
+  for (int s = 0; s < 2; ++s) {
+    const double theta = g.angles[s];
+    const SheetDev& d = G.sh[s];
+    double u[2][2];
+    u[0][0] = std::cos(theta) * d.a[0][0] - std::sin(theta) * d.a[0][1];
+    u[0][1] = std::sin(theta) * d.a[0][0] + std::cos(theta) * d.a[0][1];
+    u[1][0] = std::cos(theta) * d.a[1][0] - std::sin(theta) * d.a[1][1];
+    u[1][1] = std::sin(theta) * d.a[1][0] + std::cos(theta) * d.a[1][1];
+    const double det = u[0][0] * u[1][1] - u[0][1] * u[1][0];
+    ci.inv[s][0][0] = u[1][1] / det;
+    ci.inv[s][0][1] = -u[1][0] / det;
+    ci.inv[s][1][0] = -u[0][1] / det;
+    ci.inv[s][1][1] = u[0][0] / det;
+  }
+  if (csr->n > 0)
+    launch(ctx, "shift_configs", [&] {
+      k_shift_configs<<<grid_for(csr->n, 256, (int64_t)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
+          G, ci, csr->n, csr->grid4.p, out);
+    });
+}
+
+}  // namespace leo2d
+
+extern "C" leo2d_status leo2d_csr_shift_configs(leo2d_ctx* ctx, const leo2d_csr* csr, double* out) {
+  if (!ctx || !csr || !out) return LEO2D_ERR_BAD_ARG;
+  return guard(ctx, [&] {
+    LEO_CUDA(cudaSetDevice(ctx->device));
+    DevBuf<double> d(2 * (size_t)std::max<int64_t>(csr->n, 1));
+    csr_shift_configs(ctx, csr, d.p);
+    d2h(ctx, out, d.p, 2 * (size_t)csr->n);
+    ctx_sync(ctx);
+  });
 }

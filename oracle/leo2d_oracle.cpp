@@ -552,6 +552,71 @@ void oracle_get_pairs(const oracle_h* h, int32_t* intra_pairs, double* intra_t, 
   }
 }
 
+// Hstruct::getShiftConfigs (hstruct.cpp:672-820): for every orbital of a
+// bilayer, the fractional offset of its cell's orbital-0 site from the site
+// of the other sheet found by Hstruct::findNearest, in that sheet's rotated
+// lattice, wrapped to [0,1). Returns 1 unless there are exactly two sheets.
+int oracle_shift_configs(const oracle_h* h, double* out) {
+  const leo2d_geom& g = h->g;
+  if (g.num_sheets != 2) return 1;
+  double inv[2][2][2];
+  for (int s = 0; s < 2; ++s) {
+    const double theta = g.angles[s];
+    const SheetGeo& sh = h->sheets[s];
+    double u[2][2];
+    u[0][0] = std::cos(theta) * sh.a[0][0] - std::sin(theta) * sh.a[0][1];
+    u[0][1] = std::sin(theta) * sh.a[0][0] + std::cos(theta) * sh.a[0][1];
+    u[1][0] = std::cos(theta) * sh.a[1][0] - std::sin(theta) * sh.a[1][1];
+    u[1][1] = std::sin(theta) * sh.a[1][0] + std::cos(theta) * sh.a[1][1];
+    const double det = u[0][0] * u[1][1] - u[0][1] * u[1][0];
+    inv[s][0][0] = u[1][1] / det;
+    inv[s][0][1] = -u[1][0] / det;
+    inv[s][1][0] = -u[0][1] / det;
+    inv[s][1][1] = u[0][0] / det;
+  }
+  // Hstruct::findNearest (hstruct.cpp:224-288), solver_space 0, zero shifts
+  auto hfind = [&](const double p[3], int s, int dim) {
+    const SheetGeo& sh = h->sheets[s];
+    const double theta = -g.angles[s];
+    const double z0 = 0;
+    const double x_new = p[0] * std::cos(theta) - p[1] * std::sin(theta) + z0 * sh.a[0][0] + z0 * sh.a[1][0];
+    const double y_new = p[0] * std::sin(theta) + p[1] * std::cos(theta) + z0 * sh.a[0][1] + z0 * sh.a[1][1];
+    if (dim == 0) {
+      const double i_new = sh.a_inv[0][0] * x_new + sh.a_inv[0][1] * y_new;
+      return std::min(std::max(int(std::floor(i_new)), sh.min0), sh.max0) - sh.min0;
+    }
+    const double j_new = sh.a_inv[1][0] * x_new + sh.a_inv[1][1] * y_new;
+    return std::min(std::max(int(std::floor(j_new)), sh.min1), sh.max1) - sh.min1;
+  };
+  for (int64_t k = 0; k < h->n; ++k) {
+    const int s_here = h->grid4[4 * k + 3];
+    const int s = s_here == 0 ? 1 : 0;
+    double orig[3];
+    h->sheets[s_here].pos_grid(h->grid4[4 * k], h->grid4[4 * k + 1], 0, orig);
+    const double th = g.angles[s_here];
+    double here[3];
+    here[0] = std::cos(th) * orig[0] - std::sin(th) * orig[1];
+    here[1] = std::sin(th) * orig[0] + std::cos(th) * orig[1];
+    here[2] = 0;
+    const int ni = hfind(here, s, 0), nj = hfind(here, s, 1);
+    double sp[3];
+    h->sheets[s].pos_grid(ni, nj, 0, sp);
+    const double ts = g.angles[s];
+    const double np0 = std::cos(ts) * sp[0] - std::sin(ts) * sp[1];
+    const double np1 = std::sin(ts) * sp[0] + std::cos(ts) * sp[1];
+    const double cr0 = here[0] - np0, cr1 = here[1] - np1;
+    double c0 = cr0 * inv[s][0][0] + cr1 * inv[s][0][1];
+    double c1 = cr0 * inv[s][1][0] + cr1 * inv[s][1][1];
+    while (c0 >= 1) c0 += -1;
+    while (c0 < 0) c0 += 1;
+    while (c1 >= 1) c1 += -1;
+    while (c1 < 0) c1 += 1;
+    out[2 * k] = c0;
+    out[2 * k + 1] = c1;
+  }
+  return 0;
+}
+
 int64_t oracle_targets(const oracle_h* h, const int32_t* target_sheets, int32_t num_target_sheets,
                        int64_t* out, int64_t cap) {
   int64_t c = 0;

@@ -40,6 +40,8 @@ void oracle_get(const oracle_h* h, int64_t* rowptr, int32_t* col, double* val, d
 void oracle_get_pairs(const oracle_h* h, int32_t* intra_pairs, double* intra_t, int32_t* intra_sc,
                       int32_t* inter_pairs, int32_t* inter_sc);
 /* Hstruct::getTargetList, solver type 1 (hstruct.cpp:1049-1079): center-cell orbitals. */
+/* Hstruct::getShiftConfigs (hstruct.cpp:672-820): out[n][2]; returns 1 unless 2 sheets. */
+int oracle_shift_configs(const oracle_h* h, double* out);
 int64_t oracle_targets(const oracle_h* h, const int32_t* target_sheets, int32_t num_target_sheets,
                        int64_t* out, int64_t cap);
 

@@ -82,6 +82,13 @@ class Built:
                            _p(self.inter_pairs), _p(self.inter_sc))
         self._h = h
 
+    def shift_configs(self):
+        """Per-orbital disregistry [n][2] (Hstruct::getShiftConfigs); bilayers only."""
+        out = np.zeros(2 * self.n)
+        if lib().oracle_shift_configs(self._h, _p(out)) != 0:
+            raise ValueError("shift configurations need exactly two sheets")
+        return out.reshape(self.n, 2)
+
     def targets(self, target_sheets):
         ts = np.asarray(target_sheets, np.int32)
         out = np.zeros(16 * len(ts), np.int64)

@@ -174,6 +174,18 @@ static int dump_main(int argc, char** argv) {
   for (int k = 0; k < N; ++k)
     for (int d = 0; d < 4; ++d) index_to_grid[4 * (size_t)k + d] = index_vec[k][d];
 
+  // per-orbital local disregistry (Hstruct::getShiftConfigs, hstruct.cpp:672-820; bilayers only)
+  std::vector<double> disregistry;
+  if (loc.sdata.size() == 2) {
+    std::vector<std::vector<double>> cfg_arr;
+    h.getShiftConfigs(cfg_arr, O);
+    disregistry.resize(2 * (size_t)N);
+    for (int k = 0; k < N; ++k) {
+      disregistry[2 * (size_t)k] = cfg_arr[k][0];
+      disregistry[2 * (size_t)k + 1] = cfg_arr[k][1];
+    }
+  }
+
   std::vector<std::vector<int>> inter_vec, inter_sc;
   h.getInterPairs(inter_vec, inter_sc, O);
   std::vector<int> intra_i, intra_j;
@@ -271,6 +283,7 @@ static int dump_main(int argc, char** argv) {
   dump(outdir, "val_dx", dxH.val, (size_t)nnz);
   dump(outdir, "val_dy", dyH.val, (size_t)nnz);
   dump(outdir, "targets", tl.data(), tl.size());
+  if (!disregistry.empty()) dump(outdir, "shift_configs", disregistry.data(), disregistry.size());
 
   const int P = O.getInt("poly_order");
   const int observable = O.getInt("observable_type");

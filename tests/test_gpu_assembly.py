@@ -115,3 +115,27 @@ def test_bad_geometry_is_rejected(ctx):
     g.energy_rescale = 0.0
     with pytest.raises(L.Leo2dError, match="energy_rescale"):
         ctx.build_csr(g)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_golden_shift_configs_bit_exact(ctx, name):
+    """Disregistry (Hstruct::getShiftConfigs) against the reference's own output."""
+    gold = load(name)
+    g, kv = parse_in(name)
+    csr = ctx.build_csr(ctx.prepare(g))
+    if "shift_configs" not in gold:
+        with pytest.raises(L.Leo2dError, match="bilayer"):
+            csr.shift_configs()
+        return
+    np.testing.assert_array_equal(csr.shift_configs().ravel(), gold["shift_configs"])
+
+
+@pytest.mark.parametrize("angle", [0.5, 1.05, 3.0])
+def test_shift_configs_vs_oracle(ctx, angle):
+    g = L.make_geom(model=L.MODEL_SIMPLE, size=40, angles_deg=(0.0, angle), energy_rescale=1.0)
+    gp = ctx.prepare(g)
+    csr = ctx.build_csr(gp)
+    ref = oracle.Built(gp).shift_configs()
+    got = csr.shift_configs()
+    np.testing.assert_array_equal(got, ref)
+    assert got.min() >= 0.0 and got.max() < 1.0

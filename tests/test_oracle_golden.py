@@ -45,6 +45,15 @@ def test_csr_bit_exact(case):
         assert np.array_equal(b.val_dy, gold["val_dy"])
 
 
+def test_shift_configs_bit_exact(case):
+    name, gold, b, kv = case
+    if "shift_configs" not in gold:
+        with pytest.raises(ValueError):
+            b.shift_configs()
+        return
+    np.testing.assert_array_equal(b.shift_configs().ravel(), gold["shift_configs"])
+
+
 def test_targets(case):
     name, gold, b, kv = case
     t = b.targets(kv["target_sheets"])
