@@ -252,6 +252,43 @@ leo2d_status leo2d_batch_destroy(leo2d_batch* b);
 leo2d_status leo2d_tc_gemm(leo2d_ctx* ctx, const uint16_t* a, const uint16_t* b, int64_t M, int64_t N,
                            int64_t K, float* d);
 
+/* ---------------------------------------------------------------- learned control variate */
+
+/* A small MLP on the tensor cores: per-site features (disregistry, twist,
+ * layer, sublattice: 16 columns, FP32) -> 3 x 256 GELU -> the site's first 256
+ * Chebyshev moments. BF16 weights and activations, FP32 accumulation, FP32
+ * master weights with Adam. Trained on site-resolved moments from
+ * leo2d_kpm_ldos and used only as a control variate for the stochastic
+ * trace. No counterpart in the reference. Feature rows passed in are [n][F]
+ * FP32 with F <= 64 (zero padded to 64). */
+typedef struct leo2d_mlp leo2d_mlp;
+int64_t leo2d_mlp_param_count(void);
+/* Parameters are one FP32 vector: W0 [256][64], b0 [256], W1 [256][256], b1,
+ * W2, b2, W3, b3 (W_l row-major [out][in]). Initialised from `seed`. */
+leo2d_status leo2d_mlp_create(leo2d_ctx* ctx, uint64_t seed, leo2d_mlp** out);
+leo2d_status leo2d_mlp_destroy(leo2d_mlp* mlp);
+leo2d_status leo2d_mlp_get_params(leo2d_mlp* mlp, float* out);
+leo2d_status leo2d_mlp_set_params(leo2d_mlp* mlp, const float* in);
+/* Per-moment weights w[256] of the squared-error loss (default 1). */
+leo2d_status leo2d_mlp_set_loss_weights(leo2d_mlp* mlp, const float* w);
+/* Loss (1/n) sum_r sum_j w_j (y_rj - t_rj)^2 and its gradient with respect to
+ * every parameter (layout as the parameter vector) for one batch of n rows,
+ * n a multiple of 64 up to 65536. Does not update the parameters. */
+leo2d_status leo2d_mlp_grad(leo2d_mlp* mlp, const float* x, int32_t F, const float* t, int64_t n,
+                            double* loss, float* grad);
+/* `steps` Adam steps (lr, beta 0.9/0.999) on minibatches of `batch` rows
+ * (multiple of 64) sampled with replacement from the n training rows; one
+ * step is a CUDA graph replay. loss_hist (may be NULL) gets each step's loss. */
+leo2d_status leo2d_mlp_train(leo2d_mlp* mlp, const float* x, int32_t F, const float* t, int64_t n,
+                             int32_t steps, int32_t batch, float lr, uint64_t seed, double* loss_hist);
+/* Predicted moments y[n][256]. */
+leo2d_status leo2d_mlp_predict(leo2d_mlp* mlp, const float* x, int32_t F, int64_t n, float* y);
+/* The 16 feature columns of every orbital of a bilayer matrix: x_out[n][16]. */
+leo2d_status leo2d_mlp_site_features(leo2d_ctx* ctx, const leo2d_csr* csr, double twist_deg, float* x_out);
+/* sum over all orbitals of the predicted moments, FP64 sum_out[256] (features
+ * built on the device; no per-site output). */
+leo2d_status leo2d_mlp_site_sum(leo2d_mlp* mlp, const leo2d_csr* csr, double twist_deg, double* sum_out);
+
 /* ---------------------------------------------------------------- (c) Kubo conductivity */
 
 /* Two-index Chebyshev moments of the current-current correlation.

@@ -138,6 +138,17 @@ def _declare(lib):
     fn("leo2d_batch_info", c_i32, c_void_p, P, P, P, P, P)
     fn("leo2d_batch_destroy", c_i32, c_void_p)
     fn("leo2d_tc_gemm", c_i32, c_void_p, P, P, c_i64, c_i64, c_i64, P)
+    fn("leo2d_mlp_param_count", c_i64)
+    fn("leo2d_mlp_create", c_i32, c_void_p, c_u64, pp)
+    fn("leo2d_mlp_destroy", c_i32, c_void_p)
+    fn("leo2d_mlp_get_params", c_i32, c_void_p, P)
+    fn("leo2d_mlp_set_params", c_i32, c_void_p, P)
+    fn("leo2d_mlp_set_loss_weights", c_i32, c_void_p, P)
+    fn("leo2d_mlp_grad", c_i32, c_void_p, P, c_i32, P, c_i64, P, P)
+    fn("leo2d_mlp_train", c_i32, c_void_p, P, c_i32, P, c_i64, c_i32, c_i32, ctypes.c_float, c_u64, P)
+    fn("leo2d_mlp_predict", c_i32, c_void_p, P, c_i32, c_i64, P)
+    fn("leo2d_mlp_site_features", c_i32, c_void_p, c_void_p, c_dbl, P)
+    fn("leo2d_mlp_site_sum", c_i32, c_void_p, c_void_p, c_dbl, P)
     fn("leo2d_kpm_cond", c_i32, c_void_p, c_void_p, cp, P, c_i64, P)
     fn("leo2d_cond_transform", c_i32, c_void_p, P, c_i32, P)
     fn("leo2d_cond_sigma", c_i32, c_void_p, P, c_i32, P, c_i64, c_dbl, c_dbl, c_dbl, P)

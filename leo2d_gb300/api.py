@@ -207,6 +207,12 @@ class Csr:
         self.ctx.check(self.ctx.lib.leo2d_csr_shift_configs(self.ctx.h, self.h, _p(out)))
         return out
 
+    def site_features(self, twist_deg):
+        """The learned control variate's 16 feature columns of every orbital [n][16]."""
+        x = np.zeros((self.n, 16), np.float32)
+        self.ctx.check(self.ctx.lib.leo2d_mlp_site_features(self.ctx.h, self.h, twist_deg, _p(x)))
+        return x
+
     def bounds(self):
         lo, hi = ctypes.c_double(), ctypes.c_double()
         self.ctx.check(self.ctx.lib.leo2d_csr_bounds(self.ctx.h, self.h, ctypes.byref(lo),
@@ -280,6 +286,75 @@ class Batch:
     def close(self):
         if getattr(self, "h", None):
             self.ctx.lib.leo2d_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Mlp:
+    """The learned control variate's network (leo2d_mlp_*): 16 site features ->
+    3 x 256 GELU -> the first 256 site-resolved Chebyshev moments, on the
+    tensor cores."""
+
+    N_OUT = 256
+
+    def __init__(self, ctx, seed=0):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        ctx.check(ctx.lib.leo2d_mlp_create(ctx.h, seed, ctypes.byref(h)))
+        self.h = h
+        self.n_params = ctx.lib.leo2d_mlp_param_count()
+
+    def params(self):
+        p = np.zeros(self.n_params, np.float32)
+        self.ctx.check(self.ctx.lib.leo2d_mlp_get_params(self.h, _p(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        if p.size != self.n_params:
+            raise ValueError("wrong parameter count")
+        self.ctx.check(self.ctx.lib.leo2d_mlp_set_params(self.h, _p(p)))
+
+    def set_loss_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        self.ctx.check(self.ctx.lib.leo2d_mlp_set_loss_weights(self.h, _p(w)))
+
+    def grad(self, x, t):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        loss = ctypes.c_double()
+        g = np.zeros(self.n_params, np.float32)
+        self.ctx.check(self.ctx.lib.leo2d_mlp_grad(self.h, _p(x), x.shape[1], _p(t), x.shape[0],
+                                                   ctypes.byref(loss), _p(g)))
+        return loss.value, g
+
+    def train(self, x, t, steps, batch=4096, lr=1e-3, seed=0):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        hist = np.zeros(max(steps, 1))
+        self.ctx.check(self.ctx.lib.leo2d_mlp_train(self.h, _p(x), x.shape[1], _p(t), x.shape[0], steps, batch,
+                                                    lr, seed, _p(hist)))
+        return hist[:steps]
+
+    def predict(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.zeros((x.shape[0], self.N_OUT), np.float32)
+        self.ctx.check(self.ctx.lib.leo2d_mlp_predict(self.h, _p(x), x.shape[1], x.shape[0], _p(y)))
+        return y
+
+    def site_sum(self, csr, twist_deg):
+        out = np.zeros(self.N_OUT)
+        self.ctx.check(self.ctx.lib.leo2d_mlp_site_sum(self.h, csr.h, twist_deg, _p(out)))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.leo2d_mlp_destroy(self.h)
             self.h = None
 
     def __del__(self):

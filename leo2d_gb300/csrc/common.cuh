@@ -101,6 +101,7 @@ struct leo2d_ctx {
   int kernel_variant = 0;     // 0 = tiled (bulk copies), 1 = register streaming
   int tile_stages = 2;        // shared-memory stages of the tiled kernel
   int test_unsatisfied_wait = 0;  // test hook: tiled steps first wait on a barrier nobody completes
+  bool tc_gemm_ready = false;     // shared-memory attributes of the tensor-core GEMM set on this device
   int tile_chunk = 4;         // consecutive tiles per block between grid-wide jumps
   int tile_warps = 0;         // warps per block of the tiled kernel (0 = per shape, 8 or 24)
   int reorder = -1;           // locality ordering: -1 auto, 0 off, 1 on

@@ -186,6 +186,16 @@ void make_tmap_bf16_ld(CUtensorMap* map, const void* base, int64_t rows, int64_t
   LEO_REQUIRE(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled rejected the tensor");
 }
 
+void tc_gemm_prepare(leo2d_ctx* ctx) {
+  if (ctx->tc_gemm_ready) return;
+  const int smem = (int)gemm_smem_bytes(BN);
+  LEO_CUDA(cudaFuncSetAttribute(k_tc_gemm<kEpiF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  LEO_CUDA(cudaFuncSetAttribute(k_tc_gemm<kEpiBias>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  LEO_CUDA(cudaFuncSetAttribute(k_tc_gemm<kEpiBiasGelu>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  LEO_CUDA(cudaFuncSetAttribute(k_tc_gemm<kEpiGeluBwd>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  ctx->tc_gemm_ready = true;
+}
+
 void tc_gemm(leo2d_ctx* ctx, GemmEpi epi, const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g,
              int grid_cap) {
   LEO_REQUIRE(g.M > 0 && g.N > 0 && g.K > 0, "empty GEMM");
@@ -193,8 +203,8 @@ void tc_gemm(leo2d_ctx* ctx, GemmEpi epi, const CUtensorMap& ta, const CUtensorM
   const int tiles = ((g.M + BM - 1) / BM) * ((g.N + BN - 1) / BN);
   int grid = std::min(tiles, ctx->sm_count);
   if (grid_cap > 0) grid = std::min(grid, grid_cap);
+  tc_gemm_prepare(ctx);
   auto go = [&](auto kern) {
-    LEO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     launch(ctx, "tc_gemm", [&] { kern<<<grid, 128, smem, ctx->stream>>>(ta, tb, g); });
   };
   switch (epi) {

@@ -58,6 +58,10 @@ void make_tmap_bf16_ld(CUtensorMap* map, const void* base, int64_t rows, int64_t
 // Blocks a GEMM of this output shape launches (one per SM at most).
 int tc_gemm_grid(leo2d_ctx* ctx, int M, int N);
 
+// Sets the kernels' shared-memory attributes on the context's device (once;
+// call before capturing GEMM launches into a graph).
+void tc_gemm_prepare(leo2d_ctx* ctx);
+
 // Launches D = A B^T with the epilogue; A is [M][K] behind ta, B is [N][K] behind tb.
 void tc_gemm(leo2d_ctx* ctx, GemmEpi epi, const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g,
              int grid_cap = 0);

@@ -1,0 +1,41 @@
+"""The MLP oracle's backward pass against central finite differences (float64,
+no BF16 rounding): relative agreement 1e-6 on randomly chosen parameters of
+every layer."""
+import numpy as np
+
+from oracle import mlp_oracle as mo
+
+
+def test_finite_differences():
+    rng = np.random.default_rng(0)
+    n = 32
+    p = rng.normal(0, 0.1, mo.param_count())
+    x = rng.uniform(-1, 1, (n, mo.N_FEAT))
+    t = rng.normal(0, 0.3, (n, mo.OUT))
+    w = rng.uniform(0.5, 2.0, mo.OUT)
+    _, g = mo.loss_and_grad(p, x, t, w, exact=True)
+    offs = np.cumsum([0] + [mo.HID * d + mo.HID for d in mo.IN_DIM])
+    picks = []
+    for l in range(4):
+        wl = mo.HID * mo.IN_DIM[l]
+        cols = rng.integers(0, min(mo.IN_DIM[l], mo.N_FEAT if l == 0 else mo.IN_DIM[l]), 4)
+        rows = rng.integers(0, mo.HID, 4)
+        picks += [offs[l] + r * mo.IN_DIM[l] + c for r, c in zip(rows, cols)]
+        picks += list(offs[l] + wl + rng.integers(0, mo.HID, 2))
+    eps = 1e-6
+    for i in picks:
+        q = p.copy()
+        q[i] += eps
+        lp, _ = mo.loss_and_grad(q, x, t, w, exact=True)
+        q[i] -= 2 * eps
+        lm, _ = mo.loss_and_grad(q, x, t, w, exact=True)
+        fd = (lp - lm) / (2 * eps)
+        assert abs(fd - g[i]) <= 1e-6 * max(1e-3, abs(g[i])) + 1e-9, (i, fd, g[i])
+
+
+def test_bf16_rounding():
+    x = np.array([1.0, 1.00390625, 1.005859375, -2.5e-3, 3.0e38], np.float32)
+    r = mo.bf16(x)
+    # 1 + 2^-8 is a tie between 1 and 1 + 2^-7: ties go to even (1.0)
+    assert r[0] == 1.0 and r[1] == 1.0 and r[2] == 1.0078125
+    assert np.all(np.abs(r[:4] - x[:4]) <= np.abs(x[:4]) * 2.0 ** -8)
