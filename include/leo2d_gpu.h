@@ -289,6 +289,22 @@ leo2d_status leo2d_mlp_site_features(leo2d_ctx* ctx, const leo2d_csr* csr, doubl
  * built on the device; no per-site output). */
 leo2d_status leo2d_mlp_site_sum(leo2d_mlp* mlp, const leo2d_csr* csr, double twist_deg, double* sum_out);
 
+/* Trace moments with the network as a control variate: mu_out[n] estimates
+ * Tr T_n(H~) (the scale of leo2d_kpm_dos's per-vector moments) for n < P.
+ * For n < 256 it is  w_n * CV_n + (1 - w_n) * PH_n  and for n >= 256 PH_n, where
+ *   PH_n = mean over cfg->num_vectors random vectors of <r|T_n|r> (leo2d_kpm_dos;
+ *          0 vectors gives PH = 0),
+ *   CV_n = sum_i f_n(i) over every orbital (network) + N * mean over num_sites
+ *          orbitals s drawn uniformly (splitmix64 stream of site_seed) of
+ *          (<s|T_n|s> - f_n(s)) (exact unit-vector moments, leo2d_kpm_ldos).
+ * Both parts are unbiased, so the combination is for any fixed weights w
+ * (NULL: w = 1). parts_out (optional) = [3][256]: sum_i f, the site
+ * correction, PH. Locality::computeDosTraceKPM (src/locality.cpp:6138-6346)
+ * is the plain estimator this extends; the reference has no control variate. */
+leo2d_status leo2d_kpm_dos_cv(leo2d_ctx* ctx, const leo2d_csr* csr, leo2d_mlp* mlp, const leo2d_kpm_cfg* cfg,
+                              double twist_deg, int64_t num_sites, uint64_t site_seed, const double* weights,
+                              double* mu_out, double* parts_out);
+
 /* ---------------------------------------------------------------- (c) Kubo conductivity */
 
 /* Two-index Chebyshev moments of the current-current correlation.

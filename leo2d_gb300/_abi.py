@@ -149,6 +149,7 @@ def _declare(lib):
     fn("leo2d_mlp_predict", c_i32, c_void_p, P, c_i32, c_i64, P)
     fn("leo2d_mlp_site_features", c_i32, c_void_p, c_void_p, c_dbl, P)
     fn("leo2d_mlp_site_sum", c_i32, c_void_p, c_void_p, c_dbl, P)
+    fn("leo2d_kpm_dos_cv", c_i32, c_void_p, c_void_p, c_void_p, cp, c_dbl, c_i64, c_u64, P, P, P)
     fn("leo2d_kpm_cond", c_i32, c_void_p, c_void_p, cp, P, c_i64, P)
     fn("leo2d_cond_transform", c_i32, c_void_p, P, c_i32, P)
     fn("leo2d_cond_sigma", c_i32, c_void_p, P, c_i32, P, c_i64, c_dbl, c_dbl, c_dbl, P)

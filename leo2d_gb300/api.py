@@ -229,6 +229,16 @@ class Csr:
                                                   _p(mu)))
         return mu
 
+    def kpm_dos_cv(self, mlp, cfg, twist_deg, num_sites, site_seed=0, weights=None, parts=False):
+        """Trace moments [P] with the network as control variate (leo2d_kpm_dos_cv)."""
+        P = cfg.poly_order
+        mu = np.zeros(P)
+        w = None if weights is None else np.ascontiguousarray(weights, np.float64)
+        pt = np.zeros((3, 256)) if parts else None
+        self.ctx.check(self.ctx.lib.leo2d_kpm_dos_cv(self.ctx.h, self.h, mlp.h, ctypes.byref(cfg), twist_deg,
+                                                     num_sites, site_seed, _p(w), _p(mu), _p(pt)))
+        return (mu, pt) if parts else mu
+
     def autotune(self, cfg):
         b, r = ctypes.c_int32(), ctypes.c_int32()
         self.ctx.check(self.ctx.lib.leo2d_kpm_autotune(self.ctx.h, self.h, ctypes.byref(cfg),

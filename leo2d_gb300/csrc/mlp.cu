@@ -80,6 +80,17 @@ __global__ void k_features(int64_t n, int64_t first, const double* __restrict__ 
   }
 }
 
+// Features of selected orbitals rows[r] -> BF16 [n][64].
+__global__ void k_features_at(int64_t n, const int64_t* __restrict__ rows, const double* __restrict__ cfg,
+                              const int32_t* __restrict__ grid4, float twist_deg, __nv_bfloat16* __restrict__ X) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = rows[r];
+    float f[kFeat];
+    site_features(cfg[2 * k], cfg[2 * k + 1], twist_deg, grid4[4 * k + 3], grid4[4 * k + 2], f);
+    for (int c = 0; c < kIn; ++c) X[r * kIn + c] = __float2bfloat16_rn(c < kFeat ? f[c] : 0.0f);
+  }
+}
+
 // Host feature rows [n][F] (F <= 64, FP32) -> BF16 [n][64] and its transpose [64][ldt].
 __global__ void k_pack_x(int64_t n, int F, const float* __restrict__ src, __nv_bfloat16* __restrict__ X,
                          __nv_bfloat16* __restrict__ Xt, int64_t ldt) {
@@ -682,6 +693,84 @@ leo2d_status leo2d_mlp_site_sum(leo2d_mlp* M, const leo2d_csr* csr, double twist
     infer_rows(M, X.p, n, nullptr, sums.p);
     d2h(ctx, sum_out, sums.p, kOut);
     ctx_check_status(ctx, "MLP site sum");
+  });
+}
+
+// Control-variate trace moments (see leo2d_gpu.h).
+leo2d_status leo2d_kpm_dos_cv(leo2d_ctx* ctx, const leo2d_csr* csr, leo2d_mlp* M, const leo2d_kpm_cfg* cfg,
+                              double twist_deg, int64_t num_sites, uint64_t site_seed, const double* weights,
+                              double* mu_out, double* parts_out) {
+  if (!ctx || !csr || !M || !cfg || !mu_out) return LEO2D_ERR_BAD_ARG;
+  return guard(ctx, [&] {
+    const int P = cfg->poly_order;
+    LEO_REQUIRE(P >= 4 && P % 4 == 0, "poly_order must be a positive multiple of 4");
+    LEO_REQUIRE(num_sites >= 0, "num_sites must be >= 0");
+    LEO_REQUIRE(M->ctx == ctx, "the network belongs to another context");
+    auto check = [&](leo2d_status st) {
+      if (st != LEO2D_OK) fail(st, ctx->last_error);
+    };
+    LEO_CUDA(cudaSetDevice(ctx->device));
+    const int64_t n = csr->n;
+    const int Pc = std::min(P, kOut);  // moments covered by the network (even)
+    // (1) random-phase estimate of every moment: mean over the vectors
+    std::vector<double> phase(P, 0.0);
+    const int R = cfg->num_vectors;
+    if (R > 0) {
+      std::vector<double> mu((size_t)R * P);
+      check(leo2d_kpm_dos(ctx, csr, cfg, nullptr, mu.data()));
+      for (int v = 0; v < R; ++v)
+        for (int j = 0; j < P; ++j) phase[j] += mu[(size_t)v * P + j];
+      for (int j = 0; j < P; ++j) phase[j] /= R;
+    }
+    // (2) the network's sum over every orbital
+    std::vector<double> F(kOut, 0.0);
+    check(leo2d_mlp_site_sum(M, csr, twist_deg, F.data()));
+    // (3) exact moments at uniformly drawn orbitals minus the network there
+    std::vector<double> corr(kOut, 0.0);
+    if (num_sites > 0) {
+      std::vector<int64_t> sites((size_t)num_sites);
+      uint64_t st = site_seed;
+      for (auto& x : sites) x = (int64_t)(((unsigned __int128)splitmix(st) * (uint64_t)n) >> 64);
+      leo2d_kpm_cfg lc = *cfg;
+      lc.poly_order = ((Pc + 3) / 4) * 4;
+      lc.num_vectors = 1;
+      std::vector<double> ld((size_t)num_sites * lc.poly_order);
+      check(leo2d_kpm_ldos(ctx, csr, &lc, sites.data(), num_sites, ld.data()));
+      DevBuf<int64_t> drows((size_t)num_sites);
+      h2d(ctx, drows.p, sites.data(), (size_t)num_sites);
+      DevBuf<double> dcfg(2 * (size_t)n);
+      csr_shift_configs(ctx, csr, dcfg.p);
+      DevBuf<__nv_bfloat16> X((size_t)num_sites * kIn);
+      DevBuf<float> Y((size_t)num_sites * kOut);
+      launch(ctx, "mlp_features", [&] {
+        k_features_at<<<grid_for(num_sites, 256, ctx->sm_count * 8), 256, 0, ctx->stream>>>(
+            num_sites, drows.p, dcfg.p, csr->grid4.p, (float)twist_deg, X.p);
+      });
+      infer_rows(M, X.p, num_sites, Y.p, nullptr);
+      std::vector<float> f((size_t)num_sites * kOut);
+      d2h(ctx, f.data(), Y.p, f.size());
+      ctx_check_status(ctx, "control-variate sites");
+      for (int64_t s_ = 0; s_ < num_sites; ++s_)
+        for (int j = 0; j < Pc; ++j)
+          corr[j] += ld[(size_t)s_ * lc.poly_order + j] - (double)f[(size_t)s_ * kOut + j];
+      for (int j = 0; j < Pc; ++j) corr[j] = corr[j] / (double)num_sites * (double)n;
+    }
+    for (int j = 0; j < P; ++j) {
+      if (j < Pc) {
+        const double w = weights ? weights[j] : 1.0;
+        const double cv = F[j] + corr[j];
+        mu_out[j] = w * cv + (1.0 - w) * phase[j];
+      } else {
+        mu_out[j] = phase[j];
+      }
+    }
+    if (parts_out) {
+      for (int j = 0; j < kOut; ++j) {
+        parts_out[j] = F[j];
+        parts_out[kOut + j] = corr[j];
+        parts_out[2 * kOut + j] = j < P ? phase[j] : 0.0;
+      }
+    }
   });
 }
 
