@@ -209,6 +209,137 @@ def kernel_case(args):
                                           "step_gbs": round(gbs, 1)}}))
 
 
+# ---------------------------------------------------------------- learned control variate
+
+CV_EDGE = 40.0      # A: orbitals nearer the edge are not a function of the stacking features
+CV_SITES_PER_FLAKE = 4096
+
+
+def cv_training_set(L, ctx, a, b):
+    """Site-resolved moments (first 256) from the commensurate 1.05 deg supercell
+    (31,32) with periodic boundaries (every orbital), four flakes of the batched
+    family (twist 0.8-3.0 deg) and two flakes at 0.5 and 0.65 deg so that the
+    twist input covers the target's (bulk orbitals, 4096 per flake), at spectral
+    scale (a, b)."""
+    cfg = L.kpm_cfg(256, R=1)
+    xs, ts = [], []
+    g = L.make_geom(model=L.MODEL_SIMPLE, boundary_condition=1, size=70, supercell_mn=(31, 32),
+                    energy_rescale=1.0)
+    gp = ctx.prepare(g)
+    csr = ctx.build_csr(gp)
+    twist = math.degrees(abs(gp.angles[1] - gp.angles[0]))
+    lo, hi = csr.bounds()
+    systems = [(csr, twist, None, max(abs(lo - b), abs(hi - b)))]
+    rng = np.random.default_rng(11)
+    twists, radii = batch_flakes()
+    for th, rad in list(zip(twists, radii))[:4] + [(0.5, 260.0), (0.65, 260.0)]:
+        rad = float(min(max(rad, 150.0), 260.0))
+        c = ctx.build_csr(ctx.prepare(geom(L, radius=rad, twist=float(th))))
+        lo, hi = c.bounds()
+        systems.append((c, float(th), rad, max(abs(lo - b), abs(hi - b))))
+    a_needed = max(x[3] for x in systems)  # Gershgorin bounds the spectrum: a must cover it
+    for c, th, rad, _ in systems:
+        c.rescale(a, -b)
+        if rad is None:
+            sel = np.arange(c.n)
+        else:
+            _, pos = c.geometry()
+            p = pos.reshape(-1, 3)
+            bulk = np.nonzero(np.hypot(p[:, 0], p[:, 1]) < rad - CV_EDGE)[0]
+            sel = np.sort(rng.choice(bulk, size=min(CV_SITES_PER_FLAKE, len(bulk)), replace=False))
+        xs.append(c.site_features(th)[sel])
+        ts.append(c.kpm_ldos(cfg, sel))
+        c.close()
+    return np.concatenate(xs), np.concatenate(ts).astype(np.float32), a_needed
+
+
+def run_cv(L, ctx, csr, a, b, n, dos_of, d_ref, mu_cal, R_plain, t_plain, stream):
+    """Time-to-DOS at the same 1e-3 L1 target with the learned control variate.
+
+    Estimator (leo2d_kpm_dos_cv): moments n < 256 = w_n [sum_i f_n(i) + N mean over
+    S uniform orbitals of (mu_n(s) - f_n(s))] + (1 - w_n) [random-phase mean], the
+    rest from the random-phase vectors; w_n fixed from pilot variances (phase: the
+    spread of the calibration vectors; sites: an independent pilot draw), so the
+    estimate is unbiased. The cheapest (vectors, sites) pair that reaches 1e-3 is
+    found on one realisation, as for the plain count, then timed end to end."""
+    import torch
+    t0 = time.perf_counter()
+    x, t, a_needed = cv_training_set(L, ctx, a, b)
+    if a_needed > a * 1.0000001:
+        return {"skipped": f"training systems need spectral scale {a_needed:.4f} > {a:.4f}"}
+    mlp = L.Mlp(ctx, seed=0)
+    hist = mlp.train(x, t, steps=3000, batch=4096, lr=2e-3, seed=1)
+    t_train = time.perf_counter() - t0
+    twist = TWIST_DEG
+    # pilot: residual variance of the network on the target (independent sites)
+    pilot_sites = 128
+    rng = np.random.default_rng(999)
+    ps = rng.integers(0, n, pilot_sites)
+    mu_p = csr.kpm_ldos(L.kpm_cfg(256, R=1), ps)
+    f_p = mlp.predict(csr.site_features(twist)[ps]).astype(np.float64)
+    var_res = (mu_p - f_p).var(axis=0, ddof=1)
+    var_site = mu_p.var(axis=0, ddof=1)
+    var_phase = mu_cal[:, :256].var(axis=0, ddof=1)  # per vector, trace units
+    # one realisation: per-vector phase moments and the control-variate parts per
+    # site count, combined exactly as leo2d_kpm_dos_cv combines them
+    R_max = 2 * R_plain
+    ph_all = csr.kpm_dos(L.kpm_cfg(P, R=R_max, seed=4242))
+    R_same = None  # plain vector count on this realisation
+    for R in range(1, R_max + 1):
+        if l1(dos_of(ph_all[:R].mean(axis=0)), d_ref) <= TARGET_L1:
+            R_same = R
+            break
+    best = None
+    for S in (64, 128):
+        _, parts = csr.kpm_dos_cv(mlp, L.kpm_cfg(P, R=0), twist, S, site_seed=17 + S, parts=True)
+        cvp = parts[0] + parts[1]
+        v_cv = n * n * var_res / S
+        for R in range(1, R_max + 1):
+            w = (var_phase / R) / (var_phase / R + v_cv)
+            mu = ph_all[:R].mean(axis=0)
+            mu[:256] = w * cvp + (1 - w) * mu[:256]
+            e = l1(dos_of(mu), d_ref)
+            if e <= TARGET_L1:
+                if best is None or R < best[0]:
+                    best = (R, S, e, w)
+                break
+    out = {"train_rows": int(x.shape[0]), "train_steps": 3000, "train_s": round(t_train, 2),
+           "train_loss_first_last": [float(hist[0]), float(hist[-1])],
+           "site_var_over_residual_var": {f"{lo}-{hi}": float(var_site[lo:hi].mean() / var_res[lo:hi].mean())
+                                          for lo, hi in ((1, 16), (16, 128), (128, 256))},
+           "phase_var_over_site_var_per_unit": float(np.mean(var_phase[16:128]) / (n * n * var_site[16:128].mean())),
+           "pilot_sites": pilot_sites, "plain_vectors_same_realisation": R_same}
+    if best is None:
+        out["time_to_dos_s"] = None
+        out["note"] = "no (vectors <= 2 x plain count, sites <= 128) pair reached 1e-3"
+        mlp.close()
+        return out
+    R, S, e, w = best
+    cfg = L.kpm_cfg(P, R=R, seed=4242)
+    csr.kpm_dos_cv(mlp, cfg, twist, S, site_seed=17 + S, weights=w)  # warm
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    mu = csr.kpm_dos_cv(mlp, cfg, twist, S, site_seed=17 + S, weights=w)
+    d = dos_of(mu)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_cv = ev0.elapsed_time(ev1) / 1000.0
+    out.update({"time_to_dos_s": round(t_cv, 6), "vectors": R, "sites": S, "l1": e,
+                "speedup_vs_plain": round(t_plain / t_cv, 4), "plain_vectors": R_plain})
+    if R_same is not None:
+        cfg_p = L.kpm_cfg(P, R=R_same, seed=4242)
+        ev0.record(stream)
+        dos_of(csr.kpm_dos(cfg_p).mean(axis=0))
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        t_same = ev0.elapsed_time(ev1) / 1000.0
+        out.update({"plain_time_same_realisation_s": round(t_same, 6),
+                    "speedup_vs_plain_same_realisation": round(t_same / t_cv, 4)})
+    mlp.close()
+    return out
+
+
 # ---------------------------------------------------------------- batched flakes
 
 BATCH_F, BATCH_P, BATCH_R = 32, 2048, 32
@@ -306,6 +437,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--radius", type=float, default=RADIUS)
     ap.add_argument("--ref-vectors", type=int, default=256)
+    ap.add_argument("--no-cv", action="store_true", help="skip the learned control-variate comparison")
     ap.add_argument("--max-vectors", type=int, default=128)
     ap.add_argument("--workload", default="flake10m", choices=["flake10m", "batch32"],
                     help="flake10m: time-to-DOS on the 10M-orbital flake (the headline); batch32: 32 "
@@ -400,6 +532,11 @@ def main():
     t_dev_max = max_over_ranks(pg, t_dev)
     final_err = l1(d, d_ref)
 
+    # the learned control variate (same target, same reference DOS)
+    cv = None
+    if not args.no_cv and ws == 1:
+        cv = run_cv(L, ctx, csr, a, b, n, dos_of, d_ref, mu_cal, R_needed, t_dev, stream)
+
     # e2e: geometry description on the host -> DOS in host memory, through the C ABI
     def e2e_once():
         c2 = ctx.build_csr(g)
@@ -462,6 +599,7 @@ def main():
         "clocks": clk.summary(),
         "build_s": round(t_build, 3),
         "l1_curve": [round(x, 6) for x in errs[:16]],
+        "cv": cv,
     }
     if rank == 0 and ws == 1:
         sample = cpu_sample(threads)
