@@ -251,6 +251,13 @@ leo2d_status leo2d_batch_destroy(leo2d_batch* b);
  * K must be a multiple of 8. No counterpart in the reference. */
 leo2d_status leo2d_tc_gemm(leo2d_ctx* ctx, const uint16_t* a, const uint16_t* b, int64_t M, int64_t N,
                            int64_t K, float* d);
+/* D[128][N] = A[128][K] * B[N][K]^T in FP32 (host buffers) from three TF32
+ * tensor-core products per K step (hi*hi + hi*lo + lo*hi, about 22 significant
+ * bits), A held in tensor memory and B written into shared memory by the
+ * threads: the arithmetic of the tensor-core Chebyshev step, exposed on its own
+ * so it can be checked. K in {32, 64, 96, 128}, N a multiple of 8 up to 256,
+ * N*K <= 24576. No counterpart in the reference. */
+leo2d_status leo2d_tc_gemm_tf32x3(leo2d_ctx* ctx, const float* a, const float* b, int64_t N, int64_t K, float* d);
 
 /* ---------------------------------------------------------------- learned control variate */
 

@@ -139,6 +139,16 @@ class Context:
         self.check(self.lib.leo2d_tc_gemm(self.h, _p(a), _p(b), M, N, K, _p(d)))
         return d
 
+    def tc_gemm_tf32x3(self, a, b):
+        """D [128][N] = A [128][K] B [N][K]^T from three TF32 tensor-core products per K step."""
+        a = np.ascontiguousarray(a, np.float32)
+        b = np.ascontiguousarray(b, np.float32)
+        if a.shape[0] != 128 or a.shape[1] != b.shape[1]:
+            raise ValueError("a must be [128][K] and b [N][K]")
+        d = np.zeros((128, b.shape[0]), np.float32)
+        self.check(self.lib.leo2d_tc_gemm_tf32x3(self.h, _p(a), _p(b), b.shape[0], b.shape[1], _p(d)))
+        return d
+
     def dos_reconstruct(self, mu, energies, rescale, center, scale=1.0):
         mu = np.ascontiguousarray(mu, np.float64)
         E = np.ascontiguousarray(energies, np.float64)

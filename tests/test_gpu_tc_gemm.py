@@ -53,3 +53,17 @@ def test_tc_gemm_identity_structure(ctx):
 def test_tc_gemm_rejects_bad_k(ctx):
     with pytest.raises(L.Leo2dError, match="multiple of 8"):
         ctx.tc_gemm(np.zeros((4, 6), np.uint16), np.zeros((4, 6), np.uint16))
+
+
+@pytest.mark.parametrize("N,K", [(8, 32), (32, 64), (32, 128), (64, 96), (128, 128), (256, 64)])
+def test_tf32x3_product(ctx, N, K):
+    """Three TF32 products per K step (A in tensor memory, B in swizzled shared
+    memory): error within 2^-19 of sum_k |a||b| per element (three products
+    keep about 22 bits; FP32 accumulation adds K * 2^-24)."""
+    rng = np.random.default_rng(N + 7 * K)
+    a = rng.normal(size=(128, K)).astype(np.float32)
+    b = rng.normal(size=(N, K)).astype(np.float32)
+    d = ctx.tc_gemm_tf32x3(a, b)
+    ref = a.astype(np.float64) @ b.T.astype(np.float64)
+    bound = np.abs(a).astype(np.float64) @ np.abs(b).T.astype(np.float64)
+    assert np.all(np.abs(d - ref) <= 2.0 ** -19 * bound + 1e-30), np.max(np.abs(d - ref) / bound)
