@@ -44,6 +44,19 @@ struct leo2d_csr {
   leo2d::DevBuf<double> pval64;
   int perm_tile_rows = 0;
   int64_t perm_tile_max_nnz = 0;
+  // tensor-core tiles of the locality-ordered copy (tc_spmm.cu): for each tile
+  // of 128 rows the sorted distinct columns (its window, <= 1024), and each
+  // row's entries as (window position, FP32 value) sorted by position
+  bool tc_built = false;
+  double tc_patch = 0.0;
+  int64_t tc_tiles = 0;
+  int tc_max_ent = 0;                 // most entries in one tile
+  int tc_max_win = 0;                 // widest window
+  double tc_mean_win = 0.0;
+  leo2d::DevBuf<int32_t> tc_win;      // [tiles][1024] window rows, padded with the last row
+  leo2d::DevBuf<int32_t> tc_nwin;     // [tiles] window width
+  leo2d::DevBuf<uint2> tc_ent;        // nnz (+pad): (position, value bits), rows as prow
+  leo2d::DevBuf<uint8_t> tc_cstart;   // [n][16] first entry of each 64-position chunk, from the row start
 };
 
 namespace leo2d {
@@ -57,4 +70,9 @@ void csr_build_reordered(leo2d_ctx* ctx, leo2d_csr* csr, double patch, bool with
 // Per-orbital disregistry (Hstruct::getShiftConfigs) into device memory out[n][2]; bilayers.
 void csr_shift_configs(leo2d_ctx* ctx, const leo2d_csr* csr, double* out);
 void csr_drop_reordered(leo2d_csr* csr);
+// Builds the tensor-core tiles of the locality-ordered copy; returns false (and
+// builds nothing) when a tile has more than 1024 distinct columns, 16384
+// entries or a row of more than 255 entries.
+bool csr_build_tc(leo2d_ctx* ctx, leo2d_csr* csr);
+void csr_drop_tc(leo2d_csr* csr);
 }  // namespace leo2d

@@ -206,6 +206,13 @@ void enqueue_steps(Recursion& r) {
     a.partials = r.partials.p + (size_t)(k % 2) * r.grid * 2 * C;
     a.prev_partials = k == 0 ? nullptr : r.partials.p + (size_t)((k + 1) % 2) * r.grid * 2 * C;
     a.prev_dots = k == 0 ? nullptr : r.dots.p + (size_t)(k - 1) * 2 * C;
+    if constexpr (std::is_same<T, float>::value) {
+      if (r.shape.tc) {
+        tc_launch_step(ctx, r.csr, C, r.grid, r.dyn_smem, a.tn, a.tp, nullptr, a.first, 0.0f, a.partials,
+                       a.prev_partials, a.prev_dots);
+        continue;
+      }
+    }
     if (r.shape.tiled) {
       TileArgs<T> ta{};
       ta.s = a;
@@ -252,13 +259,25 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
   LEO_REQUIRE(m->nnz == 0 || (s.fp64 ? m->val64.p != nullptr : m->val32.p != nullptr),
               "matrix has no values");
   leo2d_csr* mm = const_cast<leo2d_csr*>(m);
+  if (shape.tc && !(allow_perm && m->pos.p != nullptr && m->nnz > 0)) shape.tc = false;
   const bool want_perm = allow_perm && m->pos.p != nullptr && m->nnz > 0 &&
-                         (ctx->reorder == 1 || (ctx->reorder == -1 && n >= 100000));
+                         (shape.tc || ctx->reorder == 1 || (ctx->reorder == -1 && n >= 100000));
   if (want_perm && (!m->reordered || (s.fp64 && !m->reorder_fp64) ||
                     m->reorder_patch != ctx->reorder_patch))
     csr_build_reordered(ctx, mm, ctx->reorder_patch, s.fp64 || m->reorder_fp64);
   use_perm = want_perm;
-  if (shape.tiled) {
+  if (shape.tc) {
+    // tensor-core tiles of the locality-ordered copy (built once per matrix)
+    if (!m->tc_built || m->tc_patch != m->reorder_patch) csr_build_tc(ctx, mm);
+    if (m->tc_built && tc_smem_bytes(m, s.cols) <= ctx->smem_optin) {
+      dyn_smem = tc_smem_bytes(m, s.cols);
+      grid = (unsigned)std::min<int64_t>((int64_t)ctx->sm_count, m->tc_tiles);
+      shape.tiled = false;
+    } else {
+      shape.tc = false;  // a tile too wide for the tensor-core step: the gather kernels run
+    }
+  }
+  if (shape.tiled && !shape.tc) {
     const int ns = tile_slots(s.cols, s.fp64, s.warps);
     const int ri = s.rows_per_item > 0 ? s.rows_per_item : std::max(1, 32 / ns);
     tile_rows = ns * ri;
@@ -306,7 +325,7 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
       grid = (unsigned)g;
     }
   }
-  if (!shape.tiled) {
+  if (!shape.tiled && !shape.tc) {
     if (shape.rows_per_item <= 0) shape.rows_per_item = 4;
     const int occ = std::max(1, occupancy(s.cols, s.fp64));
     const int lpr = s.cols <= 32 ? s.cols : 32;  // lanes per row slot
@@ -328,7 +347,7 @@ template <typename T>
 void one_step(Recursion& r, const void* in, void* out, const void* prev, bool first, double alpha, int matrix) {
   leo2d_ctx* ctx = r.ctx;
   const int C = r.shape.cols;
-  LEO_REQUIRE(!r.use_perm, "a recursion over dxH needs the unpermuted matrix");
+  LEO_REQUIRE(!r.use_perm && !r.shape.tc, "a recursion over dxH needs the unpermuted matrix");
   StepArgs<T> a;
   a.n = r.n;
   a.rowptr = r.csr->rowptr.p;
@@ -372,7 +391,7 @@ void Recursion::step(const void* in, void* out, const void* prev, bool first, do
 void Recursion::run() {
   if (shape.fp64) enqueue_steps<double>(*this);
   else enqueue_steps<float>(*this);
-  if (shape.tiled) ctx_check_status(ctx, "Chebyshev recursion");
+  if (shape.tiled || shape.tc) ctx_check_status(ctx, "Chebyshev recursion");
 }
 
 Recursion::~Recursion() {
@@ -403,6 +422,7 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
   else if (it != g_shape_cache.end() && it->second.warps > 0) s.warps = it->second.warps;
   else s.warps = (!fp64 && (s.cols == 32 || s.cols == 64)) ? 24 : 8;
   s.tiled = ctx->kernel_variant != 1;
+  s.tc = ctx->kernel_variant == 2 && !fp64 && (s.cols == 32 || s.cols == 64);
   LEO_REQUIRE(s.rows_per_item >= 0 && s.rows_per_item <= 64, "rows_per_warp must be 0..64");
   return s;
 }

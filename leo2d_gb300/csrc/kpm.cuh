@@ -13,6 +13,7 @@ struct StepShape {
   bool fp64 = false;
   bool tiled = true;       // bulk-copy tiled kernel (else the register-streaming kernel)
   int warps = 8;           // warps per block of the tiled kernel (8 or 24)
+  bool tc = false;         // tensor-core step (tc_spmm.cu) over the locality-ordered tiles
 };
 
 // Vector block resident on the device: two buffers of n x cols (T_k, T_{k-1}).
@@ -44,6 +45,13 @@ struct Recursion {
   void step(const void* in, void* out, const void* prev, bool first, double alpha, int matrix);
   ~Recursion();
 };
+
+// The tensor-core step (tc_spmm.cu): dynamic shared memory for a block width,
+// and one launch (partials / prev_* as in the gather kernels).
+size_t tc_smem_bytes(const leo2d_csr* csr, int cols);
+void tc_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, int cols, unsigned grid, size_t smem, const float* tn,
+                    float* tp, const float* tprev, int first, float alpha, double* partials,
+                    const double* prev_partials, double* prev_dots);
 
 // Chooses the shape for a matrix; cached per context and matrix.
 StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols_needed,

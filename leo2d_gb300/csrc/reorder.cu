@@ -158,6 +158,7 @@ __global__ void k_perm_fill(const int64_t* __restrict__ rp, const int32_t* __res
 namespace leo2d {
 
 void csr_build_reordered(leo2d_ctx* ctx, leo2d_csr* csr, double patch, bool with_fp64) {
+  csr_drop_tc(csr);
   const int64_t n = csr->n;
   LEO_REQUIRE(csr->pos.p, "locality ordering needs orbital positions");
   LEO_REQUIRE(patch > 0.5, "patch size must exceed 0.5 A");
@@ -238,6 +239,7 @@ void csr_build_reordered(leo2d_ctx* ctx, leo2d_csr* csr, double patch, bool with
 }
 
 void csr_drop_reordered(leo2d_csr* csr) {
+  csr_drop_tc(csr);
   csr->reordered = false;
   csr->reorder_fp64 = false;
   csr->new2old.release();
