@@ -191,6 +191,8 @@ def kernel_case(args):
     import leo2d_gb300 as L
     radius = args.radius if args.radius != RADIUS else 1000.0
     with L.Context(0) as ctx:
+        if args.step_kernel >= 0:
+            ctx.set_option("step_kernel", args.step_kernel)
         csr = ctx.build_csr(ctx.prepare(geom(L, radius=radius)))
         lo, hi = csr.bounds()
         csr.rescale(1.01 * (hi - lo) / 2, -(hi + lo) / 2)
@@ -205,8 +207,8 @@ def kernel_case(args):
         nnz_true = csr.nnz
         gbs = step_bytes(csr.n, nnz_true, args.kernel_case) / (ms / k * 1e-3) / 1e9
         print(json.dumps({"kernel_case": {"n": csr.n, "nnz": csr.nnz, "cols": args.kernel_case,
-                                          "radius_A": radius, "step_ms": round(ms / k, 4),
-                                          "step_gbs": round(gbs, 1)}}))
+                                          "step_kernel": args.step_kernel, "radius_A": radius,
+                                          "step_ms": round(ms / k, 4), "step_gbs": round(gbs, 1)}}))
 
 
 # ---------------------------------------------------------------- learned control variate
@@ -442,6 +444,9 @@ def main():
     ap.add_argument("--workload", default="flake10m", choices=["flake10m", "batch32"],
                     help="flake10m: time-to-DOS on the 10M-orbital flake (the headline); batch32: 32 "
                          "flakes of 20k-500k orbitals in one batched, graph-replayed run")
+    ap.add_argument("--step-kernel", type=int, default=-1, choices=[-1, 0, 1, 2],
+                    help="force the Chebyshev step kernel: 0 tiled gathers, 1 register gathers, 2 tensor cores "
+                         "(default: the autotuner's choice)")
     ap.add_argument("--kernel-case", type=int, default=0, metavar="COLS",
                     help="profiling case: two short DOS runs (P=16) of COLS-wide vector blocks on the flake "
                          "of --radius (1000 A: 2.4M orbitals), then exit; prints no bench line")

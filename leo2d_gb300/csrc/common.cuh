@@ -98,7 +98,7 @@ struct leo2d_ctx {
   std::vector<leo2d::PendingTimer> pending;
   std::vector<cudaEvent_t> free_events;
   int64_t launches = 0;
-  int kernel_variant = 0;     // 0 = tiled (bulk copies), 1 = register streaming, 2 = tensor cores
+  int kernel_variant = -1;    // -1 autotuned, 0 tiled gathers, 1 register gathers, 2 tensor cores
   int tile_stages = 2;        // shared-memory stages of the tiled kernel
   int test_unsatisfied_wait = 0;  // test hook: tiled steps first wait on a barrier nobody completes
   bool tc_gemm_ready = false;     // shared-memory attributes of the tensor-core GEMM set on this device

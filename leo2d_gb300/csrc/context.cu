@@ -283,7 +283,8 @@ leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value
   return guard(ctx, [&] {
     const std::string k(key);
     if (k == "step_kernel") {
-      LEO_REQUIRE(value >= 0 && value <= 2, "step_kernel must be 0 (tiled), 1 (register) or 2 (tensor cores)");
+      LEO_REQUIRE(value >= -1 && value <= 2,
+                  "step_kernel must be -1 (autotuned), 0 (tiled), 1 (register) or 2 (tensor cores)");
       ctx->kernel_variant = (int)value;
     } else if (k == "test_unsatisfied_wait") {
       // every tiled step waits on an mbarrier that never completes, gives up

@@ -241,6 +241,7 @@ struct ShapeKey {
 };
 struct Tuned {
   int rows = 0, warps = 0;
+  bool tc = false;  // the tensor-core step won for this block width
 };
 std::map<std::pair<leo2d_ctx*, ShapeKey>, Tuned> g_shape_cache;
 // best block width per (context, matrix, precision, columns requested)
@@ -422,7 +423,9 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
   else if (it != g_shape_cache.end() && it->second.warps > 0) s.warps = it->second.warps;
   else s.warps = (!fp64 && (s.cols == 32 || s.cols == 64)) ? 24 : 8;
   s.tiled = ctx->kernel_variant != 1;
-  s.tc = ctx->kernel_variant == 2 && !fp64 && (s.cols == 32 || s.cols == 64);
+  const bool tc_ok = !fp64 && (s.cols == 32 || s.cols == 64);
+  s.tc = tc_ok && (ctx->kernel_variant == 2 ||
+                   (ctx->kernel_variant == -1 && it != g_shape_cache.end() && it->second.tc));
   LEO_REQUIRE(s.rows_per_item >= 0 && s.rows_per_item <= 64, "rows_per_warp must be 0..64");
   return s;
 }
@@ -626,6 +629,7 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
           StepShape sh = choose_shape(ctx, csr, fp64, cols, cols, rows > 0 ? rows : 0);
           sh.rows_per_item = rows;
           sh.warps = warps;
+          sh.tc = false;
           Recursion r;
           r.setup(ctx, csr, sh, steps);
           fill_phase(ctx, r, 1, 0, cols / 2);
@@ -640,6 +644,27 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
             best_c = per;
             best_t.rows = rows;
             best_t.warps = warps;
+          }
+        }
+      }
+      // the tensor-core step (one shape) where it applies
+      if (!fp64 && (cols == 32 || cols == 64) && ctx->kernel_variant != 0 && ctx->kernel_variant != 1) {
+        StepShape sh = choose_shape(ctx, csr, fp64, cols, cols, 0);
+        sh.tc = true;
+        Recursion r;
+        r.setup(ctx, csr, sh, steps);
+        if (r.shape.tc) {
+          fill_phase(ctx, r, 1, 0, cols / 2);
+          r.run();  // warm
+          ctx_sync(ctx);
+          const auto before = ctx->stats["cheb_step"];
+          r.run();
+          ctx_sync(ctx);
+          const auto after = ctx->stats["cheb_step"];
+          const double per = (after.ms - before.ms) / std::max<int64_t>(1, after.launches - before.launches);
+          if (per < best_c) {
+            best_c = per;
+            best_t.tc = true;
           }
         }
       }

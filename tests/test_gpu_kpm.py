@@ -74,7 +74,7 @@ def _with_options(ctx, opts, fn):
     try:
         return fn()
     finally:
-        for k, v in {"step_kernel": 0, "reorder": -1, "tile_warps": 0, "tile_chunk": 4,
+        for k, v in {"step_kernel": -1, "reorder": -1, "tile_warps": 0, "tile_chunk": 4,
                      "tile_stages": 2}.items():
             ctx.set_option(k, v)
 

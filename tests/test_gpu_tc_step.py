@@ -37,7 +37,7 @@ def _run(ctx, variant, fn):
     try:
         return fn()
     finally:
-        ctx.set_option("step_kernel", 0)
+        ctx.set_option("step_kernel", -1)
 
 
 @pytest.mark.parametrize("block", [32, 64])
