@@ -208,6 +208,7 @@ def kernel_case(args):
         gbs = step_bytes(csr.n, nnz_true, args.kernel_case) / (ms / k * 1e-3) / 1e9
         print(json.dumps({"kernel_case": {"n": csr.n, "nnz": csr.nnz, "cols": args.kernel_case,
                                           "step_kernel": args.step_kernel, "radius_A": radius,
+                                          "tc_tiles": list(csr.tc_info()),
                                           "step_ms": round(ms / k, 4), "step_gbs": round(gbs, 1)}}))
 
 

@@ -257,6 +257,11 @@ leo2d_status leo2d_tc_gemm(leo2d_ctx* ctx, const uint16_t* a, const uint16_t* b,
  * threads: the arithmetic of the tensor-core Chebyshev step, exposed on its own
  * so it can be checked. K in {32, 64, 96, 128}, N a multiple of 8 up to 256,
  * N*K <= 24576. No counterpart in the reference. */
+/* Tensor-core tiles of a matrix (built on first use of the tensor-core step):
+ * tile count (0 if not built), mean and largest window (distinct columns of a
+ * 128-row tile) and most entries in one tile. */
+leo2d_status leo2d_csr_tc_info(const leo2d_csr* csr, int64_t* tiles, double* mean_window, int32_t* max_window,
+                               int32_t* max_tile_entries);
 leo2d_status leo2d_tc_gemm_tf32x3(leo2d_ctx* ctx, const float* a, const float* b, int64_t N, int64_t K, float* d);
 
 /* ---------------------------------------------------------------- learned control variate */

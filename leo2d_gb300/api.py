@@ -223,6 +223,13 @@ class Csr:
         self.ctx.check(self.ctx.lib.leo2d_mlp_site_features(self.ctx.h, self.h, twist_deg, _p(x)))
         return x
 
+    def tc_info(self):
+        """Tensor-core tiles: (tiles, mean window, largest window, most entries per tile)."""
+        t, w, mw, me = ctypes.c_int64(), ctypes.c_double(), ctypes.c_int32(), ctypes.c_int32()
+        self.ctx.check(self.ctx.lib.leo2d_csr_tc_info(self.h, ctypes.byref(t), ctypes.byref(w), ctypes.byref(mw),
+                                                      ctypes.byref(me)))
+        return t.value, w.value, mw.value, me.value
+
     def bounds(self):
         lo, hi = ctypes.c_double(), ctypes.c_double()
         self.ctx.check(self.ctx.lib.leo2d_csr_bounds(self.ctx.h, self.h, ctypes.byref(lo),

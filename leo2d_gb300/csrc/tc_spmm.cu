@@ -332,19 +332,21 @@ template <int C>
 __global__ void __launch_bounds__(kTcThreads, 1) k_cheb_tc(const TcArgs a) {
   static_assert(C == 32 || C == 64, "the tensor-core step takes 32 or 64 columns");
   using S = TcSmem<C>;
+  constexpr int BV = kTcChunk * C / kTcThreads;  // window-row values per thread per chunk
+  constexpr int CH = C / 2;                      // columns per thread in the epilogue
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  unsigned char* bbase = smem;                                       // [stage][hi, lo][kB]
+  unsigned char* bbase = smem;  // [stage][hi, lo][kB]
   float* arows = reinterpret_cast<float*>(smem + S::kBAll);
   uint8_t* cst = smem + S::kBAll + S::kArows;
   int32_t* winl = reinterpret_cast<int32_t*>(smem + S::kBAll + S::kArows + S::kCst);
   int64_t* rp = reinterpret_cast<int64_t*>(smem + S::kBAll + S::kArows + S::kCst + S::kWin);
   uint2* ents = reinterpret_cast<uint2*>(smem + S::kFixed);
-  __shared__ __align__(8) uint64_t load_bar, mma_bar[2], tile_bar;
+  __shared__ __align__(8) uint64_t load_bar, mma_bar[2], tile_bar, drain_bar;
   __shared__ uint32_t tmem_base;
   __shared__ int s_nwin;
-  __shared__ double red[2][4][2 * (C / 2)];
+  __shared__ double red[2][4][2 * CH];
 
   if (a.prev_partials) reduce_prev<C, kTcThreads>(a.prev_partials, a.prev_dots, gridDim.x, blockIdx.x, gridDim.x);
 
@@ -355,6 +357,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cheb_tc(const TcArgs a) {
     umma::bar_init(&mma_bar[0], 1);
     umma::bar_init(&mma_bar[1], 1);
     umma::bar_init(&tile_bar, 1);
+    umma::bar_init(&drain_bar, 1);
     umma::bar_fence_init();
   }
   if (warp == 0) umma::tmem_alloc(&tmem_base, 512);
@@ -366,39 +369,55 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cheb_tc(const TcArgs a) {
   const float alpha = a.alpha != 0.0f ? a.alpha : (a.first ? 1.0f : 2.0f);
   const float* tprev = a.tprev ? a.tprev : a.tp;
   const int64_t tiles = (a.n + kTcRows - 1) / kTcRows;
-  constexpr int CH = C / 2;  // columns per thread in the epilogue
   double d0[CH], d1[CH];
 #pragma unroll
   for (int j = 0; j < CH; ++j) d0[j] = d1[j] = 0.0;
   uint32_t chunk_ctr = 0;  // chunks issued by this block (stage = ctr & 1)
-  int local = 0;
+  uint32_t loads = 0;      // tile stagings issued (load_bar phases)
+  int local = 0;           // tiles finished (tile_bar phases)
   bool failed = false;
+  float xb[BV];            // the next chunk's window-row values (prefetched)
 
-  for (int64_t t = blockIdx.x; t < tiles && !failed; t += gridDim.x, ++local) {
+  // tile staging (one lane): row pointers, entries, chunk starts, window
+  auto stage_tile = [&](int64_t t) {
     const int64_t r0 = t * kTcRows;
     const int rows = (int)min((int64_t)kTcRows, a.n - r0);
-    // ---- stage the tile: row pointers, entries, chunk starts, window
-    if (tid == 0) {
-      const int W = a.nwin[t];
-      s_nwin = W;
-      const int Wp = (W + kTcChunk - 1) / kTcChunk * kTcChunk;
-      const int64_t ra = r0 & ~1ll;
-      const int64_t rcount = ((r0 + rows + 1 - ra) + 1) & ~1ll;
-      const int64_t q0 = a.rowptr[r0], q1 = a.rowptr[r0 + rows];
-      const int64_t qa = q0 & ~1ll;
-      const int64_t qcount = ((q1 - qa) + 1) & ~1ll;
-      const uint32_t total = (uint32_t)(rcount * 8 + qcount * 8 + (uint32_t)((rows * kTcChunks + 15) & ~15) + Wp * 4);
-      umma::bar_expect_tx(&load_bar, total);
-      bulk_g2s(rp, a.rowptr + ra, (uint32_t)(rcount * 8), &load_bar);
-      bulk_g2s(ents, a.ent + qa, (uint32_t)(qcount * 8), &load_bar);
-      bulk_g2s(cst, a.cstart + r0 * kTcChunks, (uint32_t)((rows * kTcChunks + 15) & ~15), &load_bar);
-      bulk_g2s(winl, a.win + t * kTcMaxWin, (uint32_t)(Wp * 4), &load_bar);
+    const int W = a.nwin[t];
+    s_nwin = W;
+    const int Wp = (W + kTcChunk - 1) / kTcChunk * kTcChunk;
+    const int64_t ra = r0 & ~1ll;
+    const int64_t rcount = ((r0 + rows + 1 - ra) + 1) & ~1ll;
+    const int64_t q0 = a.rowptr[r0], q1 = a.rowptr[r0 + rows];
+    const int64_t qa = q0 & ~1ll;
+    const int64_t qcount = ((q1 - qa) + 1) & ~1ll;
+    const uint32_t cbytes = (uint32_t)((rows * kTcChunks + 15) & ~15);
+    umma::bar_expect_tx(&load_bar, (uint32_t)(rcount * 8 + qcount * 8 + cbytes + Wp * 4));
+    bulk_g2s(rp, a.rowptr + ra, (uint32_t)(rcount * 8), &load_bar);
+    bulk_g2s(ents, a.ent + qa, (uint32_t)(qcount * 8), &load_bar);
+    bulk_g2s(cst, a.cstart + r0 * kTcChunks, cbytes, &load_bar);
+    bulk_g2s(winl, a.win + t * kTcMaxWin, (uint32_t)(Wp * 4), &load_bar);
+  };
+  // window rows of chunk k of the staged tile into registers
+  auto load_b = [&](int k) {
+#pragma unroll
+    for (int j = 0; j < BV; ++j) {
+      const int idx = tid + j * kTcThreads;
+      const int w = idx / C, c = idx % C;
+      xb[j] = __ldg(a.tn + (int64_t)winl[k * kTcChunk + w] * C + c);
     }
-    const int late_load = umma::bar_wait(&load_bar, (uint32_t)local & 1u) ? 0 : 1;
-    if (__syncthreads_or(late_load)) {
-      failed = true;
-      break;
-    }
+  };
+
+  int64_t t = blockIdx.x;
+  if (t < tiles) {
+    if (tid == 0) stage_tile(t);
+    ++loads;
+    const int late = umma::bar_wait(&load_bar, 0u) ? 0 : 1;
+    if (__syncthreads_or(late)) failed = true;
+    else load_b(0);
+  }
+  for (; t < tiles && !failed; t += gridDim.x, ++local) {
+    const int64_t r0 = t * kTcRows;
+    const int rows = (int)min((int64_t)kTcRows, a.n - r0);
     const int W = s_nwin;
     const int nch = (W + kTcChunk - 1) / kTcChunk;
     const int64_t ra = r0 & ~1ll;
@@ -420,14 +439,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cheb_tc(const TcArgs a) {
       }
       unsigned char* bhi = bbase + (size_t)s * 2 * S::kB;
       unsigned char* blo = bhi + S::kB;
-      // B: window rows of T_n (hi, lo), K-major swizzled, N = C columns
-      for (int idx = tid; idx < kTcChunk * C; idx += kTcThreads) {
-        const int w = idx / C, c = idx % C;
-        const float x = a.tn[(int64_t)winl[k * kTcChunk + w] * C + c];
-        const uint32_t off = umma::k128_offset_b32(c, w, C);
-        *reinterpret_cast<uint32_t*>(bhi + off) = tf32_hi(x);
-        *reinterpret_cast<uint32_t*>(blo + off) = tf32_lo(x);
+      // B: this chunk's window rows (prefetched) as hi / lo parts
+#pragma unroll
+      for (int j = 0; j < BV; ++j) {
+        const int idx = tid + j * kTcThreads;
+        const uint32_t off = umma::k128_offset_b32(idx % C, idx / C, C);
+        *reinterpret_cast<uint32_t*>(bhi + off) = tf32_hi(xb[j]);
+        *reinterpret_cast<uint32_t*>(blo + off) = tf32_lo(xb[j]);
       }
+      if (k + 1 < nch) load_b(k + 1);  // in flight while this chunk is built
       // A: this thread's half (32 positions) of its row's chunk
       float* arow = arows + m * S::kArowStride + half * 32;
 #pragma unroll
@@ -471,48 +491,66 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cheb_tc(const TcArgs a) {
           umma::mma_tf32_ta(tmem + kTcColD, a_lo + 8 * ks, umma::desc_k128(b0 + boff), idesc, 1u);
         }
         umma::mma_commit(&mma_bar[s]);
+        if (k + 1 == nch) umma::mma_commit(&tile_bar);  // the tile's accumulator
       }
     }
     if (failed) break;
-    // ---- the accumulator of the tile
-    if (tid == 0) umma::mma_commit(&tile_bar);
+    // the staging areas are free: stage the next tile while this one finishes
+    const int64_t tn_next = t + gridDim.x;
+    const bool has_next = tn_next < tiles;
+    if (has_next && tid == 0) {
+      umma::fence_proxy_async();  // the threads' reads of the staging areas precede the copies
+      stage_tile(tn_next);
+    }
+    // epilogue operands of this tile's rows, loaded while the MMAs drain
+    const int64_t off = (r0 + m) * C + half * CH;
+    float4 xn[CH / 4], xp[CH / 4];
+    if (row_ok) {
+#pragma unroll
+      for (int c0 = 0; c0 < CH; c0 += 4) {
+        xn[c0 / 4] = __ldg(reinterpret_cast<const float4*>(a.tn + off + c0));
+        xp[c0 / 4] = a.first ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4*>(tprev + off + c0);
+      }
+    }
     __syncwarp();
     const int late_t = umma::bar_wait(&tile_bar, (uint32_t)local & 1u) ? 0 : 1;
-    if (__syncthreads_or(late_t)) {
+    int late_l = 0;
+    if (has_next) late_l = umma::bar_wait(&load_bar, loads & 1u) ? 0 : 1;
+    if (__syncthreads_or(late_t | late_l)) {
       failed = true;
       break;
+    }
+    if (has_next) {
+      ++loads;
+      load_b(0);  // the next tile's first window rows, in flight during this epilogue
     }
     umma::fence_after_sync();
     float v[CH];
 #pragma unroll
     for (int c0 = 0; c0 < CH; c0 += 16) umma::tmem_ld16(tmem + lane_base + kTcColD + half * CH + c0, v + c0);
     if (row_ok) {
-      const int64_t off = (r0 + m) * C + half * CH;
 #pragma unroll
       for (int c0 = 0; c0 < CH; c0 += 4) {
-        const float4 xn = *reinterpret_cast<const float4*>(a.tn + off + c0);
-        float4 y;
-        if (a.first) {
-          y = make_float4(alpha * v[c0], alpha * v[c0 + 1], alpha * v[c0 + 2], alpha * v[c0 + 3]);
-        } else {
-          const float4 xp = *reinterpret_cast<const float4*>(tprev + off + c0);
-          y = make_float4(alpha * v[c0] - xp.x, alpha * v[c0 + 1] - xp.y, alpha * v[c0 + 2] - xp.z,
-                          alpha * v[c0 + 3] - xp.w);
-        }
+        const float4 x = xn[c0 / 4], p = xp[c0 / 4];
+        const float4 y = make_float4(alpha * v[c0] - p.x, alpha * v[c0 + 1] - p.y, alpha * v[c0 + 2] - p.z,
+                                     alpha * v[c0 + 3] - p.w);
         *reinterpret_cast<float4*>(a.tp + off + c0) = y;
-        d0[c0] += (double)(xn.x * xn.x); d1[c0] += (double)(y.x * xn.x);
-        d0[c0 + 1] += (double)(xn.y * xn.y); d1[c0 + 1] += (double)(y.y * xn.y);
-        d0[c0 + 2] += (double)(xn.z * xn.z); d1[c0 + 2] += (double)(y.z * xn.z);
-        d0[c0 + 3] += (double)(xn.w * xn.w); d1[c0 + 3] += (double)(y.w * xn.w);
+        d0[c0] += (double)(x.x * x.x); d1[c0] += (double)(y.x * x.x);
+        d0[c0 + 1] += (double)(x.y * x.y); d1[c0 + 1] += (double)(y.y * x.y);
+        d0[c0 + 2] += (double)(x.z * x.z); d1[c0 + 2] += (double)(y.z * x.z);
+        d0[c0 + 3] += (double)(x.w * x.w); d1[c0 + 3] += (double)(y.w * x.w);
       }
     }
     umma::fence_before_sync();
     __syncthreads();
   }
-  // drain: every MMA this block issued must finish before tensor memory is freed
-  if (tid == 0 && chunk_ctr > 0) {
-    umma::mma_commit(&tile_bar);
-    umma::bar_wait(&tile_bar, (uint32_t)local & 1u);
+  // drain: every MMA and copy this block issued must finish before it exits
+  if (tid == 0) {
+    if (chunk_ctr > 0) {
+      umma::mma_commit(&drain_bar);  // arrives once every earlier MMA of this thread is done
+      umma::bar_wait(&drain_bar, 0u);
+    }
+    if (failed && loads > 0) umma::bar_wait(&load_bar, (loads - 1) & 1u);
   }
   if (tid == 0 && failed) atomicExch(a.status, kStatusTimeout);
   // block partials: rows (lanes) of each warp by shuffles, then the 4 warps of
@@ -632,3 +670,13 @@ void tc_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, int cols, unsigned gri
 }
 
 }  // namespace leo2d
+
+extern "C" leo2d_status leo2d_csr_tc_info(const leo2d_csr* csr, int64_t* tiles, double* mean_window,
+                                          int32_t* max_window, int32_t* max_tile_entries) {
+  if (!csr) return LEO2D_ERR_BAD_ARG;
+  if (tiles) *tiles = csr->tc_built ? csr->tc_tiles : 0;
+  if (mean_window) *mean_window = csr->tc_built ? csr->tc_mean_win : 0.0;
+  if (max_window) *max_window = csr->tc_built ? csr->tc_max_win : 0;
+  if (max_tile_entries) *max_tile_entries = csr->tc_built ? csr->tc_max_ent : 0;
+  return LEO2D_OK;
+}
