@@ -226,7 +226,7 @@ def cv_training_set(L, ctx, a, b):
     scale (a, b)."""
     cfg = L.kpm_cfg(256, R=1)
     xs, ts = [], []
-    g = L.make_geom(model=L.MODEL_SIMPLE, boundary_condition=1, size=70, supercell_mn=(31, 32),
+    g = L.make_geom(model=L.MODEL_SIMPLE, boundary_condition=1, size=100, supercell_mn=(31, 32),
                     energy_rescale=1.0)
     gp = ctx.prepare(g)
     csr = ctx.build_csr(gp)
@@ -343,6 +343,121 @@ def run_cv(L, ctx, csr, a, b, n, dos_of, d_ref, mu_cal, R_plain, t_plain, stream
     return out
 
 
+# ---------------------------------------------------------------- periodic supercell and Kubo
+
+def _timed(stream, fn, steps, warmup):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        out = fn()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / 1000.0 / steps, out
+
+
+def run_periodic(args):
+    """Commensurate TBLG (31,32), 1.05 deg, periodic: 11,908 orbitals, P = 4096, one block
+    of 64 random-phase vectors, FP32 recursion; per-energy error against the FP64
+    recursion on the same vectors (itself checked against the CPU oracle on one vector)."""
+    import torch
+    import leo2d_gb300 as L
+    from oracle import oracle
+    ctx = L.Context(0)
+    g = L.make_geom(model=L.MODEL_SIMPLE, boundary_condition=1, size=100, supercell_mn=(31, 32),
+                    energy_rescale=1.0)
+    gp = ctx.prepare(g)
+    csr = ctx.build_csr(gp)
+    lo, hi = csr.bounds()
+    a, b = 1.01 * (hi - lo) / 2, (hi + lo) / 2
+    csr.rescale(a, -b)
+    Pp, R = 4096, 64
+    cfg32 = L.kpm_cfg(Pp, R=R, seed=3)
+    cfg64 = L.kpm_cfg(Pp, R=R, seed=3, precision=L.FP64)
+    cols, rows = csr.autotune(cfg32)  # untimed
+    stream = torch.cuda.ExternalStream(ctx.lib.leo2d_ctx_stream(ctx.h))
+    E = energies(a, b)
+    dos = lambda mu: ctx.dos_reconstruct(mu.mean(axis=0), E, a, b, 1.0 / csr.n)
+    l0 = ctx.launch_count()
+    t32, d32 = _timed(stream, lambda: dos(csr.kpm_dos(cfg32)), args.steps, args.warmup)
+    launches = (ctx.launch_count() - l0) // (args.steps + args.warmup)
+    t64, d64 = _timed(stream, lambda: dos(csr.kpm_dos(cfg64)), 1, 1)
+    err = np.abs(d32 - d64) / np.abs(d64).max()
+    # the FP64 recursion against the CPU oracle, one vector
+    rp, col, val = csr.download()
+    re_, im_ = oracle.phase_vectors(3, 0, 1, csr.n)
+    mo = (oracle.kpm_trace(rp, col, val, re_, Pp, literal=False) +
+          oracle.kpm_trace(rp, col, val, im_, Pp, literal=False))[0]
+    m64 = csr.kpm_dos(L.kpm_cfg(Pp, R=1, seed=3, precision=L.FP64))[0]
+    out = {"metric": "periodic-supercell DOS (P=4096, 64 vectors, FP32 recursion)", "value": round(t32, 6),
+           "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": round(t32 * 1000, 3), "higher_is_better": False, "dtype": "fp32",
+           "data": "synthetic (commensurate supercell, Philox vectors)",
+           "config": {"workload": "TBLG (31,32) 1.05 deg periodic, simple model, P=4096, 64 random-phase vectors, "
+                                  "4001 energies", "orbitals": csr.n, "nnz": csr.nnz,
+                      "twist_deg": math.degrees(abs(gp.angles[1] - gp.angles[0])), "block_cols": cols},
+           "fp64_time_s": round(t64, 6),
+           "error_vs_fp64_per_energy": {"max": float(err.max()), "mean": float(err.mean()),
+                                        "p99": float(np.quantile(err, 0.99))},
+           "l1_vs_fp64": l1(d32, d64),
+           "fp64_gpu_vs_cpu_oracle_moments": float(np.abs(m64 - mo).max() / np.abs(mo).max()),
+           "gpu_launches": int(launches)}
+    print(json.dumps(out))
+    ctx.close()
+
+
+def run_kubo(args):
+    """Kubo sigma_xx(E): 1.5 deg flake of ~2M orbitals, 512 x 512 moments, 32 random-phase
+    vectors (trace), FP32 recursion with FP64 moment products, 2001 energies. FP32 against
+    the FP64 CPU oracle on a 20k-orbital flake of the same model and twist (one vector)."""
+    import torch
+    import leo2d_gb300 as L
+    from oracle import oracle
+    ctx = L.Context(0)
+    M, R, twist = 512, 32, 1.5
+    radius = math.sqrt(2.0e6 / 2.398)
+    csr = ctx.build_csr(ctx.prepare(geom(L, radius=radius, twist=twist)), with_dx=True)
+    lo, hi = csr.bounds()
+    a, b = 1.01 * (hi - lo) / 2, (hi + lo) / 2
+    csr.rescale(a, -b)
+    cfg = L.kpm_cfg(M, R=R, seed=21)
+    stream = torch.cuda.ExternalStream(ctx.lib.leo2d_ctx_stream(ctx.h))
+    Ek = b + a * np.linspace(-0.99, 0.99, 2001)
+    sig = lambda mu: ctx.cond_sigma(mu, Ek, a, b, 1.0 / csr.n)
+    l0 = ctx.launch_count()
+    t, s = _timed(stream, lambda: sig(csr.kpm_cond(cfg)), args.steps, min(args.warmup, 1))
+    launches = (ctx.launch_count() - l0) // (args.steps + min(args.warmup, 1))
+    # FP32 vs FP64 oracle on a small flake
+    small = ctx.build_csr(ctx.prepare(geom(L, radius=math.sqrt(2.0e4 / 2.398), twist=twist)), with_dx=True)
+    slo, shi = small.bounds()
+    sa, sb = 1.01 * (shi - slo) / 2, (shi + slo) / 2
+    small.rescale(sa, -sb)
+    Ms = 128
+    mu32 = small.kpm_cond(L.kpm_cfg(Ms, R=1, seed=5))
+    rp, col, val, dx, dy = small.download(dx=True)
+    re_, im_ = oracle.phase_vectors(5, 0, 1, small.n)
+    mu64 = oracle.kpm_cond_trace(rp, col, val, dx, re_, Ms) + oracle.kpm_cond_trace(rp, col, val, dx, im_, Ms)
+    Es = sb + sa * np.linspace(-0.99, 0.99, 2001)
+    s32 = ctx.cond_sigma(mu32, Es, sa, sb, 1.0 / small.n)
+    s64 = ctx.cond_sigma(mu64, Es, sa, sb, 1.0 / small.n)
+    out = {"metric": "Kubo sigma_xx(E) (512x512 moments, 32 random-phase vectors, 2001 energies)",
+           "value": round(t, 6), "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": min(args.warmup, 1),
+           "ms_per_step": round(t * 1000, 3), "higher_is_better": False, "dtype": "fp32",
+           "data": "synthetic (geometry generated on the GPU, Philox vectors)",
+           "config": {"workload": f"TBLG flake {twist} deg, ~2M orbitals, simple model, J=i[H,x] on the fly, "
+                                  "M=512, 32 vectors, 2001 energies", "orbitals": csr.n, "nnz": csr.nnz},
+           "fp32_vs_fp64_oracle": {"orbitals": small.n, "moments": Ms,
+                                   "mu_max_rel": float(np.abs(mu32 - mu64).max() / np.abs(mu64).max()),
+                                   "sigma_max_rel": float(np.abs(s32 - s64).max() / np.abs(s64).max())},
+           "sigma_range": [float(s.min()), float(s.max())],
+           "gpu_launches": int(launches)}
+    print(json.dumps(out))
+    ctx.close()
+
+
 # ---------------------------------------------------------------- batched flakes
 
 BATCH_F, BATCH_P, BATCH_R = 32, 2048, 32
@@ -442,9 +557,11 @@ def main():
     ap.add_argument("--ref-vectors", type=int, default=256)
     ap.add_argument("--no-cv", action="store_true", help="skip the learned control-variate comparison")
     ap.add_argument("--max-vectors", type=int, default=128)
-    ap.add_argument("--workload", default="flake10m", choices=["flake10m", "batch32"],
+    ap.add_argument("--workload", default="flake10m", choices=["flake10m", "batch32", "periodic", "kubo2m"],
                     help="flake10m: time-to-DOS on the 10M-orbital flake (the headline); batch32: 32 "
-                         "flakes of 20k-500k orbitals in one batched, graph-replayed run")
+                         "flakes of 20k-500k orbitals in one batched, graph-replayed run; periodic: the "
+                         "1.05 deg (31,32) supercell, P=4096, 64 vectors, FP32 vs FP64 per energy; kubo2m: "
+                         "sigma_xx(E) of a 2M-orbital 1.5 deg flake, 512x512 moments, 32 vectors")
     ap.add_argument("--step-kernel", type=int, default=-1, choices=[-1, 0, 1, 2],
                     help="force the Chebyshev step kernel: 0 tiled gathers, 1 register gathers, 2 tensor cores "
                          "(default: the autotuner's choice)")
@@ -456,6 +573,10 @@ def main():
         return kernel_case(args)
     if args.workload == "batch32" and args.impl == "ours":
         return run_batch(args)
+    if args.workload == "periodic" and args.impl == "ours":
+        return run_periodic(args)
+    if args.workload == "kubo2m" and args.impl == "ours":
+        return run_kubo(args)
     ws, rank, local, pg = dist_setup()
     threads = os.cpu_count() or 1
 

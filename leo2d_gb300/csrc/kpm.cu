@@ -27,7 +27,8 @@
 //   rows in flight form one band and their gathered neighbours stay in L2.
 //   Block partials of step k are reduced, in fixed order, by the first 2C blocks
 //   of step k+1 (deterministic, no extra launch per step).
-// The step launches of a whole recursion are captured in one CUDA graph.
+// One launch per step; whole runs are captured in CUDA graphs by the batched
+// driver (batch.cu).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
