@@ -430,6 +430,12 @@ def run_kubo(args):
     l0 = ctx.launch_count()
     t, s = _timed(stream, lambda: sig(csr.kpm_cond(cfg)), args.steps, min(args.warmup, 1))
     launches = (ctx.launch_count() - l0) // (args.steps + min(args.warmup, 1))
+    # where the time goes (one more run with per-launch events)
+    ctx.reset_stats()
+    ctx.set_profiling(True)
+    csr.kpm_cond(cfg)
+    ctx.set_profiling(False)
+    split = {k: round(ctx.kernel_stats(k)[1] / 1000.0, 4) for k in ("cheb_step", "cond_gemm")}
     # FP32 vs FP64 oracle on a small flake
     small = ctx.build_csr(ctx.prepare(geom(L, radius=math.sqrt(2.0e4 / 2.398), twist=twist)), with_dx=True)
     slo, shi = small.bounds()
@@ -452,7 +458,7 @@ def run_kubo(args):
            "fp32_vs_fp64_oracle": {"orbitals": small.n, "moments": Ms,
                                    "mu_max_rel": float(np.abs(mu32 - mu64).max() / np.abs(mu64).max()),
                                    "sigma_max_rel": float(np.abs(s32 - s64).max() / np.abs(s64).max())},
-           "sigma_range": [float(s.min()), float(s.max())],
+           "sigma_range": [float(s.min()), float(s.max())], "kernel_seconds": split,
            "gpu_launches": int(launches)}
     print(json.dumps(out))
     ctx.close()

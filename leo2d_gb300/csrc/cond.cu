@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "kpm.cuh"
+#include "tc_gemm.cuh"
 
 using namespace leo2d;
 
@@ -257,8 +258,9 @@ leo2d_status leo2d_kpm_cond(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kp
           ctx_sync(ctx);
         }
       } else {
-        // every column of the block: K = n x C; complex vectors add their two parts
-        gemm(ctx, U.p, Bv.p, P, (int64_t)vec, (int64_t)vec, (int64_t)vec, 1, acc.p);
+        // every column of the block: K = n x C; complex vectors add their two parts.
+        // mu += U Bv^T on the tensor cores (three TF32 products, FP64 sum of ranges)
+        tc_gemm_f32x3_acc(ctx, U.p, Bv.p, P, P, (int64_t)vec, acc.p);
       }
     }
     ctx_check_status(ctx, "Kubo recursion");

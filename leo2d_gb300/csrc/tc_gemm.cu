@@ -251,3 +251,236 @@ extern "C" leo2d_status leo2d_tc_gemm(leo2d_ctx* ctx, const uint16_t* a, const u
     ctx_check_status(ctx, "tensor-core GEMM");
   });
 }
+
+// ============================================================================
+// FP32 GEMM from three TF32 products (the Kubo moment product mu = U B^T)
+//
+// Work items are (128 x 256 output tile, K range of at most kF3Chunk k-blocks of
+// 32). Per item: warp 4 (one lane) streams 128x32 and 256x32 FP32 tiles with TMA
+// into a 2-stage ring; warps 0-3 write each tile's low part x - tf32(x)
+// elementwise into a parallel buffer (same swizzled layout); warp 5 (one lane)
+// issues 4 K steps x 3 tcgen05.mma.kind::tf32 (A_hi B_hi + A_hi B_lo + A_lo B_hi;
+// the tensor core reads the raw FP32 tile as its high part) into a 256-column TMEM
+// accumulator; warps 0-3 then store the item's FP32 partial tile. A second kernel
+// adds the partials of each output element in FP64 in a fixed order.
+// ============================================================================
+
+namespace {
+
+constexpr int F3_BM = 128, F3_BN = 256, F3_BK = 32, F3_ST = 2, kF3Chunk = 4096, kF3Flush = 64;
+constexpr uint32_t kF3A = F3_BM * F3_BK * 4, kF3B = F3_BN * F3_BK * 4;  // 16 KB, 32 KB
+constexpr uint32_t kF3Raw = kF3A + kF3B, kF3Stage = 2 * kF3Raw;         // raw + low parts
+constexpr uint32_t kF3Idesc = umma::idesc_tf32(F3_BM, F3_BN);
+
+struct F3Args {
+  int M, N;
+  int64_t K;
+  int m_tiles, n_tiles, splits;
+  int64_t chunk_kb;  // k-blocks per work item
+  double* partial;   // [items][128][256] FP64
+  int* status;
+};
+
+__device__ __forceinline__ float tf32_low(float x) {
+  return x - __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+}
+
+// Work items: (output tile, K range of chunk_kb k-blocks). The FP32 accumulator
+// is added into the item's FP64 tile every kF3Flush k-blocks (2048 products).
+__global__ void __launch_bounds__(192, 1)
+    k_tc_gemm_f32x3(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const F3Args g) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ __align__(8) uint64_t full[F3_ST], conv[F3_ST], empty[F3_ST], tfull, tfree;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < F3_ST; ++s) {
+      umma::bar_init(&full[s], 1);
+      umma::bar_init(&conv[s], 128);
+      umma::bar_init(&empty[s], 1);
+    }
+    umma::bar_init(&tfull, 1);
+    umma::bar_init(&tfree, 128);
+    umma::bar_fence_init();
+    abort_flag = 0;
+  }
+  if (warp == 0) umma::tmem_alloc(&tmem_base, F3_BN);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  const int64_t nkb = (g.K + F3_BK - 1) / F3_BK;
+  const int64_t items = (int64_t)g.m_tiles * g.n_tiles * g.splits;
+  uint32_t it = 0;   // k-blocks of this block so far (stage ring position)
+  uint32_t sub = 0;  // accumulator sub-ranges of this block so far
+  for (int64_t item = blockIdx.x; item < items && !abort_flag; item += gridDim.x) {
+    const int split = (int)(item % g.splits);
+    const int tile = (int)(item / g.splits);
+    const int mt = tile % g.m_tiles, nt = tile / g.m_tiles;
+    const int64_t kb0 = (int64_t)split * g.chunk_kb;
+    const int nk = (int)(min(nkb, kb0 + g.chunk_kb) - kb0);
+    const int nsub = (nk + kF3Flush - 1) / kF3Flush;
+    if (warp == 4) {
+      if (lane == 0)
+        for (int k = 0; k < nk && !abort_flag; ++k) {
+          const uint32_t i = it + k, s = i % F3_ST, ph = (i / F3_ST) & 1u;
+          if (!umma::bar_wait(&empty[s], ph ^ 1u)) {
+            abort_flag = 1;
+            break;
+          }
+          unsigned char* st = smem + (size_t)s * kF3Stage;
+          umma::bar_expect_tx(&full[s], kF3Raw);
+          umma::tma_load_2d(st, &ta, (int)((kb0 + k) * F3_BK), mt * F3_BM, &full[s]);
+          umma::tma_load_2d(st + kF3A, &tb, (int)((kb0 + k) * F3_BK), nt * F3_BN, &full[s]);
+        }
+    } else if (warp == 5) {
+      if (lane == 0)
+        for (int k = 0; k < nk && !abort_flag; ++k) {
+          const uint32_t i = it + k, s = i % F3_ST, ph = (i / F3_ST) & 1u;
+          const bool first_of_sub = (k % kF3Flush) == 0;
+          const uint32_t q = sub + (uint32_t)(k / kF3Flush);  // this sub-range's index
+          // the accumulator must have been read out by the previous sub-range's flush
+          if (first_of_sub && q > 0 && !umma::bar_wait(&tfree, (q - 1) & 1u)) {
+            abort_flag = 1;
+            break;
+          }
+          if (!umma::bar_wait(&conv[s], ph)) {
+            abort_flag = 1;
+            break;
+          }
+          umma::fence_after_sync();
+          const uint32_t a_hi = umma::saddr(smem + (size_t)s * kF3Stage), b_hi = a_hi + kF3A;
+          const uint32_t a_lo = a_hi + kF3Raw, b_lo = b_hi + kF3Raw;
+#pragma unroll
+          for (int ks = 0; ks < F3_BK / 8; ++ks) {
+            const uint32_t o = 32 * ks;
+            umma::mma_tf32_ss(tmem, umma::desc_k128(a_hi + o), umma::desc_k128(b_hi + o), kF3Idesc,
+                              (!first_of_sub || ks > 0) ? 1u : 0u);
+            umma::mma_tf32_ss(tmem, umma::desc_k128(a_hi + o), umma::desc_k128(b_lo + o), kF3Idesc, 1u);
+            umma::mma_tf32_ss(tmem, umma::desc_k128(a_lo + o), umma::desc_k128(b_hi + o), kF3Idesc, 1u);
+          }
+          umma::mma_commit(&empty[s]);
+          if ((k % kF3Flush) == kF3Flush - 1 || k == nk - 1) umma::mma_commit(&tfull);
+        }
+    } else {
+      // warps 0-3: low parts of each arriving stage; accumulator flushes into
+      // this item's FP64 tile (one row per thread)
+      double* acc = g.partial + (size_t)item * F3_BM * F3_BN + (size_t)threadIdx.x * F3_BN;
+      for (int c = 0; c < F3_BN; c += 2) *reinterpret_cast<double2*>(acc + c) = make_double2(0.0, 0.0);
+      for (int k = 0; k < nk; ++k) {
+        const uint32_t i = it + k, s = i % F3_ST, ph = (i / F3_ST) & 1u;
+        if (!umma::bar_wait(&full[s], ph)) {
+          abort_flag = 1;
+          break;
+        }
+        const float4* src = reinterpret_cast<const float4*>(smem + (size_t)s * kF3Stage);
+        float4* dst = reinterpret_cast<float4*>(smem + (size_t)s * kF3Stage + kF3Raw);
+        for (int e = threadIdx.x; e < (int)(kF3Raw / 16); e += 128) {
+          const float4 x = src[e];
+          dst[e] = make_float4(tf32_low(x.x), tf32_low(x.y), tf32_low(x.z), tf32_low(x.w));
+        }
+        umma::fence_proxy_async();
+        umma::bar_arrive(&conv[s]);
+        if ((k % kF3Flush) == kF3Flush - 1 || k == nk - 1) {
+          const uint32_t q = sub + (uint32_t)(k / kF3Flush);
+          if (!umma::bar_wait(&tfull, q & 1u)) {
+            abort_flag = 1;
+            break;
+          }
+          umma::fence_after_sync();
+          for (int c0 = 0; c0 < F3_BN; c0 += 16) {
+            float v[16];
+            umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+#pragma unroll
+            for (int j = 0; j < 16; j += 2) {
+              double2 a = *reinterpret_cast<double2*>(acc + c0 + j);
+              a.x += (double)v[j];
+              a.y += (double)v[j + 1];
+              *reinterpret_cast<double2*>(acc + c0 + j) = a;
+            }
+          }
+          umma::fence_before_sync();
+          umma::bar_arrive(&tfree);
+        }
+      }
+    }
+    it += nk;
+    sub += nsub;
+    __syncthreads();
+  }
+  // drain: the last sub-range's MMAs were waited for by its flush; a block that
+  // gave up waits (bounded) for whatever it issued
+  umma::fence_before_sync();
+  __syncthreads();
+  if (abort_flag && threadIdx.x == 0) atomicExch(g.status, kStatusTimeout);
+  if (warp == 0) umma::tmem_dealloc(tmem, F3_BN);
+}
+
+// out[m][n] += sum over the K ranges of the FP64 partial tiles, fixed order.
+__global__ void k_f3_reduce(const double* __restrict__ partial, int M, int N, int m_tiles, int splits,
+                            double* __restrict__ out) {
+  const int64_t total = (int64_t)M * N;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int m = (int)(e / N), n = (int)(e % N);
+    const int tile = (n / F3_BN) * m_tiles + m / F3_BM;
+    const size_t in_tile = (size_t)(m % F3_BM) * F3_BN + (n % F3_BN);
+    double s = 0.0;
+    for (int sp = 0; sp < splits; ++sp) s += partial[((size_t)tile * splits + sp) * F3_BM * F3_BN + in_tile];
+    out[e] += s;
+  }
+}
+
+}  // namespace
+
+namespace leo2d {
+
+void make_tmap_f32(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, int64_t ld, int box_rows) {
+  auto fn = encode_fn();
+  LEO_REQUIRE(fn != nullptr, "cuTensorMapEncodeTiled is not available from the driver");
+  LEO_REQUIRE(((uintptr_t)base & 15) == 0, "tensor base must be 16-byte aligned");
+  LEO_REQUIRE((ld * 4) % 16 == 0, "tensor row stride must be a multiple of 16 bytes");
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * 4)};
+  cuuint32_t box[2] = {(cuuint32_t)F3_BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  LEO_REQUIRE(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled rejected the tensor");
+}
+
+void tc_gemm_f32x3_acc(leo2d_ctx* ctx, const float* A, const float* B, int M, int N, int64_t K, double* out) {
+  LEO_REQUIRE(M > 0 && N > 0 && K > 0, "empty GEMM");
+  LEO_REQUIRE(K % 4 == 0, "K must be a multiple of 4");
+  LEO_REQUIRE((K + F3_BK - 1) / F3_BK * F3_BK < (1ll << 31), "K too large for TMA coordinates");
+  CUtensorMap ta, tb;
+  make_tmap_f32(&ta, A, M, K, K, F3_BM);
+  make_tmap_f32(&tb, B, N, K, K, F3_BN);
+  F3Args g{};
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.m_tiles = (M + F3_BM - 1) / F3_BM;
+  g.n_tiles = (N + F3_BN - 1) / F3_BN;
+  const int64_t nkb = (K + F3_BK - 1) / F3_BK;
+  g.splits = (int)((nkb + kF3Chunk - 1) / kF3Chunk);
+  g.chunk_kb = kF3Chunk;
+  const int64_t items = (int64_t)g.m_tiles * g.n_tiles * g.splits;
+  DevBuf<double> partial((size_t)items * F3_BM * F3_BN);
+  g.partial = partial.p;
+  g.status = ctx->status.p;
+  const size_t smem = (size_t)F3_ST * kF3Stage + 1024;
+  LEO_CUDA(cudaFuncSetAttribute(k_tc_gemm_f32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const unsigned grid = (unsigned)std::min<int64_t>(items, ctx->sm_count);
+  launch(ctx, "cond_gemm", [&] { k_tc_gemm_f32x3<<<grid, 192, smem, ctx->stream>>>(ta, tb, g); });
+  launch(ctx, "cond_gemm_sum", [&] {
+    k_f3_reduce<<<grid_for((int64_t)M * N, 256, (int64_t)ctx->sm_count * 8), 256, 0, ctx->stream>>>(
+        partial.p, M, N, g.m_tiles, g.splits, out);
+  });
+  ctx_check_status(ctx, "tensor-core FP32 product");
+}
+
+}  // namespace leo2d

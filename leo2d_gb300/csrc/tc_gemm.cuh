@@ -58,6 +58,16 @@ void make_tmap_bf16_ld(CUtensorMap* map, const void* base, int64_t rows, int64_t
 // Blocks a GEMM of this output shape launches (one per SM at most).
 int tc_gemm_grid(leo2d_ctx* ctx, int M, int N);
 
+// TMA map for a row-major FP32 matrix [rows][cols] (row stride `ld` elements),
+// boxes of 32 columns (128 bytes) x box_rows rows, 128-byte swizzle.
+void make_tmap_f32(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, int64_t ld, int box_rows);
+
+// out[M][N] (FP64, row-major) += A[M][K] * B[N][K]^T with FP32 operands, on the
+// tensor cores: three TF32 products per K step (hi*hi + hi*lo + lo*hi), FP32
+// accumulation over 2048 products at a time, added into FP64 partial tiles that
+// are summed in a fixed order. K must be a multiple of 4 (16-byte rows).
+void tc_gemm_f32x3_acc(leo2d_ctx* ctx, const float* A, const float* B, int M, int N, int64_t K, double* out);
+
 // Sets the kernels' shared-memory attributes on the context's device (once;
 // call before capturing GEMM launches into a graph).
 void tc_gemm_prepare(leo2d_ctx* ctx);

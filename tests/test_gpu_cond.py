@@ -74,3 +74,18 @@ def test_cond_needs_dx(ctx):
     csr = ctx.build_csr(ctx.prepare(g))
     with pytest.raises(L.Leo2dError, match="WITH_DX"):
         csr.kpm_cond(L.kpm_cfg(8), [0])
+
+
+def test_trace_cond_large_product(ctx):
+    """256 x 256 trace moments: the moment product runs on the tensor cores over
+    several output tiles and K ranges (three TF32 products, FP64 sum)."""
+    g = L.make_geom(model=L.MODEL_SIMPLE, size=40, max_R=60.0, angles_deg=(0.0, 2.0), energy_rescale=1.0)
+    csr = ctx.build_csr(ctx.prepare(g), with_dx=True)
+    lo, hi = csr.bounds()
+    csr.rescale(1.01 * (hi - lo) / 2, -(hi + lo) / 2)
+    rp, col, val, dx, dy = csr.download(dx=True)
+    M, R, seed = 256, 2, 8
+    mu = csr.kpm_cond(L.kpm_cfg(M, R=R, kind=L.VEC_PHASE, seed=seed))
+    re, im = oracle.phase_vectors(seed, 0, R, csr.n)
+    ref = (oracle.kpm_cond_trace(rp, col, val, dx, re, M) + oracle.kpm_cond_trace(rp, col, val, dx, im, M)) / R
+    assert _rel(mu, ref) < FP32_RTOL
