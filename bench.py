@@ -464,6 +464,51 @@ def run_kubo(args):
     ctx.close()
 
 
+def run_mlp(args):
+    """The learned control variate's network on the tensor cores: Adam training steps
+    (batch 8192, graph-replayed) and inference of the moment sum over every orbital of
+    the flake of --radius (default: the 10M-orbital 0.5 deg flake)."""
+    import torch
+    import leo2d_gb300 as L
+    ctx = L.Context(0)
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1, 1, (65536, 16)).astype(np.float32)
+    t = rng.normal(0, 0.3, (65536, 256)).astype(np.float32)
+    mlp = L.Mlp(ctx, seed=0)
+    B = 8192
+    stream = torch.cuda.ExternalStream(ctx.lib.leo2d_ctx_stream(ctx.h))
+    t_step = float("nan")
+    if not args.mlp_infer_only:
+        mlp.train(x, t, steps=5, batch=B)
+        t_short, _ = _timed(stream, lambda: mlp.train(x, t, steps=20, batch=B, seed=2), 1, 0)
+        t_long, _ = _timed(stream, lambda: mlp.train(x, t, steps=220, batch=B, seed=3), 1, 0)
+        t_step = (t_long - t_short) / 200.0
+    layer_macs = 64 * 256 + 3 * 256 * 256
+    flops_step = 2 * B * layer_macs * 2 + 2 * B * 3 * 256 * 256  # forward, weight gradients, input gradients
+    csr = ctx.build_csr(ctx.prepare(geom(L, radius=args.radius)))
+    mlp.site_sum(csr, TWIST_DEG)
+    t_inf, _ = _timed(stream, lambda: mlp.site_sum(csr, TWIST_DEG), args.steps, 1)
+    flops_inf = 2 * csr.n * layer_macs
+    peak = 1900.0
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+    except (OSError, ValueError, KeyError):
+        pass
+    out = {"metric": "control-variate network: inference over every orbital (16 -> 3x256 GELU -> 256, BF16)",
+           "value": round(t_inf, 6), "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": 1,
+           "higher_is_better": False, "dtype": "bf16 (fp32 accumulation)", "data": "synthetic",
+           "config": {"workload": f"site sums over {csr.n} orbitals; training batch {B}", "orbitals": csr.n},
+           "inference_tflops": round(flops_inf / t_inf / 1e12, 1),
+           "train_step_ms": round(t_step * 1000, 4), "train_tflops": round(flops_step / t_step / 1e12, 1),
+           "roofline": {"bound": "tensor", "achieved": round(flops_inf / t_inf / 1e12, 1), "peak": peak,
+                        "unit": "TFLOP/s", "frac": round(flops_inf / t_inf / 1e12 / peak, 4),
+                        "peak_kind": "measured (cuBLAS bf16 burst)"}}
+    print(json.dumps(out))
+    mlp.close()
+    ctx.close()
+
+
 # ---------------------------------------------------------------- batched flakes
 
 BATCH_F, BATCH_P, BATCH_R = 32, 2048, 32
@@ -562,12 +607,16 @@ def main():
     ap.add_argument("--radius", type=float, default=RADIUS)
     ap.add_argument("--ref-vectors", type=int, default=256)
     ap.add_argument("--no-cv", action="store_true", help="skip the learned control-variate comparison")
+    ap.add_argument("--mlp-infer-only", action="store_true",
+                    help="mlp workload: skip the training measurement (profiling the inference products)")
     ap.add_argument("--max-vectors", type=int, default=128)
-    ap.add_argument("--workload", default="flake10m", choices=["flake10m", "batch32", "periodic", "kubo2m"],
+    ap.add_argument("--workload", default="flake10m",
+                    choices=["flake10m", "batch32", "periodic", "kubo2m", "mlp"],
                     help="flake10m: time-to-DOS on the 10M-orbital flake (the headline); batch32: 32 "
                          "flakes of 20k-500k orbitals in one batched, graph-replayed run; periodic: the "
                          "1.05 deg (31,32) supercell, P=4096, 64 vectors, FP32 vs FP64 per energy; kubo2m: "
-                         "sigma_xx(E) of a 2M-orbital 1.5 deg flake, 512x512 moments, 32 vectors")
+                         "sigma_xx(E) of a 2M-orbital 1.5 deg flake, 512x512 moments, 32 vectors; mlp: the "
+                         "control variate's network (training steps, inference over the flake of --radius)")
     ap.add_argument("--step-kernel", type=int, default=-1, choices=[-1, 0, 1, 2],
                     help="force the Chebyshev step kernel: 0 tiled gathers, 1 register gathers, 2 tensor cores "
                          "(default: the autotuner's choice)")
@@ -583,6 +632,8 @@ def main():
         return run_periodic(args)
     if args.workload == "kubo2m" and args.impl == "ours":
         return run_kubo(args)
+    if args.workload == "mlp" and args.impl == "ours":
+        return run_mlp(args)
     ws, rank, local, pg = dist_setup()
     threads = os.cpu_count() or 1
 

@@ -33,6 +33,7 @@ namespace {
 constexpr int kIn = 64, kHid = 256, kOut = 256, kLayers = 4, kFeat = 16;
 constexpr int kInDim[kLayers] = {kIn, kHid, kHid, kHid};
 constexpr int64_t kChunk = 1 << 20;  // sites per inference pass
+constexpr int kDwSplits = 32;        // K-range splits of the weight-gradient products
 
 __device__ __forceinline__ uint32_t mix32(uint64_t a, uint64_t b) {
   // splitmix64 of (a, b): minibatch indices
@@ -236,7 +237,7 @@ struct leo2d_mlp {
   // training workspace (batch B)
   int B = 0;
   DevBuf<__nv_bfloat16> Xb, Xbt, A[kLayers], At[kLayers], dZ[2], dZt[2];
-  DevBuf<float> Tb, Z[kLayers], Y, dZ32[2], cs_part;
+  DevBuf<float> Tb, Z[kLayers], Y, dZ32[2], cs_part, dw_split;
   DevBuf<double> loss_part, loss_last, loss_hist;
   int64_t hist_cap = 0;
   CUtensorMap tX, tA[kLayers], tWt[kLayers], tWn[kLayers], tXt, tAt[kLayers], tdZ[2], tdZt[2];
@@ -289,6 +290,7 @@ void ensure_batch(leo2d_mlp* M, int B) {
     M->dZt[i].alloc((size_t)kHid * B);
     M->dZ32[i].alloc((size_t)B * kHid);
   }
+  M->dw_split.alloc((size_t)kDwSplits * kHid * kHid);
   const int cs_blocks = (B + 63) / 64;
   M->cs_part.alloc((size_t)cs_blocks * kOut);
   M->loss_part.alloc(1024);
@@ -360,6 +362,9 @@ void backward_train(leo2d_mlp* M, int n) {
       g.K = n;
       g.out_f32 = M->g.p + M->w_off[l];
       g.status = ctx->status.p;
+      // K = n rows: split over up to 32 work items per output tile
+      g.k_splits = std::max(1, std::min(kDwSplits, n / 256));
+      g.split_buf = M->dw_split.p;
       tc_gemm(ctx, kEpiF32, M->tdZt[cur], l == 0 ? M->tXt : M->tAt[l], g);
     }
     if (l == 0) break;

@@ -20,7 +20,7 @@ __device__ __forceinline__ float gelu_grad(float z) {
 }
 
 template <int EPI>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(256, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const GemmArgs g) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(128, 1)
     abort_flag = 0;
   }
   if (EPI == kEpiBias)
-    for (int i = threadIdx.x; i < 4 * BN; i += 128) (&wsum[0][0])[i] = 0.0;
+    for (int i = threadIdx.x; i < 4 * BN; i += blockDim.x) (&wsum[0][0])[i] = 0.0;
   if (warp == 0) umma::tmem_alloc(&tmem_base, BN);
   umma::fence_before_sync();
   __syncthreads();
@@ -49,11 +49,16 @@ __global__ void __launch_bounds__(128, 1)
   const uint32_t tmem = tmem_base;
 
   const int m_tiles = (g.M + BM - 1) / BM, n_tiles = (g.N + BN - 1) / BN;
-  const int nkb = (g.K + BK - 1) / BK;
+  const int nkb_all = (g.K + BK - 1) / BK;
+  const int splits = g.k_splits > 1 ? g.k_splits : 1;
+  const int kpb = (nkb_all + splits - 1) / splits;  // k-blocks per split
   uint32_t it = 0;
   int local = 0;
-  for (int t = blockIdx.x; t < m_tiles * n_tiles; t += gridDim.x, ++local) {
-    const int mt = t % m_tiles, nt = t / m_tiles;
+  for (int t = blockIdx.x; t < m_tiles * n_tiles * splits; t += gridDim.x, ++local) {
+    const int split = t % splits, tile = t / splits;
+    const int mt = tile % m_tiles, nt = tile / m_tiles;
+    const int kb_first = split * kpb;
+    const int nkb = max(0, min(nkb_all, kb_first + kpb) - kb_first);
     if (warp == 0 && lane == 0) {
       // producer: TMA tiles of A and B into the ring
       for (int kb = 0; kb < nkb && !abort_flag; ++kb) {
@@ -64,8 +69,8 @@ __global__ void __launch_bounds__(128, 1)
         }
         unsigned char* st = smem + (size_t)s * kStage;
         umma::bar_expect_tx(&full[s], kStage);
-        umma::tma_load_2d(st, &ta, kb * BK, mt * BM, &full[s]);
-        umma::tma_load_2d(st + kABytes, &tb, kb * BK, nt * BN, &full[s]);
+        umma::tma_load_2d(st, &ta, (kb_first + kb) * BK, mt * BM, &full[s]);
+        umma::tma_load_2d(st + kABytes, &tb, (kb_first + kb) * BK, nt * BN, &full[s]);
       }
     } else if (warp == 1 && lane == 0) {
       // MMA issuer
@@ -94,14 +99,22 @@ __global__ void __launch_bounds__(128, 1)
     }
     umma::fence_after_sync();
 
-    // epilogue: thread = one row of the tile
-    const int r = mt * BM + warp * 32 + lane;
+    // epilogue: thread = one row of the tile; warps w and w + 4 share the
+    // tensor-memory lanes of quarter w and split the columns
+    const int quarter = warp & 3, chalf = warp >> 2;
+    const int r = mt * BM + quarter * 32 + lane;
     const bool row_ok = r < g.M;
-    for (int c0 = 0; c0 < BN; c0 += 16) {
+    float* out32 = (EPI == kEpiF32 && splits > 1) ? g.split_buf + (size_t)split * g.M * g.N : g.out_f32;
+    for (int c0 = chalf * (BN / 2); c0 < (chalf + 1) * (BN / 2); c0 += 16) {
       const int n0 = nt * BN + c0;
       if (n0 >= g.N) break;
       float v[16];
-      umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      if (nkb > 0) {
+        umma::tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0, v);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = 0.0f;  // an empty K range contributes nothing
+      }
       const int cnt = min(16, g.N - n0);
       if (EPI == kEpiBias && g.colsum) {
 #pragma unroll
@@ -109,32 +122,86 @@ __global__ void __launch_bounds__(128, 1)
           double x = (row_ok && j < cnt) ? (double)(v[j] + g.bias[n0 + j]) : 0.0;
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-          if (lane == 0 && j < cnt) wsum[warp][c0 + j] += x;
+          if (lane == 0 && j < cnt) wsum[quarter][c0 + j] += x;
         }
         continue;
       }
       if (!row_ok) continue;
       const size_t base = (size_t)r * g.N + n0;
-      if (EPI == kEpiF32) {
-        for (int j = 0; j < cnt; ++j) g.out_f32[base + j] = v[j];
-      } else if (EPI == kEpiBias) {
-        for (int j = 0; j < cnt; ++j) g.out_f32[base + j] = v[j] + g.bias[n0 + j];
+      // full 16-column chunks of 16-byte-aligned rows go out as vectors
+      const bool vec = cnt == 16 && (g.N & 15) == 0;
+      if (EPI == kEpiF32 || EPI == kEpiBias) {
+        float o[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) o[j] = EPI == kEpiBias && j < cnt ? v[j] + g.bias[n0 + j] : v[j];
+        if (vec) {
+#pragma unroll
+          for (int j = 0; j < 16; j += 4)
+            *reinterpret_cast<float4*>(out32 + base + j) = make_float4(o[j], o[j + 1], o[j + 2], o[j + 3]);
+        } else {
+          for (int j = 0; j < cnt; ++j) out32[base + j] = o[j];
+        }
       } else if (EPI == kEpiBiasGelu) {
-        for (int j = 0; j < cnt; ++j) {
-          const float z = v[j] + g.bias[n0 + j];
-          if (g.zout) g.zout[base + j] = z;
-          const __nv_bfloat16 h = __float2bfloat16_rn(gelu(z));
-          if (g.out_bf16) g.out_bf16[base + j] = h;
-          if (g.out_bf16_t) g.out_bf16_t[(size_t)(n0 + j) * g.ld_t + r] = h;
+        float z[16];
+        __nv_bfloat16 h[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          z[j] = j < cnt ? v[j] + g.bias[n0 + j] : 0.0f;
+          h[j] = __float2bfloat16_rn(gelu(z[j]));
         }
+        if (vec) {
+          if (g.zout)
+#pragma unroll
+            for (int j = 0; j < 16; j += 4)
+              *reinterpret_cast<float4*>(g.zout + base + j) = make_float4(z[j], z[j + 1], z[j + 2], z[j + 3]);
+          if (g.out_bf16) {
+            const uint4* hv = reinterpret_cast<const uint4*>(h);
+            reinterpret_cast<uint4*>(g.out_bf16 + base)[0] = hv[0];
+            reinterpret_cast<uint4*>(g.out_bf16 + base)[1] = hv[1];
+          }
+        } else {
+          for (int j = 0; j < cnt; ++j) {
+            if (g.zout) g.zout[base + j] = z[j];
+            if (g.out_bf16) g.out_bf16[base + j] = h[j];
+          }
+        }
+        if (g.out_bf16_t)
+          for (int j = 0; j < cnt; ++j) g.out_bf16_t[(size_t)(n0 + j) * g.ld_t + r] = h[j];
       } else {  // kEpiGeluBwd
-        for (int j = 0; j < cnt; ++j) {
-          const float gz = v[j] * gelu_grad(g.zin[base + j]);
-          if (g.out_f32) g.out_f32[base + j] = gz;
-          const __nv_bfloat16 h = __float2bfloat16_rn(gz);
-          if (g.out_bf16) g.out_bf16[base + j] = h;
-          if (g.out_bf16_t) g.out_bf16_t[(size_t)(n0 + j) * g.ld_t + r] = h;
+        float zi[16], gz[16];
+        __nv_bfloat16 h[16];
+        if (vec) {
+#pragma unroll
+          for (int j = 0; j < 16; j += 4) {
+            const float4 q = *reinterpret_cast<const float4*>(g.zin + base + j);
+            zi[j] = q.x; zi[j + 1] = q.y; zi[j + 2] = q.z; zi[j + 3] = q.w;
+          }
+        } else {
+          for (int j = 0; j < 16; ++j) zi[j] = j < cnt ? g.zin[base + j] : 0.0f;
         }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          gz[j] = v[j] * gelu_grad(zi[j]);
+          h[j] = __float2bfloat16_rn(gz[j]);
+        }
+        if (vec) {
+          if (g.out_f32)
+#pragma unroll
+            for (int j = 0; j < 16; j += 4)
+              *reinterpret_cast<float4*>(g.out_f32 + base + j) = make_float4(gz[j], gz[j + 1], gz[j + 2], gz[j + 3]);
+          if (g.out_bf16) {
+            const uint4* hv = reinterpret_cast<const uint4*>(h);
+            reinterpret_cast<uint4*>(g.out_bf16 + base)[0] = hv[0];
+            reinterpret_cast<uint4*>(g.out_bf16 + base)[1] = hv[1];
+          }
+        } else {
+          for (int j = 0; j < cnt; ++j) {
+            if (g.out_f32) g.out_f32[base + j] = gz[j];
+            if (g.out_bf16) g.out_bf16[base + j] = h[j];
+          }
+        }
+        if (g.out_bf16_t)
+          for (int j = 0; j < cnt; ++j) g.out_bf16_t[(size_t)(n0 + j) * g.ld_t + r] = h[j];
       }
     }
     umma::fence_before_sync();
@@ -144,9 +211,18 @@ __global__ void __launch_bounds__(128, 1)
   __syncthreads();
   if (abort_flag && threadIdx.x == 0) atomicExch(g.status, kStatusTimeout);
   if (EPI == kEpiBias && g.colsum)
-    for (int n = threadIdx.x; n < g.N && n < BN; n += 128)
+    for (int n = threadIdx.x; n < g.N && n < BN; n += blockDim.x)
       g.colsum[(size_t)blockIdx.x * g.N + n] = ((wsum[0][n] + wsum[1][n]) + wsum[2][n]) + wsum[3][n];
   if (warp == 0) umma::tmem_dealloc(tmem, BN);
+}
+
+// out[e] = sum over the K-range splits of part[s][e] (fixed order).
+__global__ void k_split_sum(const float* __restrict__ part, int splits, int64_t total, float* __restrict__ out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.0f;
+    for (int k = 0; k < splits; ++k) s += part[(size_t)k * total + e];
+    out[e] = s;
+  }
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -200,15 +276,26 @@ void tc_gemm(leo2d_ctx* ctx, GemmEpi epi, const CUtensorMap& ta, const CUtensorM
              int grid_cap) {
   LEO_REQUIRE(g.M > 0 && g.N > 0 && g.K > 0, "empty GEMM");
   const size_t smem = gemm_smem_bytes(BN);
-  const int tiles = ((g.M + BM - 1) / BM) * ((g.N + BN - 1) / BN);
+  const int splits = (epi == kEpiF32 && g.k_splits > 1 && g.split_buf) ? g.k_splits : 1;
+  LEO_REQUIRE(splits == 1 || epi == kEpiF32, "only the plain product splits its K range");
+  const int tiles = ((g.M + BM - 1) / BM) * ((g.N + BN - 1) / BN) * splits;
   int grid = std::min(tiles, ctx->sm_count);
   if (grid_cap > 0) grid = std::min(grid, grid_cap);
   tc_gemm_prepare(ctx);
+  GemmArgs ga = g;
+  ga.k_splits = splits;
   auto go = [&](auto kern) {
-    launch(ctx, "tc_gemm", [&] { kern<<<grid, 128, smem, ctx->stream>>>(ta, tb, g); });
+    launch(ctx, "tc_gemm", [&] { kern<<<grid, 256, smem, ctx->stream>>>(ta, tb, ga); });
   };
   switch (epi) {
-    case kEpiF32: return go(k_tc_gemm<kEpiF32>);
+    case kEpiF32:
+      go(k_tc_gemm<kEpiF32>);
+      if (splits > 1)
+        launch(ctx, "tc_gemm_sum", [&] {
+          k_split_sum<<<grid_for((int64_t)g.M * g.N, 256, (int64_t)ctx->sm_count * 8), 256, 0, ctx->stream>>>(
+              g.split_buf, splits, (int64_t)g.M * g.N, g.out_f32);
+        });
+      return;
     case kEpiBias: return go(k_tc_gemm<kEpiBias>);
     case kEpiBiasGelu: return go(k_tc_gemm<kEpiBiasGelu>);
     case kEpiGeluBwd: return go(k_tc_gemm<kEpiGeluBwd>);

@@ -42,6 +42,10 @@ struct GemmArgs {
   float* zout;                 // [M][N]
   double* colsum;              // [gridDim.x][N] (kEpiBias only, optional)
   int* status;
+  // kEpiF32 only: the K range is split over k_splits work items per output tile;
+  // item s writes split_buf + s*M*N and a second pass adds them into out_f32
+  int k_splits;
+  float* split_buf;
 };
 
 constexpr int kGemmBM = 128, kGemmBK = 64, kGemmStages = 4;
