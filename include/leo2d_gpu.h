@@ -262,6 +262,16 @@ leo2d_status leo2d_tc_gemm(leo2d_ctx* ctx, const uint16_t* a, const uint16_t* b,
  * 128-row tile) and most entries in one tile. */
 leo2d_status leo2d_csr_tc_info(const leo2d_csr* csr, int64_t* tiles, double* mean_window, int32_t* max_window,
                                int32_t* max_tile_entries);
+/* Row blocks of the locality-ordered copy (built by the first recursion that
+ * runs the row-block step, step_kernel = 3 or autotuned): blocks of 8 rows
+ * stored as the sorted union of their rows' columns with a dense 8 x slots
+ * panel of FP32 values, so that one gathered T_n row serves 8 rows. Reports the
+ * row-block count, slots stored (padded to multiples of 4 per block), distinct
+ * slots before padding, the most slots of one block and the largest tile of 16
+ * blocks in bytes; zeros when not built. Replaces, for the recursion only, the
+ * CSR stream of SpMatrix::vectorMultiply (src/matrix/spmatrix.cpp:346-360). */
+leo2d_status leo2d_csr_rb_info(const leo2d_csr* csr, int64_t* row_blocks, int64_t* slots, int64_t* union_slots,
+                               int32_t* max_slots, int64_t* max_tile_bytes);
 leo2d_status leo2d_tc_gemm_tf32x3(leo2d_ctx* ctx, const float* a, const float* b, int64_t N, int64_t K, float* d);
 
 /* ---------------------------------------------------------------- learned control variate */

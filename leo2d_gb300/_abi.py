@@ -140,6 +140,7 @@ def _declare(lib):
     fn("leo2d_tc_gemm", c_i32, c_void_p, P, P, c_i64, c_i64, c_i64, P)
     fn("leo2d_tc_gemm_tf32x3", c_i32, c_void_p, P, P, c_i64, c_i64, P)
     fn("leo2d_csr_tc_info", c_i32, c_void_p, P, P, P, P)
+    fn("leo2d_csr_rb_info", c_i32, c_void_p, P, P, P, P, P)
     fn("leo2d_mlp_param_count", c_i64)
     fn("leo2d_mlp_create", c_i32, c_void_p, c_u64, pp)
     fn("leo2d_mlp_destroy", c_i32, c_void_p)

@@ -230,6 +230,14 @@ class Csr:
                                                       ctypes.byref(me)))
         return t.value, w.value, mw.value, me.value
 
+    def rb_info(self):
+        """Row blocks: (blocks, slots stored, distinct slots, most slots of a block, largest tile bytes)."""
+        b, s, u, ms, mt = (ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int32(),
+                           ctypes.c_int64())
+        self.ctx.check(self.ctx.lib.leo2d_csr_rb_info(self.h, ctypes.byref(b), ctypes.byref(s), ctypes.byref(u),
+                                                      ctypes.byref(ms), ctypes.byref(mt)))
+        return b.value, s.value, u.value, ms.value, mt.value
+
     def bounds(self):
         lo, hi = ctypes.c_double(), ctypes.c_double()
         self.ctx.check(self.ctx.lib.leo2d_csr_bounds(self.ctx.h, self.h, ctypes.byref(lo),

@@ -98,14 +98,17 @@ struct leo2d_ctx {
   std::vector<leo2d::PendingTimer> pending;
   std::vector<cudaEvent_t> free_events;
   int64_t launches = 0;
-  int kernel_variant = -1;    // -1 autotuned, 0 tiled gathers, 1 register gathers, 2 tensor cores
+  int kernel_variant = -1;    // -1 autotuned, 0 tiled gathers, 1 register gathers, 2 tensor cores, 3 row blocks
+  int rb_packed = -1;         // row-block step: paired FP32 FMAs (fma.rn.f32x2): -1 autotuned, 0 no, 1 yes
+  int rb_warps = 0;           // row-block step: warps per block (= row blocks per tile): 0 autotuned, 16, 24, 32
+  int rb_unroll = 0;          // row-block step: slot batches in flight per lane: 0 autotuned, 4, 8
   int tile_stages = 2;        // shared-memory stages of the tiled kernel
   int test_unsatisfied_wait = 0;  // test hook: tiled steps first wait on a barrier nobody completes
   bool tc_gemm_ready = false;     // shared-memory attributes of the tensor-core GEMM set on this device
   int tile_chunk = 4;         // consecutive tiles per block between grid-wide jumps
   int tile_warps = 0;         // warps per block of the tiled kernel (0 = per shape, 8 or 24)
   int reorder = -1;           // locality ordering: -1 auto, 0 off, 1 on
-  double reorder_patch = 16.0;  // patch edge (A)
+  double reorder_patch = 0.0;   // patch edge (A); 0: the step kernel's own (16 A; 32 A for row blocks)
   leo2d::DevBuf<int> status;  // one int, reset before kernels that may set it
 };
 

@@ -283,9 +283,18 @@ leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value
   return guard(ctx, [&] {
     const std::string k(key);
     if (k == "step_kernel") {
-      LEO_REQUIRE(value >= -1 && value <= 2,
-                  "step_kernel must be -1 (autotuned), 0 (tiled), 1 (register) or 2 (tensor cores)");
+      LEO_REQUIRE(value >= -1 && value <= 3,
+                  "step_kernel must be -1 (autotuned), 0 (tiled), 1 (register), 2 (tensor cores) or 3 (row blocks)");
       ctx->kernel_variant = (int)value;
+    } else if (k == "rb_packed") {
+      LEO_REQUIRE(value >= -1 && value <= 1, "rb_packed must be -1 (autotuned), 0 or 1");
+      ctx->rb_packed = (int)value;
+    } else if (k == "rb_warps") {
+      LEO_REQUIRE(value == 0 || value == 16 || value == 24 || value == 32, "rb_warps must be 0, 16, 24 or 32");
+      ctx->rb_warps = (int)value;
+    } else if (k == "rb_unroll") {
+      LEO_REQUIRE(value == 0 || value == 4 || value == 8, "rb_unroll must be 0, 4 or 8");
+      ctx->rb_unroll = (int)value;
     } else if (k == "test_unsatisfied_wait") {
       // every tiled step waits on an mbarrier that never completes, gives up
       // after the spin limit and reports LEO2D_ERR_TIMEOUT (tests the bounded
@@ -304,7 +313,8 @@ leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value
       LEO_REQUIRE(value >= -1 && value <= 1, "reorder must be -1, 0 or 1");
       ctx->reorder = (int)value;
     } else if (k == "reorder_patch_dA") {
-      LEO_REQUIRE(value >= 5 && value <= 2000, "reorder_patch_dA must be 5..2000 (tenths of A)");
+      LEO_REQUIRE(value == 0 || (value >= 5 && value <= 2000),
+                  "reorder_patch_dA must be 0 (per step kernel) or 5..2000 (tenths of A)");
       ctx->reorder_patch = value / 10.0;
     } else {
       fail(LEO2D_ERR_BAD_ARG, "unknown option " + k);

@@ -57,6 +57,18 @@ struct leo2d_csr {
   leo2d::DevBuf<int32_t> tc_nwin;     // [tiles] window width
   leo2d::DevBuf<uint2> tc_ent;        // nnz (+pad): (position, value bits), rows as prow
   leo2d::DevBuf<uint8_t> tc_cstart;   // [n][16] first entry of each 64-position chunk, from the row start
+  // row blocks of the locality-ordered copy (rb_spmm.cu): blocks of 4 rows, each
+  // the sorted union of its rows' columns (slots) with a dense 4 x slots panel
+  bool rb_built = false;
+  double rb_patch = 0.0;
+  int64_t rb_blocks = 0;              // row blocks
+  int64_t rb_slots = 0;               // slots stored (padded to multiples of 4 per block)
+  int64_t rb_union = 0;               // slots before padding
+  int rb_max_slots = 0;               // most slots of one block (before padding)
+  int rb_tile_warps = 0;              // tile width (blocks) of rb_tile_max_bytes
+  int64_t rb_tile_max_bytes = 0;      // largest tile of rb_tile_warps blocks (data bytes)
+  leo2d::DevBuf<int64_t> rb_off;      // [blocks + 1 + pad] first slot of each block
+  leo2d::DevBuf<unsigned char> rb_data;  // 20 bytes per slot: columns, then the value panel
 };
 
 namespace leo2d {
@@ -75,4 +87,8 @@ void csr_drop_reordered(leo2d_csr* csr);
 // entries or a row of more than 255 entries.
 bool csr_build_tc(leo2d_ctx* ctx, leo2d_csr* csr);
 void csr_drop_tc(leo2d_csr* csr);
+// Builds the row blocks of the locality-ordered copy; returns false (and builds
+// nothing) when a block of 4 rows has more than 4096 entries or 2048 distinct columns.
+bool csr_build_rb(leo2d_ctx* ctx, leo2d_csr* csr);
+void csr_drop_rb(leo2d_csr* csr);
 }  // namespace leo2d

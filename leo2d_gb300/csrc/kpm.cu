@@ -213,6 +213,11 @@ void enqueue_steps(Recursion& r) {
                        a.prev_partials, a.prev_dots);
         continue;
       }
+      if (r.shape.rb) {
+        rb_launch_step(ctx, r.csr, r.shape, r.grid, r.dyn_smem, a.tn, a.tp, nullptr, a.first, 0.0f, a.partials,
+                       a.prev_partials, a.prev_dots);
+        continue;
+      }
     }
     if (r.shape.tiled) {
       TileArgs<T> ta{};
@@ -243,6 +248,9 @@ struct ShapeKey {
 struct Tuned {
   int rows = 0, warps = 0;
   bool tc = false;  // the tensor-core step won for this block width
+  bool rb = false;  // the row-block step won for this block width
+  int rb_warps = 0, rb_unroll = 0;
+  bool rb_packed = true;
 };
 std::map<std::pair<leo2d_ctx*, ShapeKey>, Tuned> g_shape_cache;
 // best block width per (context, matrix, precision, columns requested)
@@ -261,12 +269,15 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
   LEO_REQUIRE(m->nnz == 0 || (s.fp64 ? m->val64.p != nullptr : m->val32.p != nullptr),
               "matrix has no values");
   leo2d_csr* mm = const_cast<leo2d_csr*>(m);
-  if (shape.tc && !(allow_perm && m->pos.p != nullptr && m->nnz > 0)) shape.tc = false;
-  const bool want_perm = allow_perm && m->pos.p != nullptr && m->nnz > 0 &&
-                         (shape.tc || ctx->reorder == 1 || (ctx->reorder == -1 && n >= 100000));
-  if (want_perm && (!m->reordered || (s.fp64 && !m->reorder_fp64) ||
-                    m->reorder_patch != ctx->reorder_patch))
-    csr_build_reordered(ctx, mm, ctx->reorder_patch, s.fp64 || m->reorder_fp64);
+  const bool can_perm = allow_perm && m->pos.p != nullptr && m->nnz > 0;
+  if (shape.tc && !can_perm) shape.tc = false;
+  if (shape.rb && (!can_perm || s.fp64 || s.cols != 32 || ctx->reorder == 0)) shape.rb = false;
+  if (shape.rb) shape.tc = false;
+  const bool want_perm = can_perm && (shape.tc || shape.rb || ctx->reorder == 1 ||
+                                      (ctx->reorder == -1 && n >= 100000));
+  const double patch = reorder_patch_for(ctx, shape.rb);
+  if (want_perm && (!m->reordered || (s.fp64 && !m->reorder_fp64) || m->reorder_patch != patch))
+    csr_build_reordered(ctx, mm, patch, s.fp64 || m->reorder_fp64);
   use_perm = want_perm;
   if (shape.tc) {
     // tensor-core tiles of the locality-ordered copy (built once per matrix)
@@ -279,7 +290,18 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
       shape.tc = false;  // a tile too wide for the tensor-core step: the gather kernels run
     }
   }
-  if (shape.tiled && !shape.tc) {
+  if (shape.rb) {
+    // row blocks of the locality-ordered copy (built once per matrix)
+    if (!m->rb_built || m->rb_patch != m->reorder_patch) csr_build_rb(ctx, mm);
+    if (m->rb_built && rb_stages(ctx, mm, shape.rb_warps) >= 2) {
+      dyn_smem = rb_smem_bytes(ctx, mm, shape.rb_warps);
+      grid = rb_grid(ctx, m, shape.rb_warps);
+      shape.tiled = false;
+    } else {
+      shape.rb = false;  // blocks too wide for the row-block step: the gather kernels run
+    }
+  }
+  if (shape.tiled && !shape.tc && !shape.rb) {
     const int ns = tile_slots(s.cols, s.fp64, s.warps);
     const int ri = s.rows_per_item > 0 ? s.rows_per_item : std::max(1, 32 / ns);
     tile_rows = ns * ri;
@@ -327,7 +349,7 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
       grid = (unsigned)g;
     }
   }
-  if (!shape.tiled && !shape.tc) {
+  if (!shape.tiled && !shape.tc && !shape.rb) {
     if (shape.rows_per_item <= 0) shape.rows_per_item = 4;
     const int occ = std::max(1, occupancy(s.cols, s.fp64));
     const int lpr = s.cols <= 32 ? s.cols : 32;  // lanes per row slot
@@ -349,7 +371,7 @@ template <typename T>
 void one_step(Recursion& r, const void* in, void* out, const void* prev, bool first, double alpha, int matrix) {
   leo2d_ctx* ctx = r.ctx;
   const int C = r.shape.cols;
-  LEO_REQUIRE(!r.use_perm && !r.shape.tc, "a recursion over dxH needs the unpermuted matrix");
+  LEO_REQUIRE(!r.use_perm && !r.shape.tc && !r.shape.rb, "a recursion over dxH needs the unpermuted matrix");
   StepArgs<T> a;
   a.n = r.n;
   a.rowptr = r.csr->rowptr.p;
@@ -393,7 +415,7 @@ void Recursion::step(const void* in, void* out, const void* prev, bool first, do
 void Recursion::run() {
   if (shape.fp64) enqueue_steps<double>(*this);
   else enqueue_steps<float>(*this);
-  if (shape.tiled || shape.tc) ctx_check_status(ctx, "Chebyshev recursion");
+  if (shape.tiled || shape.tc || shape.rb) ctx_check_status(ctx, "Chebyshev recursion");
 }
 
 Recursion::~Recursion() {
@@ -427,6 +449,16 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
   const bool tc_ok = !fp64 && (s.cols == 32 || s.cols == 64);
   s.tc = tc_ok && (ctx->kernel_variant == 2 ||
                    (ctx->kernel_variant == -1 && it != g_shape_cache.end() && it->second.tc));
+  // the row-block step: when asked for, when the autotuner chose it, and by
+  // default where the matrix is large enough to be locality-ordered
+  const bool rb_ok = !fp64 && s.cols == 32 && ctx->reorder != 0 && csr->pos.p != nullptr && csr->nnz > 0;
+  const bool cached = it != g_shape_cache.end();
+  if (ctx->kernel_variant == 3) s.rb = rb_ok;
+  else if (ctx->kernel_variant == -1) s.rb = rb_ok && (cached ? it->second.rb : (ctx->reorder == 1 || csr->n >= 100000));
+  if (s.rb) s.tc = false;
+  s.rb_warps = ctx->rb_warps > 0 ? ctx->rb_warps : (cached && it->second.rb_warps > 0 ? it->second.rb_warps : 24);
+  s.rb_unroll = ctx->rb_unroll > 0 ? ctx->rb_unroll : (cached && it->second.rb_unroll > 0 ? it->second.rb_unroll : 8);
+  s.rb_packed = ctx->rb_packed >= 0 ? ctx->rb_packed != 0 : (cached ? it->second.rb_packed : true);
   LEO_REQUIRE(s.rows_per_item >= 0 && s.rows_per_item <= 64, "rows_per_warp must be 0..64");
   return s;
 }
@@ -631,6 +663,7 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
           sh.rows_per_item = rows;
           sh.warps = warps;
           sh.tc = false;
+          sh.rb = false;
           Recursion r;
           r.setup(ctx, csr, sh, steps);
           fill_phase(ctx, r, 1, 0, cols / 2);
@@ -652,6 +685,7 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
       if (!fp64 && (cols == 32 || cols == 64) && ctx->kernel_variant != 0 && ctx->kernel_variant != 1) {
         StepShape sh = choose_shape(ctx, csr, fp64, cols, cols, 0);
         sh.tc = true;
+        sh.rb = false;
         Recursion r;
         r.setup(ctx, csr, sh, steps);
         if (r.shape.tc) {
@@ -666,6 +700,38 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
           if (per < best_c) {
             best_c = per;
             best_t.tc = true;
+          }
+        }
+      }
+      // the row-block step where it applies: a few block shapes
+      if (!fp64 && cols == 32 && ctx->kernel_variant != 0 && ctx->kernel_variant != 1 &&
+          ctx->kernel_variant != 2 && ctx->reorder != 0) {
+        struct RbTry { int warps, unroll; bool packed; };
+        for (const RbTry t : {RbTry{24, 8, true}, RbTry{32, 4, true}, RbTry{24, 8, false}, RbTry{16, 8, true}}) {
+          StepShape sh = choose_shape(ctx, csr, fp64, cols, cols, 0);
+          sh.tc = false;
+          sh.rb = true;
+          sh.rb_warps = ctx->rb_warps > 0 ? ctx->rb_warps : t.warps;
+          sh.rb_unroll = ctx->rb_unroll > 0 ? ctx->rb_unroll : t.unroll;
+          sh.rb_packed = ctx->rb_packed >= 0 ? ctx->rb_packed != 0 : t.packed;
+          Recursion r;
+          r.setup(ctx, csr, sh, steps);
+          if (!r.shape.rb) break;
+          fill_phase(ctx, r, 1, 0, cols / 2);
+          r.run();  // warm
+          ctx_sync(ctx);
+          const auto before = ctx->stats["cheb_step"];
+          r.run();
+          ctx_sync(ctx);
+          const auto after = ctx->stats["cheb_step"];
+          const double per = (after.ms - before.ms) / std::max<int64_t>(1, after.launches - before.launches);
+          if (per < best_c) {
+            best_c = per;
+            best_t.tc = false;
+            best_t.rb = true;
+            best_t.rb_warps = sh.rb_warps;
+            best_t.rb_unroll = sh.rb_unroll;
+            best_t.rb_packed = sh.rb_packed;
           }
         }
       }

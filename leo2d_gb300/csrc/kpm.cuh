@@ -14,6 +14,10 @@ struct StepShape {
   bool tiled = true;       // bulk-copy tiled kernel (else the register-streaming kernel)
   int warps = 8;           // warps per block of the tiled kernel (8 or 24)
   bool tc = false;         // tensor-core step (tc_spmm.cu) over the locality-ordered tiles
+  bool rb = false;         // row-block step (rb_spmm.cu) over the locality-ordered copy (FP32, 32 columns)
+  int rb_warps = 24;       // row-block step: warps per block = row blocks per tile (16, 24, 32)
+  bool rb_packed = true;   // row-block step: paired FP32 FMAs
+  int rb_unroll = 8;       // row-block step: slot batches in flight per lane (4, 8)
 };
 
 // Vector block resident on the device: two buffers of n x cols (T_k, T_{k-1}).
@@ -52,6 +56,22 @@ size_t tc_smem_bytes(const leo2d_csr* csr, int cols);
 void tc_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, int cols, unsigned grid, size_t smem, const float* tn,
                     float* tp, const float* tprev, int first, float alpha, double* partials,
                     const double* prev_partials, double* prev_dots);
+
+// The row-block step (rb_spmm.cu): shared-memory stages that fit (0: none),
+// dynamic shared memory, grid, and one launch.
+int rb_stages(leo2d_ctx* ctx, leo2d_csr* csr, int warps);
+size_t rb_smem_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps);
+unsigned rb_grid(leo2d_ctx* ctx, const leo2d_csr* csr, int warps);
+void rb_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape, unsigned grid, size_t smem,
+                    const float* tn, float* tp, const float* tprev, int first, float alpha, double* partials,
+                    const double* prev_partials, double* prev_dots);
+
+// Patch edge (A) of the locality ordering for a step kernel: the context's
+// setting, else 32 A for the row-block step (larger blocks of neighbours, fewer
+// slots) and 16 A for the gather kernels (smaller gathered working set).
+inline double reorder_patch_for(const leo2d_ctx* ctx, bool row_blocks) {
+  return ctx->reorder_patch > 0.0 ? ctx->reorder_patch : (row_blocks ? 32.0 : 16.0);
+}
 
 // Chooses the shape for a matrix; cached per context and matrix.
 StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols_needed,

@@ -159,6 +159,7 @@ namespace leo2d {
 
 void csr_build_reordered(leo2d_ctx* ctx, leo2d_csr* csr, double patch, bool with_fp64) {
   csr_drop_tc(csr);
+  csr_drop_rb(csr);
   const int64_t n = csr->n;
   LEO_REQUIRE(csr->pos.p, "locality ordering needs orbital positions");
   LEO_REQUIRE(patch > 0.5, "patch size must exceed 0.5 A");
@@ -240,6 +241,7 @@ void csr_build_reordered(leo2d_ctx* ctx, leo2d_csr* csr, double patch, bool with
 
 void csr_drop_reordered(leo2d_csr* csr) {
   csr_drop_tc(csr);
+  csr_drop_rb(csr);
   csr->reordered = false;
   csr->reorder_fp64 = false;
   csr->new2old.release();

@@ -124,9 +124,17 @@ __global__ void __launch_bounds__(kThreads, 3) k_cheb_step(const StepArgs<T> a) 
   const T alpha = a.alpha != T(0) ? a.alpha : (a.first ? T(1) : T(2));
   const T* tprev = a.tprev ? a.tprev : a.tp;
 
+  // dots: T within a work item, then T over kDotFlush items, then FP64 (see
+  // tile_body)
+  constexpr int kDotFlush = std::is_same<T, float>::value ? 16 : 1;
   double d0[V], d1[V];
+  T e0[V], e1[V];
+  int since_flush = 0;
 #pragma unroll
-  for (int v = 0; v < V; ++v) d0[v] = d1[v] = 0.0;
+  for (int v = 0; v < V; ++v) {
+    d0[v] = d1[v] = 0.0;
+    e0[v] = e1[v] = T(0);
+  }
 
   for (int64_t item = (int64_t)blockIdx.x * kWarps + warp; item < n_items; item += warps_total) {
     Acc f0[V], f1[V];
@@ -195,9 +203,23 @@ __global__ void __launch_bounds__(kThreads, 3) k_cheb_step(const StepArgs<T> a) 
     }
 #pragma unroll
     for (int v = 0; v < V; ++v) {
-      d0[v] += (double)f0[v];
-      d1[v] += (double)f1[v];
+      e0[v] += f0[v];
+      e1[v] += f1[v];
     }
+    if (++since_flush == kDotFlush) {  // warp-uniform
+      since_flush = 0;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        d0[v] += (double)e0[v];
+        d1[v] += (double)e1[v];
+        e0[v] = e1[v] = T(0);
+      }
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    d0[v] += (double)e0[v];
+    d1[v] += (double)e1[v];
   }
 
   // combine the row slots of the warp (lanes with equal `sub`)
@@ -386,9 +408,18 @@ __device__ __forceinline__ void tile_body(const TileArgs<T>& ta, const int bid, 
   const int gslot = warp * RPW + slot;
   const T alpha = a.alpha != T(0) ? a.alpha : (a.first ? T(1) : T(2));
   const T* tprev = a.tprev ? a.tprev : a.tp;
+  // dots: T within a tile, then T over kDotFlush tiles, then FP64 (in FP32 mode
+  // the FP64 pipe is a small fraction of the FP32 one: converting every tile's
+  // partials would bound the kernel)
+  constexpr int kDotFlush = std::is_same<T, float>::value ? 16 : 1;
   double d0[V], d1[V];
+  T e0[V], e1[V];
+  int since_flush = 0;
 #pragma unroll
-  for (int v = 0; v < V; ++v) d0[v] = d1[v] = 0.0;
+  for (int v = 0; v < V; ++v) {
+    d0[v] = d1[v] = 0.0;
+    e0[v] = e1[v] = T(0);
+  }
 
   bool gave_up = false;
   if (ta.never_wait && !bounded_wait(&never, 0u, ta.spin_limit)) {
@@ -482,8 +513,17 @@ __device__ __forceinline__ void tile_body(const TileArgs<T>& ta, const int bid, 
     }
 #pragma unroll
     for (int v = 0; v < V; ++v) {
-      d0[v] += (double)f0[v];
-      d1[v] += (double)f1[v];
+      e0[v] += f0[v];
+      e1[v] += f1[v];
+    }
+    if (++since_flush == kDotFlush) {  // warp-uniform
+      since_flush = 0;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        d0[v] += (double)e0[v];
+        d1[v] += (double)e1[v];
+        e0[v] = e1[v] = T(0);
+      }
     }
     // release the stage; the last warp refills it
     __syncwarp();
@@ -505,6 +545,11 @@ __device__ __forceinline__ void tile_body(const TileArgs<T>& ta, const int bid, 
     for (int i = 0; i < nst; ++i)
       if (issued[i] > 0) bounded_wait(&full[i], (uint32_t)(issued[i] - 1) & 1u, ~0ull);
 
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    d0[v] += (double)e0[v];
+    d1[v] += (double)e1[v];
+  }
 #pragma unroll
   for (int o = LPR; o < 32; o <<= 1)
 #pragma unroll

@@ -369,9 +369,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cheb_tc(const TcArgs a) {
   const float alpha = a.alpha != 0.0f ? a.alpha : (a.first ? 1.0f : 2.0f);
   const float* tprev = a.tprev ? a.tprev : a.tp;
   const int64_t tiles = (a.n + kTcRows - 1) / kTcRows;
+  // dots: FP32 over kDotFlush tiles (one row each), then FP64 (the FP64 pipe is
+  // a small fraction of the FP32 one)
+  constexpr int kDotFlush = 16;
   double d0[CH], d1[CH];
+  float e0[CH], e1[CH];
+  int since_flush = 0;
 #pragma unroll
-  for (int j = 0; j < CH; ++j) d0[j] = d1[j] = 0.0;
+  for (int j = 0; j < CH; ++j) {
+    d0[j] = d1[j] = 0.0;
+    e0[j] = e1[j] = 0.f;
+  }
   uint32_t chunk_ctr = 0;  // chunks issued by this block (stage = ctr & 1)
   uint32_t loads = 0;      // tile stagings issued (load_bar phases)
   int local = 0;           // tiles finished (tile_bar phases)
@@ -535,10 +543,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cheb_tc(const TcArgs a) {
         const float4 y = make_float4(alpha * v[c0] - p.x, alpha * v[c0 + 1] - p.y, alpha * v[c0 + 2] - p.z,
                                      alpha * v[c0 + 3] - p.w);
         *reinterpret_cast<float4*>(a.tp + off + c0) = y;
-        d0[c0] += (double)(x.x * x.x); d1[c0] += (double)(y.x * x.x);
-        d0[c0 + 1] += (double)(x.y * x.y); d1[c0 + 1] += (double)(y.y * x.y);
-        d0[c0 + 2] += (double)(x.z * x.z); d1[c0 + 2] += (double)(y.z * x.z);
-        d0[c0 + 3] += (double)(x.w * x.w); d1[c0 + 3] += (double)(y.w * x.w);
+        e0[c0] += x.x * x.x; e1[c0] += y.x * x.x;
+        e0[c0 + 1] += x.y * x.y; e1[c0 + 1] += y.y * x.y;
+        e0[c0 + 2] += x.z * x.z; e1[c0 + 2] += y.z * x.z;
+        e0[c0 + 3] += x.w * x.w; e1[c0 + 3] += y.w * x.w;
+      }
+    }
+    if (++since_flush == kDotFlush) {  // block-uniform
+      since_flush = 0;
+#pragma unroll
+      for (int j = 0; j < CH; ++j) {
+        d0[j] += (double)e0[j];
+        d1[j] += (double)e1[j];
+        e0[j] = e1[j] = 0.f;
       }
     }
     umma::fence_before_sync();
@@ -553,6 +570,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cheb_tc(const TcArgs a) {
     if (failed && loads > 0) umma::bar_wait(&load_bar, (loads - 1) & 1u);
   }
   if (tid == 0 && failed) atomicExch(a.status, kStatusTimeout);
+#pragma unroll
+  for (int j = 0; j < CH; ++j) {
+    d0[j] += (double)e0[j];
+    d1[j] += (double)e1[j];
+  }
   // block partials: rows (lanes) of each warp by shuffles, then the 4 warps of
   // each column half in order
 #pragma unroll

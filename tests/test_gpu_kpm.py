@@ -75,7 +75,7 @@ def _with_options(ctx, opts, fn):
         return fn()
     finally:
         for k, v in {"step_kernel": -1, "reorder": -1, "tile_warps": 0, "tile_chunk": 4,
-                     "tile_stages": 2}.items():
+                     "tile_stages": 2, "reorder_patch_dA": 0}.items():
             ctx.set_option(k, v)
 
 
