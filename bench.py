@@ -208,7 +208,8 @@ def kernel_case(args):
         gbs = step_bytes(csr.n, nnz_true, args.kernel_case) / (ms / k * 1e-3) / 1e9
         print(json.dumps({"kernel_case": {"n": csr.n, "nnz": csr.nnz, "cols": args.kernel_case,
                                           "step_kernel": args.step_kernel, "radius_A": radius,
-                                          "tc_tiles": list(csr.tc_info()),
+                                          "step_kernel_run": csr.step_kernel(cfg)[0],
+                                          "rb_info": list(csr.rb_info()),
                                           "step_ms": round(ms / k, 4), "step_gbs": round(gbs, 1)}}))
 
 
@@ -617,9 +618,9 @@ def main():
                          "1.05 deg (31,32) supercell, P=4096, 64 vectors, FP32 vs FP64 per energy; kubo2m: "
                          "sigma_xx(E) of a 2M-orbital 1.5 deg flake, 512x512 moments, 32 vectors; mlp: the "
                          "control variate's network (training steps, inference over the flake of --radius)")
-    ap.add_argument("--step-kernel", type=int, default=-1, choices=[-1, 0, 1, 2],
-                    help="force the Chebyshev step kernel: 0 tiled gathers, 1 register gathers, 2 tensor cores "
-                         "(default: the autotuner's choice)")
+    ap.add_argument("--step-kernel", type=int, default=-1, choices=[-1, 0, 1, 2, 3],
+                    help="force the Chebyshev step kernel: 0 tiled gathers, 1 register gathers, 2 tensor cores, "
+                         "3 row blocks (default: the autotuner's choice)")
     ap.add_argument("--kernel-case", type=int, default=0, metavar="COLS",
                     help="profiling case: two short DOS runs (P=16) of COLS-wide vector blocks on the flake "
                          "of --radius (1000 A: 2.4M orbitals), then exit; prints no bench line")
@@ -645,6 +646,8 @@ def main():
 
     import leo2d_gb300 as L
     ctx = L.Context(local)
+    if args.step_kernel >= 0:
+        ctx.set_option("step_kernel", args.step_kernel)
     g = ctx.prepare(geom(L, radius=args.radius))
     t0 = time.perf_counter()
     csr = ctx.build_csr(g)
@@ -683,8 +686,11 @@ def main():
     first, count = vector_share(R_needed, rank, ws)
     cfg = L.kpm_cfg(P, R=max(count, 1), seed=7, first_vector=first)
     t_tune = time.perf_counter()
-    cols, rows = csr.autotune(cfg)  # untimed: picks block width, rows per slot, warps
+    cols, rows = csr.autotune(cfg)  # untimed: picks the step kernel, block width and its shape
     t_tune = time.perf_counter() - t_tune
+    kernel_id, _ = csr.step_kernel(cfg)
+    kernel_name = {0: "k_cheb_tile (tiled CSR gathers)", 1: "k_cheb_step (register gathers)",
+                   2: "k_cheb_tc (tensor cores)", 3: "k_cheb_rb (row blocks)"}[kernel_id]
 
     import torch
     torch.cuda.set_device(local)
@@ -748,12 +754,12 @@ def main():
     achieved = bytes_step / (k_ms / k_n / 1000.0) / 1e9 if k_n else None
     # DRAM bytes per launch from the committed ncu capture of the same kernel on
     # a 2.4M-orbital flake, scaled to this launch by the algorithmic bytes
-    # (traffic grows with rows and entries; the capture's ratio is 0.995)
+    # (traffic grows with rows and entries)
     traffic = None
     tp = os.path.join(REPO, "profiles", "cheb_step_traffic.json")
     if os.path.exists(tp):
         try:
-            t = json.load(open(tp))
+            t = json.load(open(tp))[{0: "tiled", 3: "row_blocks"}[kernel_id]]
             traffic = int(bytes_step * t["dram_bytes_per_launch"] / t["algorithmic_bytes_per_launch"])
         except (OSError, ValueError, KeyError, ZeroDivisionError):
             traffic = None
@@ -777,7 +783,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4) if achieved else None, "traffic": traffic,
-                     "kernel": "cheb_step", "bytes_per_launch": bytes_step,
+                     "kernel": kernel_name, "bytes_per_launch": bytes_step,
                      "launch_ms": round(k_ms / k_n, 4) if k_n else None,
                      "peak_kind": peak_kind},
         "clocks": clk.summary(),

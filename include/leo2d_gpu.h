@@ -204,6 +204,12 @@ leo2d_status leo2d_kpm_ldos(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kp
  * them. No counterpart in the reference (its SpMV has no tunable shape). */
 leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg,
                                 int32_t* block_out, int32_t* rows_out);
+/* The step kernel a leo2d_kpm_dos call with this cfg would run on this matrix:
+ * *kernel = 0 tiled CSR gathers, 1 register-streaming gathers, 2 tensor cores,
+ * 3 row blocks; *block = the vector-block width in columns. Builds nothing and
+ * launches nothing. No counterpart in the reference. */
+leo2d_status leo2d_kpm_step_kernel(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg,
+                                   int32_t* kernel, int32_t* block);
 
 /* Param_tools::densityTransform (param_tools.cpp:661-705) for one moment set, or
  * densityTransformTrace (707-768) when num_sets > 1 (mean over sets first):

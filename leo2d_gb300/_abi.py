@@ -131,6 +131,7 @@ def _declare(lib):
     fn("leo2d_kpm_dos", c_i32, c_void_p, c_void_p, cp, P, P)
     fn("leo2d_kpm_ldos", c_i32, c_void_p, c_void_p, cp, P, c_i64, P)
     fn("leo2d_kpm_autotune", c_i32, c_void_p, c_void_p, cp, P, P)
+    fn("leo2d_kpm_step_kernel", c_i32, c_void_p, c_void_p, cp, P, P)
     fn("leo2d_dos_transform", c_i32, c_void_p, P, c_i32, c_i32, c_dbl, c_dbl, c_dbl, P, P)
     fn("leo2d_dos_reconstruct", c_i32, c_void_p, P, c_i32, P, c_i64, c_dbl, c_dbl, c_dbl, P)
     fn("leo2d_batch_create", c_i32, c_void_p, P, c_i32, cp, pp)

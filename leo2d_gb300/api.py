@@ -264,6 +264,14 @@ class Csr:
                                                      num_sites, site_seed, _p(w), _p(mu), _p(pt)))
         return (mu, pt) if parts else mu
 
+    def step_kernel(self, cfg):
+        """(kernel, block): the step kernel a kpm_dos call with cfg runs (0 tiled, 1 register,
+        2 tensor cores, 3 row blocks) and its vector-block width."""
+        k, b = ctypes.c_int32(), ctypes.c_int32()
+        self.ctx.check(self.ctx.lib.leo2d_kpm_step_kernel(self.ctx.h, self.h, ctypes.byref(cfg),
+                                                          ctypes.byref(k), ctypes.byref(b)))
+        return k.value, b.value
+
     def autotune(self, cfg):
         b, r = ctypes.c_int32(), ctypes.c_int32()
         self.ctx.check(self.ctx.lib.leo2d_kpm_autotune(self.ctx.h, self.h, ctypes.byref(cfg),

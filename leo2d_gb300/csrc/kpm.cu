@@ -750,6 +750,23 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
   });
 }
 
+extern "C" leo2d_status leo2d_kpm_step_kernel(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg,
+                                              int32_t* kernel, int32_t* block) {
+  if (!ctx || !csr || !cfg || !kernel || !block) return LEO2D_ERR_BAD_ARG;
+  return guard(ctx, [&] {
+    validate_cfg(cfg);
+    const bool fp64 = cfg->precision == LEO2D_FP64;
+    const int group = cfg->vector_kind == LEO2D_VEC_PHASE ? 2 : 1;
+    StepShape s = choose_shape(ctx, csr, fp64, std::max(1, cfg->num_vectors) * group, cfg->block, cfg->rows_per_warp);
+    // the demotions Recursion::setup applies before any build
+    const bool can_perm = csr->pos.p != nullptr && csr->nnz > 0;
+    if (s.rb && (!can_perm || s.fp64 || s.cols != 32 || ctx->reorder == 0)) s.rb = false;
+    if (s.tc && !can_perm) s.tc = false;
+    *kernel = s.rb ? 3 : s.tc ? 2 : s.tiled ? 0 : 1;
+    *block = s.cols;
+  });
+}
+
 // ---------------------------------------------------------------- allocation-free entry point
 //
 // leo2d_kpm_dos_noalloc: the trace recursion of leo2d_kpm_dos for callers that
