@@ -690,7 +690,8 @@ def main():
     t_tune = time.perf_counter() - t_tune
     kernel_id, _ = csr.step_kernel(cfg)
     kernel_name = {0: "k_cheb_tile (tiled CSR gathers)", 1: "k_cheb_step (register gathers)",
-                   2: "k_cheb_tc (tensor cores)", 3: "k_cheb_rb (row blocks)"}[kernel_id]
+                   2: "k_cheb_tc (tensor cores)", 3: "k_cheb_rb (row blocks)",
+                   4: "k_cheb_rbw (row blocks, shared-memory windows)"}[kernel_id]
 
     import torch
     torch.cuda.set_device(local)
@@ -759,7 +760,7 @@ def main():
     tp = os.path.join(REPO, "profiles", "cheb_step_traffic.json")
     if os.path.exists(tp):
         try:
-            t = json.load(open(tp))[{0: "tiled", 3: "row_blocks"}[kernel_id]]
+            t = json.load(open(tp))[{0: "tiled", 3: "row_blocks", 4: "row_blocks_windows"}[kernel_id]]
             traffic = int(bytes_step * t["dram_bytes_per_launch"] / t["algorithmic_bytes_per_launch"])
         except (OSError, ValueError, KeyError, ZeroDivisionError):
             traffic = None

@@ -206,7 +206,8 @@ leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2
                                 int32_t* block_out, int32_t* rows_out);
 /* The step kernel a leo2d_kpm_dos call with this cfg would run on this matrix:
  * *kernel = 0 tiled CSR gathers, 1 register-streaming gathers, 2 tensor cores,
- * 3 row blocks; *block = the vector-block width in columns. Builds nothing and
+ * 3 row blocks, 4 row blocks over shared-memory windows; *block = the
+ * vector-block width in columns. Builds nothing and
  * launches nothing. No counterpart in the reference. */
 leo2d_status leo2d_kpm_step_kernel(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg,
                                    int32_t* kernel, int32_t* block);

@@ -102,6 +102,7 @@ struct leo2d_ctx {
   int rb_packed = -1;         // row-block step: paired FP32 FMAs (fma.rn.f32x2): -1 autotuned, 0 no, 1 yes
   int rb_warps = 0;           // row-block step: warps per block (= row blocks per tile): 0 autotuned, 16, 24, 32
   int rb_unroll = 0;          // row-block step: slot batches in flight per lane: 0 autotuned, 4, 8
+  int rb_window = -1;         // row-block step over shared-memory windows: -1 autotuned, 0 no, 1 yes
   int tile_stages = 2;        // shared-memory stages of the tiled kernel
   int test_unsatisfied_wait = 0;  // test hook: tiled steps first wait on a barrier nobody completes
   bool tc_gemm_ready = false;     // shared-memory attributes of the tensor-core GEMM set on this device

@@ -292,8 +292,11 @@ leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value
     } else if (k == "rb_warps") {
       LEO_REQUIRE(value == 0 || value == 16 || value == 24 || value == 32, "rb_warps must be 0, 16, 24 or 32");
       ctx->rb_warps = (int)value;
+    } else if (k == "rb_window") {
+      LEO_REQUIRE(value >= -1 && value <= 1, "rb_window must be -1 (autotuned), 0 or 1");
+      ctx->rb_window = (int)value;
     } else if (k == "rb_unroll") {
-      LEO_REQUIRE(value == 0 || value == 4 || value == 8, "rb_unroll must be 0, 4 or 8");
+      LEO_REQUIRE(value == 0 || value == 4 || value == 8, "rb_unroll must be 0 (autotuned), 4 or 8");
       ctx->rb_unroll = (int)value;
     } else if (k == "test_unsatisfied_wait") {
       // every tiled step waits on an mbarrier that never completes, gives up

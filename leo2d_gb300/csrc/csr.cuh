@@ -69,6 +69,18 @@ struct leo2d_csr {
   int64_t rb_tile_max_bytes = 0;      // largest tile of rb_tile_warps blocks (data bytes)
   leo2d::DevBuf<int64_t> rb_off;      // [blocks + 1 + pad] first slot of each block
   leo2d::DevBuf<unsigned char> rb_data;  // 20 bytes per slot: columns, then the value panel
+  // shared-memory windows of the row blocks (rbw_spmm.cu): per tile of 16 blocks
+  // the sorted distinct columns of its slots; slots hold window positions
+  bool rbw_built = false;
+  int64_t rbw_tiles = 0;
+  int rbw_max_win = 0;                // widest window (rows)
+  int64_t rbw_win_rows = 0;           // window rows over all tiles
+  int64_t rbw_tile_max_bytes = 0;     // largest tile's slots (bytes)
+  int64_t rbw_runs_total = 0;         // runs over all tiles
+  leo2d::DevBuf<int64_t> rbw_roff;    // [tiles + 1] first run of each tile
+  leo2d::DevBuf<int32_t> rbw_runs;    // (first column, rows) per run
+  leo2d::DevBuf<int32_t> rbw_wrows;   // [tiles] window rows
+  leo2d::DevBuf<unsigned char> rbw_data;  // rb_data with window positions over the columns
 };
 
 namespace leo2d {
@@ -91,4 +103,10 @@ void csr_drop_tc(leo2d_csr* csr);
 // nothing) when a block of 4 rows has more than 4096 entries or 2048 distinct columns.
 bool csr_build_rb(leo2d_ctx* ctx, leo2d_csr* csr);
 void csr_drop_rb(leo2d_csr* csr);
+// Largest data bytes of a tile of `tile` consecutive row blocks.
+int64_t rb_tile_max_bytes(leo2d_ctx* ctx, const leo2d_csr* csr, int tile);
+// Builds the shared-memory windows of the row blocks; returns false (and builds
+// nothing) when a tile of 16 blocks has more than 8192 slots or 2048 distinct columns.
+bool csr_build_rbw(leo2d_ctx* ctx, leo2d_csr* csr);
+void csr_drop_rbw(leo2d_csr* csr);
 }  // namespace leo2d

@@ -213,6 +213,11 @@ void enqueue_steps(Recursion& r) {
                        a.prev_partials, a.prev_dots);
         continue;
       }
+      if (r.shape.rb && r.shape.rb_window) {
+        rbw_launch_step(ctx, r.csr, r.shape, r.grid, r.dyn_smem, a.tn, a.tp, nullptr, a.first, 0.0f, a.partials,
+                        a.prev_partials, a.prev_dots);
+        continue;
+      }
       if (r.shape.rb) {
         rb_launch_step(ctx, r.csr, r.shape, r.grid, r.dyn_smem, a.tn, a.tp, nullptr, a.first, 0.0f, a.partials,
                        a.prev_partials, a.prev_dots);
@@ -251,6 +256,7 @@ struct Tuned {
   bool rb = false;  // the row-block step won for this block width
   int rb_warps = 0, rb_unroll = 0;
   bool rb_packed = true;
+  bool rb_window = false;
 };
 std::map<std::pair<leo2d_ctx*, ShapeKey>, Tuned> g_shape_cache;
 // best block width per (context, matrix, precision, columns requested)
@@ -293,7 +299,13 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
   if (shape.rb) {
     // row blocks of the locality-ordered copy (built once per matrix)
     if (!m->rb_built || m->rb_patch != m->reorder_patch) csr_build_rb(ctx, mm);
-    if (m->rb_built && rb_stages(ctx, mm, shape.rb_warps) >= 2) {
+    if (shape.rb_window && m->rb_built && !m->rbw_built) csr_build_rbw(ctx, mm);
+    if (shape.rb_window && !(m->rbw_built && rbw_stages(ctx, mm) >= 2)) shape.rb_window = false;
+    if (shape.rb_window) {
+      dyn_smem = rbw_smem_bytes(ctx, mm);
+      grid = rbw_grid(ctx, m);
+      shape.tiled = false;
+    } else if (m->rb_built && rb_stages(ctx, mm, shape.rb_warps) >= 2) {
       dyn_smem = rb_smem_bytes(ctx, mm, shape.rb_warps);
       grid = rb_grid(ctx, m, shape.rb_warps);
       shape.tiled = false;
@@ -459,6 +471,7 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
   s.rb_warps = ctx->rb_warps > 0 ? ctx->rb_warps : (cached && it->second.rb_warps > 0 ? it->second.rb_warps : 24);
   s.rb_unroll = ctx->rb_unroll > 0 ? ctx->rb_unroll : (cached && it->second.rb_unroll > 0 ? it->second.rb_unroll : 8);
   s.rb_packed = ctx->rb_packed >= 0 ? ctx->rb_packed != 0 : (cached ? it->second.rb_packed : true);
+  s.rb_window = ctx->rb_window >= 0 ? ctx->rb_window != 0 : (cached ? it->second.rb_window : false);
   LEO_REQUIRE(s.rows_per_item >= 0 && s.rows_per_item <= 64, "rows_per_warp must be 0..64");
   return s;
 }
@@ -706,17 +719,23 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
       // the row-block step where it applies: a few block shapes
       if (!fp64 && cols == 32 && ctx->kernel_variant != 0 && ctx->kernel_variant != 1 &&
           ctx->kernel_variant != 2 && ctx->reorder != 0) {
-        struct RbTry { int warps, unroll; bool packed; };
-        for (const RbTry t : {RbTry{24, 8, true}, RbTry{32, 4, true}, RbTry{24, 8, false}, RbTry{16, 8, true}}) {
+        struct RbTry { int warps, unroll; bool packed, window; };
+        // (the windowed form is timed only when asked for: it measured slower on
+        // twisted-bilayer flakes and builds a second copy of the blocks)
+        for (const RbTry t : {RbTry{24, 8, true, false}, RbTry{32, 4, true, false}, RbTry{24, 8, false, false},
+                              RbTry{16, 8, true, false}, RbTry{16, 4, true, true}}) {
+          if ((ctx->rb_window == 1) != t.window) continue;
           StepShape sh = choose_shape(ctx, csr, fp64, cols, cols, 0);
           sh.tc = false;
           sh.rb = true;
           sh.rb_warps = ctx->rb_warps > 0 ? ctx->rb_warps : t.warps;
           sh.rb_unroll = ctx->rb_unroll > 0 ? ctx->rb_unroll : t.unroll;
           sh.rb_packed = ctx->rb_packed >= 0 ? ctx->rb_packed != 0 : t.packed;
+          sh.rb_window = t.window;
           Recursion r;
           r.setup(ctx, csr, sh, steps);
           if (!r.shape.rb) break;
+          if (r.shape.rb_window != t.window) continue;
           fill_phase(ctx, r, 1, 0, cols / 2);
           r.run();  // warm
           ctx_sync(ctx);
@@ -732,6 +751,7 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
             best_t.rb_warps = sh.rb_warps;
             best_t.rb_unroll = sh.rb_unroll;
             best_t.rb_packed = sh.rb_packed;
+            best_t.rb_window = sh.rb_window;
           }
         }
       }
@@ -762,7 +782,7 @@ extern "C" leo2d_status leo2d_kpm_step_kernel(leo2d_ctx* ctx, const leo2d_csr* c
     const bool can_perm = csr->pos.p != nullptr && csr->nnz > 0;
     if (s.rb && (!can_perm || s.fp64 || s.cols != 32 || ctx->reorder == 0)) s.rb = false;
     if (s.tc && !can_perm) s.tc = false;
-    *kernel = s.rb ? 3 : s.tc ? 2 : s.tiled ? 0 : 1;
+    *kernel = s.rb ? (s.rb_window ? 4 : 3) : s.tc ? 2 : s.tiled ? 0 : 1;
     *block = s.cols;
   });
 }

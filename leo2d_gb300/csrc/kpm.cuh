@@ -18,6 +18,7 @@ struct StepShape {
   int rb_warps = 24;       // row-block step: warps per block = row blocks per tile (16, 24, 32)
   bool rb_packed = true;   // row-block step: paired FP32 FMAs
   int rb_unroll = 8;       // row-block step: slot batches in flight per lane (4, 8)
+  bool rb_window = false;  // row-block step over shared-memory windows (rbw_spmm.cu)
 };
 
 // Vector block resident on the device: two buffers of n x cols (T_k, T_{k-1}).
@@ -65,6 +66,14 @@ unsigned rb_grid(leo2d_ctx* ctx, const leo2d_csr* csr, int warps);
 void rb_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape, unsigned grid, size_t smem,
                     const float* tn, float* tp, const float* tprev, int first, float alpha, double* partials,
                     const double* prev_partials, double* prev_dots);
+
+// The windowed row-block step (rbw_spmm.cu), as above.
+int rbw_stages(leo2d_ctx* ctx, leo2d_csr* csr);
+size_t rbw_smem_bytes(leo2d_ctx* ctx, leo2d_csr* csr);
+unsigned rbw_grid(leo2d_ctx* ctx, const leo2d_csr* csr);
+void rbw_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape, unsigned grid, size_t smem,
+                     const float* tn, float* tp, const float* tprev, int first, float alpha, double* partials,
+                     const double* prev_partials, double* prev_dots);
 
 // Patch edge (A) of the locality ordering for a step kernel: the context's
 // setting, else 32 A for the row-block step (larger blocks of neighbours, fewer

@@ -45,8 +45,8 @@ using namespace leo2d;
 
 namespace {
 
-constexpr int kRbRows = 4;          // rows per row block
-constexpr int kRbSlotBytes = 20;    // 4 (column) + 4 x 4 (values)
+#include "rb_common.cuh"
+
 constexpr int kRbBuildThreads = 256;
 constexpr int kRbMaxEnt = 4096;     // stored entries of one row block (build limit)
 constexpr int kRbMaxSlots = 2048;   // slots of one row block (build limit)
@@ -73,83 +73,6 @@ struct RbArgs {
   int* status;
   int never_wait;  // test hook: wait on a barrier that nobody completes
 };
-
-__device__ __forceinline__ unsigned long long pack2(float lo, float hi) {
-  unsigned long long r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ float2 unpack2(unsigned long long r) {
-  float2 f;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(f.x), "=f"(f.y) : "l"(r));
-  return f;
-}
-// acc += a * b on two FP32 lanes at once
-__device__ __forceinline__ void fma2(unsigned long long& acc, unsigned long long a, unsigned long long b) {
-  asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc) : "l"(a), "l"(b));
-}
-
-// A lane's share of one slot: rows 0..3 of the block += v[r] * x over its 4 columns.
-template <bool PACKED>
-struct PanelAcc;
-template <>
-struct PanelAcc<false> {
-  float a[4][4];
-  __device__ __forceinline__ void zero() {
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) a[r][c] = 0.f;
-  }
-  __device__ __forceinline__ void add(const float4& x, const float4& v) {
-    const float w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      a[r][0] += w[r] * x.x;
-      a[r][1] += w[r] * x.y;
-      a[r][2] += w[r] * x.z;
-      a[r][3] += w[r] * x.w;
-    }
-  }
-  __device__ __forceinline__ void get(float (&o)[4][4]) const {
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) o[r][c] = a[r][c];
-  }
-};
-// Pairs of rows (0,1), (2,3) per column: the value pairs come straight from the
-// 16-byte load, each column of x is duplicated once per slot.
-template <>
-struct PanelAcc<true> {
-  unsigned long long a[2][4];
-  __device__ __forceinline__ void zero() {
-#pragma unroll
-    for (int p = 0; p < 2; ++p)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) a[p][c] = 0ull;
-  }
-  __device__ __forceinline__ void add(const float4& x, const float4& v) {
-    const unsigned long long v01 = pack2(v.x, v.y), v23 = pack2(v.z, v.w);
-    const float xs[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const unsigned long long xx = pack2(xs[c], xs[c]);
-      fma2(a[0][c], v01, xx);
-      fma2(a[1][c], v23, xx);
-    }
-  }
-  __device__ __forceinline__ void get(float (&o)[4][4]) const {
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const float2 l = unpack2(a[0][c]), h = unpack2(a[1][c]);
-      o[0][c] = l.x; o[1][c] = l.y; o[2][c] = h.x; o[3][c] = h.y;
-    }
-  }
-};
-
-__device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
-__device__ __forceinline__ float4 ldcs4(const float* p) { return __ldcs(reinterpret_cast<const float4*>(p)); }
 
 template <int WARPS, bool PACKED, int U>
 __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant__ RbArgs a) {
@@ -206,16 +129,38 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
   const float* tq = a.tn + 4 * q;
   // dots: FP32 over kDotFlush row blocks (64 rows), then FP64 (the FP64 pipe
   // is a small fraction of the FP32 one: converting every block's partials
-  // would bound the kernel)
+  // would bound the kernel). A flush sums the four groups' FP32 partials and
+  // hands column `lane` to lane `lane`, so the FP64 sums take 2 registers.
   constexpr int kDotFlush = 16;
-  double d0[4], d1[4];
-  float e0[4], e1[4];
+  double d0 = 0.0, d1 = 0.0;  // column `lane`
+  float e0[4], e1[4];         // columns 4q..4q+3, this lane's rows
   int since_flush = 0;
 #pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    d0[c] = d1[c] = 0.0;
-    e0[c] = e1[c] = 0.f;
-  }
+  for (int c = 0; c < 4; ++c) e0[c] = e1[c] = 0.f;
+  auto flush = [&]() {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      e0[c] += __shfl_xor_sync(0xffffffffu, e0[c], 8);
+      e1[c] += __shfl_xor_sync(0xffffffffu, e1[c], 8);
+      e0[c] += __shfl_xor_sync(0xffffffffu, e0[c], 16);
+      e1[c] += __shfl_xor_sync(0xffffffffu, e1[c], 16);
+    }
+    // column `lane` = 4 * (lane >> 2) + (lane & 3) lives in lane (lane >> 2)
+    float v0 = 0.f, v1 = 0.f;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float s0 = __shfl_sync(0xffffffffu, e0[c], lane >> 2);
+      const float s1 = __shfl_sync(0xffffffffu, e1[c], lane >> 2);
+      if ((lane & 3) == c) {
+        v0 = s0;
+        v1 = s1;
+      }
+    }
+    d0 += (double)v0;
+    d1 += (double)v1;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) e0[c] = e1[c] = 0.f;
+  };
 
   bool gave_up = false;
   if (a.never_wait && !bounded_wait(&never, 0u, a.spin_limit)) {
@@ -322,12 +267,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
       }
       if (++since_flush == kDotFlush) {  // warp-uniform
         since_flush = 0;
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          d0[c] += (double)e0[c];
-          d1[c] += (double)e1[c];
-          e0[c] = e1[c] = 0.f;
-        }
+        flush();
       }
     }
     // release the stage; the last warp refills it
@@ -348,29 +288,15 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
     for (int i = 0; i < nst; ++i)
       if (issued[i] > 0) bounded_wait(&full[i], (uint32_t)(issued[i] - 1) & 1u, ~0ull);
 
-#pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    d0[c] += (double)e0[c];
-    d1[c] += (double)e1[c];
-  }
-  // lanes with equal q hold the same columns: fold the four groups
-#pragma unroll
-  for (int o = 8; o < 32; o <<= 1)
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      d0[c] += __shfl_xor_sync(0xffffffffu, d0[c], o);
-      d1[c] += __shfl_xor_sync(0xffffffffu, d1[c], o);
-    }
+  flush();
+  // warps add their columns in warp order (deterministic)
   __shared__ double bsum[2 * C];
   for (int t = threadIdx.x; t < 2 * C; t += NT) bsum[t] = 0.0;
   __syncthreads();
   for (int w = 0; w < WARPS; ++w) {
-    if (warp == w && g == 0) {
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        bsum[2 * (4 * q + c)] += d0[c];
-        bsum[2 * (4 * q + c) + 1] += d1[c];
-      }
+    if (warp == w) {
+      bsum[2 * lane] += d0;
+      bsum[2 * lane + 1] += d1;
     }
     __syncthreads();
   }
@@ -560,7 +486,22 @@ int64_t rb_stage_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps) {
 
 namespace leo2d {
 
+int64_t rb_tile_max_bytes(leo2d_ctx* ctx, const leo2d_csr* csr, int tile) {
+  DevBuf<unsigned long long> mx(1);
+  LEO_CUDA(cudaMemsetAsync(mx.p, 0, sizeof(unsigned long long), ctx->stream));
+  const int64_t tiles = (csr->rb_blocks + tile - 1) / tile;
+  launch(ctx, "rb_tile_max", [&] {
+    k_rb_tile_max<<<grid_for(tiles, 256, (int64_t)ctx->sm_count * 8), 256, 0, ctx->stream>>>(
+        csr->rb_off.p, csr->rb_blocks, tile, mx.p);
+  });
+  unsigned long long hm = 0;
+  d2h(ctx, &hm, mx.p, 1);
+  ctx_sync(ctx);
+  return (int64_t)hm;
+}
+
 void csr_drop_rb(leo2d_csr* csr) {
+  csr_drop_rbw(csr);
   csr->rb_built = false;
   csr->rb_blocks = 0;
   csr->rb_slots = 0;

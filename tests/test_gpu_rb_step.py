@@ -47,6 +47,7 @@ def _run(ctx, variant, fn, **opts):
         ctx.set_option("rb_packed", -1)
         ctx.set_option("rb_warps", 0)
         ctx.set_option("rb_unroll", 0)
+        ctx.set_option("rb_window", -1)
         ctx.set_option("reorder_patch_dA", 0)
         ctx.set_option("tile_stages", 2)
         ctx.set_option("tile_chunk", 4)
@@ -68,7 +69,7 @@ def test_rb_dos_matches(ctx, size, twist, model):
     again = _run(ctx, 3, lambda: csr.kpm_dos(cfg))
     np.testing.assert_array_equal(got, again)
     for opts in ({"rb_packed": 0}, {"rb_warps": 16, "rb_unroll": 4}, {"rb_warps": 32, "rb_packed": 1},
-                 {"reorder_patch_dA": 160}):
+                 {"reorder_patch_dA": 160}, {"rb_window": 1}, {"rb_window": 1, "rb_unroll": 8, "rb_packed": 0}):
         other = _run(ctx, 3, lambda: csr.kpm_dos(cfg), **opts)
         assert _rel(other, got) < 2e-5, opts
     rp, col, val = csr.download()
@@ -78,7 +79,8 @@ def test_rb_dos_matches(ctx, size, twist, model):
     assert _rel(got, o) < 1e-4
 
 
-@pytest.mark.parametrize("opts", [{"tile_stages": 3}, {"tile_chunk": 1}, {"tile_stages": 4, "tile_chunk": 16}])
+@pytest.mark.parametrize("opts", [{"tile_stages": 3}, {"tile_chunk": 1}, {"tile_stages": 4, "tile_chunk": 16},
+                                  {"rb_window": 1}, {"rb_window": 1, "tile_chunk": 1, "tile_stages": 3}])
 def test_rb_pipeline_shapes(ctx, opts):
     """Stage counts and tile orders change the schedule, not the sums."""
     csr = _flake(ctx, 30, 2.0)
@@ -125,27 +127,29 @@ def test_rb_ragged_last_block(ctx):
         csr = _flake(ctx, size, 4.0)
         cfg = L.kpm_cfg(32, R=16, seed=9, block=32)
         ref = _run(ctx, 0, lambda: csr.kpm_dos(cfg))
-        got = _run(ctx, 3, lambda: csr.kpm_dos(cfg))
-        assert _rel(got, ref) < 2e-5, (size, csr.n)
+        for window in (0, 1):
+            got = _run(ctx, 3, lambda: csr.kpm_dos(cfg), rb_window=window)
+            assert _rel(got, ref) < 2e-5, (size, csr.n, window)
 
 
-def test_rb_timeout_reports(ctx):
-    """The bounded wait of the row-block step: a barrier nobody completes gives
+@pytest.mark.parametrize("window", [0, 1])
+def test_rb_timeout_reports(ctx, window):
+    """The bounded wait of the row-block steps: a barrier nobody completes gives
     LEO2D_ERR_TIMEOUT, and the context keeps working afterwards."""
     csr = _flake(ctx, 20, 3.0)
     cfg = L.kpm_cfg(16, R=16, seed=1, block=32)
-    ok = _run(ctx, 3, lambda: csr.kpm_dos(cfg))
+    ok = _run(ctx, 3, lambda: csr.kpm_dos(cfg), rb_window=window)
     ctx.set_spin_limit(2000)
     ctx.set_option("test_unsatisfied_wait", 1)
     try:
         with pytest.raises(L.Leo2dError) as e:
-            _run(ctx, 3, lambda: csr.kpm_dos(cfg))
+            _run(ctx, 3, lambda: csr.kpm_dos(cfg), rb_window=window)
         assert e.value.status == L._abi.ERR_TIMEOUT
         assert "wait ran out" in str(e.value)
     finally:
         ctx.set_option("test_unsatisfied_wait", 0)
         ctx.set_spin_limit(0)
-    again = _run(ctx, 3, lambda: csr.kpm_dos(cfg))
+    again = _run(ctx, 3, lambda: csr.kpm_dos(cfg), rb_window=window)
     np.testing.assert_array_equal(ok, again)
 
 
