@@ -260,10 +260,23 @@ struct RowOut {
   double* dy;
 };
 
+// FP32 copy of the positions for the candidate prefilter of k_flake_rows.
+__global__ void k_pos32(const double* __restrict__ pos, int64_t n, float4* __restrict__ p32) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    p32[k] = make_float4((float)pos[3 * k], (float)pos[3 * k + 1], (float)pos[3 * k + 2], 0.f);
+}
+
+// FP32 distances decide a candidate only when they clear a threshold by this
+// margin (A). FP32 positions of up to 2^14 A are off by at most 1e-3 A, so an
+// in-plane distance is off by at most 3e-3 A; nearer the threshold the FP64
+// test decides, so the kept pairs and their values are those of FP64 alone.
+constexpr float kPrefilterMargin = 0.05f;
+
 template <bool kFill>
 __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ GeomDev G, int64_t n,
                                                     const int32_t* __restrict__ grid4,
-                                                    const double* __restrict__ pos, RowOut out) {
+                                                    const double* __restrict__ pos,
+                                                    const float4* __restrict__ pos32, RowOut out) {
   const unsigned lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -295,7 +308,8 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
           if (k2 != -1) {
             k2g = k2 + sh.base;
             const double raw = intralayer(G.model, l0, l, i - ih, j - jh);
-            t = k2g == row ? (raw + G.shift) / G.rescale : raw / G.rescale;
+            // (0 / rescale is 0: the FP64 division runs for nonzero entries only)
+            t = k2g == row ? (raw + G.shift) / G.rescale : (raw != 0.0 ? raw / G.rescale : 0.0);
           }
         }
         const bool keep = k2g >= 0;
@@ -321,6 +335,10 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
     // interlayer: sheet below, then sheet above; window +-6 clipped; d_xy < 12.5 A
     {
       const double ph[3] = {x1, y1, z1};
+      const float x1f = (float)x1, y1f = (float)y1, z1f = (float)z1;
+      constexpr float kWinLo = (float)(kInterCutoff - kPrefilterMargin), kWinHi = (float)(kInterCutoff + kPrefilterMargin);
+      // every hopping is zero from 8 A on (in-plane for the reference model, 3-D for the simple one)
+      constexpr float kHopHi = 8.0f + kPrefilterMargin;
       for (int side_k = 0; side_k < 2; ++side_k) {
         const int s0 = side_k == 0 ? s - 1 : s + 1;
         if (s0 < 0 || s0 >= G.S) continue;
@@ -342,14 +360,25 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
             const int k2 = grid_to_index(o0, i, j, l);
             if (k2 != -1) {
               const int64_t kk = k2 + o0.base;
-              const double x2 = pos[3 * kk], y2 = pos[3 * kk + 1];
-              if ((x2 - ph[0]) * (x2 - ph[0]) + (y2 - ph[1]) * (y2 - ph[1]) <
-                  kInterCutoff * kInterCutoff) {
+              const float4 q = pos32[kk];
+              const float dxf = q.x - x1f, dyf = q.y - y1f, dzf = q.z - z1f;
+              const float d2f = dxf * dxf + dyf * dyf;
+              bool in_window;
+              if (d2f < kWinLo * kWinLo) {
+                in_window = true;
+              } else if (d2f > kWinHi * kWinHi) {
+                in_window = false;
+              } else {
+                const double x2 = pos[3 * kk], y2 = pos[3 * kk + 1];
+                in_window = (x2 - ph[0]) * (x2 - ph[0]) + (y2 - ph[1]) * (y2 - ph[1]) < kInterCutoff * kInterCutoff;
+              }
+              if (in_window) {
                 k2g = kk;
-                if (kFill || !G.keep_zeros) {
-                  const double z2 = pos[3 * kk + 2];
-                  t = interlayer(G.model, l0, l, x2 - x1, y2 - y1, z2 - z1, sh.angle, o0.angle) /
-                      G.rescale;
+                const float h2f = G.model == LEO2D_MODEL_SIMPLE ? d2f + dzf * dzf : d2f;
+                if ((kFill || !G.keep_zeros) && h2f < kHopHi * kHopHi) {
+                  const double x2 = pos[3 * kk], y2 = pos[3 * kk + 1], z2 = pos[3 * kk + 2];
+                  const double v = interlayer(G.model, l0, l, x2 - x1, y2 - y1, z2 - z1, sh.angle, o0.angle);
+                  t = v != 0.0 ? v / G.rescale : 0.0;
                 }
               }
             }
@@ -874,11 +903,16 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
       LEO_CUDA(cudaFuncSetAttribute(k_periodic_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
     const unsigned rows_grid = grid_for(n, 8, (int64_t)ctx->sm_count * 64);
+    DevBuf<float4> pos32(G.bc == 0 ? std::max<int64_t>(n, 1) : 1);
+    if (G.bc == 0 && n > 0)
+      launch(ctx, "pos32", [&] {
+        k_pos32<<<grid_for(n, 256, (int64_t)ctx->sm_count * 32), 256, 0, ctx->stream>>>(csr->pos.p, n, pos32.p);
+      });
     const unsigned cta_grid = grid_for(n, 1, (int64_t)ctx->sm_count * 8);
     if (n > 0) {
       if (G.bc == 0)
         launch(ctx, "flake_rows_count", [&] {
-          k_flake_rows<false><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, ro);
+          k_flake_rows<false><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, ro);
         });
       else
         launch(ctx, "periodic_rows_count", [&] {
@@ -902,7 +936,7 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     if (n > 0) {
       if (G.bc == 0)
         launch(ctx, "flake_rows_fill", [&] {
-          k_flake_rows<true><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, ro);
+          k_flake_rows<true><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, ro);
         });
       else
         launch(ctx, "periodic_rows_fill", [&] {
