@@ -77,6 +77,12 @@ typedef struct {
   int32_t sheet_sc_stride[LEO2D_MAX_SHEETS][2][2];
   double supercell[2][2];                       /* sheet 0's supercell (Job_params "supercell") */
   int32_t prepared;
+  /* B_FIELD with USE_B_FIELD = 1 (tesla, perpendicular): when non-zero the
+   * Hamiltonian is complex, each entry t e^{i phi} with the Peierls phase
+   * phi = 3.14e-5 B (x_col - x_row)(y_row + y_col)/2 of Locality::peierlsPhase
+   * (src/locality.cpp:7157-7161), as generateCpxH builds it
+   * (src/locality.cpp:4485-5310). Flakes only (BOUNDARY_CONDITION = 0). */
+  double b_field;
 } leo2d_geom;
 
 typedef struct leo2d_ctx leo2d_ctx;
@@ -143,6 +149,10 @@ leo2d_status leo2d_csr_info(const leo2d_csr* csr, int64_t* n, int64_t* nnz,
 /* Copies the CSR to host arrays (any pointer may be NULL to skip it). */
 leo2d_status leo2d_csr_download(leo2d_ctx* ctx, const leo2d_csr* csr, int64_t* rowptr,
                                 int32_t* col, double* val, double* val_dx, double* val_dy);
+/* Imaginary parts of the stored entries (complex H: leo2d_geom.b_field != 0),
+ * in the order of leo2d_csr_download's values; val is the real part there.
+ * generateCpxH keeps std::complex<double> val_c (src/locality.cpp:4928-4941). */
+leo2d_status leo2d_csr_download_imag(leo2d_ctx* ctx, const leo2d_csr* csr, double* val_im);
 /* index_to_grid [n][4] = (i, j, orbital, sheet) as Hstruct::getIndexArray
  * (hstruct.cpp:69-110); pos [n][3] = i2pos of setConfigPositions
  * (locality.cpp:3618-3642, zero shifts). Either pointer may be NULL. */

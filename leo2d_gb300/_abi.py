@@ -36,7 +36,7 @@ class Geom(ctypes.Structure):
         ("angles", c_dbl * MAX_SHEETS), ("energy_rescale", c_dbl), ("energy_shift", c_dbl),
         ("lattice", c_dbl * 2 * 2 * MAX_SHEETS), ("sheet_supercell", c_dbl * 2 * 2 * MAX_SHEETS),
         ("sheet_sc_stride", c_i32 * 2 * 2 * MAX_SHEETS), ("supercell", c_dbl * 2 * 2),
-        ("prepared", c_i32),
+        ("prepared", c_i32), ("b_field", c_dbl),
     ]
 
 
@@ -51,7 +51,7 @@ class KpmCfg(ctypes.Structure):
 
 def make_geom(num_sheets=2, model=MODEL_REF, boundary_condition=0, size=50, max_R=None,
               heights=(0.0, 3.35), angles_deg=(0.0, 0.0), energy_rescale=20.0,
-              energy_shift=0.0, supercell_mn=None, sc_search_size=1):
+              energy_shift=0.0, supercell_mn=None, sc_search_size=1, b_field=0.0):
     """A Geom filled the way main.cpp fills Sdata for MAXSIZE=size, MINSIZE=-size.
 
     Angles are given in degrees and converted as main.cpp:345-351 does.
@@ -74,6 +74,7 @@ def make_geom(num_sheets=2, model=MODEL_REF, boundary_condition=0, size=50, max_
     g.energy_shift = energy_shift
     if supercell_mn is not None:
         g.supercell_m, g.supercell_n = supercell_mn
+    g.b_field = float(b_field)
     return g
 
 
@@ -142,6 +143,7 @@ def _declare(lib):
     fn("leo2d_tc_gemm_tf32x3", c_i32, c_void_p, P, P, c_i64, c_i64, P)
     fn("leo2d_csr_tc_info", c_i32, c_void_p, P, P, P, P)
     fn("leo2d_csr_rb_info", c_i32, c_void_p, P, P, P, P, P)
+    fn("leo2d_csr_download_imag", c_i32, c_void_p, c_void_p, P)
     fn("leo2d_mlp_param_count", c_i64)
     fn("leo2d_mlp_create", c_i32, c_void_p, c_u64, pp)
     fn("leo2d_mlp_destroy", c_i32, c_void_p)

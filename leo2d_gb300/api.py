@@ -205,6 +205,12 @@ class Csr:
                                                        _p(vdx), _p(vdy)))
         return (rp, col, val, vdx, vdy) if dx else (rp, col, val)
 
+    def download_imag(self):
+        """Imaginary parts of the stored entries (a complex Hamiltonian: b_field != 0)."""
+        im = np.zeros(self.nnz)
+        self.ctx.check(self.ctx.lib.leo2d_csr_download_imag(self.ctx.h, self.h, _p(im)))
+        return im
+
     def geometry(self):
         grid = np.zeros(4 * self.n, np.int32)
         pos = np.zeros(3 * self.n)

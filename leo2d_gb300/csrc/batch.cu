@@ -395,6 +395,8 @@ leo2d_status leo2d_batch_create(leo2d_ctx* ctx, const leo2d_csr* const* csrs, in
     LEO_REQUIRE(cfg->block == 0 || cfg->block == 8 || cfg->block == 16 || cfg->block == 32 || cfg->block == 64 ||
                     cfg->block == 128,
                 "block must be 0 (autotuned), 8, 16, 32, 64 or 128");
+    for (int32_t f = 0; f < num; ++f)
+      LEO_REQUIRE(csrs[f] && !csrs[f]->complex_h, "batched runs take real Hamiltonians (no magnetic field)");
     LEO_CUDA(cudaSetDevice(ctx->device));
     auto b = std::make_unique<leo2d_batch>();
     b->ctx = ctx;

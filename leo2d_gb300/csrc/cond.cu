@@ -194,6 +194,7 @@ leo2d_status leo2d_kpm_cond(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kp
     LEO_REQUIRE(P >= 4 && P % 4 == 0, "poly_order must be a positive multiple of 4");
     LEO_REQUIRE(cfg->precision == LEO2D_FP32 || cfg->precision == LEO2D_FP64, "unknown precision");
     LEO_REQUIRE(csr->dx64.p, "Kubo moments need dxH: build with LEO2D_CSR_WITH_DX");
+    LEO_REQUIRE(!csr->complex_h, "Kubo moments are built for a real Hamiltonian (no magnetic field)");
     const bool local = targets != nullptr;
     if (local) {
       LEO_REQUIRE(num_targets >= 1, "num_targets must be >= 1");

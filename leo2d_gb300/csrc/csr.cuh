@@ -24,6 +24,9 @@ struct leo2d_csr {
   leo2d::DevBuf<uint2> ent;       // nnz, (column, FP32 value bits) streamed by the FP32 recursion
   leo2d::DevBuf<uint2> entd;      // nnz, (column, FP32 dxH bits)
   leo2d::DevBuf<double> dx64, dy64;
+  bool complex_h = false;         // Peierls phases: entries have imaginary parts
+  leo2d::DevBuf<double> val_im64; // nnz, FP64 imaginary parts (complex_h)
+  leo2d::DevBuf<float> val_im32;  // nnz, FP32 copy
   leo2d::DevBuf<float> dx32;
   leo2d::DevBuf<int32_t> grid4;   // n x 4 (i, j, orbital, sheet)
   leo2d::DevBuf<double> pos;      // n x 3
@@ -42,6 +45,7 @@ struct leo2d_csr {
   leo2d::DevBuf<float> pval32;
   leo2d::DevBuf<uint2> pent;
   leo2d::DevBuf<double> pval64;
+  leo2d::DevBuf<float> pval_im32;   // permuted FP32 imaginary parts (complex_h)
   int perm_tile_rows = 0;
   int64_t perm_tile_max_nnz = 0;
   // tensor-core tiles of the locality-ordered copy (tc_spmm.cu): for each tile
@@ -69,6 +73,7 @@ struct leo2d_csr {
   int64_t rb_tile_max_bytes = 0;      // largest tile of rb_tile_warps blocks (data bytes)
   leo2d::DevBuf<int64_t> rb_off;      // [blocks + 1 + pad] first slot of each block
   leo2d::DevBuf<unsigned char> rb_data;  // 20 bytes per slot: columns, then the value panel
+  leo2d::DevBuf<float> rb_im;         // [slots][4] imaginary value panel (complex_h)
   // shared-memory windows of the row blocks (rbw_spmm.cu): per tile of 16 blocks
   // the sorted distinct columns of its slots; slots hold window positions
   bool rbw_built = false;

@@ -10,16 +10,17 @@ using namespace leo2d;
 namespace {
 
 // Per-row Gershgorin interval of the stored matrix, reduced with min/max.
+// A complex (Hermitian) matrix uses the moduli |H_ij| and the real diagonal.
 __global__ void k_gershgorin(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
-                             const double* __restrict__ val, double* __restrict__ lo_out,
-                             double* __restrict__ hi_out) {
+                             const double* __restrict__ val, const double* __restrict__ im,
+                             double* __restrict__ lo_out, double* __restrict__ hi_out) {
   double lo = INFINITY, hi = -INFINITY;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
        r += (int64_t)gridDim.x * blockDim.x) {
     double c = 0, rad = 0;
     for (int64_t i = rp[r]; i < rp[r + 1]; ++i) {
       if (col[i] == r) c += val[i];
-      else rad += fabs(val[i]);
+      else rad += im ? hypot(val[i], im[i]) : fabs(val[i]);
     }
     lo = fmin(lo, c - rad);
     hi = fmax(hi, c + rad);
@@ -41,13 +42,15 @@ __global__ void k_gershgorin(int64_t n, const int64_t* __restrict__ rp, const in
 }
 
 // H <- (H + shift I) / rescale on the stored entries (diagonal gets the shift).
+// (a complex matrix: the imaginary parts are divided, the shift is real)
 __global__ void k_rescale(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
-                          double* __restrict__ val, double* __restrict__ dx, double* __restrict__ dy,
-                          double rescale, double shift) {
+                          double* __restrict__ val, double* __restrict__ im, double* __restrict__ dx,
+                          double* __restrict__ dy, double rescale, double shift) {
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
        r += (int64_t)gridDim.x * blockDim.x) {
     for (int64_t i = rp[r]; i < rp[r + 1]; ++i) {
       val[i] = col[i] == r ? (val[i] + shift) / rescale : val[i] / rescale;
+      if (im) im[i] = im[i] / rescale;
       if (dx) dx[i] = dx[i] / rescale;
       if (dy) dy[i] = dy[i] / rescale;
     }
@@ -159,6 +162,16 @@ leo2d_status leo2d_csr_upload(leo2d_ctx* ctx, int64_t n, int64_t nnz, const int6
   return LEO2D_OK;
 }
 
+leo2d_status leo2d_csr_download_imag(leo2d_ctx* ctx, const leo2d_csr* csr, double* val_im) {
+  if (!ctx || !csr || !val_im) return LEO2D_ERR_BAD_ARG;
+  return guard(ctx, [&] {
+    LEO_REQUIRE(csr->complex_h, "the matrix is real (built without a magnetic field)");
+    LEO_CUDA(cudaSetDevice(ctx->device));
+    d2h(ctx, val_im, csr->val_im64.p, (size_t)csr->nnz);
+    ctx_sync(ctx);
+  });
+}
+
 leo2d_status leo2d_csr_bounds(leo2d_ctx* ctx, const leo2d_csr* csr, double* emin, double* emax) {
   if (!ctx || !csr || !emin || !emax) return LEO2D_ERR_BAD_ARG;
   return guard(ctx, [&] {
@@ -166,7 +179,8 @@ leo2d_status leo2d_csr_bounds(leo2d_ctx* ctx, const leo2d_csr* csr, double* emin
     const unsigned g = grid_for(csr->n, 256, (int64_t)ctx->sm_count * 4);
     DevBuf<double> lo(g), hi(g);
     launch(ctx, "gershgorin", [&] {
-      k_gershgorin<<<g, 256, 0, ctx->stream>>>(csr->n, csr->rowptr.p, csr->col.p, csr->val64.p, lo.p, hi.p);
+      k_gershgorin<<<g, 256, 0, ctx->stream>>>(csr->n, csr->rowptr.p, csr->col.p, csr->val64.p,
+                                                csr->complex_h ? csr->val_im64.p : nullptr, lo.p, hi.p);
     });
     std::vector<double> hl(g), hh(g);
     d2h(ctx, hl.data(), lo.p, g);
@@ -190,7 +204,8 @@ leo2d_status leo2d_csr_rescale(leo2d_ctx* ctx, leo2d_csr* csr, double rescale, d
     LEO_CUDA(cudaSetDevice(ctx->device));
     launch(ctx, "rescale", [&] {
       k_rescale<<<grid_for(csr->n, 256, (int64_t)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
-          csr->n, csr->rowptr.p, csr->col.p, csr->val64.p, csr->dx64.p, csr->dy64.p, rescale, shift);
+          csr->n, csr->rowptr.p, csr->col.p, csr->val64.p, csr->complex_h ? csr->val_im64.p : nullptr,
+          csr->dx64.p, csr->dy64.p, rescale, shift);
     });
     csr_refresh_fp32(ctx, csr);
     ctx_sync(ctx);

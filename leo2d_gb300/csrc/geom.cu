@@ -60,6 +60,7 @@ struct GeomDev {
   int S, model, bc, sc_search, keep_zeros, with_dx;
   double supercell[2][2];
   double rescale, shift;
+  double b_field;  // non-zero: complex entries t e^{i phi} (Peierls phase)
   SheetDev sh[kMaxSheets];
 };
 
@@ -258,7 +259,33 @@ struct RowOut {
   double* val;
   double* dx;
   double* dy;
+  double* val_im;  // imaginary parts (b_field != 0)
 };
+
+// Locality::peierlsPhase (locality.cpp:7157-7161): the phase of the hopping
+// from (x1, y1) (the row's orbital) to (x2, y2) (the column's) in the field B.
+__device__ __forceinline__ double peierls_phase(double x1, double x2, double y1, double y2, double B) {
+  const double pre = 3.14e-5;
+  return pre * B * (x2 - x1) * (0.5) * (y1 + y2);
+}
+
+// One stored entry: real H (value t) or, in a field, std::polar(t, phi) as
+// generateCpxH adds it (locality.cpp:4896-4941: zero couplings stay 0).
+__device__ __forceinline__ void store_value(const GeomDev& G, const RowOut& out, int64_t e, double t, double x1,
+                                            double y1, double x2, double y2) {
+  if (G.b_field == 0.0) {
+    out.val[e] = t != 0 ? 0.0 + t : 0.0;
+    return;
+  }
+  if (t == 0) {
+    out.val[e] = 0.0;
+    out.val_im[e] = 0.0;
+    return;
+  }
+  const double ph = peierls_phase(x1, x2, y1, y2, G.b_field);
+  out.val[e] = 0.0 + t * cos(ph);
+  out.val_im[e] = 0.0 + t * sin(ph);
+}
 
 // FP32 copy of the positions for the candidate prefilter of k_flake_rows.
 __global__ void k_pos32(const double* __restrict__ pos, int64_t n, float4* __restrict__ p32) {
@@ -320,9 +347,9 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
         if (kFill && store) {
           const int64_t e = o + __popc(m & lt_mask);
           out.col[e] = (int32_t)k2g;
-          out.val[e] = t != 0 ? 0.0 + t : 0.0;
+          const double x2 = pos[3 * k2g], y2 = pos[3 * k2g + 1];
+          store_value(G, out, e, t, x1, y1, x2, y2);
           if (G.with_dx) {
-            const double x2 = pos[3 * k2g], y2 = pos[3 * k2g + 1];
             out.dx[e] = t != 0 ? 0.0 + (x1 - x2) * t : 0.0;
             out.dy[e] = t != 0 ? 0.0 + (y1 - y2) * t : 0.0;
           }
@@ -390,9 +417,9 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
           if (kFill && store) {
             const int64_t e = o + __popc(m & lt_mask);
             out.col[e] = (int32_t)k2g;
-            out.val[e] = t != 0 ? 0.0 + t : 0.0;
+            const double x2 = pos[3 * k2g], y2 = pos[3 * k2g + 1];
+            store_value(G, out, e, t, x1, y1, x2, y2);
             if (G.with_dx) {
-              const double x2 = pos[3 * k2g], y2 = pos[3 * k2g + 1];
               out.dx[e] = t != 0 ? 0.0 + (x1 - x2) * t : 0.0;
               out.dy[e] = t != 0 ? 0.0 + (y1 - y2) * t : 0.0;
             }
@@ -762,6 +789,9 @@ void validate_geom(const leo2d_geom* g) {
   }
   if (g->boundary_condition == 1)
     LEO_REQUIRE(g->sc_search_size >= 0 && g->sc_search_size <= 3, "sc_search_size must be 0..3");
+  LEO_REQUIRE(std::isfinite(g->b_field), "b_field must be finite");
+  LEO_REQUIRE(g->b_field == 0.0 || g->boundary_condition == 0,
+              "a magnetic field is supported for flakes (BOUNDARY_CONDITION = 0)");
 }
 
 }  // namespace
@@ -801,6 +831,14 @@ void csr_refresh_fp32(leo2d_ctx* ctx, leo2d_csr* csr) {
     k_pack_ent<<<grid_for(csr->nnz, 256, (int64_t)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
         csr->col.p, csr->val32.p, csr->ent.p, csr->nnz);
   });
+  if (csr->complex_h) {
+    csr->val_im32.alloc(csr->nnz + kCsrPad);
+    LEO_CUDA(cudaMemsetAsync(csr->val_im32.p + csr->nnz, 0, kCsrPad * sizeof(float), ctx->stream));
+    launch(ctx, "to_f32", [&] {
+      k_to_f32<<<grid_for(csr->nnz, 256, (int64_t)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
+          csr->val_im64.p, csr->val_im32.p, csr->nnz);
+    });
+  }
   if (csr->dx64.p) {
     csr->dx32.alloc(csr->nnz + kCsrPad);
     LEO_CUDA(cudaMemsetAsync(csr->dx32.p + csr->nnz, 0, kCsrPad * sizeof(float), ctx->stream));
@@ -839,6 +877,9 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     G.sc_search = g->boundary_condition == 1 ? g->sc_search_size : 0;
     G.keep_zeros = (flags & LEO2D_CSR_KEEP_ZEROS) ? 1 : 0;
     G.with_dx = (flags & LEO2D_CSR_WITH_DX) ? 1 : 0;
+    G.b_field = g->b_field;
+    LEO_REQUIRE(g->b_field == 0.0 || !G.with_dx,
+                "the velocity operator (WITH_DX, conductivity) is not built for a complex Hamiltonian");
     std::memcpy(G.supercell, g->supercell, sizeof(G.supercell));
     G.rescale = g->energy_rescale;
     G.shift = g->energy_shift;
@@ -887,7 +928,7 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     DevBuf<int64_t> cnt_ent(std::max<int64_t>(n, 1)), cnt_intra(std::max<int64_t>(n, 1)),
         cnt_inter(std::max<int64_t>(n, 1));
     csr_alloc_rowptr(ctx, csr, n);
-    RowOut ro{cnt_ent.p, cnt_intra.p, cnt_inter.p, csr->rowptr.p, nullptr, nullptr, nullptr, nullptr};
+    RowOut ro{cnt_ent.p, cnt_intra.p, cnt_inter.p, csr->rowptr.p, nullptr, nullptr, nullptr, nullptr, nullptr};
     int cap = 0;
     size_t smem = 0;
     if (G.bc == 1) {
@@ -929,10 +970,16 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     csr->n_intra = reduce_sum_i64(ctx, cnt_intra.p, n);
     csr->n_inter = reduce_sum_i64(ctx, cnt_inter.p, n);
     csr_alloc_entries(ctx, csr, nnz, G.with_dx != 0);
+    csr->complex_h = g->b_field != 0.0;
+    if (csr->complex_h) {
+      csr->val_im64.alloc(nnz + kCsrPad);
+      LEO_CUDA(cudaMemsetAsync(csr->val_im64.p, 0, (nnz + kCsrPad) * sizeof(double), ctx->stream));
+    }
     ro.col = csr->col.p;
     ro.val = csr->val64.p;
     ro.dx = csr->dx64.p;
     ro.dy = csr->dy64.p;
+    ro.val_im = csr->val_im64.p;
     if (n > 0) {
       if (G.bc == 0)
         launch(ctx, "flake_rows_fill", [&] {

@@ -277,6 +277,9 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
   leo2d_csr* mm = const_cast<leo2d_csr*>(m);
   const bool can_perm = allow_perm && m->pos.p != nullptr && m->nnz > 0;
   if (shape.tc && !can_perm) shape.tc = false;
+  if (m->complex_h)
+    LEO_REQUIRE(shape.rb && can_perm && !s.fp64 && s.cols == 32 && ctx->reorder != 0,
+                "a complex Hamiltonian needs the row-block step (FP32, 32 columns, locality ordering on)");
   if (shape.rb && (!can_perm || s.fp64 || s.cols != 32 || ctx->reorder == 0)) shape.rb = false;
   if (shape.rb) shape.tc = false;
   const bool want_perm = can_perm && (shape.tc || shape.rb || ctx->reorder == 1 ||
@@ -299,6 +302,13 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
   if (shape.rb) {
     // row blocks of the locality-ordered copy (built once per matrix)
     if (!m->rb_built || m->rb_patch != m->reorder_patch) csr_build_rb(ctx, mm);
+    // a complex H has no other step kernel: narrower tiles when 24 blocks do not fit
+    if (m->complex_h && m->rb_built)
+      for (int w : {24, 16, 8})
+        if (rb_stages(ctx, mm, w) >= 2) {
+          shape.rb_warps = w;
+          break;
+        }
     if (shape.rb_window && m->rb_built && !m->rbw_built) csr_build_rbw(ctx, mm);
     if (shape.rb_window && !(m->rbw_built && rbw_stages(ctx, mm) >= 2)) shape.rb_window = false;
     if (shape.rb_window) {
@@ -310,6 +320,7 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
       grid = rb_grid(ctx, m, shape.rb_warps);
       shape.tiled = false;
     } else {
+      LEO_REQUIRE(!m->complex_h, "row blocks of the complex Hamiltonian do not fit shared memory");
       shape.rb = false;  // blocks too wide for the row-block step: the gather kernels run
     }
   }
@@ -468,10 +479,23 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
   if (ctx->kernel_variant == 3) s.rb = rb_ok;
   else if (ctx->kernel_variant == -1) s.rb = rb_ok && (cached ? it->second.rb : (ctx->reorder == 1 || csr->n >= 100000));
   if (s.rb) s.tc = false;
+  if (csr->complex_h) {
+    // a complex H runs on the row-block step only: 16 complex vectors (32 columns), FP32
+    LEO_REQUIRE(!fp64, "a complex Hamiltonian (magnetic field) runs in FP32");
+    LEO_REQUIRE(s.cols == 32 || requested_cols <= 0, "a complex Hamiltonian takes 32-column blocks");
+    s.cols = 32;
+    s.rb = true;
+    s.tc = false;
+    s.tiled = true;
+  }
   s.rb_warps = ctx->rb_warps > 0 ? ctx->rb_warps : (cached && it->second.rb_warps > 0 ? it->second.rb_warps : 24);
   s.rb_unroll = ctx->rb_unroll > 0 ? ctx->rb_unroll : (cached && it->second.rb_unroll > 0 ? it->second.rb_unroll : 8);
   s.rb_packed = ctx->rb_packed >= 0 ? ctx->rb_packed != 0 : (cached ? it->second.rb_packed : true);
   s.rb_window = ctx->rb_window >= 0 ? ctx->rb_window != 0 : (cached ? it->second.rb_window : false);
+  if (csr->complex_h) {
+    s.rb_window = false;
+    s.rb_warps = 24;
+  }
   LEO_REQUIRE(s.rows_per_item >= 0 && s.rows_per_item <= 64, "rows_per_warp must be 0..64");
   return s;
 }
@@ -494,11 +518,11 @@ void fill_gaussian(leo2d_ctx* ctx, Recursion& r, uint64_t seed, uint64_t first, 
   const unsigned g = grid_for(total, 256, (int64_t)ctx->sm_count * 32);
   if (r.shape.fp64)
     launch(ctx, "fill_gauss", [&] {
-      k_fill_gauss<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, seed, first, n_vec, r.perm());
+      k_fill_gauss<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, seed, first, n_vec, r.perm(), r.pairs());
     });
   else
     launch(ctx, "fill_gauss", [&] {
-      k_fill_gauss<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, seed, first, n_vec, r.perm());
+      k_fill_gauss<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, seed, first, n_vec, r.perm(), r.pairs());
     });
 }
 
@@ -509,11 +533,11 @@ void fill_host(leo2d_ctx* ctx, Recursion& r, const double* host_vectors, int fir
   const unsigned g = grid_for(total, 256, (int64_t)ctx->sm_count * 32);
   if (r.shape.fp64)
     launch(ctx, "fill_host", [&] {
-      k_fill_from<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, src.p, n_vec, r.perm());
+      k_fill_from<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, src.p, n_vec, r.perm(), r.pairs());
     });
   else
     launch(ctx, "fill_host", [&] {
-      k_fill_from<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, src.p, n_vec, r.perm());
+      k_fill_from<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, src.p, n_vec, r.perm(), r.pairs());
     });
   LEO_CUDA(cudaStreamSynchronize(ctx->stream));
 }
@@ -525,11 +549,11 @@ void fill_unit(leo2d_ctx* ctx, Recursion& r, const int64_t* targets, int n_t) {
   const unsigned g = grid_for(total, 256, (int64_t)ctx->sm_count * 32);
   if (r.shape.fp64)
     launch(ctx, "fill_unit", [&] {
-      k_fill_unit<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, t.p, n_t, r.perm());
+      k_fill_unit<double><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (double*)r.x0.p, t.p, n_t, r.perm(), r.pairs());
     });
   else
     launch(ctx, "fill_unit", [&] {
-      k_fill_unit<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, t.p, n_t, r.perm());
+      k_fill_unit<float><<<g, 256, 0, ctx->stream>>>(r.n, r.shape.cols, (float*)r.x0.p, t.p, n_t, r.perm(), r.pairs());
     });
   LEO_CUDA(cudaStreamSynchronize(ctx->stream));
 }
@@ -576,7 +600,8 @@ void run_trace(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg, c
   const int P = cfg->poly_order;
   const int steps = P / 2;
   const bool fp64 = cfg->precision == LEO2D_FP64;
-  const int group = cfg->vector_kind == LEO2D_VEC_PHASE ? 2 : 1;
+  // complex H: every vector is a (real, imaginary) column pair
+  const int group = (cfg->vector_kind == LEO2D_VEC_PHASE || csr->complex_h) ? 2 : 1;
   const int total_cols = cfg->num_vectors * group;
   StepShape shape = choose_shape(ctx, csr, fp64, total_cols, cfg->block, cfg->rows_per_warp);
   LEO_REQUIRE(shape.cols % group == 0, "block width must hold whole complex vectors");
@@ -628,18 +653,20 @@ leo2d_status leo2d_kpm_ldos(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kp
     LEO_CUDA(cudaSetDevice(ctx->device));
     const int P = cfg->poly_order, steps = P / 2;
     const bool fp64 = cfg->precision == LEO2D_FP64;
-    StepShape shape = choose_shape(ctx, csr, fp64, (int)std::min<int64_t>(num_targets, 128),
+    const int group = csr->complex_h ? 2 : 1;  // complex H: a (real, imaginary) column pair per target
+    StepShape shape = choose_shape(ctx, csr, fp64, (int)std::min<int64_t>(num_targets * group, 128),
                                    cfg->block, cfg->rows_per_warp);
     Recursion r;
     r.setup(ctx, csr, shape, steps);
     std::vector<double> dots((size_t)steps * 2 * shape.cols);
-    for (int64_t t0 = 0; t0 < num_targets; t0 += shape.cols) {
-      const int nt = (int)std::min<int64_t>(shape.cols, num_targets - t0);
+    const int per_block = shape.cols / group;
+    for (int64_t t0 = 0; t0 < num_targets; t0 += per_block) {
+      const int nt = (int)std::min<int64_t>(per_block, num_targets - t0);
       fill_unit(ctx, r, targets + t0, nt);
       r.run();
       d2h(ctx, dots.data(), r.dots.p, dots.size());
       ctx_sync(ctx);
-      dots_to_moments(dots, shape.cols, steps, 1, nt, mu_out + (size_t)t0 * P, P);
+      dots_to_moments(dots, shape.cols, steps, group, nt, mu_out + (size_t)t0 * P, P);
     }
   });
 }
@@ -656,6 +683,11 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
     LEO_REQUIRE(cfg->num_vectors >= 1, "num_vectors must be >= 1");
     LEO_CUDA(cudaSetDevice(ctx->device));
     const bool fp64 = cfg->precision == LEO2D_FP64;
+    if (csr->complex_h) {  // one step kernel and width for a complex Hamiltonian
+      if (block_out) *block_out = 32;
+      if (rows_out) *rows_out = 0;
+      return;
+    }
     const int group = cfg->vector_kind == LEO2D_VEC_PHASE ? 2 : 1;
     const int total_cols = cfg->num_vectors * group;
     const int steps = 8;

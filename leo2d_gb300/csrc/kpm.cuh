@@ -40,6 +40,8 @@ struct Recursion {
   bool use_perm = false;  // stream the locality-ordered copy of the matrix
   bool allow_perm = true; // set false before setup() to keep the reference row order
   const int32_t* perm() const { return use_perm ? csr->new2old.p : nullptr; }
+  // complex H: vector v occupies columns 2v (real part) and 2v + 1 (imaginary part)
+  int pairs() const { return csr->complex_h ? 1 : 0; }
 
   void setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_);
   void* buf(int i) { return i == 0 ? (void*)x0.p : (void*)x1.p; }

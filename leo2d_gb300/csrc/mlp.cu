@@ -711,6 +711,7 @@ leo2d_status leo2d_kpm_dos_cv(leo2d_ctx* ctx, const leo2d_csr* csr, leo2d_mlp* M
     LEO_REQUIRE(P >= 4 && P % 4 == 0, "poly_order must be a positive multiple of 4");
     LEO_REQUIRE(num_sites >= 0, "num_sites must be >= 0");
     LEO_REQUIRE(M->ctx == ctx, "the network belongs to another context");
+    LEO_REQUIRE(!csr->complex_h, "the control variate is trained on real Hamiltonians (no magnetic field)");
     auto check = [&](leo2d_status st) {
       if (st != LEO2D_OK) fail(st, ctx->last_error);
     };

@@ -91,3 +91,32 @@ __device__ __forceinline__ float4 ld_once4(const float* p) {
   return r;
 }
 
+
+// Complex H: the lane's 4 columns are two complex numbers (re, im, re, im); a
+// slot's values are a + ib per row (a from the value panel, b from the
+// imaginary panel): y += (a + ib)(x_re + i x_im).
+struct PanelAccCpx {
+  float a[4][4];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) a[r][c] = 0.f;
+  }
+  __device__ __forceinline__ void add(const float4& x, const float4& v, const float4& w) {
+    const float re[4] = {v.x, v.y, v.z, v.w}, im[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      a[r][0] += re[r] * x.x - im[r] * x.y;
+      a[r][1] += re[r] * x.y + im[r] * x.x;
+      a[r][2] += re[r] * x.z - im[r] * x.w;
+      a[r][3] += re[r] * x.w + im[r] * x.z;
+    }
+  }
+  __device__ __forceinline__ void get(float (&o)[4][4]) const {
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) o[r][c] = a[r][c];
+  }
+};

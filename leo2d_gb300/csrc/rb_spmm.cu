@@ -65,16 +65,18 @@ struct RbArgs {
   double* __restrict__ partials;
   const double* __restrict__ prev_partials;
   double* __restrict__ prev_dots;
+  const float* __restrict__ im;  // complex H: [slots][4] imaginary panel
   int stages;      // 2..4
   int chunk;       // consecutive tiles per block between grid-wide jumps
   int off_bytes;   // offsets region of a stage
-  int stage_bytes; // offsets + data, multiple of 128
+  int im_at;       // complex H: start of the imaginary panel in a stage
+  int stage_bytes; // offsets + data (+ imaginary panel), multiple of 128
   uint64_t spin_limit;
   int* status;
   int never_wait;  // test hook: wait on a barrier that nobody completes
 };
 
-template <int WARPS, bool PACKED, int U>
+template <int WARPS, bool PACKED, int U, bool CPX = false>
 __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant__ RbArgs a) {
   constexpr int C = 32;
   constexpr int NT = WARPS * 32;
@@ -108,10 +110,12 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
     const int64_t s0 = a.off[b0], s1 = a.off[b1];
     const uint32_t dbytes = (uint32_t)((s1 - s0) * kRbSlotBytes);
     unsigned char* st = smem + (size_t)stage * a.stage_bytes;
+    const uint32_t ibytes = CPX ? (uint32_t)((s1 - s0) * kRbRows * sizeof(float)) : 0u;
     issued[stage] += 1;
-    mbar_expect_tx(&full[stage], (uint32_t)(ocount * 8) + dbytes);
+    mbar_expect_tx(&full[stage], (uint32_t)(ocount * 8) + dbytes + ibytes);
     bulk_g2s(st, a.off + ba, (uint32_t)(ocount * 8), &full[stage]);
     if (dbytes) bulk_g2s(st + a.off_bytes, a.data + s0 * kRbSlotBytes, dbytes, &full[stage]);
+    if (CPX && ibytes) bulk_g2s(st + a.im_at, a.im + s0 * kRbRows, ibytes, &full[stage]);
   };
   const int64_t chunk = a.chunk;
   auto tile_of = [&](int64_t i) -> int64_t {
@@ -199,8 +203,13 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
       const int nb = K >> 2;
       const int32_t* csg = cs + g;
       const float4* vsg = vs + g;
-      PanelAcc<PACKED> acc;
+      const float4* wsg = reinterpret_cast<const float4*>(st + a.im_at) + (sb - off_s[b0 - ba]) + g;
+      typename std::conditional<CPX, PanelAccCpx, PanelAcc<PACKED>>::type acc;
       acc.zero();
+      auto add = [&](const float4& x, int slot4) {
+        if constexpr (CPX) acc.add(x, vsg[slot4], wsg[slot4]);
+        else acc.add(x, vsg[slot4]);
+      };
       int b = 0;
       for (; b + U <= nb; b += U) {
         const int32_t* cb = csg + 4 * b;
@@ -212,7 +221,8 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
 #pragma unroll
         for (int u = 0; u < U; ++u) x[u] = ldg4(tq + (size_t)c[u] * C);
 #pragma unroll
-        for (int u = 0; u < U; ++u) acc.add(x[u], vb[4 * u]);
+        for (int u = 0; u < U; ++u) add(x[u], 4 * (b + u));
+        (void)vb;
       }
       for (; b < nb; b += 4) {
         const int rem = nb - b;  // warp-uniform
@@ -224,7 +234,8 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
           x[u] = u < rem ? ldg4(tq + (size_t)(uint32_t)cb[4 * u] * C) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-          if (u < rem) acc.add(x[u], vb[4 * u]);
+          if (u < rem) add(x[u], 4 * (b + u));
+        (void)vb;
       }
       // reduce-scatter over the four groups: group g keeps row g
       float p[4][4];
@@ -347,10 +358,12 @@ __device__ int rb_block_scan(int x, int* total) {
 // kRbMaxSlots slots; err[1] most slots (before padding); ssum: sum of slots.
 __global__ void __launch_bounds__(kRbBuildThreads) k_rb_build(int64_t n, int64_t nrb, const int64_t* __restrict__ prow,
                                                               const int32_t* __restrict__ pcol,
-                                                              const float* __restrict__ pval, int pass,
+                                                              const float* __restrict__ pval,
+                                                              const float* __restrict__ pval_im, int pass,
                                                               int64_t* __restrict__ count,
                                                               const int64_t* __restrict__ off,
-                                                              unsigned char* __restrict__ data, int* __restrict__ err,
+                                                              unsigned char* __restrict__ data, float* __restrict__ im_out,
+                                                              int* __restrict__ err,
                                                               unsigned long long* __restrict__ ssum) {
   extern __shared__ unsigned long long rb_keys[];  // kRbMaxEnt keys: column << 16 | entry
   __shared__ int64_t srp[kRbRows + 1];
@@ -426,12 +439,15 @@ __global__ void __launch_bounds__(kRbBuildThreads) k_rb_build(int64_t n, int64_t
       }
       if (start) {
         float v = pval[q0 + e];
+        float vi = pval_im ? pval_im[q0 + e] : 0.f;
         for (int m = i + 1; m < E && (uint32_t)(rb_keys[m] >> 16) == c; ++m) {
           const int em = (int)(rb_keys[m] & 0xFFFFu);
           if (em >= srp[r + 1] - q0) break;
           v += pval[q0 + em];
+          if (pval_im) vi += pval_im[q0 + em];
         }
         val_out[s * kRbRows + r] = v;
+        if (im_out) im_out[(off[b] + s) * kRbRows + r] = vi;
       }
     }
     __syncthreads();
@@ -478,8 +494,14 @@ int64_t rb_tile_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps) {
   return csr->rb_tile_max_bytes;
 }
 
+// Imaginary panel of the largest tile (complex H): 16 of every 20 slot bytes.
+int64_t rb_im_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps) {
+  if (!csr->complex_h) return 0;
+  return (rb_tile_bytes(ctx, csr, warps) / kRbSlotBytes * kRbRows * (int64_t)sizeof(float) + 127) / 128 * 128;
+}
+
 int64_t rb_stage_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps) {
-  return rb_off_bytes(warps) + (rb_tile_bytes(ctx, csr, warps) + 127) / 128 * 128;
+  return rb_off_bytes(warps) + (rb_tile_bytes(ctx, csr, warps) + 127) / 128 * 128 + rb_im_bytes(ctx, csr, warps);
 }
 
 }  // namespace
@@ -509,6 +531,7 @@ void csr_drop_rb(leo2d_csr* csr) {
   csr->rb_tile_max_bytes = 0;
   csr->rb_off.release();
   csr->rb_data.release();
+  csr->rb_im.release();
 }
 
 bool csr_build_rb(leo2d_ctx* ctx, leo2d_csr* csr) {
@@ -528,8 +551,9 @@ bool csr_build_rb(leo2d_ctx* ctx, leo2d_csr* csr) {
   LEO_CUDA(cudaFuncSetAttribute(k_rb_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const unsigned grid = (unsigned)std::min<int64_t>(nrb, (int64_t)ctx->sm_count * 4);
   launch(ctx, "rb_build", [&] {
-    k_rb_build<<<grid, kRbBuildThreads, smem, ctx->stream>>>(n, nrb, csr->prow.p, csr->pcol.p, csr->pval32.p, 0,
-                                                              cnt.p, nullptr, nullptr, err.p, ssum.p);
+    k_rb_build<<<grid, kRbBuildThreads, smem, ctx->stream>>>(n, nrb, csr->prow.p, csr->pcol.p, csr->pval32.p,
+                                                              nullptr, 0, cnt.p, nullptr, nullptr, nullptr, err.p,
+                                                              ssum.p);
   });
   int h[2] = {0, 0};
   unsigned long long hs = 0;
@@ -548,10 +572,16 @@ bool csr_build_rb(leo2d_ctx* ctx, leo2d_csr* csr) {
   std::vector<int64_t> pad(kRbOffPad, total);
   h2d(ctx, csr->rb_off.p + nrb + 1, pad.data(), pad.size());
   csr->rb_data.alloc((size_t)std::max<int64_t>(total, 1) * kRbSlotBytes);
+  if (csr->complex_h) {
+    LEO_REQUIRE(csr->pval_im32.p, "the ordered copy lacks the imaginary parts");
+    csr->rb_im.alloc((size_t)std::max<int64_t>(total, 1) * kRbRows);
+    LEO_CUDA(cudaMemsetAsync(csr->rb_im.p, 0, (size_t)std::max<int64_t>(total, 1) * kRbRows * sizeof(float),
+                             ctx->stream));
+  }
   launch(ctx, "rb_build", [&] {
-    k_rb_build<<<grid, kRbBuildThreads, smem, ctx->stream>>>(n, nrb, csr->prow.p, csr->pcol.p, csr->pval32.p, 1,
-                                                              nullptr, csr->rb_off.p, csr->rb_data.p, err.p,
-                                                              ssum.p);
+    k_rb_build<<<grid, kRbBuildThreads, smem, ctx->stream>>>(
+        n, nrb, csr->prow.p, csr->pcol.p, csr->pval32.p, csr->complex_h ? csr->pval_im32.p : nullptr, 1, nullptr,
+        csr->rb_off.p, csr->rb_data.p, csr->complex_h ? csr->rb_im.p : nullptr, err.p, ssum.p);
   });
   ctx_sync(ctx);
   csr->rb_blocks = nrb;
@@ -604,6 +634,8 @@ void rb_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
   a.chunk = std::max(1, ctx->tile_chunk);
   a.off_bytes = rb_off_bytes(w);
   a.stage_bytes = (int)rb_stage_bytes(ctx, m, w);
+  a.im = csr->complex_h ? csr->rb_im.p : nullptr;
+  a.im_at = (int)(a.stage_bytes - rb_im_bytes(ctx, m, w));
   LEO_REQUIRE((size_t)a.stages * a.stage_bytes <= smem, "row-block shared memory changed since setup");
   a.spin_limit = ctx->spin_limit;
   a.status = ctx->status.p;
@@ -612,6 +644,14 @@ void rb_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
     LEO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     launch(ctx, "cheb_step", [&] { kern<<<grid, warps * 32, smem, ctx->stream>>>(a); });
   };
+  if (csr->complex_h) {
+    switch (w) {
+      case 24: return go(k_cheb_rb<24, false, 4, true>, 24);
+      case 16: return go(k_cheb_rb<16, false, 4, true>, 16);
+      case 8: return go(k_cheb_rb<8, false, 4, true>, 8);
+    }
+    fail(LEO2D_ERR_BAD_ARG, "the complex row-block step runs 8, 16 or 24 warps");
+  }
   // variant: warps (16, 24, 32) x FMA form x slot batches in flight (4, 8)
   const int key = (w / 8) * 100 + (shape.rb_packed ? 10 : 0) + (shape.rb_unroll == 8 ? 1 : 0);
 #define LEO2D_RB_CASE(W, P, U) \

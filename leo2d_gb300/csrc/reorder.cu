@@ -135,9 +135,10 @@ __global__ void k_perm_lengths(const int64_t* __restrict__ rp, const int32_t* __
 // One warp per permuted row: copy entries in their original order, columns renumbered.
 __global__ void k_perm_fill(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
                             const float* __restrict__ v32, const double* __restrict__ v64,
-                            const int32_t* __restrict__ new2old, const int32_t* __restrict__ old2new,
-                            const int64_t* __restrict__ prp, int64_t n, int32_t* __restrict__ pcol,
-                            float* __restrict__ pv32, double* __restrict__ pv64, uint2* __restrict__ pent) {
+                            const float* __restrict__ im32, const int32_t* __restrict__ new2old,
+                            const int32_t* __restrict__ old2new, const int64_t* __restrict__ prp, int64_t n,
+                            int32_t* __restrict__ pcol, float* __restrict__ pv32, double* __restrict__ pv64,
+                            float* __restrict__ pim32, uint2* __restrict__ pent) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
@@ -149,6 +150,7 @@ __global__ void k_perm_fill(const int64_t* __restrict__ rp, const int32_t* __res
       pv32[o + (i - b)] = v32[i];
       pent[o + (i - b)] = make_uint2((unsigned)c, __float_as_uint(v32[i]));
       if (pv64) pv64[o + (i - b)] = v64[i];
+      if (pim32) pim32[o + (i - b)] = im32[i];
     }
   }
 }
@@ -227,10 +229,15 @@ void csr_build_reordered(leo2d_ctx* ctx, leo2d_csr* csr, double patch, bool with
   } else {
     csr->pval64.release();
   }
+  if (csr->complex_h) {
+    csr->pval_im32.alloc(nnz + kCsrPad);
+    LEO_CUDA(cudaMemsetAsync(csr->pval_im32.p + nnz, 0, kCsrPad * sizeof(float), ctx->stream));
+  }
   launch(ctx, "perm_fill", [&] {
     k_perm_fill<<<grid_for(n, 8, (int64_t)ctx->sm_count * 32), 256, 0, ctx->stream>>>(
-        csr->rowptr.p, csr->col.p, csr->val32.p, csr->val64.p, csr->new2old.p, csr->old2new.p,
-        csr->prow.p, n, csr->pcol.p, csr->pval32.p, with_fp64 ? csr->pval64.p : nullptr, csr->pent.p);
+        csr->rowptr.p, csr->col.p, csr->val32.p, csr->val64.p, csr->val_im32.p, csr->new2old.p, csr->old2new.p,
+        csr->prow.p, n, csr->pcol.p, csr->pval32.p, with_fp64 ? csr->pval64.p : nullptr,
+        csr->complex_h ? csr->pval_im32.p : nullptr, csr->pent.p);
   });
   ctx_sync(ctx);
   csr->reordered = true;
@@ -251,6 +258,7 @@ void csr_drop_reordered(leo2d_csr* csr) {
   csr->pval32.release();
   csr->pval64.release();
   csr->pent.release();
+  csr->pval_im32.release();
 }
 
 }  // namespace leo2d

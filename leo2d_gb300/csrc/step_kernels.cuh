@@ -641,16 +641,18 @@ __global__ void k_fill_phase(int64_t n, int C, T* __restrict__ x, uint64_t seed,
 }
 
 // Gaussian columns (Box-Muller on Philox).
+// (pairs: complex H, vector v in columns 2v (real part) and 2v + 1 (zero))
 template <typename T>
 __global__ void k_fill_gauss(int64_t n, int C, T* __restrict__ x, uint64_t seed, uint64_t first,
-                             int n_vec, const int32_t* __restrict__ new2old) {
+                             int n_vec, const int32_t* __restrict__ new2old, int pairs) {
   const int64_t total = n * C;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = new2old ? (int64_t)new2old[e / C] : e / C;
-    const int c = (int)(e % C);
+    const int cc = (int)(e % C);
+    const int c = pairs ? cc >> 1 : cc;
     T out = T(0);
-    if (c < n_vec) {
+    if (c < n_vec && !(pairs && (cc & 1))) {
       const uint64_t vv = first + (uint64_t)c;
       uint32_t ctr[4] = {(uint32_t)row, (uint32_t)((uint64_t)row >> 32), (uint32_t)vv, (uint32_t)(vv >> 32)};
       philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32));
@@ -666,25 +668,27 @@ __global__ void k_fill_gauss(int64_t n, int C, T* __restrict__ x, uint64_t seed,
 // Host vectors [R][n] (FP64) -> block columns.
 template <typename T>
 __global__ void k_fill_from(int64_t n, int C, T* __restrict__ x, const double* __restrict__ src,
-                            int n_vec, const int32_t* __restrict__ new2old) {
+                            int n_vec, const int32_t* __restrict__ new2old, int pairs) {
   const int64_t total = n * C;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = new2old ? (int64_t)new2old[e / C] : e / C;
-    const int c = (int)(e % C);
-    x[e] = c < n_vec ? (T)src[(int64_t)c * n + row] : T(0);
+    const int cc = (int)(e % C);
+    const int c = pairs ? cc >> 1 : cc;
+    x[e] = (c < n_vec && !(pairs && (cc & 1))) ? (T)src[(int64_t)c * n + row] : T(0);
   }
 }
 
 template <typename T>
 __global__ void k_fill_unit(int64_t n, int C, T* __restrict__ x, const int64_t* __restrict__ targets,
-                            int n_t, const int32_t* __restrict__ new2old) {
+                            int n_t, const int32_t* __restrict__ new2old, int pairs) {
   const int64_t total = n * C;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = new2old ? (int64_t)new2old[e / C] : e / C;
-    const int c = (int)(e % C);
-    x[e] = (c < n_t && targets[c] == row) ? T(1) : T(0);
+    const int cc = (int)(e % C);
+    const int c = pairs ? cc >> 1 : cc;
+    x[e] = (c < n_t && !(pairs && (cc & 1)) && targets[c] == row) ? T(1) : T(0);
   }
 }
 

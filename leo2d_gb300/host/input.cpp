@@ -164,7 +164,11 @@ bool parse_input(const std::string& path, JobSpec& spec, std::string& err) {
       } else if (key == "STRAIN_TYPE") {
         const std::string v = value();
         if (std::atoi(v.c_str()) != 0) spec.unsupported.push_back("STRAIN_TYPE = " + v);
-      } else if (key == "USE_B_FIELD" || key == "USE_E_FIELD" || key == "DIAGONALIZE" ||
+      } else if (key == "USE_B_FIELD") {
+        spec.use_b = std::atoi(value().c_str());
+      } else if (key == "B_FIELD") {
+        spec.b_field = std::atof(value().c_str());
+      } else if (key == "USE_E_FIELD" || key == "DIAGONALIZE" ||
                  key == "K_SAMPLING" || key == "MLMC" || key == "CHIRAL_ON" || key == "BALLISTIC_TRANSPORT" ||
                  key == "MAT_FROM_FILE" || key == "GLOBAL_SHIFTS_ON" || key == "UNIFORM_STRAIN" ||
                  key == "COND_POLY_PAR" || key == "MAT_SOC_ON") {
@@ -210,6 +214,12 @@ bool parse_input(const std::string& path, JobSpec& spec, std::string& err) {
     g.angles[s] = angles[s];
   }
   if (spec.target_sheets.empty()) spec.target_sheets.push_back(0);
+  // a magnetic field: the complex Hamiltonian of generateCpxH (locality.cpp:2906-2909)
+  if (spec.use_b == 1) {
+    g.b_field = spec.b_field;
+    if (g.boundary_condition != 0) spec.unsupported.push_back("USE_B_FIELD = 1 with BOUNDARY_CONDITION = 1");
+    if (spec.observable_type == 1) spec.unsupported.push_back("USE_B_FIELD = 1 with OBSERVABLE_TYPE = COND");
+  }
   return true;
 }
 

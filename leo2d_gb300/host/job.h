@@ -36,6 +36,8 @@ struct JobSpec {
   uint64_t seed = 0;
   int precision = -1;         // -1: the path's default (DOS FP64 as the reference, Kubo FP32)
   int bounds = 0;             // 0 = ENERGY_RESCALE/SHIFT as given, 1 = Gershgorin x 1.01
+  int use_b = 0;              // USE_B_FIELD: the complex Hamiltonian (generateCpxH)
+  double b_field = 0.0;       // B_FIELD, tesla
   int energies = 0;           // > 0: also write a DOS on this many equispaced energies
   int block = 0;
   std::vector<std::string> unsupported;  // keys that select paths outside this build

@@ -122,6 +122,8 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
   }
   uint32_t flags = 0;
   if (spec.observable_type == 1 || spec.matrix_save > 1) flags |= LEO2D_CSR_WITH_DX;
+  // generateCpxH's matrix save lists every stored pair, zeros included (locality.cpp:5213-5228)
+  if (spec.use_b == 1 && spec.matrix_save > 0) flags |= LEO2D_CSR_KEEP_ZEROS;
   Csr csr;
   CHECK(leo2d_build_csr(ctx.h, &g, flags, &csr.h));
   int64_t n = 0, nnz = 0, ni = 0, ne = 0;
@@ -170,12 +172,17 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     } else {
       cheb << "NO_TAR \n";
     }
+    if (spec.use_b == 1) {  // the field lines of the header (param_tools.cpp:572-575)
+      cheb << "MAG_ON  = " << spec.use_b << ", B = " << spec.b_field << " \n";
+      cheb << "ELEC_ON = " << 0 << ", E = " << 0.0 << " \n";
+    }
   }
 
   leo2d_kpm_cfg cfg{};
   cfg.poly_order = P;
+  // (the complex Hamiltonian of a magnetic field runs the FP32 recursion only)
   cfg.precision = spec.precision >= 0 ? spec.precision
-                                      : (spec.observable_type == 1 ? LEO2D_FP32 : LEO2D_FP64);
+                                      : ((spec.observable_type == 1 || spec.use_b == 1) ? LEO2D_FP32 : LEO2D_FP64);
   cfg.block = spec.block;
   cfg.seed = spec.seed;
 
@@ -292,13 +299,21 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     }
     CHECK(leo2d_csr_download(ctx.h, csr.h, rp.data(), col.data(), val.data(),
                              dx.empty() ? nullptr : dx.data(), dy.empty() ? nullptr : dy.data()));
+    if (spec.use_b == 1) {  // generateCpxH's matrix save (locality.cpp:5213-5228): every entry, re and im
+      std::vector<double> im(nnz, 0.0);
+      if (spec.geom.b_field != 0.0) CHECK(leo2d_csr_download_imag(ctx.h, csr.h, im.data()));
+      std::ofstream f(join_path(out_dir, spec.job_name + "_matrix.dat"));
+      for (int64_t i = 0; i < n; ++i)
+        for (int64_t j = rp[i]; j < rp[i + 1]; ++j)
+          f << col[j] + 1 << ", " << i + 1 << ", " << val[j] << ", " << im[j] << "\n";
+    }
     auto dump = [&](const std::string& suffix, const std::vector<double>& v) {
       std::ofstream f(join_path(out_dir, spec.job_name + suffix));
       for (int64_t i = 0; i < n; ++i)
         for (int64_t j = rp[i]; j < rp[i + 1]; ++j)
           if (std::fabs(v[j]) > 1e-12) f << col[j] + 1 << ", " << i + 1 << ", " << v[j] << "\n";
     };
-    dump("_matrix.dat", val);
+    if (spec.use_b != 1) dump("_matrix.dat", val);
     if (spec.matrix_save > 1) {
       dump("_dxH_matrix.dat", dx);
       dump("_dyH_matrix.dat", dy);

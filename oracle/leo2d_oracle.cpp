@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -689,6 +690,151 @@ void oracle_kpm_trace(int64_t n, const int64_t* rp, const int32_t* col, const do
         mu[2 * j] = 2 * an_an - mu[0];
         mu[2 * j + 1] = 2 * anp_an - mu[1];
       }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- complex H (magnetic field)
+
+void oracle_peierls(int64_t n, const int64_t* rp, const int32_t* col, const double* val, const double* pos,
+                    double B, double* re, double* im) {
+  for (int64_t r = 0; r < n; ++r) {
+    const double x1 = pos[3 * r], y1 = pos[3 * r + 1];
+    for (int64_t e = rp[r]; e < rp[r + 1]; ++e) {
+      const int64_t c = col[e];
+      const double x2 = pos[3 * c], y2 = pos[3 * c + 1];
+      // Locality::peierlsPhase (locality.cpp:7157-7161), then std::polar(t, phase)
+      const double pre = 3.14e-5;
+      const double phase = pre * B * (x2 - x1) * (0.5) * (y1 + y2);
+      const std::complex<double> z = std::polar(val[e], phase);
+      // v_c starts at 0 and zero couplings are skipped (locality.cpp:4928-4941)
+      const std::complex<double> v = z != std::complex<double>(0.0) ? std::complex<double>(0.0) + z
+                                                                    : std::complex<double>(0.0);
+      re[e] = v.real();
+      im[e] = v.imag();
+    }
+  }
+}
+
+namespace {
+using cplx = std::complex<double>;
+// SpMatrix::vectorMultiply, complex loop form (spmatrix.cpp:397-409)
+void zspmv(int64_t n, const int64_t* rp, const int32_t* col, const cplx* v, const cplx* in, cplx* out,
+           cplx alpha, cplx beta) {
+  for (int64_t r = 0; r < n; ++r) {
+    cplx s(0, 0);
+    for (int64_t i = rp[r]; i < rp[r + 1]; ++i) s += in[col[i]] * v[i];
+    out[r] = alpha * s + beta * out[r];
+  }
+}
+std::vector<cplx> zvals(int64_t nnz, const double* re, const double* im) {
+  std::vector<cplx> v((size_t)nnz);
+  for (int64_t e = 0; e < nnz; ++e) v[e] = cplx(re[e], im[e]);
+  return v;
+}
+}  // namespace
+
+void oracle_kpm_trace_cpx(int64_t n, const int64_t* rp, const int32_t* col, const double* re,
+                          const double* im, int32_t R, const double* vectors, int32_t P, double* mu_out) {
+  const std::vector<cplx> V = zvals(rp[n], re, im);
+  std::vector<cplx> Tp(n), Tj(n), Tn(n);
+  for (int t = 0; t < R; ++t) {
+    const double* v = vectors + (size_t)t * n;
+    double* mu = mu_out + (size_t)t * P;
+    for (int64_t i = 0; i < n; ++i) Tp[i] = v[i];
+    std::fill(Tj.begin(), Tj.end(), cplx(0.0));
+    zspmv(n, rp, col, V.data(), Tp.data(), Tj.data(), 1, 0);
+    std::fill(Tn.begin(), Tn.end(), cplx(0.0));
+    cplx s = 0.0;
+    for (int64_t i = 0; i < n; ++i) s += v[i] * v[i];
+    mu[0] = s.real();
+    s = 0.0;
+    for (int64_t i = 0; i < n; ++i) s += Tj[i] * v[i];
+    mu[1] = s.real();
+    zspmv(n, rp, col, V.data(), Tj.data(), Tn.data(), 2, 0);
+    for (int64_t c = 0; c < n; ++c) Tn[c] = Tn[c] - Tp[c];
+    for (int j = 2; j < P / 2; ++j) {
+      for (int64_t c = 0; c < n; ++c) { Tp[c] = Tj[c]; Tj[c] = Tn[c]; }
+      s = 0.0;
+      for (int64_t i = 0; i < n; ++i) s += Tj[i] * v[i];
+      mu[j] = s.real();
+      zspmv(n, rp, col, V.data(), Tj.data(), Tn.data(), 2, 0);
+      for (int64_t c = 0; c < n; ++c) Tn[c] = Tn[c] - Tp[c];
+      if (j >= P / 4) {
+        double an_an = 0, anp_an = 0;
+        for (int64_t c = 0; c < n; ++c) {
+          an_an += (std::conj(Tj[c]) * Tj[c]).real();
+          anp_an += (std::conj(Tn[c]) * Tj[c]).real();
+        }
+        mu[2 * j] = 2 * an_an - mu[0];
+        mu[2 * j + 1] = 2 * anp_an - mu[1];
+      }
+    }
+  }
+}
+
+void oracle_kpm_ldos_cpx(int64_t n, const int64_t* rp, const int32_t* col, const double* re,
+                         const double* im, const int64_t* targets, int64_t T, int32_t P, double* mu_out) {
+  const std::vector<cplx> V = zvals(rp[n], re, im);
+  std::vector<cplx> Tp(n), Tj(n), Tn(n);
+  for (int64_t t = 0; t < T; ++t) {
+    const int64_t ti = targets[t];
+    double* mu = mu_out + (size_t)t * P;
+    std::fill(Tp.begin(), Tp.end(), cplx(0.0));
+    Tp[ti] = 1.0;
+    std::fill(Tj.begin(), Tj.end(), cplx(0.0));
+    zspmv(n, rp, col, V.data(), Tp.data(), Tj.data(), 1, 0);
+    std::fill(Tn.begin(), Tn.end(), cplx(0.0));
+    mu[0] = 1;
+    mu[1] = Tj[ti].real();
+    zspmv(n, rp, col, V.data(), Tj.data(), Tn.data(), 2, 0);
+    for (int64_t c = 0; c < n; ++c) Tn[c] = Tn[c] - Tp[c];
+    for (int j = 2; j < P / 2; ++j) {
+      for (int64_t c = 0; c < n; ++c) { Tp[c] = Tj[c]; Tj[c] = Tn[c]; }
+      mu[j] = Tj[ti].real();
+      zspmv(n, rp, col, V.data(), Tj.data(), Tn.data(), 2, 0);
+      for (int64_t c = 0; c < n; ++c) Tn[c] = Tn[c] - Tp[c];
+      if (j >= P / 4) {
+        double an_an = 0, anp_an = 0;
+        for (int64_t c = 0; c < n; ++c) {
+          an_an += (std::conj(Tj[c]) * Tj[c]).real();
+          anp_an += (std::conj(Tn[c]) * Tj[c]).real();
+        }
+        mu[2 * j] = 2 * an_an - mu[0];
+        mu[2 * j + 1] = 2 * anp_an - mu[1];
+      }
+    }
+  }
+}
+
+void oracle_kpm_trace_cpx_doubling(int64_t n, const int64_t* rp, const int32_t* col, const double* re,
+                                   const double* im, int32_t R, const double* vre, const double* vim,
+                                   int32_t P, double* mu_out) {
+  const std::vector<cplx> V = zvals(rp[n], re, im);
+  std::vector<cplx> Tp(n), Tj(n), Tn(n);
+  for (int t = 0; t < R; ++t) {
+    double* mu = mu_out + (size_t)t * P;
+    for (int64_t i = 0; i < n; ++i) Tj[i] = cplx(vre[(size_t)t * n + i], vim[(size_t)t * n + i]);  // T_0
+    std::fill(Tn.begin(), Tn.end(), cplx(0.0));
+    zspmv(n, rp, col, V.data(), Tj.data(), Tn.data(), 1, 0);  // T_1
+    double mu0 = 0, mu1 = 0;
+    for (int64_t c = 0; c < n; ++c) {
+      mu0 += (std::conj(Tj[c]) * Tj[c]).real();
+      mu1 += (std::conj(Tn[c]) * Tj[c]).real();
+    }
+    mu[0] = mu0;
+    mu[1] = mu1;
+    for (int k = 1; k < P / 2; ++k) {
+      for (int64_t c = 0; c < n; ++c) { Tp[c] = Tj[c]; Tj[c] = Tn[c]; }
+      zspmv(n, rp, col, V.data(), Tj.data(), Tn.data(), 2, 0);
+      for (int64_t c = 0; c < n; ++c) Tn[c] = Tn[c] - Tp[c];
+      double an_an = 0, anp_an = 0;
+      for (int64_t c = 0; c < n; ++c) {
+        an_an += (std::conj(Tj[c]) * Tj[c]).real();
+        anp_an += (std::conj(Tn[c]) * Tj[c]).real();
+      }
+      mu[2 * k] = 2 * an_an - mu0;
+      mu[2 * k + 1] = 2 * anp_an - mu1;
     }
   }
 }

@@ -54,6 +54,26 @@ void oracle_kpm_trace(int64_t n, const int64_t* rowptr, const int32_t* col, cons
 void oracle_kpm_trace_doubling(int64_t n, const int64_t* rowptr, const int32_t* col,
                                const double* val, int32_t R, const double* vectors, int32_t P,
                                double* mu_out);
+/* Complex Hamiltonian of a flake in a perpendicular field B (tesla), as
+ * Locality::generateCpxH builds it (locality.cpp:4485-5310) without SOC or
+ * k-sampling: every entry of the real H~ becomes std::polar(t, phi) with the
+ * Peierls phase phi = 3.14e-5 B (x_col - x_row) (y_row + y_col) / 2
+ * (Locality::peierlsPhase, locality.cpp:7157-7161). pos [n][3]. */
+void oracle_peierls(int64_t n, const int64_t* rowptr, const int32_t* col, const double* val,
+                    const double* pos, double B, double* re, double* im);
+/* computeDosTraceKPM's complex branch (locality.cpp:6240-6346), literal: real
+ * start vectors [R][n]. */
+void oracle_kpm_trace_cpx(int64_t n, const int64_t* rowptr, const int32_t* col, const double* re,
+                          const double* im, int32_t R, const double* vectors, int32_t P, double* mu_out);
+/* computeDosKPM's complex branch (locality.cpp:6043-6136): unit start vectors. */
+void oracle_kpm_ldos_cpx(int64_t n, const int64_t* rowptr, const int32_t* col, const double* re,
+                         const double* im, const int64_t* targets, int64_t T, int32_t P, double* mu_out);
+/* Complex recursion from complex start vectors (vre + i vim, [R][n]) with every
+ * moment from the doubling identities mu_{2k} = 2<T_k|T_k> - mu_0,
+ * mu_{2k+1} = 2 Re<T_{k+1}|T_k> - mu_1: the form the GPU kernel evaluates. */
+void oracle_kpm_trace_cpx_doubling(int64_t n, const int64_t* rowptr, const int32_t* col, const double* re,
+                                   const double* im, int32_t R, const double* vre, const double* vim,
+                                   int32_t P, double* mu_out);
 /* Locality::computeDosKPM (locality.cpp:5945-6036): unit start vectors at targets. */
 void oracle_kpm_ldos(int64_t n, const int64_t* rowptr, const int32_t* col, const double* val,
                      const int64_t* targets, int64_t T, int32_t P, double* mu_out);

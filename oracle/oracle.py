@@ -140,6 +140,49 @@ def kpm_trace(rowptr, col, val, vectors, P, literal=True):
     return mu
 
 
+def peierls(rowptr, col, val, pos, B):
+    """Complex H~ of a flake in the field B (tesla): (re, im) per entry."""
+    rowptr = np.ascontiguousarray(rowptr, np.int64)
+    col = np.ascontiguousarray(col, np.int32)
+    val = np.ascontiguousarray(val, np.float64)
+    pos = np.ascontiguousarray(pos, np.float64).reshape(-1)
+    re, im = np.zeros(len(val)), np.zeros(len(val))
+    lib().oracle_peierls(ctypes.c_int64(len(rowptr) - 1), _p(rowptr), _p(col), _p(val), _p(pos),
+                         ctypes.c_double(B), _p(re), _p(im))
+    return re, im
+
+
+def kpm_trace_cpx(rowptr, col, re, im, vectors, P):
+    """computeDosTraceKPM's complex branch with real start vectors [R][n]."""
+    args = [np.ascontiguousarray(x, t) for x, t in ((rowptr, np.int64), (col, np.int32), (re, np.float64),
+                                                    (im, np.float64), (vectors, np.float64))]
+    R = args[4].shape[0]
+    mu = np.zeros((R, P))
+    lib().oracle_kpm_trace_cpx(ctypes.c_int64(len(rowptr) - 1), *(_p(a) for a in args[:4]), ctypes.c_int32(R),
+                               _p(args[4]), ctypes.c_int32(P), _p(mu))
+    return mu
+
+
+def kpm_ldos_cpx(rowptr, col, re, im, targets, P):
+    args = [np.ascontiguousarray(x, t) for x, t in ((rowptr, np.int64), (col, np.int32), (re, np.float64),
+                                                    (im, np.float64), (targets, np.int64))]
+    mu = np.zeros((len(targets), P))
+    lib().oracle_kpm_ldos_cpx(ctypes.c_int64(len(rowptr) - 1), *(_p(a) for a in args[:5]),
+                              ctypes.c_int64(len(targets)), ctypes.c_int32(P), _p(mu))
+    return mu
+
+
+def kpm_trace_cpx_doubling(rowptr, col, re, im, vre, vim, P):
+    """Complex recursion from complex start vectors, every moment by doubling."""
+    args = [np.ascontiguousarray(x, t) for x, t in ((rowptr, np.int64), (col, np.int32), (re, np.float64),
+                                                    (im, np.float64), (vre, np.float64), (vim, np.float64))]
+    R = args[4].shape[0]
+    mu = np.zeros((R, P))
+    lib().oracle_kpm_trace_cpx_doubling(ctypes.c_int64(len(rowptr) - 1), *(_p(a) for a in args[:4]),
+                                        ctypes.c_int32(R), _p(args[4]), _p(args[5]), ctypes.c_int32(P), _p(mu))
+    return mu
+
+
 def kpm_ldos(rowptr, col, val, targets, P):
     rowptr = np.ascontiguousarray(rowptr, np.int64)
     col = np.ascontiguousarray(col, np.int32)

@@ -130,6 +130,8 @@ static int dump_main(int argc, char** argv) {
       if (key == "ENERGY_RESCALE") opts.setParam("energy_rescale", std::atof(val(2).c_str()));
       if (key == "ENERGY_SHIFT") opts.setParam("energy_shift", std::atof(val(2).c_str()));
       if (key == "POLY_ORDER") opts.setParam("poly_order", std::atoi(val(2).c_str()));
+      if (key == "USE_B_FIELD") opts.setParam("magOn", std::atoi(val(2).c_str()));
+      if (key == "B_FIELD") opts.setParam("B", std::atof(val(2).c_str()));
       if (key == "SOLVER_TYPE" && val(2) == "SQ") opts.setParam("solver_type", 1);
       if (key == "OBSERVABLE_TYPE") {
         if (val(2) == "DOS") opts.setParam("observable_type", 0);
@@ -261,9 +263,21 @@ static int dump_main(int argc, char** argv) {
   std::vector<int> cir(N + 1, 0);
   SpMatrix H, dxH, dyH;
   std::vector<double> a0x((size_t)num_targets * N + 1), a0y((size_t)num_targets * N + 1);
-  loc.generateRealH(H, dxH, dyH, a0x.data(), a0y.data(), job, index_to_grid.data(), i2pos.data(),
-                    inter_pairs.data(), inter_sc, intra_pairs.data(), intra_t.data(), intra_sc,
-                    strain, cir, N);
+  // a magnetic field makes the worker build the complex Hamiltonian
+  // (locality.cpp:2906-2909, 3061-3071): generateCpxH with no SOC terms
+  const bool cpx = O.getInt("magOn") == 1;
+  if (cpx) {
+    SpMatrix jbx, jby, jtx, jty, jtbx, jtby;
+    std::vector<std::vector<int>> soc_pairs;
+    std::vector<std::complex<double>> soc_terms;
+    loc.generateCpxH(H, dxH, dyH, jbx, jby, jtx, jty, jtbx, jtby, a0x.data(), a0y.data(), job,
+                     index_to_grid.data(), i2pos.data(), inter_pairs.data(), inter_sc, intra_pairs.data(),
+                     intra_t.data(), soc_pairs, soc_terms, intra_sc, strain, cir, N);
+  } else {
+    loc.generateRealH(H, dxH, dyH, a0x.data(), a0y.data(), job, index_to_grid.data(), i2pos.data(),
+                      inter_pairs.data(), inter_sc, intra_pairs.data(), intra_t.data(), intra_sc,
+                      strain, cir, N);
+  }
 
   const int nnz = H.rowPointer[N];
   int meta[8] = {N, nnz, loc.max_intra_pairs, loc.max_inter_pairs, num_targets,
@@ -279,9 +293,19 @@ static int dump_main(int argc, char** argv) {
   dump(outdir, "inter_sc", inter_scf.data(), inter_scf.size());
   dump(outdir, "rowptr", H.rowPointer, (size_t)N + 1);
   dump(outdir, "col", H.colIndex, (size_t)nnz);
-  dump(outdir, "val", H.val, (size_t)nnz);
-  dump(outdir, "val_dx", dxH.val, (size_t)nnz);
-  dump(outdir, "val_dy", dyH.val, (size_t)nnz);
+  if (cpx) {
+    std::vector<double> re((size_t)nnz), im((size_t)nnz);
+    for (int e = 0; e < nnz; ++e) {
+      re[e] = H.val_c[e].real();
+      im[e] = H.val_c[e].imag();
+    }
+    dump(outdir, "val", re.data(), re.size());
+    dump(outdir, "val_im", im.data(), im.size());
+  } else {
+    dump(outdir, "val", H.val, (size_t)nnz);
+    dump(outdir, "val_dx", dxH.val, (size_t)nnz);
+    dump(outdir, "val_dy", dyH.val, (size_t)nnz);
+  }
   dump(outdir, "targets", tl.data(), tl.size());
   if (!disregistry.empty()) dump(outdir, "shift_configs", disregistry.data(), disregistry.size());
 

@@ -74,7 +74,16 @@ def parse_in(name):
                 kv["P"] = int(v(2))
             elif key == "TARGET_SHEETS":
                 kv["target_sheets"] = [int(v(2)) - 1]
+            elif key == "USE_B_FIELD":
+                kv["use_b"] = int(v(2))
+            elif key == "B_FIELD":
+                kv["b_field"] = float(v(2))
+    if kv.get("use_b"):
+        g.b_field = kv.get("b_field", 0.0)
     return g, kv
 
 
-CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+ALL = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+# real Hamiltonians (generateRealH) and complex ones in a magnetic field (generateCpxH)
+CASES = [c for c in ALL if "bfield" not in c]
+BFIELD_CASES = [c for c in ALL if "bfield" in c]

@@ -3,7 +3,7 @@
 Run in the build container (it needs the reference sources, compiled by
 `make -f oracle/Makefile.ref`):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [name ...]   # default: every input
 
 For every LEO2D input in tests/golden/inputs/ it runs
   * oracle/_ref/ref_dump  - the reference's geometry, generateRealH and KPM
@@ -45,7 +45,7 @@ def run_dump(inp, name):
             out[key] = np.fromfile(os.path.join(d, f), dtype=dt)
     meta = out["meta"]
     is_cond = meta[7] == 1
-    if not is_cond:
+    if not is_cond and "val_im" not in out:
         # dxH / dyH only matter for the conductivity fixtures
         out.pop("val_dx", None)
         out.pop("val_dy", None)
@@ -74,6 +74,8 @@ def main():
     if not os.path.exists(os.path.join(REF_DIR, "ref_dump")):
         sys.exit("build the reference first: make -f oracle/Makefile.ref -j8")
     inputs = sorted(f for f in os.listdir(os.path.join(HERE, "inputs")) if f.endswith(".in"))
+    if len(sys.argv) > 1:
+        inputs = [f for f in inputs if f[:-3] in sys.argv[1:]]
     for f in inputs:
         name = f[:-3]
         inp = os.path.join(HERE, "inputs", f)

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from leo2d_gb300 import _abi
-from tests._golden import CASES, GOLDEN, parse_in
+from tests._golden import BFIELD_CASES, CASES, GOLDEN, parse_in
 
 
 def _parse(path):
@@ -36,11 +36,29 @@ def test_geometry_matches_fixture_spec(name):
 
 def test_unsupported_options_are_reported(tmp_path):
     p = tmp_path / "x.in"
-    p.write_text("NUM_SHEETS = 1\nSTART_SHEET 1\nMATERIAL = MoS2\nEND_SHEET 1\nUSE_B_FIELD = 1\n"
+    p.write_text("NUM_SHEETS = 1\nSTART_SHEET 1\nMATERIAL = MoS2\nEND_SHEET 1\nUSE_E_FIELD = 1\n"
                  "STRAIN_TYPE = 2\nPOLY_ORDER = 30\nSOLVER_TYPE = LC\n")
     st, g, ints, msg = _parse(p)
     assert st == 0
-    assert ints[7] == 4 and "MoS2" in msg and "USE_B_FIELD" in msg and "STRAIN_TYPE" in msg
+    assert ints[7] == 4 and "MoS2" in msg and "USE_E_FIELD" in msg and "STRAIN_TYPE" in msg
+
+
+@pytest.mark.parametrize("name", BFIELD_CASES)
+def test_magnetic_field_inputs(name):
+    """USE_B_FIELD = 1 with B_FIELD: the complex Hamiltonian's field reaches the geometry."""
+    st, g, ints, msg = _parse(os.path.join(GOLDEN, "inputs", name + ".in"))
+    assert st == 0 and ints[7] == 0, msg
+    ref, kv = parse_in(name)
+    assert g.b_field == kv["b_field"] == 1500.0
+    assert bytes(g) == bytes(ref)
+
+
+def test_magnetic_field_limits(tmp_path):
+    p = tmp_path / "x.in"
+    p.write_text("NUM_SHEETS = 1\nSTART_SHEET 1\nMATERIAL = Graphene\nEND_SHEET 1\nBOUNDARY_CONDITION = 1\n"
+                 "SUPERCELL_M_N = 2 3\nUSE_B_FIELD = 1\nB_FIELD = 10\nPOLY_ORDER = 32\n")
+    st, g, ints, msg = _parse(p)
+    assert st == 0 and ints[7] == 1 and "BOUNDARY_CONDITION" in msg
 
 
 def test_missing_file():

@@ -122,3 +122,50 @@ def test_dct_matches_scipy():
     ref = scipy.dct(g * mu, type=3)
     ref = ref / (np.pi * np.sqrt(1.0 - np.cos((np.arange(P) + 0.5) * np.pi / P) ** 2))
     np.testing.assert_allclose(dos, ref, rtol=1e-11, atol=1e-12)
+
+
+# ---------------------------------------------------------------- magnetic field (generateCpxH)
+
+from tests._golden import BFIELD_CASES  # noqa: E402
+
+
+@pytest.fixture(scope="module", params=BFIELD_CASES)
+def bcase(request):
+    name = request.param
+    gold = load(name)
+    g, kv = parse_in(name)
+    return name, gold, oracle.Built(g), kv
+
+
+def test_bfield_csr(bcase):
+    """Structure of the real H; every value std::polar(t, Peierls phase)."""
+    name, gold, b, kv = bcase
+    assert np.array_equal(b.rowptr, gold["rowptr"].astype(np.int64))
+    assert np.array_equal(b.col, gold["col"])
+    re, im = oracle.peierls(b.rowptr, b.col, b.val, b.pos, kv["b_field"])
+    np.testing.assert_array_equal(re, gold["val"])
+    np.testing.assert_array_equal(im, gold["val_im"])
+    assert np.abs(im).max() > 0.05 * np.abs(re).max()  # the field really twists the hoppings
+
+
+def test_bfield_moments(bcase):
+    name, gold, b, kv = bcase
+    meta = gold["meta"]
+    P, trace = int(meta[5]), int(meta[6])
+    re, im = oracle.peierls(b.rowptr, b.col, b.val, b.pos, kv["b_field"])
+    if trace == 1:
+        R = int(meta[4])
+        vec = oracle.reference_gaussian(R, b.n)
+        ref = gold["moments"].reshape(R, P)
+        mu = oracle.kpm_trace_cpx(b.rowptr, b.col, re, im, vec, P)
+        np.testing.assert_allclose(mu, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+        mu2 = oracle.kpm_trace_cpx_doubling(b.rowptr, b.col, re, im, vec, np.zeros_like(vec), P)
+        np.testing.assert_allclose(mu2, ref, rtol=0, atol=1e-11 * np.abs(ref).max())
+        # the field changes the moments
+        mu0 = oracle.kpm_trace(b.rowptr, b.col, b.val, vec, P)
+        assert np.abs(mu0 - ref).max() > 1e-4 * np.abs(ref).max()
+    else:
+        tg = gold["targets"].astype(np.int64)
+        ref = gold["moments"].reshape(len(tg), P)
+        mu = oracle.kpm_ldos_cpx(b.rowptr, b.col, re, im, tg, P)
+        np.testing.assert_allclose(mu, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
