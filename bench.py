@@ -410,6 +410,70 @@ def run_periodic(args):
     ctx.close()
 
 
+def run_bfield(args):
+    """The headline flake in a perpendicular field (complex Hamiltonian, Peierls phases):
+    one DOS of 16 random-phase vectors (32 columns), P = 1024, FP32 complex row-block step;
+    against the same recursion in FP64 on the CPU oracle for a 162k-orbital flake."""
+    import torch
+    import leo2d_gb300 as L
+    from oracle import oracle
+    B = 20.0
+    ctx = L.Context(0)
+    g = geom(L, radius=args.radius)
+    g.b_field = B
+    t0 = time.perf_counter()
+    csr = ctx.build_csr(ctx.prepare(g))
+    lo, hi = csr.bounds()
+    a, b = 1.01 * (hi - lo) / 2, (hi + lo) / 2
+    csr.rescale(a, -b)
+    t_build = time.perf_counter() - t0
+    n, nnz = csr.n, csr.nnz
+    cfg = L.kpm_cfg(P, R=16, seed=7)
+    stream = torch.cuda.ExternalStream(ctx.lib.leo2d_ctx_stream(ctx.h))
+    E = energies(a, b)
+    dos = lambda mu: ctx.dos_reconstruct(mu.mean(axis=0), E, a, b, 1.0 / n)
+    csr.kpm_dos(cfg)  # builds the ordered copy and the row blocks (untimed)
+    ctx.reset_stats()
+    ctx.set_profiling(True)
+    l0 = ctx.launch_count()
+    t, d = _timed(stream, lambda: dos(csr.kpm_dos(cfg)), args.steps, args.warmup)
+    launches = (ctx.launch_count() - l0) // (args.steps + args.warmup)
+    k_n, k_ms = ctx.kernel_stats("cheb_step")
+    ctx.set_profiling(False)
+    step_ms = k_ms / k_n
+    # complex H: (col, re, im) per entry, 32 FP32 columns (16 complex vectors)
+    bytes_step = nnz * 12 + (n + 1) * 8 + 3 * n * 32 * 4
+    peak, peak_kind = peaks()
+    # parity on a 162k-orbital flake of the same model and field: FP32 GPU vs FP64 CPU oracle
+    gs = geom(L, radius=260.0)
+    gs.b_field = B
+    cs = ctx.build_csr(ctx.prepare(gs))
+    los, his = cs.bounds()
+    cs.rescale(1.01 * (his - los) / 2, -(his + los) / 2)
+    Ps, Rs = 256, 2
+    ms = cs.kpm_dos(L.kpm_cfg(Ps, R=Rs, seed=5))
+    rp, col, val = cs.download()
+    im = cs.download_imag()
+    vr, vi = oracle.phase_vectors(5, 0, Rs, cs.n)
+    mo = oracle.kpm_trace_cpx_doubling(rp, col, val, im, vr, vi, Ps)
+    out = {"metric": "DOS in a magnetic field (complex H, P=1024, 16 vectors, FP32 recursion)",
+           "value": round(t, 6), "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": round(t * 1000, 3), "higher_is_better": False, "dtype": "fp32",
+           "data": "synthetic (geometry generated on the GPU; random-phase vectors, Philox)",
+           "config": {"workload": f"TBLG flake {TWIST_DEG} deg, R={args.radius:.0f} A, B={B} T, simple model, "
+                                  f"P={P}, 16 complex vectors, {N_E} energies",
+                      "orbitals": n, "nnz": nnz, "b_field_T": B},
+           "build_s": round(t_build, 3),
+           "roofline": {"bound": "hbm", "achieved": round(bytes_step / (step_ms / 1000) / 1e9, 1), "peak": peak,
+                        "unit": "GB/s", "frac": round(bytes_step / (step_ms / 1000) / 1e9 / peak, 4),
+                        "kernel": "k_cheb_rb complex", "bytes_per_launch": bytes_step,
+                        "launch_ms": round(step_ms, 4), "peak_kind": peak_kind},
+           "fp32_gpu_vs_fp64_oracle_moments_162k": float(np.abs(ms - mo).max() / np.abs(mo).max()),
+           "gpu_launches": int(launches)}
+    print(json.dumps(out))
+    ctx.close()
+
+
 def run_kubo(args):
     """Kubo sigma_xx(E): 1.5 deg flake of ~2M orbitals, 512 x 512 moments, 32 random-phase
     vectors (trace), FP32 recursion with FP64 moment products, 2001 energies. FP32 against
@@ -612,12 +676,13 @@ def main():
                     help="mlp workload: skip the training measurement (profiling the inference products)")
     ap.add_argument("--max-vectors", type=int, default=128)
     ap.add_argument("--workload", default="flake10m",
-                    choices=["flake10m", "batch32", "periodic", "kubo2m", "mlp"],
+                    choices=["flake10m", "batch32", "periodic", "kubo2m", "mlp", "bfield"],
                     help="flake10m: time-to-DOS on the 10M-orbital flake (the headline); batch32: 32 "
                          "flakes of 20k-500k orbitals in one batched, graph-replayed run; periodic: the "
                          "1.05 deg (31,32) supercell, P=4096, 64 vectors, FP32 vs FP64 per energy; kubo2m: "
                          "sigma_xx(E) of a 2M-orbital 1.5 deg flake, 512x512 moments, 32 vectors; mlp: the "
-                         "control variate's network (training steps, inference over the flake of --radius)")
+                         "control variate's network (training steps, inference over the flake of --radius); "
+                         "bfield: the flake of --radius in a 20 T field (complex Hamiltonian)")
     ap.add_argument("--step-kernel", type=int, default=-1, choices=[-1, 0, 1, 2, 3],
                     help="force the Chebyshev step kernel: 0 tiled gathers, 1 register gathers, 2 tensor cores, "
                          "3 row blocks (default: the autotuner's choice)")
@@ -635,6 +700,8 @@ def main():
         return run_kubo(args)
     if args.workload == "mlp" and args.impl == "ours":
         return run_mlp(args)
+    if args.workload == "bfield" and args.impl == "ours":
+        return run_bfield(args)
     ws, rank, local, pg = dist_setup()
     threads = os.cpu_count() or 1
 
