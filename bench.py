@@ -484,7 +484,8 @@ def run_kubo(args):
     ctx = L.Context(0)
     M, R, twist = 512, 32, 1.5
     radius = math.sqrt(2.0e6 / 2.398)
-    csr = ctx.build_csr(ctx.prepare(geom(L, radius=radius, twist=twist)), with_dx=True)
+    # no stored dxH: the trace moments build it inside the row-block step
+    csr = ctx.build_csr(ctx.prepare(geom(L, radius=radius, twist=twist)))
     lo, hi = csr.bounds()
     a, b = 1.01 * (hi - lo) / 2, (hi + lo) / 2
     csr.rescale(a, -b)
@@ -500,7 +501,9 @@ def run_kubo(args):
     ctx.set_profiling(True)
     csr.kpm_cond(cfg)
     ctx.set_profiling(False)
-    split = {k: round(ctx.kernel_stats(k)[1] / 1000.0, 4) for k in ("cheb_step", "cond_gemm")}
+    split = {k: round(ctx.kernel_stats(k)[1] / 1000.0, 4)
+             for k in ("cheb_step", "cond_gemm", "cond_gemm_sum", "x_hilo")}
+    steps_run = ctx.kernel_stats("cheb_step")[0]
     # FP32 vs FP64 oracle on a small flake
     small = ctx.build_csr(ctx.prepare(geom(L, radius=math.sqrt(2.0e4 / 2.398), twist=twist)), with_dx=True)
     slo, shi = small.bounds()
@@ -523,7 +526,7 @@ def run_kubo(args):
            "fp32_vs_fp64_oracle": {"orbitals": small.n, "moments": Ms,
                                    "mu_max_rel": float(np.abs(mu32 - mu64).max() / np.abs(mu64).max()),
                                    "sigma_max_rel": float(np.abs(s32 - s64).max() / np.abs(s64).max())},
-           "sigma_range": [float(s.min()), float(s.max())], "kernel_seconds": split,
+           "sigma_range": [float(s.min()), float(s.max())], "kernel_seconds": split, "step_launches": int(steps_run),
            "gpu_launches": int(launches)}
     print(json.dumps(out))
     ctx.close()

@@ -117,7 +117,11 @@ int64_t leo2d_ctx_launch_count(const leo2d_ctx* ctx);
  * jumps, default 4), "tile_warps" (8 or 24 warps per block of the tiled
  * kernel; 0 = chosen per block width, the default), "reorder" (locality ordering of the streamed matrix:
  * -1 = automatic for >= 1e5 orbitals with positions, 0 = off, 1 = on),
- * "reorder_patch_dA" (patch edge of that ordering in tenths of A, default 160). */
+ * "reorder_patch_dA" (patch edge of that ordering in tenths of A, default 160),
+ * "kubo_velocity" (trace Kubo moments: -1 = dxH built inside the row-block
+ * step from the flake's positions, the default where it applies; 0 = the
+ * stored dxH), "kubo_chunk" (trace Kubo moments: T_m vectors held at once,
+ * a multiple of 4; 0 = as many as device memory allows). */
 leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value);
 
 /* ---------------------------------------------------------------- geometry */
@@ -354,8 +358,11 @@ leo2d_status leo2d_kpm_dos_cv(leo2d_ctx* ctx, const leo2d_csr* csr, leo2d_mlp* m
  * Without targets (NULL): the stochastic trace mu_out[n][m] =
  * (1/R) sum_r Re <T_n J r | J T_m r> = Tr[J T_n J T_m] estimate, J = i dxH, over
  * cfg->num_vectors random-phase or Gaussian vectors. The recursion runs in
- * FP32; the moment GEMM accumulates in FP64 across K chunks. The matrix must
- * be built with LEO2D_CSR_WITH_DX. */
+ * FP32; the moment GEMM accumulates in FP64 across K chunks. The per-target
+ * form needs a matrix built with LEO2D_CSR_WITH_DX. The trace form on a
+ * flake with its geometry builds dxH inside the row-block step,
+ * (dxH)_ij = (x_i - x_j) H~_ij, and needs no stored dxH; elsewhere it needs
+ * LEO2D_CSR_WITH_DX too. */
 leo2d_status leo2d_kpm_cond(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg,
                             const int64_t* targets, int64_t num_targets, double* mu_out);
 /* Param_tools::matrixResponseTransform (param_tools.cpp:838-905), real case:

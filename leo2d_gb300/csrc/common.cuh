@@ -110,6 +110,8 @@ struct leo2d_ctx {
   int tile_warps = 0;         // warps per block of the tiled kernel (0 = per shape, 8 or 24)
   int reorder = -1;           // locality ordering: -1 auto, 0 off, 1 on
   double reorder_patch = 0.0;   // patch edge (A); 0: the step kernel's own (16 A; 32 A for row blocks)
+  int kubo_velocity = -1;     // Kubo trace: -1 D built in the row-block step where possible, 0 stored dxH
+  int64_t kubo_chunk = 0;     // Kubo trace: B-side moments held at once (0: as many as memory allows)
   leo2d::DevBuf<int> status;  // one int, reset before kernels that may set it
 };
 

@@ -17,6 +17,13 @@
 // and C = U B^T is one GEMM over K = n_orbitals x columns, FP32 tiles with
 // FP64 accumulation across K chunks. The reference never writes beta_{P-1}
 // (its loop stops at P-2); in the per-target form that column is left 0.
+//
+// The trace form on a flake runs on the row-block step (32 columns per pass,
+// locality-ordered rows) and stores no dxH: on a flake (dxH)_ij =
+// (x_i - x_j) H~_ij exactly as assembled (geom.cu), so the A-side step forms
+// D T_n from the gathers of the H~ T_n it computes anyway, with the rows' x
+// positions as FP32 (hi, lo) pairs. U is held whole; B is built in chunks of
+// moments, each chunk's product added into the columns of mu it covers.
 #include <cmath>
 #include <vector>
 
@@ -168,6 +175,108 @@ __global__ void k_cond_sigma(const double* __restrict__ mu, int M, const double*
   }
 }
 
+// x positions of the rows in the streamed order as FP32 pairs: hi = x rounded,
+// lo = (x - hi) rounded, so (hi_i - hi_j) + (lo_i - lo_j) is x_i - x_j to the
+// FP32 rounding of the difference (neighbours' hi parts subtract exactly).
+__global__ void k_x_hilo(int64_t n, const double* __restrict__ pos, const int32_t* __restrict__ new2old,
+                         float2* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = pos[3 * (int64_t)(new2old ? new2old[i] : i)] + 0.0;
+    const float hi = (float)x;
+    out[i] = make_float2(hi, (float)(x - (double)hi));
+  }
+}
+
+// Whether the trace moments can take the row-block path: a flake assembled
+// here (positions, no periodic images in dxH), the ordering allowed.
+bool velocity_in_step(const leo2d_ctx* ctx, const leo2d_csr* csr) {
+  return ctx->kubo_velocity != 0 && ctx->reorder != 0 && csr->has_geom && csr->geom.boundary_condition == 0 &&
+         csr->pos.p != nullptr && csr->nnz > 0 && !csr->complex_h;
+}
+
+// acc[n][m] += sum over the vectors of <D T_n D r, T_m r> (note the sign: a_0
+// = +D r here) on the row-block step; false when the row blocks do not fit
+// (the stored-dxH path runs instead).
+bool cond_trace_rows(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg, int P, double* acc) {
+  leo2d_csr* m = const_cast<leo2d_csr*>(csr);
+  StepShape s = choose_shape(ctx, csr, false, 32, 32, 0);
+  s.rb = true;
+  s.tc = false;
+  s.rb_window = false;
+  Recursion r;
+  r.setup(ctx, csr, s, 1);
+  if (!r.shape.rb || !r.use_perm || rb_stages(ctx, m, 16) < 2) return false;
+  StepShape sv = r.shape;
+  sv.rb_warps = 16;  // the velocity step's width
+  const size_t smem_v = rb_smem_bytes(ctx, m, 16);
+  const unsigned grid_v = rb_grid(ctx, csr, 16);
+  constexpr int C = 32;
+  const int64_t n = csr->n;
+  const size_t vec = (size_t)n * C;
+  DevBuf<float2> xhl((size_t)n);
+  launch(ctx, "x_hilo", [&] {
+    k_x_hilo<<<grid_for(n, 256), 256, 0, ctx->stream>>>(n, csr->pos.p, csr->new2old.p, xhl.p);
+  });
+  DevBuf<double> part((size_t)2 * std::max<unsigned>(ctx->sm_count, std::max(grid_v, r.grid)) * 2 * C);
+  DevBuf<float> U((size_t)P * vec), ta(vec), tb(vec), junk(vec);
+  // B-side moments held at once: the setting, else what fits next to U
+  int64_t mc = P;
+  if (ctx->kubo_chunk > 0) {
+    mc = std::min<int64_t>(P, ctx->kubo_chunk);
+  } else {
+    size_t fr = 0, tot = 0;
+    LEO_CUDA(cudaMemGetInfo(&fr, &tot));
+    const size_t reserve = (size_t)3 << 30;  // GEMM partials, ordering and launch scratch
+    const int64_t fit = fr > reserve ? (int64_t)((fr - reserve) / (vec * sizeof(float))) - 2 : 0;
+    if (fit < P) mc = fit >= 256 ? fit / 256 * 256 : fit / 4 * 4;
+    if (mc < 4) fail(LEO2D_ERR_OOM, "no room for the Kubo B-side vectors next to the A side");
+  }
+  DevBuf<float> Bc((size_t)(mc + 2) * vec);  // [carry T_{m0-2}, T_{m0-1}][T_{m0} ...]
+  const int group = cfg->vector_kind == LEO2D_VEC_PHASE ? 2 : 1;
+  const int per_block = C / group;
+  for (int64_t v0 = 0; v0 < cfg->num_vectors; v0 += per_block) {
+    const int nv = (int)std::min<int64_t>(per_block, cfg->num_vectors - v0);
+    if (cfg->vector_kind == LEO2D_VEC_PHASE) fill_phase(ctx, r, cfg->seed, cfg->first_vector + v0, nv);
+    else fill_gaussian(ctx, r, cfg->seed, cfg->first_vector + v0, nv);
+    const float* X0 = reinterpret_cast<const float*>(r.x0.p);
+    // a_0 = D r (its H~ r is not used)
+    rb_launch_step(ctx, csr, sv, grid_v, smem_v, X0, junk.p, nullptr, 1, 1.f, part.p, nullptr, nullptr, xhl.p,
+                   ta.p);
+    // A side: u_n = D T_n a_0 and T_{n+1} a_0 (over T_{n-1} a_0) from one launch
+    float* cur = ta.p;
+    float* nxt = tb.p;
+    for (int k = 0; k < P; ++k) {
+      rb_launch_step(ctx, csr, sv, grid_v, smem_v, cur, nxt, nullptr, k == 0 ? 1 : 0, k == 0 ? 1.f : 2.f, part.p,
+                     nullptr, nullptr, xhl.p, U.p + (size_t)k * vec);
+      std::swap(cur, nxt);
+    }
+    // B side in chunks: T_m in slot 2 + m - m0 (slots 0, 1: the previous chunk's last two)
+    for (int64_t m0 = 0; m0 < P; m0 += mc) {
+      const int64_t mn = std::min<int64_t>(mc, P - m0);
+      auto slot = [&](int64_t mm) { return Bc.p + (size_t)(2 + mm - m0) * vec; };
+      for (int64_t mm = m0; mm < m0 + mn; ++mm) {
+        if (mm == 0)
+          LEO_CUDA(cudaMemcpyAsync(slot(0), X0, vec * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+        else if (mm == 1)
+          rb_launch_step(ctx, csr, r.shape, r.grid, r.dyn_smem, slot(0), slot(1), nullptr, 1, 1.f, part.p,
+                         nullptr, nullptr);
+        else
+          rb_launch_step(ctx, csr, r.shape, r.grid, r.dyn_smem, slot(mm - 1), slot(mm), slot(mm - 2), 0, 2.f,
+                         part.p, nullptr, nullptr);
+      }
+      // mu[:, m0:m0+mn] += U B_chunk^T (three TF32 products, FP64 sums)
+      tc_gemm_f32x3_acc(ctx, U.p, slot(m0), P, (int)mn, (int64_t)vec, acc + m0, P);
+      if (m0 + mn < P) {
+        LEO_CUDA(cudaMemcpyAsync(Bc.p, slot(m0 + mn - 2), vec * sizeof(float), cudaMemcpyDeviceToDevice,
+                                 ctx->stream));
+        LEO_CUDA(cudaMemcpyAsync(Bc.p + vec, slot(m0 + mn - 1), vec * sizeof(float), cudaMemcpyDeviceToDevice,
+                                 ctx->stream));
+      }
+    }
+  }
+  return true;
+}
+
 void gemm(leo2d_ctx* ctx, const float* A, const float* Bm, int M, int64_t K, int64_t lda, int64_t ldb,
           int64_t es, double* out) {
   const int tiles = ((M + kBM - 1) / kBM) * ((M + kBN - 1) / kBN);
@@ -193,7 +302,6 @@ leo2d_status leo2d_kpm_cond(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kp
     const int P = cfg->poly_order;
     LEO_REQUIRE(P >= 4 && P % 4 == 0, "poly_order must be a positive multiple of 4");
     LEO_REQUIRE(cfg->precision == LEO2D_FP32 || cfg->precision == LEO2D_FP64, "unknown precision");
-    LEO_REQUIRE(csr->dx64.p, "Kubo moments need dxH: build with LEO2D_CSR_WITH_DX");
     LEO_REQUIRE(!csr->complex_h, "Kubo moments are built for a real Hamiltonian (no magnetic field)");
     const bool local = targets != nullptr;
     if (local) {
@@ -208,6 +316,24 @@ leo2d_status leo2d_kpm_cond(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kp
     LEO_CUDA(cudaSetDevice(ctx->device));
     const bool fp64 = cfg->precision == LEO2D_FP64;
     LEO_REQUIRE(!fp64, "the Kubo recursion runs in FP32 (FP64 moments accumulate the GEMM)");
+    if (!local && velocity_in_step(ctx, csr)) {
+      DevBuf<double> acc((size_t)P * P);
+      LEO_CUDA(cudaMemsetAsync(acc.p, 0, sizeof(double) * P * P, ctx->stream));
+      if (cond_trace_rows(ctx, csr, cfg, P, acc.p)) {
+        ctx_check_status(ctx, "Kubo recursion");
+        // a_0 = +D r above: the sign of -D r goes into the mean
+        launch(ctx, "scale", [&] {
+          k_scale<<<grid_for((int64_t)P * P, 256), 256, 0, ctx->stream>>>(acc.p, (int64_t)P * P,
+                                                                          -1.0 / (double)cfg->num_vectors);
+        });
+        d2h(ctx, mu_out, acc.p, (size_t)P * P);
+        ctx_sync(ctx);
+        for (size_t i = 0; i < (size_t)P * P; ++i)
+          if (!std::isfinite(mu_out[i])) fail(LEO2D_ERR_NONFINITE, "non-finite conductivity moment");
+        return;
+      }
+    }
+    LEO_REQUIRE(csr->dx64.p, "Kubo moments need dxH: build with LEO2D_CSR_WITH_DX");
     const int group = (!local && cfg->vector_kind == LEO2D_VEC_PHASE) ? 2 : 1;
     const int64_t total_cols = local ? num_targets : (int64_t)cfg->num_vectors * group;
     StepShape shape = choose_shape(ctx, csr, false, (int)std::min<int64_t>(total_cols, 8),

@@ -315,6 +315,12 @@ leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value
     } else if (k == "reorder") {
       LEO_REQUIRE(value >= -1 && value <= 1, "reorder must be -1, 0 or 1");
       ctx->reorder = (int)value;
+    } else if (k == "kubo_velocity") {
+      LEO_REQUIRE(value == -1 || value == 0, "kubo_velocity must be -1 (built in the step) or 0 (stored dxH)");
+      ctx->kubo_velocity = (int)value;
+    } else if (k == "kubo_chunk") {
+      LEO_REQUIRE(value == 0 || (value >= 4 && value % 4 == 0), "kubo_chunk must be 0 or a multiple of 4");
+      ctx->kubo_chunk = value;
     } else if (k == "reorder_patch_dA") {
       LEO_REQUIRE(value == 0 || (value >= 5 && value <= 2000),
                   "reorder_patch_dA must be 0 (per step kernel) or 5..2000 (tenths of A)");

@@ -69,8 +69,9 @@ struct leo2d_csr {
   int64_t rb_slots = 0;               // slots stored (padded to multiples of 4 per block)
   int64_t rb_union = 0;               // slots before padding
   int rb_max_slots = 0;               // most slots of one block (before padding)
-  int rb_tile_warps = 0;              // tile width (blocks) of rb_tile_max_bytes
+  int rb_tile_warps = 0;              // tile width (blocks) of rb_tile_max_bytes (the last one asked for)
   int64_t rb_tile_max_bytes = 0;      // largest tile of rb_tile_warps blocks (data bytes)
+  int64_t rb_tile_bytes_w[5] = {};    // the same per tile width 8 w (w = 1..4), 0: not measured
   leo2d::DevBuf<int64_t> rb_off;      // [blocks + 1 + pad] first slot of each block
   leo2d::DevBuf<unsigned char> rb_data;  // 20 bytes per slot: columns, then the value panel
   leo2d::DevBuf<float> rb_im;         // [slots][4] imaginary value panel (complex_h)

@@ -66,6 +66,10 @@ struct RbArgs {
   const double* __restrict__ prev_partials;
   double* __restrict__ prev_dots;
   const float* __restrict__ im;  // complex H: [slots][4] imaginary panel
+  // velocity mode: x positions of the (ordered) rows as FP32 (hi, lo) pairs, and
+  // the output of J-free product D T_n with D_ij = (x_i - x_j) H~_ij
+  const float2* __restrict__ xhl;
+  float* __restrict__ out2;
   int stages;      // 2..4
   int chunk;       // consecutive tiles per block between grid-wide jumps
   int off_bytes;   // offsets region of a stage
@@ -76,7 +80,7 @@ struct RbArgs {
   int never_wait;  // test hook: wait on a barrier that nobody completes
 };
 
-template <int WARPS, bool PACKED, int U, bool CPX = false>
+template <int WARPS, bool PACKED, int U, bool CPX = false, bool DJ = false>
 __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant__ RbArgs a) {
   constexpr int C = 32;
   constexpr int NT = WARPS * 32;
@@ -206,9 +210,36 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
       const float4* wsg = reinterpret_cast<const float4*>(st + a.im_at) + (sb - off_s[b0 - ba]) + g;
       typename std::conditional<CPX, PanelAccCpx, PanelAcc<PACKED>>::type acc;
       acc.zero();
-      auto add = [&](const float4& x, int slot4) {
-        if constexpr (CPX) acc.add(x, vsg[slot4], wsg[slot4]);
-        else acc.add(x, vsg[slot4]);
+      // velocity mode: the block's row positions, and a second accumulator for
+      // D T_n, D_ij = (x_i - x_j) H~_ij built from the positions on the fly; the
+      // hi parts of neighbouring positions subtract exactly, so the difference
+      // keeps about FP64 accuracy
+      PanelAcc<false> accj;
+      float2 xr[4];
+      if constexpr (DJ) {
+        accj.zero();
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int64_t rk = rb * kRbRows + k;
+          xr[k] = rk < a.n ? __ldg(a.xhl + rk) : make_float2(0.f, 0.f);
+        }
+      }
+      auto add = [&](const float4& x, int slot4, uint32_t c) {
+        if constexpr (CPX) {
+          acc.add(x, vsg[slot4], wsg[slot4]);
+        } else {
+          const float4 v = vsg[slot4];
+          acc.add(x, v);
+          if constexpr (DJ) {
+            const float2 xc = __ldg(a.xhl + c);
+            const float4 w = make_float4(v.x * ((xr[0].x - xc.x) + (xr[0].y - xc.y)),
+                                         v.y * ((xr[1].x - xc.x) + (xr[1].y - xc.y)),
+                                         v.z * ((xr[2].x - xc.x) + (xr[2].y - xc.y)),
+                                         v.w * ((xr[3].x - xc.x) + (xr[3].y - xc.y)));
+            accj.add(x, w);
+          }
+        }
+        (void)c;
       };
       int b = 0;
       for (; b + U <= nb; b += U) {
@@ -221,7 +252,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
 #pragma unroll
         for (int u = 0; u < U; ++u) x[u] = ldg4(tq + (size_t)c[u] * C);
 #pragma unroll
-        for (int u = 0; u < U; ++u) add(x[u], 4 * (b + u));
+        for (int u = 0; u < U; ++u) add(x[u], 4 * (b + u), c[u]);
         (void)vb;
       }
       for (; b < nb; b += 4) {
@@ -234,28 +265,39 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
           x[u] = u < rem ? ldg4(tq + (size_t)(uint32_t)cb[4 * u] * C) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-          if (u < rem) add(x[u], 4 * (b + u));
+          if (u < rem) add(x[u], 4 * (b + u), (uint32_t)cb[4 * u]);
         (void)vb;
       }
       // reduce-scatter over the four groups: group g keeps row g
-      float p[4][4];
-      acc.get(p);
       const bool upper = g >= 2, odd = (g & 1) != 0;
-      float hh[2][4];
+      auto scatter = [&](const float (&p)[4][4], float (&h)[4]) {
+        float hh[2][4];
 #pragma unroll
-      for (int i = 0; i < 2; ++i)
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const float send = upper ? p[i][c] : p[2 + i][c];
+            const float keep = upper ? p[2 + i][c] : p[i][c];
+            hh[i][c] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+          }
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-          const float send = upper ? p[i][c] : p[2 + i][c];
-          const float keep = upper ? p[2 + i][c] : p[i][c];
-          hh[i][c] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+          const float send = odd ? hh[0][c] : hh[1][c];
+          const float keep = odd ? hh[1][c] : hh[0][c];
+          h[c] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
         }
+      };
       float h[4];
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const float send = odd ? hh[0][c] : hh[1][c];
-        const float keep = odd ? hh[1][c] : hh[0][c];
-        h[c] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+      {
+        float p[4][4];
+        acc.get(p);
+        scatter(p, h);
+      }
+      if constexpr (DJ) {
+        float p[4][4], hj[4];
+        accj.get(p);
+        scatter(p, hj);
+        if (ok) *reinterpret_cast<float4*>(a.out2 + row * C + 4 * q) = make_float4(hj[0], hj[1], hj[2], hj[3]);
       }
       if (ok) {
         const float4 xn = ldg4(tq + row * C);
@@ -478,6 +520,12 @@ int rb_off_bytes(int warps) { return ((warps + 4) * 8 + 127) / 128 * 128; }
 
 // Largest tile (data bytes) for tiles of `warps` row blocks (cached per width).
 int64_t rb_tile_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps) {
+  const bool slot = warps % 8 == 0 && warps >= 8 && warps <= 32;
+  if (slot && csr->rb_tile_bytes_w[warps / 8] > 0) {
+    csr->rb_tile_warps = warps;
+    csr->rb_tile_max_bytes = csr->rb_tile_bytes_w[warps / 8];
+    return csr->rb_tile_max_bytes;
+  }
   if (csr->rb_tile_warps == warps) return csr->rb_tile_max_bytes;
   DevBuf<unsigned long long> mx(1);
   LEO_CUDA(cudaMemsetAsync(mx.p, 0, sizeof(unsigned long long), ctx->stream));
@@ -491,6 +539,7 @@ int64_t rb_tile_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps) {
   ctx_sync(ctx);
   csr->rb_tile_warps = warps;
   csr->rb_tile_max_bytes = (int64_t)hm;
+  if (slot) csr->rb_tile_bytes_w[warps / 8] = (int64_t)hm;
   return csr->rb_tile_max_bytes;
 }
 
@@ -529,6 +578,7 @@ void csr_drop_rb(leo2d_csr* csr) {
   csr->rb_slots = 0;
   csr->rb_tile_warps = 0;
   csr->rb_tile_max_bytes = 0;
+  for (int64_t& b : csr->rb_tile_bytes_w) b = 0;
   csr->rb_off.release();
   csr->rb_data.release();
   csr->rb_im.release();
@@ -613,7 +663,7 @@ unsigned rb_grid(leo2d_ctx* ctx, const leo2d_csr* csr, int warps) {
 
 void rb_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape, unsigned grid, size_t smem,
                     const float* tn, float* tp, const float* tprev, int first, float alpha, double* partials,
-                    const double* prev_partials, double* prev_dots) {
+                    const double* prev_partials, double* prev_dots, const float2* xhl, float* out2) {
   leo2d_csr* m = const_cast<leo2d_csr*>(csr);
   RbArgs a{};
   a.n = csr->n;
@@ -640,10 +690,19 @@ void rb_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
   a.spin_limit = ctx->spin_limit;
   a.status = ctx->status.p;
   a.never_wait = ctx->test_unsatisfied_wait;
+  a.xhl = xhl;
+  a.out2 = out2;
   auto go = [&](auto kern, int warps) {
     LEO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     launch(ctx, "cheb_step", [&] { kern<<<grid, warps * 32, smem, ctx->stream>>>(a); });
   };
+  if (xhl) {
+    // the velocity step: T_{n+1} and D T_n from the same gathers
+    LEO_REQUIRE(out2 && !csr->complex_h, "the velocity step takes a real matrix and an output for D T_n");
+    // (16 warps: the second accumulator and the row positions fit the registers)
+    LEO_REQUIRE(w == 16, "the velocity row-block step runs 16 warps");
+    return go(k_cheb_rb<16, false, 4, false, true>, 16);
+  }
   if (csr->complex_h) {
     switch (w) {
       case 24: return go(k_cheb_rb<24, false, 4, true>, 24);

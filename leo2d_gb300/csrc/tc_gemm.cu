@@ -508,7 +508,7 @@ __global__ void __launch_bounds__(192, 1)
 
 // out[m][n] += sum over the K ranges of the FP64 partial tiles, fixed order.
 __global__ void k_f3_reduce(const double* __restrict__ partial, int M, int N, int m_tiles, int splits,
-                            double* __restrict__ out) {
+                            double* __restrict__ out, int64_t ldo) {
   const int64_t total = (int64_t)M * N;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int m = (int)(e / N), n = (int)(e % N);
@@ -516,7 +516,7 @@ __global__ void k_f3_reduce(const double* __restrict__ partial, int M, int N, in
     const size_t in_tile = (size_t)(m % F3_BM) * F3_BN + (n % F3_BN);
     double s = 0.0;
     for (int sp = 0; sp < splits; ++sp) s += partial[((size_t)tile * splits + sp) * F3_BM * F3_BN + in_tile];
-    out[e] += s;
+    out[(int64_t)m * ldo + n] += s;
   }
 }
 
@@ -539,7 +539,9 @@ void make_tmap_f32(CUtensorMap* map, const void* base, int64_t rows, int64_t col
   LEO_REQUIRE(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled rejected the tensor");
 }
 
-void tc_gemm_f32x3_acc(leo2d_ctx* ctx, const float* A, const float* B, int M, int N, int64_t K, double* out) {
+void tc_gemm_f32x3_acc(leo2d_ctx* ctx, const float* A, const float* B, int M, int N, int64_t K, double* out,
+                       int64_t ldo) {
+  if (ldo <= 0) ldo = N;
   LEO_REQUIRE(M > 0 && N > 0 && K > 0, "empty GEMM");
   LEO_REQUIRE(K % 4 == 0, "K must be a multiple of 4");
   LEO_REQUIRE((K + F3_BK - 1) / F3_BK * F3_BK < (1ll << 31), "K too large for TMA coordinates");
@@ -565,7 +567,7 @@ void tc_gemm_f32x3_acc(leo2d_ctx* ctx, const float* A, const float* B, int M, in
   launch(ctx, "cond_gemm", [&] { k_tc_gemm_f32x3<<<grid, 192, smem, ctx->stream>>>(ta, tb, g); });
   launch(ctx, "cond_gemm_sum", [&] {
     k_f3_reduce<<<grid_for((int64_t)M * N, 256, (int64_t)ctx->sm_count * 8), 256, 0, ctx->stream>>>(
-        partial.p, M, N, g.m_tiles, g.splits, out);
+        partial.p, M, N, g.m_tiles, g.splits, out, ldo);
   });
   ctx_check_status(ctx, "tensor-core FP32 product");
 }

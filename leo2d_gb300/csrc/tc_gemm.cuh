@@ -69,8 +69,10 @@ void make_tmap_f32(CUtensorMap* map, const void* base, int64_t rows, int64_t col
 // out[M][N] (FP64, row-major) += A[M][K] * B[N][K]^T with FP32 operands, on the
 // tensor cores: three TF32 products per K step (hi*hi + hi*lo + lo*hi), FP32
 // accumulation over 2048 products at a time, added into FP64 partial tiles that
-// are summed in a fixed order. K must be a multiple of 4 (16-byte rows).
-void tc_gemm_f32x3_acc(leo2d_ctx* ctx, const float* A, const float* B, int M, int N, int64_t K, double* out);
+// are summed in a fixed order. K must be a multiple of 4 (16-byte rows). `ldo`:
+// the row stride of out (<= 0: N).
+void tc_gemm_f32x3_acc(leo2d_ctx* ctx, const float* A, const float* B, int M, int N, int64_t K, double* out,
+                       int64_t ldo = 0);
 
 // Sets the kernels' shared-memory attributes on the context's device (once;
 // call before capturing GEMM launches into a graph).

@@ -89,3 +89,64 @@ def test_trace_cond_large_product(ctx):
     re, im = oracle.phase_vectors(seed, 0, R, csr.n)
     ref = (oracle.kpm_cond_trace(rp, col, val, dx, re, M) + oracle.kpm_cond_trace(rp, col, val, dx, im, M)) / R
     assert _rel(mu, ref) < FP32_RTOL
+
+
+def _flake(ctx, size, twist, with_dx=True, max_R=None):
+    g = L.make_geom(model=L.MODEL_SIMPLE, size=size, max_R=max_R, angles_deg=(0.0, twist), energy_rescale=1.0)
+    csr = ctx.build_csr(ctx.prepare(g), with_dx=with_dx)
+    lo, hi = csr.bounds()
+    csr.rescale(1.01 * (hi - lo) / 2, -(hi + lo) / 2)
+    return csr
+
+
+def _opts(ctx, fn, **opts):
+    for k, v in opts.items():
+        ctx.set_option(k, v)
+    try:
+        return fn()
+    finally:
+        ctx.set_option("kubo_velocity", -1)
+        ctx.set_option("kubo_chunk", 0)
+
+
+@pytest.mark.parametrize("size,twist,R,kind", [(13, 3.0, 20, L.VEC_PHASE), (11, 4.4, 7, L.VEC_GAUSSIAN),
+                                              (9, 2.0, 3, L.VEC_PHASE)])
+def test_velocity_in_step_matches_stored_dx(ctx, size, twist, R, kind):
+    """dxH built inside the row-block step from the flake's positions against the
+    stored dxH (gather kernels, reference row order) and the FP64 oracle; ragged
+    last passes (R not a multiple of the vectors per pass) and row counts that
+    leave a partial last row block."""
+    csr = _flake(ctx, size, twist)
+    M, seed = 32, 17
+    cfg = L.kpm_cfg(M, R=R, kind=kind, seed=seed)
+    fly = csr.kpm_cond(cfg)
+    assert csr.rb_info()[0] == (csr.n + 3) // 4  # the row blocks were built and used
+    stored = _opts(ctx, lambda: csr.kpm_cond(cfg), kubo_velocity=0)
+    assert _rel(fly, stored) < 2e-5
+    if kind == L.VEC_PHASE:  # (Gaussian vectors: the stored-dxH path above is the check)
+        rp, col, val, dx, dy = csr.download(dx=True)
+        re, im = oracle.phase_vectors(seed, 0, R, csr.n)
+        ref = (oracle.kpm_cond_trace(rp, col, val, dx, re, M) + oracle.kpm_cond_trace(rp, col, val, dx, im, M)) / R
+        assert _rel(fly, ref) < FP32_RTOL
+
+
+def test_velocity_in_step_needs_no_stored_dx(ctx):
+    """A flake built without LEO2D_CSR_WITH_DX gives the same trace moments; the
+    stored-dxH path still asks for it."""
+    with_dx = _flake(ctx, 12, 2.5)
+    without = _flake(ctx, 12, 2.5, with_dx=False)
+    cfg = L.kpm_cfg(24, R=16, kind=L.VEC_PHASE, seed=3)
+    np.testing.assert_array_equal(with_dx.kpm_cond(cfg), without.kpm_cond(cfg))
+    with pytest.raises(L.Leo2dError, match="WITH_DX"):
+        _opts(ctx, lambda: without.kpm_cond(cfg), kubo_velocity=0)
+
+
+@pytest.mark.parametrize("chunk", [4, 8, 12, 64])
+def test_velocity_chunks_of_b_side(ctx, chunk):
+    """The B side built in chunks of moments (two-vector carry between chunks,
+    each chunk's product into its columns of mu) gives the moments of one chunk."""
+    csr = _flake(ctx, 14, 1.8)
+    cfg = L.kpm_cfg(48, R=16, kind=L.VEC_PHASE, seed=9)
+    whole = csr.kpm_cond(cfg)
+    got = _opts(ctx, lambda: csr.kpm_cond(cfg), kubo_chunk=chunk)
+    np.testing.assert_allclose(got, whole, rtol=0, atol=1e-12 * np.abs(whole).max())
