@@ -502,8 +502,8 @@ def run_kubo(args):
     csr.kpm_cond(cfg)
     ctx.set_profiling(False)
     split = {k: round(ctx.kernel_stats(k)[1] / 1000.0, 4)
-             for k in ("cheb_step", "cond_gemm", "cond_gemm_sum", "x_hilo")}
-    steps_run = ctx.kernel_stats("cheb_step")[0]
+             for k in ("cheb_step", "cheb_step_vel", "cond_gemm", "cond_gemm_sum", "rb_xrel")}
+    steps_run = ctx.kernel_stats("cheb_step")[0] + ctx.kernel_stats("cheb_step_vel")[0]
     # FP32 vs FP64 oracle on a small flake
     small = ctx.build_csr(ctx.prepare(geom(L, radius=math.sqrt(2.0e4 / 2.398), twist=twist)), with_dx=True)
     slo, shi = small.bounds()

@@ -175,18 +175,6 @@ __global__ void k_cond_sigma(const double* __restrict__ mu, int M, const double*
   }
 }
 
-// x positions of the rows in the streamed order as FP32 pairs: hi = x rounded,
-// lo = (x - hi) rounded, so (hi_i - hi_j) + (lo_i - lo_j) is x_i - x_j to the
-// FP32 rounding of the difference (neighbours' hi parts subtract exactly).
-__global__ void k_x_hilo(int64_t n, const double* __restrict__ pos, const int32_t* __restrict__ new2old,
-                         float2* __restrict__ out) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double x = pos[3 * (int64_t)(new2old ? new2old[i] : i)] + 0.0;
-    const float hi = (float)x;
-    out[i] = make_float2(hi, (float)(x - (double)hi));
-  }
-}
-
 // Whether the trace moments can take the row-block path: a flake assembled
 // here (positions, no periodic images in dxH), the ordering allowed.
 bool velocity_in_step(const leo2d_ctx* ctx, const leo2d_csr* csr) {
@@ -205,18 +193,24 @@ bool cond_trace_rows(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* 
   s.rb_window = false;
   Recursion r;
   r.setup(ctx, csr, s, 1);
-  if (!r.shape.rb || !r.use_perm || rb_stages(ctx, m, 16) < 2) return false;
+  // the velocity step's variant: the context's row-block settings where given,
+  // else 16 warps, paired FMAs, 8 batches in flight
   StepShape sv = r.shape;
-  sv.rb_warps = 16;  // the velocity step's width
-  const size_t smem_v = rb_smem_bytes(ctx, m, 16);
-  const unsigned grid_v = rb_grid(ctx, csr, 16);
+  sv.rb_warps = ctx->rb_warps > 0 ? ctx->rb_warps : 16;
+  sv.rb_packed = ctx->rb_packed >= 0 ? ctx->rb_packed != 0 : true;
+  sv.rb_unroll = ctx->rb_unroll > 0 ? ctx->rb_unroll : 8;
+  if (sv.rb_warps != 16) {
+    sv.rb_warps = 24;
+    sv.rb_packed = false;
+    sv.rb_unroll = 4;
+  }
+  if (!r.shape.rb || !r.use_perm || rb_stages(ctx, m, sv.rb_warps, true) < 2) return false;
+  csr_build_rb_xs(ctx, m);
+  const size_t smem_v = rb_smem_bytes(ctx, m, sv.rb_warps, true);
+  const unsigned grid_v = rb_grid(ctx, csr, sv.rb_warps);
   constexpr int C = 32;
   const int64_t n = csr->n;
   const size_t vec = (size_t)n * C;
-  DevBuf<float2> xhl((size_t)n);
-  launch(ctx, "x_hilo", [&] {
-    k_x_hilo<<<grid_for(n, 256), 256, 0, ctx->stream>>>(n, csr->pos.p, csr->new2old.p, xhl.p);
-  });
   DevBuf<double> part((size_t)2 * std::max<unsigned>(ctx->sm_count, std::max(grid_v, r.grid)) * 2 * C);
   DevBuf<float> U((size_t)P * vec), ta(vec), tb(vec), junk(vec);
   // B-side moments held at once: the setting, else what fits next to U
@@ -240,14 +234,13 @@ bool cond_trace_rows(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* 
     else fill_gaussian(ctx, r, cfg->seed, cfg->first_vector + v0, nv);
     const float* X0 = reinterpret_cast<const float*>(r.x0.p);
     // a_0 = D r (its H~ r is not used)
-    rb_launch_step(ctx, csr, sv, grid_v, smem_v, X0, junk.p, nullptr, 1, 1.f, part.p, nullptr, nullptr, xhl.p,
-                   ta.p);
+    rb_launch_step(ctx, csr, sv, grid_v, smem_v, X0, junk.p, nullptr, 1, 1.f, part.p, nullptr, nullptr, ta.p);
     // A side: u_n = D T_n a_0 and T_{n+1} a_0 (over T_{n-1} a_0) from one launch
     float* cur = ta.p;
     float* nxt = tb.p;
     for (int k = 0; k < P; ++k) {
       rb_launch_step(ctx, csr, sv, grid_v, smem_v, cur, nxt, nullptr, k == 0 ? 1 : 0, k == 0 ? 1.f : 2.f, part.p,
-                     nullptr, nullptr, xhl.p, U.p + (size_t)k * vec);
+                     nullptr, nullptr, U.p + (size_t)k * vec);
       std::swap(cur, nxt);
     }
     // B side in chunks: T_m in slot 2 + m - m0 (slots 0, 1: the previous chunk's last two)

@@ -75,6 +75,9 @@ struct leo2d_csr {
   leo2d::DevBuf<int64_t> rb_off;      // [blocks + 1 + pad] first slot of each block
   leo2d::DevBuf<unsigned char> rb_data;  // 20 bytes per slot: columns, then the value panel
   leo2d::DevBuf<float> rb_im;         // [slots][4] imaginary value panel (complex_h)
+  bool rb_xs_built = false;           // positions for the velocity step (Kubo)
+  leo2d::DevBuf<float> rb_xrel;       // [blocks][4] x of each row minus x of its block's first row
+  leo2d::DevBuf<float> rb_xs;         // [slots] x of the slot's column minus the same
   // shared-memory windows of the row blocks (rbw_spmm.cu): per tile of 16 blocks
   // the sorted distinct columns of its slots; slots hold window positions
   bool rbw_built = false;
@@ -109,6 +112,10 @@ void csr_drop_tc(leo2d_csr* csr);
 // nothing) when a block of 4 rows has more than 4096 entries or 2048 distinct columns.
 bool csr_build_rb(leo2d_ctx* ctx, leo2d_csr* csr);
 void csr_drop_rb(leo2d_csr* csr);
+// x positions of the ordered rows and of every row-block slot's column relative
+// to the block's first row (the velocity step's D_ij = (x_i - x_j) H~_ij); once
+// per matrix.
+void csr_build_rb_xs(leo2d_ctx* ctx, leo2d_csr* csr);
 // Largest data bytes of a tile of `tile` consecutive row blocks.
 int64_t rb_tile_max_bytes(leo2d_ctx* ctx, const leo2d_csr* csr, int tile);
 // Builds the shared-memory windows of the row blocks; returns false (and builds

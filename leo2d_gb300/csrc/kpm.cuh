@@ -62,15 +62,16 @@ void tc_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, int cols, unsigned gri
 
 // The row-block step (rb_spmm.cu): shared-memory stages that fit (0: none),
 // dynamic shared memory, grid, and one launch.
-int rb_stages(leo2d_ctx* ctx, leo2d_csr* csr, int warps);
-size_t rb_smem_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps);
+// (velocity: the stages of the velocity step, which also copy the slots' positions)
+int rb_stages(leo2d_ctx* ctx, leo2d_csr* csr, int warps, bool velocity = false);
+size_t rb_smem_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps, bool velocity = false);
 unsigned rb_grid(leo2d_ctx* ctx, const leo2d_csr* csr, int warps);
-// With `xhl` (the ordered rows' x positions as FP32 hi/lo pairs) the launch also
-// writes out2 = D T_n, D_ij = (x_i - x_j) H~_ij (a flake's dxH), from the same gathers.
+// With out2 (the velocity step; csr_build_rb_xs first, smem and grid for
+// velocity stages) the launch also writes out2 = D T_n, D_ij = (x_i - x_j) H~_ij
+// (a flake's dxH), from the same gathers, and computes no moment dots.
 void rb_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape, unsigned grid, size_t smem,
                     const float* tn, float* tp, const float* tprev, int first, float alpha, double* partials,
-                    const double* prev_partials, double* prev_dots, const float2* xhl = nullptr,
-                    float* out2 = nullptr);
+                    const double* prev_partials, double* prev_dots, float* out2 = nullptr);
 
 // The windowed row-block step (rbw_spmm.cu), as above.
 int rbw_stages(leo2d_ctx* ctx, leo2d_csr* csr);

@@ -66,14 +66,16 @@ struct RbArgs {
   const double* __restrict__ prev_partials;
   double* __restrict__ prev_dots;
   const float* __restrict__ im;  // complex H: [slots][4] imaginary panel
-  // velocity mode: x positions of the (ordered) rows as FP32 (hi, lo) pairs, and
-  // the output of J-free product D T_n with D_ij = (x_i - x_j) H~_ij
-  const float2* __restrict__ xhl;
+  // velocity mode: x of each row and of each slot's column relative to the
+  // block's first row ([blocks][4] and [slots]), and the output for D T_n,
+  // D_ij = (x_i - x_j) H~_ij
+  const float* __restrict__ xrel;
+  const float* __restrict__ xs;
   float* __restrict__ out2;
   int stages;      // 2..4
   int chunk;       // consecutive tiles per block between grid-wide jumps
   int off_bytes;   // offsets region of a stage
-  int im_at;       // complex H: start of the imaginary panel in a stage
+  int panel_at;    // start of the second panel in a stage (complex H: imaginary values; velocity: x)
   int stage_bytes; // offsets + data (+ imaginary panel), multiple of 128
   uint64_t spin_limit;
   int* status;
@@ -114,12 +116,15 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
     const int64_t s0 = a.off[b0], s1 = a.off[b1];
     const uint32_t dbytes = (uint32_t)((s1 - s0) * kRbSlotBytes);
     unsigned char* st = smem + (size_t)stage * a.stage_bytes;
-    const uint32_t ibytes = CPX ? (uint32_t)((s1 - s0) * kRbRows * sizeof(float)) : 0u;
+    const uint32_t ibytes = CPX  ? (uint32_t)((s1 - s0) * kRbRows * sizeof(float))
+                            : DJ ? (uint32_t)((s1 - s0) * sizeof(float))
+                                 : 0u;
     issued[stage] += 1;
     mbar_expect_tx(&full[stage], (uint32_t)(ocount * 8) + dbytes + ibytes);
     bulk_g2s(st, a.off + ba, (uint32_t)(ocount * 8), &full[stage]);
     if (dbytes) bulk_g2s(st + a.off_bytes, a.data + s0 * kRbSlotBytes, dbytes, &full[stage]);
-    if (CPX && ibytes) bulk_g2s(st + a.im_at, a.im + s0 * kRbRows, ibytes, &full[stage]);
+    if (CPX && ibytes) bulk_g2s(st + a.panel_at, a.im + s0 * kRbRows, ibytes, &full[stage]);
+    if (DJ && ibytes) bulk_g2s(st + a.panel_at, a.xs + s0, ibytes, &full[stage]);
   };
   const int64_t chunk = a.chunk;
   auto tile_of = [&](int64_t i) -> int64_t {
@@ -199,7 +204,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
       const bool ok = row < a.n;
       // the epilogue's rows, fetched into L1 while the slots run
       if (ok) {
-        asm volatile("prefetch.global.L1 [%0];" ::"l"(tq + row * C));
+        if (!DJ) asm volatile("prefetch.global.L1 [%0];" ::"l"(tq + row * C));
         if (!a.first) asm volatile("prefetch.global.L1 [%0];" ::"l"(tprev + row * C + 4 * q));
       }
       // batches of 4 slots, U batches in flight per lane; the main loop runs
@@ -207,39 +212,31 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
       const int nb = K >> 2;
       const int32_t* csg = cs + g;
       const float4* vsg = vs + g;
-      const float4* wsg = reinterpret_cast<const float4*>(st + a.im_at) + (sb - off_s[b0 - ba]) + g;
+      const float4* wsg = reinterpret_cast<const float4*>(st + a.panel_at) + (sb - off_s[b0 - ba]) + g;
+      const float* xsg = reinterpret_cast<const float*>(st + a.panel_at) + (sb - off_s[b0 - ba]) + g;
       typename std::conditional<CPX, PanelAccCpx, PanelAcc<PACKED>>::type acc;
       acc.zero();
-      // velocity mode: the block's row positions, and a second accumulator for
-      // D T_n, D_ij = (x_i - x_j) H~_ij built from the positions on the fly; the
-      // hi parts of neighbouring positions subtract exactly, so the difference
-      // keeps about FP64 accuracy
-      PanelAcc<false> accj;
-      float2 xr[4];
+      // velocity mode: a second accumulator for D T_n, D_ij = (x_i - x_j) H~_ij
+      // built on the fly from positions relative to the block's first row (FP64
+      // differences rounded once: small numbers, so x_i - x_j keeps the FP32
+      // accuracy of the difference itself)
+      PanelAcc<PACKED> accj;
+      float4 xr;
       if constexpr (DJ) {
         accj.zero();
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const int64_t rk = rb * kRbRows + k;
-          xr[k] = rk < a.n ? __ldg(a.xhl + rk) : make_float2(0.f, 0.f);
-        }
+        xr = __ldg(reinterpret_cast<const float4*>(a.xrel) + rb);
       }
-      auto add = [&](const float4& x, int slot4, uint32_t c) {
+      auto add = [&](const float4& x, int slot4) {
         if constexpr (CPX) {
           acc.add(x, vsg[slot4], wsg[slot4]);
         } else {
           const float4 v = vsg[slot4];
           acc.add(x, v);
           if constexpr (DJ) {
-            const float2 xc = __ldg(a.xhl + c);
-            const float4 w = make_float4(v.x * ((xr[0].x - xc.x) + (xr[0].y - xc.y)),
-                                         v.y * ((xr[1].x - xc.x) + (xr[1].y - xc.y)),
-                                         v.z * ((xr[2].x - xc.x) + (xr[2].y - xc.y)),
-                                         v.w * ((xr[3].x - xc.x) + (xr[3].y - xc.y)));
-            accj.add(x, w);
+            const float e = xsg[slot4];
+            accj.add(x, make_float4(v.x * (xr.x - e), v.y * (xr.y - e), v.z * (xr.z - e), v.w * (xr.w - e)));
           }
         }
-        (void)c;
       };
       int b = 0;
       for (; b + U <= nb; b += U) {
@@ -252,7 +249,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
 #pragma unroll
         for (int u = 0; u < U; ++u) x[u] = ldg4(tq + (size_t)c[u] * C);
 #pragma unroll
-        for (int u = 0; u < U; ++u) add(x[u], 4 * (b + u), c[u]);
+        for (int u = 0; u < U; ++u) add(x[u], 4 * (b + u));
         (void)vb;
       }
       for (; b < nb; b += 4) {
@@ -265,7 +262,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
           x[u] = u < rem ? ldg4(tq + (size_t)(uint32_t)cb[4 * u] * C) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-          if (u < rem) add(x[u], 4 * (b + u), (uint32_t)cb[4 * u]);
+          if (u < rem) add(x[u], 4 * (b + u));
         (void)vb;
       }
       // reduce-scatter over the four groups: group g keeps row g
@@ -300,7 +297,6 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
         if (ok) *reinterpret_cast<float4*>(a.out2 + row * C + 4 * q) = make_float4(hj[0], hj[1], hj[2], hj[3]);
       }
       if (ok) {
-        const float4 xn = ldg4(tq + row * C);
         float4 y;
         if (a.first) {
           y = make_float4(alpha * h[0], alpha * h[1], alpha * h[2], alpha * h[3]);
@@ -309,18 +305,23 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
           y = make_float4(alpha * h[0] - xp.x, alpha * h[1] - xp.y, alpha * h[2] - xp.z, alpha * h[3] - xp.w);
         }
         *reinterpret_cast<float4*>(a.tp + row * C + 4 * q) = y;
-        e0[0] += xn.x * xn.x;
-        e0[1] += xn.y * xn.y;
-        e0[2] += xn.z * xn.z;
-        e0[3] += xn.w * xn.w;
-        e1[0] += y.x * xn.x;
-        e1[1] += y.y * xn.y;
-        e1[2] += y.z * xn.z;
-        e1[3] += y.w * xn.w;
+        if constexpr (!DJ) {
+          const float4 xn = ldg4(tq + row * C);
+          e0[0] += xn.x * xn.x;
+          e0[1] += xn.y * xn.y;
+          e0[2] += xn.z * xn.z;
+          e0[3] += xn.w * xn.w;
+          e1[0] += y.x * xn.x;
+          e1[1] += y.y * xn.y;
+          e1[2] += y.z * xn.z;
+          e1[3] += y.w * xn.w;
+        }
       }
-      if (++since_flush == kDotFlush) {  // warp-uniform
-        since_flush = 0;
-        flush();
+      if constexpr (!DJ) {
+        if (++since_flush == kDotFlush) {  // warp-uniform
+          since_flush = 0;
+          flush();
+        }
       }
     }
     // release the stage; the last warp refills it
@@ -341,6 +342,8 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
     for (int i = 0; i < nst; ++i)
       if (issued[i] > 0) bounded_wait(&full[i], (uint32_t)(issued[i] - 1) & 1u, ~0ull);
 
+  // (the velocity step computes no moment dots and writes no partials)
+  if constexpr (DJ) return;
   flush();
   // warps add their columns in warp order (deterministic)
   __shared__ double bsum[2 * C];
@@ -357,6 +360,28 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
 }
 
 // ---------------------------------------------------------------- format build
+
+// Positions for the velocity step, relative to each row block's first row and
+// rounded once from the FP64 difference: xrel[4b + k] = x(row 4b + k) - x(row 4b)
+// (0 past the last row), xs[s] = x(column of slot s) - x(row 4b) (one warp per
+// row block; rows and columns in the ordered numbering).
+__global__ void k_rb_xrel(int64_t n, int64_t nrb, const int64_t* __restrict__ off,
+                          const unsigned char* __restrict__ data, const double* __restrict__ pos,
+                          const int32_t* __restrict__ new2old, float* __restrict__ xrel, float* __restrict__ xs) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nrb; b += warps) {
+    const double x0 = pos[3 * (int64_t)new2old[b * kRbRows]];
+    if (lane < kRbRows) {
+      const int64_t r = b * kRbRows + lane;
+      xrel[r] = r < n ? (float)(pos[3 * (int64_t)new2old[r]] - x0) : 0.f;
+    }
+    const int64_t s0 = off[b];
+    const int K = (int)(off[b + 1] - s0);
+    const int32_t* col = reinterpret_cast<const int32_t*>(data + s0 * kRbSlotBytes);
+    for (int k = lane; k < K; k += 32) xs[s0 + k] = (float)(pos[3 * (int64_t)new2old[col[k]]] - x0);
+  }
+}
 
 // Ascending bitonic sort of n (a power of two >= blockDim.x) keys in shared memory.
 __device__ void bitonic_sort_u64(unsigned long long* key, int n) {
@@ -544,13 +569,17 @@ int64_t rb_tile_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps) {
 }
 
 // Imaginary panel of the largest tile (complex H): 16 of every 20 slot bytes.
-int64_t rb_im_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps) {
-  if (!csr->complex_h) return 0;
-  return (rb_tile_bytes(ctx, csr, warps) / kRbSlotBytes * kRbRows * (int64_t)sizeof(float) + 127) / 128 * 128;
+// Bytes of a stage's second panel: the imaginary values (complex H, 16 per
+// slot) or the slots' column positions (velocity step, 4 per slot).
+int64_t rb_panel_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps, bool velocity) {
+  const int64_t per = velocity ? (int64_t)sizeof(float) : (csr->complex_h ? kRbRows * (int64_t)sizeof(float) : 0);
+  if (per == 0) return 0;
+  return (rb_tile_bytes(ctx, csr, warps) / kRbSlotBytes * per + 127) / 128 * 128;
 }
 
-int64_t rb_stage_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps) {
-  return rb_off_bytes(warps) + (rb_tile_bytes(ctx, csr, warps) + 127) / 128 * 128 + rb_im_bytes(ctx, csr, warps);
+int64_t rb_stage_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps, bool velocity) {
+  return rb_off_bytes(warps) + (rb_tile_bytes(ctx, csr, warps) + 127) / 128 * 128 +
+         rb_panel_bytes(ctx, csr, warps, velocity);
 }
 
 }  // namespace
@@ -573,6 +602,9 @@ int64_t rb_tile_max_bytes(leo2d_ctx* ctx, const leo2d_csr* csr, int tile) {
 
 void csr_drop_rb(leo2d_csr* csr) {
   csr_drop_rbw(csr);
+  csr->rb_xs_built = false;
+  csr->rb_xrel.release();
+  csr->rb_xs.release();
   csr->rb_built = false;
   csr->rb_blocks = 0;
   csr->rb_slots = 0;
@@ -643,16 +675,16 @@ bool csr_build_rb(leo2d_ctx* ctx, leo2d_csr* csr) {
   return true;
 }
 
-int rb_stages(leo2d_ctx* ctx, leo2d_csr* csr, int warps) {
+int rb_stages(leo2d_ctx* ctx, leo2d_csr* csr, int warps, bool velocity) {
   if (!csr->rb_built) return 0;
-  const int64_t stage = rb_stage_bytes(ctx, csr, warps);
+  const int64_t stage = rb_stage_bytes(ctx, csr, warps, velocity);
   const int64_t budget = (int64_t)ctx->smem_optin - 6 * 1024;  // static shared memory of the kernel (4.7 KB)
   const int64_t s = std::min<int64_t>(4, budget / std::max<int64_t>(stage, 1));
   return s >= 2 ? (int)std::min<int64_t>(s, std::max(2, ctx->tile_stages)) : 0;
 }
 
-size_t rb_smem_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps) {
-  return (size_t)rb_stages(ctx, csr, warps) * (size_t)rb_stage_bytes(ctx, csr, warps);
+size_t rb_smem_bytes(leo2d_ctx* ctx, leo2d_csr* csr, int warps, bool velocity) {
+  return (size_t)rb_stages(ctx, csr, warps, velocity) * (size_t)rb_stage_bytes(ctx, csr, warps, velocity);
 }
 
 unsigned rb_grid(leo2d_ctx* ctx, const leo2d_csr* csr, int warps) {
@@ -663,8 +695,10 @@ unsigned rb_grid(leo2d_ctx* ctx, const leo2d_csr* csr, int warps) {
 
 void rb_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape, unsigned grid, size_t smem,
                     const float* tn, float* tp, const float* tprev, int first, float alpha, double* partials,
-                    const double* prev_partials, double* prev_dots, const float2* xhl, float* out2) {
+                    const double* prev_partials, double* prev_dots, float* out2) {
   leo2d_csr* m = const_cast<leo2d_csr*>(csr);
+  const bool vel = out2 != nullptr;
+  if (vel) LEO_REQUIRE(csr->rb_xs_built && !csr->complex_h, "the velocity step needs the slots' positions");
   RbArgs a{};
   a.n = csr->n;
   a.nrb = csr->rb_blocks;
@@ -679,29 +713,36 @@ void rb_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
   a.prev_partials = prev_partials;
   a.prev_dots = prev_dots;
   const int w = shape.rb_warps;
-  a.stages = rb_stages(ctx, m, w);
+  a.stages = rb_stages(ctx, m, w, vel);
   LEO_REQUIRE(a.stages >= 2, "row-block tiles too large for shared memory");
   a.chunk = std::max(1, ctx->tile_chunk);
   a.off_bytes = rb_off_bytes(w);
-  a.stage_bytes = (int)rb_stage_bytes(ctx, m, w);
+  a.stage_bytes = (int)rb_stage_bytes(ctx, m, w, vel);
   a.im = csr->complex_h ? csr->rb_im.p : nullptr;
-  a.im_at = (int)(a.stage_bytes - rb_im_bytes(ctx, m, w));
+  a.panel_at = (int)(a.stage_bytes - rb_panel_bytes(ctx, m, w, vel));
   LEO_REQUIRE((size_t)a.stages * a.stage_bytes <= smem, "row-block shared memory changed since setup");
   a.spin_limit = ctx->spin_limit;
   a.status = ctx->status.p;
   a.never_wait = ctx->test_unsatisfied_wait;
-  a.xhl = xhl;
+  a.xrel = vel ? csr->rb_xrel.p : nullptr;
+  a.xs = vel ? csr->rb_xs.p : nullptr;
   a.out2 = out2;
   auto go = [&](auto kern, int warps) {
     LEO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    launch(ctx, "cheb_step", [&] { kern<<<grid, warps * 32, smem, ctx->stream>>>(a); });
+    launch(ctx, vel ? "cheb_step_vel" : "cheb_step", [&] { kern<<<grid, warps * 32, smem, ctx->stream>>>(a); });
   };
-  if (xhl) {
+  if (vel) {
     // the velocity step: T_{n+1} and D T_n from the same gathers
-    LEO_REQUIRE(out2 && !csr->complex_h, "the velocity step takes a real matrix and an output for D T_n");
-    // (16 warps: the second accumulator and the row positions fit the registers)
-    LEO_REQUIRE(w == 16, "the velocity row-block step runs 16 warps");
-    return go(k_cheb_rb<16, false, 4, false, true>, 16);
+    // (the variants whose two accumulators fit the registers without spills)
+    const int vkey = (w / 8) * 100 + (shape.rb_packed ? 10 : 0) + (shape.rb_unroll == 8 ? 1 : 0);
+    switch (vkey) {
+      case 200: return go(k_cheb_rb<16, false, 4, false, true>, 16);
+      case 201: return go(k_cheb_rb<16, false, 8, false, true>, 16);
+      case 210: return go(k_cheb_rb<16, true, 4, false, true>, 16);
+      case 211: return go(k_cheb_rb<16, true, 8, false, true>, 16);
+      case 300: return go(k_cheb_rb<24, false, 4, false, true>, 24);
+    }
+    fail(LEO2D_ERR_BAD_ARG, "the velocity row-block step runs 16 warps, or 24 with scalar FMAs and 4 batches");
   }
   if (csr->complex_h) {
     switch (w) {
@@ -728,6 +769,23 @@ void rb_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
 #undef LEO2D_RB_W
 #undef LEO2D_RB_CASE
   fail(LEO2D_ERR_BAD_ARG, "row-block warps must be 16, 24 or 32 and batches 4 or 8");
+}
+
+}  // namespace leo2d
+
+namespace leo2d {
+
+void csr_build_rb_xs(leo2d_ctx* ctx, leo2d_csr* csr) {
+  LEO_REQUIRE(csr->rb_built && csr->reordered && csr->pos.p, "slot positions need the row blocks and the geometry");
+  if (csr->rb_xs_built) return;
+  csr->rb_xrel.alloc((size_t)csr->rb_blocks * kRbRows);
+  csr->rb_xs.alloc((size_t)std::max<int64_t>(csr->rb_slots, 1));
+  launch(ctx, "rb_xrel", [&] {
+    k_rb_xrel<<<grid_for(csr->rb_blocks * 32, 256, (int64_t)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
+        csr->n, csr->rb_blocks, csr->rb_off.p, csr->rb_data.p, csr->pos.p, csr->new2old.p, csr->rb_xrel.p,
+        csr->rb_xs.p);
+  });
+  csr->rb_xs_built = true;
 }
 
 }  // namespace leo2d

@@ -150,3 +150,17 @@ def test_velocity_chunks_of_b_side(ctx, chunk):
     whole = csr.kpm_cond(cfg)
     got = _opts(ctx, lambda: csr.kpm_cond(cfg), kubo_chunk=chunk)
     np.testing.assert_allclose(got, whole, rtol=0, atol=1e-12 * np.abs(whole).max())
+
+
+def test_velocity_step_variants(ctx):
+    """Every velocity-step variant (warps, FMA form, batches in flight) gives the
+    same moments: the variants change the schedule, not the sums of a row block."""
+    csr = _flake(ctx, 15, 2.2)
+    cfg = L.kpm_cfg(32, R=16, kind=L.VEC_PHASE, seed=12)
+    base = csr.kpm_cond(cfg)
+    for w, p, u in ((16, 0, 4), (16, 1, 4), (16, 0, 8), (24, 0, 4)):
+        got = _opts(ctx, lambda: csr.kpm_cond(cfg), rb_warps=w, rb_packed=p, rb_unroll=u)
+        ctx.set_option("rb_warps", 0)
+        ctx.set_option("rb_packed", -1)
+        ctx.set_option("rb_unroll", 0)
+        assert _rel(got, base) < 1e-6, (w, p, u)
