@@ -167,6 +167,18 @@ leo2d_status leo2d_csr_geometry(leo2d_ctx* ctx, const leo2d_csr* csr, int32_t* i
 leo2d_status leo2d_csr_upload(leo2d_ctx* ctx, int64_t n, int64_t nnz, const int64_t* rowptr,
                               const int32_t* col, const double* val, const double* val_dx,
                               const double* pos, leo2d_csr** out);
+/* The matrix of a job with vacancies: the listed orbitals (0-based, `count`
+ * entries; duplicates and indices outside [0, n) remove nothing) are removed with
+ * their rows and columns, and the kept orbitals keep their order, renumbered:
+ * orbital i becomes i - (removed orbitals below i). Values (real and imaginary),
+ * dxH/dyH, positions and grid indices follow. The reference builds this matrix
+ * directly for its vacancy solvers (SOLVER_TYPE = MLMC_VAC / VD_FILE):
+ * workerChebSolve's relabelling (src/locality.cpp:2989-3016) and the skips of
+ * generateRealH / generateCpxH (locality.cpp:3970-4010, 4215-4220, 4188, 4305).
+ * A target t of the reference's numbering is row t - (removed orbitals below t)
+ * (computeDosKPM, locality.cpp:5963). *out is a new matrix; src is unchanged. */
+leo2d_status leo2d_csr_remove_orbitals(leo2d_ctx* ctx, const leo2d_csr* src, const int64_t* orbitals,
+                                       int64_t count, leo2d_csr** out);
 /* Gershgorin bounds of the stored matrix, FP64: emin = min_i (H_ii - sum_{j!=i}|H_ij|),
  * emax = max_i (H_ii + sum_{j!=i}|H_ij|). */
 leo2d_status leo2d_csr_bounds(leo2d_ctx* ctx, const leo2d_csr* csr, double* emin, double* emax);

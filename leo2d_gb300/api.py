@@ -158,6 +158,18 @@ class Context:
         return out
 
 
+def vacancy_rows(n, vacancies, orbitals):
+    """Rows of `orbitals` (reference numbering) in the matrix with `vacancies`
+    removed: i - (removed orbitals below i), as computeDosKPM maps its targets
+    (locality.cpp:5963). Duplicates and out-of-range vacancies count nothing."""
+    gone = np.zeros(n, bool)
+    v = np.asarray(vacancies, np.int64)
+    gone[v[(v >= 0) & (v < n)]] = True
+    below = np.concatenate([[0], np.cumsum(gone)])
+    o = np.asarray(orbitals, np.int64)
+    return o - below[o]
+
+
 def run_input(path, out_dir=".", device=0):
     """The `leo2d` driver through the C ABI; raises Leo2dError with the reason."""
     lib = _abi.load()
@@ -204,6 +216,15 @@ class Csr:
         self.ctx.check(self.ctx.lib.leo2d_csr_download(self.ctx.h, self.h, _p(rp), _p(col), _p(val),
                                                        _p(vdx), _p(vdy)))
         return (rp, col, val, vdx, vdy) if dx else (rp, col, val)
+
+    def remove_orbitals(self, orbitals):
+        """The matrix with these orbitals (vacancies, 0-based) removed, the rest
+        renumbered in order (the reference's vacancy solvers); a new Csr."""
+        orb = np.ascontiguousarray(orbitals, np.int64)
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.leo2d_csr_remove_orbitals(self.ctx.h, self.h, _p(orb) if len(orb) else None,
+                                                              len(orb), ctypes.byref(h)))
+        return Csr(self.ctx, h)
 
     def download_imag(self):
         """Imaginary parts of the stored entries (a complex Hamiltonian: b_field != 0)."""

@@ -696,6 +696,43 @@ void oracle_kpm_trace(int64_t n, const int64_t* rp, const int32_t* col, const do
 
 // ---------------------------------------------------------------- complex H (magnetic field)
 
+int64_t oracle_vacancy_reduction(int64_t n, const int64_t* orbitals, int64_t count, int64_t* reduction) {
+  // workerChebSolve's loop: orbital i is removed when it equals any list entry
+  std::vector<char> gone((size_t)n, 0);
+  for (int64_t j = 0; j < count; ++j)
+    if (orbitals[j] >= 0 && orbitals[j] < n) gone[(size_t)orbitals[j]] = 1;
+  int64_t counter = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    reduction[i] = counter;
+    counter += gone[(size_t)i];
+  }
+  reduction[n] = counter;
+  return n - counter;
+}
+
+int64_t oracle_remove_orbitals(int64_t n, const int64_t* rp, const int32_t* col, const double* v0,
+                               const double* v1, const double* v2, const int64_t* red, int64_t* rp_out,
+                               int32_t* col_out, double* v0_out, double* v1_out, double* v2_out) {
+  // orbital i is a vacancy when reduction steps up across it
+  auto removed = [&](int64_t i) { return red[i] + 1 == red[i + 1]; };
+  int64_t out = 0;
+  for (int64_t r = 0; r < n; ++r) {
+    if (removed(r)) continue;
+    rp_out[r - red[r]] = out;
+    for (int64_t e = rp[r]; e < rp[r + 1]; ++e) {
+      const int64_t c = col[e];
+      if (removed(c)) continue;
+      col_out[out] = (int32_t)(c - red[c]);
+      if (v0) v0_out[out] = v0[e];
+      if (v1) v1_out[out] = v1[e];
+      if (v2) v2_out[out] = v2[e];
+      ++out;
+    }
+  }
+  rp_out[n - red[n]] = out;
+  return out;
+}
+
 void oracle_peierls(int64_t n, const int64_t* rp, const int32_t* col, const double* val, const double* pos,
                     double B, double* re, double* im) {
   for (int64_t r = 0; r < n; ++r) {

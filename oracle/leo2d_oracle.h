@@ -101,6 +101,20 @@ void oracle_cond_transform(const double* M, int32_t P, double* out);
 void oracle_cond_sigma(const double* mu, int32_t M, const double* E, int64_t nE, double rescale,
                        double center, double scale, double* out);
 
+/* Vacancies, as workerChebSolve relabels orbitals (locality.cpp:2989-3016):
+ * reduction[i] = number of listed orbitals below i (0-based; duplicates and
+ * entries outside [0, n) count nothing), reduction[n] = total; returns the kept
+ * count. */
+int64_t oracle_vacancy_reduction(int64_t n, const int64_t* orbitals, int64_t count, int64_t* reduction);
+/* generateRealH's vacancy skips (locality.cpp:3970-4010, 4215-4220, 4188,
+ * 4305): rows of removed orbitals and entries in their columns are dropped, kept
+ * columns become col - reduction[col]. Up to three value arrays (NULL skips one)
+ * are carried. rp_out [kept + 1]; col/val outputs sized nnz. Returns the kept nnz. */
+int64_t oracle_remove_orbitals(int64_t n, const int64_t* rowptr, const int32_t* col, const double* v0,
+                               const double* v1, const double* v2, const int64_t* reduction,
+                               int64_t* rp_out, int32_t* col_out, double* v0_out, double* v1_out,
+                               double* v2_out);
+
 /* Gershgorin bounds (FP64). */
 void oracle_gershgorin(int64_t n, const int64_t* rowptr, const int32_t* col, const double* val,
                        double* emin, double* emax);

@@ -258,6 +258,32 @@ def cond_sigma(mu, energies, rescale, center, scale=1.0):
     return out
 
 
+def vacancy_reduction(n, orbitals):
+    """reduction[i] = removed orbitals below i (workerChebSolve's relabelling); kept count."""
+    orb = np.ascontiguousarray(orbitals, np.int64)
+    red = np.zeros(n + 1, np.int64)
+    lib().oracle_vacancy_reduction.restype = ctypes.c_int64
+    kept = lib().oracle_vacancy_reduction(ctypes.c_int64(n), _p(orb), ctypes.c_int64(len(orb)), _p(red))
+    return red, int(kept)
+
+
+def remove_orbitals(rowptr, col, values, orbitals):
+    """generateRealH's vacancy skips on a full CSR: (rowptr, col, [values...]) of the
+    kept orbitals, renumbered in order; `values` is a list of up to three arrays."""
+    lib().oracle_remove_orbitals.restype = ctypes.c_int64
+    rowptr = np.ascontiguousarray(rowptr, np.int64)
+    col = np.ascontiguousarray(col, np.int32)
+    n = len(rowptr) - 1
+    red, kept = vacancy_reduction(n, orbitals)
+    vals = [np.ascontiguousarray(v, np.float64) for v in values] + [None] * (3 - len(values))
+    outs = [np.zeros(len(col)) if v is not None else None for v in vals]
+    rp = np.zeros(kept + 1, np.int64)
+    c = np.zeros(len(col), np.int32)
+    nnz = lib().oracle_remove_orbitals(ctypes.c_int64(n), _p(rowptr), _p(col), *[_p(v) for v in vals],
+                                       _p(red), _p(rp), _p(c), *[_p(o) for o in outs])
+    return rp, c[:nnz], [o[:nnz] for o in outs if o is not None]
+
+
 def gershgorin(rowptr, col, val):
     lo, hi = ctypes.c_double(), ctypes.c_double()
     n, a, b, c = _csr_args(rowptr, col, val)

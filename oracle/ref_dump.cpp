@@ -78,6 +78,9 @@ static int dump_main(int argc, char** argv) {
   double height = 0, angle = 0;
   std::string strain_file;
   Job_params opts;
+  // (this driver only) orbitals removed from the matrix, 0-based, as the
+  // vacancy solvers hand generateRealH a job's vacancy_list
+  std::vector<int> vacancies;
 
   std::ifstream in(argv[1]);
   if (!in.is_open()) { std::fprintf(stderr, "cannot open %s\n", argv[1]); return 2; }
@@ -88,6 +91,11 @@ static int dump_main(int argc, char** argv) {
       const std::string& key = tk[p];
       auto val = [&](size_t k) { return p + k < tk.size() ? tk[p + k] : std::string(); };
       if (key == "JOB_NAME") opts.setParam("job_name", val(2));
+      if (key == "REF_DUMP_VACANCIES") {
+        std::istringstream vs(val(2));
+        std::string t;
+        while (std::getline(vs, t, ',')) vacancies.push_back(std::atoi(t.c_str()));
+      }
       if (key == "MAXSIZE") {
         max_size = std::atoi(val(2).c_str());
         mx.push_back(max_size); mx.push_back(max_size); mx.push_back(max_size);
@@ -227,7 +235,31 @@ static int dump_main(int argc, char** argv) {
   // ---- job 1, shifts = 0, as rootChebSolve + workerChebSolve build it ----
   const int num_s = (int)loc.sdata.size();
   std::vector<std::vector<double>> shifts(num_s, std::vector<double>(3, 0.0));
+  // a vacancy list takes the MLMC_VAC solver's path through generateRealH and
+  // the KPM functions (solver_type 3, locality.cpp:1392-1450, 2985-3016)
+  if (!vacancies.empty()) O.setParam("solver_type", 3);
   Job_params job(O);
+  if (!vacancies.empty()) {
+    job.setParam("num_vacancies", (int)vacancies.size());
+    job.setParam("vacancy_list", vacancies);
+  }
+  // the relabelling of workerChebSolve (locality.cpp:2989-3016): reduction[i] =
+  // vacancies below orbital i; the matrix keeps max_index - vacancies rows
+  std::vector<int> cir(N + 1, 0);
+  int Nloc = N;
+  if (!vacancies.empty()) {
+    int counter = 0;
+    for (int i = 0; i < N; ++i) {
+      cir[i] = counter;
+      for (int v : vacancies)
+        if (v == i) {
+          ++counter;
+          break;
+        }
+    }
+    cir[N] = counter;
+    Nloc = N - counter;
+  }
   job.setParam("shifts", shifts);
   job.setParam("jobID", 1);
   job.setParam("max_jobs", 1);
@@ -246,9 +278,10 @@ static int dump_main(int argc, char** argv) {
     }
     std::default_random_engine generator;
     std::normal_distribution<double> distribution(0.0, 1.0);
-    trace_vectors.assign(S, std::vector<double>(N));
+    // (rootChebSolve draws vectors of the reduced length, locality.cpp:2280-2300)
+    trace_vectors.assign(S, std::vector<double>(Nloc));
     for (int s = 0; s < S; ++s)
-      for (int i = 0; i < N; ++i) trace_vectors[s][i] = distribution(generator);
+      for (int i = 0; i < Nloc; ++i) trace_vectors[s][i] = distribution(generator);
     job.setParam("kpm_trace_vectors", trace_vectors);
     job.setParam("num_targets", S);
   }
@@ -260,9 +293,8 @@ static int dump_main(int argc, char** argv) {
                          shift_configs, strain, job);
 
   const int num_targets = job.getInt("num_targets");
-  std::vector<int> cir(N + 1, 0);
   SpMatrix H, dxH, dyH;
-  std::vector<double> a0x((size_t)num_targets * N + 1), a0y((size_t)num_targets * N + 1);
+  std::vector<double> a0x((size_t)num_targets * Nloc + 1), a0y((size_t)num_targets * Nloc + 1);
   // a magnetic field makes the worker build the complex Hamiltonian
   // (locality.cpp:2906-2909, 3061-3071): generateCpxH with no SOC terms
   const bool cpx = O.getInt("magOn") == 1;
@@ -272,16 +304,22 @@ static int dump_main(int argc, char** argv) {
     std::vector<std::complex<double>> soc_terms;
     loc.generateCpxH(H, dxH, dyH, jbx, jby, jtx, jty, jtbx, jtby, a0x.data(), a0y.data(), job,
                      index_to_grid.data(), i2pos.data(), inter_pairs.data(), inter_sc, intra_pairs.data(),
-                     intra_t.data(), soc_pairs, soc_terms, intra_sc, strain, cir, N);
+                     intra_t.data(), soc_pairs, soc_terms, intra_sc, strain, cir, Nloc);
   } else {
     loc.generateRealH(H, dxH, dyH, a0x.data(), a0y.data(), job, index_to_grid.data(), i2pos.data(),
                       inter_pairs.data(), inter_sc, intra_pairs.data(), intra_t.data(), intra_sc,
-                      strain, cir, N);
+                      strain, cir, Nloc);
   }
 
-  const int nnz = H.rowPointer[N];
+  const int nnz = H.rowPointer[Nloc];
   int meta[8] = {N, nnz, loc.max_intra_pairs, loc.max_inter_pairs, num_targets,
                  O.getInt("poly_order"), kpm_trace, O.getInt("observable_type")};
+  if (!vacancies.empty()) {
+    // the matrix has Nloc rows; meta keeps the full orbital count
+    dump(outdir, "vacancies", vacancies.data(), vacancies.size());
+    int nl = Nloc;
+    dump(outdir, "n_kept", &nl, 1);
+  }
   dump(outdir, "meta", meta, 8);
   dump(outdir, "index_to_grid", index_to_grid.data(), index_to_grid.size());
   dump(outdir, "index_to_pos", index_to_pos.data(), index_to_pos.size());
@@ -291,7 +329,7 @@ static int dump_main(int argc, char** argv) {
   dump(outdir, "intra_sc", intra_scf.data(), intra_scf.size());
   dump(outdir, "inter_pairs", inter_pairs.data(), inter_pairs.size());
   dump(outdir, "inter_sc", inter_scf.data(), inter_scf.size());
-  dump(outdir, "rowptr", H.rowPointer, (size_t)N + 1);
+  dump(outdir, "rowptr", H.rowPointer, (size_t)Nloc + 1);
   dump(outdir, "col", H.colIndex, (size_t)nnz);
   if (cpx) {
     std::vector<double> re((size_t)nnz), im((size_t)nnz);
@@ -313,8 +351,8 @@ static int dump_main(int argc, char** argv) {
   const int observable = O.getInt("observable_type");
   if (observable == 0) {
     std::vector<std::vector<double>> cheb(num_targets, std::vector<double>(P));
-    if (kpm_trace == 0) loc.computeDosKPM(cheb, H, job, cir, N);
-    else loc.computeDosTraceKPM(cheb, H, job, cir, N);
+    if (kpm_trace == 0) loc.computeDosKPM(cheb, H, job, cir, Nloc);
+    else loc.computeDosTraceKPM(cheb, H, job, cir, Nloc);
     std::vector<double> flat;
     for (auto& r : cheb) flat.insert(flat.end(), r.begin(), r.end());
     dump(outdir, "moments", flat.data(), flat.size());
@@ -324,7 +362,9 @@ static int dump_main(int argc, char** argv) {
       dump(outdir, "trace_vectors", tv.data(), tv.size());
       Job_params res(job);
       res.setParam("cheb_coeffs", cheb);
-      Param_tools::densityTransformTrace(res, 1.0 / (double)N);
+      // the worker's DOS scale, 1 / (local_max_index - num_vacancies)
+      // (locality.cpp:3124-3128): the vacancies are subtracted a second time
+      Param_tools::densityTransformTrace(res, 1.0 / (double)(Nloc - (int)vacancies.size()));
       std::vector<double> dos = res.getDoubleVec("kpm_trace_dos");
       dump(outdir, "dos", dos.data(), dos.size());
     } else {
@@ -338,11 +378,11 @@ static int dump_main(int argc, char** argv) {
     }
   } else {
     std::vector<std::vector<double>> cheb(num_targets, std::vector<double>((size_t)P * P));
-    loc.computeCondKPM(cheb, H, dxH, job, cir, N, a0x.data());
+    loc.computeCondKPM(cheb, H, dxH, job, cir, Nloc, a0x.data());
     std::vector<double> flat;
     for (auto& r : cheb) flat.insert(flat.end(), r.begin(), r.end());
     dump(outdir, "cond_moments", flat.data(), flat.size());
-    dump(outdir, "alpha0_x", a0x.data(), (size_t)num_targets * N);
+    dump(outdir, "alpha0_x", a0x.data(), (size_t)num_targets * Nloc);
     Job_params res(job);
     res.setParam("kpm_M_xx", cheb);
     Param_tools::conductivityTransform(res);

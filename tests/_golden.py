@@ -85,5 +85,12 @@ def parse_in(name):
 
 ALL = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
 # real Hamiltonians (generateRealH) and complex ones in a magnetic field (generateCpxH)
-CASES = [c for c in ALL if "bfield" not in c]
+CASES = [c for c in ALL if "bfield" not in c and "_vac_" not in c]
 BFIELD_CASES = [c for c in ALL if "bfield" in c]
+# vacancies (the vacancy solvers' matrix): <base>_vac_<kind> pairs with <base>_<kind>
+VAC_CASES = [c for c in ALL if "_vac_" in c]
+
+
+def vac_base(name):
+    """The fixture of the same job without vacancies."""
+    return name.replace("_vac_", "_")

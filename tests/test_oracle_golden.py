@@ -7,8 +7,9 @@ rounding.
 import numpy as np
 import pytest
 
+import leo2d_gb300 as L
 from oracle import oracle
-from tests._golden import CASES, load, parse_in
+from tests._golden import CASES, VAC_CASES, load, parse_in, vac_base
 
 
 @pytest.fixture(scope="module", params=CASES)
@@ -169,3 +170,63 @@ def test_bfield_moments(bcase):
         ref = gold["moments"].reshape(len(tg), P)
         mu = oracle.kpm_ldos_cpx(b.rowptr, b.col, re, im, tg, P)
         np.testing.assert_allclose(mu, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+
+
+# ------------------------------------------------------------- vacancies
+
+@pytest.fixture(scope="module", params=VAC_CASES)
+def vcase(request):
+    name = request.param
+    gold = load(name)
+    g, kv = parse_in(vac_base(name))
+    built = oracle.Built(g)
+    return name, gold, built, kv
+
+
+def test_vacancy_csr_bit_exact(vcase):
+    """generateRealH's vacancy skips restated on the full matrix: rows, columns and
+    values of the reference's reduced matrix (duplicates and out-of-range list
+    entries change nothing)."""
+    name, gold, b, kv = vcase
+    vac = gold["vacancies"].astype(np.int64)
+    vals = [b.val] + ([b.val_dx, b.val_dy] if "val_dx" in gold else [])
+    rp, col, out = oracle.remove_orbitals(b.rowptr, b.col, vals, vac)
+    red, kept = oracle.vacancy_reduction(b.n, vac)
+    assert kept == int(gold["n_kept"][0]) == len(rp) - 1
+    assert np.array_equal(rp, gold["rowptr"].astype(np.int64))
+    assert np.array_equal(col, gold["col"])
+    assert np.array_equal(out[0], gold["val"])
+    if "val_dx" in gold:
+        assert np.array_equal(out[1], gold["val_dx"])
+        assert np.array_equal(out[2], gold["val_dy"])
+
+
+def test_vacancy_moments(vcase):
+    """Moments on the reduced matrix: targets renumbered as computeDosKPM does
+    (t - reduction[t]), trace vectors of the reduced length."""
+    name, gold, b, kv = vcase
+    meta = gold["meta"]
+    P, trace, observable = int(meta[5]), int(meta[6]), int(meta[7])
+    vac = gold["vacancies"].astype(np.int64)
+    vals = [b.val] + ([b.val_dx] if observable == 1 else [])
+    rp, col, out = oracle.remove_orbitals(b.rowptr, b.col, vals, vac)
+    red, kept = oracle.vacancy_reduction(b.n, vac)
+    tg = gold["targets"].astype(np.int64)
+    tl = tg - red[tg]
+    # the library's host-side mapping of reference orbitals to reduced rows
+    assert np.array_equal(L.vacancy_rows(b.n, vac, tg), tl)
+    if observable == 1:
+        C = oracle.kpm_cond(rp, col, out[0], out[1], tl, P)
+        ref = gold["cond_moments"].reshape(len(tg), P, P)
+        np.testing.assert_array_equal(C[0, :, :P - 1], ref[0, :, :P - 1])
+    elif trace == 1:
+        R = int(meta[4])
+        mu = oracle.kpm_trace(rp, col, out[0], oracle.reference_gaussian(R, kept), P)
+        np.testing.assert_array_equal(mu, gold["moments"].reshape(R, P))
+        # the worker's DOS scale subtracts the list length once more (locality.cpp:3124-3128)
+        dos, E = oracle.dos_transform(mu, P, b.geom.energy_rescale, b.geom.energy_shift,
+                                      1.0 / (kept - len(vac)))
+        np.testing.assert_allclose(dos.ravel(), gold["dos"], rtol=1e-12, atol=1e-13 * np.abs(gold["dos"]).max())
+    else:
+        mu = oracle.kpm_ldos(rp, col, out[0], tl, P)
+        np.testing.assert_array_equal(mu, gold["moments"].reshape(len(tg), P))
