@@ -83,6 +83,12 @@ typedef struct {
    * (src/locality.cpp:7157-7161), as generateCpxH builds it
    * (src/locality.cpp:4485-5310). Flakes only (BOUNDARY_CONDITION = 0). */
   double b_field;
+  /* Bloch vector (1/A) of a k-sampled job (K_SAMPLING = 1, Job_params "k_vec",
+   * locality.cpp:1615-1650): when non-zero the Hamiltonian is complex, each
+   * periodic image's hopping t e^{i k.(r_col - r_row)} with r_row shifted into
+   * that image, summed per entry, as generateCpxH does (locality.cpp:4896-4941).
+   * The energy shift then goes to the home image's diagonal only. */
+  double k_vec[2];
 } leo2d_geom;
 
 typedef struct leo2d_ctx leo2d_ctx;

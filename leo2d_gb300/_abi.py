@@ -36,7 +36,7 @@ class Geom(ctypes.Structure):
         ("angles", c_dbl * MAX_SHEETS), ("energy_rescale", c_dbl), ("energy_shift", c_dbl),
         ("lattice", c_dbl * 2 * 2 * MAX_SHEETS), ("sheet_supercell", c_dbl * 2 * 2 * MAX_SHEETS),
         ("sheet_sc_stride", c_i32 * 2 * 2 * MAX_SHEETS), ("supercell", c_dbl * 2 * 2),
-        ("prepared", c_i32), ("b_field", c_dbl),
+        ("prepared", c_i32), ("b_field", c_dbl), ("k_vec", c_dbl * 2),
     ]
 
 
@@ -51,7 +51,7 @@ class KpmCfg(ctypes.Structure):
 
 def make_geom(num_sheets=2, model=MODEL_REF, boundary_condition=0, size=50, max_R=None,
               heights=(0.0, 3.35), angles_deg=(0.0, 0.0), energy_rescale=20.0,
-              energy_shift=0.0, supercell_mn=None, sc_search_size=1, b_field=0.0):
+              energy_shift=0.0, supercell_mn=None, sc_search_size=1, b_field=0.0, k_vec=None):
     """A Geom filled the way main.cpp fills Sdata for MAXSIZE=size, MINSIZE=-size.
 
     Angles are given in degrees and converted as main.cpp:345-351 does.
@@ -75,6 +75,8 @@ def make_geom(num_sheets=2, model=MODEL_REF, boundary_condition=0, size=50, max_
     if supercell_mn is not None:
         g.supercell_m, g.supercell_n = supercell_mn
     g.b_field = float(b_field)
+    if k_vec is not None:
+        g.k_vec[0], g.k_vec[1] = float(k_vec[0]), float(k_vec[1])
     return g
 
 

@@ -170,6 +170,30 @@ def vacancy_rows(n, vacancies, orbitals):
     return o - below[o]
 
 
+def k_grid(geom, n1, n2):
+    """Bloch vectors of grid k-sampling (K_TYPE = 0, locality.cpp:1617-1650), in job
+    order (k1 outer, k2 inner): k = (k1/n1) b1 + (k2/n2) b2, with b1, b2 the
+    reciprocal vectors of the prepared supercell (Locality::getReciprocal,
+    locality.cpp:7215-7262). Returns [n1 * n2][2]."""
+    a = np.array([[geom.supercell[0][0], geom.supercell[0][1], 0.0],
+                  [geom.supercell[1][0], geom.supercell[1][1], 0.0], [0.0, 0.0, 1.0]])
+
+    def cross(x, y, d):
+        return (x[1] * y[2] - x[2] * y[1], x[2] * y[0] - x[0] * y[2], x[0] * y[1] - x[1] * y[0])[d]
+
+    den1 = den2 = 0.0
+    for j in range(3):
+        den1 += a[0][j] * cross(a[1], a[2], j)
+        den2 += a[1][j] * cross(a[2], a[0], j)
+    b = [[2 * np.pi * cross(a[1], a[2], k) / den1 for k in range(2)],
+         [2 * np.pi * cross(a[2], a[0], k) / den2 for k in range(2)]]
+    out = []
+    for k1 in range(n1):
+        for k2 in range(n2):
+            out.append([(k1 / n1) * b[0][0] + (k2 / n2) * b[1][0], (k1 / n1) * b[0][1] + (k2 / n2) * b[1][1]])
+    return np.array(out)
+
+
 def run_input(path, out_dir=".", device=0):
     """The `leo2d` driver through the C ABI; raises Leo2dError with the reason."""
     lib = _abi.load()

@@ -61,6 +61,8 @@ struct GeomDev {
   double supercell[2][2];
   double rescale, shift;
   double b_field;  // non-zero: complex entries t e^{i phi} (Peierls phase)
+  double kx, ky;   // Bloch vector: phases k.(r_col - r_row) per periodic image
+  int cpx;         // complex entries (a field or a Bloch vector)
   SheetDev sh[kMaxSheets];
 };
 
@@ -259,7 +261,7 @@ struct RowOut {
   double* val;
   double* dx;
   double* dy;
-  double* val_im;  // imaginary parts (b_field != 0)
+  double* val_im;  // imaginary parts (complex entries)
 };
 
 // Locality::peierlsPhase (locality.cpp:7157-7161): the phase of the hopping
@@ -273,7 +275,7 @@ __device__ __forceinline__ double peierls_phase(double x1, double x2, double y1,
 // generateCpxH adds it (locality.cpp:4896-4941: zero couplings stay 0).
 __device__ __forceinline__ void store_value(const GeomDev& G, const RowOut& out, int64_t e, double t, double x1,
                                             double y1, double x2, double y2) {
-  if (G.b_field == 0.0) {
+  if (!G.cpx) {
     out.val[e] = t != 0 ? 0.0 + t : 0.0;
     return;
   }
@@ -282,7 +284,9 @@ __device__ __forceinline__ void store_value(const GeomDev& G, const RowOut& out,
     out.val_im[e] = 0.0;
     return;
   }
-  const double ph = peierls_phase(x1, x2, y1, y2, G.b_field);
+  // generateCpxH's phase: the Peierls phase plus k.(r2 - r1) (locality.cpp:4896-4900)
+  double ph = peierls_phase(x1, x2, y1, y2, G.b_field);
+  ph = ph + G.kx * (x2 - x1) + G.ky * (y2 - y1);
   out.val[e] = 0.0 + t * cos(ph);
   out.val_im[e] = 0.0 + t * sin(ph);
 }
@@ -448,7 +452,9 @@ __device__ __forceinline__ void image_of(int img, int ss, int& dxs, int& dys) {
   dys = img % side - ss;
 }
 
-// Value of one candidate (row, k2, image), generateRealH's rescaling included.
+// Value of one candidate (row, k2, image), generateRealH's rescaling included
+// (generateCpxH, for complex entries, shifts the home image's diagonal only:
+// locality.cpp:4885).
 __device__ double periodic_value(const GeomDev& G, int64_t row, const int32_t* grid4,
                                  const double* pos, bool inter, int64_t k2, int img,
                                  double& x1, double& y1) {
@@ -467,7 +473,8 @@ __device__ double periodic_value(const GeomDev& G, int64_t row, const int32_t* g
     gd0 = gd0 - dxs * sh.stride[0][0] - dys * sh.stride[1][0];
     gd1 = gd1 - dxs * sh.stride[0][1] - dys * sh.stride[1][1];
     const double raw = intralayer(G.model, l0, l2, gd0, gd1);
-    return k2 == row ? (raw + G.shift) / G.rescale : raw / G.rescale;
+    const bool diag = k2 == row && (!G.cpx || (dxs == 0 && dys == 0));
+    return diag ? (raw + G.shift) / G.rescale : raw / G.rescale;
   }
   const double z1 = pos[3 * row + 2];
   const double x2 = pos[3 * k2], y2 = pos[3 * k2 + 1], z2 = pos[3 * k2 + 2];
@@ -634,13 +641,20 @@ __global__ void __launch_bounds__(256) k_periodic_rows(const __grid_constant__ G
         while (q > 0 && (keys[q - 1] >> 16) == (keys[p] >> 16)) --q;
         const bool inter = (keys[p] & kKeyInter) != 0;
         const int64_t k2 = (int64_t)((keys[p] >> 16) & 0xffffffffull);
-        double v = 0.0, vdx = 0.0, vdy = 0.0;
+        double v = 0.0, vdx = 0.0, vdy = 0.0, vim = 0.0;
         for (int e = q; e <= p; ++e) {
           const int img = (int)(keys[e] & 0xffffull);
           double x1, y1;
           const double t = periodic_value(G, row, grid4, pos, inter, k2, img, x1, y1);
           if (t != 0) {
-            v += t;
+            if (G.cpx) {
+              // std::polar(t, k.(r2 - r1)) summed over the images (locality.cpp:4896-4941)
+              const double ph = G.kx * (pos[3 * k2] - x1) + G.ky * (pos[3 * k2 + 1] - y1);
+              v += t * cos(ph);
+              vim += t * sin(ph);
+            } else {
+              v += t;
+            }
             vdx += (x1 - pos[3 * k2]) * t;
             vdy += (y1 - pos[3 * k2 + 1]) * t;
           }
@@ -648,6 +662,7 @@ __global__ void __launch_bounds__(256) k_periodic_rows(const __grid_constant__ G
         const int64_t e = base_out + before;
         out.col[e] = (int32_t)k2;
         out.val[e] = v;
+        if (G.cpx) out.val_im[e] = vim;
         if (G.with_dx) {
           out.dx[e] = vdx;
           out.dy[e] = vdy;
@@ -790,6 +805,7 @@ void validate_geom(const leo2d_geom* g) {
   if (g->boundary_condition == 1)
     LEO_REQUIRE(g->sc_search_size >= 0 && g->sc_search_size <= 3, "sc_search_size must be 0..3");
   LEO_REQUIRE(std::isfinite(g->b_field), "b_field must be finite");
+  LEO_REQUIRE(std::isfinite(g->k_vec[0]) && std::isfinite(g->k_vec[1]), "k_vec must be finite");
   LEO_REQUIRE(g->b_field == 0.0 || g->boundary_condition == 0,
               "a magnetic field is supported for flakes (BOUNDARY_CONDITION = 0)");
 }
@@ -878,7 +894,10 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     G.keep_zeros = (flags & LEO2D_CSR_KEEP_ZEROS) ? 1 : 0;
     G.with_dx = (flags & LEO2D_CSR_WITH_DX) ? 1 : 0;
     G.b_field = g->b_field;
-    LEO_REQUIRE(g->b_field == 0.0 || !G.with_dx,
+    G.kx = g->k_vec[0];
+    G.ky = g->k_vec[1];
+    G.cpx = (g->b_field != 0.0 || g->k_vec[0] != 0.0 || g->k_vec[1] != 0.0) ? 1 : 0;
+    LEO_REQUIRE(!G.cpx || !G.with_dx,
                 "the velocity operator (WITH_DX, conductivity) is not built for a complex Hamiltonian");
     std::memcpy(G.supercell, g->supercell, sizeof(G.supercell));
     G.rescale = g->energy_rescale;
@@ -970,7 +989,7 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     csr->n_intra = reduce_sum_i64(ctx, cnt_intra.p, n);
     csr->n_inter = reduce_sum_i64(ctx, cnt_inter.p, n);
     csr_alloc_entries(ctx, csr, nnz, G.with_dx != 0);
-    csr->complex_h = g->b_field != 0.0;
+    csr->complex_h = G.cpx != 0;
     if (csr->complex_h) {
       csr->val_im64.alloc(nnz + kCsrPad);
       LEO_CUDA(cudaMemsetAsync(csr->val_im64.p, 0, (nnz + kCsrPad) * sizeof(double), ctx->stream));

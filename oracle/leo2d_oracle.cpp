@@ -519,6 +519,59 @@ int oracle_build(const leo2d_geom* gin, oracle_h** out) {
   return 0;
 }
 
+void oracle_bloch(const oracle_h* h, double kx, double ky, double* re, double* im) {
+  const leo2d_geom& g = h->g;
+  const int64_t n = h->n;
+  const double rescale = g.energy_rescale, shift = g.energy_shift;
+  const double* P = h->i2pos.data();
+  const size_t n_intra = h->intra.size(), n_inter = h->inter.size();
+  std::vector<std::complex<double>> v(h->col.size(), std::complex<double>(0.0));
+  size_t ic = 0, ec = 0, cnt = 0;
+  // one pair: its value and the image shift of the row (generateCpxH, as generateRealH)
+  auto add = [&](const Pair& pr, int64_t ki, double t) {
+    double shx = 0.0, shy = 0.0;
+    if (g.boundary_condition == 1) {
+      shx = pr.sc0 * g.supercell[0][0] + pr.sc1 * g.supercell[1][0];
+      shy = pr.sc0 * g.supercell[0][1] + pr.sc1 * g.supercell[1][1];
+    }
+    const double x1 = P[3 * ki] + shx, y1 = P[3 * ki + 1] + shy;
+    const double x2 = P[3 * pr.j], y2 = P[3 * pr.j + 1];
+    double phase = 0.0;  // peierlsPhase with B = 0
+    phase = phase + kx * (x2 - x1) + ky * (y2 - y1);
+    const std::complex<double> z = std::polar(t, phase);
+    if (z != std::complex<double>(0.0)) v[cnt] += z;
+  };
+  for (int64_t ki = 0; ki < n; ++ki) {
+    while (ic < n_intra && h->intra[ic].i == ki) {
+      const Pair& pr = h->intra[ic];
+      const bool home = pr.sc0 == 0 && pr.sc1 == 0;
+      const double t = (pr.j == ki && home) ? (pr.t + shift) / rescale : pr.t / rescale;
+      add(pr, ki, t);
+      if (ic + 1 == n_intra || h->intra[ic + 1].i != ki || h->intra[ic + 1].j != pr.j) ++cnt;
+      ++ic;
+    }
+    while (ec < n_inter && h->inter[ec].i == ki) {
+      const Pair& pr = h->inter[ec];
+      double shx = 0.0, shy = 0.0;
+      if (g.boundary_condition == 1) {
+        shx = pr.sc0 * g.supercell[0][0] + pr.sc1 * g.supercell[1][0];
+        shy = pr.sc0 * g.supercell[0][1] + pr.sc1 * g.supercell[1][1];
+      }
+      const double x1 = P[3 * ki] + shx, y1 = P[3 * ki + 1] + shy, z1 = P[3 * ki + 2];
+      const double x2 = P[3 * pr.j], y2 = P[3 * pr.j + 1], z2 = P[3 * pr.j + 2];
+      const int o1 = h->grid4[4 * ki + 2], o2 = h->grid4[4 * pr.j + 2];
+      const double th1 = g.angles[h->grid4[4 * ki + 3]], th2 = g.angles[h->grid4[4 * pr.j + 3]];
+      add(pr, ki, interlayer(g.model, o1, o2, x2 - x1, y2 - y1, z2 - z1, th1, th2) / rescale);
+      if (ec + 1 == n_inter || h->inter[ec + 1].i != ki || h->inter[ec + 1].j != pr.j) ++cnt;
+      ++ec;
+    }
+  }
+  for (size_t e = 0; e < v.size(); ++e) {
+    re[e] = v[e].real();
+    im[e] = v[e].imag();
+  }
+}
+
 void oracle_free(oracle_h* h) { delete h; }
 
 void oracle_info(const oracle_h* h, int64_t* n, int64_t* nnz, int64_t* n_intra, int64_t* n_inter) {

@@ -61,6 +61,12 @@ void oracle_kpm_trace_doubling(int64_t n, const int64_t* rowptr, const int32_t* 
  * (Locality::peierlsPhase, locality.cpp:7157-7161). pos [n][3]. */
 void oracle_peierls(int64_t n, const int64_t* rowptr, const int32_t* col, const double* val,
                     const double* pos, double B, double* re, double* im);
+/* Complex H~ of a k-sampled job, as generateCpxH builds it with the job's k_vec
+ * (locality.cpp:4517-4524, 4885-4941): every pair of the built job becomes
+ * std::polar(t, k.(r_col - r_row)) with r_row shifted into the pair's image,
+ * summed per entry in pair order; the energy shift goes to the home image's
+ * diagonal only. re/im [nnz] in the CSR order of oracle_get. */
+void oracle_bloch(const oracle_h* h, double kx, double ky, double* re, double* im);
 /* computeDosTraceKPM's complex branch (locality.cpp:6240-6346), literal: real
  * start vectors [R][n]. */
 void oracle_kpm_trace_cpx(int64_t n, const int64_t* rowptr, const int32_t* col, const double* re,

@@ -96,6 +96,12 @@ class Built:
                                  ctypes.c_int64(len(out)))
         return out[:c]
 
+    def bloch(self, kx, ky):
+        """(re, im) of the k-sampled job's complex H~ (generateCpxH with k_vec), CSR order."""
+        re, im = np.zeros(self.nnz), np.zeros(self.nnz)
+        lib().oracle_bloch(self._h, ctypes.c_double(kx), ctypes.c_double(ky), _p(re), _p(im))
+        return re, im
+
     def compact(self):
         """(rowptr, col, val) without the entries whose value is exactly zero."""
         keep = self.val != 0.0

@@ -81,6 +81,8 @@ static int dump_main(int argc, char** argv) {
   // (this driver only) orbitals removed from the matrix, 0-based, as the
   // vacancy solvers hand generateRealH a job's vacancy_list
   std::vector<int> vacancies;
+  // (this driver only) a Bloch vector (1/A): the job of a k-sampled run with that k_vec
+  std::vector<double> k_vec;
 
   std::ifstream in(argv[1]);
   if (!in.is_open()) { std::fprintf(stderr, "cannot open %s\n", argv[1]); return 2; }
@@ -91,6 +93,11 @@ static int dump_main(int argc, char** argv) {
       const std::string& key = tk[p];
       auto val = [&](size_t k) { return p + k < tk.size() ? tk[p + k] : std::string(); };
       if (key == "JOB_NAME") opts.setParam("job_name", val(2));
+      if (key == "REF_DUMP_KVEC") {
+        std::istringstream ks(val(2));
+        std::string t;
+        while (std::getline(ks, t, ',')) k_vec.push_back(std::atof(t.c_str()));
+      }
       if (key == "REF_DUMP_VACANCIES") {
         std::istringstream vs(val(2));
         std::string t;
@@ -238,7 +245,11 @@ static int dump_main(int argc, char** argv) {
   // a vacancy list takes the MLMC_VAC solver's path through generateRealH and
   // the KPM functions (solver_type 3, locality.cpp:1392-1450, 2985-3016)
   if (!vacancies.empty()) O.setParam("solver_type", 3);
+  // a k vector takes the k-sampling path: the worker builds the complex H
+  // (locality.cpp:2906-2909) with the job's k_vec (generateCpxH, 4517-4524)
+  if (k_vec.size() == 2) O.setParam("k_sampling", 1);
   Job_params job(O);
+  if (k_vec.size() == 2) job.setParam("k_vec", k_vec);
   if (!vacancies.empty()) {
     job.setParam("num_vacancies", (int)vacancies.size());
     job.setParam("vacancy_list", vacancies);
@@ -297,7 +308,7 @@ static int dump_main(int argc, char** argv) {
   std::vector<double> a0x((size_t)num_targets * Nloc + 1), a0y((size_t)num_targets * Nloc + 1);
   // a magnetic field makes the worker build the complex Hamiltonian
   // (locality.cpp:2906-2909, 3061-3071): generateCpxH with no SOC terms
-  const bool cpx = O.getInt("magOn") == 1;
+  const bool cpx = O.getInt("magOn") == 1 || O.getInt("k_sampling") == 1;
   if (cpx) {
     SpMatrix jbx, jby, jtx, jty, jtbx, jtby;
     std::vector<std::vector<int>> soc_pairs;

@@ -78,15 +78,22 @@ def parse_in(name):
                 kv["use_b"] = int(v(2))
             elif key == "B_FIELD":
                 kv["b_field"] = float(v(2))
+            elif key == "REF_DUMP_KVEC":  # a fixture-generator key: the job's Bloch vector
+                kv["k_vec"] = [float(x) for x in v(2).split(",")]
     if kv.get("use_b"):
         g.b_field = kv.get("b_field", 0.0)
+    if "k_vec" in kv:
+        g.k_vec[0], g.k_vec[1] = kv["k_vec"]
     return g, kv
 
 
 ALL = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
 # real Hamiltonians (generateRealH) and complex ones in a magnetic field (generateCpxH)
-CASES = [c for c in ALL if "bfield" not in c and "_vac_" not in c]
+CASES = [c for c in ALL if "bfield" not in c and "_vac_" not in c and "_kvec_" not in c]
 BFIELD_CASES = [c for c in ALL if "bfield" in c]
+# complex Hamiltonians: a magnetic field, or a Bloch vector of a k-sampled periodic job
+KVEC_CASES = [c for c in ALL if "_kvec_" in c]
+COMPLEX_CASES = BFIELD_CASES + KVEC_CASES
 # vacancies (the vacancy solvers' matrix): <base>_vac_<kind> pairs with <base>_<kind>
 VAC_CASES = [c for c in ALL if "_vac_" in c]
 

@@ -46,7 +46,7 @@ def run_dump(inp, name):
             out[key] = np.fromfile(os.path.join(d, f), dtype=dt)
     meta = out["meta"]
     is_cond = meta[7] == 1
-    if not is_cond and "val_im" not in out:
+    if not is_cond:
         # dxH / dyH only matter for the conductivity fixtures
         out.pop("val_dx", None)
         out.pop("val_dy", None)
@@ -81,9 +81,10 @@ def main():
         name = f[:-3]
         inp = os.path.join(HERE, "inputs", f)
         arrs = run_dump(inp, name)
-        # a vacancy list is a ref_dump key (the reference's own main() takes
-        # vacancies from its solver files): no end-to-end files for those
-        if "REF_DUMP_VACANCIES" not in open(inp).read():
+        # vacancy lists and k vectors are ref_dump keys (the reference's own
+        # main() takes them from its solver files and k grids): no end-to-end
+        # files for those
+        if "REF_DUMP_" not in open(inp).read():
             run_e2e(inp, name)
         m = arrs["meta"]
         print(f"{name}: N={m[0]} nnz={m[1]} intra={m[2]} inter={m[3]} targets={m[4]} P={m[5]}")

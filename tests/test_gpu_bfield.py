@@ -1,6 +1,6 @@
-"""A perpendicular magnetic field: the complex Hamiltonian (generateCpxH with
-Peierls phases) against fixtures generated by the reference's own code, and
-against the oracle.
+"""Complex Hamiltonians (generateCpxH): a perpendicular magnetic field (Peierls
+phases on a flake) and k-sampled periodic supercells (Bloch phases per image),
+against fixtures generated by the reference's own code, and against the oracle.
 
 The complex matrix must equal the reference's to rounding (CUDA's cos/sin
 against glibc's: 1e-15 of the largest entry). Moments come from the FP32
@@ -14,7 +14,7 @@ import pytest
 
 import leo2d_gb300 as L
 from oracle import oracle
-from tests._golden import BFIELD_CASES, GOLDEN, e2e_text, load, parse_in
+from tests._golden import BFIELD_CASES, COMPLEX_CASES, GOLDEN, e2e_text, load, parse_in
 
 pytestmark = pytest.mark.gpu
 FP32_RTOL = 1e-4
@@ -30,7 +30,7 @@ def _rel(a, b):
     return np.max(np.abs(a - b)) / np.max(np.abs(b))
 
 
-@pytest.mark.parametrize("name", BFIELD_CASES)
+@pytest.mark.parametrize("name", COMPLEX_CASES)
 def test_complex_csr_matches_reference(ctx, name):
     gold = load(name)
     g, kv = parse_in(name)
@@ -44,7 +44,7 @@ def test_complex_csr_matches_reference(ctx, name):
     np.testing.assert_allclose(im, gold["val_im"], rtol=0, atol=1e-15 * scale)
 
 
-@pytest.mark.parametrize("name", BFIELD_CASES)
+@pytest.mark.parametrize("name", COMPLEX_CASES)
 def test_complex_moments_match_reference(ctx, name):
     gold = load(name)
     g, kv = parse_in(name)
@@ -129,3 +129,36 @@ def test_driver_files(tmp_path, name):
     mr = _numbers(e2e_text(name, "_matrix.dat"))
     assert len(mo) == len(mr)
     np.testing.assert_allclose(np.array(mo, float), np.array(mr, float), rtol=1e-5, atol=1e-6)
+
+
+def test_bloch_supercell_on_a_k_grid(ctx):
+    """A (4,5) twisted supercell at the points of a 2 x 3 k grid: the device's
+    image-resolved Bloch sums against the oracle's, and the complex recursion
+    (random-phase vectors) against the oracle's; k = 0 gives the real matrix."""
+    g = ctx.prepare(L.make_geom(boundary_condition=1, supercell_mn=(4, 5), size=16, energy_rescale=13.0))
+    ks = L.k_grid(g, 2, 3)
+    assert ks.shape == (6, 2) and np.all(ks[0] == 0.0)
+    b1 = ks[3]  # k1 = 1: half of the first reciprocal vector
+    a = np.array(g.supercell)
+    assert abs(2 * b1 @ a[0] - 2 * np.pi) < 1e-9 and abs(b1 @ a[1]) < 1e-9
+    real = ctx.build_csr(g)
+    assert np.abs(real.download()[2]).max() > 0
+    with pytest.raises(L.Leo2dError, match="real"):
+        real.download_imag()
+    for k in ks[1:3]:
+        gk = L.make_geom(boundary_condition=1, supercell_mn=(4, 5), size=16, energy_rescale=13.0, k_vec=k)
+        gk = ctx.prepare(gk)
+        csr = ctx.build_csr(gk, keep_zeros=True)
+        rp, col, re = csr.download()
+        im = csr.download_imag()
+        b = oracle.Built(gk)
+        ore, oim = b.bloch(*k)
+        assert np.array_equal(rp, b.rowptr) and np.array_equal(col, b.col)
+        scale = np.abs(ore).max()
+        np.testing.assert_allclose(re, ore, rtol=0, atol=4e-15 * scale)
+        np.testing.assert_allclose(im, oim, rtol=0, atol=4e-15 * scale)
+        P, R, seed = 64, 16, 3
+        mu = csr.kpm_dos(L.kpm_cfg(P, R=R, kind=L.VEC_PHASE, precision=L.FP32, seed=seed))
+        vre, vim = oracle.phase_vectors(seed, 0, R, csr.n)
+        ref = oracle.kpm_trace_cpx_doubling(rp, col, ore, oim, vre, vim, P)
+        assert _rel(mu, ref) < FP32_RTOL

@@ -127,10 +127,10 @@ def test_dct_matches_scipy():
 
 # ---------------------------------------------------------------- magnetic field (generateCpxH)
 
-from tests._golden import BFIELD_CASES  # noqa: E402
+from tests._golden import COMPLEX_CASES  # noqa: E402
 
 
-@pytest.fixture(scope="module", params=BFIELD_CASES)
+@pytest.fixture(scope="module", params=COMPLEX_CASES)
 def bcase(request):
     name = request.param
     gold = load(name)
@@ -138,22 +138,30 @@ def bcase(request):
     return name, gold, oracle.Built(g), kv
 
 
+def _complex_values(b, kv):
+    """A flake in a field: std::polar(t, Peierls phase) per entry of the real H;
+    a k-sampled periodic job: the image-resolved Bloch sums."""
+    if "k_vec" in kv:
+        return b.bloch(*kv["k_vec"])
+    return oracle.peierls(b.rowptr, b.col, b.val, b.pos, kv["b_field"])
+
+
 def test_bfield_csr(bcase):
-    """Structure of the real H; every value std::polar(t, Peierls phase)."""
+    """Structure of the real H; the complex values as generateCpxH builds them."""
     name, gold, b, kv = bcase
     assert np.array_equal(b.rowptr, gold["rowptr"].astype(np.int64))
     assert np.array_equal(b.col, gold["col"])
-    re, im = oracle.peierls(b.rowptr, b.col, b.val, b.pos, kv["b_field"])
+    re, im = _complex_values(b, kv)
     np.testing.assert_array_equal(re, gold["val"])
     np.testing.assert_array_equal(im, gold["val_im"])
-    assert np.abs(im).max() > 0.05 * np.abs(re).max()  # the field really twists the hoppings
+    assert np.abs(im).max() > 0.05 * np.abs(re).max()  # the phases really twist the hoppings
 
 
 def test_bfield_moments(bcase):
     name, gold, b, kv = bcase
     meta = gold["meta"]
     P, trace = int(meta[5]), int(meta[6])
-    re, im = oracle.peierls(b.rowptr, b.col, b.val, b.pos, kv["b_field"])
+    re, im = _complex_values(b, kv)
     if trace == 1:
         R = int(meta[4])
         vec = oracle.reference_gaussian(R, b.n)
