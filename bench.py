@@ -482,8 +482,8 @@ def run_kubo(args):
     import leo2d_gb300 as L
     from oracle import oracle
     ctx = L.Context(0)
-    M, R, twist = 512, 32, 1.5
-    radius = math.sqrt(2.0e6 / 2.398)
+    M, R, twist = args.kubo_moments, args.kubo_vectors, 1.5
+    radius = math.sqrt(args.kubo_orbitals / 2.398)
     # no stored dxH: the trace moments build it inside the row-block step
     csr = ctx.build_csr(ctx.prepare(geom(L, radius=radius, twist=twist)))
     lo, hi = csr.bounds()
@@ -517,12 +517,13 @@ def run_kubo(args):
     Es = sb + sa * np.linspace(-0.99, 0.99, 2001)
     s32 = ctx.cond_sigma(mu32, Es, sa, sb, 1.0 / small.n)
     s64 = ctx.cond_sigma(mu64, Es, sa, sb, 1.0 / small.n)
-    out = {"metric": "Kubo sigma_xx(E) (512x512 moments, 32 random-phase vectors, 2001 energies)",
+    out = {"metric": f"Kubo sigma_xx(E) ({M}x{M} moments, {R} random-phase vectors, 2001 energies)",
            "value": round(t, 6), "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": min(args.warmup, 1),
            "ms_per_step": round(t * 1000, 3), "higher_is_better": False, "dtype": "fp32",
            "data": "synthetic (geometry generated on the GPU, Philox vectors)",
-           "config": {"workload": f"TBLG flake {twist} deg, ~2M orbitals, simple model, J=i[H,x] on the fly, "
-                                  "M=512, 32 vectors, 2001 energies", "orbitals": csr.n, "nnz": csr.nnz},
+           "config": {"workload": f"TBLG flake {twist} deg, ~{args.kubo_orbitals:.3g} orbitals, simple model, "
+                                  f"J=i[H,x] built in the step, M={M}, {R} vectors, 2001 energies",
+                      "orbitals": csr.n, "nnz": csr.nnz},
            "fp32_vs_fp64_oracle": {"orbitals": small.n, "moments": Ms,
                                    "mu_max_rel": float(np.abs(mu32 - mu64).max() / np.abs(mu64).max()),
                                    "sigma_max_rel": float(np.abs(s32 - s64).max() / np.abs(s64).max())},
@@ -678,6 +679,10 @@ def main():
     ap.add_argument("--mlp-infer-only", action="store_true",
                     help="mlp workload: skip the training measurement (profiling the inference products)")
     ap.add_argument("--max-vectors", type=int, default=128)
+    ap.add_argument("--kubo-orbitals", type=float, default=2.0e6,
+                    help="kubo2m: flake size in orbitals (smaller cases for profiling)")
+    ap.add_argument("--kubo-moments", type=int, default=512, help="kubo2m: M of the M x M moments")
+    ap.add_argument("--kubo-vectors", type=int, default=32, help="kubo2m: random-phase vectors")
     ap.add_argument("--workload", default="flake10m",
                     choices=["flake10m", "batch32", "periodic", "kubo2m", "mlp", "bfield"],
                     help="flake10m: time-to-DOS on the 10M-orbital flake (the headline); batch32: 32 "
