@@ -188,7 +188,9 @@ leo2d_status leo2d_csr_remove_orbitals(leo2d_ctx* ctx, const leo2d_csr* src, con
 /* Gershgorin bounds of the stored matrix, FP64: emin = min_i (H_ii - sum_{j!=i}|H_ij|),
  * emax = max_i (H_ii + sum_{j!=i}|H_ij|). */
 leo2d_status leo2d_csr_bounds(leo2d_ctx* ctx, const leo2d_csr* csr, double* emin, double* emax);
-/* In place: H <- (H + shift*I) / rescale (FP64, then the FP32 copy is refreshed). */
+/* In place: H <- (H + shift*I) / rescale (FP64, as a product with the FP64
+ * reciprocal of rescale, within an ulp of the quotient; then the FP32 copy is
+ * refreshed). */
 leo2d_status leo2d_csr_rescale(leo2d_ctx* ctx, leo2d_csr* csr, double rescale, double shift);
 
 /* Per-orbital local stacking disregistry of a bilayer, out[n][2] in [0,1)^2:

@@ -43,16 +43,20 @@ __global__ void k_gershgorin(int64_t n, const int64_t* __restrict__ rp, const in
 
 // H <- (H + shift I) / rescale on the stored entries (diagonal gets the shift).
 // (a complex matrix: the imaginary parts are divided, the shift is real)
+// The division is a multiplication by the FP64 reciprocal (within an ulp of
+// the quotient): FP64 division would bound the kernel on GB300's FP64 pipe.
 __global__ void k_rescale(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
                           double* __restrict__ val, double* __restrict__ im, double* __restrict__ dx,
-                          double* __restrict__ dy, double rescale, double shift) {
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
-       r += (int64_t)gridDim.x * blockDim.x) {
-    for (int64_t i = rp[r]; i < rp[r + 1]; ++i) {
-      val[i] = col[i] == r ? (val[i] + shift) / rescale : val[i] / rescale;
-      if (im) im[i] = im[i] / rescale;
-      if (dx) dx[i] = dx[i] / rescale;
-      if (dy) dy[i] = dy[i] / rescale;
+                          double* __restrict__ dy, double inv, double shift) {
+  // a warp per row, lanes over its entries (coalesced)
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+    for (int64_t i = rp[r] + lane; i < rp[r + 1]; i += 32) {
+      val[i] = col[i] == r ? (val[i] + shift) * inv : val[i] * inv;
+      if (im) im[i] = im[i] * inv;
+      if (dx) dx[i] = dx[i] * inv;
+      if (dy) dy[i] = dy[i] * inv;
     }
   }
 }
@@ -203,9 +207,9 @@ leo2d_status leo2d_csr_rescale(leo2d_ctx* ctx, leo2d_csr* csr, double rescale, d
                 "rescale must be finite and non-zero, shift finite");
     LEO_CUDA(cudaSetDevice(ctx->device));
     launch(ctx, "rescale", [&] {
-      k_rescale<<<grid_for(csr->n, 256, (int64_t)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
+      k_rescale<<<grid_for(csr->n * 32, 256, (int64_t)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
           csr->n, csr->rowptr.p, csr->col.p, csr->val64.p, csr->complex_h ? csr->val_im64.p : nullptr,
-          csr->dx64.p, csr->dy64.p, rescale, shift);
+          csr->dx64.p, csr->dy64.p, 1.0 / rescale, shift);
     });
     csr_refresh_fp32(ctx, csr);
     ctx_sync(ctx);

@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
       const float x1f = (float)x1, y1f = (float)y1, z1f = (float)z1;
       constexpr float kWinLo = (float)(kInterCutoff - kPrefilterMargin), kWinHi = (float)(kInterCutoff + kPrefilterMargin);
       // every hopping is zero from 8 A on (in-plane for the reference model, 3-D for the simple one)
-      constexpr float kHopHi = 8.0f + kPrefilterMargin;
+      constexpr float kHopHi = 8.0f + kPrefilterMargin, kHopLo = 8.0f - kPrefilterMargin;
       for (int side_k = 0; side_k < 2; ++side_k) {
         const int s0 = side_k == 0 ? s - 1 : s + 1;
         if (s0 < 0 || s0 >= G.S) continue;
@@ -406,7 +406,17 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
               if (in_window) {
                 k2g = kk;
                 const float h2f = G.model == LEO2D_MODEL_SIMPLE ? d2f + dzf * dzf : d2f;
-                if ((kFill || !G.keep_zeros) && h2f < kHopHi * kHopHi) {
+                if (!kFill && !G.keep_zeros && G.model == LEO2D_MODEL_SIMPLE && h2f < kHopHi * kHopHi) {
+                  // counting only needs t != 0: the simple model's hopping (and its
+                  // quotient by a finite rescale) is non-zero exactly when the FP64
+                  // distance of `interlayer` is below 8 A; FP32 decides away from 8 A
+                  bool nz = h2f < kHopLo * kHopLo;
+                  if (!nz) {
+                    const double v0 = pos[3 * kk] - x1, v1 = pos[3 * kk + 1] - y1, v2 = pos[3 * kk + 2] - z1;
+                    nz = sqrt(v0 * v0 + v1 * v1 + v2 * v2) < 8.0;
+                  }
+                  t = nz ? 1.0 : 0.0;
+                } else if ((kFill || !G.keep_zeros) && h2f < kHopHi * kHopHi) {
                   const double x2 = pos[3 * kk], y2 = pos[3 * kk + 1], z2 = pos[3 * kk + 2];
                   const double v = interlayer(G.model, l0, l, x2 - x1, y2 - y1, z2 - z1, sh.angle, o0.angle);
                   t = v != 0.0 ? v / G.rescale : 0.0;

@@ -419,10 +419,141 @@ __device__ int rb_block_scan(int x, int* total) {
   return incl - x;
 }
 
+constexpr int kRbWarpCap = 512;     // entries of a row block the warp-per-block build sorts
+constexpr int kRbWarpsPerCta = 8;
+
+// The same two passes with one warp per row block, for blocks of at most
+// kRbWarpCap entries (a twisted bilayer's 4 rows hold about 260): the keys are
+// sorted in the warp's slice of shared memory with warp barriers only. Larger
+// blocks are appended to `big` in pass 0 and left to k_rb_build.
+__global__ void __launch_bounds__(kRbWarpsPerCta * 32)
+    k_rb_build_warp(int64_t n, int64_t nrb, const int64_t* __restrict__ prow, const int32_t* __restrict__ pcol,
+                    const float* __restrict__ pval, const float* __restrict__ pval_im, int pass,
+                    int64_t* __restrict__ count, const int64_t* __restrict__ off, unsigned char* __restrict__ data,
+                    float* __restrict__ im_out, int* __restrict__ err, unsigned long long* __restrict__ ssum,
+                    int64_t* __restrict__ big, unsigned long long* __restrict__ n_big) {
+  __shared__ unsigned long long keys_all[kRbWarpsPerCta][kRbWarpCap];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long* keys = keys_all[w];
+  const int64_t warps = (int64_t)gridDim.x * kRbWarpsPerCta;
+  for (int64_t b = (int64_t)blockIdx.x * kRbWarpsPerCta + w; b < nrb; b += warps) {
+    const int64_t r0 = b * kRbRows;
+    const int rows = (int)min((int64_t)kRbRows, n - r0);
+    const int64_t mine = lane <= kRbRows ? prow[r0 + min(lane, rows)] : 0;
+    int64_t srp[kRbRows + 1];
+#pragma unroll
+    for (int k = 0; k <= kRbRows; ++k) srp[k] = __shfl_sync(0xffffffffu, mine, k);
+    // srp[k] with k in registers (a run-time index would put srp in local memory)
+    auto srp_at = [&](int k) {
+      int64_t v = srp[0];
+#pragma unroll
+      for (int kk = 1; kk <= kRbRows; ++kk)
+        if (k == kk) v = srp[kk];
+      return v;
+    };
+    const int64_t q0 = srp[0];
+    const int E = (int)(srp_at(rows) - q0);
+    if (E > kRbWarpCap) {
+      if (pass == 0 && lane == 0) big[atomicAdd(n_big, 1ull)] = b;
+      continue;
+    }
+    int P2 = 32;
+    while (P2 < E) P2 <<= 1;
+    __syncwarp();  // the previous block's keys are read
+    for (int i = lane; i < P2; i += 32)
+      keys[i] = i < E ? (((unsigned long long)(uint32_t)pcol[q0 + i] << 16) | (unsigned long long)i) : ~0ull;
+    __syncwarp();
+    for (int k = 2; k <= P2; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int i = lane; i < P2; i += 32) {
+          const int ixj = i ^ j;
+          if (ixj > i) {
+            const bool up = (i & k) == 0;
+            const unsigned long long x = keys[i], y = keys[ixj];
+            if ((x > y) == up) {
+              keys[i] = y;
+              keys[ixj] = x;
+            }
+          }
+        }
+        __syncwarp();
+      }
+    // slot of each sorted entry: distinct columns counted in order
+    const int per = P2 / 32;
+    const int i0 = lane * per;
+    int cnt = 0;
+    for (int j = 0; j < per; ++j) {
+      const int i = i0 + j;
+      if (i < E && (i == 0 || (keys[i] >> 16) != (keys[i - 1] >> 16))) ++cnt;
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int K = __shfl_sync(0xffffffffu, incl, 31);
+    const int first_slot = incl - cnt;
+    const int Kp = (K + 3) & ~3;
+    if (pass == 0) {
+      if (lane == 0) {
+        if (Kp > kRbMaxSlots) atomicOr(&err[0], 2);
+        count[b] = Kp;
+        atomicMax(&err[1], K);
+        atomicAdd(ssum, (unsigned long long)K);
+      }
+      continue;
+    }
+    int32_t* col_out = reinterpret_cast<int32_t*>(data + off[b] * kRbSlotBytes);
+    float* val_out = reinterpret_cast<float*>(data + off[b] * kRbSlotBytes + (size_t)Kp * 4);
+    for (int i = lane; i < Kp * kRbRows; i += 32) val_out[i] = 0.f;
+    const int32_t pad_col = K > 0 ? (int32_t)(keys[0] >> 16) : 0;
+    for (int s = K + lane; s < Kp; s += 32) col_out[s] = pad_col;
+    __syncwarp();
+    int s = first_slot - 1;
+    for (int j = 0; j < per; ++j) {
+      const int i = i0 + j;
+      if (i >= E) break;
+      const unsigned long long k = keys[i];
+      const uint32_t c = (uint32_t)(k >> 16);
+      const int e = (int)(k & 0xFFFFu);
+      const bool new_col = i == 0 || (keys[i - 1] >> 16) != c;
+      if (new_col) {
+        ++s;
+        col_out[s] = (int32_t)c;
+      }
+      int r = 0;
+#pragma unroll
+      for (int k = 1; k < kRbRows; ++k) r += (k < rows && srp[k] - q0 <= e) ? 1 : 0;
+      const int64_t row_lo = srp_at(r) - q0, row_hi = srp_at(r + 1) - q0;
+      // the first entry of each (column, row) run sums the run in entry order
+      bool start = new_col;
+      if (!start) {
+        const int ep = (int)(keys[i - 1] & 0xFFFFu);
+        start = !(row_lo <= ep);
+      }
+      if (start) {
+        float v = pval[q0 + e];
+        float vi = pval_im ? pval_im[q0 + e] : 0.f;
+        for (int m = i + 1; m < E && (uint32_t)(keys[m] >> 16) == c; ++m) {
+          const int em = (int)(keys[m] & 0xFFFFu);
+          if (em >= row_hi) break;
+          v += pval[q0 + em];
+          if (pval_im) vi += pval_im[q0 + em];
+        }
+        val_out[s * kRbRows + r] = v;
+        if (im_out) im_out[(off[b] + s) * kRbRows + r] = vi;
+      }
+    }
+  }
+}
+
 // Pass 0: count[b] = slots of row block b (union of its rows' columns, padded
 // to a multiple of 4). Pass 1: writes row block b at data + 20 * off[b].
 // err[0]: bit 0 a block with more than kRbMaxEnt entries, bit 1 more than
 // kRbMaxSlots slots; err[1] most slots (before padding); ssum: sum of slots.
+// One block of threads per row block: the row blocks in `list` (n_list of
+// them), or every row block when list is null.
 __global__ void __launch_bounds__(kRbBuildThreads) k_rb_build(int64_t n, int64_t nrb, const int64_t* __restrict__ prow,
                                                               const int32_t* __restrict__ pcol,
                                                               const float* __restrict__ pval,
@@ -431,10 +562,13 @@ __global__ void __launch_bounds__(kRbBuildThreads) k_rb_build(int64_t n, int64_t
                                                               const int64_t* __restrict__ off,
                                                               unsigned char* __restrict__ data, float* __restrict__ im_out,
                                                               int* __restrict__ err,
-                                                              unsigned long long* __restrict__ ssum) {
+                                                              unsigned long long* __restrict__ ssum,
+                                                              const int64_t* __restrict__ list, int64_t n_list) {
   extern __shared__ unsigned long long rb_keys[];  // kRbMaxEnt keys: column << 16 | entry
   __shared__ int64_t srp[kRbRows + 1];
-  for (int64_t b = blockIdx.x; b < nrb; b += gridDim.x) {
+  const int64_t todo = list ? n_list : nrb;
+  for (int64_t t = blockIdx.x; t < todo; t += gridDim.x) {
+    const int64_t b = list ? list[t] : t;
     const int64_t r0 = b * kRbRows;
     const int rows = (int)min((int64_t)kRbRows, n - r0);
     if (threadIdx.x <= kRbRows) srp[threadIdx.x] = prow[r0 + min((int)threadIdx.x, rows)];
@@ -631,12 +765,29 @@ bool csr_build_rb(leo2d_ctx* ctx, leo2d_csr* csr) {
   LEO_CUDA(cudaMemsetAsync(ssum.p, 0, sizeof(unsigned long long), ctx->stream));
   const size_t smem = (size_t)kRbMaxEnt * sizeof(unsigned long long);
   LEO_CUDA(cudaFuncSetAttribute(k_rb_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const unsigned grid = (unsigned)std::min<int64_t>(nrb, (int64_t)ctx->sm_count * 4);
+  // a warp per row block; the blocks with more entries than it sorts go to the
+  // block-wide kernel (listed in pass 0, the same list in pass 1)
+  DevBuf<int64_t> big((size_t)nrb);
+  DevBuf<unsigned long long> n_big(1);
+  LEO_CUDA(cudaMemsetAsync(n_big.p, 0, sizeof(unsigned long long), ctx->stream));
+  const unsigned wgrid =
+      (unsigned)std::min<int64_t>((nrb + kRbWarpsPerCta - 1) / kRbWarpsPerCta, (int64_t)ctx->sm_count * 16);
   launch(ctx, "rb_build", [&] {
-    k_rb_build<<<grid, kRbBuildThreads, smem, ctx->stream>>>(n, nrb, csr->prow.p, csr->pcol.p, csr->pval32.p,
-                                                              nullptr, 0, cnt.p, nullptr, nullptr, nullptr, err.p,
-                                                              ssum.p);
+    k_rb_build_warp<<<wgrid, kRbWarpsPerCta * 32, 0, ctx->stream>>>(n, nrb, csr->prow.p, csr->pcol.p,
+                                                                    csr->pval32.p, nullptr, 0, cnt.p, nullptr,
+                                                                    nullptr, nullptr, err.p, ssum.p, big.p, n_big.p);
   });
+  unsigned long long hb = 0;
+  d2h(ctx, &hb, n_big.p, 1);
+  ctx_sync(ctx);
+  const int64_t nb = (int64_t)hb;
+  const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(nb, (int64_t)ctx->sm_count * 4));
+  if (nb > 0)
+    launch(ctx, "rb_build", [&] {
+      k_rb_build<<<grid, kRbBuildThreads, smem, ctx->stream>>>(n, nrb, csr->prow.p, csr->pcol.p, csr->pval32.p,
+                                                                nullptr, 0, cnt.p, nullptr, nullptr, nullptr, err.p,
+                                                                ssum.p, big.p, nb);
+    });
   int h[2] = {0, 0};
   unsigned long long hs = 0;
   d2h(ctx, h, err.p, 2);
@@ -661,9 +812,15 @@ bool csr_build_rb(leo2d_ctx* ctx, leo2d_csr* csr) {
                              ctx->stream));
   }
   launch(ctx, "rb_build", [&] {
-    k_rb_build<<<grid, kRbBuildThreads, smem, ctx->stream>>>(
+    k_rb_build_warp<<<wgrid, kRbWarpsPerCta * 32, 0, ctx->stream>>>(
         n, nrb, csr->prow.p, csr->pcol.p, csr->pval32.p, csr->complex_h ? csr->pval_im32.p : nullptr, 1, nullptr,
-        csr->rb_off.p, csr->rb_data.p, csr->complex_h ? csr->rb_im.p : nullptr, err.p, ssum.p);
+        csr->rb_off.p, csr->rb_data.p, csr->complex_h ? csr->rb_im.p : nullptr, err.p, ssum.p, big.p, n_big.p);
+  });
+  if (nb > 0)
+    launch(ctx, "rb_build", [&] {
+      k_rb_build<<<grid, kRbBuildThreads, smem, ctx->stream>>>(
+          n, nrb, csr->prow.p, csr->pcol.p, csr->pval32.p, csr->complex_h ? csr->pval_im32.p : nullptr, 1, nullptr,
+          csr->rb_off.p, csr->rb_data.p, csr->complex_h ? csr->rb_im.p : nullptr, err.p, ssum.p, big.p, nb);
   });
   ctx_sync(ctx);
   csr->rb_blocks = nrb;

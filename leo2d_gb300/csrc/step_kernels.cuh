@@ -628,15 +628,31 @@ __device__ __forceinline__ double phase_entry(int64_t row, int c, uint64_t seed,
   return (c & 1) ? sin(phi) : cos(phi);
 }
 
+// One thread per (row, complex vector): one Philox draw and one FP64 sincos for
+// both columns (the values of phase_entry's cos and sin).
 template <typename T>
 __global__ void k_fill_phase(int64_t n, int C, T* __restrict__ x, uint64_t seed, uint64_t first,
                              int n_complex, const int32_t* __restrict__ new2old) {
-  const int64_t total = n * C;
+  const int V = C >> 1;
+  const int64_t total = n * V;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t row = new2old ? (int64_t)new2old[e / C] : e / C;
-    const int c = (int)(e % C);
-    x[e] = (c >> 1) < n_complex ? (T)(float)phase_entry(row, c, seed, first) : T(0);
+    const int64_t r = e / V;
+    const int v = (int)(e % V);
+    T re = T(0), im = T(0);
+    if (v < n_complex) {
+      const int64_t row = new2old ? (int64_t)new2old[r] : r;
+      const uint64_t vv = first + (uint64_t)v;
+      uint32_t ctr[4] = {(uint32_t)row, (uint32_t)((uint64_t)row >> 32), (uint32_t)vv, (uint32_t)(vv >> 32)};
+      philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32));
+      const double u = (double)(ctr[0] >> 8) * (1.0 / 16777216.0);
+      double s, c;
+      sincos(6.283185307179586 * u, &s, &c);
+      re = (T)(float)c;
+      im = (T)(float)s;
+    }
+    x[r * C + 2 * v] = re;
+    x[r * C + 2 * v + 1] = im;
   }
 }
 
