@@ -60,6 +60,7 @@ struct GeomDev {
   int S, model, bc, sc_search, keep_zeros, with_dx;
   double supercell[2][2];
   double rescale, shift;
+  double simple_amp;  // 0.33 / rescale (the simple model's interlayer prefactor)
   double b_field;  // non-zero: complex entries t e^{i phi} (Peierls phase)
   double kx, ky;   // Bloch vector: phases k.(r_col - r_row) per periodic image
   int cpx;         // complex entries (a field or a Bloch vector)
@@ -174,13 +175,21 @@ __device__ double c_to_c(int orow, int ocol, double v0, double v1, double v2, do
   return 0.;
 }
 
-__device__ __forceinline__ double interlayer(int model, int orow, int ocol, double v0, double v1,
-                                             double v2, double th_row, double th_col) {
+// Interlayer hopping divided by the energy rescale (generateRealH's
+// raw_t / energy_rescale). The simple model, (0.33 / rescale) exp(-(r - 3.35) /
+// 0.45) for the 3-D distance r < 8 A, takes both quotients as products (by the
+// host's 0.33 / rescale and by the FP64 value of 1 / 0.45): FP64 division is
+// the costly part of assembly on GB300's FP64 pipe. The reference model keeps
+// the division, bit for bit.
+__device__ __forceinline__ double interlayer_t(int model, int orow, int ocol, double v0, double v1, double v2,
+                                               double th_row, double th_col, double rescale, double simple_amp) {
   if (model == LEO2D_MODEL_SIMPLE) {
-    double r = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
-    return r < 8.0 ? 0.33 * exp(-(r - 3.35) / 0.45) : 0.0;
+    constexpr double kInvDecay = 1.0 / 0.45;
+    const double r = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
+    return r < 8.0 ? simple_amp * exp(-(r - 3.35) * kInvDecay) : 0.0;
   }
-  return c_to_c(orow, ocol, v0, v1, v2, th_row, th_col);
+  const double v = c_to_c(orow, ocol, v0, v1, v2, th_row, th_col);
+  return v != 0.0 ? v / rescale : 0.0;
 }
 
 __device__ __forceinline__ int sheet_of(const GeomDev& G, int64_t k) {
@@ -418,8 +427,8 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
                   t = nz ? 1.0 : 0.0;
                 } else if ((kFill || !G.keep_zeros) && h2f < kHopHi * kHopHi) {
                   const double x2 = pos[3 * kk], y2 = pos[3 * kk + 1], z2 = pos[3 * kk + 2];
-                  const double v = interlayer(G.model, l0, l, x2 - x1, y2 - y1, z2 - z1, sh.angle, o0.angle);
-                  t = v != 0.0 ? v / G.rescale : 0.0;
+                  t = interlayer_t(G.model, l0, l, x2 - x1, y2 - y1, z2 - z1, sh.angle, o0.angle, G.rescale,
+                                   G.simple_amp);
                 }
               }
             }
@@ -488,8 +497,8 @@ __device__ double periodic_value(const GeomDev& G, int64_t row, const int32_t* g
   }
   const double z1 = pos[3 * row + 2];
   const double x2 = pos[3 * k2], y2 = pos[3 * k2 + 1], z2 = pos[3 * k2 + 2];
-  return interlayer(G.model, l0, l2, x2 - x1, y2 - y1, z2 - z1, G.sh[s].angle, G.sh[s2].angle) /
-         G.rescale;
+  return interlayer_t(G.model, l0, l2, x2 - x1, y2 - y1, z2 - z1, G.sh[s].angle, G.sh[s2].angle, G.rescale,
+                      G.simple_amp);
 }
 
 __device__ void block_bitonic_sort(uint64_t* keys, int n2) {
@@ -911,6 +920,7 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
                 "the velocity operator (WITH_DX, conductivity) is not built for a complex Hamiltonian");
     std::memcpy(G.supercell, g->supercell, sizeof(G.supercell));
     G.rescale = g->energy_rescale;
+    G.simple_amp = 0.33 / g->energy_rescale;
     G.shift = g->energy_shift;
     for (int s = 0; s < G.S; ++s) fill_sheet(*g, s, G.sh[s]);
 

@@ -104,17 +104,23 @@ double c_to_c(int orow, int ocol, double v0, double v1, double v2, double theta_
   return 0.;
 }
 
-// Simple interlayer model: 0.33 exp(-(r - 3.35)/0.45) eV for 3-D distance r < 8 A.
-double simple_inter(double v0, double v1, double v2) {
+// Simple interlayer model, already divided by the energy rescale:
+// (0.33 / rescale) exp(-(r - 3.35) / 0.45) for the 3-D distance r < 8 A, with
+// the quotients taken as products by (0.33 / rescale) and by the FP64 value of
+// 1 / 0.45 (the form the device assembly evaluates).
+double simple_inter_t(double v0, double v1, double v2, double rescale) {
+  const double inv_decay = 1.0 / 0.45;
+  const double amp = 0.33 / rescale;
   double r = std::sqrt(v0 * v0 + v1 * v1 + v2 * v2);
-  if (r < 8.0) return 0.33 * std::exp(-(r - 3.35) / 0.45);
+  if (r < 8.0) return amp * std::exp(-(r - 3.35) * inv_decay);
   return 0.0;
 }
 
-double interlayer(int model, int orow, int ocol, double v0, double v1, double v2, double th_row,
-                  double th_col) {
-  if (model == LEO2D_MODEL_SIMPLE) return simple_inter(v0, v1, v2);
-  return c_to_c(orow, ocol, v0, v1, v2, th_row, th_col);
+// Interlayer hopping divided by the energy rescale (generateRealH's t / energy_rescale).
+double interlayer_t(int model, int orow, int ocol, double v0, double v1, double v2, double th_row,
+                    double th_col, double rescale) {
+  if (model == LEO2D_MODEL_SIMPLE) return simple_inter_t(v0, v1, v2, rescale);
+  return c_to_c(orow, ocol, v0, v1, v2, th_row, th_col) / rescale;
 }
 
 // ---------------------------------------------------------------- sheets
@@ -497,7 +503,7 @@ int oracle_build(const leo2d_geom* gin, oracle_h** out) {
       double x2 = P[3 * nk], y2 = P[3 * nk + 1], z2 = P[3 * nk + 2];
       int o1 = h->grid4[4 * ki + 2], o2 = h->grid4[4 * nk + 2];
       double th1 = g.angles[h->grid4[4 * ki + 3]], th2 = g.angles[h->grid4[4 * nk + 3]];
-      double t = interlayer(g.model, o1, o2, x2 - x1, y2 - y1, z2 - z1, th1, th2) / rescale;
+      double t = interlayer_t(g.model, o1, o2, x2 - x1, y2 - y1, z2 - z1, th1, th2, rescale);
       if (t != 0) {
         h->val[cnt] += t;
         h->dx[cnt] += (x1 - x2) * t;
@@ -561,7 +567,7 @@ void oracle_bloch(const oracle_h* h, double kx, double ky, double* re, double* i
       const double x2 = P[3 * pr.j], y2 = P[3 * pr.j + 1], z2 = P[3 * pr.j + 2];
       const int o1 = h->grid4[4 * ki + 2], o2 = h->grid4[4 * pr.j + 2];
       const double th1 = g.angles[h->grid4[4 * ki + 3]], th2 = g.angles[h->grid4[4 * pr.j + 3]];
-      add(pr, ki, interlayer(g.model, o1, o2, x2 - x1, y2 - y1, z2 - z1, th1, th2) / rescale);
+      add(pr, ki, interlayer_t(g.model, o1, o2, x2 - x1, y2 - y1, z2 - z1, th1, th2, rescale));
       if (ec + 1 == n_inter || h->inter[ec + 1].i != ki || h->inter[ec + 1].j != pr.j) ++cnt;
       ++ec;
     }
