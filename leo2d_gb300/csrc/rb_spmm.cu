@@ -423,9 +423,10 @@ constexpr int kRbWarpCap = 512;     // entries of a row block the warp-per-block
 constexpr int kRbWarpsPerCta = 8;
 
 // The same two passes with one warp per row block, for blocks of at most
-// kRbWarpCap entries (a twisted bilayer's 4 rows hold about 260): the keys are
-// sorted in the warp's slice of shared memory with warp barriers only. Larger
-// blocks are appended to `big` in pass 0 and left to k_rb_build.
+// kRbWarpCap entries (a twisted bilayer's 4 rows hold about 260), with warp
+// barriers only: pass 0 counts the distinct columns in a hash set, pass 1 sorts
+// the keys in the warp's slice of shared memory. Larger blocks are appended to
+// `big` in pass 0 and left to k_rb_build.
 __global__ void __launch_bounds__(kRbWarpsPerCta * 32)
     k_rb_build_warp(int64_t n, int64_t nrb, const int64_t* __restrict__ prow, const int32_t* __restrict__ pcol,
                     const float* __restrict__ pval, const float* __restrict__ pval_im, int pass,
@@ -457,9 +458,41 @@ __global__ void __launch_bounds__(kRbWarpsPerCta * 32)
       if (pass == 0 && lane == 0) big[atomicAdd(n_big, 1ull)] = b;
       continue;
     }
+    __syncwarp();  // the previous block's keys are read
+    if (pass == 0) {
+      // counting needs the distinct columns only: a hash set in the warp's slice
+      // (2 x kRbWarpCap 32-bit slots, load <= 1/2), no sort
+      uint32_t* set = reinterpret_cast<uint32_t*>(keys);
+      constexpr int kSet = 2 * kRbWarpCap;
+      for (int i = lane; i < kSet; i += 32) set[i] = 0xFFFFFFFFu;
+      __syncwarp();
+      int fresh = 0;
+      for (int i = lane; i < E; i += 32) {
+        const uint32_t c = (uint32_t)pcol[q0 + i];
+        uint32_t h = (c * 2654435761u) & (kSet - 1);
+        for (int probe = 0; probe < kSet; ++probe) {  // bounded: the set never fills
+          const uint32_t prev = atomicCAS(&set[h], 0xFFFFFFFFu, c);
+          if (prev == 0xFFFFFFFFu) {
+            ++fresh;
+            break;
+          }
+          if (prev == c) break;
+          h = (h + 1) & (kSet - 1);
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) fresh += __shfl_xor_sync(0xffffffffu, fresh, o);
+      if (lane == 0) {
+        const int K = fresh, Kp = (K + 3) & ~3;
+        if (Kp > kRbMaxSlots) atomicOr(&err[0], 2);
+        count[b] = Kp;
+        atomicMax(&err[1], K);
+        atomicAdd(ssum, (unsigned long long)K);
+      }
+      continue;
+    }
     int P2 = 32;
     while (P2 < E) P2 <<= 1;
-    __syncwarp();  // the previous block's keys are read
     for (int i = lane; i < P2; i += 32)
       keys[i] = i < E ? (((unsigned long long)(uint32_t)pcol[q0 + i] << 16) | (unsigned long long)i) : ~0ull;
     __syncwarp();
@@ -495,15 +528,6 @@ __global__ void __launch_bounds__(kRbWarpsPerCta * 32)
     const int K = __shfl_sync(0xffffffffu, incl, 31);
     const int first_slot = incl - cnt;
     const int Kp = (K + 3) & ~3;
-    if (pass == 0) {
-      if (lane == 0) {
-        if (Kp > kRbMaxSlots) atomicOr(&err[0], 2);
-        count[b] = Kp;
-        atomicMax(&err[1], K);
-        atomicAdd(ssum, (unsigned long long)K);
-      }
-      continue;
-    }
     int32_t* col_out = reinterpret_cast<int32_t*>(data + off[b] * kRbSlotBytes);
     float* val_out = reinterpret_cast<float*>(data + off[b] * kRbSlotBytes + (size_t)Kp * 4);
     for (int i = lane; i < Kp * kRbRows; i += 32) val_out[i] = 0.f;

@@ -162,3 +162,22 @@ def test_bloch_supercell_on_a_k_grid(ctx):
         vre, vim = oracle.phase_vectors(seed, 0, R, csr.n)
         ref = oracle.kpm_trace_cpx_doubling(rp, col, ore, oim, vre, vim, P)
         assert _rel(mu, ref) < FP32_RTOL
+
+
+def test_bloch_phase_on_a_flake_is_a_gauge(ctx):
+    """On a flake, k.(r_col - r_row) phases are a diagonal unitary change of basis:
+    local DOS moments are unchanged (to FP32 rounding) and the matrix entries keep
+    their moduli."""
+    g0 = L.make_geom(model=L.MODEL_SIMPLE, size=20, angles_deg=(0.0, 3.0), energy_rescale=13.0)
+    gk = L.make_geom(model=L.MODEL_SIMPLE, size=20, angles_deg=(0.0, 3.0), energy_rescale=13.0, k_vec=(0.31, -0.17))
+    c0 = ctx.build_csr(ctx.prepare(g0), keep_zeros=True)
+    ck = ctx.build_csr(ctx.prepare(gk), keep_zeros=True)
+    rp0, col0, v0 = c0.download()
+    rpk, colk, vk = ck.download()
+    imk = ck.download_imag()
+    assert np.array_equal(rp0, rpk) and np.array_equal(col0, colk)
+    np.testing.assert_allclose(np.hypot(vk, imk), np.abs(v0), rtol=1e-14, atol=1e-16)
+    assert np.abs(imk).max() > 0.1 * np.abs(v0).max()
+    targets = np.array([5, 100, 333])
+    cfg = L.kpm_cfg(64, precision=L.FP32)
+    assert _rel(ck.kpm_ldos(cfg, targets), c0.kpm_ldos(cfg, targets)) < FP32_RTOL
