@@ -271,6 +271,8 @@ struct RowOut {
   double* dx;
   double* dy;
   double* val_im;  // imaginary parts (complex entries)
+  int pad_cap;     // padded single pass: entries per row of the padded arrays
+  int* overflow;   // padded single pass: set when a row has more entries than pad_cap
 };
 
 // Locality::peierlsPhase (locality.cpp:7157-7161): the phase of the hopping
@@ -296,8 +298,10 @@ __device__ __forceinline__ void store_value(const GeomDev& G, const RowOut& out,
   // generateCpxH's phase: the Peierls phase plus k.(r2 - r1) (locality.cpp:4896-4900)
   double ph = peierls_phase(x1, x2, y1, y2, G.b_field);
   ph = ph + G.kx * (x2 - x1) + G.ky * (y2 - y1);
-  out.val[e] = 0.0 + t * cos(ph);
-  out.val_im[e] = 0.0 + t * sin(ph);
+  double sn, cs;
+  sincos(ph, &sn, &cs);  // one argument reduction for both
+  out.val[e] = 0.0 + t * cs;
+  out.val_im[e] = 0.0 + t * sn;
 }
 
 // FP32 copy of the positions for the candidate prefilter of k_flake_rows.
@@ -312,11 +316,15 @@ __global__ void k_pos32(const double* __restrict__ pos, int64_t n, float4* __res
 // test decides, so the kept pairs and their values are those of FP64 alone.
 constexpr float kPrefilterMargin = 0.05f;
 
-template <bool kFill>
+// kMode 0: count entries per row; 1: fill at the scanned row pointers; 2: fill
+// and count in one pass, row r at r * pad_cap of padded arrays (entries past
+// pad_cap are counted, not stored, and raise `overflow`).
+template <int kMode>
 __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ GeomDev G, int64_t n,
                                                     const int32_t* __restrict__ grid4,
                                                     const double* __restrict__ pos,
                                                     const float4* __restrict__ pos32, RowOut out) {
+  constexpr bool kFill = kMode != 0, kPad = kMode == 2;
   const unsigned lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -325,7 +333,8 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
               s = grid4[4 * row + 3];
     const SheetDev& sh = G.sh[s];
     const double x1 = pos[3 * row] + 0.0, y1 = pos[3 * row + 1] + 0.0, z1 = pos[3 * row + 2];
-    int64_t o = kFill ? out.rowptr[row] : 0;
+    int64_t o = kPad ? row * (int64_t)out.pad_cap : (kFill ? out.rowptr[row] : 0);
+    const int64_t o_end = kPad ? o + out.pad_cap : 0;
     int64_t n_ent = 0, n_intra = 0, n_inter = 0;
 
     // intralayer: window [i0-4, i0+4) x [j0-4, j0+4) x orbitals, every candidate kept
@@ -357,7 +366,7 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
         const bool store = keep && (G.keep_zeros || t != 0 || k2g == row);
         const unsigned m = __ballot_sync(0xffffffffu, store);
         n_intra += __popc(__ballot_sync(0xffffffffu, keep));
-        if (kFill && store) {
+        if (kFill && store && (!kPad || o + __popc(m & lt_mask) < o_end)) {
           const int64_t e = o + __popc(m & lt_mask);
           out.col[e] = (int32_t)k2g;
           const double x2 = pos[3 * k2g], y2 = pos[3 * k2g + 1];
@@ -437,7 +446,7 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
           const bool store = keep && (G.keep_zeros || t != 0);
           const unsigned m = __ballot_sync(0xffffffffu, store);
           n_inter += __popc(__ballot_sync(0xffffffffu, keep));
-          if (kFill && store) {
+          if (kFill && store && (!kPad || o + __popc(m & lt_mask) < o_end)) {
             const int64_t e = o + __popc(m & lt_mask);
             out.col[e] = (int32_t)k2g;
             const double x2 = pos[3 * k2g], y2 = pos[3 * k2g + 1];
@@ -452,10 +461,30 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
         }
       }
     }
-    if (!kFill && lane == 0) {
+    if ((!kFill || kPad) && lane == 0) {
       out.cnt_ent[row] = n_ent;
       out.cnt_intra[row] = n_intra;
       out.cnt_inter[row] = n_inter;
+      if (kPad && n_ent > out.pad_cap) atomicOr(out.overflow, 1);
+    }
+  }
+}
+
+// Copies each row's entries from the padded arrays of the single pass into the
+// CSR arrays (a warp per row).
+__global__ void k_unpad_rows(int64_t n, int cap, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ pcol,
+                             const double* __restrict__ pval, const double* __restrict__ pdx,
+                             const double* __restrict__ pdy, const double* __restrict__ pim, RowOut out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+    const int64_t o = rowptr[r], len = rowptr[r + 1] - o, src = r * (int64_t)cap;
+    for (int64_t i = lane; i < len; i += 32) {
+      out.col[o + i] = pcol[src + i];
+      out.val[o + i] = pval[src + i];
+      if (pdx) out.dx[o + i] = pdx[src + i];
+      if (pdy) out.dy[o + i] = pdy[src + i];
+      if (pim) out.val_im[o + i] = pim[src + i];
     }
   }
 }
@@ -669,8 +698,10 @@ __global__ void __launch_bounds__(256) k_periodic_rows(const __grid_constant__ G
             if (G.cpx) {
               // std::polar(t, k.(r2 - r1)) summed over the images (locality.cpp:4896-4941)
               const double ph = G.kx * (pos[3 * k2] - x1) + G.ky * (pos[3 * k2 + 1] - y1);
-              v += t * cos(ph);
-              vim += t * sin(ph);
+              double sn, cs;
+              sincos(ph, &sn, &cs);
+              v += t * cs;
+              vim += t * sn;
             } else {
               v += t;
             }
@@ -989,10 +1020,71 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
         k_pos32<<<grid_for(n, 256, (int64_t)ctx->sm_count * 32), 256, 0, ctx->stream>>>(csr->pos.p, n, pos32.p);
       });
     const unsigned cta_grid = grid_for(n, 1, (int64_t)ctx->sm_count * 8);
+    // A flake of the simple model without stored zeros (about 67 entries per
+    // row) takes one pass: rows are filled into padded arrays of kPadCap
+    // entries while they are counted, then compacted. A row with more entries,
+    // or padded arrays too large for a quarter of free memory, takes the
+    // count and fill passes.
+    constexpr int kPadCap = 96;
+    if (G.bc == 0 && n > 0 && G.model == LEO2D_MODEL_SIMPLE && !G.keep_zeros) {
+      const size_t per = sizeof(int32_t) + sizeof(double) * (1 + (G.with_dx ? 2 : 0) + (G.cpx ? 1 : 0));
+      size_t fr = 0, tot = 0;
+      LEO_CUDA(cudaMemGetInfo(&fr, &tot));
+      if ((size_t)n * kPadCap * per <= fr / 4) {
+        const size_t pn = (size_t)n * kPadCap;
+        DevBuf<int32_t> pcol(pn);
+        DevBuf<double> pval(pn), pdx(G.with_dx ? pn : 0), pdy(G.with_dx ? pn : 0), pim(G.cpx ? pn : 0);
+        DevBuf<int> overflow(1);
+        LEO_CUDA(cudaMemsetAsync(overflow.p, 0, sizeof(int), ctx->stream));
+        RowOut rp = ro;
+        rp.col = pcol.p;
+        rp.val = pval.p;
+        rp.dx = pdx.p;
+        rp.dy = pdy.p;
+        rp.val_im = pim.p;
+        rp.pad_cap = kPadCap;
+        rp.overflow = overflow.p;
+        launch(ctx, "flake_rows_fill", [&] {
+          k_flake_rows<2><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, rp);
+        });
+        int over = 0;
+        d2h(ctx, &over, overflow.p, 1);
+        ctx_sync(ctx);
+        if (!over) {
+          exclusive_scan_i64(ctx, cnt_ent.p, csr->rowptr.p, n);
+          int64_t nnz = 0;
+          d2h(ctx, &nnz, csr->rowptr.p + n, 1);
+          ctx_sync(ctx);
+          csr->nnz = nnz;
+          csr->n_intra = reduce_sum_i64(ctx, cnt_intra.p, n);
+          csr->n_inter = reduce_sum_i64(ctx, cnt_inter.p, n);
+          csr_alloc_entries(ctx, csr, nnz, G.with_dx != 0);
+          csr->complex_h = G.cpx != 0;
+          if (csr->complex_h) {
+            csr->val_im64.alloc(nnz + kCsrPad);
+            LEO_CUDA(cudaMemsetAsync(csr->val_im64.p, 0, (nnz + kCsrPad) * sizeof(double), ctx->stream));
+          }
+          RowOut fo = ro;
+          fo.col = csr->col.p;
+          fo.val = csr->val64.p;
+          fo.dx = csr->dx64.p;
+          fo.dy = csr->dy64.p;
+          fo.val_im = csr->val_im64.p;
+          launch(ctx, "unpad_rows", [&] {
+            k_unpad_rows<<<grid_for(n * 32, 256, (int64_t)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
+                n, kPadCap, csr->rowptr.p, pcol.p, pval.p, pdx.p, pdy.p, pim.p, fo);
+          });
+          ctx_check_status(ctx, "leo2d_build_csr (single pass)");
+          csr_refresh_fp32(ctx, csr);
+          ctx_sync(ctx);
+          return;  // (the guard's lambda)
+        }
+      }
+    }
     if (n > 0) {
       if (G.bc == 0)
         launch(ctx, "flake_rows_count", [&] {
-          k_flake_rows<false><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, ro);
+          k_flake_rows<0><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, ro);
         });
       else
         launch(ctx, "periodic_rows_count", [&] {
@@ -1022,7 +1114,7 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     if (n > 0) {
       if (G.bc == 0)
         launch(ctx, "flake_rows_fill", [&] {
-          k_flake_rows<true><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, ro);
+          k_flake_rows<1><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, ro);
         });
       else
         launch(ctx, "periodic_rows_fill", [&] {

@@ -54,13 +54,21 @@ def test_flake_vs_oracle(ctx, model, angle, size):
     np.testing.assert_allclose(val, ref.val, rtol=0, atol=VAL_TOL)
     np.testing.assert_allclose(dx, ref.val_dx, rtol=0, atol=1e-10)
     # compact layout: the reference's entries with non-zero value, diagonal always kept
-    c = ctx.build_csr(gp)
-    crp, ccol, cval = c.download()
+    # (the simple model's compact build is the padded single pass)
+    _check_compact(ctx, gp, ref)
+
+
+def _check_compact(ctx, gp, ref):
+    c = ctx.build_csr(gp, with_dx=True)
+    crp, ccol, cval, cdx, cdy = c.download(dx=True)
     keep = (ref.val != 0) | (ref.col == np.repeat(np.arange(ref.n), np.diff(ref.rowptr)))
     exp_rp = np.concatenate([[0], np.cumsum(np.add.reduceat(keep.astype(np.int64), ref.rowptr[:-1]))])
     assert np.array_equal(crp, exp_rp)
     assert np.array_equal(ccol, ref.col[keep])
     np.testing.assert_allclose(cval, ref.val[keep], rtol=0, atol=VAL_TOL)
+    np.testing.assert_allclose(cdx, ref.val_dx[keep], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(cdy, ref.val_dy[keep], rtol=0, atol=1e-10)
+    return int(np.diff(exp_rp).max())
 
 
 @pytest.mark.parametrize("mn", [(5, 4), (4, 5), (7, 6)])
@@ -83,6 +91,9 @@ def test_trilayer_simple_model(ctx):
     rp, col, val = csr.download()
     assert np.array_equal(rp, ref.rowptr) and np.array_equal(col, ref.col)
     np.testing.assert_allclose(val, ref.val, rtol=0, atol=VAL_TOL)
+    # the middle sheet's rows have more entries than the single pass pads for:
+    # the compact build falls back to the count and fill passes
+    assert _check_compact(ctx, gp, ref) > 96
 
 
 def test_bounds_and_rescale(ctx):
