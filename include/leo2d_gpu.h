@@ -89,6 +89,12 @@ typedef struct {
    * that image, summed per entry, as generateCpxH does (locality.cpp:4896-4941).
    * The energy shift then goes to the home image's diagonal only. */
   double k_vec[2];
+  /* The job's sheet shifts (Job_params "shifts", recursiveShiftCalc,
+   * locality.cpp:1222-1269): sheet s moves by shifts[s][0] a1 + shifts[s][1] a2
+   * of its rotated lattice (setConfigPositions, locality.cpp:3618-3642). As in
+   * the reference, the pairs come from the unshifted geometry and the values,
+   * dxH and the positions the matrix keeps from the shifted one. |shift| <= 1. */
+  double shifts[LEO2D_MAX_SHEETS][2];
 } leo2d_geom;
 
 typedef struct leo2d_ctx leo2d_ctx;

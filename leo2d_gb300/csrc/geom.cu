@@ -52,6 +52,7 @@ struct SheetDev {
   double cos_mt, sin_mt;  // cos/sin(-angle)
   double s1a[2][2];       // rotated lattice of setConfigPositions
   double angle, height;
+  double shift[2];        // the job's sheet shift (fractions of the rotated lattice vectors)
   int64_t base;           // first global index of the sheet
   const int32_t* grid;    // [H][W][n_orb] local index or -1
 };
@@ -64,6 +65,7 @@ struct GeomDev {
   double b_field;  // non-zero: complex entries t e^{i phi} (Peierls phase)
   double kx, ky;   // Bloch vector: phases k.(r_col - r_row) per periodic image
   int cpx;         // complex entries (a field or a Bloch vector)
+  int shifted;     // some sheet is shifted: values from the shifted positions
   SheetDev sh[kMaxSheets];
 };
 
@@ -232,7 +234,7 @@ __global__ void k_site_fill(int64_t cells, const int64_t* __restrict__ mask,
 // grid4 and i2pos of every orbital (Hstruct::setIndex, posAtomIndex, setConfigPositions).
 __global__ void k_sites(const __grid_constant__ GeomDev G, int64_t n,
                         const int32_t* const* __restrict__ site_cells, int32_t* __restrict__ grid4,
-                        double* __restrict__ pos) {
+                        double* __restrict__ pos, double* __restrict__ spos) {
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * blockDim.x) {
     const int s = sheet_of(G, k);
@@ -252,10 +254,16 @@ __global__ void k_sites(const __grid_constant__ GeomDev G, int64_t n,
     double x = lp[0] * sh.cos_t - lp[1] * sh.sin_t + z0 * sh.a[0][0] + z0 * sh.a[1][0];
     double y = lp[0] * sh.sin_t + lp[1] * sh.cos_t + z0 * sh.a[0][1] + z0 * sh.a[1][1];
     double z = lp[2] + sh.height;
-    // i2pos (setConfigPositions with zero job shifts)
+    // i2pos (setConfigPositions with zero job shifts): the positions the pairs come from
     pos[3 * k + 0] = x + z0 * sh.s1a[0][0] + z0 * sh.s1a[1][0];
     pos[3 * k + 1] = y + z0 * sh.s1a[0][1] + z0 * sh.s1a[1][1];
     pos[3 * k + 2] = z;
+    // i2pos with the job's sheet shifts (locality.cpp:3640-3642): the values
+    if (spos) {
+      spos[3 * k + 0] = x + sh.shift[0] * sh.s1a[0][0] + sh.shift[1] * sh.s1a[1][0];
+      spos[3 * k + 1] = y + sh.shift[0] * sh.s1a[0][1] + sh.shift[1] * sh.s1a[1][1];
+      spos[3 * k + 2] = z;
+    }
   }
 }
 
@@ -323,7 +331,9 @@ template <int kMode>
 __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ GeomDev G, int64_t n,
                                                     const int32_t* __restrict__ grid4,
                                                     const double* __restrict__ pos,
-                                                    const float4* __restrict__ pos32, RowOut out) {
+                                                    const float4* __restrict__ pos32,
+                                                    const double* __restrict__ spos,
+                                                    const float4* __restrict__ spos32, RowOut out) {
   constexpr bool kFill = kMode != 0, kPad = kMode == 2;
   const unsigned lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -332,7 +342,11 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
     const int ih = grid4[4 * row], jh = grid4[4 * row + 1], l0 = grid4[4 * row + 2],
               s = grid4[4 * row + 3];
     const SheetDev& sh = G.sh[s];
+    // pos: the unshifted positions, which choose the pairs (the reference's pair
+    // lists come from the unshifted geometry); spos: the job's shifted i2pos,
+    // which give the values (setConfigPositions, locality.cpp:3618-3642)
     const double x1 = pos[3 * row] + 0.0, y1 = pos[3 * row + 1] + 0.0, z1 = pos[3 * row + 2];
+    const double sx1 = spos[3 * row] + 0.0, sy1 = spos[3 * row + 1] + 0.0, sz1 = spos[3 * row + 2];
     int64_t o = kPad ? row * (int64_t)out.pad_cap : (kFill ? out.rowptr[row] : 0);
     const int64_t o_end = kPad ? o + out.pad_cap : 0;
     int64_t n_ent = 0, n_intra = 0, n_inter = 0;
@@ -369,11 +383,11 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
         if (kFill && store && (!kPad || o + __popc(m & lt_mask) < o_end)) {
           const int64_t e = o + __popc(m & lt_mask);
           out.col[e] = (int32_t)k2g;
-          const double x2 = pos[3 * k2g], y2 = pos[3 * k2g + 1];
-          store_value(G, out, e, t, x1, y1, x2, y2);
+          const double x2 = spos[3 * k2g], y2 = spos[3 * k2g + 1];
+          store_value(G, out, e, t, sx1, sy1, x2, y2);
           if (G.with_dx) {
-            out.dx[e] = t != 0 ? 0.0 + (x1 - x2) * t : 0.0;
-            out.dy[e] = t != 0 ? 0.0 + (y1 - y2) * t : 0.0;
+            out.dx[e] = t != 0 ? 0.0 + (sx1 - x2) * t : 0.0;
+            out.dy[e] = t != 0 ? 0.0 + (sy1 - y2) * t : 0.0;
           }
         }
         o += __popc(m);
@@ -385,6 +399,7 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
     {
       const double ph[3] = {x1, y1, z1};
       const float x1f = (float)x1, y1f = (float)y1, z1f = (float)z1;
+      const float sx1f = (float)sx1, sy1f = (float)sy1, sz1f = (float)sz1;
       constexpr float kWinLo = (float)(kInterCutoff - kPrefilterMargin), kWinHi = (float)(kInterCutoff + kPrefilterMargin);
       // every hopping is zero from 8 A on (in-plane for the reference model, 3-D for the simple one)
       constexpr float kHopHi = 8.0f + kPrefilterMargin, kHopLo = 8.0f - kPrefilterMargin;
@@ -410,7 +425,7 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
             if (k2 != -1) {
               const int64_t kk = k2 + o0.base;
               const float4 q = pos32[kk];
-              const float dxf = q.x - x1f, dyf = q.y - y1f, dzf = q.z - z1f;
+              const float dxf = q.x - x1f, dyf = q.y - y1f;
               const float d2f = dxf * dxf + dyf * dyf;
               bool in_window;
               if (d2f < kWinLo * kWinLo) {
@@ -423,20 +438,24 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
               }
               if (in_window) {
                 k2g = kk;
-                const float h2f = G.model == LEO2D_MODEL_SIMPLE ? d2f + dzf * dzf : d2f;
+                // the hopping cutoffs test the shifted positions
+                const float4 sq = G.shifted ? spos32[kk] : q;
+                const float hdx = sq.x - sx1f, hdy = sq.y - sy1f, hdz = sq.z - sz1f;
+                const float hd2 = hdx * hdx + hdy * hdy;
+                const float h2f = G.model == LEO2D_MODEL_SIMPLE ? hd2 + hdz * hdz : hd2;
                 if (!kFill && !G.keep_zeros && G.model == LEO2D_MODEL_SIMPLE && h2f < kHopHi * kHopHi) {
                   // counting only needs t != 0: the simple model's hopping (and its
                   // quotient by a finite rescale) is non-zero exactly when the FP64
                   // distance of `interlayer` is below 8 A; FP32 decides away from 8 A
                   bool nz = h2f < kHopLo * kHopLo;
                   if (!nz) {
-                    const double v0 = pos[3 * kk] - x1, v1 = pos[3 * kk + 1] - y1, v2 = pos[3 * kk + 2] - z1;
+                    const double v0 = spos[3 * kk] - sx1, v1 = spos[3 * kk + 1] - sy1, v2 = spos[3 * kk + 2] - sz1;
                     nz = sqrt(v0 * v0 + v1 * v1 + v2 * v2) < 8.0;
                   }
                   t = nz ? 1.0 : 0.0;
                 } else if ((kFill || !G.keep_zeros) && h2f < kHopHi * kHopHi) {
-                  const double x2 = pos[3 * kk], y2 = pos[3 * kk + 1], z2 = pos[3 * kk + 2];
-                  t = interlayer_t(G.model, l0, l, x2 - x1, y2 - y1, z2 - z1, sh.angle, o0.angle, G.rescale,
+                  const double x2 = spos[3 * kk], y2 = spos[3 * kk + 1], z2 = spos[3 * kk + 2];
+                  t = interlayer_t(G.model, l0, l, x2 - sx1, y2 - sy1, z2 - sz1, sh.angle, o0.angle, G.rescale,
                                    G.simple_amp);
                 }
               }
@@ -449,11 +468,11 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
           if (kFill && store && (!kPad || o + __popc(m & lt_mask) < o_end)) {
             const int64_t e = o + __popc(m & lt_mask);
             out.col[e] = (int32_t)k2g;
-            const double x2 = pos[3 * k2g], y2 = pos[3 * k2g + 1];
-            store_value(G, out, e, t, x1, y1, x2, y2);
+            const double x2 = spos[3 * k2g], y2 = spos[3 * k2g + 1];
+            store_value(G, out, e, t, sx1, sy1, x2, y2);
             if (G.with_dx) {
-              out.dx[e] = t != 0 ? 0.0 + (x1 - x2) * t : 0.0;
-              out.dy[e] = t != 0 ? 0.0 + (y1 - y2) * t : 0.0;
+              out.dx[e] = t != 0 ? 0.0 + (sx1 - x2) * t : 0.0;
+              out.dy[e] = t != 0 ? 0.0 + (sy1 - y2) * t : 0.0;
             }
           }
           o += __popc(m);
@@ -552,7 +571,8 @@ __device__ void block_bitonic_sort(uint64_t* keys, int n2) {
 template <bool kFill>
 __global__ void __launch_bounds__(256) k_periodic_rows(const __grid_constant__ GeomDev G, int64_t n,
                                                        const int32_t* __restrict__ grid4,
-                                                       const double* __restrict__ pos, int cap,
+                                                       const double* __restrict__ pos,
+                                                       const double* __restrict__ spos, int cap,
                                                        RowOut out, int* status) {
   extern __shared__ uint64_t keys[];
   __shared__ int cnt, n_intra_s, n_inter_s, n_run;
@@ -631,7 +651,7 @@ __global__ void __launch_bounds__(256) k_periodic_rows(const __grid_constant__ G
           atomicAdd(&n_inter_s, 1);
           if (!G.keep_zeros) {
             double xx, yy;
-            const double t = periodic_value(G, row, grid4, pos, true, kk, img, xx, yy);
+            const double t = periodic_value(G, row, grid4, spos, true, kk, img, xx, yy);
             if (t == 0) continue;
           }
           const int slot = atomicAdd(&cnt, 1);
@@ -693,11 +713,11 @@ __global__ void __launch_bounds__(256) k_periodic_rows(const __grid_constant__ G
         for (int e = q; e <= p; ++e) {
           const int img = (int)(keys[e] & 0xffffull);
           double x1, y1;
-          const double t = periodic_value(G, row, grid4, pos, inter, k2, img, x1, y1);
+          const double t = periodic_value(G, row, grid4, spos, inter, k2, img, x1, y1);
           if (t != 0) {
             if (G.cpx) {
               // std::polar(t, k.(r2 - r1)) summed over the images (locality.cpp:4896-4941)
-              const double ph = G.kx * (pos[3 * k2] - x1) + G.ky * (pos[3 * k2 + 1] - y1);
+              const double ph = G.kx * (spos[3 * k2] - x1) + G.ky * (spos[3 * k2 + 1] - y1);
               double sn, cs;
               sincos(ph, &sn, &cs);
               v += t * cs;
@@ -705,8 +725,8 @@ __global__ void __launch_bounds__(256) k_periodic_rows(const __grid_constant__ G
             } else {
               v += t;
             }
-            vdx += (x1 - pos[3 * k2]) * t;
-            vdy += (y1 - pos[3 * k2 + 1]) * t;
+            vdx += (x1 - spos[3 * k2]) * t;
+            vdy += (y1 - spos[3 * k2 + 1]) * t;
           }
         }
         const int64_t e = base_out + before;
@@ -791,6 +811,8 @@ void fill_sheet(const leo2d_geom& g, int s, SheetDev& d) {
   d.W = d.max1 - d.min1;
   d.n_orb = 2;
   d.max_R = g.max_R[s];
+  d.shift[0] = g.shifts[s][0];
+  d.shift[1] = g.shifts[s][1];
   const double a = g.model == LEO2D_MODEL_SIMPLE ? 2.46 : 2.4768;
   for (int x = 0; x < 2; ++x)
     for (int y = 0; y < 2; ++y) d.a[x][y] = g.lattice[s][x][y];
@@ -856,6 +878,10 @@ void validate_geom(const leo2d_geom* g) {
     LEO_REQUIRE(g->sc_search_size >= 0 && g->sc_search_size <= 3, "sc_search_size must be 0..3");
   LEO_REQUIRE(std::isfinite(g->b_field), "b_field must be finite");
   LEO_REQUIRE(std::isfinite(g->k_vec[0]) && std::isfinite(g->k_vec[1]), "k_vec must be finite");
+  for (int s = 0; s < LEO2D_MAX_SHEETS; ++s)
+    LEO_REQUIRE(std::isfinite(g->shifts[s][0]) && std::isfinite(g->shifts[s][1]) &&
+                    std::fabs(g->shifts[s][0]) <= 1.0 && std::fabs(g->shifts[s][1]) <= 1.0,
+                "sheet shifts must be finite fractions of the lattice vectors (|shift| <= 1)");
   LEO_REQUIRE(g->b_field == 0.0 || g->boundary_condition == 0,
               "a magnetic field is supported for flakes (BOUNDARY_CONDITION = 0)");
 }
@@ -947,6 +973,8 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     G.kx = g->k_vec[0];
     G.ky = g->k_vec[1];
     G.cpx = (g->b_field != 0.0 || g->k_vec[0] != 0.0 || g->k_vec[1] != 0.0) ? 1 : 0;
+    for (int s = 0; s < g->num_sheets; ++s)
+      if (g->shifts[s][0] != 0.0 || g->shifts[s][1] != 0.0) G.shifted = 1;
     LEO_REQUIRE(!G.cpx || !G.with_dx,
                 "the velocity operator (WITH_DX, conductivity) is not built for a complex Hamiltonian");
     std::memcpy(G.supercell, g->supercell, sizeof(G.supercell));
@@ -984,6 +1012,10 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     csr->n = n;
     csr->grid4.alloc(4 * (size_t)std::max<int64_t>(n, 1));
     csr->pos.alloc(3 * (size_t)std::max<int64_t>(n, 1));
+    // a shifted job: the pairs from the unshifted positions (csr->pos during
+    // assembly), the values from the shifted ones, which the matrix keeps
+    DevBuf<double> spos_buf(G.shifted ? 3 * (size_t)std::max<int64_t>(n, 1) : 0);
+    const double* spos = G.shifted ? spos_buf.p : csr->pos.p;
     DevBuf<const int32_t*> cell_ptrs(G.S);
     std::vector<const int32_t*> hp(G.S);
     for (int s = 0; s < G.S; ++s) hp[s] = site_cells[s].p;
@@ -991,7 +1023,7 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     if (n > 0)
       launch(ctx, "sites", [&] {
         k_sites<<<grid_for(n, 256, (int64_t)ctx->sm_count * 32), 256, 0, ctx->stream>>>(
-            G, n, cell_ptrs.p, csr->grid4.p, csr->pos.p);
+            G, n, cell_ptrs.p, csr->grid4.p, csr->pos.p, G.shifted ? spos_buf.p : nullptr);
       });
 
     // count -> scan -> fill
@@ -1015,10 +1047,18 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     }
     const unsigned rows_grid = grid_for(n, 8, (int64_t)ctx->sm_count * 64);
     DevBuf<float4> pos32(G.bc == 0 ? std::max<int64_t>(n, 1) : 1);
+    DevBuf<float4> spos32(G.bc == 0 && G.shifted ? std::max<int64_t>(n, 1) : 0);
     if (G.bc == 0 && n > 0)
       launch(ctx, "pos32", [&] {
         k_pos32<<<grid_for(n, 256, (int64_t)ctx->sm_count * 32), 256, 0, ctx->stream>>>(csr->pos.p, n, pos32.p);
+        if (G.shifted)
+          k_pos32<<<grid_for(n, 256, (int64_t)ctx->sm_count * 32), 256, 0, ctx->stream>>>(spos, n, spos32.p);
       });
+    const float4* spos32p = G.shifted ? spos32.p : pos32.p;
+    // the matrix keeps the job's (shifted) positions
+    auto keep_shifted_positions = [&] {
+      if (G.shifted) csr->pos = std::move(spos_buf);
+    };
     const unsigned cta_grid = grid_for(n, 1, (int64_t)ctx->sm_count * 8);
     // A flake of the simple model without stored zeros (about 67 entries per
     // row) takes one pass: rows are filled into padded arrays of kPadCap
@@ -1045,7 +1085,8 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
         rp.pad_cap = kPadCap;
         rp.overflow = overflow.p;
         launch(ctx, "flake_rows_fill", [&] {
-          k_flake_rows<2><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, rp);
+          k_flake_rows<2><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, spos,
+                                                              spos32p, rp);
         });
         int over = 0;
         d2h(ctx, &over, overflow.p, 1);
@@ -1075,6 +1116,7 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
                 n, kPadCap, csr->rowptr.p, pcol.p, pval.p, pdx.p, pdy.p, pim.p, fo);
           });
           ctx_check_status(ctx, "leo2d_build_csr (single pass)");
+          keep_shifted_positions();
           csr_refresh_fp32(ctx, csr);
           ctx_sync(ctx);
           return;  // (the guard's lambda)
@@ -1084,11 +1126,12 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     if (n > 0) {
       if (G.bc == 0)
         launch(ctx, "flake_rows_count", [&] {
-          k_flake_rows<0><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, ro);
+          k_flake_rows<0><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, spos,
+                                                              spos32p, ro);
         });
       else
         launch(ctx, "periodic_rows_count", [&] {
-          k_periodic_rows<false><<<cta_grid, 256, smem, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p,
+          k_periodic_rows<false><<<cta_grid, 256, smem, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, spos,
                                                                        cap, ro, ctx->status.p);
         });
     }
@@ -1114,15 +1157,17 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     if (n > 0) {
       if (G.bc == 0)
         launch(ctx, "flake_rows_fill", [&] {
-          k_flake_rows<1><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, ro);
+          k_flake_rows<1><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, spos,
+                                                              spos32p, ro);
         });
       else
         launch(ctx, "periodic_rows_fill", [&] {
-          k_periodic_rows<true><<<cta_grid, 256, smem, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p,
+          k_periodic_rows<true><<<cta_grid, 256, smem, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, spos,
                                                                       cap, ro, ctx->status.p);
         });
     }
     ctx_check_status(ctx, "leo2d_build_csr (fill)");
+    keep_shifted_positions();
     csr_refresh_fp32(ctx, csr);
     ctx_sync(ctx);
   });

@@ -152,6 +152,13 @@ bool parse_input(const std::string& path, JobSpec& spec, std::string& err) {
         spec.kpm_trace = std::atoi(value().c_str());
       } else if (key == "KPM_TRACE_SAMPS") {
         spec.kpm_trace_samps = std::atoi(value().c_str());
+      } else if (key == "NUM_SHIFT_SHEETS") {
+        spec.num_shift_sheets = std::atoi(value().c_str());
+      } else if (key == "SHIFT_SHEETS") {  // main.cpp:874-884
+        next();
+        spec.shift_sheets.assign(spec.num_shift_sheets > 0 ? spec.num_shift_sheets : 0, 0);
+        for (size_t i = 0; i < spec.shift_sheets.size(); ++i)
+          spec.shift_sheets[i] = std::atoi(next().c_str()) - 1;
       } else if (key == "NUM_TARGET_SHEETS") {
         spec.num_target_sheets = std::atoi(value().c_str());
       } else if (key == "TARGET_SHEETS") {

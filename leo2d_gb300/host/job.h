@@ -28,7 +28,9 @@ struct JobSpec {
   int matrix_save = 0;
   int matrix_pos_save = 0;
   int verbose_save = 1;
-  int nshifts = 1;
+  int nshifts = 1;            // NSHIFTS: an N x N grid of shifts per shift sheet
+  int num_shift_sheets = 1;   // NUM_SHIFT_SHEETS (job_params.cpp:44)
+  std::vector<int> shift_sheets;  // SHIFT_SHEETS, 0-based
   int num_target_sheets = 1;
   std::vector<int> target_sheets;  // 0-based
   // additive keys

@@ -100,9 +100,18 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     err = "SOLVER_TYPE must be SQ (only the uniform-sampling job list is built)";
     return LEO2D_ERR_UNSUPPORTED;
   }
-  if (spec.nshifts != 1) {
-    err = "NSHIFTS > 1 (shifted sheet configurations) is not built";
-    return LEO2D_ERR_UNSUPPORTED;
+  if (spec.nshifts < 1) {
+    err = "NSHIFTS must be >= 1";
+    return LEO2D_ERR_BAD_ARG;
+  }
+  for (int s : spec.shift_sheets)
+    if (s < 0 || s >= spec.geom.num_sheets) {
+      err = "SHIFT_SHEETS names a sheet that does not exist";
+      return LEO2D_ERR_BAD_ARG;
+    }
+  if (spec.nshifts > 1 && (int)spec.shift_sheets.size() < spec.num_shift_sheets) {
+    err = "NSHIFTS > 1 needs SHIFT_SHEETS for its NUM_SHIFT_SHEETS sheets";
+    return LEO2D_ERR_BAD_ARG;
   }
   Ctx ctx;
   {
@@ -112,183 +121,231 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
       return st;
     }
   }
-  leo2d_geom g = spec.geom;
-  CHECK(leo2d_geom_prepare(&g));
-  const bool gersh = spec.bounds == 1;
-  double rescale = g.energy_rescale, shift = g.energy_shift, center = -shift;
-  if (gersh) {
-    g.energy_rescale = 1.0;
-    g.energy_shift = 0.0;
+  leo2d_geom g0 = spec.geom;
+  CHECK(leo2d_geom_prepare(&g0));
+  // the job list of the SQ solver (recursiveShiftCalc, locality.cpp:1222-1269):
+  // for the last shift sheet every (i/N, j/N), i outer, j inner, and for each
+  // of those the list of the remaining shift sheets
+  std::vector<std::vector<double>> jobs;  // [job][2 * sheet]
+  {
+    std::vector<double> sh(2 * LEO2D_MAX_SHEETS, 0.0);
+    const int levels = spec.nshifts > 1 ? spec.num_shift_sheets : 0;
+    const int N = spec.nshifts;
+    auto rec = [&](auto&& self, int k) -> void {
+      if (k == 0) {
+        jobs.push_back(sh);
+        return;
+      }
+      const int tar = spec.shift_sheets[k - 1];
+      for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j) {
+          sh[2 * tar] = (1.0 / (double)(N)) * i;
+          sh[2 * tar + 1] = (1.0 / (double)(N)) * j;
+          self(self, k - 1);
+        }
+    };
+    rec(rec, levels);
   }
+  const bool gersh = spec.bounds == 1;
   uint32_t flags = 0;
   if (spec.observable_type == 1 || spec.matrix_save > 1) flags |= LEO2D_CSR_WITH_DX;
   // generateCpxH's matrix save lists every stored pair, zeros included (locality.cpp:5213-5228)
   if (spec.use_b == 1 && spec.matrix_save > 0) flags |= LEO2D_CSR_KEEP_ZEROS;
-  Csr csr;
-  CHECK(leo2d_build_csr(ctx.h, &g, flags, &csr.h));
-  int64_t n = 0, nnz = 0, ni = 0, ne = 0;
-  CHECK(leo2d_csr_info(csr.h, &n, &nnz, &ni, &ne));
-  std::printf("Heterostructure has %lld orbitals. \n%lld entries expected from intra. \n"
-              "%lld entries expected from inter. \n",
-              (long long)n, (long long)ni, (long long)ne);
-  if (gersh) {
-    double lo = 0, hi = 0;
-    CHECK(leo2d_csr_bounds(ctx.h, csr.h, &lo, &hi));
-    rescale = 1.01 * (hi - lo) / 2;
-    center = (hi + lo) / 2;
-    shift = -center;
-    CHECK(leo2d_csr_rescale(ctx.h, csr.h, rescale, shift));
-  }
-  std::vector<int32_t> grid4(4 * n);
-  std::vector<double> pos(3 * n);
-  CHECK(leo2d_csr_geometry(ctx.h, csr.h, grid4.data(), pos.data()));
-  std::vector<int64_t> targets;
-  if (!target_list(spec, grid4, targets, err)) return LEO2D_ERR_BAD_ARG;
-
-  // Chebyshev nodes of Param_tools::save (param_tools.cpp:57-62); with
-  // Gershgorin bounds the axis is centre + rescale x.
-  std::vector<double> E(P);
-  for (int i = 0; i < P; ++i) {
-    const double x = std::cos((i * 1.0 + 0.5) * M_PI / P);
-    E[i] = gersh ? center + rescale * x : shift + rescale * x;
-  }
-
   std::ofstream cheb(join_path(out_dir, spec.job_name + ".cheb"));
   if (!cheb.is_open()) {
     err = "cannot write " + spec.job_name + ".cheb";
     return LEO2D_ERR_IO;
   }
   cheb << std::fixed;
-  if (spec.verbose_save != 0) {  // Param_tools::saveHeader (param_tools.cpp:467-505)
-    cheb << "JOBID = " << 1 << " \n";
-    cheb << "SHEET: SHIFT_X, SHIFT_Y, SHIFT_Z \n";
-    for (int s = 0; s < g.num_sheets; ++s)
-      cheb << s + 1 << "    : " << 0.0 << ", " << 0.0 << ", " << 0.0 << " \n";
-    cheb << "NUM_TAR = " << targets.size() << "\n";
-    if (!targets.empty()) {
-      cheb << "TAR_LIST: ";
-      for (size_t t = 0; t + 1 < targets.size(); ++t) cheb << targets[t] << ", ";
-      cheb << targets.back() << " \n";
-    } else {
-      cheb << "NO_TAR \n";
+  // one generator draws every job's trace vectors in job order (locality.cpp:2274-2305)
+  std::default_random_engine generator;
+  std::normal_distribution<double> distribution(0.0, 1.0);
+  Csr csr;
+  int64_t n = 0, nnz = 0;
+  std::vector<int32_t> grid4;
+  std::vector<double> pos;
+  std::vector<int64_t> targets;
+  for (size_t job = 0; job < jobs.size(); ++job) {
+    const bool first_job = job == 0;
+    leo2d_geom g = g0;
+    for (int s = 0; s < g.num_sheets; ++s) {
+      g.shifts[s][0] = jobs[job][2 * s];
+      g.shifts[s][1] = jobs[job][2 * s + 1];
     }
-    if (spec.use_b == 1) {  // the field lines of the header (param_tools.cpp:572-575)
-      cheb << "MAG_ON  = " << spec.use_b << ", B = " << spec.b_field << " \n";
-      cheb << "ELEC_ON = " << 0 << ", E = " << 0.0 << " \n";
+    double rescale = g.energy_rescale, shift = g.energy_shift, center = -shift;
+    if (gersh) {
+      g.energy_rescale = 1.0;
+      g.energy_shift = 0.0;
     }
-  }
+    if (csr.h) {
+      leo2d_csr_destroy(csr.h);
+      csr.h = nullptr;
+    }
+    CHECK(leo2d_build_csr(ctx.h, &g, flags, &csr.h));
+    int64_t ni = 0, ne = 0;
+    CHECK(leo2d_csr_info(csr.h, &n, &nnz, &ni, &ne));
+    if (first_job)  // constructGeom reports the geometry once
+      std::printf("Heterostructure has %lld orbitals. \n%lld entries expected from intra. \n"
+                  "%lld entries expected from inter. \n",
+                  (long long)n, (long long)ni, (long long)ne);
+    if (gersh) {
+      double lo = 0, hi = 0;
+      CHECK(leo2d_csr_bounds(ctx.h, csr.h, &lo, &hi));
+      rescale = 1.01 * (hi - lo) / 2;
+      center = (hi + lo) / 2;
+      shift = -center;
+      CHECK(leo2d_csr_rescale(ctx.h, csr.h, rescale, shift));
+    }
+    grid4.assign(4 * n, 0);
+    pos.assign(3 * n, 0.0);
+    CHECK(leo2d_csr_geometry(ctx.h, csr.h, grid4.data(), pos.data()));
+    if (first_job && !target_list(spec, grid4, targets, err)) return LEO2D_ERR_BAD_ARG;
 
-  leo2d_kpm_cfg cfg{};
-  cfg.poly_order = P;
-  // (the complex Hamiltonian of a magnetic field runs the FP32 recursion only)
-  cfg.precision = spec.precision >= 0 ? spec.precision
-                                      : ((spec.observable_type == 1 || spec.use_b == 1) ? LEO2D_FP32 : LEO2D_FP64);
-  cfg.block = spec.block;
-  cfg.seed = spec.seed;
+    // Chebyshev nodes of Param_tools::save (param_tools.cpp:57-62); with
+    // Gershgorin bounds the axis is centre + rescale x.
+    std::vector<double> E(P);
+    for (int i = 0; i < P; ++i) {
+      const double x = std::cos((i * 1.0 + 0.5) * M_PI / P);
+      E[i] = gersh ? center + rescale * x : shift + rescale * x;
+    }
 
-  if (spec.observable_type == 0 && spec.kpm_trace == 1) {
-    // rootChebSolve's trace samples (locality.cpp:2254-2309)
-    int S = spec.kpm_trace_samps;
-    if (S == -1) {
-      S = (int)1.0e6 / ((double)n);
-      if (S < 1) S = 1;
-      if (S > 100) S = 100;
-    }
-    cfg.num_vectors = S;
-    std::vector<double> mu((size_t)S * P);
-    if (spec.vectors == 0) {
-      std::vector<double> vec((size_t)S * n);
-      std::default_random_engine generator;
-      std::normal_distribution<double> distribution(0.0, 1.0);
-      for (int s = 0; s < S; ++s)
-        for (int64_t i = 0; i < n; ++i) vec[(size_t)s * n + i] = distribution(generator);
-      cfg.vector_kind = LEO2D_VEC_HOST;
-      CHECK(leo2d_kpm_dos(ctx.h, csr.h, &cfg, vec.data(), mu.data()));
-    } else {
-      cfg.vector_kind = LEO2D_VEC_PHASE;
-      CHECK(leo2d_kpm_dos(ctx.h, csr.h, &cfg, nullptr, mu.data()));
-    }
-    std::vector<double> dos(P), Ek(P);
-    // densityTransformTrace(results, 1/num_dofs) (locality.cpp:3126-3131)
-    CHECK(leo2d_dos_transform(ctx.h, mu.data(), P, S, rescale, shift, 1.0 / (double)n, dos.data(), Ek.data()));
-    if (spec.verbose_save == 1) {
-      cheb << "E: ";
-      write_energies(cheb, E);
-      cheb << "T: \n";
-      // save() prints cheb_coeffs rows for the job's target list (param_tools.cpp:65-71)
-      for (size_t t = 0; t < targets.size() && t < (size_t)S; ++t) {
-        cheb << targets[t] << ": ";
-        for (int j = 0; j < P - 1; ++j) cheb << mu[t * P + j] << ", ";
-        cheb << mu[t * P + P - 1] << "\n";
+    if (spec.verbose_save != 0) {  // Param_tools::saveHeader (param_tools.cpp:467-505)
+      cheb << "JOBID = " << job + 1 << " \n";
+      cheb << "SHEET: SHIFT_X, SHIFT_Y, SHIFT_Z \n";
+      for (int s = 0; s < g.num_sheets; ++s)
+        cheb << s + 1 << "    : " << g.shifts[s][0] << ", " << g.shifts[s][1] << ", " << 0.0 << " \n";
+      cheb << "NUM_TAR = " << targets.size() << "\n";
+      if (!targets.empty()) {
+        cheb << "TAR_LIST: ";
+        for (size_t t = 0; t + 1 < targets.size(); ++t) cheb << targets[t] << ", ";
+        cheb << targets.back() << " \n";
+      } else {
+        cheb << "NO_TAR \n";
       }
-      cheb << "\n";
-    } else {
-      write_energies(cheb, E);
-      for (int j = 0; j < P - 1; ++j) cheb << dos[j] << " ";
-      cheb << dos[P - 1] << "\n";
-    }
-    if (spec.energies > 0) {
-      std::vector<double> mean(P, 0.0), Eg(spec.energies), d(spec.energies);
-      for (int s = 0; s < S; ++s)
-        for (int j = 0; j < P; ++j) mean[j] += mu[(size_t)s * P + j] / S;
-      for (int k = 0; k < spec.energies; ++k)
-        Eg[k] = center + rescale * (-1.0 + 2.0 * (k + 0.5) / spec.energies);
-      CHECK(leo2d_dos_reconstruct(ctx.h, mean.data(), P, Eg.data(), spec.energies, rescale, center,
-                                  1.0 / (double)n, d.data()));
-      std::ofstream f(join_path(out_dir, spec.job_name + "_dos.dat"));
-      f << std::setprecision(17);
-      for (int k = 0; k < spec.energies; ++k) f << Eg[k] << " " << d[k] << "\n";
-    }
-  } else if (spec.observable_type == 0) {
-    const int64_t T = (int64_t)targets.size();
-    std::vector<double> mu((size_t)T * P);
-    CHECK(leo2d_kpm_ldos(ctx.h, csr.h, &cfg, targets.data(), T, mu.data()));
-    std::vector<double> out = mu;
-    if (spec.dos_transform == 1) {  // Param_tools::densityTransform
-      std::vector<double> Ek(P);
-      for (int64_t t = 0; t < T; ++t)
-        CHECK(leo2d_dos_transform(ctx.h, mu.data() + t * P, P, 1, rescale, shift, 1.0, out.data() + t * P,
-                                  Ek.data()));
-    }
-    if (spec.verbose_save == 1) {
-      cheb << "E: ";
-      write_energies(cheb, E);
-      cheb << "T: \n";
-      for (int64_t t = 0; t < T; ++t) {
-        cheb << targets[t] << ": ";
-        for (int j = 0; j < P - 1; ++j) cheb << out[t * P + j] << ", ";
-        cheb << out[t * P + P - 1] << "\n";
-      }
-      cheb << "\n";
-    } else {
-      write_energies(cheb, E);
-      for (int64_t t = 0; t < T; ++t) {
-        for (int j = 0; j < P - 1; ++j) cheb << out[t * P + j] << " ";
-        cheb << out[t * P + P - 1] << "\n";
+      if (spec.use_b == 1) {  // the field lines of the header (param_tools.cpp:572-575)
+        cheb << "MAG_ON  = " << spec.use_b << ", B = " << spec.b_field << " \n";
+        cheb << "ELEC_ON = " << 0 << ", E = " << 0.0 << " \n";
       }
     }
-  } else {
-    const int64_t T = (int64_t)targets.size();
-    std::vector<double> M((size_t)T * P * P);
-    CHECK(leo2d_kpm_cond(ctx.h, csr.h, &cfg, targets.data(), T, M.data()));
-    std::vector<double> out = M;
-    if (spec.cond_transform == 1)
-      for (int64_t t = 0; t < T; ++t)
-        CHECK(leo2d_cond_transform(ctx.h, M.data() + t * P * P, P, out.data() + t * P * P));
-    if (spec.verbose_save == 0) {  // param_tools.cpp:288-316
-      write_energies(cheb, E);
-      cheb << "\n";
-      for (int64_t t = 0; t < T; ++t) {
-        for (int i = 0; i < P; ++i) {
-          for (int j = 0; j < P; ++j) cheb << out[(size_t)t * P * P + (size_t)i * P + j] << " ";
-          cheb << "\n";
+
+    leo2d_kpm_cfg cfg{};
+    cfg.poly_order = P;
+    // (the complex Hamiltonian of a magnetic field runs the FP32 recursion only)
+    cfg.precision = spec.precision >= 0 ? spec.precision
+                                        : ((spec.observable_type == 1 || spec.use_b == 1) ? LEO2D_FP32 : LEO2D_FP64);
+    cfg.block = spec.block;
+    cfg.seed = spec.seed;
+
+    if (spec.observable_type == 0 && spec.kpm_trace == 1) {
+      // rootChebSolve's trace samples (locality.cpp:2254-2309)
+      int S = spec.kpm_trace_samps;
+      if (S == -1) {
+        S = (int)1.0e6 / ((double)n);
+        if (S < 1) S = 1;
+        if (S > 100) S = 100;
+      }
+      cfg.num_vectors = S;
+      std::vector<double> mu((size_t)S * P);
+      if (spec.vectors == 0) {
+        std::vector<double> vec((size_t)S * n);
+        for (int s = 0; s < S; ++s)
+          for (int64_t i = 0; i < n; ++i) vec[(size_t)s * n + i] = distribution(generator);
+        cfg.vector_kind = LEO2D_VEC_HOST;
+        CHECK(leo2d_kpm_dos(ctx.h, csr.h, &cfg, vec.data(), mu.data()));
+      } else {
+        cfg.vector_kind = LEO2D_VEC_PHASE;
+        CHECK(leo2d_kpm_dos(ctx.h, csr.h, &cfg, nullptr, mu.data()));
+      }
+      std::vector<double> dos(P), Ek(P);
+      // densityTransformTrace(results, 1/num_dofs) (locality.cpp:3126-3131)
+      CHECK(leo2d_dos_transform(ctx.h, mu.data(), P, S, rescale, shift, 1.0 / (double)n, dos.data(), Ek.data()));
+      if (spec.verbose_save == 1) {
+        if (first_job) {
+          cheb << "E: ";
+          write_energies(cheb, E);
+        }
+        cheb << "T: \n";
+        // save() prints cheb_coeffs rows for the job's target list (param_tools.cpp:65-71)
+        for (size_t t = 0; t < targets.size() && t < (size_t)S; ++t) {
+          cheb << targets[t] << ": ";
+          for (int j = 0; j < P - 1; ++j) cheb << mu[t * P + j] << ", ";
+          cheb << mu[t * P + P - 1] << "\n";
         }
         cheb << "\n";
+      } else {
+        if (first_job) write_energies(cheb, E);
+        for (int j = 0; j < P - 1; ++j) cheb << dos[j] << " ";
+        cheb << dos[P - 1] << "\n";
+      }
+      if (spec.energies > 0) {
+        std::vector<double> mean(P, 0.0), Eg(spec.energies), d(spec.energies);
+        for (int s = 0; s < S; ++s)
+          for (int j = 0; j < P; ++j) mean[j] += mu[(size_t)s * P + j] / S;
+        for (int k = 0; k < spec.energies; ++k)
+          Eg[k] = center + rescale * (-1.0 + 2.0 * (k + 0.5) / spec.energies);
+        CHECK(leo2d_dos_reconstruct(ctx.h, mean.data(), P, Eg.data(), spec.energies, rescale, center,
+                                    1.0 / (double)n, d.data()));
+        std::ofstream f(join_path(out_dir, spec.job_name + "_dos.dat"));
+        f << std::setprecision(17);
+        for (int k = 0; k < spec.energies; ++k) f << Eg[k] << " " << d[k] << "\n";
+      }
+    } else if (spec.observable_type == 0) {
+      const int64_t T = (int64_t)targets.size();
+      std::vector<double> mu((size_t)T * P);
+      CHECK(leo2d_kpm_ldos(ctx.h, csr.h, &cfg, targets.data(), T, mu.data()));
+      std::vector<double> out = mu;
+      if (spec.dos_transform == 1) {  // Param_tools::densityTransform
+        std::vector<double> Ek(P);
+        for (int64_t t = 0; t < T; ++t)
+          CHECK(leo2d_dos_transform(ctx.h, mu.data() + t * P, P, 1, rescale, shift, 1.0, out.data() + t * P,
+                                    Ek.data()));
+      }
+      if (spec.verbose_save == 1) {
+        if (first_job) {
+          cheb << "E: ";
+          write_energies(cheb, E);
+        }
+        cheb << "T: \n";
+        for (int64_t t = 0; t < T; ++t) {
+          cheb << targets[t] << ": ";
+          for (int j = 0; j < P - 1; ++j) cheb << out[t * P + j] << ", ";
+          cheb << out[t * P + P - 1] << "\n";
+        }
+        cheb << "\n";
+      } else {
+        if (first_job) write_energies(cheb, E);
+        for (int64_t t = 0; t < T; ++t) {
+          for (int j = 0; j < P - 1; ++j) cheb << out[t * P + j] << " ";
+          cheb << out[t * P + P - 1] << "\n";
+        }
+      }
+    } else {
+      const int64_t T = (int64_t)targets.size();
+      std::vector<double> M((size_t)T * P * P);
+      CHECK(leo2d_kpm_cond(ctx.h, csr.h, &cfg, targets.data(), T, M.data()));
+      std::vector<double> out = M;
+      if (spec.cond_transform == 1)
+        for (int64_t t = 0; t < T; ++t)
+          CHECK(leo2d_cond_transform(ctx.h, M.data() + t * P * P, P, out.data() + t * P * P));
+      if (spec.verbose_save == 0) {  // param_tools.cpp:288-316
+        if (first_job) {
+          write_energies(cheb, E);
+          cheb << "\n";
+        }
+        for (int64_t t = 0; t < T; ++t) {
+          for (int i = 0; i < P; ++i) {
+            for (int j = 0; j < P; ++j) cheb << out[(size_t)t * P * P + (size_t)i * P + j] << " ";
+            cheb << "\n";
+          }
+          cheb << "\n";
+        }
       }
     }
-  }
+  }  // jobs
   cheb.close();
 
+  // (the matrix and position files of the last job: the reference's jobs
+  // overwrite each other's, locality.cpp:4362-4365)
   if (spec.matrix_save > 0) {  // generateRealH's matrix save (locality.cpp:4366-4383)
     std::vector<int64_t> rp(n + 1);
     std::vector<int32_t> col(nnz);

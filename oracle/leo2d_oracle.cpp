@@ -450,9 +450,10 @@ int oracle_build(const leo2d_geom* gin, oracle_h** out) {
       s1a[d][0] = std::cos(theta) * sh.a[d][0] - std::sin(theta) * sh.a[d][1];
       s1a[d][1] = std::sin(theta) * sh.a[d][0] + std::cos(theta) * sh.a[d][1];
     }
-    double z0 = 0;
-    h->i2pos[3 * i + 0] = h->index_to_pos[3 * i + 0] + z0 * s1a[0][0] + z0 * s1a[1][0];
-    h->i2pos[3 * i + 1] = h->index_to_pos[3 * i + 1] + z0 * s1a[0][1] + z0 * s1a[1][1];
+    // the job's sheet shifts (Job_params "shifts"; zero unless set)
+    const double sh0 = g.shifts[s][0], sh1 = g.shifts[s][1];
+    h->i2pos[3 * i + 0] = h->index_to_pos[3 * i + 0] + sh0 * s1a[0][0] + sh1 * s1a[1][0];
+    h->i2pos[3 * i + 1] = h->index_to_pos[3 * i + 1] + sh0 * s1a[0][1] + sh1 * s1a[1][1];
     h->i2pos[3 * i + 2] = h->index_to_pos[3 * i + 2];
   }
 

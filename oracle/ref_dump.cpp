@@ -83,6 +83,9 @@ static int dump_main(int argc, char** argv) {
   std::vector<int> vacancies;
   // (this driver only) a Bloch vector (1/A): the job of a k-sampled run with that k_vec
   std::vector<double> k_vec;
+  // (this driver only) a sheet shift "sheet,s1,s2" (1-based sheet, fractions of
+  // its lattice vectors): the job of a shifted configuration
+  std::vector<double> dump_shift;
 
   std::ifstream in(argv[1]);
   if (!in.is_open()) { std::fprintf(stderr, "cannot open %s\n", argv[1]); return 2; }
@@ -93,6 +96,11 @@ static int dump_main(int argc, char** argv) {
       const std::string& key = tk[p];
       auto val = [&](size_t k) { return p + k < tk.size() ? tk[p + k] : std::string(); };
       if (key == "JOB_NAME") opts.setParam("job_name", val(2));
+      if (key == "REF_DUMP_SHIFT") {
+        std::istringstream ss(val(2));
+        std::string t;
+        while (std::getline(ss, t, ',')) dump_shift.push_back(std::atof(t.c_str()));
+      }
       if (key == "REF_DUMP_KVEC") {
         std::istringstream ks(val(2));
         std::string t;
@@ -242,6 +250,10 @@ static int dump_main(int argc, char** argv) {
   // ---- job 1, shifts = 0, as rootChebSolve + workerChebSolve build it ----
   const int num_s = (int)loc.sdata.size();
   std::vector<std::vector<double>> shifts(num_s, std::vector<double>(3, 0.0));
+  if (dump_shift.size() == 3) {
+    shifts[(int)dump_shift[0] - 1][0] = dump_shift[1];
+    shifts[(int)dump_shift[0] - 1][1] = dump_shift[2];
+  }
   // a vacancy list takes the MLMC_VAC solver's path through generateRealH and
   // the KPM functions (solver_type 3, locality.cpp:1392-1450, 2985-3016)
   if (!vacancies.empty()) O.setParam("solver_type", 3);

@@ -80,10 +80,16 @@ def parse_in(name):
                 kv["b_field"] = float(v(2))
             elif key == "REF_DUMP_KVEC":  # a fixture-generator key: the job's Bloch vector
                 kv["k_vec"] = [float(x) for x in v(2).split(",")]
+            elif key == "REF_DUMP_SHIFT":  # a fixture-generator key: "sheet,s1,s2" of the job
+                sh = v(2).split(",")
+                kv["shift"] = (int(sh[0]) - 1, float(sh[1]), float(sh[2]))
     if kv.get("use_b"):
         g.b_field = kv.get("b_field", 0.0)
     if "k_vec" in kv:
         g.k_vec[0], g.k_vec[1] = kv["k_vec"]
+    if "shift" in kv:
+        s, a, b = kv["shift"]
+        g.shifts[s][0], g.shifts[s][1] = a, b
     return g, kv
 
 
@@ -93,6 +99,8 @@ CASES = [c for c in ALL if "bfield" not in c and "_vac_" not in c and "_kvec_" n
 BFIELD_CASES = [c for c in ALL if "bfield" in c]
 # complex Hamiltonians: a magnetic field, or a Bloch vector of a k-sampled periodic job
 KVEC_CASES = [c for c in ALL if "_kvec_" in c]
+# the cases whose .cheb and _matrix.dat the reference's own main() wrote
+E2E_CASES = [c for c in CASES if os.path.exists(os.path.join(GOLDEN, "e2e", c + ".cheb.gz"))]
 COMPLEX_CASES = BFIELD_CASES + KVEC_CASES
 # vacancies (the vacancy solvers' matrix): <base>_vac_<kind> pairs with <base>_<kind>
 VAC_CASES = [c for c in ALL if "_vac_" in c]

@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 import leo2d_gb300 as L
-from tests._golden import CASES, GOLDEN, e2e_text
+from tests._golden import E2E_CASES, GOLDEN, e2e_text
 
 pytestmark = pytest.mark.gpu
 
@@ -46,7 +46,7 @@ def _cond_rows(text, P):
     return np.array(lines[0].split(), dtype=float), np.stack(rows).reshape(-1, P, P)
 
 
-@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("name", E2E_CASES)
 def test_cheb_and_matrix_files(tmp_path, name):
     L.run_input(os.path.join(GOLDEN, "inputs", name + ".in"), tmp_path)
     ours = (tmp_path / (name + ".cheb")).read_text()
