@@ -132,8 +132,15 @@ bool parse_input(const std::string& path, JobSpec& spec, std::string& err) {
       } else if (key == "SOLVER_TYPE") {
         const std::string v = value();
         if (v == "SQ") spec.solver_type = 1;
-        else if (v == "LC" || v == "MLMC_VAC" || v == "VD_FILE" || v == "STRAIN" || v == "FIXED_SHIFT")
+        else if (v == "LC") spec.solver_type = 2;
+        else if (v == "MLMC_VAC" || v == "VD_FILE" || v == "STRAIN" || v == "FIXED_SHIFT")
           spec.unsupported.push_back("SOLVER_TYPE = " + v);
+      } else if (key == "NUM_LC_POINTS") {
+        spec.num_lc_points = std::atoi(value().c_str());
+      } else if (key == "LC_POINTS") {  // main.cpp:438-454: pairs of fractions
+        next();
+        spec.lc_points.assign(2 * (size_t)std::max(spec.num_lc_points, 0), 0.0);
+        for (size_t i = 0; i < spec.lc_points.size(); ++i) spec.lc_points[i] = std::atof(next().c_str());
       } else if (key == "OBSERVABLE_TYPE") {
         const std::string v = value();
         if (v == "DOS") spec.observable_type = 0;

@@ -96,9 +96,13 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     err = "poly_order = " + std::to_string(P) + " is NOT divisible 4 (needed for KPM iterative method)";
     return LEO2D_ERR_BAD_ARG;
   }
-  if (spec.solver_type != 1) {
-    err = "SOLVER_TYPE must be SQ (only the uniform-sampling job list is built)";
+  if (spec.solver_type != 1 && spec.solver_type != 2) {
+    err = "SOLVER_TYPE must be SQ or LC (the uniform-sampling and line-cut job lists are built)";
     return LEO2D_ERR_UNSUPPORTED;
+  }
+  if (spec.solver_type == 2 && (spec.num_lc_points < 2 || spec.lc_points.size() < 2 * (size_t)spec.num_lc_points)) {
+    err = "SOLVER_TYPE = LC needs NUM_LC_POINTS >= 2 and its LC_POINTS";
+    return LEO2D_ERR_BAD_ARG;
   }
   if (spec.nshifts < 1) {
     err = "NSHIFTS must be >= 1";
@@ -127,7 +131,25 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
   // for the last shift sheet every (i/N, j/N), i outer, j inner, and for each
   // of those the list of the remaining shift sheets
   std::vector<std::vector<double>> jobs;  // [job][2 * sheet]
-  {
+  if (spec.solver_type == 2) {
+    // line cuts (locality.cpp:1330-1386): NSHIFTS jobs along the polyline of
+    // LC_POINTS, each shifting the last sheet
+    const int nj = spec.nshifts, m = spec.num_lc_points;
+    const int last = g0.num_sheets - 1;
+    for (int i = 0; i < nj; ++i) {
+      const double x = (1.0 / ((double)nj)) * i;
+      const double total_x = x * (m - 1);
+      const int idx = (int)std::floor(total_x);
+      const double eff_x = std::fmod(total_x, 1);
+      const double* a = &spec.lc_points[2 * (size_t)idx];
+      const double* b = &spec.lc_points[2 * (size_t)std::min(idx + 1, m - 1)];
+      std::vector<double> sh(2 * LEO2D_MAX_SHEETS, 0.0);
+      sh[2 * last] = a[0] + eff_x * (b[0] - a[0]);
+      sh[2 * last + 1] = a[1] + eff_x * (b[1] - a[1]);
+      std::printf("shifts[%d] = [%lf %lf] \n", last, sh[2 * last], sh[2 * last + 1]);
+      jobs.push_back(sh);
+    }
+  } else {
     std::vector<double> sh(2 * LEO2D_MAX_SHEETS, 0.0);
     const int levels = spec.nshifts > 1 ? spec.num_shift_sheets : 0;
     const int N = spec.nshifts;

@@ -156,6 +156,7 @@ static int dump_main(int argc, char** argv) {
       if (key == "USE_B_FIELD") opts.setParam("magOn", std::atoi(val(2).c_str()));
       if (key == "B_FIELD") opts.setParam("B", std::atof(val(2).c_str()));
       if (key == "SOLVER_TYPE" && val(2) == "SQ") opts.setParam("solver_type", 1);
+      if (key == "SOLVER_TYPE" && val(2) == "LC") opts.setParam("solver_type", 2);
       if (key == "OBSERVABLE_TYPE") {
         if (val(2) == "DOS") opts.setParam("observable_type", 0);
         if (val(2) == "COND") opts.setParam("observable_type", 1);

@@ -33,14 +33,14 @@ def test_geometry_matches_fixture_spec(name):
     for s in range(len(ref.shifts)):
         ref.shifts[s][0] = ref.shifts[s][1] = 0.0
     assert bytes(g) == bytes(ref)
-    assert ints[2] == kv["P"] and ints[0] == 1
+    assert ints[2] == kv["P"] and ints[0] == (2 if "_lc_" in name else 1)  # SOLVER_TYPE SQ / LC
     assert ints[8] == kv["target_sheets"][0]
 
 
 def test_unsupported_options_are_reported(tmp_path):
     p = tmp_path / "x.in"
     p.write_text("NUM_SHEETS = 1\nSTART_SHEET 1\nMATERIAL = MoS2\nEND_SHEET 1\nUSE_E_FIELD = 1\n"
-                 "STRAIN_TYPE = 2\nPOLY_ORDER = 30\nSOLVER_TYPE = LC\n")
+                 "STRAIN_TYPE = 2\nPOLY_ORDER = 30\nSOLVER_TYPE = MLMC_VAC\n")
     st, g, ints, msg = _parse(p)
     assert st == 0
     assert ints[7] == 4 and "MoS2" in msg and "USE_E_FIELD" in msg and "STRAIN_TYPE" in msg
