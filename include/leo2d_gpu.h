@@ -95,6 +95,10 @@ typedef struct {
    * the reference, the pairs come from the unshifted geometry and the values,
    * dxH and the positions the matrix keeps from the shifted one. |shift| <= 1. */
   double shifts[LEO2D_MAX_SHEETS][2];
+  /* E_FIELD with USE_E_FIELD = 1: every diagonal entry becomes
+   * (H_ii + energy_shift + z_i E) / energy_rescale, the on-site term of
+   * Locality::onSiteE (src/locality.cpp:7163-7166, 4166-4172). 0 = off. */
+  double e_field;
 } leo2d_geom;
 
 typedef struct leo2d_ctx leo2d_ctx;

@@ -37,7 +37,7 @@ class Geom(ctypes.Structure):
         ("lattice", c_dbl * 2 * 2 * MAX_SHEETS), ("sheet_supercell", c_dbl * 2 * 2 * MAX_SHEETS),
         ("sheet_sc_stride", c_i32 * 2 * 2 * MAX_SHEETS), ("supercell", c_dbl * 2 * 2),
         ("prepared", c_i32), ("b_field", c_dbl), ("k_vec", c_dbl * 2),
-        ("shifts", c_dbl * 2 * MAX_SHEETS),
+        ("shifts", c_dbl * 2 * MAX_SHEETS), ("e_field", c_dbl),
     ]
 
 
@@ -53,7 +53,7 @@ class KpmCfg(ctypes.Structure):
 def make_geom(num_sheets=2, model=MODEL_REF, boundary_condition=0, size=50, max_R=None,
               heights=(0.0, 3.35), angles_deg=(0.0, 0.0), energy_rescale=20.0,
               energy_shift=0.0, supercell_mn=None, sc_search_size=1, b_field=0.0, k_vec=None,
-              shifts=None):
+              shifts=None, e_field=0.0):
     """A Geom filled the way main.cpp fills Sdata for MAXSIZE=size, MINSIZE=-size.
 
     Angles are given in degrees and converted as main.cpp:345-351 does.
@@ -79,6 +79,7 @@ def make_geom(num_sheets=2, model=MODEL_REF, boundary_condition=0, size=50, max_
     g.b_field = float(b_field)
     if k_vec is not None:
         g.k_vec[0], g.k_vec[1] = float(k_vec[0]), float(k_vec[1])
+    g.e_field = float(e_field)
     if shifts is not None:  # {sheet: (s1, s2)}: fractions of the sheet's lattice vectors
         for s, (a, b) in dict(shifts).items():
             g.shifts[s][0], g.shifts[s][1] = float(a), float(b)

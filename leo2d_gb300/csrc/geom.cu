@@ -62,6 +62,7 @@ struct GeomDev {
   double supercell[2][2];
   double rescale, shift;
   double simple_amp;  // 0.33 / rescale (the simple model's interlayer prefactor)
+  double e_field;     // USE_E_FIELD's E: the diagonal gains z E (Locality::onSiteE)
   double b_field;  // non-zero: complex entries t e^{i phi} (Peierls phase)
   double kx, ky;   // Bloch vector: phases k.(r_col - r_row) per periodic image
   int cpx;         // complex entries (a field or a Bloch vector)
@@ -312,6 +313,13 @@ __device__ __forceinline__ void store_value(const GeomDev& G, const RowOut& out,
   out.val_im[e] = 0.0 + t * sn;
 }
 
+// A diagonal entry: (raw + shift) / rescale, with the on-site term z E of a
+// perpendicular electric field (Locality::onSiteE, locality.cpp:7163-7166;
+// generateRealH 4166-4172).
+__device__ __forceinline__ double diag_value(const GeomDev& G, double raw, double z) {
+  return G.e_field != 0.0 ? (raw + G.shift + z * G.e_field) / G.rescale : (raw + G.shift) / G.rescale;
+}
+
 // FP32 copy of the positions for the candidate prefilter of k_flake_rows.
 __global__ void k_pos32(const double* __restrict__ pos, int64_t n, float4* __restrict__ p32) {
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
@@ -372,7 +380,7 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
             k2g = k2 + sh.base;
             const double raw = intralayer(G.model, l0, l, i - ih, j - jh);
             // (0 / rescale is 0: the FP64 division runs for nonzero entries only)
-            t = k2g == row ? (raw + G.shift) / G.rescale : (raw != 0.0 ? raw / G.rescale : 0.0);
+            t = k2g == row ? diag_value(G, raw, sz1) : (raw != 0.0 ? raw / G.rescale : 0.0);
           }
         }
         const bool keep = k2g >= 0;
@@ -541,7 +549,7 @@ __device__ double periodic_value(const GeomDev& G, int64_t row, const int32_t* g
     gd1 = gd1 - dxs * sh.stride[0][1] - dys * sh.stride[1][1];
     const double raw = intralayer(G.model, l0, l2, gd0, gd1);
     const bool diag = k2 == row && (!G.cpx || (dxs == 0 && dys == 0));
-    return diag ? (raw + G.shift) / G.rescale : raw / G.rescale;
+    return diag ? diag_value(G, raw, pos[3 * row + 2]) : raw / G.rescale;
   }
   const double z1 = pos[3 * row + 2];
   const double x2 = pos[3 * k2], y2 = pos[3 * k2 + 1], z2 = pos[3 * k2 + 2];
@@ -878,6 +886,7 @@ void validate_geom(const leo2d_geom* g) {
     LEO_REQUIRE(g->sc_search_size >= 0 && g->sc_search_size <= 3, "sc_search_size must be 0..3");
   LEO_REQUIRE(std::isfinite(g->b_field), "b_field must be finite");
   LEO_REQUIRE(std::isfinite(g->k_vec[0]) && std::isfinite(g->k_vec[1]), "k_vec must be finite");
+  LEO_REQUIRE(std::isfinite(g->e_field), "e_field must be finite");
   for (int s = 0; s < LEO2D_MAX_SHEETS; ++s)
     LEO_REQUIRE(std::isfinite(g->shifts[s][0]) && std::isfinite(g->shifts[s][1]) &&
                     std::fabs(g->shifts[s][0]) <= 1.0 && std::fabs(g->shifts[s][1]) <= 1.0,
@@ -981,6 +990,7 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     G.rescale = g->energy_rescale;
     G.simple_amp = 0.33 / g->energy_rescale;
     G.shift = g->energy_shift;
+    G.e_field = g->e_field;
     for (int s = 0; s < G.S; ++s) fill_sheet(*g, s, G.sh[s]);
 
     // sites of every sheet

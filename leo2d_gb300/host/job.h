@@ -42,6 +42,8 @@ struct JobSpec {
   int bounds = 0;             // 0 = ENERGY_RESCALE/SHIFT as given, 1 = Gershgorin x 1.01
   int use_b = 0;              // USE_B_FIELD: the complex Hamiltonian (generateCpxH)
   double b_field = 0.0;       // B_FIELD, tesla
+  int use_e = 0;              // USE_E_FIELD: the on-site z E term
+  double e_field = 0.0;       // E_FIELD
   int energies = 0;           // > 0: also write a DOS on this many equispaced energies
   int block = 0;
   std::vector<std::string> unsupported;  // keys that select paths outside this build

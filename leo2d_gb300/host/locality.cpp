@@ -244,9 +244,9 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
       } else {
         cheb << "NO_TAR \n";
       }
-      if (spec.use_b == 1) {  // the field lines of the header (param_tools.cpp:572-575)
+      if (spec.use_b == 1 || spec.use_e == 1) {  // the field lines of the header (param_tools.cpp:572-575)
         cheb << "MAG_ON  = " << spec.use_b << ", B = " << spec.b_field << " \n";
-        cheb << "ELEC_ON = " << 0 << ", E = " << 0.0 << " \n";
+        cheb << "ELEC_ON = " << spec.use_e << ", E = " << spec.e_field << " \n";
       }
     }
 

@@ -480,7 +480,10 @@ int oracle_build(const leo2d_geom* gin, oracle_h** out) {
       }
       double x1 = P[3 * ki] + shx, y1 = P[3 * ki + 1] + shy;
       double x2 = P[3 * nk], y2 = P[3 * nk + 1];
-      double t = nk == ki ? (pr.t + shift) / rescale : pr.t / rescale;
+      // (the diagonal: generateRealH's onSiteE term z E with USE_E_FIELD)
+      double t = nk == ki ? (g.e_field != 0.0 ? (pr.t + shift + P[3 * ki + 2] * g.e_field) / rescale
+                                              : (pr.t + shift) / rescale)
+                          : pr.t / rescale;
       if (t != 0) {
         h->val[cnt] += t;
         h->dx[cnt] += (x1 - x2) * t;
@@ -552,7 +555,9 @@ void oracle_bloch(const oracle_h* h, double kx, double ky, double* re, double* i
     while (ic < n_intra && h->intra[ic].i == ki) {
       const Pair& pr = h->intra[ic];
       const bool home = pr.sc0 == 0 && pr.sc1 == 0;
-      const double t = (pr.j == ki && home) ? (pr.t + shift) / rescale : pr.t / rescale;
+      const double t = (pr.j == ki && home) ? (g.e_field != 0.0 ? (pr.t + shift + P[3 * ki + 2] * g.e_field) / rescale
+                                                                 : (pr.t + shift) / rescale)
+                                            : pr.t / rescale;
       add(pr, ki, t);
       if (ic + 1 == n_intra || h->intra[ic + 1].i != ki || h->intra[ic + 1].j != pr.j) ++cnt;
       ++ic;

@@ -155,6 +155,8 @@ static int dump_main(int argc, char** argv) {
       if (key == "POLY_ORDER") opts.setParam("poly_order", std::atoi(val(2).c_str()));
       if (key == "USE_B_FIELD") opts.setParam("magOn", std::atoi(val(2).c_str()));
       if (key == "B_FIELD") opts.setParam("B", std::atof(val(2).c_str()));
+      if (key == "USE_E_FIELD") opts.setParam("elecOn", std::atoi(val(2).c_str()));
+      if (key == "E_FIELD") opts.setParam("E", std::atof(val(2).c_str()));
       if (key == "SOLVER_TYPE" && val(2) == "SQ") opts.setParam("solver_type", 1);
       if (key == "SOLVER_TYPE" && val(2) == "LC") opts.setParam("solver_type", 2);
       if (key == "OBSERVABLE_TYPE") {

@@ -78,6 +78,10 @@ def parse_in(name):
                 kv["use_b"] = int(v(2))
             elif key == "B_FIELD":
                 kv["b_field"] = float(v(2))
+            elif key == "USE_E_FIELD":
+                kv["use_e"] = int(v(2))
+            elif key == "E_FIELD":
+                kv["e_field"] = float(v(2))
             elif key == "REF_DUMP_KVEC":  # a fixture-generator key: the job's Bloch vector
                 kv["k_vec"] = [float(x) for x in v(2).split(",")]
             elif key == "REF_DUMP_SHIFT":  # a fixture-generator key: "sheet,s1,s2" of the job
@@ -85,6 +89,8 @@ def parse_in(name):
                 kv["shift"] = (int(sh[0]) - 1, float(sh[1]), float(sh[2]))
     if kv.get("use_b"):
         g.b_field = kv.get("b_field", 0.0)
+    if kv.get("use_e"):
+        g.e_field = kv.get("e_field", 0.0)
     if "k_vec" in kv:
         g.k_vec[0], g.k_vec[1] = kv["k_vec"]
     if "shift" in kv:

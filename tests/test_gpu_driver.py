@@ -80,8 +80,8 @@ def test_driver_executable(tmp_path):
 
 def test_unsupported_input_is_refused(tmp_path):
     p = tmp_path / "bad.in"
-    p.write_text(open(os.path.join(GOLDEN, "inputs", "flake_trace.in")).read() + "USE_E_FIELD = 1\n")
-    with pytest.raises(L.Leo2dError, match="USE_E_FIELD"):
+    p.write_text(open(os.path.join(GOLDEN, "inputs", "flake_trace.in")).read() + "DIAGONALIZE = 1\n")
+    with pytest.raises(L.Leo2dError, match="DIAGONALIZE"):
         L.run_input(p, tmp_path)
     p.write_text(open(os.path.join(GOLDEN, "inputs", "flake_trace.in")).read().replace(
         "POLY_ORDER = 64", "POLY_ORDER = 62"))

@@ -39,11 +39,11 @@ def test_geometry_matches_fixture_spec(name):
 
 def test_unsupported_options_are_reported(tmp_path):
     p = tmp_path / "x.in"
-    p.write_text("NUM_SHEETS = 1\nSTART_SHEET 1\nMATERIAL = MoS2\nEND_SHEET 1\nUSE_E_FIELD = 1\n"
+    p.write_text("NUM_SHEETS = 1\nSTART_SHEET 1\nMATERIAL = MoS2\nEND_SHEET 1\nDIAGONALIZE = 1\n"
                  "STRAIN_TYPE = 2\nPOLY_ORDER = 30\nSOLVER_TYPE = MLMC_VAC\n")
     st, g, ints, msg = _parse(p)
     assert st == 0
-    assert ints[7] == 4 and "MoS2" in msg and "USE_E_FIELD" in msg and "STRAIN_TYPE" in msg
+    assert ints[7] == 4 and "MoS2" in msg and "DIAGONALIZE" in msg and "STRAIN_TYPE" in msg
 
 
 @pytest.mark.parametrize("name", BFIELD_CASES)
