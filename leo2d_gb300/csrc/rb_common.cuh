@@ -92,6 +92,14 @@ __device__ __forceinline__ float4 ld_once4(const float* p) {
 }
 
 
+// T_{n+1} (and D T_n) rows are not read again by the launch that writes them:
+// their stores keep out of L1, which holds the gathered T_n rows
+__device__ __forceinline__ void st_na4(float* p, const float4& v) {
+  asm volatile("st.global.L1::no_allocate.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z),
+               "f"(v.w)
+               : "memory");
+}
+
 // Complex H: the lane's 4 columns are two complex numbers (re, im, re, im); a
 // slot's values are a + ib per row (a from the value panel, b from the
 // imaginary panel): y += (a + ib)(x_re + i x_im).

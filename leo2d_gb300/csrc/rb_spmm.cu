@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
         float p[4][4], hj[4];
         accj.get(p);
         scatter(p, hj);
-        if (ok) *reinterpret_cast<float4*>(a.out2 + row * C + 4 * q) = make_float4(hj[0], hj[1], hj[2], hj[3]);
+        if (ok) st_na4(a.out2 + row * C + 4 * q, make_float4(hj[0], hj[1], hj[2], hj[3]));
       }
       if (ok) {
         float4 y;
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
           const float4 xp = ldcs4(tprev + row * C + 4 * q);
           y = make_float4(alpha * h[0] - xp.x, alpha * h[1] - xp.y, alpha * h[2] - xp.z, alpha * h[3] - xp.w);
         }
-        *reinterpret_cast<float4*>(a.tp + row * C + 4 * q) = y;
+        st_na4(a.tp + row * C + 4 * q, y);
         if constexpr (!DJ) {
           const float4 xn = ldg4(tq + row * C);
           e0[0] += xn.x * xn.x;
