@@ -133,7 +133,8 @@ bool parse_input(const std::string& path, JobSpec& spec, std::string& err) {
         const std::string v = value();
         if (v == "SQ") spec.solver_type = 1;
         else if (v == "LC") spec.solver_type = 2;
-        else if (v == "MLMC_VAC" || v == "VD_FILE" || v == "STRAIN" || v == "FIXED_SHIFT")
+        else if (v == "FIXED_SHIFT") spec.solver_type = 6;
+        else if (v == "MLMC_VAC" || v == "VD_FILE" || v == "STRAIN")
           spec.unsupported.push_back("SOLVER_TYPE = " + v);
       } else if (key == "NUM_LC_POINTS") {
         spec.num_lc_points = std::atoi(value().c_str());

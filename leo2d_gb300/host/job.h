@@ -18,7 +18,7 @@ namespace leo2d_host {
 struct JobSpec {
   std::string job_name = "LEO2D_JOB";
   leo2d_geom geom{};
-  int solver_type = 0;        // SOLVER_TYPE: 1 = SQ, 2 = LC
+  int solver_type = 0;        // SOLVER_TYPE: 1 = SQ, 2 = LC, 6 = FIXED_SHIFT
   int num_lc_points = 0;      // NUM_LC_POINTS (LC: the polyline of shifts of the last sheet)
   std::vector<double> lc_points;  // LC_POINTS, (s1, s2) pairs
   int observable_type = 0;    // 0 = DOS, 1 = COND

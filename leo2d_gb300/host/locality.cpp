@@ -96,8 +96,8 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     err = "poly_order = " + std::to_string(P) + " is NOT divisible 4 (needed for KPM iterative method)";
     return LEO2D_ERR_BAD_ARG;
   }
-  if (spec.solver_type != 1 && spec.solver_type != 2) {
-    err = "SOLVER_TYPE must be SQ or LC (the uniform-sampling and line-cut job lists are built)";
+  if (spec.solver_type != 1 && spec.solver_type != 2 && spec.solver_type != 6) {
+    err = "SOLVER_TYPE must be SQ, LC or FIXED_SHIFT (their job lists are built)";
     return LEO2D_ERR_UNSUPPORTED;
   }
   if (spec.solver_type == 2 && (spec.num_lc_points < 2 || spec.lc_points.size() < 2 * (size_t)spec.num_lc_points)) {
@@ -131,7 +131,12 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
   // for the last shift sheet every (i/N, j/N), i outer, j inner, and for each
   // of those the list of the remaining shift sheets
   std::vector<std::vector<double>> jobs;  // [job][2 * sheet]
-  if (spec.solver_type == 2) {
+  if (spec.solver_type == 6) {
+    // one job, every sheet but the first shifted by (1/3, 1/3) (locality.cpp:1580-1608)
+    std::vector<double> sh(2 * LEO2D_MAX_SHEETS, 0.0);
+    for (int s = 1; s < g0.num_sheets; ++s) sh[2 * s] = sh[2 * s + 1] = 1.0 / 3.0;
+    jobs.push_back(sh);
+  } else if (spec.solver_type == 2) {
     // line cuts (locality.cpp:1330-1386): NSHIFTS jobs along the polyline of
     // LC_POINTS, each shifting the last sheet
     const int nj = spec.nshifts, m = spec.num_lc_points;
@@ -231,8 +236,9 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
       E[i] = gersh ? center + rescale * x : shift + rescale * x;
     }
 
-    if (spec.verbose_save != 0) {  // Param_tools::saveHeader (param_tools.cpp:467-505)
-      cheb << "JOBID = " << job + 1 << " \n";
+    // (the sheet and target lines are written for the SQ and LC solvers only)
+    if (spec.verbose_save != 0) cheb << "JOBID = " << job + 1 << " \n";
+    if (spec.verbose_save != 0 && spec.solver_type != 6) {  // Param_tools::saveHeader (param_tools.cpp:467-505)
       cheb << "SHEET: SHIFT_X, SHIFT_Y, SHIFT_Z \n";
       for (int s = 0; s < g.num_sheets; ++s)
         cheb << s + 1 << "    : " << g.shifts[s][0] << ", " << g.shifts[s][1] << ", " << 0.0 << " \n";
@@ -244,10 +250,10 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
       } else {
         cheb << "NO_TAR \n";
       }
-      if (spec.use_b == 1 || spec.use_e == 1) {  // the field lines of the header (param_tools.cpp:572-575)
-        cheb << "MAG_ON  = " << spec.use_b << ", B = " << spec.b_field << " \n";
-        cheb << "ELEC_ON = " << spec.use_e << ", E = " << spec.e_field << " \n";
-      }
+    }
+    if (spec.verbose_save != 0 && (spec.use_b == 1 || spec.use_e == 1)) {  // param_tools.cpp:572-575
+      cheb << "MAG_ON  = " << spec.use_b << ", B = " << spec.b_field << " \n";
+      cheb << "ELEC_ON = " << spec.use_e << ", E = " << spec.e_field << " \n";
     }
 
     leo2d_kpm_cfg cfg{};

@@ -159,6 +159,7 @@ static int dump_main(int argc, char** argv) {
       if (key == "E_FIELD") opts.setParam("E", std::atof(val(2).c_str()));
       if (key == "SOLVER_TYPE" && val(2) == "SQ") opts.setParam("solver_type", 1);
       if (key == "SOLVER_TYPE" && val(2) == "LC") opts.setParam("solver_type", 2);
+      if (key == "SOLVER_TYPE" && val(2) == "FIXED_SHIFT") opts.setParam("solver_type", 6);
       if (key == "OBSERVABLE_TYPE") {
         if (val(2) == "DOS") opts.setParam("observable_type", 0);
         if (val(2) == "COND") opts.setParam("observable_type", 1);
@@ -253,6 +254,9 @@ static int dump_main(int argc, char** argv) {
   // ---- job 1, shifts = 0, as rootChebSolve + workerChebSolve build it ----
   const int num_s = (int)loc.sdata.size();
   std::vector<std::vector<double>> shifts(num_s, std::vector<double>(3, 0.0));
+  // the fixed-shift solver's one job (locality.cpp:1580-1608)
+  if (O.getInt("solver_type") == 6)
+    for (int s = 1; s < num_s; ++s) shifts[s][0] = shifts[s][1] = 1.0 / 3.0;
   if (dump_shift.size() == 3) {
     shifts[(int)dump_shift[0] - 1][0] = dump_shift[1];
     shifts[(int)dump_shift[0] - 1][1] = dump_shift[2];

@@ -78,6 +78,8 @@ def parse_in(name):
                 kv["use_b"] = int(v(2))
             elif key == "B_FIELD":
                 kv["b_field"] = float(v(2))
+            elif key == "SOLVER_TYPE":
+                kv["solver"] = v(2)
             elif key == "USE_E_FIELD":
                 kv["use_e"] = int(v(2))
             elif key == "E_FIELD":
@@ -93,6 +95,9 @@ def parse_in(name):
         g.e_field = kv.get("e_field", 0.0)
     if "k_vec" in kv:
         g.k_vec[0], g.k_vec[1] = kv["k_vec"]
+    if kv.get("solver") == "FIXED_SHIFT":  # its one job shifts every sheet but the first
+        for s in range(1, g.num_sheets):
+            g.shifts[s][0] = g.shifts[s][1] = 1.0 / 3.0
     if "shift" in kv:
         s, a, b = kv["shift"]
         g.shifts[s][0], g.shifts[s][1] = a, b

@@ -33,7 +33,7 @@ def test_geometry_matches_fixture_spec(name):
     for s in range(len(ref.shifts)):
         ref.shifts[s][0] = ref.shifts[s][1] = 0.0
     assert bytes(g) == bytes(ref)
-    assert ints[2] == kv["P"] and ints[0] == (2 if "_lc_" in name else 1)  # SOLVER_TYPE SQ / LC
+    assert ints[2] == kv["P"] and ints[0] == {"LC": 2, "FIXED_SHIFT": 6}.get(kv.get("solver"), 1)
     assert ints[8] == kv["target_sheets"][0]
 
 
