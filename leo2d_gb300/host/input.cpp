@@ -183,12 +183,20 @@ bool parse_input(const std::string& path, JobSpec& spec, std::string& err) {
         spec.use_b = std::atoi(value().c_str());
       } else if (key == "B_FIELD") {
         spec.b_field = std::atof(value().c_str());
+      } else if (key == "K_SAMPLING") {  // main.cpp:175-200
+        spec.k_sampling = std::atoi(value().c_str());
+      } else if (key == "K_TYPE") {
+        spec.k_type = std::atoi(value().c_str());
+      } else if (key == "K_GRID") {
+        next();
+        spec.num_k1 = std::atoi(next().c_str());
+        spec.num_k2 = std::atoi(next().c_str());
       } else if (key == "USE_E_FIELD") {  // main.cpp:832-842
         spec.use_e = std::atoi(value().c_str());
       } else if (key == "E_FIELD") {
         spec.e_field = std::atof(value().c_str());
       } else if (key == "DIAGONALIZE" ||
-                 key == "K_SAMPLING" || key == "MLMC" || key == "CHIRAL_ON" || key == "BALLISTIC_TRANSPORT" ||
+                 key == "MLMC" || key == "CHIRAL_ON" || key == "BALLISTIC_TRANSPORT" ||
                  key == "MAT_FROM_FILE" || key == "GLOBAL_SHIFTS_ON" || key == "UNIFORM_STRAIN" ||
                  key == "COND_POLY_PAR" || key == "MAT_SOC_ON") {
         const std::string v = value();
@@ -235,6 +243,11 @@ bool parse_input(const std::string& path, JobSpec& spec, std::string& err) {
   if (spec.target_sheets.empty()) spec.target_sheets.push_back(0);
   // a magnetic field: the complex Hamiltonian of generateCpxH (locality.cpp:2906-2909)
   if (spec.use_e == 1) g.e_field = spec.e_field;
+  if (spec.k_sampling == 1) {
+    if (spec.k_type != 0) spec.unsupported.push_back("K_TYPE = " + std::to_string(spec.k_type));
+    if (g.boundary_condition != 1) spec.unsupported.push_back("K_SAMPLING = 1 with BOUNDARY_CONDITION = 0");
+    if (spec.observable_type == 1) spec.unsupported.push_back("K_SAMPLING = 1 with OBSERVABLE_TYPE = COND");
+  }
   if (spec.use_b == 1) {
     g.b_field = spec.b_field;
     if (g.boundary_condition != 0) spec.unsupported.push_back("USE_B_FIELD = 1 with BOUNDARY_CONDITION = 1");

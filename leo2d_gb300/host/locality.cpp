@@ -8,6 +8,7 @@
 // the transforms run there (leo2d_dos_transform / leo2d_cond_transform), and
 // the files are written as Param_tools::save (src/params/param_tools.cpp:19-316)
 // and generateRealH (src/locality.cpp:4366-4448) write them.
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -173,11 +174,44 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     };
     rec(rec, levels);
   }
+  // K_SAMPLING with K_TYPE = 0 (locality.cpp:1615-1650): each job at every
+  // point k = (k1/n1) b1 + (k2/n2) b2 of the supercell's reciprocal grid, k1
+  // outer, k2 inner; b from Locality::getReciprocal (locality.cpp:7215-7262)
+  std::vector<std::array<double, 2>> kjobs;
+  if (spec.k_sampling == 1) {
+    const double a[3][3] = {{g0.supercell[0][0], g0.supercell[0][1], 0.0},
+                            {g0.supercell[1][0], g0.supercell[1][1], 0.0},
+                            {0.0, 0.0, 1.0}};
+    auto cross = [](const double* x, const double* y, int d) {
+      return d == 0 ? x[1] * y[2] - x[2] * y[1] : (d == 1 ? x[2] * y[0] - x[0] * y[2] : x[0] * y[1] - x[1] * y[0]);
+    };
+    double den1 = 0.0, den2 = 0.0;
+    for (int j = 0; j < 3; ++j) {
+      den1 += a[0][j] * cross(a[1], a[2], j);
+      den2 += a[1][j] * cross(a[2], a[0], j);
+    }
+    double b[2][2];
+    for (int k = 0; k < 2; ++k) {
+      b[0][k] = 2 * M_PI * cross(a[1], a[2], k) / den1;
+      b[1][k] = 2 * M_PI * cross(a[2], a[0], k) / den2;
+    }
+    std::vector<std::vector<double>> shift_jobs = jobs;
+    jobs.clear();
+    for (const auto& sj : shift_jobs)
+      for (int k1 = 0; k1 < spec.num_k1; ++k1)
+        for (int k2 = 0; k2 < spec.num_k2; ++k2) {
+          jobs.push_back(sj);
+          kjobs.push_back({(k1 / (double)spec.num_k1) * b[0][0] + (k2 / (double)spec.num_k2) * b[1][0],
+                           (k1 / (double)spec.num_k1) * b[0][1] + (k2 / (double)spec.num_k2) * b[1][1]});
+        }
+  }
+  // a complex Hamiltonian: a magnetic field or Bloch phases (locality.cpp:2906-2909)
+  const bool cpx_run = spec.use_b == 1 || spec.k_sampling == 1;
   const bool gersh = spec.bounds == 1;
   uint32_t flags = 0;
   if (spec.observable_type == 1 || spec.matrix_save > 1) flags |= LEO2D_CSR_WITH_DX;
   // generateCpxH's matrix save lists every stored pair, zeros included (locality.cpp:5213-5228)
-  if (spec.use_b == 1 && spec.matrix_save > 0) flags |= LEO2D_CSR_KEEP_ZEROS;
+  if (cpx_run && spec.matrix_save > 0) flags |= LEO2D_CSR_KEEP_ZEROS;
   std::ofstream cheb(join_path(out_dir, spec.job_name + ".cheb"));
   if (!cheb.is_open()) {
     err = "cannot write " + spec.job_name + ".cheb";
@@ -192,6 +226,7 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
   std::vector<int32_t> grid4;
   std::vector<double> pos;
   std::vector<int64_t> targets;
+  bool last_complex = false;
   for (size_t job = 0; job < jobs.size(); ++job) {
     const bool first_job = job == 0;
     leo2d_geom g = g0;
@@ -199,6 +234,11 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
       g.shifts[s][0] = jobs[job][2 * s];
       g.shifts[s][1] = jobs[job][2 * s + 1];
     }
+    if (!kjobs.empty()) {
+      g.k_vec[0] = kjobs[job][0];
+      g.k_vec[1] = kjobs[job][1];
+    }
+    last_complex = g.b_field != 0.0 || g.k_vec[0] != 0.0 || g.k_vec[1] != 0.0;
     double rescale = g.energy_rescale, shift = g.energy_shift, center = -shift;
     if (gersh) {
       g.energy_rescale = 1.0;
@@ -260,7 +300,7 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     cfg.poly_order = P;
     // (the complex Hamiltonian of a magnetic field runs the FP32 recursion only)
     cfg.precision = spec.precision >= 0 ? spec.precision
-                                        : ((spec.observable_type == 1 || spec.use_b == 1) ? LEO2D_FP32 : LEO2D_FP64);
+                                        : ((spec.observable_type == 1 || cpx_run) ? LEO2D_FP32 : LEO2D_FP64);
     cfg.block = spec.block;
     cfg.seed = spec.seed;
 
@@ -371,6 +411,17 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     }
   }  // jobs
   cheb.close();
+  if (!kjobs.empty()) {  // Param_tools::saveKpts (param_tools.cpp:579-602), one line per job
+    std::ofstream kf(join_path(out_dir, spec.job_name + ".kpts"));
+    kf << std::fixed;
+    kf.precision(10);
+    for (const auto& k : kjobs) {
+      if (k[0] >= 0) kf << " ";
+      kf << k[0] << "\t\t";
+      if (k[1] >= 0) kf << " ";
+      kf << k[1] << " \n";
+    }
+  }
 
   // (the matrix and position files of the last job: the reference's jobs
   // overwrite each other's, locality.cpp:4362-4365)
@@ -384,9 +435,9 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     }
     CHECK(leo2d_csr_download(ctx.h, csr.h, rp.data(), col.data(), val.data(),
                              dx.empty() ? nullptr : dx.data(), dy.empty() ? nullptr : dy.data()));
-    if (spec.use_b == 1) {  // generateCpxH's matrix save (locality.cpp:5213-5228): every entry, re and im
+    if (cpx_run) {  // generateCpxH's matrix save (locality.cpp:5213-5228): every entry, re and im
       std::vector<double> im(nnz, 0.0);
-      if (spec.geom.b_field != 0.0) CHECK(leo2d_csr_download_imag(ctx.h, csr.h, im.data()));
+      if (last_complex) CHECK(leo2d_csr_download_imag(ctx.h, csr.h, im.data()));
       std::ofstream f(join_path(out_dir, spec.job_name + "_matrix.dat"));
       for (int64_t i = 0; i < n; ++i)
         for (int64_t j = rp[i]; j < rp[i + 1]; ++j)
@@ -398,7 +449,7 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
         for (int64_t j = rp[i]; j < rp[i + 1]; ++j)
           if (std::fabs(v[j]) > 1e-12) f << col[j] + 1 << ", " << i + 1 << ", " << v[j] << "\n";
     };
-    if (spec.use_b != 1) dump("_matrix.dat", val);
+    if (!cpx_run) dump("_matrix.dat", val);
     if (spec.matrix_save > 1) {
       dump("_dxH_matrix.dat", dx);
       dump("_dyH_matrix.dat", dy);

@@ -62,7 +62,7 @@ def run_e2e(inp, name):
         env = dict(os.environ, LEO2D_REF_RANKS="2")
         subprocess.run([os.path.join(REF_DIR, "leo2d_ref"), os.path.basename(inp)], cwd=d,
                        check=True, stdout=subprocess.DEVNULL, env=env)
-        for suffix in (".cheb", "_matrix.dat"):
+        for suffix in (".cheb", "_matrix.dat", ".kpts"):
             src = os.path.join(d, name + suffix)
             if os.path.exists(src):
                 dst = os.path.join(HERE, "e2e", name + suffix + ".gz")

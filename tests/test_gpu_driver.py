@@ -52,7 +52,16 @@ def test_cheb_and_matrix_files(tmp_path, name):
     ours = (tmp_path / (name + ".cheb")).read_text()
     ref = e2e_text(name, ".cheb")
     assert ours.count("\n") == ref.count("\n")
-    if name == "flake_cond":
+    if "_ksamp_" in name:
+        # k-sampled jobs run the complex FP32 recursion: 1e-4 of the largest value;
+        # the k points themselves are written as the reference writes them
+        fo = np.array([x for x in _numbers(ours) if isinstance(x, float)])
+        fr = np.array([x for x in _numbers(ref) if isinstance(x, float)])
+        assert [x for x in _numbers(ours) if not isinstance(x, float)] == \
+            [x for x in _numbers(ref) if not isinstance(x, float)]
+        assert len(fo) == len(fr) and np.abs(fo - fr).max() <= 1e-4 * np.abs(fr).max() + 2e-6
+        assert (tmp_path / (name + ".kpts")).read_text() == e2e_text(name, ".kpts")
+    elif name == "flake_cond":
         # Kubo moments: the recursion is FP32, so compare at 1e-4 of the largest
         # moment. The reference defines the first target's columns 0..P-2 only
         # (the second target's block is NaN and column P-1 is never written).
