@@ -170,11 +170,8 @@ def vacancy_rows(n, vacancies, orbitals):
     return o - below[o]
 
 
-def k_grid(geom, n1, n2):
-    """Bloch vectors of grid k-sampling (K_TYPE = 0, locality.cpp:1617-1650), in job
-    order (k1 outer, k2 inner): k = (k1/n1) b1 + (k2/n2) b2, with b1, b2 the
-    reciprocal vectors of the prepared supercell (Locality::getReciprocal,
-    locality.cpp:7215-7262). Returns [n1 * n2][2]."""
+def _reciprocal(geom):
+    """b1, b2 of the prepared supercell (Locality::getReciprocal, locality.cpp:7215-7262)."""
     a = np.array([[geom.supercell[0][0], geom.supercell[0][1], 0.0],
                   [geom.supercell[1][0], geom.supercell[1][1], 0.0], [0.0, 0.0, 1.0]])
 
@@ -185,12 +182,42 @@ def k_grid(geom, n1, n2):
     for j in range(3):
         den1 += a[0][j] * cross(a[1], a[2], j)
         den2 += a[1][j] * cross(a[2], a[0], j)
-    b = [[2 * np.pi * cross(a[1], a[2], k) / den1 for k in range(2)],
-         [2 * np.pi * cross(a[2], a[0], k) / den2 for k in range(2)]]
+    return [[2 * np.pi * cross(a[1], a[2], k) / den1 for k in range(2)],
+            [2 * np.pi * cross(a[2], a[0], k) / den2 for k in range(2)]]
+
+
+def k_grid(geom, n1, n2):
+    """Bloch vectors of grid k-sampling (K_TYPE = 0, locality.cpp:1617-1650), in job
+    order (k1 outer, k2 inner): k = (k1/n1) b1 + (k2/n2) b2, with b1, b2 the
+    reciprocal vectors of the prepared supercell (Locality::getReciprocal,
+    locality.cpp:7215-7262). Returns [n1 * n2][2]."""
+    b = _reciprocal(geom)
     out = []
     for k1 in range(n1):
         for k2 in range(n2):
             out.append([(k1 / n1) * b[0][0] + (k2 / n2) * b[1][0], (k1 / n1) * b[0][1] + (k2 / n2) * b[1][1]])
+    return np.array(out)
+
+
+def k_path(geom, n):
+    """Bloch vectors of the supercell zone's path K -> Gamma -> M -> K (K_TYPE = 1,
+    locality.cpp:1655-1797), n points in job order: point i sits at c = 3i/n on the
+    path, K = b2 turned by -30 degrees and divided by 2 cos 30, M = b2 / 2,
+    Gamma = 0. Returns [n][2]."""
+    b = _reciprocal(geom)
+    r = 1.0 / (2.0 * np.cos(np.pi / 6))
+    kk = [r * (np.cos(-np.pi / 6) * b[1][0] - np.sin(-np.pi / 6) * b[1][1]),
+          r * (np.sin(-np.pi / 6) * b[1][0] + np.cos(-np.pi / 6) * b[1][1])]
+    gm, mm = [0.0, 0.0], [b[1][0] / 2.0, b[1][1] / 2.0]
+    out = []
+    for i in range(n):
+        c = (3.0 / n) * i
+        if c <= 1:
+            out.append([(1.0 - c) * kk[d] + c * gm[d] for d in range(2)])
+        elif c <= 2:
+            out.append([(2.0 - c) * gm[d] + (c - 1.0) * mm[d] for d in range(2)])
+        else:
+            out.append([(3.0 - c) * mm[d] + (c - 2.0) * kk[d] for d in range(2)])
     return np.array(out)
 
 

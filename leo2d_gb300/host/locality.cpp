@@ -105,6 +105,14 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     err = "SOLVER_TYPE = LC needs NUM_LC_POINTS >= 2 and its LC_POINTS";
     return LEO2D_ERR_BAD_ARG;
   }
+  if (spec.k_sampling == 1 && spec.k_type == 1 && spec.geom.num_sheets < 2) {  // locality.cpp:1661-1663
+    err = "cannot use K_TYPE == 1 (twisted BZ) for a single layer";
+    return LEO2D_ERR_BAD_ARG;
+  }
+  if (spec.k_sampling == 1 && (spec.num_k1 < 1 || (spec.k_type == 0 && spec.num_k2 < 1))) {
+    err = "K_GRID must name at least one k point";
+    return LEO2D_ERR_BAD_ARG;
+  }
   if (spec.nshifts < 1) {
     err = "NSHIFTS must be >= 1";
     return LEO2D_ERR_BAD_ARG;
@@ -197,7 +205,27 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     }
     std::vector<std::vector<double>> shift_jobs = jobs;
     jobs.clear();
-    for (const auto& sj : shift_jobs)
+    if (spec.k_type == 1) {
+      // K_TYPE = 1 (locality.cpp:1655-1797): each job at NUM_K1 points of the
+      // supercell zone's path K -> Gamma -> M -> K, c = 3i/NUM_K1 the position on
+      // it; K = b2 turned by -30 degrees over 2 cos 30, M = b2 / 2, Gamma = 0
+      const double r = 1.0 / (2.0 * std::cos(M_PI / 6));
+      const double kk[2] = {r * (std::cos(-M_PI / 6) * b[1][0] - std::sin(-M_PI / 6) * b[1][1]),
+                            r * (std::sin(-M_PI / 6) * b[1][0] + std::cos(-M_PI / 6) * b[1][1])};
+      const double gm[2] = {0.0, 0.0};
+      const double mm[2] = {b[1][0] / 2.0, b[1][1] / 2.0};
+      for (const auto& sj : shift_jobs)
+        for (int i = 0; i < spec.num_k1; ++i) {
+          const double c = (3.0 / (double)spec.num_k1) * i;
+          std::array<double, 2> k;
+          for (int d = 0; d < 2; ++d)
+            k[d] = c <= 1 ? (1.0 - c) * kk[d] + (c - 0.0) * gm[d]
+                          : (c <= 2 ? (2.0 - c) * gm[d] + (c - 1.0) * mm[d] : (3.0 - c) * mm[d] + (c - 2.0) * kk[d]);
+          jobs.push_back(sj);
+          kjobs.push_back(k);
+        }
+    }
+    for (const auto& sj : spec.k_type == 0 ? shift_jobs : std::vector<std::vector<double>>())
       for (int k1 = 0; k1 < spec.num_k1; ++k1)
         for (int k2 = 0; k2 < spec.num_k2; ++k2) {
           jobs.push_back(sj);

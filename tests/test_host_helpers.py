@@ -27,3 +27,33 @@ def test_vacancy_rows_match_the_relabelling():
     assert kept == n - 4
     orbitals = np.arange(n)
     np.testing.assert_array_equal(L.vacancy_rows(n, vac, orbitals), orbitals - red[:n])
+
+
+def _kpts_text(ks):
+    """Param_tools::saveKpts (param_tools.cpp:579-602): 10 decimals, a space before
+    a non-negative value, two tabs between the components."""
+    out = []
+    for kx, ky in ks:
+        out.append((" " if kx >= 0 else "") + f"{kx:.10f}\t\t" + (" " if ky >= 0 else "") + f"{ky:.10f} \n")
+    return "".join(out)
+
+
+def test_k_lists_match_the_reference_kpts_files():
+    """The k points the reference's own main() wrote for a K_TYPE = 0 grid (2 x 2)
+    and a K_TYPE = 1 path (6 points, every leg of K -> Gamma -> M -> K)."""
+    from tests._golden import e2e_text, parse_in
+    for name, ks in (("sc32_ksamp_ldos", lambda g: L.k_grid(g, 2, 2)),
+                     ("sc32_ksamp_path_ldos", lambda g: L.k_path(g, 6))):
+        g, _ = parse_in(name)
+        g = oracle.geom_prepare(g)
+        assert _kpts_text(ks(g)) == e2e_text(name, ".kpts"), name
+
+
+def test_k_path_corners():
+    """Gamma at a third of the way, M at two thirds; |K| = |b2| / (2 cos 30) = |b2| / sqrt 3."""
+    g = oracle.geom_prepare(L.make_geom(boundary_condition=1, supercell_mn=(4, 5), size=16, energy_rescale=13.0))
+    ks = L.k_path(g, 9)
+    b2 = 2 * L.k_grid(g, 1, 2)[1]
+    np.testing.assert_allclose(ks[3], [0.0, 0.0], atol=1e-15)
+    np.testing.assert_allclose(ks[6], b2 / 2, atol=1e-15)
+    np.testing.assert_allclose(np.linalg.norm(ks[0]), np.linalg.norm(b2) / np.sqrt(3), rtol=1e-14)
