@@ -170,10 +170,9 @@ def vacancy_rows(n, vacancies, orbitals):
     return o - below[o]
 
 
-def _reciprocal(geom):
-    """b1, b2 of the prepared supercell (Locality::getReciprocal, locality.cpp:7215-7262)."""
-    a = np.array([[geom.supercell[0][0], geom.supercell[0][1], 0.0],
-                  [geom.supercell[1][0], geom.supercell[1][1], 0.0], [0.0, 0.0, 1.0]])
+def _reciprocal(a2):
+    """b1, b2 of the lattice a1, a2 (Locality::getReciprocal, locality.cpp:7215-7262)."""
+    a = np.array([[a2[0][0], a2[0][1], 0.0], [a2[1][0], a2[1][1], 0.0], [0.0, 0.0, 1.0]])
 
     def cross(x, y, d):
         return (x[1] * y[2] - x[2] * y[1], x[2] * y[0] - x[0] * y[2], x[0] * y[1] - x[1] * y[0])[d]
@@ -191,7 +190,7 @@ def k_grid(geom, n1, n2):
     order (k1 outer, k2 inner): k = (k1/n1) b1 + (k2/n2) b2, with b1, b2 the
     reciprocal vectors of the prepared supercell (Locality::getReciprocal,
     locality.cpp:7215-7262). Returns [n1 * n2][2]."""
-    b = _reciprocal(geom)
+    b = _reciprocal(geom.supercell)
     out = []
     for k1 in range(n1):
         for k2 in range(n2):
@@ -199,25 +198,42 @@ def k_grid(geom, n1, n2):
     return np.array(out)
 
 
-def k_path(geom, n):
-    """Bloch vectors of the supercell zone's path K -> Gamma -> M -> K (K_TYPE = 1,
-    locality.cpp:1655-1797), n points in job order: point i sits at c = 3i/n on the
-    path, K = b2 turned by -30 degrees and divided by 2 cos 30, M = b2 / 2,
-    Gamma = 0. Returns [n][2]."""
-    b = _reciprocal(geom)
-    r = 1.0 / (2.0 * np.cos(np.pi / 6))
-    kk = [r * (np.cos(-np.pi / 6) * b[1][0] - np.sin(-np.pi / 6) * b[1][1]),
-          r * (np.sin(-np.pi / 6) * b[1][0] + np.cos(-np.pi / 6) * b[1][1])]
-    gm, mm = [0.0, 0.0], [b[1][0] / 2.0, b[1][1] / 2.0]
+def k_path(geom, n, k_type=1):
+    """Bloch vectors of a k path, n points in job order, point i at c = 3i/n on it.
+
+    k_type 1 (locality.cpp:1655-1797): the supercell zone, K -> Gamma -> M -> K, with
+    K = b2 turned by -30 degrees over 2 cos 30, M = b2 / 2, b from the supercell.
+    k_type 2 (locality.cpp:1800-1915): sheet 0's own zone, Gamma -> M -> K -> Gamma,
+    with b from sheet 0's lattice turned by its angle (Locality::getReciprocal(int),
+    locality.cpp:7168-7213), M = b1 / 2 and K = M turned by 30 degrees over cos 30.
+    Returns [n][2]."""
+    if k_type == 1:
+        b = _reciprocal(geom.supercell)
+        r = 1.0 / (2.0 * np.cos(np.pi / 6))
+        p0 = [r * (np.cos(-np.pi / 6) * b[1][0] - np.sin(-np.pi / 6) * b[1][1]),
+              r * (np.sin(-np.pi / 6) * b[1][0] + np.cos(-np.pi / 6) * b[1][1])]
+        p1, p2 = [0.0, 0.0], [b[1][0] / 2.0, b[1][1] / 2.0]
+    elif k_type == 2:
+        th = geom.angles[0]
+        lat = geom.lattice[0]
+        a0 = [[lat[i][0] * np.cos(th) - lat[i][1] * np.sin(th), lat[i][0] * np.sin(th) + lat[i][1] * np.cos(th)]
+              for i in range(2)]
+        b = _reciprocal(a0)
+        h = (np.pi / 3.0) / 2.0
+        p1 = [b[0][0] / 2.0, b[0][1] / 2.0]
+        p0 = [0.0, 0.0]
+        p2 = [(p1[0] * np.cos(h) - p1[1] * np.sin(h)) / np.cos(h), (p1[0] * np.sin(h) + p1[1] * np.cos(h)) / np.cos(h)]
+    else:
+        raise ValueError("k_type must be 1 or 2")
     out = []
     for i in range(n):
         c = (3.0 / n) * i
         if c <= 1:
-            out.append([(1.0 - c) * kk[d] + c * gm[d] for d in range(2)])
+            out.append([(1.0 - c) * p0[d] + c * p1[d] for d in range(2)])
         elif c <= 2:
-            out.append([(2.0 - c) * gm[d] + (c - 1.0) * mm[d] for d in range(2)])
+            out.append([(2.0 - c) * p1[d] + (c - 1.0) * p2[d] for d in range(2)])
         else:
-            out.append([(3.0 - c) * mm[d] + (c - 2.0) * kk[d] for d in range(2)])
+            out.append([(3.0 - c) * p2[d] + (c - 2.0) * p0[d] for d in range(2)])
     return np.array(out)
 
 

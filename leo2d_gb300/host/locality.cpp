@@ -187,22 +187,23 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
   // outer, k2 inner; b from Locality::getReciprocal (locality.cpp:7215-7262)
   std::vector<std::array<double, 2>> kjobs;
   if (spec.k_sampling == 1) {
-    const double a[3][3] = {{g0.supercell[0][0], g0.supercell[0][1], 0.0},
-                            {g0.supercell[1][0], g0.supercell[1][1], 0.0},
-                            {0.0, 0.0, 1.0}};
-    auto cross = [](const double* x, const double* y, int d) {
-      return d == 0 ? x[1] * y[2] - x[2] * y[1] : (d == 1 ? x[2] * y[0] - x[0] * y[2] : x[0] * y[1] - x[1] * y[0]);
+    auto reciprocal = [](const double (&a2)[2][2], double (&b)[2][2]) {
+      const double a[3][3] = {{a2[0][0], a2[0][1], 0.0}, {a2[1][0], a2[1][1], 0.0}, {0.0, 0.0, 1.0}};
+      auto cross = [](const double* x, const double* y, int d) {
+        return d == 0 ? x[1] * y[2] - x[2] * y[1] : (d == 1 ? x[2] * y[0] - x[0] * y[2] : x[0] * y[1] - x[1] * y[0]);
+      };
+      double den1 = 0.0, den2 = 0.0;
+      for (int j = 0; j < 3; ++j) {
+        den1 += a[0][j] * cross(a[1], a[2], j);
+        den2 += a[1][j] * cross(a[2], a[0], j);
+      }
+      for (int k = 0; k < 2; ++k) {
+        b[0][k] = 2 * M_PI * cross(a[1], a[2], k) / den1;
+        b[1][k] = 2 * M_PI * cross(a[2], a[0], k) / den2;
+      }
     };
-    double den1 = 0.0, den2 = 0.0;
-    for (int j = 0; j < 3; ++j) {
-      den1 += a[0][j] * cross(a[1], a[2], j);
-      den2 += a[1][j] * cross(a[2], a[0], j);
-    }
     double b[2][2];
-    for (int k = 0; k < 2; ++k) {
-      b[0][k] = 2 * M_PI * cross(a[1], a[2], k) / den1;
-      b[1][k] = 2 * M_PI * cross(a[2], a[0], k) / den2;
-    }
+    reciprocal(g0.supercell, b);
     std::vector<std::vector<double>> shift_jobs = jobs;
     jobs.clear();
     if (spec.k_type == 1) {
@@ -221,6 +222,34 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
           for (int d = 0; d < 2; ++d)
             k[d] = c <= 1 ? (1.0 - c) * kk[d] + (c - 0.0) * gm[d]
                           : (c <= 2 ? (2.0 - c) * gm[d] + (c - 1.0) * mm[d] : (3.0 - c) * mm[d] + (c - 2.0) * kk[d]);
+          jobs.push_back(sj);
+          kjobs.push_back(k);
+        }
+    }
+    if (spec.k_type == 2) {
+      // K_TYPE = 2 (locality.cpp:1800-1915): each job at NUM_K1 points of sheet 0's
+      // own zone, path Gamma -> M -> K -> Gamma; b1 from sheet 0's lattice turned by
+      // its angle (Locality::getReciprocal(int), locality.cpp:7168-7213), M = b1[0] / 2,
+      // K = M turned by phi / 2 over cos(phi / 2) with phi = 60 degrees
+      double a0[2][2], b1[2][2];
+      const double th = g0.angles[0];
+      for (int i = 0; i < 2; ++i) {
+        a0[i][0] = g0.lattice[0][i][0] * std::cos(th) - g0.lattice[0][i][1] * std::sin(th);
+        a0[i][1] = g0.lattice[0][i][0] * std::sin(th) + g0.lattice[0][i][1] * std::cos(th);
+      }
+      reciprocal(a0, b1);
+      const double phi = M_PI / 3.0;
+      const double gm[2] = {0.0, 0.0};
+      const double mm[2] = {b1[0][0] / 2.0, b1[0][1] / 2.0};
+      const double kk[2] = {(mm[0] * std::cos(phi / 2.0) - mm[1] * std::sin(phi / 2.0)) / std::cos(phi / 2.0),
+                            (mm[0] * std::sin(phi / 2.0) + mm[1] * std::cos(phi / 2.0)) / std::cos(phi / 2.0)};
+      for (const auto& sj : shift_jobs)
+        for (int i = 0; i < spec.num_k1; ++i) {
+          const double c = (3.0 / (double)spec.num_k1) * i;
+          std::array<double, 2> k;
+          for (int d = 0; d < 2; ++d)
+            k[d] = c <= 1 ? (1.0 - c) * gm[d] + (c - 0.0) * mm[d]
+                          : (c <= 2 ? (2.0 - c) * mm[d] + (c - 1.0) * kk[d] : (3.0 - c) * kk[d] + (c - 2.0) * gm[d]);
           jobs.push_back(sj);
           kjobs.push_back(k);
         }
