@@ -199,41 +199,51 @@ def k_grid(geom, n1, n2):
 
 
 def k_path(geom, n, k_type=1):
-    """Bloch vectors of a k path, n points in job order, point i at c = 3i/n on it.
+    """Bloch vectors of a k path (locality.cpp:1655-1990), n points in job order.
 
-    k_type 1 (locality.cpp:1655-1797): the supercell zone, K -> Gamma -> M -> K, with
-    K = b2 turned by -30 degrees over 2 cos 30, M = b2 / 2, b from the supercell.
-    k_type 2 (locality.cpp:1800-1915): sheet 0's own zone, Gamma -> M -> K -> Gamma,
-    with b from sheet 0's lattice turned by its angle (Locality::getReciprocal(int),
-    locality.cpp:7168-7213), M = b1 / 2 and K = M turned by 30 degrees over cos 30.
-    Returns [n][2]."""
-    if k_type == 1:
-        b = _reciprocal(geom.supercell)
-        r = 1.0 / (2.0 * np.cos(np.pi / 6))
-        p0 = [r * (np.cos(-np.pi / 6) * b[1][0] - np.sin(-np.pi / 6) * b[1][1]),
-              r * (np.sin(-np.pi / 6) * b[1][0] + np.cos(-np.pi / 6) * b[1][1])]
-        p1, p2 = [0.0, 0.0], [b[1][0] / 2.0, b[1][1] / 2.0]
-    elif k_type == 2:
+    The path runs through corners P_0 .. P_L; point i sits at c = L i / n, on leg j
+    = the first with c <= j + 1 (the last leg takes the rest), at
+    (j+1-c) P_j + (c-j) P_j+1.
+      k_type 1: supercell zone, K -> Gamma -> M -> K
+      k_type 2: sheet 0's own zone, Gamma -> M -> K -> Gamma
+      k_type 3: supercell zone, Gamma -> M -> K -> K' -> Gamma
+    Supercell zone: K = b2 turned by -30 degrees over 2 cos 30, K' = K turned by
+    -60 degrees, M = b2 / 2. Sheet 0's zone: b from its lattice turned by its angle
+    (Locality::getReciprocal(int), locality.cpp:7168-7213), M = b1 / 2, K = M
+    turned by 30 degrees over cos 30. Returns [n][2]."""
+    gm = [0.0, 0.0]
+    if k_type == 2:
         th = geom.angles[0]
         lat = geom.lattice[0]
         a0 = [[lat[i][0] * np.cos(th) - lat[i][1] * np.sin(th), lat[i][0] * np.sin(th) + lat[i][1] * np.cos(th)]
               for i in range(2)]
         b = _reciprocal(a0)
         h = (np.pi / 3.0) / 2.0
-        p1 = [b[0][0] / 2.0, b[0][1] / 2.0]
-        p0 = [0.0, 0.0]
-        p2 = [(p1[0] * np.cos(h) - p1[1] * np.sin(h)) / np.cos(h), (p1[0] * np.sin(h) + p1[1] * np.cos(h)) / np.cos(h)]
+        mm = [b[0][0] / 2.0, b[0][1] / 2.0]
+        kk = [(mm[0] * np.cos(h) - mm[1] * np.sin(h)) / np.cos(h), (mm[0] * np.sin(h) + mm[1] * np.cos(h)) / np.cos(h)]
+        pts = [gm, mm, kk, gm]
+    elif k_type in (1, 3):
+        b = _reciprocal(geom.supercell)
+        r = 1.0 / (2.0 * np.cos(np.pi / 6))
+        kk = [r * (np.cos(-np.pi / 6) * b[1][0] - np.sin(-np.pi / 6) * b[1][1]),
+              r * (np.sin(-np.pi / 6) * b[1][0] + np.cos(-np.pi / 6) * b[1][1])]
+        mm = [b[1][0] / 2.0, b[1][1] / 2.0]
+        if k_type == 1:
+            pts = [kk, gm, mm, kk]
+        else:
+            k2 = [np.cos(-np.pi / 3) * kk[0] - np.sin(-np.pi / 3) * kk[1],
+                  np.sin(-np.pi / 3) * kk[0] + np.cos(-np.pi / 3) * kk[1]]
+            pts = [gm, mm, kk, k2, gm]
     else:
-        raise ValueError("k_type must be 1 or 2")
+        raise ValueError("k_type must be 1, 2 or 3")
+    legs = len(pts) - 1
     out = []
     for i in range(n):
-        c = (3.0 / n) * i
-        if c <= 1:
-            out.append([(1.0 - c) * p0[d] + c * p1[d] for d in range(2)])
-        elif c <= 2:
-            out.append([(2.0 - c) * p1[d] + (c - 1.0) * p2[d] for d in range(2)])
-        else:
-            out.append([(3.0 - c) * p2[d] + (c - 2.0) * p0[d] for d in range(2)])
+        c = (float(legs) / n) * i
+        j = 0
+        while j < legs - 1 and c > j + 1:
+            j += 1
+        out.append([((j + 1.0) - c) * pts[j][d] + (c - j) * pts[j + 1][d] for d in range(2)])
     return np.array(out)
 
 

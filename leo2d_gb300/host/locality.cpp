@@ -206,50 +206,54 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     reciprocal(g0.supercell, b);
     std::vector<std::vector<double>> shift_jobs = jobs;
     jobs.clear();
-    if (spec.k_type == 1) {
-      // K_TYPE = 1 (locality.cpp:1655-1797): each job at NUM_K1 points of the
-      // supercell zone's path K -> Gamma -> M -> K, c = 3i/NUM_K1 the position on
-      // it; K = b2 turned by -30 degrees over 2 cos 30, M = b2 / 2, Gamma = 0
-      const double r = 1.0 / (2.0 * std::cos(M_PI / 6));
-      const double kk[2] = {r * (std::cos(-M_PI / 6) * b[1][0] - std::sin(-M_PI / 6) * b[1][1]),
-                            r * (std::sin(-M_PI / 6) * b[1][0] + std::cos(-M_PI / 6) * b[1][1])};
-      const double gm[2] = {0.0, 0.0};
-      const double mm[2] = {b[1][0] / 2.0, b[1][1] / 2.0};
-      for (const auto& sj : shift_jobs)
-        for (int i = 0; i < spec.num_k1; ++i) {
-          const double c = (3.0 / (double)spec.num_k1) * i;
-          std::array<double, 2> k;
-          for (int d = 0; d < 2; ++d)
-            k[d] = c <= 1 ? (1.0 - c) * kk[d] + (c - 0.0) * gm[d]
-                          : (c <= 2 ? (2.0 - c) * gm[d] + (c - 1.0) * mm[d] : (3.0 - c) * mm[d] + (c - 2.0) * kk[d]);
-          jobs.push_back(sj);
-          kjobs.push_back(k);
+    if (spec.k_type >= 1) {
+      // k paths (locality.cpp:1655-1990): each job at NUM_K1 points of a path through
+      // the corners P_0 .. P_L; point i sits at c = L i / NUM_K1 and on leg j = the
+      // first with c <= j + 1 (the last leg takes the rest), at (j+1-c) P_j + (c-j) P_j+1.
+      //   K_TYPE 1: supercell zone, K -> Gamma -> M -> K
+      //   K_TYPE 2: sheet 0's own zone, Gamma -> M -> K -> Gamma
+      //   K_TYPE 3: supercell zone, Gamma -> M -> K -> K' -> Gamma
+      // Supercell zone: K = b2 turned by -30 degrees over 2 cos 30, K' = K turned by
+      // -60 degrees, M = b2 / 2. Sheet 0's zone: b1 from its lattice turned by its
+      // angle (Locality::getReciprocal(int), locality.cpp:7168-7213), M = b1[0] / 2,
+      // K = M turned by 30 degrees over cos 30.
+      using Pt = std::array<double, 2>;
+      const Pt gm = {0.0, 0.0};
+      std::vector<Pt> pts;
+      if (spec.k_type == 2) {
+        double a0[2][2], b1[2][2];
+        const double th = g0.angles[0];
+        for (int i = 0; i < 2; ++i) {
+          a0[i][0] = g0.lattice[0][i][0] * std::cos(th) - g0.lattice[0][i][1] * std::sin(th);
+          a0[i][1] = g0.lattice[0][i][0] * std::sin(th) + g0.lattice[0][i][1] * std::cos(th);
         }
-    }
-    if (spec.k_type == 2) {
-      // K_TYPE = 2 (locality.cpp:1800-1915): each job at NUM_K1 points of sheet 0's
-      // own zone, path Gamma -> M -> K -> Gamma; b1 from sheet 0's lattice turned by
-      // its angle (Locality::getReciprocal(int), locality.cpp:7168-7213), M = b1[0] / 2,
-      // K = M turned by phi / 2 over cos(phi / 2) with phi = 60 degrees
-      double a0[2][2], b1[2][2];
-      const double th = g0.angles[0];
-      for (int i = 0; i < 2; ++i) {
-        a0[i][0] = g0.lattice[0][i][0] * std::cos(th) - g0.lattice[0][i][1] * std::sin(th);
-        a0[i][1] = g0.lattice[0][i][0] * std::sin(th) + g0.lattice[0][i][1] * std::cos(th);
+        reciprocal(a0, b1);
+        const double h = (M_PI / 3.0) / 2.0;
+        const Pt mm = {b1[0][0] / 2.0, b1[0][1] / 2.0};
+        const Pt kk = {(mm[0] * std::cos(h) - mm[1] * std::sin(h)) / std::cos(h),
+                       (mm[0] * std::sin(h) + mm[1] * std::cos(h)) / std::cos(h)};
+        pts = {gm, mm, kk, gm};
+      } else {
+        const double r = 1.0 / (2.0 * std::cos(M_PI / 6));
+        const Pt kk = {r * (std::cos(-M_PI / 6) * b[1][0] - std::sin(-M_PI / 6) * b[1][1]),
+                       r * (std::sin(-M_PI / 6) * b[1][0] + std::cos(-M_PI / 6) * b[1][1])};
+        const Pt mm = {b[1][0] / 2.0, b[1][1] / 2.0};
+        if (spec.k_type == 1) {
+          pts = {kk, gm, mm, kk};
+        } else {
+          const Pt k2 = {std::cos(-M_PI / 3) * kk[0] - std::sin(-M_PI / 3) * kk[1],
+                         std::sin(-M_PI / 3) * kk[0] + std::cos(-M_PI / 3) * kk[1]};
+          pts = {gm, mm, kk, k2, gm};
+        }
       }
-      reciprocal(a0, b1);
-      const double phi = M_PI / 3.0;
-      const double gm[2] = {0.0, 0.0};
-      const double mm[2] = {b1[0][0] / 2.0, b1[0][1] / 2.0};
-      const double kk[2] = {(mm[0] * std::cos(phi / 2.0) - mm[1] * std::sin(phi / 2.0)) / std::cos(phi / 2.0),
-                            (mm[0] * std::sin(phi / 2.0) + mm[1] * std::cos(phi / 2.0)) / std::cos(phi / 2.0)};
+      const int legs = (int)pts.size() - 1;
       for (const auto& sj : shift_jobs)
         for (int i = 0; i < spec.num_k1; ++i) {
-          const double c = (3.0 / (double)spec.num_k1) * i;
-          std::array<double, 2> k;
-          for (int d = 0; d < 2; ++d)
-            k[d] = c <= 1 ? (1.0 - c) * gm[d] + (c - 0.0) * mm[d]
-                          : (c <= 2 ? (2.0 - c) * mm[d] + (c - 1.0) * kk[d] : (3.0 - c) * kk[d] + (c - 2.0) * gm[d]);
+          const double c = ((double)legs / (double)spec.num_k1) * i;
+          int j = 0;
+          while (j < legs - 1 && c > j + 1) ++j;
+          Pt k;
+          for (int d = 0; d < 2; ++d) k[d] = ((j + 1.0) - c) * pts[j][d] + (c - j) * pts[j + 1][d];
           jobs.push_back(sj);
           kjobs.push_back(k);
         }

@@ -96,8 +96,8 @@ def test_unsupported_input_is_refused(tmp_path):
         "POLY_ORDER = 64", "POLY_ORDER = 62"))
     with pytest.raises(L.Leo2dError, match="divisible 4"):
         L.run_input(p, tmp_path)
-    # the k lists of K_TYPE 2-5 (monolayer and trilayer zone paths) are not built
+    # the k lists of K_TYPE 4 and 5 (trilayer Dirac-point paths) are not built
     p.write_text(open(os.path.join(GOLDEN, "inputs", "sc32_ksamp_path_ldos.in")).read().replace(
-        "K_TYPE = 1", "K_TYPE = 3"))
-    with pytest.raises(L.Leo2dError, match="K_TYPE = 3"):
+        "K_TYPE = 1", "K_TYPE = 4"))
+    with pytest.raises(L.Leo2dError, match="K_TYPE = 4"):
         L.run_input(p, tmp_path)

@@ -40,12 +40,14 @@ def _kpts_text(ks):
 
 def test_k_lists_match_the_reference_kpts_files():
     """The k points the reference's own main() wrote for a K_TYPE = 0 grid (2 x 2),
-    a K_TYPE = 1 path (6 points, every leg of K -> Gamma -> M -> K) and a K_TYPE = 2
-    path (5 points of sheet 0's zone, Gamma -> M -> K -> Gamma)."""
+    a K_TYPE = 1 path (6 points, every leg of K -> Gamma -> M -> K), a K_TYPE = 2
+    path (5 points of sheet 0's zone, Gamma -> M -> K -> Gamma) and a K_TYPE = 3
+    path (7 points, Gamma -> M -> K -> K' -> Gamma)."""
     from tests._golden import e2e_text, parse_in
     for name, ks in (("sc32_ksamp_ldos", lambda g: L.k_grid(g, 2, 2)),
                      ("sc32_ksamp_path_ldos", lambda g: L.k_path(g, 6)),
-                     ("sc32_ksamp_mono_ldos", lambda g: L.k_path(g, 5, k_type=2))):
+                     ("sc32_ksamp_mono_ldos", lambda g: L.k_path(g, 5, k_type=2)),
+                     ("sc32_ksamp_loop_ldos", lambda g: L.k_path(g, 7, k_type=3))):
         g, _ = parse_in(name)
         g = oracle.geom_prepare(g)
         assert _kpts_text(ks(g)) == e2e_text(name, ".kpts"), name
