@@ -209,7 +209,7 @@ def kernel_case(args):
         print(json.dumps({"kernel_case": {"n": csr.n, "nnz": csr.nnz, "cols": args.kernel_case,
                                           "step_kernel": args.step_kernel, "radius_A": radius,
                                           "step_kernel_run": csr.step_kernel(cfg)[0],
-                                          "rb_info": list(csr.rb_info()),
+                                          "rb_info": list(csr.rb_info()), "rt_info": list(csr.rt_info()),
                                           "step_ms": round(ms / k, 4), "step_gbs": round(gbs, 1)}}))
 
 
@@ -691,9 +691,9 @@ def main():
                          "sigma_xx(E) of a 2M-orbital 1.5 deg flake, 512x512 moments, 32 vectors; mlp: the "
                          "control variate's network (training steps, inference over the flake of --radius); "
                          "bfield: the flake of --radius in a 20 T field (complex Hamiltonian)")
-    ap.add_argument("--step-kernel", type=int, default=-1, choices=[-1, 0, 1, 2, 3],
+    ap.add_argument("--step-kernel", type=int, default=-1, choices=[-1, 0, 1, 2, 3, 5],
                     help="force the Chebyshev step kernel: 0 tiled gathers, 1 register gathers, 2 tensor cores, "
-                         "3 row blocks (default: the autotuner's choice)")
+                         "3 row blocks, 5 row blocks of 8 on the tensor cores (default: the autotuner's choice)")
     ap.add_argument("--kernel-case", type=int, default=0, metavar="COLS",
                     help="profiling case: two short DOS runs (P=16) of COLS-wide vector blocks on the flake "
                          "of --radius (1000 A: 2.4M orbitals), then exit; prints no bench line")
@@ -766,7 +766,8 @@ def main():
     kernel_id, _ = csr.step_kernel(cfg)
     kernel_name = {0: "k_cheb_tile (tiled CSR gathers)", 1: "k_cheb_step (register gathers)",
                    2: "k_cheb_tc (tensor cores)", 3: "k_cheb_rb (row blocks)",
-                   4: "k_cheb_rbw (row blocks, shared-memory windows)"}[kernel_id]
+                   4: "k_cheb_rbw (row blocks, shared-memory windows)",
+                   5: "k_cheb_rt (8-row blocks, tensor cores)"}[kernel_id]
 
     import torch
     torch.cuda.set_device(local)

@@ -126,11 +126,22 @@ leo2d_status leo2d_ctx_kernel_stats(leo2d_ctx* ctx, const char* kernel,
 leo2d_status leo2d_ctx_reset_stats(leo2d_ctx* ctx);
 /* Total kernel launches made through this context since creation. */
 int64_t leo2d_ctx_launch_count(const leo2d_ctx* ctx);
-/* Tuning switches of a context. Keys: "step_kernel" (0 = shared-memory tiles
- * filled by bulk copies, the default; 1 = register streaming of the matrix),
+/* Tuning switches of a context. Keys: "step_kernel" (-1 = autotuned or the
+ * default for the matrix; 0 = shared-memory tiles filled by bulk copies;
+ * 1 = register streaming of the matrix; 2 = tensor-core tiles; 3 = row blocks of
+ * 4 rows; 5 = row blocks of 8 rows on the tensor cores),
  * "tile_stages" (2..4 shared-memory stages of the tiled kernel, default 2),
- * "tile_chunk" (1..64 consecutive row tiles per block between grid-wide
- * jumps, default 4), "tile_warps" (8 or 24 warps per block of the tiled
+ * "tile_chunk" (1..65536 consecutive row tiles per block between grid-wide
+ * jumps, default 4), "rt_warps" / "rt_depth" / "rt_group" / "rt_chunk" (the
+ * 8-row tensor-core step: warps per CTA 8, 12, 16 or 24; k-steps of T_n rows in
+ * flight per warp 3, 4 or 6; blocks per warp run 1..16, default 2; tiles per
+ * CTA between grid-wide jumps 1..64, default 2; 0 = autotuned or default),
+ * "alloc_cap_mb" (the largest single device allocation a call on this context
+ * may make, in MiB; a larger one fails with LEO2D_ERR_OOM and a message naming
+ * its size; 0 = no limit, the default),
+ * "reorder_curve" (1 = inside each patch of the locality ordering, orbitals go
+ * by sheet and along a Hilbert curve of 1/32-patch cells, the default; 0 = by
+ * the reference index), "tile_warps" (8 or 24 warps per block of the tiled
  * kernel; 0 = chosen per block width, the default), "reorder" (locality ordering of the streamed matrix:
  * -1 = automatic for >= 1e5 orbitals with positions, 0 = off, 1 = on),
  * "reorder_patch_dA" (patch edge of that ordering in tenths of A, default 160),
@@ -250,7 +261,8 @@ leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2
                                 int32_t* block_out, int32_t* rows_out);
 /* The step kernel a leo2d_kpm_dos call with this cfg would run on this matrix:
  * *kernel = 0 tiled CSR gathers, 1 register-streaming gathers, 2 tensor cores,
- * 3 row blocks, 4 row blocks over shared-memory windows; *block = the
+ * 3 row blocks, 4 row blocks over shared-memory windows, 5 row blocks of 8 rows
+ * on the tensor cores; *block = the
  * vector-block width in columns. Builds nothing and
  * launches nothing. No counterpart in the reference. */
 leo2d_status leo2d_kpm_step_kernel(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg,
@@ -314,15 +326,25 @@ leo2d_status leo2d_tc_gemm(leo2d_ctx* ctx, const uint16_t* a, const uint16_t* b,
 leo2d_status leo2d_csr_tc_info(const leo2d_csr* csr, int64_t* tiles, double* mean_window, int32_t* max_window,
                                int32_t* max_tile_entries);
 /* Row blocks of the locality-ordered copy (built by the first recursion that
- * runs the row-block step, step_kernel = 3 or autotuned): blocks of 8 rows
- * stored as the sorted union of their rows' columns with a dense 8 x slots
- * panel of FP32 values, so that one gathered T_n row serves 8 rows. Reports the
+ * runs the row-block step, step_kernel = 3 or autotuned): blocks of 4 rows
+ * stored as the sorted union of their rows' columns with a dense 4 x slots
+ * panel of FP32 values, so that one gathered T_n row serves 4 rows. Reports the
  * row-block count, slots stored (padded to multiples of 4 per block), distinct
  * slots before padding, the most slots of one block and the largest tile of 16
  * blocks in bytes; zeros when not built. Replaces, for the recursion only, the
  * CSR stream of SpMatrix::vectorMultiply (src/matrix/spmatrix.cpp:346-360). */
 leo2d_status leo2d_csr_rb_info(const leo2d_csr* csr, int64_t* row_blocks, int64_t* slots, int64_t* union_slots,
                                int32_t* max_slots, int64_t* max_tile_bytes);
+/* Blocks of 8 rows of the tensor-core step (built by the first recursion that
+ * runs it, step_kernel = 5 or autotuned): each block's slots are the sorted
+ * union of its rows' columns in k-steps of 8 (288 bytes: 8 columns and the
+ * 8 x 8 FP32 value panel in MMA fragment order), stored in the order one launch
+ * shape processes them. Reports the block count, k-steps stored, distinct slots
+ * before padding and the most slots of one block; zeros when not built.
+ * Replaces, for the recursion only, the CSR stream of SpMatrix::vectorMultiply
+ * (src/matrix/spmatrix.cpp:346-360). */
+leo2d_status leo2d_csr_rt_info(const leo2d_csr* csr, int64_t* row_blocks, int64_t* ksteps, int64_t* union_slots,
+                               int32_t* max_slots);
 leo2d_status leo2d_tc_gemm_tf32x3(leo2d_ctx* ctx, const float* a, const float* b, int64_t N, int64_t K, float* d);
 
 /* ---------------------------------------------------------------- learned control variate */

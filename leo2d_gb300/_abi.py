@@ -151,6 +151,7 @@ def _declare(lib):
     fn("leo2d_tc_gemm_tf32x3", c_i32, c_void_p, P, P, c_i64, c_i64, P)
     fn("leo2d_csr_tc_info", c_i32, c_void_p, P, P, P, P)
     fn("leo2d_csr_rb_info", c_i32, c_void_p, P, P, P, P, P)
+    fn("leo2d_csr_rt_info", c_i32, c_void_p, P, P, P, P)
     fn("leo2d_csr_download_imag", c_i32, c_void_p, c_void_p, P)
     fn("leo2d_csr_remove_orbitals", c_i32, c_void_p, c_void_p, P, c_i64, pp)
     fn("leo2d_mlp_param_count", c_i64)

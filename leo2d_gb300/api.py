@@ -212,6 +212,8 @@ def k_path(geom, n, k_type=1):
     (Locality::getReciprocal(int), locality.cpp:7168-7213), M = b1 / 2, K = M
     turned by 30 degrees over cos 30. Returns [n][2]."""
     gm = [0.0, 0.0]
+    if k_type == 1 and geom.num_sheets < 2:  # locality.cpp:1661-1663, as the driver
+        raise ValueError("cannot use K_TYPE == 1 (twisted BZ) for a single layer")
     if k_type == 2:
         th = geom.angles[0]
         lat = geom.lattice[0]
@@ -341,6 +343,13 @@ class Csr:
         self.ctx.check(self.ctx.lib.leo2d_csr_rb_info(self.h, ctypes.byref(b), ctypes.byref(s), ctypes.byref(u),
                                                       ctypes.byref(ms), ctypes.byref(mt)))
         return b.value, s.value, u.value, ms.value, mt.value
+
+    def rt_info(self):
+        """8-row blocks of the tensor-core step: (blocks, k-steps stored, distinct slots, most slots of a block)."""
+        b, k, u, ms = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int32()
+        self.ctx.check(self.ctx.lib.leo2d_csr_rt_info(self.h, ctypes.byref(b), ctypes.byref(k), ctypes.byref(u),
+                                                      ctypes.byref(ms)))
+        return b.value, k.value, u.value, ms.value
 
     def bounds(self):
         lo, hi = ctypes.c_double(), ctypes.c_double()

@@ -412,8 +412,9 @@ leo2d_status leo2d_batch_create(leo2d_ctx* ctx, const leo2d_csr* const* csrs, in
       LEO_REQUIRE(m->ent.p != nullptr || m->nnz == 0, "matrix has no FP32 values");
       const bool perm = m->pos.p != nullptr && m->nnz > 0 &&
                         (ctx->reorder == 1 || (ctx->reorder == -1 && m->n >= 100000));
-      if (perm && (!m->reordered || m->reorder_patch != reorder_patch_for(ctx, false)))
-        csr_build_reordered(ctx, mm, reorder_patch_for(ctx, false), m->reorder_fp64);
+      if (perm && (!m->reordered || m->reorder_patch != reorder_patch_for(ctx, false) ||
+                   m->reorder_curve_req != ctx->reorder_curve))
+        csr_build_reordered(ctx, mm, reorder_patch_for(ctx, false), m->reorder_fp64, ctx->reorder_curve != 0);
       FlakeView v;
       v.csr = m;
       v.n = m->n;

@@ -41,6 +41,11 @@ struct Error : std::exception {
     if (!(cond)) ::leo2d::fail(LEO2D_ERR_BAD_ARG, msg); \
   } while (0)
 
+// Largest single device allocation the calling context allows, in bytes (0: no
+// limit): the context's "alloc_cap_mb" option, in force for the duration of one
+// API call (guard() sets it for the calling thread).
+inline thread_local size_t g_alloc_cap = 0;
+
 // Owning device allocation (move-only).
 template <class T>
 struct DevBuf {
@@ -59,6 +64,9 @@ struct DevBuf {
   void alloc(size_t count) {
     release();
     if (count == 0) return;
+    if (g_alloc_cap && count * sizeof(T) > g_alloc_cap)
+      fail(LEO2D_ERR_OOM, "device allocation of " + std::to_string(count * sizeof(T)) +
+                              " bytes exceeds the context's alloc_cap_mb");
     LEO_CUDA(cudaMalloc(&p, count * sizeof(T)));
     n = count;
   }
@@ -98,11 +106,18 @@ struct leo2d_ctx {
   std::vector<leo2d::PendingTimer> pending;
   std::vector<cudaEvent_t> free_events;
   int64_t launches = 0;
-  int kernel_variant = -1;    // -1 autotuned, 0 tiled gathers, 1 register gathers, 2 tensor cores, 3 row blocks
+  int kernel_variant = -1;    // -1 autotuned, 0 tiled gathers, 1 register gathers, 2 tensor cores, 3 row blocks,
+                              // 5 row blocks of 8 on the tensor cores
   int rb_packed = -1;         // row-block step: paired FP32 FMAs (fma.rn.f32x2): -1 autotuned, 0 no, 1 yes
   int rb_warps = 0;           // row-block step: warps per block (= row blocks per tile): 0 autotuned, 16, 24, 32
   int rb_unroll = 0;          // row-block step: slot batches in flight per lane: 0 autotuned, 4, 8
   int rb_window = -1;         // row-block step over shared-memory windows: -1 autotuned, 0 no, 1 yes
+  int rt_warps = 0;           // 8-row tensor-core step: warps per CTA: 0 autotuned, 8, 12, 16, 24
+  int rt_depth = 0;           // 8-row tensor-core step: k-steps of T_n rows in flight per warp: 0 autotuned, 2, 3, 4, 6
+  int rt_stage = -1;          // 8-row tensor-core step: T_n rows staged in -1 autotuned, 0 registers, 1 shared memory
+  int rt_group = 0;           // 8-row tensor-core step: consecutive blocks per warp run: 0 default (2), 1..16
+  int rt_chunk = 0;           // 8-row tensor-core step: tiles per CTA between grid-wide jumps: 0 default (2)
+  int reorder_curve = 1;      // locality ordering inside a patch: 1 sheet then a fine Hilbert curve, 0 reference index
   int tile_stages = 2;        // shared-memory stages of the tiled kernel
   int test_unsatisfied_wait = 0;  // test hook: tiled steps first wait on a barrier nobody completes
   bool tc_gemm_ready = false;     // shared-memory attributes of the tensor-core GEMM set on this device
@@ -110,6 +125,7 @@ struct leo2d_ctx {
   int tile_warps = 0;         // warps per block of the tiled kernel (0 = per shape, 8 or 24)
   int reorder = -1;           // locality ordering: -1 auto, 0 off, 1 on
   double reorder_patch = 0.0;   // patch edge (A); 0: the step kernel's own (16 A; 32 A for row blocks)
+  size_t alloc_cap = 0;       // largest single device allocation of a call, bytes (0: no limit)
   int kubo_velocity = -1;     // Kubo trace: -1 D built in the row-block step where possible, 0 stored dxH
   int64_t kubo_chunk = 0;     // Kubo trace: B-side moments held at once (0: as many as memory allows)
   leo2d::DevBuf<int> status;  // one int, reset before kernels that may set it
@@ -120,6 +136,11 @@ namespace leo2d {
 // Runs f, converting exceptions into a status and the context's last error.
 template <class F>
 leo2d_status guard(leo2d_ctx* ctx, F&& f) {
+  struct CapScope {  // the context's allocation cap for this call, restored on exit
+    size_t saved;
+    explicit CapScope(size_t cap) : saved(g_alloc_cap) { g_alloc_cap = cap; }
+    ~CapScope() { g_alloc_cap = saved; }
+  } cap_scope(ctx ? ctx->alloc_cap : g_alloc_cap);
   try {
     f();
     if (ctx) ctx->last_error.clear();

@@ -283,8 +283,9 @@ leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value
   return guard(ctx, [&] {
     const std::string k(key);
     if (k == "step_kernel") {
-      LEO_REQUIRE(value >= -1 && value <= 3,
-                  "step_kernel must be -1 (autotuned), 0 (tiled), 1 (register), 2 (tensor cores) or 3 (row blocks)");
+      LEO_REQUIRE(value >= -1 && value <= 5 && value != 4,
+                  "step_kernel must be -1 (autotuned), 0 (tiled), 1 (register), 2 (tensor cores), 3 (row blocks) "
+                  "or 5 (row blocks of 8 on the tensor cores)");
       ctx->kernel_variant = (int)value;
     } else if (k == "rb_packed") {
       LEO_REQUIRE(value >= -1 && value <= 1, "rb_packed must be -1 (autotuned), 0 or 1");
@@ -295,6 +296,29 @@ leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value
     } else if (k == "rb_window") {
       LEO_REQUIRE(value >= -1 && value <= 1, "rb_window must be -1 (autotuned), 0 or 1");
       ctx->rb_window = (int)value;
+    } else if (k == "rt_warps") {
+      LEO_REQUIRE(value == 0 || value == 8 || value == 12 || value == 16 || value == 24,
+                  "rt_warps must be 0 (autotuned), 8, 12, 16 or 24");
+      ctx->rt_warps = (int)value;
+    } else if (k == "rt_depth") {
+      LEO_REQUIRE(value == 0 || value == 2 || value == 3 || value == 4 || value == 6,
+                  "rt_depth must be 0 (autotuned), 2, 3, 4 or 6");
+      ctx->rt_depth = (int)value;
+    } else if (k == "rt_stage") {
+      LEO_REQUIRE(value >= -1 && value <= 1, "rt_stage must be -1 (autotuned), 0 (registers) or 1 (shared memory)");
+      ctx->rt_stage = (int)value;
+    } else if (k == "rt_group") {
+      LEO_REQUIRE(value >= 0 && value <= 16, "rt_group must be 0 (default) or 1..16");
+      ctx->rt_group = (int)value;
+    } else if (k == "rt_chunk") {
+      LEO_REQUIRE(value >= 0 && value <= 64, "rt_chunk must be 0 (default) or 1..64");
+      ctx->rt_chunk = (int)value;
+    } else if (k == "alloc_cap_mb") {
+      LEO_REQUIRE(value >= 0, "alloc_cap_mb must be >= 0 (0: no limit)");
+      ctx->alloc_cap = (size_t)value << 20;
+    } else if (k == "reorder_curve") {
+      LEO_REQUIRE(value == 0 || value == 1, "reorder_curve must be 0 or 1");
+      ctx->reorder_curve = (int)value;
     } else if (k == "rb_unroll") {
       LEO_REQUIRE(value == 0 || value == 4 || value == 8, "rb_unroll must be 0 (autotuned), 4 or 8");
       ctx->rb_unroll = (int)value;
@@ -307,7 +331,7 @@ leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value
       LEO_REQUIRE(value >= 2 && value <= 4, "tile_stages must be 2..4");
       ctx->tile_stages = (int)value;
     } else if (k == "tile_chunk") {
-      LEO_REQUIRE(value >= 1 && value <= 64, "tile_chunk must be 1..64");
+      LEO_REQUIRE(value >= 1 && value <= 65536, "tile_chunk must be 1..65536");
       ctx->tile_chunk = (int)value;
     } else if (k == "tile_warps") {
       LEO_REQUIRE(value == 0 || value == 8 || value == 24, "tile_warps must be 0, 8 or 24");

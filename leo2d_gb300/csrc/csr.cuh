@@ -39,6 +39,8 @@ struct leo2d_csr {
   bool reordered = false;
   bool reorder_fp64 = false;
   double reorder_patch = 0.0;
+  int reorder_curve = 0;          // 1: patch, sheet, then a fine Hilbert curve inside the patch
+  int reorder_curve_req = -1;     // the curve setting the copy was built for (may fall back to 0)
   leo2d::DevBuf<int32_t> new2old, old2new;
   leo2d::DevBuf<int64_t> prow;
   leo2d::DevBuf<int32_t> pcol;
@@ -78,6 +80,22 @@ struct leo2d_csr {
   bool rb_xs_built = false;           // positions for the velocity step (Kubo)
   leo2d::DevBuf<float> rb_xrel;       // [blocks][4] x of each row minus x of its block's first row
   leo2d::DevBuf<float> rb_xs;         // [slots] x of the slot's column minus the same
+  // row blocks of 8 rows for the tensor-core step (rt_spmm.cu): the union of
+  // each block's columns in k-steps of 8 slots, stored in the processing order
+  // of one launch shape (warps, group, chunk, grid)
+  bool rt_counted = false;            // rt_kst holds the k-steps of every block
+  bool rt_built = false;
+  double rt_patch = 0.0;              // ordering the blocks were built from
+  int rt_curve = -1;
+  int64_t rt_blocks = 0;
+  int64_t rt_ksteps = 0;              // k-steps stored
+  int64_t rt_union = 0;               // slots before padding
+  int rt_max_slots = 0;
+  int rt_warps = 0, rt_group = 0, rt_chunk = 0;
+  unsigned rt_grid = 0;
+  leo2d::DevBuf<int64_t> rt_kst;      // [blocks] k-steps of each block
+  leo2d::DevBuf<int64_t> rt_wbeg;     // [grid * warps + 1] first k-step of each warp
+  leo2d::DevBuf<unsigned char> rt_data;  // 288 bytes per k-step
   // shared-memory windows of the row blocks (rbw_spmm.cu): per tile of 16 blocks
   // the sorted distinct columns of its slots; slots hold window positions
   bool rbw_built = false;
@@ -98,8 +116,10 @@ void csr_refresh_fp32(leo2d_ctx* ctx, leo2d_csr* csr);
 // Allocates rowptr (n+1), col and val64 (nnz) with zeroed kCsrPad padding.
 void csr_alloc_rowptr(leo2d_ctx* ctx, leo2d_csr* csr, int64_t n);
 void csr_alloc_entries(leo2d_ctx* ctx, leo2d_csr* csr, int64_t nnz, bool with_dx);
-// Builds / drops the locality-ordered copy (patch = real-space patch edge, A).
-void csr_build_reordered(leo2d_ctx* ctx, leo2d_csr* csr, double patch, bool with_fp64);
+// Builds / drops the locality-ordered copy (patch = real-space patch edge, A;
+// curve: inside a patch by sheet, then along a Hilbert curve of 1/32-patch
+// cells, else by the reference index).
+void csr_build_reordered(leo2d_ctx* ctx, leo2d_csr* csr, double patch, bool with_fp64, bool curve = false);
 // Per-orbital disregistry (Hstruct::getShiftConfigs) into device memory out[n][2]; bilayers.
 void csr_shift_configs(leo2d_ctx* ctx, const leo2d_csr* csr, double* out);
 void csr_drop_reordered(leo2d_csr* csr);
@@ -118,6 +138,10 @@ void csr_drop_rb(leo2d_csr* csr);
 void csr_build_rb_xs(leo2d_ctx* ctx, leo2d_csr* csr);
 // Largest data bytes of a tile of `tile` consecutive row blocks.
 int64_t rb_tile_max_bytes(leo2d_ctx* ctx, const leo2d_csr* csr, int tile);
+// Builds the 8-row blocks of the tensor-core step for one launch shape; returns
+// false (and builds nothing) when a block holds more than 2048 stored entries.
+bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chunk);
+void csr_drop_rt(leo2d_csr* csr);
 // Builds the shared-memory windows of the row blocks; returns false (and builds
 // nothing) when a tile of 16 blocks has more than 8192 slots or 2048 distinct columns.
 bool csr_build_rbw(leo2d_ctx* ctx, leo2d_csr* csr);

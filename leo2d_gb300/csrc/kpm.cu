@@ -213,6 +213,11 @@ void enqueue_steps(Recursion& r) {
                        a.prev_partials, a.prev_dots);
         continue;
       }
+      if (r.shape.rt) {
+        rt_launch_step(ctx, r.csr, r.shape, r.grid, r.dyn_smem, a.tn, a.tp, nullptr, a.first, 0.0f, a.partials,
+                       a.prev_partials, a.prev_dots);
+        continue;
+      }
       if (r.shape.rb && r.shape.rb_window) {
         rbw_launch_step(ctx, r.csr, r.shape, r.grid, r.dyn_smem, a.tn, a.tp, nullptr, a.first, 0.0f, a.partials,
                         a.prev_partials, a.prev_dots);
@@ -257,6 +262,9 @@ struct Tuned {
   int rb_warps = 0, rb_unroll = 0;
   bool rb_packed = true;
   bool rb_window = false;
+  bool rt = false;  // the 8-row tensor-core step won for this block width
+  int rt_warps = 0, rt_depth = 0;
+  bool rt_regs = true;
 };
 std::map<std::pair<leo2d_ctx*, ShapeKey>, Tuned> g_shape_cache;
 // best block width per (context, matrix, precision, columns requested)
@@ -281,12 +289,15 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
     LEO_REQUIRE(shape.rb && can_perm && !s.fp64 && s.cols == 32 && ctx->reorder != 0,
                 "a complex Hamiltonian needs the row-block step (FP32, 32 columns, locality ordering on)");
   if (shape.rb && (!can_perm || s.fp64 || s.cols != 32 || ctx->reorder == 0)) shape.rb = false;
-  if (shape.rb) shape.tc = false;
-  const bool want_perm = can_perm && (shape.tc || shape.rb || ctx->reorder == 1 ||
+  if (shape.rt && (!can_perm || s.fp64 || s.cols != 32 || ctx->reorder == 0 || m->complex_h)) shape.rt = false;
+  if (shape.rt) shape.rb = false;
+  if (shape.rb || shape.rt) shape.tc = false;
+  const bool want_perm = can_perm && (shape.tc || shape.rb || shape.rt || ctx->reorder == 1 ||
                                       (ctx->reorder == -1 && n >= 100000));
-  const double patch = reorder_patch_for(ctx, shape.rb);
-  if (want_perm && (!m->reordered || (s.fp64 && !m->reorder_fp64) || m->reorder_patch != patch))
-    csr_build_reordered(ctx, mm, patch, s.fp64 || m->reorder_fp64);
+  const double patch = reorder_patch_for(ctx, shape.rb || shape.rt);
+  if (want_perm && (!m->reordered || (s.fp64 && !m->reorder_fp64) || m->reorder_patch != patch ||
+                    m->reorder_curve_req != ctx->reorder_curve))
+    csr_build_reordered(ctx, mm, patch, s.fp64 || m->reorder_fp64, ctx->reorder_curve != 0);
   use_perm = want_perm;
   if (shape.tc) {
     // tensor-core tiles of the locality-ordered copy (built once per matrix)
@@ -324,7 +335,19 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
       shape.rb = false;  // blocks too wide for the row-block step: the gather kernels run
     }
   }
-  if (shape.tiled && !shape.tc && !shape.rb) {
+  if (shape.rt) {
+    // 8-row blocks of the locality-ordered copy, stored for this launch shape
+    const int w = shape.rt_warps;
+    const bool fits = rt_smem_bytes(w, shape.rt_depth, shape.rt_regs) + 8 * 1024 <= ctx->smem_optin;
+    if (fits && csr_build_rt(ctx, mm, w, rt_group_of(ctx), rt_chunk_of(ctx))) {
+      dyn_smem = rt_smem_bytes(w, shape.rt_depth, shape.rt_regs);
+      grid = m->rt_grid;
+      shape.tiled = false;
+    } else {
+      shape.rt = false;  // a block too heavy for the 8-row build: the gather kernels run
+    }
+  }
+  if (shape.tiled && !shape.tc && !shape.rb && !shape.rt) {
     const int ns = tile_slots(s.cols, s.fp64, s.warps);
     const int ri = s.rows_per_item > 0 ? s.rows_per_item : std::max(1, 32 / ns);
     tile_rows = ns * ri;
@@ -372,7 +395,7 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
       grid = (unsigned)g;
     }
   }
-  if (!shape.tiled && !shape.tc && !shape.rb) {
+  if (!shape.tiled && !shape.tc && !shape.rb && !shape.rt) {
     if (shape.rows_per_item <= 0) shape.rows_per_item = 4;
     const int occ = std::max(1, occupancy(s.cols, s.fp64));
     const int lpr = s.cols <= 32 ? s.cols : 32;  // lanes per row slot
@@ -394,7 +417,8 @@ template <typename T>
 void one_step(Recursion& r, const void* in, void* out, const void* prev, bool first, double alpha, int matrix) {
   leo2d_ctx* ctx = r.ctx;
   const int C = r.shape.cols;
-  LEO_REQUIRE(!r.use_perm && !r.shape.tc && !r.shape.rb, "a recursion over dxH needs the unpermuted matrix");
+  LEO_REQUIRE(!r.use_perm && !r.shape.tc && !r.shape.rb && !r.shape.rt,
+              "a recursion over dxH needs the unpermuted matrix");
   StepArgs<T> a;
   a.n = r.n;
   a.rowptr = r.csr->rowptr.p;
@@ -478,7 +502,11 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
   const bool cached = it != g_shape_cache.end();
   if (ctx->kernel_variant == 3) s.rb = rb_ok;
   else if (ctx->kernel_variant == -1) s.rb = rb_ok && (cached ? it->second.rb : (ctx->reorder == 1 || csr->n >= 100000));
-  if (s.rb) s.tc = false;
+  const bool rt_ok = rb_ok && !csr->complex_h;
+  if (ctx->kernel_variant == 5) s.rt = rt_ok;
+  else if (ctx->kernel_variant == -1) s.rt = rt_ok && cached && it->second.rt;
+  if (s.rt) s.rb = false;
+  if (s.rb || s.rt) s.tc = false;
   if (csr->complex_h) {
     // a complex H runs on the row-block step only: 16 complex vectors (32 columns), FP32
     LEO_REQUIRE(!fp64, "a complex Hamiltonian (magnetic field) runs in FP32");
@@ -496,6 +524,10 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
     s.rb_window = false;
     s.rb_warps = 24;
   }
+  s.rt_warps = ctx->rt_warps > 0 ? ctx->rt_warps : (cached && it->second.rt_warps > 0 ? it->second.rt_warps : 16);
+  s.rt_regs = ctx->rt_stage >= 0 ? ctx->rt_stage == 0 : (cached && it->second.rt ? it->second.rt_regs : true);
+  s.rt_depth = ctx->rt_depth > 0 ? ctx->rt_depth
+                                 : (cached && it->second.rt_depth > 0 ? it->second.rt_depth : (s.rt_regs ? 3 : 4));
   LEO_REQUIRE(s.rows_per_item >= 0 && s.rows_per_item <= 64, "rows_per_warp must be 0..64");
   return s;
 }
@@ -709,6 +741,7 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
           sh.warps = warps;
           sh.tc = false;
           sh.rb = false;
+          sh.rt = false;
           Recursion r;
           r.setup(ctx, csr, sh, steps);
           fill_phase(ctx, r, 1, 0, cols / 2);
@@ -731,6 +764,7 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
         StepShape sh = choose_shape(ctx, csr, fp64, cols, cols, 0);
         sh.tc = true;
         sh.rb = false;
+        sh.rt = false;
         Recursion r;
         r.setup(ctx, csr, sh, steps);
         if (r.shape.tc) {
@@ -760,6 +794,7 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
           StepShape sh = choose_shape(ctx, csr, fp64, cols, cols, 0);
           sh.tc = false;
           sh.rb = true;
+          sh.rt = false;
           sh.rb_warps = ctx->rb_warps > 0 ? ctx->rb_warps : t.warps;
           sh.rb_unroll = ctx->rb_unroll > 0 ? ctx->rb_unroll : t.unroll;
           sh.rb_packed = ctx->rb_packed >= 0 ? ctx->rb_packed != 0 : t.packed;
@@ -785,6 +820,43 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
             best_t.rb_packed = sh.rb_packed;
             best_t.rb_window = sh.rb_window;
           }
+        }
+      }
+      // the 8-row tensor-core step where it applies: a few (warps, depth) shapes
+      if (!fp64 && cols == 32 && !csr->complex_h && ctx->reorder != 0 &&
+          (ctx->kernel_variant == -1 || ctx->kernel_variant == 5)) {
+        struct RtTry { int warps, depth; bool regs; };
+        for (const RtTry t : {RtTry{16, 3, true}, RtTry{16, 2, true}, RtTry{12, 4, true}, RtTry{16, 4, false},
+                              RtTry{16, 3, false}}) {
+          if (ctx->rt_stage >= 0 && (ctx->rt_stage == 0) != t.regs) continue;
+          StepShape sh = choose_shape(ctx, csr, fp64, cols, cols, 0);
+          sh.tc = false;
+          sh.rb = false;
+          sh.rt = true;
+          sh.rt_regs = t.regs;
+          sh.rt_warps = ctx->rt_warps > 0 ? ctx->rt_warps : t.warps;
+          sh.rt_depth = ctx->rt_depth > 0 ? ctx->rt_depth : t.depth;
+          Recursion r;
+          r.setup(ctx, csr, sh, steps);
+          if (!r.shape.rt) break;
+          fill_phase(ctx, r, 1, 0, cols / 2);
+          r.run();  // warm
+          ctx_sync(ctx);
+          const auto before = ctx->stats["cheb_step"];
+          r.run();
+          ctx_sync(ctx);
+          const auto after = ctx->stats["cheb_step"];
+          const double per = (after.ms - before.ms) / std::max<int64_t>(1, after.launches - before.launches);
+          if (per < best_c) {
+            best_c = per;
+            best_t.tc = false;
+            best_t.rb = false;
+            best_t.rt = true;
+            best_t.rt_warps = sh.rt_warps;
+            best_t.rt_depth = sh.rt_depth;
+            best_t.rt_regs = sh.rt_regs;
+          }
+          if (ctx->rt_warps > 0 && ctx->rt_depth > 0) break;  // one shape asked for
         }
       }
       g_shape_cache[{ctx, ShapeKey{csr, csr->n, csr->nnz, fp64, cols}}] = best_t;
@@ -813,8 +885,9 @@ extern "C" leo2d_status leo2d_kpm_step_kernel(leo2d_ctx* ctx, const leo2d_csr* c
     // the demotions Recursion::setup applies before any build
     const bool can_perm = csr->pos.p != nullptr && csr->nnz > 0;
     if (s.rb && (!can_perm || s.fp64 || s.cols != 32 || ctx->reorder == 0)) s.rb = false;
+    if (s.rt && (!can_perm || s.fp64 || s.cols != 32 || ctx->reorder == 0 || csr->complex_h)) s.rt = false;
     if (s.tc && !can_perm) s.tc = false;
-    *kernel = s.rb ? (s.rb_window ? 4 : 3) : s.tc ? 2 : s.tiled ? 0 : 1;
+    *kernel = s.rt ? 5 : s.rb ? (s.rb_window ? 4 : 3) : s.tc ? 2 : s.tiled ? 0 : 1;
     *block = s.cols;
   });
 }

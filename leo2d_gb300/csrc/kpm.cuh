@@ -19,6 +19,10 @@ struct StepShape {
   bool rb_packed = true;   // row-block step: paired FP32 FMAs
   int rb_unroll = 8;       // row-block step: slot batches in flight per lane (4, 8)
   bool rb_window = false;  // row-block step over shared-memory windows (rbw_spmm.cu)
+  bool rt = false;         // 8-row blocks on the tensor cores (rt_spmm.cu; FP32, 32 columns)
+  int rt_warps = 16;       // 8-row step: warps per CTA (8, 12, 16, 24)
+  int rt_depth = 4;        // 8-row step: k-steps of T_n rows in flight per warp (2, 3, 4, 6)
+  bool rt_regs = true;     // 8-row step: T_n rows staged in registers (else shared memory)
 };
 
 // Vector block resident on the device: two buffers of n x cols (T_k, T_{k-1}).
@@ -72,6 +76,17 @@ unsigned rb_grid(leo2d_ctx* ctx, const leo2d_csr* csr, int warps);
 void rb_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape, unsigned grid, size_t smem,
                     const float* tn, float* tp, const float* tprev, int first, float alpha, double* partials,
                     const double* prev_partials, double* prev_dots, float* out2 = nullptr);
+
+// The 8-row tensor-core step (rt_spmm.cu): shared memory of a shape, the grid
+// its blocks are built for (csr_build_rt with rt_group_of / rt_chunk_of), and
+// one launch.
+size_t rt_smem_bytes(int warps, int depth, bool regs);
+unsigned rt_grid(leo2d_ctx* ctx, const leo2d_csr* csr, int warps);
+int rt_group_of(const leo2d_ctx* ctx);
+int rt_chunk_of(const leo2d_ctx* ctx);
+void rt_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape, unsigned grid, size_t smem,
+                    const float* tn, float* tp, const float* tprev, int first, float alpha, double* partials,
+                    const double* prev_partials, double* prev_dots);
 
 // The windowed row-block step (rbw_spmm.cu), as above.
 int rbw_stages(leo2d_ctx* ctx, leo2d_csr* csr);

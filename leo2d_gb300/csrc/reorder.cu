@@ -4,10 +4,15 @@
 // (Sheet::setIndex, src/geom/sheet.cpp:217-285), so the interlayer neighbours
 // of a run of consecutive rows lie in a long strip of the other sheet. The
 // recursion streams a permuted copy instead: orbitals of both sheets are
-// grouped by square real-space patches (row-major patch order; within a patch
-// by sheet, then by the reference index), which makes the T_n rows gathered by
-// a row tile compact and L1-resident. The permutation is a stable sort by patch
-// id (device LSD radix sort, 8-bit digits). Traces are invariant under the
+// grouped by square real-space patches (row-major patch order), which makes the
+// T_n rows gathered by a row tile compact and L1-resident. Within a patch the
+// orbitals go by sheet and then either by the reference index or (the curve
+// ordering) along a Hilbert curve over 32 x 32 cells of the patch, so that any
+// run of consecutive rows of one sheet is a compact cluster: 8 such rows share
+// most of their neighbours (the 8-row blocks of rt_spmm.cu hold about 16 slots
+// per row on twisted bilayers, against 18 with the reference index). The
+// permutation is a stable sort of 32-bit keys (device LSD radix sort, 8-bit
+// digits). Traces are invariant under the
 // permutation; start vectors are generated from the reference index of each
 // row, so moments equal those of the unpermuted matrix up to summation order.
 #include <algorithm>
@@ -32,6 +37,43 @@ __global__ void k_patch_keys(const double* __restrict__ pos, int64_t n, double x
     const int px = (int)floor((pos[3 * k] - x0) * inv_s);
     const int py = (int)floor((pos[3 * k + 1] - y0) * inv_s);
     keys[k] = (uint32_t)(max(py, 0) * nx + max(px, 0));
+    vals[k] = (int32_t)k;
+  }
+}
+
+// Index of cell (x, y), 0 <= x, y < 32, along a Hilbert curve of the 32 x 32 cells.
+__device__ __forceinline__ uint32_t hilbert32(uint32_t x, uint32_t y) {
+  uint32_t d = 0;
+  for (uint32_t s = 16; s > 0; s >>= 1) {
+    const uint32_t rx = (x & s) ? 1u : 0u, ry = (y & s) ? 1u : 0u;
+    d += s * s * ((3u * rx) ^ ry);
+    if (ry == 0) {
+      if (rx == 1) {
+        x = 31u - x;
+        y = 31u - y;
+      }
+      const uint32_t tt = x;
+      x = y;
+      y = tt;
+    }
+  }
+  return d;
+}
+
+// Curve keys: patch id (row-major) << 12 | sheet (2 bits) << 10 | Hilbert index of
+// the orbital's 1/32-patch cell.
+__global__ void k_curve_keys(const double* __restrict__ pos, const int32_t* __restrict__ grid4, int64_t n, double x0,
+                             double y0, double patch, int nx, uint32_t* __restrict__ keys,
+                             int32_t* __restrict__ vals) {
+  const double inv_s = 1.0 / patch, inv_c = 32.0 / patch;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const double dx = pos[3 * k] - x0, dy = pos[3 * k + 1] - y0;
+    const int px = max((int)floor(dx * inv_s), 0), py = max((int)floor(dy * inv_s), 0);
+    const int cx = min(max((int)floor(dx * inv_c) - 32 * px, 0), 31);
+    const int cy = min(max((int)floor(dy * inv_c) - 32 * py, 0), 31);
+    const uint32_t sheet = grid4 ? (uint32_t)min(max(grid4[4 * k + 3], 0), 3) : 0u;
+    keys[k] = ((uint32_t)(py * nx + px) << 12) | (sheet << 10) | hilbert32((uint32_t)cx, (uint32_t)cy);
     vals[k] = (int32_t)k;
   }
 }
@@ -159,9 +201,11 @@ __global__ void k_perm_fill(const int64_t* __restrict__ rp, const int32_t* __res
 
 namespace leo2d {
 
-void csr_build_reordered(leo2d_ctx* ctx, leo2d_csr* csr, double patch, bool with_fp64) {
+void csr_build_reordered(leo2d_ctx* ctx, leo2d_csr* csr, double patch, bool with_fp64, bool curve) {
+  const int curve_req = curve ? 1 : 0;
   csr_drop_tc(csr);
   csr_drop_rb(csr);
+  csr_drop_rt(csr);
   const int64_t n = csr->n;
   LEO_REQUIRE(csr->pos.p, "locality ordering needs orbital positions");
   LEO_REQUIRE(patch > 0.5, "patch size must exceed 0.5 A");
@@ -181,18 +225,26 @@ void csr_build_reordered(leo2d_ctx* ctx, leo2d_csr* csr, double patch, bool with
   const int nx = (int)std::floor((xh - xl) / patch) + 1;
   const int ny = (int)std::floor((yh - yl) / patch) + 1;
   LEO_REQUIRE((int64_t)nx * ny < (1ll << 24), "too many patches");
+  // the curve keys hold 20 bits of patch id
+  if ((int64_t)nx * ny >= (1ll << 20)) curve = false;
   // keys and stable sort
   DevBuf<uint32_t> ka(n), kb(n);
   DevBuf<int32_t> va(n), vb(n);
-  launch(ctx, "patch_keys", [&] {
-    k_patch_keys<<<grid_for(n, 256, (int64_t)ctx->sm_count * 32), 256, 0, ctx->stream>>>(
-        csr->pos.p, n, xl, yl, 1.0 / patch, nx, ka.p, va.p);
-  });
+  if (curve)
+    launch(ctx, "patch_keys", [&] {
+      k_curve_keys<<<grid_for(n, 256, (int64_t)ctx->sm_count * 32), 256, 0, ctx->stream>>>(
+          csr->pos.p, csr->grid4.p, n, xl, yl, patch, nx, ka.p, va.p);
+    });
+  else
+    launch(ctx, "patch_keys", [&] {
+      k_patch_keys<<<grid_for(n, 256, (int64_t)ctx->sm_count * 32), 256, 0, ctx->stream>>>(
+          csr->pos.p, n, xl, yl, 1.0 / patch, nx, ka.p, va.p);
+    });
   const int nb = (int)((n + kRsTile - 1) / kRsTile);
   DevBuf<int64_t> hist((size_t)kRsBins * nb), offs((size_t)kRsBins * nb + 1);
   uint32_t *kin = ka.p, *kout = kb.p;
   int32_t *vin = va.p, *vout = vb.p;
-  for (int shift = 0; shift < 24; shift += 8) {
+  for (int shift = 0; shift < (curve ? 32 : 24); shift += 8) {
     launch(ctx, "rs_hist", [&] { k_rs_hist<<<nb, kRsThreads, 0, ctx->stream>>>(kin, n, shift, hist.p, nb); });
     exclusive_scan_i64(ctx, hist.p, offs.p, (int64_t)kRsBins * nb);
     launch(ctx, "rs_scatter", [&] {
@@ -201,7 +253,7 @@ void csr_build_reordered(leo2d_ctx* ctx, leo2d_csr* csr, double patch, bool with
     std::swap(kin, kout);
     std::swap(vin, vout);
   }
-  // after 3 passes the sorted order is in (kin, vin)
+  // after the passes the sorted order is in (kin, vin)
   csr->new2old.alloc(n);
   csr->old2new.alloc(n);
   LEO_CUDA(cudaMemcpyAsync(csr->new2old.p, vin, n * sizeof(int32_t), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -243,12 +295,15 @@ void csr_build_reordered(leo2d_ctx* ctx, leo2d_csr* csr, double patch, bool with
   csr->reordered = true;
   csr->reorder_fp64 = with_fp64;
   csr->reorder_patch = patch;
+  csr->reorder_curve = curve ? 1 : 0;
+  csr->reorder_curve_req = curve_req;
   csr->perm_tile_rows = 0;
 }
 
 void csr_drop_reordered(leo2d_csr* csr) {
   csr_drop_tc(csr);
   csr_drop_rb(csr);
+  csr_drop_rt(csr);
   csr->reordered = false;
   csr->reorder_fp64 = false;
   csr->new2old.release();

@@ -1,0 +1,905 @@
+// rt_spmm.cu - the Chebyshev step over row blocks of 8 rows on the tensor cores
+// (FP32 recursion, 32 columns).
+//
+// Same step as the other step kernels (T_{n+1} = a H~ T_n - T_{n-1} with the
+// two moment dots fused; Locality::computeDosTraceKPM, src/locality.cpp:
+// 6195-6234, with SpMatrix::vectorMultiply, src/matrix/spmatrix.cpp:346-360, as
+// its product). The 4-row block step (rb_spmm.cu) is bound by the L1 / shared
+// memory pipe: every slot costs one wavefront for the gathered T_n row and one
+// for the broadcast of its 4 values. Here 8 consecutive rows (a compact cluster
+// of one sheet under the curve ordering of reorder.cu) share the union of their
+// columns, and the product of a k-step (8 slots) is two TF32 MMAs per split
+// term: D^T (32 columns x 8 rows) = X^T (32 x 8 slots) V^T (8 slots x 8 rows),
+// m16n8k8, the 32 columns as M. The tensor core consumes the value panel and
+// the staged T_n rows from shared memory at full width, so a slot costs about
+// half the pipe work of the 4-row step and 8 rows share each gathered row.
+//
+// FP32 accuracy from TF32 units: every operand x is split x = hi + lo (hi =
+// x rounded to TF32, lo = the rest rounded to TF32) and the product is taken as
+// lo*hi + hi*lo + hi*hi, accumulated in FP32 (relative error about 2^-21).
+//
+// Format (built once per matrix and launch shape, from the locality-ordered copy)
+//   row block b = rows 8b..8b+7 of the ordered numbering; its slots are the
+//   sorted union of its rows' columns, padded to a multiple of 8 (padding: a
+//   valid column with zero values). Slots go in k-steps of 8; a k-step is
+//   288 bytes:
+//     int32 col[8]       slots in the order 0 4 1 5 2 6 3 7, so lane q of a
+//                        quarter-warp reads (slot q, slot q + 4) as one int2;
+//                        bit 31 of the last entry marks the block's last k-step
+//     float2 v[32]       lane 4g + t holds (V[row g][slot t], V[row g][slot t+4]),
+//                        the B fragment of mma.m16n8k8 (B = V^T, k = slot, n = row)
+//   Blocks are stored in the order the kernel processes them: warp w of CTA c
+//   takes runs of G consecutive blocks (one run per tile of W runs, tiles in
+//   chunked round-robin over the CTAs), so each warp streams one contiguous
+//   range of k-steps, rt_wbeg[c W + w] .. rt_wbeg[c W + w + 1].
+// Kernel (one CTA per SM, W warps, no CTA-wide barrier in the main loop)
+//   Each warp runs a software pipeline over its k-steps with cp.async groups:
+//   at iteration u it copies the matrix data of k-step u + D + DM (cp.async.cg,
+//   L2 only) and the 8 T_n rows of k-step u + D (cp.async.ca, so rows stay in
+//   L1 for the neighbouring blocks; the columns come from the matrix data that
+//   landed DM iterations earlier), then waits for k-step u's group and runs its
+//   MMAs. T_n rows land in a 1 KB ring entry with 16-byte chunk c of row s at
+//   chunk c ^ s; lane (g, t) reads columns 4 cg .. 4 cg + 3, cg = (g >> 1) |
+//   ((g & 1) << 2), of slots t and t + 4 with no bank conflicts (memory column
+//   4 cg + i is logical column g + 8 i of the MMA). At a block's last k-step
+//   the lane owns rows 2t and 2t + 1 of the block, columns 4 cg .. 4 cg + 3: it
+//   writes T_{n+1} and adds its moment dots (FP32 over 16 blocks, then FP64).
+//   cp.async waits are hardware waits on copies already issued: no spin loop.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "kpm.cuh"
+
+using namespace leo2d;
+
+#include "step_kernels.cuh"
+
+namespace {
+
+#include "rb_common.cuh"
+
+constexpr int kRtRows = 8;           // rows per block
+constexpr int kRtStepBytes = 288;    // one k-step: 8 columns + 32 value pairs
+constexpr int kRtMaxEnt = 2048;      // stored entries of one block (build limit)
+constexpr int kRtBuildWarps = 4;
+
+__device__ __forceinline__ void cp_async_cg16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_ca16(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void prefetch_l2_bulk(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// x = hi + lo with hi, lo TF32 values (bit patterns for mma .tf32 operands)
+__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
+  uint32_t h;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+  const float r = x - __uint_as_float(h);
+  uint32_t l;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(r));
+  hi = h;
+  lo = l;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+struct RtArgs {
+  int64_t n;    // rows
+  int64_t nrb;  // row blocks
+  const unsigned char* __restrict__ data;  // k-steps in processing order
+  const int64_t* __restrict__ wbeg;        // [grid * W + 1] first k-step of each warp
+  const float* __restrict__ tn;
+  float* __restrict__ tp;
+  const float* __restrict__ tprev;  // null: T_{n-1} is read from tp
+  int first;
+  float alpha;  // 0: the default (1 for the first step, else 2)
+  double* __restrict__ partials;
+  const double* __restrict__ prev_partials;
+  double* __restrict__ prev_dots;
+  int group;        // G: consecutive blocks per run
+  int chunk;        // consecutive tiles per CTA between grid-wide jumps
+};
+
+// Block index of the j-th block of warp w of CTA bid (the build's processing order).
+__device__ __forceinline__ int64_t rt_block_of(int64_t j, int w, int W, int G, int chunk, int bid, int nblk) {
+  const int64_t i = j / G;
+  const int64_t tile = ((int64_t)bid + (i / chunk) * (int64_t)nblk) * chunk + i % chunk;
+  return (tile * W + w) * G + j % G;
+}
+
+}  // namespace
+
+namespace {
+
+// ---------------------------------------------------------------- the step kernel
+
+template <int W, int D, int DM>
+__global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ RtArgs a) {
+  constexpr int C = 32;
+  constexpr int NT = W * 32;
+  constexpr int XS = D + 1;       // ring of staged T_n rows (k-steps)
+  constexpr int MS = D + DM + 1;  // ring of matrix k-steps
+  constexpr int kWarpBytes = XS * 1024 + MS * kRtStepBytes;
+  constexpr int kPf = 32;         // matrix k-steps prefetched into L2 ahead of the copies
+  static_assert(DM >= D + 1, "the matrix lookahead must exceed the row lookahead");
+  extern __shared__ __align__(1024) unsigned char rt_smem[];
+  const int bid = (int)blockIdx.x, nblk = (int)gridDim.x;
+  if (a.prev_partials) reduce_prev<C, NT>(a.prev_partials, a.prev_dots, nblk, bid, nblk);
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, t = lane & 3;        // MMA fragment coordinates
+  const int q = lane >> 3, p = lane & 7;        // copies: slots q and q + 4, 16-byte chunk p
+  const int cg = (g >> 1) | ((g & 1) << 2);     // the lane's chunk of 4 columns
+  unsigned char* xr = rt_smem + (size_t)warp * kWarpBytes;
+  unsigned char* mr = xr + XS * 1024;
+  const int64_t k0 = a.wbeg[bid * W + warp];
+  const int nk = (int)(a.wbeg[bid * W + warp + 1] - k0);
+  const unsigned char* gdata = a.data + k0 * kRtStepBytes;
+  const float alpha = a.alpha != 0.f ? a.alpha : (a.first ? 1.f : 2.f);
+  const float* tprev = a.tprev ? a.tprev : a.tp;
+  const float* tnc = a.tn + 4 * cg;
+
+  // dots: FP32 over kDotFlush blocks, then FP64; lane (g, t) ends with column 4 cg + t
+  constexpr int kDotFlush = 16;
+  double d0 = 0.0, d1 = 0.0;
+  float e0[4], e1[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) e0[c] = e1[c] = 0.f;
+  auto flush = [&]() {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      e0[c] += __shfl_xor_sync(0xffffffffu, e0[c], 1);
+      e1[c] += __shfl_xor_sync(0xffffffffu, e1[c], 1);
+      e0[c] += __shfl_xor_sync(0xffffffffu, e0[c], 2);
+      e1[c] += __shfl_xor_sync(0xffffffffu, e1[c], 2);
+    }
+    float v0 = e0[0], v1 = e1[0];
+#pragma unroll
+    for (int c = 1; c < 4; ++c)
+      if (t == c) {
+        v0 = e0[c];
+        v1 = e1[c];
+      }
+    d0 += (double)v0;
+    d1 += (double)v1;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) e0[c] = e1[c] = 0.f;
+  };
+
+  float acc0[4], acc1[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) acc0[i] = acc1[i] = 0.f;
+  float4 xn0 = make_float4(0.f, 0.f, 0.f, 0.f), xn1 = xn0, xp0 = xn0, xp1 = xn0;
+  int64_t jblk = 0, row0 = 0;
+  bool start = true;
+  int since_flush = 0;
+  // ring slots: im of matrix k-step u + D + DM, ix of row k-step u + D
+  int im = 0;
+  int ix = (XS - (DM % XS)) % XS;
+  for (int u = -(D + DM); u < nk; ++u) {
+    __syncwarp();  // every lane is done with the entries these copies overwrite
+    const int vm = u + D + DM, vx = u + D;
+    if (vm < nk && lane < kRtStepBytes / 16)
+      cp_async_cg16(mr + im * kRtStepBytes + 16 * lane, gdata + (size_t)vm * kRtStepBytes + 16 * lane);
+    if (lane == 0 && (vm & 7) == 0 && vm + kPf < nk)
+      prefetch_l2_bulk(gdata + (size_t)(vm + kPf) * kRtStepBytes, (uint32_t)min(8, nk - vm - kPf) * kRtStepBytes);
+    if (vx >= 0 && vx < nk) {
+      // the columns of k-step vx landed DM iterations ago (slot im - DM)
+      const int jm = im >= DM ? im - DM : im + MS - DM;
+      const int2 cc = *reinterpret_cast<const int2*>(mr + jm * kRtStepBytes + 8 * q);
+      unsigned char* dst = xr + ix * 1024;
+      cp_async_ca16(dst + q * 128 + 16 * (p ^ q), a.tn + (size_t)(uint32_t)(cc.x & 0x7fffffff) * C + 4 * p);
+      cp_async_ca16(dst + (q + 4) * 128 + 16 * (p ^ (q + 4)),
+                    a.tn + (size_t)(uint32_t)(cc.y & 0x7fffffff) * C + 4 * p);
+    }
+    cp_async_commit();
+    cp_async_wait<D>();  // k-step u's rows (and k-step u + D + 1's matrix data) have landed
+    __syncwarp();
+    const int sm = im == MS - 1 ? 0 : im + 1;  // slot of matrix k-step u
+    const int sx = ix == XS - 1 ? 0 : ix + 1;  // slot of row k-step u
+    im = sm;
+    ix = sx;
+    if (u < 0) continue;
+    if (start) {
+      const int64_t blk = rt_block_of(jblk, warp, W, a.group, a.chunk, bid, nblk);
+      row0 = blk * kRtRows;
+      const int64_t r0 = row0 + 2 * t;
+      if (r0 < a.n) {
+        xn0 = ldg4(tnc + r0 * C);
+        if (!a.first) xp0 = ld_once4(tprev + r0 * C + 4 * cg);
+      }
+      if (r0 + 1 < a.n) {
+        xn1 = ldg4(tnc + (r0 + 1) * C);
+        if (!a.first) xp1 = ld_once4(tprev + (r0 + 1) * C + 4 * cg);
+      }
+      start = false;
+    }
+    const unsigned char* xs = xr + sx * 1024;
+    const unsigned char* ms = mr + sm * kRtStepBytes;
+    const float4 xa = *reinterpret_cast<const float4*>(xs + t * 128 + 16 * (cg ^ t));
+    const float4 xb = *reinterpret_cast<const float4*>(xs + (t + 4) * 128 + 16 * (cg ^ (t + 4)));
+    const float2 vv = *reinterpret_cast<const float2*>(ms + 32 + 8 * lane);
+    const bool last = *reinterpret_cast<const int*>(ms + 28) < 0;
+    uint32_t ah[8], al[8], bh0, bl0, bh1, bl1;
+    split_tf32(xa.x, ah[0], al[0]);
+    split_tf32(xa.y, ah[1], al[1]);
+    split_tf32(xa.z, ah[2], al[2]);
+    split_tf32(xa.w, ah[3], al[3]);
+    split_tf32(xb.x, ah[4], al[4]);
+    split_tf32(xb.y, ah[5], al[5]);
+    split_tf32(xb.z, ah[6], al[6]);
+    split_tf32(xb.w, ah[7], al[7]);
+    split_tf32(vv.x, bh0, bl0);
+    split_tf32(vv.y, bh1, bl1);
+    // columns 0..15 (logical g, g + 8) and 16..31 (g + 16, g + 24): lo*hi + hi*lo + hi*hi
+    mma_tf32(acc0, al[0], al[1], al[4], al[5], bh0, bh1);
+    mma_tf32(acc1, al[2], al[3], al[6], al[7], bh0, bh1);
+    mma_tf32(acc0, ah[0], ah[1], ah[4], ah[5], bl0, bl1);
+    mma_tf32(acc1, ah[2], ah[3], ah[6], ah[7], bl0, bl1);
+    mma_tf32(acc0, ah[0], ah[1], ah[4], ah[5], bh0, bh1);
+    mma_tf32(acc1, ah[2], ah[3], ah[6], ah[7], bh0, bh1);
+    if (last) {  // warp-uniform: the block's epilogue
+      const int64_t r0 = row0 + 2 * t;
+      const float4 h0 = make_float4(acc0[0], acc0[2], acc1[0], acc1[2]);  // row 2t
+      const float4 h1 = make_float4(acc0[1], acc0[3], acc1[1], acc1[3]);  // row 2t + 1
+      float4 y0, y1;
+      if (a.first) {
+        y0 = make_float4(alpha * h0.x, alpha * h0.y, alpha * h0.z, alpha * h0.w);
+        y1 = make_float4(alpha * h1.x, alpha * h1.y, alpha * h1.z, alpha * h1.w);
+      } else {
+        y0 = make_float4(alpha * h0.x - xp0.x, alpha * h0.y - xp0.y, alpha * h0.z - xp0.z, alpha * h0.w - xp0.w);
+        y1 = make_float4(alpha * h1.x - xp1.x, alpha * h1.y - xp1.y, alpha * h1.z - xp1.z, alpha * h1.w - xp1.w);
+      }
+      if (r0 < a.n) {
+        st_na4(a.tp + r0 * C + 4 * cg, y0);
+        e0[0] += xn0.x * xn0.x;
+        e0[1] += xn0.y * xn0.y;
+        e0[2] += xn0.z * xn0.z;
+        e0[3] += xn0.w * xn0.w;
+        e1[0] += y0.x * xn0.x;
+        e1[1] += y0.y * xn0.y;
+        e1[2] += y0.z * xn0.z;
+        e1[3] += y0.w * xn0.w;
+      }
+      if (r0 + 1 < a.n) {
+        st_na4(a.tp + (r0 + 1) * C + 4 * cg, y1);
+        e0[0] += xn1.x * xn1.x;
+        e0[1] += xn1.y * xn1.y;
+        e0[2] += xn1.z * xn1.z;
+        e0[3] += xn1.w * xn1.w;
+        e1[0] += y1.x * xn1.x;
+        e1[1] += y1.y * xn1.y;
+        e1[2] += y1.z * xn1.z;
+        e1[3] += y1.w * xn1.w;
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc0[i] = acc1[i] = 0.f;
+      ++jblk;
+      start = true;
+      if (++since_flush == kDotFlush) {
+        since_flush = 0;
+        flush();
+      }
+    }
+  }
+  cp_async_wait<0>();
+  flush();
+  // warps add their columns in warp order (deterministic)
+  __shared__ double bsum[2 * C];
+  for (int i = threadIdx.x; i < 2 * C; i += NT) bsum[i] = 0.0;
+  __syncthreads();
+  const int col = 4 * cg + t;
+  for (int w = 0; w < W; ++w) {
+    if (warp == w) {
+      bsum[2 * col] += d0;
+      bsum[2 * col + 1] += d1;
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < 2 * C; i += NT) a.partials[(size_t)bid * 2 * C + i] = bsum[i];
+}
+
+// The same step with every operand in registers (no shared memory, so the whole
+// L1 caches T_n rows): lane (q, p) loads 16-byte chunk p of the T_n rows of slots
+// q and q + 4 (one 128-byte row per quarter-warp, one L1 wavefront per slot) U
+// k-steps ahead, and the A fragments are gathered from those registers with
+// eight shuffles per k-step (lane (g, t) takes chunk cg of slots t and t + 4 from
+// lane 8t + cg). The matrix stream is read with plain loads that skip L1: the
+// columns 2U k-steps ahead (they address the row loads), the values U ahead, and
+// kPf k-steps further the stream is prefetched into L2 in bulk.
+__device__ __forceinline__ int2 ld_stream_i2(const void* p) {
+  int2 r;
+  asm volatile("ld.global.nc.L1::no_allocate.v2.s32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "l"(p));
+  return r;
+}
+__device__ __forceinline__ float2 ld_stream_f2(const void* p) {
+  float2 r;
+  asm volatile("ld.global.nc.L1::no_allocate.v2.f32 {%0, %1}, [%2];" : "=f"(r.x), "=f"(r.y) : "l"(p));
+  return r;
+}
+
+template <int W, int U>
+__global__ void __launch_bounds__(W * 32, 1) k_cheb_rtr(const __grid_constant__ RtArgs a) {
+  constexpr int C = 32;
+  constexpr int NT = W * 32;
+  constexpr int kPf = 48;  // matrix k-steps prefetched into L2 ahead of the loads
+  const int bid = (int)blockIdx.x, nblk = (int)gridDim.x;
+  if (a.prev_partials) reduce_prev<C, NT>(a.prev_partials, a.prev_dots, nblk, bid, nblk);
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int q = lane >> 3, p = lane & 7;
+  const int cg = (g >> 1) | ((g & 1) << 2);
+  const int src = 8 * t + cg;  // the lane holding chunk cg of slots t and t + 4
+  const int64_t k0 = a.wbeg[bid * W + warp];
+  const int nk = (int)(a.wbeg[bid * W + warp + 1] - k0);
+  const unsigned char* gdata = a.data + k0 * kRtStepBytes;
+  const float alpha = a.alpha != 0.f ? a.alpha : (a.first ? 1.f : 2.f);
+  const float* tprev = a.tprev ? a.tprev : a.tp;
+  const float* tnc = a.tn + 4 * cg;
+  const float* tnp = a.tn + 4 * p;
+
+  constexpr int kDotFlush = 16;
+  double d0 = 0.0, d1 = 0.0;
+  float e0[4], e1[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) e0[c] = e1[c] = 0.f;
+  auto flush = [&]() {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      e0[c] += __shfl_xor_sync(0xffffffffu, e0[c], 1);
+      e1[c] += __shfl_xor_sync(0xffffffffu, e1[c], 1);
+      e0[c] += __shfl_xor_sync(0xffffffffu, e0[c], 2);
+      e1[c] += __shfl_xor_sync(0xffffffffu, e1[c], 2);
+    }
+    float v0 = e0[0], v1 = e1[0];
+#pragma unroll
+    for (int c = 1; c < 4; ++c)
+      if (t == c) {
+        v0 = e0[c];
+        v1 = e1[c];
+      }
+    d0 += (double)v0;
+    d1 += (double)v1;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) e0[c] = e1[c] = 0.f;
+  };
+
+  float acc0[4], acc1[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) acc0[i] = acc1[i] = 0.f;
+  float4 xn0 = make_float4(0.f, 0.f, 0.f, 0.f), xn1 = xn0, xp0 = xn0, xp1 = xn0;
+  int64_t jblk = 0, row0 = 0;
+  bool start = true;
+  int since_flush = 0;
+
+  // rings (slot j = k-step mod U): columns of k-steps u + U .. u + 2U - 1, rows,
+  // values and block-end flags of k-steps u .. u + U - 1
+  int2 cc[U];
+  float4 xa[U], xb[U];
+  float2 vv[U];
+  bool lastf[U];
+  auto load_cols = [&](int v) { return ld_stream_i2(gdata + (size_t)v * kRtStepBytes + 8 * q); };
+  auto issue = [&](int j, int v) {  // k-step v (its columns in cc[j]) into slot j
+    const int2 c = cc[j];
+    lastf[j] = __any_sync(0xffffffffu, q == 3 && c.y < 0);
+    xa[j] = ldg4(tnp + (size_t)(uint32_t)(c.x & 0x7fffffff) * C);
+    xb[j] = ldg4(tnp + (size_t)(uint32_t)(c.y & 0x7fffffff) * C);
+    vv[j] = ld_stream_f2(gdata + (size_t)v * kRtStepBytes + 32 + 8 * lane);
+  };
+#pragma unroll
+  for (int j = 0; j < U; ++j) {
+    if (j < nk) cc[j] = load_cols(j);
+    if (lane == 0 && j == 0 && kPf < nk)
+      prefetch_l2_bulk(gdata + (size_t)kPf * kRtStepBytes, (uint32_t)min(8, nk - kPf) * kRtStepBytes);
+  }
+#pragma unroll
+  for (int j = 0; j < U; ++j) {
+    if (j < nk) {
+      issue(j, j);
+      if (j + U < nk) cc[j] = load_cols(j + U);
+    }
+  }
+  for (int u0 = 0; u0 < nk; u0 += U) {
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      const int u = u0 + j;
+      if (u >= nk) break;  // warp-uniform
+      if (start) {
+        const int64_t blk = rt_block_of(jblk, warp, W, a.group, a.chunk, bid, nblk);
+        row0 = blk * kRtRows;
+        const int64_t r0 = row0 + 2 * t;
+        if (r0 < a.n) {
+          xn0 = ldg4(tnc + r0 * C);
+          if (!a.first) xp0 = ld_once4(tprev + r0 * C + 4 * cg);
+        }
+        if (r0 + 1 < a.n) {
+          xn1 = ldg4(tnc + (r0 + 1) * C);
+          if (!a.first) xp1 = ld_once4(tprev + (r0 + 1) * C + 4 * cg);
+        }
+        start = false;
+      }
+      // A fragments: chunk cg of slots t and t + 4 from lane 8t + cg
+      float4 fa, fb;
+      fa.x = __shfl_sync(0xffffffffu, xa[j].x, src);
+      fa.y = __shfl_sync(0xffffffffu, xa[j].y, src);
+      fa.z = __shfl_sync(0xffffffffu, xa[j].z, src);
+      fa.w = __shfl_sync(0xffffffffu, xa[j].w, src);
+      fb.x = __shfl_sync(0xffffffffu, xb[j].x, src);
+      fb.y = __shfl_sync(0xffffffffu, xb[j].y, src);
+      fb.z = __shfl_sync(0xffffffffu, xb[j].z, src);
+      fb.w = __shfl_sync(0xffffffffu, xb[j].w, src);
+      const float2 v = vv[j];
+      const bool last = lastf[j];
+      // the slot is free: k-step u + U goes into it, and the columns of u + 2U
+      if (u + U < nk) {
+        issue(j, u + U);
+        if (u + 2 * U < nk) cc[j] = load_cols(u + 2 * U);
+      }
+      if (lane == 0 && ((u + U) & 7) == 0 && u + U + kPf < nk)
+        prefetch_l2_bulk(gdata + (size_t)(u + U + kPf) * kRtStepBytes,
+                         (uint32_t)min(8, nk - (u + U + kPf)) * kRtStepBytes);
+      uint32_t ah[8], al[8], bh0, bl0, bh1, bl1;
+      split_tf32(fa.x, ah[0], al[0]);
+      split_tf32(fa.y, ah[1], al[1]);
+      split_tf32(fa.z, ah[2], al[2]);
+      split_tf32(fa.w, ah[3], al[3]);
+      split_tf32(fb.x, ah[4], al[4]);
+      split_tf32(fb.y, ah[5], al[5]);
+      split_tf32(fb.z, ah[6], al[6]);
+      split_tf32(fb.w, ah[7], al[7]);
+      split_tf32(v.x, bh0, bl0);
+      split_tf32(v.y, bh1, bl1);
+      mma_tf32(acc0, al[0], al[1], al[4], al[5], bh0, bh1);
+      mma_tf32(acc1, al[2], al[3], al[6], al[7], bh0, bh1);
+      mma_tf32(acc0, ah[0], ah[1], ah[4], ah[5], bl0, bl1);
+      mma_tf32(acc1, ah[2], ah[3], ah[6], ah[7], bl0, bl1);
+      mma_tf32(acc0, ah[0], ah[1], ah[4], ah[5], bh0, bh1);
+      mma_tf32(acc1, ah[2], ah[3], ah[6], ah[7], bh0, bh1);
+      if (last) {
+        const int64_t r0 = row0 + 2 * t;
+        const float4 h0 = make_float4(acc0[0], acc0[2], acc1[0], acc1[2]);
+        const float4 h1 = make_float4(acc0[1], acc0[3], acc1[1], acc1[3]);
+        float4 y0, y1;
+        if (a.first) {
+          y0 = make_float4(alpha * h0.x, alpha * h0.y, alpha * h0.z, alpha * h0.w);
+          y1 = make_float4(alpha * h1.x, alpha * h1.y, alpha * h1.z, alpha * h1.w);
+        } else {
+          y0 = make_float4(alpha * h0.x - xp0.x, alpha * h0.y - xp0.y, alpha * h0.z - xp0.z, alpha * h0.w - xp0.w);
+          y1 = make_float4(alpha * h1.x - xp1.x, alpha * h1.y - xp1.y, alpha * h1.z - xp1.z, alpha * h1.w - xp1.w);
+        }
+        if (r0 < a.n) {
+          st_na4(a.tp + r0 * C + 4 * cg, y0);
+          e0[0] += xn0.x * xn0.x;
+          e0[1] += xn0.y * xn0.y;
+          e0[2] += xn0.z * xn0.z;
+          e0[3] += xn0.w * xn0.w;
+          e1[0] += y0.x * xn0.x;
+          e1[1] += y0.y * xn0.y;
+          e1[2] += y0.z * xn0.z;
+          e1[3] += y0.w * xn0.w;
+        }
+        if (r0 + 1 < a.n) {
+          st_na4(a.tp + (r0 + 1) * C + 4 * cg, y1);
+          e0[0] += xn1.x * xn1.x;
+          e0[1] += xn1.y * xn1.y;
+          e0[2] += xn1.z * xn1.z;
+          e0[3] += xn1.w * xn1.w;
+          e1[0] += y1.x * xn1.x;
+          e1[1] += y1.y * xn1.y;
+          e1[2] += y1.z * xn1.z;
+          e1[3] += y1.w * xn1.w;
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) acc0[i] = acc1[i] = 0.f;
+        ++jblk;
+        start = true;
+        if (++since_flush == kDotFlush) {
+          since_flush = 0;
+          flush();
+        }
+      }
+    }
+  }
+  flush();
+  __shared__ double bsum[2 * C];
+  for (int i = threadIdx.x; i < 2 * C; i += NT) bsum[i] = 0.0;
+  __syncthreads();
+  const int col = 4 * cg + t;
+  for (int w = 0; w < W; ++w) {
+    if (warp == w) {
+      bsum[2 * col] += d0;
+      bsum[2 * col + 1] += d1;
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < 2 * C; i += NT) a.partials[(size_t)bid * 2 * C + i] = bsum[i];
+}
+
+// ---------------------------------------------------------------- format build
+
+// One warp per block of 8 rows, at most kRtMaxEnt stored entries: the keys
+// (column << 16 | entry index) are sorted in the warp's slice of shared memory;
+// the distinct columns are the slots. Pass 0 writes the k-steps of each block;
+// pass 1 writes the block's k-steps at kstart[b] (data zero-filled before): the
+// columns in the interleaved order, the values in fragment order, entries of
+// one (row, column) summed in entry order, and the last k-step's flag.
+__global__ void __launch_bounds__(kRtBuildWarps * 32)
+    k_rt_build(int64_t n, int64_t nrb, const int64_t* __restrict__ prow, const int32_t* __restrict__ pcol,
+               const float* __restrict__ pval, int pass, int64_t* __restrict__ kst,
+               const int64_t* __restrict__ kstart, unsigned char* __restrict__ data, int* __restrict__ err,
+               unsigned long long* __restrict__ ssum) {
+  extern __shared__ unsigned long long rt_keys[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long* keys = rt_keys + (size_t)w * kRtMaxEnt;
+  const int64_t warps = (int64_t)gridDim.x * kRtBuildWarps;
+  for (int64_t b = (int64_t)blockIdx.x * kRtBuildWarps + w; b < nrb; b += warps) {
+    const int64_t r0 = b * kRtRows;
+    const int rows = (int)min((int64_t)kRtRows, n - r0);
+    const int64_t mine = lane <= kRtRows ? prow[r0 + min(lane, rows)] : 0;
+    int64_t srp[kRtRows + 1];
+#pragma unroll
+    for (int k = 0; k <= kRtRows; ++k) srp[k] = __shfl_sync(0xffffffffu, mine, k);
+    auto srp_at = [&](int k) {
+      int64_t v = srp[0];
+#pragma unroll
+      for (int kk = 1; kk <= kRtRows; ++kk)
+        if (k == kk) v = srp[kk];
+      return v;
+    };
+    // row of the block holding entry e (offsets from the block's first entry)
+    auto row_of = [&](int e) {
+      int r = 0;
+#pragma unroll
+      for (int k = 1; k < kRtRows; ++k) r += (k < rows && srp[k] - srp[0] <= e) ? 1 : 0;
+      return r;
+    };
+    const int64_t q0 = srp[0];
+    const int E = (int)(srp_at(rows) - q0);
+    if (E > kRtMaxEnt) {
+      if (lane == 0) {
+        atomicOr(err, 1);
+        if (pass == 0) kst[b] = 1;
+      }
+      continue;
+    }
+    __syncwarp();  // the previous block's keys are read
+    int P2 = 32;
+    while (P2 < E) P2 <<= 1;
+    for (int i = lane; i < P2; i += 32)
+      keys[i] = i < E ? (((unsigned long long)(uint32_t)pcol[q0 + i] << 16) | (unsigned long long)i) : ~0ull;
+    __syncwarp();
+    for (int k = 2; k <= P2; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int i = lane; i < P2; i += 32) {
+          const int ixj = i ^ j;
+          if (ixj > i) {
+            const bool up = (i & k) == 0;
+            const unsigned long long x = keys[i], y = keys[ixj];
+            if ((x > y) == up) {
+              keys[i] = y;
+              keys[ixj] = x;
+            }
+          }
+        }
+        __syncwarp();
+      }
+    // slot of each sorted entry: distinct columns counted in order (each lane a
+    // contiguous range of the sorted keys)
+    const int per = P2 / 32;
+    const int i0 = lane * per;
+    int cnt = 0;
+    for (int j = 0; j < per; ++j) {
+      const int i = i0 + j;
+      if (i < E && (i == 0 || (keys[i] >> 16) != (keys[i - 1] >> 16))) ++cnt;
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int K = __shfl_sync(0xffffffffu, incl, 31);
+    const int KS = max(1, (K + 7) / 8);
+    if (pass == 0) {
+      if (lane == 0) {
+        kst[b] = KS;
+        atomicAdd(ssum, (unsigned long long)K);
+        atomicMax(err + 1, K);
+      }
+      continue;
+    }
+    unsigned char* base = data + (size_t)kstart[b] * kRtStepBytes;
+    auto col_at = [&](int s) {  // column entry of slot s
+      const int jj = s & 7;
+      return reinterpret_cast<int32_t*>(base + (size_t)(s >> 3) * kRtStepBytes) + (jj < 4 ? 2 * jj : 2 * (jj - 4) + 1);
+    };
+    const int32_t pad_col = K > 0 ? (int32_t)(keys[0] >> 16) : 0;
+    for (int s = K + lane; s < 8 * KS; s += 32) *col_at(s) = pad_col;
+    int s = incl - cnt - 1;
+    for (int j = 0; j < per; ++j) {
+      const int i = i0 + j;
+      if (i >= E) break;
+      const unsigned long long k = keys[i];
+      const uint32_t c = (uint32_t)(k >> 16);
+      const int e = (int)(k & 0xFFFFu);
+      const bool new_col = i == 0 || (keys[i - 1] >> 16) != c;
+      if (new_col) {
+        ++s;
+        *col_at(s) = (int32_t)c;
+      }
+      const int r = row_of(e);
+      // the first entry of each (column, row) run sums the run in entry order
+      const bool run_start = new_col || row_of((int)(keys[i - 1] & 0xFFFFu)) != r;
+      if (run_start) {
+        float v = pval[q0 + e];
+        for (int i2 = i + 1; i2 < E; ++i2) {
+          const unsigned long long k2 = keys[i2];
+          if ((uint32_t)(k2 >> 16) != c) break;
+          const int e2 = (int)(k2 & 0xFFFFu);
+          if (row_of(e2) != r) break;
+          v += pval[q0 + e2];
+        }
+        const int jj = s & 7;
+        float* vp = reinterpret_cast<float*>(base + (size_t)(s >> 3) * kRtStepBytes + 32);
+        vp[2 * (4 * r + (jj & 3)) + (jj >> 2)] = v;
+      }
+    }
+    __syncwarp();  // every column entry is written before the flag goes on
+    if (lane == 0) {
+      int32_t* lastc = reinterpret_cast<int32_t*>(base + (size_t)(KS - 1) * kRtStepBytes) + 7;
+      *lastc = (int32_t)((uint32_t)*lastc | 0x80000000u);
+    }
+  }
+}
+
+__global__ void k_rt_gather_i64(const int32_t* __restrict__ seq, const int64_t* __restrict__ src, int64_t count,
+                                int64_t* __restrict__ dst) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < count; j += (int64_t)gridDim.x * blockDim.x)
+    dst[j] = src[seq[j]];
+}
+
+__global__ void k_rt_scatter_i64(const int32_t* __restrict__ seq, const int64_t* __restrict__ pos, int64_t count,
+                                 int64_t* __restrict__ dst) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < count; j += (int64_t)gridDim.x * blockDim.x)
+    dst[seq[j]] = pos[j];
+}
+
+__global__ void k_rt_warp_begin(const int64_t* __restrict__ first_pos, const int64_t* __restrict__ pos, int count,
+                                int64_t* __restrict__ wbeg) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+    wbeg[i] = pos[first_pos[i]];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+
+namespace {
+
+struct RtShape {
+  int64_t nrb, nruns, ntiles;
+  unsigned grid;
+};
+
+RtShape rt_shape(const leo2d_ctx* ctx, int64_t n, int warps, int group, int chunk) {
+  RtShape s;
+  s.nrb = (n + kRtRows - 1) / kRtRows;
+  s.nruns = (s.nrb + group - 1) / group;
+  s.ntiles = (s.nruns + warps - 1) / warps;
+  const int64_t chunks = (s.ntiles + chunk - 1) / chunk;
+  s.grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->sm_count, chunks));
+  return s;
+}
+
+// Smem of one warp's rings for lookahead D (matrix lookahead D + 2).
+constexpr int rt_warp_bytes(int depth) { return (depth + 1) * 1024 + (2 * depth + 3) * kRtStepBytes; }
+
+}  // namespace
+
+namespace leo2d {
+
+int rt_group_of(const leo2d_ctx* ctx) { return ctx->rt_group > 0 ? ctx->rt_group : 2; }
+int rt_chunk_of(const leo2d_ctx* ctx) { return ctx->rt_chunk > 0 ? ctx->rt_chunk : 2; }
+
+size_t rt_smem_bytes(int warps, int depth, bool regs) { return regs ? 0 : (size_t)warps * rt_warp_bytes(depth); }
+
+unsigned rt_grid(leo2d_ctx* ctx, const leo2d_csr* csr, int warps) {
+  return rt_shape(ctx, csr->n, warps, rt_group_of(ctx), rt_chunk_of(ctx)).grid;
+}
+
+void csr_drop_rt(leo2d_csr* csr) {
+  csr->rt_counted = false;
+  csr->rt_built = false;
+  csr->rt_kst.release();
+  csr->rt_wbeg.release();
+  csr->rt_data.release();
+  csr->rt_blocks = csr->rt_ksteps = csr->rt_union = 0;
+  csr->rt_max_slots = 0;
+  csr->rt_warps = csr->rt_group = csr->rt_chunk = 0;
+  csr->rt_grid = 0;
+}
+
+bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chunk) {
+  LEO_REQUIRE(csr->reordered && !csr->complex_h, "the 8-row tensor-core step needs the real locality-ordered copy");
+  const int64_t n = csr->n;
+  const RtShape sh = rt_shape(ctx, n, warps, group, chunk);
+  if (csr->rt_built && csr->rt_patch == csr->reorder_patch && csr->rt_curve == csr->reorder_curve &&
+      csr->rt_warps == warps && csr->rt_group == group && csr->rt_chunk == chunk && csr->rt_grid == sh.grid)
+    return true;
+  const size_t smem = (size_t)kRtBuildWarps * kRtMaxEnt * sizeof(unsigned long long);
+  LEO_CUDA(cudaFuncSetAttribute(k_rt_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const unsigned bgrid = grid_for(sh.nrb * 32, kRtBuildWarps * 32, (int64_t)ctx->sm_count * 8);
+  DevBuf<int> err(2);
+  DevBuf<unsigned long long> ssum(1);
+  LEO_CUDA(cudaMemsetAsync(err.p, 0, 2 * sizeof(int), ctx->stream));
+  LEO_CUDA(cudaMemsetAsync(ssum.p, 0, sizeof(unsigned long long), ctx->stream));
+  if (!(csr->rt_counted && csr->rt_patch == csr->reorder_patch && csr->rt_curve == csr->reorder_curve)) {
+    csr_drop_rt(csr);
+    csr->rt_kst.alloc(std::max<int64_t>(sh.nrb, 1));
+    launch(ctx, "rt_build", [&] {
+      k_rt_build<<<bgrid, kRtBuildWarps * 32, smem, ctx->stream>>>(n, sh.nrb, csr->prow.p, csr->pcol.p,
+                                                                     csr->pval32.p, 0, csr->rt_kst.p, nullptr,
+                                                                     nullptr, err.p, ssum.p);
+    });
+    int h[2] = {0, 0};
+    unsigned long long hs = 0;
+    d2h(ctx, h, err.p, 2);
+    d2h(ctx, &hs, ssum.p, 1);
+    ctx_sync(ctx);
+    if (h[0] != 0) {
+      csr_drop_rt(csr);
+      return false;
+    }
+    csr->rt_counted = true;
+    csr->rt_patch = csr->reorder_patch;
+    csr->rt_curve = csr->reorder_curve;
+    csr->rt_union = (int64_t)hs;
+    csr->rt_max_slots = h[1];
+    LEO_CUDA(cudaMemsetAsync(err.p, 0, 2 * sizeof(int), ctx->stream));
+  }
+  csr->rt_built = false;
+  // processing order: CTA c, warp w, its runs (tile by tile), the blocks of a run
+  std::vector<int32_t> seq;
+  seq.reserve((size_t)sh.nrb);
+  std::vector<int64_t> first((size_t)sh.grid * warps + 1);
+  for (unsigned c = 0; c < sh.grid; ++c)
+    for (int w = 0; w < warps; ++w) {
+      first[(size_t)c * warps + w] = (int64_t)seq.size();
+      for (int64_t i = 0;; ++i) {
+        const int64_t tile = ((int64_t)c + (i / chunk) * (int64_t)sh.grid) * chunk + i % chunk;
+        if (tile >= sh.ntiles) break;
+        const int64_t run = tile * warps + w;
+        if (run >= sh.nruns) break;
+        for (int j = 0; j < group; ++j) {
+          const int64_t b = run * group + j;
+          if (b >= sh.nrb) break;
+          seq.push_back((int32_t)b);
+        }
+      }
+    }
+  first[(size_t)sh.grid * warps] = (int64_t)seq.size();
+  LEO_REQUIRE((int64_t)seq.size() == sh.nrb, "8-row block order does not cover the matrix");
+  DevBuf<int32_t> dseq(std::max<int64_t>(sh.nrb, 1));
+  DevBuf<int64_t> kseq(std::max<int64_t>(sh.nrb, 1)), pos(sh.nrb + 1), dfirst(first.size());
+  h2d(ctx, dseq.p, seq.data(), seq.size());
+  h2d(ctx, dfirst.p, first.data(), first.size());
+  const unsigned g = grid_for(sh.nrb, 256, (int64_t)ctx->sm_count * 16);
+  launch(ctx, "rt_order", [&] { k_rt_gather_i64<<<g, 256, 0, ctx->stream>>>(dseq.p, csr->rt_kst.p, sh.nrb, kseq.p); });
+  exclusive_scan_i64(ctx, kseq.p, pos.p, sh.nrb);
+  int64_t total = 0;
+  d2h(ctx, &total, pos.p + sh.nrb, 1);
+  ctx_sync(ctx);
+  DevBuf<int64_t> kstart(std::max<int64_t>(sh.nrb, 1));
+  launch(ctx, "rt_order", [&] { k_rt_scatter_i64<<<g, 256, 0, ctx->stream>>>(dseq.p, pos.p, sh.nrb, kstart.p); });
+  csr->rt_wbeg.alloc(first.size());
+  launch(ctx, "rt_order", [&] {
+    k_rt_warp_begin<<<grid_for((int64_t)first.size(), 256), 256, 0, ctx->stream>>>(dfirst.p, pos.p, (int)first.size(),
+                                                                                   csr->rt_wbeg.p);
+  });
+  csr->rt_data.release();
+  csr->rt_data.alloc((size_t)std::max<int64_t>(total, 1) * kRtStepBytes);
+  LEO_CUDA(cudaMemsetAsync(csr->rt_data.p, 0, (size_t)std::max<int64_t>(total, 1) * kRtStepBytes, ctx->stream));
+  launch(ctx, "rt_build", [&] {
+    k_rt_build<<<bgrid, kRtBuildWarps * 32, smem, ctx->stream>>>(n, sh.nrb, csr->prow.p, csr->pcol.p, csr->pval32.p,
+                                                                   1, nullptr, kstart.p, csr->rt_data.p, err.p,
+                                                                   ssum.p);
+  });
+  int h0 = 0;
+  d2h(ctx, &h0, err.p, 1);
+  ctx_sync(ctx);
+  LEO_REQUIRE(h0 == 0, "8-row block build: a block exceeds the entry limit after counting");
+  csr->rt_blocks = sh.nrb;
+  csr->rt_ksteps = total;
+  csr->rt_warps = warps;
+  csr->rt_group = group;
+  csr->rt_chunk = chunk;
+  csr->rt_grid = sh.grid;
+  csr->rt_built = true;
+  return true;
+}
+
+void rt_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape, unsigned grid, size_t smem,
+                    const float* tn, float* tp, const float* tprev, int first, float alpha, double* partials,
+                    const double* prev_partials, double* prev_dots) {
+  LEO_REQUIRE(csr->rt_built && csr->rt_warps == shape.rt_warps && csr->rt_grid == grid,
+              "8-row blocks built for another launch shape");
+  LEO_REQUIRE(smem >= rt_smem_bytes(shape.rt_warps, shape.rt_depth, shape.rt_regs),
+              "8-row step shared memory changed since setup");
+  RtArgs a{};
+  a.n = csr->n;
+  a.nrb = csr->rt_blocks;
+  a.data = csr->rt_data.p;
+  a.wbeg = csr->rt_wbeg.p;
+  a.tn = tn;
+  a.tp = tp;
+  a.tprev = tprev;
+  a.first = first;
+  a.alpha = alpha;
+  a.partials = partials;
+  a.prev_partials = prev_partials;
+  a.prev_dots = prev_dots;
+  a.group = csr->rt_group;
+  a.chunk = csr->rt_chunk;
+  auto go = [&](auto kern, int warps) {
+    LEO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // the register form keeps no dynamic shared memory: the carveout goes to L1
+    if (smem == 0) LEO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 0));
+    launch(ctx, "cheb_step", [&] { kern<<<grid, warps * 32, smem, ctx->stream>>>(a); });
+  };
+  const int key = shape.rt_warps * 10 + shape.rt_depth;
+  if (shape.rt_regs) {
+    switch (key) {
+      case 162: return go(k_cheb_rtr<16, 2>, 16);
+      case 163: return go(k_cheb_rtr<16, 3>, 16);
+      case 164: return go(k_cheb_rtr<16, 4>, 16);
+      case 124: return go(k_cheb_rtr<12, 4>, 12);
+      case 126: return go(k_cheb_rtr<12, 6>, 12);
+      case 86: return go(k_cheb_rtr<8, 6>, 8);
+    }
+    fail(LEO2D_ERR_BAD_ARG, "8-row step in registers: warps 16 (depth 2, 3, 4), 12 (4, 6) or 8 (6)");
+  }
+  switch (key) {
+    case 83: return go(k_cheb_rt<8, 3, 5>, 8);
+    case 84: return go(k_cheb_rt<8, 4, 6>, 8);
+    case 86: return go(k_cheb_rt<8, 6, 8>, 8);
+    case 123: return go(k_cheb_rt<12, 3, 5>, 12);
+    case 124: return go(k_cheb_rt<12, 4, 6>, 12);
+    case 126: return go(k_cheb_rt<12, 6, 8>, 12);
+    case 163: return go(k_cheb_rt<16, 3, 5>, 16);
+    case 164: return go(k_cheb_rt<16, 4, 6>, 16);
+    case 166: return go(k_cheb_rt<16, 6, 8>, 16);
+    case 243: return go(k_cheb_rt<24, 3, 5>, 24);
+    case 244: return go(k_cheb_rt<24, 4, 6>, 24);
+  }
+  fail(LEO2D_ERR_BAD_ARG, "8-row step: warps 8, 12, 16 (depth 3, 4, 6) or 24 (depth 3, 4)");
+}
+
+}  // namespace leo2d
+
+extern "C" leo2d_status leo2d_csr_rt_info(const leo2d_csr* csr, int64_t* row_blocks, int64_t* ksteps,
+                                          int64_t* union_slots, int32_t* max_slots) {
+  if (!csr) return LEO2D_ERR_BAD_ARG;
+  const bool b = csr->rt_built;
+  if (row_blocks) *row_blocks = b ? csr->rt_blocks : 0;
+  if (ksteps) *ksteps = b ? csr->rt_ksteps : 0;
+  if (union_slots) *union_slots = b ? csr->rt_union : 0;
+  if (max_slots) *max_slots = b ? csr->rt_max_slots : 0;
+  return LEO2D_OK;
+}

@@ -20,13 +20,19 @@ def e2e_text(name, suffix):
         return f.read()
 
 
-def parse_in(name):
+def load_config(name):
+    """Digests of a full-size workload (tests/golden/configs)."""
+    with np.load(os.path.join(GOLDEN, "configs", name + ".npz")) as z:
+        return {k: z[k] for k in z.files}
+
+
+def parse_in(name, folder="inputs"):
     """Reads a fixture's .in with the token rules of main.cpp:75-911 (subset).
 
     Test helper only: the product parser is C++ (leo2d_gb300/host/input.cpp)
     and is checked against the same files.
     """
-    path = os.path.join(GOLDEN, "inputs", name + ".in")
+    path = os.path.join(GOLDEN, folder, name + ".in")
     g = Geom()
     g.sc_search_size = 1
     g.model = MODEL_REF

@@ -1,6 +1,7 @@
 """Host-side helpers of the Python API (no GPU): the k grid of K_TYPE = 0 and the
 row numbering of a matrix with vacancies."""
 import numpy as np
+import pytest
 
 import leo2d_gb300 as L
 from oracle import oracle
@@ -61,3 +62,14 @@ def test_k_path_corners():
     np.testing.assert_allclose(ks[3], [0.0, 0.0], atol=1e-15)
     np.testing.assert_allclose(ks[6], b2 / 2, atol=1e-15)
     np.testing.assert_allclose(np.linalg.norm(ks[0]), np.linalg.norm(b2) / np.sqrt(3), rtol=1e-14)
+
+
+def test_k_path_twisted_zone_needs_two_sheets():
+    """K_TYPE = 1 walks the twisted (supercell) zone: a single layer has none, and
+    the helper refuses it with the reference's message (locality.cpp:1661-1663),
+    as the driver does; the other k lists still run."""
+    g = oracle.geom_prepare(L.make_geom(num_sheets=1, boundary_condition=1, supercell_mn=(4, 5), size=16,
+                                        energy_rescale=13.0))
+    with pytest.raises(ValueError, match="single layer"):
+        L.k_path(g, 4, k_type=1)
+    assert L.k_path(g, 4, k_type=2).shape == (4, 2)
