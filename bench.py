@@ -43,6 +43,8 @@ RADIUS = 2042.0
 P = 1024
 N_E = 4001
 TARGET_L1 = 1e-3
+CPU_STEPS = 4       # Chebyshev steps the CPU baseline times on the full flake
+REF_VECTORS = 13    # vectors the device arm needs for 1e-3 L1 on this flake (its calibration, seeds fixed)
 
 
 def geom(L, radius=RADIUS, twist=TWIST_DEG):
@@ -155,33 +157,59 @@ def max_over_ranks(pg, x):
 
 # ---------------------------------------------------------------- CPU baseline
 
-def cpu_sample(threads, sample_radius=260.0, steps=8, rng_seed=0):
-    """Reference CPU recursion on a bounded sample: a same-model flake of radius
-    `sample_radius` built by the oracle, `threads` vectors on `threads` threads,
-    `steps` Chebyshev steps. Returns seconds per (step, vector-batch) and nnz."""
-    import ctypes
-    import leo2d_gb300 as L
-    from oracle import oracle
-    g = oracle.geom_prepare(geom(L, radius=sample_radius))
-    g.energy_rescale = 14.0
-    b = oracle.Built(g)
-    rp, col, val = b.compact()
-    lib = oracle.lib()
-    lib.oracle_cpu_kpm_steps.restype = ctypes.c_double
-    chk = ctypes.c_double()
-    t = lib.oracle_cpu_kpm_steps(ctypes.c_int64(b.n), oracle._p(np.ascontiguousarray(rp)),
-                                 oracle._p(np.ascontiguousarray(col)),
-                                 oracle._p(np.ascontiguousarray(val)), ctypes.c_int32(threads),
-                                 ctypes.c_int32(steps), ctypes.c_int32(threads), ctypes.byref(chk))
-    return t / steps, len(col), b.n
+class CpuFlake:
+    """The workload's flake built on the host cores (oracle_simple_flake_csr: the
+    simple model's compact Hamiltonian in the reference row order, rescaled by
+    (a, b) as H~ = (H - b) / a), for the CPU baseline at full size."""
 
+    def __init__(self, L, threads, radius=RADIUS, twist=TWIST_DEG, a=None, b=0.0):
+        import ctypes
+        from oracle import oracle
+        self.oracle = oracle
+        lib = oracle.lib()
+        lib.oracle_flake_sites.restype = ctypes.c_int64
+        lib.oracle_simple_flake_csr.restype = ctypes.c_int64
+        g = oracle.geom_prepare(geom(L, radius=radius, twist=twist))
+        t0 = time.perf_counter()
+        n = lib.oracle_flake_sites(ctypes.byref(g))
+        rp = np.zeros(n + 1, np.int64)
+        args = (ctypes.byref(g), ctypes.c_double(1.0 if a is None else a), ctypes.c_double(-b), ctypes.c_int(threads))
+        nnz = lib.oracle_simple_flake_csr(*args, oracle._p(rp), None, None, ctypes.c_int64(0))
+        col = np.empty(nnz, np.int32)
+        val = np.empty(nnz, np.float64)
+        lib.oracle_simple_flake_csr(*args, oracle._p(rp), oracle._p(col), oracle._p(val), ctypes.c_int64(nnz))
+        if a is None:  # Gershgorin bounds x 1.01 of the host-built matrix, then rescale in place
+            lo, hi = oracle.gershgorin(rp, col, val)
+            a, b = 1.01 * (hi - lo) / 2, (hi + lo) / 2
+            diag = np.repeat(np.arange(n, dtype=np.int64), np.diff(rp)) == col
+            val[diag] -= b
+            val /= a
+        self.build_s = time.perf_counter() - t0
+        self.n, self.nnz, self.rp, self.col, self.val, self.a, self.b = n, nnz, rp, col, val, a, b
 
-def cpu_time_to_dos(R, n_full, nnz_full, threads, sample):
-    t_step, nnz_s, n_s = sample
-    # per step every thread advances one vector over the sample; scale by work
-    scale = (nnz_full * 12 + n_full * 40) / (nnz_s * 12 + n_s * 40)
-    batches = math.ceil(R / threads)
-    return batches * (P // 2) * t_step * scale
+    def time_steps(self, threads, steps):
+        """Seconds per Chebyshev step of `threads` vectors on `threads` host threads."""
+        import ctypes
+        lib = self.oracle.lib()
+        lib.oracle_cpu_kpm_steps.restype = ctypes.c_double
+        chk = ctypes.c_double()
+        t = lib.oracle_cpu_kpm_steps(ctypes.c_int64(self.n), self.oracle._p(self.rp), self.oracle._p(self.col),
+                                     self.oracle._p(self.val), ctypes.c_int32(threads), ctypes.c_int32(steps),
+                                     ctypes.c_int32(threads), ctypes.byref(chk))
+        return t / steps
+
+    def moments(self, seed, first, R, P, threads):
+        """FP64 doubling moments of R Philox random-phase vectors (real and imaginary
+        parts summed), the same recursion and vectors as the device's trace."""
+        import ctypes
+        o = self.oracle
+        re, im = o.phase_vectors(seed, first, R, self.n)
+        vec = np.ascontiguousarray(np.concatenate([re, im]))
+        mu = np.zeros((2 * R, P))
+        o.lib().oracle_kpm_trace_doubling_threads(
+            ctypes.c_int64(self.n), o._p(self.rp), o._p(self.col), o._p(self.val), ctypes.c_int32(2 * R),
+            o._p(vec), ctypes.c_int32(P), ctypes.c_int32(threads), o._p(mu))
+        return mu[:R] + mu[R:]
 
 
 # ---------------------------------------------------------------- profiling case
@@ -406,6 +434,155 @@ def run_periodic(args):
            "l1_vs_fp64": l1(d32, d64),
            "fp64_gpu_vs_cpu_oracle_moments": float(np.abs(m64 - mo).max() / np.abs(mo).max()),
            "gpu_launches": int(launches)}
+    print(json.dumps(out))
+    ctx.close()
+
+
+def run_cfg0(args):
+    """Plain KPM DOS in FP64 on the 5.09 deg flake of radius 60 a = 147.6 A (simple
+    model, ~52k orbitals): Gershgorin bounds x 1.01, P = 1000 (Jackson), 16 random-
+    phase vectors, DOS on 4001 energies. value: one DOS from the resident matrix;
+    e2e: from the host geometry through the C ABI; the CPU baseline runs the
+    reference's recursion on the same flake built on the host, in full (no
+    extrapolation), and checks the device's FP64 moments against it."""
+    import torch
+    import leo2d_gb300 as L
+    radius, twist, Pc, R = 60 * 2.46, 5.09, 1000, 16
+    ctx = L.Context(0)
+    g = ctx.prepare(geom(L, radius=radius, twist=twist))
+    csr = ctx.build_csr(g)
+    lo, hi = csr.bounds()
+    a, b = 1.01 * (hi - lo) / 2, (hi + lo) / 2
+    csr.rescale(a, -b)
+    n, nnz = csr.n, csr.nnz
+    x = -1.0 + 2.0 * (np.arange(N_E) + 0.5) / N_E
+    cfg = L.kpm_cfg(Pc, R=R, seed=5, precision=L.FP64)
+    cols, _ = csr.autotune(cfg)
+    kernel_id, _ = csr.step_kernel(cfg)
+    stream = torch.cuda.ExternalStream(ctx.lib.leo2d_ctx_stream(ctx.h))
+    dos = lambda mu, c=csr, aa=a, bb=b: ctx.dos_reconstruct(mu.mean(axis=0), bb + aa * x, aa, bb, 1.0 / c.n)
+    for _ in range(max(args.warmup, 1)):
+        dos(csr.kpm_dos(cfg))
+    ctx.reset_stats()
+    ctx.set_profiling(True)
+    l0 = ctx.launch_count()
+    with Clocks(0) as clk:
+        t, d = _timed(stream, lambda: dos(csr.kpm_dos(cfg)), args.steps, 0)
+    launches = (ctx.launch_count() - l0) // args.steps
+    k_n, k_ms = ctx.kernel_stats("cheb_step")
+    ctx.set_profiling(False)
+
+    def e2e_once():
+        c2 = ctx.build_csr(g)
+        lo2, hi2 = c2.bounds()
+        a2, b2 = 1.01 * (hi2 - lo2) / 2, (hi2 + lo2) / 2
+        c2.rescale(a2, -b2)
+        mu = c2.kpm_dos(cfg)
+        out = dos(mu, c2, a2, b2)
+        c2.close()
+        return mu, out
+
+    e2e_once()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        mu_e, _ = e2e_once()
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    import ctypes
+    peak, peak_kind = peaks()
+    bytes_step = nnz * (4 + 8) + (n + 1) * 8 + 3 * n * cols * 8  # FP64 values and vectors
+    launch_ms = k_ms / k_n
+    achieved = bytes_step / (launch_ms / 1000.0) / 1e9
+    threads = os.cpu_count() or 1
+    cf = CpuFlake(L, threads, radius=radius, twist=twist, a=a, b=b)
+    t_cpu = cf.time_steps(min(threads, R), Pc // 2) * (Pc // 2) * math.ceil(R / min(threads, R))
+    mu_cpu = cf.moments(5, 0, 2, Pc, threads)
+    mu_gpu = csr.kpm_dos(L.kpm_cfg(Pc, R=2, seed=5, precision=L.FP64))
+    out = {"metric": "plain KPM DOS, FP64 (P=1000, 16 random-phase vectors, 4001 energies)",
+           "value": round(t, 6), "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 1),
+           "ms_per_step": round(t * 1000, 3), "higher_is_better": False, "scaling": "strong", "vs_baseline": None,
+           "dtype": "fp64", "data": "synthetic (geometry generated on the GPU; random-phase vectors, Philox)",
+           "config": {"workload": f"TBLG flake {twist} deg, R={radius:.1f} A, {n} orbitals, simple model, "
+                                  f"P={Pc}, {R} random-phase vectors, {N_E} energies",
+                      "orbitals": n, "nnz": nnz, "block_cols": cols,
+                      "l2": "matrix and vector blocks fit the L2 (tens of MB): the steps run from L2"},
+           "e2e": {"value": round(t_e2e, 6), "unit": "s", "h2d_bytes_per_step": ctypes.sizeof(L.Geom),
+                   "d2h_bytes_per_step": int(mu_e.nbytes + N_E * 8)},
+           "gpu_launches": int(launches),
+           "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(achieved / peak, 4), "traffic": None,
+                        "kernel": {0: "k_cheb_tile<double>", 1: "k_cheb_step<double>"}.get(kernel_id, str(kernel_id)),
+                        "bytes_per_launch": bytes_step, "launch_ms": round(launch_ms, 4), "peak_kind": peak_kind,
+                        "note": "working set in L2: the fraction of HBM is a bandwidth figure, not an HBM bound"},
+           "clocks": clk.summary(),
+           "cpu_baseline": {"value": round(t_cpu, 3), "unit": "s", "cores": min(threads, R), "kind": "port",
+                            "sample": f"the whole workload: oracle FP64 recursion, {R} vectors x {Pc // 2} steps on "
+                                      f"{min(threads, R)} threads over the same flake built on the host "
+                                      f"({cf.nnz} entries)"},
+           "parity": {"fp64_gpu_vs_fp64_host_moments_max_rel": float(np.max(np.abs(mu_gpu - mu_cpu)) /
+                                                                     np.max(np.abs(mu_cpu))),
+                      "vectors": 2, "moments": Pc}}
+    print(json.dumps(out))
+    ctx.close()
+
+
+def run_cv_bound(args):
+    """What a perfect control variate could buy: on a 0.5 deg flake of ~1e5 orbitals,
+    the exact moments of every orbital (unit start vectors, FP64-summed FP32
+    recursion, leo2d_kpm_ldos) give the exact trace moments. The plain estimate
+    takes R random-phase vectors; the ideal control variate knows moments 0..255
+    exactly (a surrogate with zero residual) and takes R' phase vectors for the
+    rest. Both are run to 1e-3 L1 of the exact DOS on several independent
+    realisations; time-to-DOS is proportional to the vector count, so R / R' is
+    the largest speed-up any surrogate of the first 256 moments can give."""
+    import leo2d_gb300 as L
+    radius = args.cv_radius
+    P_cv, P_s, seeds = P, 256, (101, 202, 303, 404)
+    ctx = L.Context(0)
+    csr = ctx.build_csr(ctx.prepare(geom(L, radius=radius)))
+    lo, hi = csr.bounds()
+    a, b = 1.01 * (hi - lo) / 2, (hi + lo) / 2
+    csr.rescale(a, -b)
+    n = csr.n
+    E = energies(a, b)
+    dos_of = lambda mu: ctx.dos_reconstruct(mu, E, a, b, 1.0 / n)
+    t0 = time.perf_counter()
+    exact = np.zeros(P_cv)
+    blk = 4096
+    for s0 in range(0, n, blk):
+        tg = np.arange(s0, min(n, s0 + blk), dtype=np.int64)
+        exact += csr.kpm_ldos(L.kpm_cfg(P_cv, R=1), tg).sum(axis=0)
+    t_exact = time.perf_counter() - t0
+    d_exact = dos_of(exact / n)
+    mean_exact = exact / n
+    R_max = args.cv_max_vectors
+    res = []
+    for sd in seeds:
+        ph = csr.kpm_dos(L.kpm_cfg(P_cv, R=R_max, seed=sd))
+        cs = np.cumsum(ph, axis=0)
+        r_plain = r_cv = None
+        for R in range(1, R_max + 1):
+            mu = cs[R - 1] / R
+            if r_plain is None and l1(dos_of(mu), d_exact) <= TARGET_L1:
+                r_plain = R
+            if r_cv is None:
+                mc = mu.copy()
+                mc[:P_s] = mean_exact[:P_s]
+                if l1(dos_of(mc), d_exact) <= TARGET_L1:
+                    r_cv = R
+            if r_plain is not None and r_cv is not None:
+                break
+        res.append((r_plain, r_cv))
+    rp = [x[0] for x in res]
+    rc = [x[1] for x in res]
+    ok = all(x is not None for x in rp + rc)
+    out = {"metric": "time-to-DOS speed-up bound of a perfect control variate of the first 256 moments",
+           "value": round(float(np.mean(rp)) / float(np.mean(rc)), 3) if ok else None, "unit": "x",
+           "higher_is_better": True, "n_gpus": 1, "dtype": "fp32 recursion, fp64 moments", "data": "synthetic",
+           "config": {"workload": f"TBLG flake {TWIST_DEG} deg, R={radius:.0f} A, {n} orbitals, simple model, "
+                                  f"P={P_cv}, {N_E} energies, 1e-3 L1 against the exact DOS",
+                      "orbitals": n, "surrogate_moments": P_s, "realisations": len(seeds)},
+           "plain_vectors": rp, "ideal_cv_vectors": rc, "exact_moments_s": round(t_exact, 1),
+           "note": "time-to-DOS is proportional to the vector count; the ideal surrogate costs nothing here"}
     print(json.dumps(out))
     ctx.close()
 
@@ -683,9 +860,15 @@ def main():
                     help="kubo2m: flake size in orbitals (smaller cases for profiling)")
     ap.add_argument("--kubo-moments", type=int, default=512, help="kubo2m: M of the M x M moments")
     ap.add_argument("--kubo-vectors", type=int, default=32, help="kubo2m: random-phase vectors")
+    ap.add_argument("--cv-radius", type=float, default=205.0,
+                    help="cvbound: flake radius (A); 205 A is about 1e5 orbitals")
+    ap.add_argument("--cv-max-vectors", type=int, default=4096, help="cvbound: most phase vectors tried")
     ap.add_argument("--workload", default="flake10m",
-                    choices=["flake10m", "batch32", "periodic", "kubo2m", "mlp", "bfield"],
-                    help="flake10m: time-to-DOS on the 10M-orbital flake (the headline); batch32: 32 "
+                    choices=["flake10m", "cfg0", "cvbound", "batch32", "periodic", "kubo2m", "mlp", "bfield"],
+                    help="flake10m: time-to-DOS on the 10M-orbital flake (the headline); cfg0: FP64 DOS of the "
+                         "5.09 deg flake of ~52k orbitals, P=1000, 16 vectors; cvbound: the speed-up a perfect "
+                         "control variate of the first 256 moments could give (exact site moments of a ~1e5-orbital "
+                         "flake); batch32: 32 "
                          "flakes of 20k-500k orbitals in one batched, graph-replayed run; periodic: the "
                          "1.05 deg (31,32) supercell, P=4096, 64 vectors, FP32 vs FP64 per energy; kubo2m: "
                          "sigma_xx(E) of a 2M-orbital 1.5 deg flake, 512x512 moments, 32 vectors; mlp: the "
@@ -700,6 +883,10 @@ def main():
     args = ap.parse_args()
     if args.kernel_case:
         return kernel_case(args)
+    if args.workload == "cvbound" and args.impl == "ours":
+        return run_cv_bound(args)
+    if args.workload == "cfg0" and args.impl == "ours":
+        return run_cfg0(args)
     if args.workload == "batch32" and args.impl == "ours":
         return run_batch(args)
     if args.workload == "periodic" and args.impl == "ours":
@@ -869,49 +1056,56 @@ def main():
         "cv": cv,
     }
     if rank == 0 and ws == 1:
-        sample = cpu_sample(threads)
-        cpu_t = cpu_time_to_dos(R_needed, n, nnz, threads, sample)
-        out["cpu_baseline"] = {"value": round(cpu_t, 3), "unit": UNIT, "cores": threads,
-                               "kind": "port",
-                               "sample": f"oracle FP64 recursion, {threads} vectors on {threads} "
-                                         f"threads, 8 steps on a {sample[2]}-orbital flake of the "
-                                         f"same model, scaled by bytes to {n} orbitals x "
-                                         f"{R_needed} vectors x {P // 2} steps"}
+        # the reference's CPU recursion on the same full-size flake, built on the
+        # host cores with the same rescale; and its FP64 moments of one of the
+        # timed phase vectors against the device's FP32 ones
+        cf = CpuFlake(L, threads, a=a, b=b)
+        cf.time_steps(threads, 1)  # warm
+        t_step = cf.time_steps(threads, CPU_STEPS)
+        cpu_t = math.ceil(R_needed / threads) * (P // 2) * t_step
+        out["cpu_baseline"] = {"value": round(cpu_t, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"oracle FP64 recursion (the reference's in-tree SpMV loop per vector) on "
+                                         f"the full {cf.n}-orbital flake built on the host ({cf.nnz} entries), "
+                                         f"{threads} vectors on {threads} threads, {CPU_STEPS} timed steps of "
+                                         f"{t_step:.3f} s; x {P // 2} steps x {math.ceil(R_needed / threads)} "
+                                         f"batch(es) for {R_needed} vectors",
+                               "host_build_s": round(cf.build_s, 2)}
+        Pc = 16
+        mu_cpu = cf.moments(7, 0, 1, Pc, threads)
+        mu_gpu = csr.kpm_dos(L.kpm_cfg(Pc, R=1, seed=7))
+        out["parity_full_size"] = {
+            "orbitals": n, "gpu_entries": nnz, "host_entries": cf.nnz, "moments": Pc, "vectors": 1,
+            "fp32_gpu_vs_fp64_host_max_rel": float(np.max(np.abs(mu_gpu - mu_cpu)) / np.max(np.abs(mu_cpu)))}
+        del cf
     if rank == 0:
         print(json.dumps(out))
     ctx.close()
 
 
 def run_reference(args, threads):
-    """CPU reference arm: the oracle port of the reference recursion on host cores."""
+    """CPU reference arm: the oracle port of the reference recursion (Locality::
+    computeDosTraceKPM with SpMatrix::vectorMultiply's in-tree loop, one vector per
+    worker) on the host cores, on the full 10M-orbital flake built on the host.
+    A step is one Chebyshev step of `threads` vectors on `threads` threads;
+    value = the mean timed step x P/2 steps x the vector batches R needs."""
     import leo2d_gb300 as L
-    from oracle import oracle
-    # sizes of the full workload from the oracle geometry formula (no GPU used)
-    steps_timed = []
-    sample = None
-    for _ in range(args.warmup):
-        cpu_sample(threads, sample_radius=180.0, steps=2)
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        sample = cpu_sample(threads)
-        steps_timed.append(time.perf_counter() - t0)
-    # full-size orbital and entry counts: area scaling of the sample flake
-    t_step, nnz_s, n_s = sample
-    scale_n = (RADIUS / 260.0) ** 2
-    n_full = int(n_s * scale_n)
-    nnz_full = int(nnz_s * scale_n)
-    R = int(os.environ.get("LEO2D_BENCH_VECTORS", "16"))
-    v = cpu_time_to_dos(R, n_full, nnz_full, threads, sample)
+    cf = CpuFlake(L, threads)
+    cf.time_steps(threads, max(1, args.warmup))
+    t_step = cf.time_steps(threads, max(1, args.steps))
+    R = int(os.environ.get("LEO2D_BENCH_VECTORS", str(REF_VECTORS)))
+    v = math.ceil(R / threads) * (P // 2) * t_step
     out = {"impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": UNIT,
            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-           "ms_per_step": round(float(np.mean(steps_timed)) * 1000, 1), "higher_is_better": False,
+           "ms_per_step": round(t_step * 1000, 1), "higher_is_better": False,
            "scaling": "strong", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
-           "config": {"workload": f"TBLG flake {TWIST_DEG} deg, R={RADIUS:.0f} A, ~{n_full} orbitals, "
-                                  f"simple model, P={P}", "vectors": R},
+           "config": {"workload": f"TBLG flake {TWIST_DEG} deg, R={RADIUS:.0f} A, {cf.n} orbitals, "
+                                  f"simple model, P={P}, {N_E} energies", "orbitals": cf.n, "nnz": cf.nnz,
+                      "vectors": R},
            "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": threads, "kind": "port",
-                            "sample": f"oracle FP64 recursion on a {n_s}-orbital flake, {threads} "
-                                      f"vectors x 8 steps, scaled to {n_full} orbitals x {R} "
-                                      f"vectors x {P // 2} steps"},
+                            "sample": f"oracle FP64 recursion on the full {cf.n}-orbital flake built on the host "
+                                      f"({cf.nnz} entries, {cf.build_s:.1f} s), {threads} vectors on {threads} "
+                                      f"threads, {max(1, args.steps)} timed steps of {t_step:.3f} s; "
+                                      f"x {P // 2} steps x {math.ceil(R / threads)} batch(es) for {R} vectors"},
            "e2e": {"value": round(v, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 

@@ -79,17 +79,6 @@ __device__ __forceinline__ void prefetch_l2_bulk(const void* p, uint32_t bytes) 
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-// x = hi + lo with hi, lo TF32 values (bit patterns for mma .tf32 operands)
-__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
-  uint32_t h;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
-  const float r = x - __uint_as_float(h);
-  uint32_t l;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(r));
-  hi = h;
-  lo = l;
-}
-
 __device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
                                          uint32_t b0, uint32_t b1) {
   asm volatile(
@@ -116,213 +105,52 @@ struct RtArgs {
   int chunk;        // consecutive tiles per CTA between grid-wide jumps
 };
 
-// Block index of the j-th block of warp w of CTA bid (the build's processing order).
-__device__ __forceinline__ int64_t rt_block_of(int64_t j, int w, int W, int G, int chunk, int bid, int nblk) {
-  const int64_t i = j / G;
-  const int64_t tile = ((int64_t)bid + (i / chunk) * (int64_t)nblk) * chunk + i % chunk;
-  return (tile * W + w) * G + j % G;
-}
-
 }  // namespace
 
 namespace {
 
-// ---------------------------------------------------------------- the step kernel
+// ---------------------------------------------------------------- the step kernels
 
-template <int W, int D, int DM>
-__global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ RtArgs a) {
-  constexpr int C = 32;
-  constexpr int NT = W * 32;
-  constexpr int XS = D + 1;       // ring of staged T_n rows (k-steps)
-  constexpr int MS = D + DM + 1;  // ring of matrix k-steps
-  constexpr int kWarpBytes = XS * 1024 + MS * kRtStepBytes;
-  constexpr int kPf = 32;         // matrix k-steps prefetched into L2 ahead of the copies
-  static_assert(DM >= D + 1, "the matrix lookahead must exceed the row lookahead");
-  extern __shared__ __align__(1024) unsigned char rt_smem[];
-  const int bid = (int)blockIdx.x, nblk = (int)gridDim.x;
-  if (a.prev_partials) reduce_prev<C, NT>(a.prev_partials, a.prev_dots, nblk, bid, nblk);
-
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int g = lane >> 2, t = lane & 3;        // MMA fragment coordinates
-  const int q = lane >> 3, p = lane & 7;        // copies: slots q and q + 4, 16-byte chunk p
-  const int cg = (g >> 1) | ((g & 1) << 2);     // the lane's chunk of 4 columns
-  unsigned char* xr = rt_smem + (size_t)warp * kWarpBytes;
-  unsigned char* mr = xr + XS * 1024;
-  const int64_t k0 = a.wbeg[bid * W + warp];
-  const int nk = (int)(a.wbeg[bid * W + warp + 1] - k0);
-  const unsigned char* gdata = a.data + k0 * kRtStepBytes;
-  const float alpha = a.alpha != 0.f ? a.alpha : (a.first ? 1.f : 2.f);
-  const float* tprev = a.tprev ? a.tprev : a.tp;
-  const float* tnc = a.tn + 4 * cg;
-
-  // dots: FP32 over kDotFlush blocks, then FP64; lane (g, t) ends with column 4 cg + t
-  constexpr int kDotFlush = 16;
-  double d0 = 0.0, d1 = 0.0;
-  float e0[4], e1[4];
+// FP32 products from TF32 units: x = hi + lo with hi = x with its low 13
+// mantissa bits cleared (a TF32 value) and lo = x - hi (exact) cleared the same
+// way; the product is taken as lo*hi + hi*lo + hi*hi. The dropped lo*lo term and
+// the truncation of lo leave a relative error below 2^-20 per product. The
+// hi*hi terms and the two cross terms go to separate FP32 accumulators (four
+// independent MMA chains per k-step), summed at the block's end.
+struct RtAcc {
+  float h0[4], h1[4], l0[4], l1[4];  // m-tiles 0 (logical columns 0..15) and 1 (16..31)
+  __device__ __forceinline__ void zero() {
 #pragma unroll
-  for (int c = 0; c < 4; ++c) e0[c] = e1[c] = 0.f;
-  auto flush = [&]() {
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      e0[c] += __shfl_xor_sync(0xffffffffu, e0[c], 1);
-      e1[c] += __shfl_xor_sync(0xffffffffu, e1[c], 1);
-      e0[c] += __shfl_xor_sync(0xffffffffu, e0[c], 2);
-      e1[c] += __shfl_xor_sync(0xffffffffu, e1[c], 2);
-    }
-    float v0 = e0[0], v1 = e1[0];
-#pragma unroll
-    for (int c = 1; c < 4; ++c)
-      if (t == c) {
-        v0 = e0[c];
-        v1 = e1[c];
-      }
-    d0 += (double)v0;
-    d1 += (double)v1;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) e0[c] = e1[c] = 0.f;
-  };
-
-  float acc0[4], acc1[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) acc0[i] = acc1[i] = 0.f;
-  float4 xn0 = make_float4(0.f, 0.f, 0.f, 0.f), xn1 = xn0, xp0 = xn0, xp1 = xn0;
-  int64_t jblk = 0, row0 = 0;
-  bool start = true;
-  int since_flush = 0;
-  // ring slots: im of matrix k-step u + D + DM, ix of row k-step u + D
-  int im = 0;
-  int ix = (XS - (DM % XS)) % XS;
-  for (int u = -(D + DM); u < nk; ++u) {
-    __syncwarp();  // every lane is done with the entries these copies overwrite
-    const int vm = u + D + DM, vx = u + D;
-    if (vm < nk && lane < kRtStepBytes / 16)
-      cp_async_cg16(mr + im * kRtStepBytes + 16 * lane, gdata + (size_t)vm * kRtStepBytes + 16 * lane);
-    if (lane == 0 && (vm & 7) == 0 && vm + kPf < nk)
-      prefetch_l2_bulk(gdata + (size_t)(vm + kPf) * kRtStepBytes, (uint32_t)min(8, nk - vm - kPf) * kRtStepBytes);
-    if (vx >= 0 && vx < nk) {
-      // the columns of k-step vx landed DM iterations ago (slot im - DM)
-      const int jm = im >= DM ? im - DM : im + MS - DM;
-      const int2 cc = *reinterpret_cast<const int2*>(mr + jm * kRtStepBytes + 8 * q);
-      unsigned char* dst = xr + ix * 1024;
-      cp_async_ca16(dst + q * 128 + 16 * (p ^ q), a.tn + (size_t)(uint32_t)(cc.x & 0x7fffffff) * C + 4 * p);
-      cp_async_ca16(dst + (q + 4) * 128 + 16 * (p ^ (q + 4)),
-                    a.tn + (size_t)(uint32_t)(cc.y & 0x7fffffff) * C + 4 * p);
-    }
-    cp_async_commit();
-    cp_async_wait<D>();  // k-step u's rows (and k-step u + D + 1's matrix data) have landed
-    __syncwarp();
-    const int sm = im == MS - 1 ? 0 : im + 1;  // slot of matrix k-step u
-    const int sx = ix == XS - 1 ? 0 : ix + 1;  // slot of row k-step u
-    im = sm;
-    ix = sx;
-    if (u < 0) continue;
-    if (start) {
-      const int64_t blk = rt_block_of(jblk, warp, W, a.group, a.chunk, bid, nblk);
-      row0 = blk * kRtRows;
-      const int64_t r0 = row0 + 2 * t;
-      if (r0 < a.n) {
-        xn0 = ldg4(tnc + r0 * C);
-        if (!a.first) xp0 = ld_once4(tprev + r0 * C + 4 * cg);
-      }
-      if (r0 + 1 < a.n) {
-        xn1 = ldg4(tnc + (r0 + 1) * C);
-        if (!a.first) xp1 = ld_once4(tprev + (r0 + 1) * C + 4 * cg);
-      }
-      start = false;
-    }
-    const unsigned char* xs = xr + sx * 1024;
-    const unsigned char* ms = mr + sm * kRtStepBytes;
-    const float4 xa = *reinterpret_cast<const float4*>(xs + t * 128 + 16 * (cg ^ t));
-    const float4 xb = *reinterpret_cast<const float4*>(xs + (t + 4) * 128 + 16 * (cg ^ (t + 4)));
-    const float2 vv = *reinterpret_cast<const float2*>(ms + 32 + 8 * lane);
-    const bool last = *reinterpret_cast<const int*>(ms + 28) < 0;
-    uint32_t ah[8], al[8], bh0, bl0, bh1, bl1;
-    split_tf32(xa.x, ah[0], al[0]);
-    split_tf32(xa.y, ah[1], al[1]);
-    split_tf32(xa.z, ah[2], al[2]);
-    split_tf32(xa.w, ah[3], al[3]);
-    split_tf32(xb.x, ah[4], al[4]);
-    split_tf32(xb.y, ah[5], al[5]);
-    split_tf32(xb.z, ah[6], al[6]);
-    split_tf32(xb.w, ah[7], al[7]);
-    split_tf32(vv.x, bh0, bl0);
-    split_tf32(vv.y, bh1, bl1);
-    // columns 0..15 (logical g, g + 8) and 16..31 (g + 16, g + 24): lo*hi + hi*lo + hi*hi
-    mma_tf32(acc0, al[0], al[1], al[4], al[5], bh0, bh1);
-    mma_tf32(acc1, al[2], al[3], al[6], al[7], bh0, bh1);
-    mma_tf32(acc0, ah[0], ah[1], ah[4], ah[5], bl0, bl1);
-    mma_tf32(acc1, ah[2], ah[3], ah[6], ah[7], bl0, bl1);
-    mma_tf32(acc0, ah[0], ah[1], ah[4], ah[5], bh0, bh1);
-    mma_tf32(acc1, ah[2], ah[3], ah[6], ah[7], bh0, bh1);
-    if (last) {  // warp-uniform: the block's epilogue
-      const int64_t r0 = row0 + 2 * t;
-      const float4 h0 = make_float4(acc0[0], acc0[2], acc1[0], acc1[2]);  // row 2t
-      const float4 h1 = make_float4(acc0[1], acc0[3], acc1[1], acc1[3]);  // row 2t + 1
-      float4 y0, y1;
-      if (a.first) {
-        y0 = make_float4(alpha * h0.x, alpha * h0.y, alpha * h0.z, alpha * h0.w);
-        y1 = make_float4(alpha * h1.x, alpha * h1.y, alpha * h1.z, alpha * h1.w);
-      } else {
-        y0 = make_float4(alpha * h0.x - xp0.x, alpha * h0.y - xp0.y, alpha * h0.z - xp0.z, alpha * h0.w - xp0.w);
-        y1 = make_float4(alpha * h1.x - xp1.x, alpha * h1.y - xp1.y, alpha * h1.z - xp1.z, alpha * h1.w - xp1.w);
-      }
-      if (r0 < a.n) {
-        st_na4(a.tp + r0 * C + 4 * cg, y0);
-        e0[0] += xn0.x * xn0.x;
-        e0[1] += xn0.y * xn0.y;
-        e0[2] += xn0.z * xn0.z;
-        e0[3] += xn0.w * xn0.w;
-        e1[0] += y0.x * xn0.x;
-        e1[1] += y0.y * xn0.y;
-        e1[2] += y0.z * xn0.z;
-        e1[3] += y0.w * xn0.w;
-      }
-      if (r0 + 1 < a.n) {
-        st_na4(a.tp + (r0 + 1) * C + 4 * cg, y1);
-        e0[0] += xn1.x * xn1.x;
-        e0[1] += xn1.y * xn1.y;
-        e0[2] += xn1.z * xn1.z;
-        e0[3] += xn1.w * xn1.w;
-        e1[0] += y1.x * xn1.x;
-        e1[1] += y1.y * xn1.y;
-        e1[2] += y1.z * xn1.z;
-        e1[3] += y1.w * xn1.w;
-      }
-#pragma unroll
-      for (int i = 0; i < 4; ++i) acc0[i] = acc1[i] = 0.f;
-      ++jblk;
-      start = true;
-      if (++since_flush == kDotFlush) {
-        since_flush = 0;
-        flush();
-      }
-    }
+    for (int i = 0; i < 4; ++i) h0[i] = h1[i] = l0[i] = l1[i] = 0.f;
   }
-  cp_async_wait<0>();
-  flush();
-  // warps add their columns in warp order (deterministic)
-  __shared__ double bsum[2 * C];
-  for (int i = threadIdx.x; i < 2 * C; i += NT) bsum[i] = 0.0;
-  __syncthreads();
-  const int col = 4 * cg + t;
-  for (int w = 0; w < W; ++w) {
-    if (warp == w) {
-      bsum[2 * col] += d0;
-      bsum[2 * col + 1] += d1;
+  // fa, fb: chunk cg of the T_n rows of slots t and t + 4; v: (V[g][t], V[g][t+4])
+  __device__ __forceinline__ void add(const float4& fa, const float4& fb, const float2& v) {
+    constexpr uint32_t m = 0xffffe000u;
+    const float xs[8] = {fa.x, fa.y, fa.z, fa.w, fb.x, fb.y, fb.z, fb.w};
+    uint32_t ah[8], al[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      ah[i] = __float_as_uint(xs[i]) & m;
+      al[i] = __float_as_uint(xs[i] - __uint_as_float(ah[i])) & m;
     }
-    __syncthreads();
+    const uint32_t bh0 = __float_as_uint(v.x) & m, bh1 = __float_as_uint(v.y) & m;
+    const uint32_t bl0 = __float_as_uint(v.x - __uint_as_float(bh0)) & m;
+    const uint32_t bl1 = __float_as_uint(v.y - __uint_as_float(bh1)) & m;
+    // logical columns g, g + 8 (m-tile 0) and g + 16, g + 24 (m-tile 1)
+    mma_tf32(l0, al[0], al[1], al[4], al[5], bh0, bh1);
+    mma_tf32(l1, al[2], al[3], al[6], al[7], bh0, bh1);
+    mma_tf32(h0, ah[0], ah[1], ah[4], ah[5], bh0, bh1);
+    mma_tf32(h1, ah[2], ah[3], ah[6], ah[7], bh0, bh1);
+    mma_tf32(l0, ah[0], ah[1], ah[4], ah[5], bl0, bl1);
+    mma_tf32(l1, ah[2], ah[3], ah[6], ah[7], bl0, bl1);
   }
-  for (int i = threadIdx.x; i < 2 * C; i += NT) a.partials[(size_t)bid * 2 * C + i] = bsum[i];
-}
+  // rows 2t and 2t + 1 of the block, memory columns 4 cg .. 4 cg + 3
+  __device__ __forceinline__ void rows(float4& r0, float4& r1) const {
+    r0 = make_float4(h0[0] + l0[0], h0[2] + l0[2], h1[0] + l1[0], h1[2] + l1[2]);
+    r1 = make_float4(h0[1] + l0[1], h0[3] + l0[3], h1[1] + l1[1], h1[3] + l1[3]);
+  }
+};
 
-// The same step with every operand in registers (no shared memory, so the whole
-// L1 caches T_n rows): lane (q, p) loads 16-byte chunk p of the T_n rows of slots
-// q and q + 4 (one 128-byte row per quarter-warp, one L1 wavefront per slot) U
-// k-steps ahead, and the A fragments are gathered from those registers with
-// eight shuffles per k-step (lane (g, t) takes chunk cg of slots t and t + 4 from
-// lane 8t + cg). The matrix stream is read with plain loads that skip L1: the
-// columns 2U k-steps ahead (they address the row loads), the values U ahead, and
-// kPf k-steps further the stream is prefetched into L2 in bulk.
 __device__ __forceinline__ int2 ld_stream_i2(const void* p) {
   int2 r;
   asm volatile("ld.global.nc.L1::no_allocate.v2.s32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "l"(p));
@@ -334,32 +162,61 @@ __device__ __forceinline__ float2 ld_stream_f2(const void* p) {
   return r;
 }
 
-template <int W, int U>
-__global__ void __launch_bounds__(W * 32, 1) k_cheb_rtr(const __grid_constant__ RtArgs a) {
+// One kernel, two ways of staging the gathered T_n rows:
+//  - REGS = false: cp.async copies into a per-warp shared-memory ring (see the
+//    file comment), D k-steps ahead, the matrix data DM ahead of those;
+//  - REGS = true: no shared memory, so the whole L1 caches T_n rows. Lane (q, p)
+//    loads 16-byte chunk p of the T_n rows of slots q and q + 4 (one 128-byte row
+//    per quarter-warp, one L1 wavefront per slot) D k-steps ahead into registers,
+//    and the A fragments are gathered from those registers with eight shuffles
+//    per k-step (lane (g, t) takes chunk cg of slots t and t + 4 from lane
+//    8t + cg). The matrix stream is read with loads that skip L1: the columns 2D
+//    k-steps ahead (they address the row loads), the values D ahead.
+// Either way the matrix stream is prefetched into L2 in bulk further ahead.
+// Each warp walks its blocks in the build's processing order: runs of G
+// consecutive blocks, run i in tile (bid + (i / chunk) grid) chunk + i % chunk.
+template <int W, int D, int DM, bool REGS>
+__global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ RtArgs a) {
   constexpr int C = 32;
   constexpr int NT = W * 32;
-  constexpr int kPf = 48;  // matrix k-steps prefetched into L2 ahead of the loads
+  constexpr int XS = D + 1;       // shared ring of staged T_n rows (k-steps)
+  constexpr int MS = D + DM + 1;  // shared ring of matrix k-steps
+  constexpr int kWarpBytes = REGS ? 0 : XS * 1024 + MS * kRtStepBytes;
+  constexpr int kPf = REGS ? 48 : 32;  // matrix k-steps prefetched into L2 ahead
+  constexpr int kDotFlush = 16;        // blocks summed in FP32 between FP64 flushes
+  static_assert(REGS || DM >= D + 1, "the matrix lookahead must exceed the row lookahead");
+  extern __shared__ __align__(1024) unsigned char rt_smem[];
   const int bid = (int)blockIdx.x, nblk = (int)gridDim.x;
   if (a.prev_partials) reduce_prev<C, NT>(a.prev_partials, a.prev_dots, nblk, bid, nblk);
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int g = lane >> 2, t = lane & 3;
-  const int q = lane >> 3, p = lane & 7;
-  const int cg = (g >> 1) | ((g & 1) << 2);
-  const int src = 8 * t + cg;  // the lane holding chunk cg of slots t and t + 4
+  const int g = lane >> 2, t = lane & 3, q = lane >> 3, p = lane & 7;
+  const int cg = (g >> 1) | ((g & 1) << 2);  // the lane's chunk of 4 memory columns
+  const int64_t n = a.n;
+  const int first = a.first, group = a.group, chunk = a.chunk;
+  const float alpha = a.alpha != 0.f ? a.alpha : (first ? 1.f : 2.f);
+  const float* tprev = a.tprev ? a.tprev : a.tp;
+  float* tp = a.tp;
+  const float* tnc = a.tn + 4 * cg;
+  const float* tnp = a.tn + 4 * p;
   const int64_t k0 = a.wbeg[bid * W + warp];
   const int nk = (int)(a.wbeg[bid * W + warp + 1] - k0);
   const unsigned char* gdata = a.data + k0 * kRtStepBytes;
-  const float alpha = a.alpha != 0.f ? a.alpha : (a.first ? 1.f : 2.f);
-  const float* tprev = a.tprev ? a.tprev : a.tp;
-  const float* tnc = a.tn + 4 * cg;
-  const float* tnp = a.tn + 4 * p;
 
-  constexpr int kDotFlush = 16;
+  // block walk and epilogue operands
+  int jb = 0, irun = 0;
+  auto run_row0 = [&](int i) -> int64_t {
+    const int tile = (bid + (i / chunk) * nblk) * chunk + i % chunk;
+    return ((int64_t)tile * W + warp) * group * kRtRows;
+  };
+  int64_t rbase = run_row0(0), row0 = 0;
+  float4 xn0 = make_float4(0.f, 0.f, 0.f, 0.f), xn1 = xn0, xp0 = xn0, xp1 = xn0;
+  // dots: FP32 over kDotFlush blocks, then FP64; lane (g, t) ends with column 4 cg + t
   double d0 = 0.0, d1 = 0.0;
   float e0[4], e1[4];
 #pragma unroll
   for (int c = 0; c < 4; ++c) e0[c] = e1[c] = 0.f;
+  int since_flush = 0;
   auto flush = [&]() {
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
@@ -380,144 +237,170 @@ __global__ void __launch_bounds__(W * 32, 1) k_cheb_rtr(const __grid_constant__ 
 #pragma unroll
     for (int c = 0; c < 4; ++c) e0[c] = e1[c] = 0.f;
   };
-
-  float acc0[4], acc1[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) acc0[i] = acc1[i] = 0.f;
-  float4 xn0 = make_float4(0.f, 0.f, 0.f, 0.f), xn1 = xn0, xp0 = xn0, xp1 = xn0;
-  int64_t jblk = 0, row0 = 0;
-  bool start = true;
-  int since_flush = 0;
-
-  // rings (slot j = k-step mod U): columns of k-steps u + U .. u + 2U - 1, rows,
-  // values and block-end flags of k-steps u .. u + U - 1
-  int2 cc[U];
-  float4 xa[U], xb[U];
-  float2 vv[U];
-  bool lastf[U];
-  auto load_cols = [&](int v) { return ld_stream_i2(gdata + (size_t)v * kRtStepBytes + 8 * q); };
-  auto issue = [&](int j, int v) {  // k-step v (its columns in cc[j]) into slot j
-    const int2 c = cc[j];
-    lastf[j] = __any_sync(0xffffffffu, q == 3 && c.y < 0);
-    xa[j] = ldg4(tnp + (size_t)(uint32_t)(c.x & 0x7fffffff) * C);
-    xb[j] = ldg4(tnp + (size_t)(uint32_t)(c.y & 0x7fffffff) * C);
-    vv[j] = ld_stream_f2(gdata + (size_t)v * kRtStepBytes + 32 + 8 * lane);
-  };
-#pragma unroll
-  for (int j = 0; j < U; ++j) {
-    if (j < nk) cc[j] = load_cols(j);
-    if (lane == 0 && j == 0 && kPf < nk)
-      prefetch_l2_bulk(gdata + (size_t)kPf * kRtStepBytes, (uint32_t)min(8, nk - kPf) * kRtStepBytes);
-  }
-#pragma unroll
-  for (int j = 0; j < U; ++j) {
-    if (j < nk) {
-      issue(j, j);
-      if (j + U < nk) cc[j] = load_cols(j + U);
+  auto begin_block = [&]() {
+    row0 = rbase + (int64_t)jb * kRtRows;
+    const int64_t r0 = row0 + 2 * t;
+    if (r0 < n) {
+      xn0 = ldg4(tnc + r0 * C);
+      if (!first) xp0 = ld_once4(tprev + r0 * C + 4 * cg);
     }
-  }
-  for (int u0 = 0; u0 < nk; u0 += U) {
-#pragma unroll
-    for (int j = 0; j < U; ++j) {
-      const int u = u0 + j;
-      if (u >= nk) break;  // warp-uniform
+    if (r0 + 1 < n) {
+      xn1 = ldg4(tnc + (r0 + 1) * C);
+      if (!first) xp1 = ld_once4(tprev + (r0 + 1) * C + 4 * cg);
+    }
+  };
+  auto row_out = [&](int64_t r, const float4& h, const float4& xp, const float4& xn) {
+    if (r >= n) return;
+    const float4 y = first ? make_float4(alpha * h.x, alpha * h.y, alpha * h.z, alpha * h.w)
+                           : make_float4(alpha * h.x - xp.x, alpha * h.y - xp.y, alpha * h.z - xp.z,
+                                         alpha * h.w - xp.w);
+    st_na4(tp + r * C + 4 * cg, y);
+    e0[0] += xn.x * xn.x;
+    e0[1] += xn.y * xn.y;
+    e0[2] += xn.z * xn.z;
+    e0[3] += xn.w * xn.w;
+    e1[0] += y.x * xn.x;
+    e1[1] += y.y * xn.y;
+    e1[2] += y.z * xn.z;
+    e1[3] += y.w * xn.w;
+  };
+  RtAcc acc;
+  acc.zero();
+  auto end_block = [&]() {
+    float4 h0, h1;
+    acc.rows(h0, h1);
+    acc.zero();
+    const int64_t r0 = row0 + 2 * t;
+    row_out(r0, h0, xp0, xn0);
+    row_out(r0 + 1, h1, xp1, xn1);
+    if (++jb == group) {
+      jb = 0;
+      rbase = run_row0(++irun);
+    }
+    if (++since_flush == kDotFlush) {
+      since_flush = 0;
+      flush();
+    }
+  };
+  bool start = true;
+
+  if constexpr (!REGS) {
+    unsigned char* xr = rt_smem + (size_t)warp * kWarpBytes;
+    unsigned char* mr = xr + XS * 1024;
+    const unsigned char* msrc = gdata + 16 * lane;
+    // per-lane offsets in a row-ring entry: writes (slot q and q + 4, chunk p) and
+    // reads (slot t and t + 4, chunk cg), 16-byte chunk c of row s at c ^ s
+    const int wo0 = q * 128 + 16 * (p ^ q), wo1 = 512 + q * 128 + 16 * (p ^ (q + 4));
+    const int ro0 = t * 128 + 16 * (cg ^ t), ro1 = 512 + t * 128 + 16 * (cg ^ (t + 4));
+    int im = 0;                      // matrix slot of k-step u + D + DM
+    int ix = (XS - (DM % XS)) % XS;  // row slot of k-step u + D
+    for (int u = -(D + DM); u < nk; ++u) {
+      __syncwarp();  // every lane is done with the entries these copies overwrite
+      const int vm = u + D + DM, vx = u + D;
+      if (vm < nk && lane < kRtStepBytes / 16) cp_async_cg16(mr + im * kRtStepBytes + 16 * lane, msrc);
+      msrc += kRtStepBytes;
+      if (lane == 0 && (vm & 7) == 0 && vm + kPf < nk)
+        prefetch_l2_bulk(gdata + (size_t)(vm + kPf) * kRtStepBytes,
+                         (uint32_t)min(8, nk - vm - kPf) * kRtStepBytes);
+      if (vx >= 0 && vx < nk) {
+        // the columns of k-step vx landed DM iterations ago (slot im - DM)
+        const int jm = im >= DM ? im - DM : im + MS - DM;
+        const int2 cc = *reinterpret_cast<const int2*>(mr + jm * kRtStepBytes + 8 * q);
+        unsigned char* dst = xr + ix * 1024;
+        cp_async_ca16(dst + wo0, tnp + (size_t)(uint32_t)(cc.x & 0x7fffffff) * C);
+        cp_async_ca16(dst + wo1, tnp + (size_t)(uint32_t)(cc.y & 0x7fffffff) * C);
+      }
+      cp_async_commit();
+      cp_async_wait<D>();  // k-step u's rows (and k-step u + D + 1's matrix data) have landed
+      __syncwarp();
+      im = im == MS - 1 ? 0 : im + 1;  // now the slot of matrix k-step u
+      ix = ix == XS - 1 ? 0 : ix + 1;  // now the slot of row k-step u
+      if (u < 0) continue;
       if (start) {
-        const int64_t blk = rt_block_of(jblk, warp, W, a.group, a.chunk, bid, nblk);
-        row0 = blk * kRtRows;
-        const int64_t r0 = row0 + 2 * t;
-        if (r0 < a.n) {
-          xn0 = ldg4(tnc + r0 * C);
-          if (!a.first) xp0 = ld_once4(tprev + r0 * C + 4 * cg);
-        }
-        if (r0 + 1 < a.n) {
-          xn1 = ldg4(tnc + (r0 + 1) * C);
-          if (!a.first) xp1 = ld_once4(tprev + (r0 + 1) * C + 4 * cg);
-        }
+        begin_block();
         start = false;
       }
-      // A fragments: chunk cg of slots t and t + 4 from lane 8t + cg
-      float4 fa, fb;
-      fa.x = __shfl_sync(0xffffffffu, xa[j].x, src);
-      fa.y = __shfl_sync(0xffffffffu, xa[j].y, src);
-      fa.z = __shfl_sync(0xffffffffu, xa[j].z, src);
-      fa.w = __shfl_sync(0xffffffffu, xa[j].w, src);
-      fb.x = __shfl_sync(0xffffffffu, xb[j].x, src);
-      fb.y = __shfl_sync(0xffffffffu, xb[j].y, src);
-      fb.z = __shfl_sync(0xffffffffu, xb[j].z, src);
-      fb.w = __shfl_sync(0xffffffffu, xb[j].w, src);
-      const float2 v = vv[j];
-      const bool last = lastf[j];
-      // the slot is free: k-step u + U goes into it, and the columns of u + 2U
-      if (u + U < nk) {
-        issue(j, u + U);
-        if (u + 2 * U < nk) cc[j] = load_cols(u + 2 * U);
-      }
-      if (lane == 0 && ((u + U) & 7) == 0 && u + U + kPf < nk)
-        prefetch_l2_bulk(gdata + (size_t)(u + U + kPf) * kRtStepBytes,
-                         (uint32_t)min(8, nk - (u + U + kPf)) * kRtStepBytes);
-      uint32_t ah[8], al[8], bh0, bl0, bh1, bl1;
-      split_tf32(fa.x, ah[0], al[0]);
-      split_tf32(fa.y, ah[1], al[1]);
-      split_tf32(fa.z, ah[2], al[2]);
-      split_tf32(fa.w, ah[3], al[3]);
-      split_tf32(fb.x, ah[4], al[4]);
-      split_tf32(fb.y, ah[5], al[5]);
-      split_tf32(fb.z, ah[6], al[6]);
-      split_tf32(fb.w, ah[7], al[7]);
-      split_tf32(v.x, bh0, bl0);
-      split_tf32(v.y, bh1, bl1);
-      mma_tf32(acc0, al[0], al[1], al[4], al[5], bh0, bh1);
-      mma_tf32(acc1, al[2], al[3], al[6], al[7], bh0, bh1);
-      mma_tf32(acc0, ah[0], ah[1], ah[4], ah[5], bl0, bl1);
-      mma_tf32(acc1, ah[2], ah[3], ah[6], ah[7], bl0, bl1);
-      mma_tf32(acc0, ah[0], ah[1], ah[4], ah[5], bh0, bh1);
-      mma_tf32(acc1, ah[2], ah[3], ah[6], ah[7], bh0, bh1);
-      if (last) {
-        const int64_t r0 = row0 + 2 * t;
-        const float4 h0 = make_float4(acc0[0], acc0[2], acc1[0], acc1[2]);
-        const float4 h1 = make_float4(acc0[1], acc0[3], acc1[1], acc1[3]);
-        float4 y0, y1;
-        if (a.first) {
-          y0 = make_float4(alpha * h0.x, alpha * h0.y, alpha * h0.z, alpha * h0.w);
-          y1 = make_float4(alpha * h1.x, alpha * h1.y, alpha * h1.z, alpha * h1.w);
-        } else {
-          y0 = make_float4(alpha * h0.x - xp0.x, alpha * h0.y - xp0.y, alpha * h0.z - xp0.z, alpha * h0.w - xp0.w);
-          y1 = make_float4(alpha * h1.x - xp1.x, alpha * h1.y - xp1.y, alpha * h1.z - xp1.z, alpha * h1.w - xp1.w);
-        }
-        if (r0 < a.n) {
-          st_na4(a.tp + r0 * C + 4 * cg, y0);
-          e0[0] += xn0.x * xn0.x;
-          e0[1] += xn0.y * xn0.y;
-          e0[2] += xn0.z * xn0.z;
-          e0[3] += xn0.w * xn0.w;
-          e1[0] += y0.x * xn0.x;
-          e1[1] += y0.y * xn0.y;
-          e1[2] += y0.z * xn0.z;
-          e1[3] += y0.w * xn0.w;
-        }
-        if (r0 + 1 < a.n) {
-          st_na4(a.tp + (r0 + 1) * C + 4 * cg, y1);
-          e0[0] += xn1.x * xn1.x;
-          e0[1] += xn1.y * xn1.y;
-          e0[2] += xn1.z * xn1.z;
-          e0[3] += xn1.w * xn1.w;
-          e1[0] += y1.x * xn1.x;
-          e1[1] += y1.y * xn1.y;
-          e1[2] += y1.z * xn1.z;
-          e1[3] += y1.w * xn1.w;
-        }
-#pragma unroll
-        for (int i = 0; i < 4; ++i) acc0[i] = acc1[i] = 0.f;
-        ++jblk;
+      const unsigned char* xs = xr + ix * 1024;
+      const unsigned char* ms = mr + im * kRtStepBytes;
+      const float4 fa = *reinterpret_cast<const float4*>(xs + ro0);
+      const float4 fb = *reinterpret_cast<const float4*>(xs + ro1);
+      const float2 v = *reinterpret_cast<const float2*>(ms + 32 + 8 * lane);
+      const bool last = *reinterpret_cast<const int*>(ms + 28) < 0;
+      acc.add(fa, fb, v);
+      if (last) {  // warp-uniform: the block's epilogue
+        end_block();
         start = true;
-        if (++since_flush == kDotFlush) {
-          since_flush = 0;
-          flush();
+      }
+    }
+    cp_async_wait<0>();
+  } else {
+    const int src = 8 * t + cg;  // the lane holding chunk cg of slots t and t + 4
+    // rings (slot j = k-step mod D): columns of k-steps u + D .. u + 2D - 1, rows,
+    // values and block-end flags of k-steps u .. u + D - 1
+    int2 cc[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) cc[j] = make_int2(0, 0);
+    float4 xa[D], xb[D];
+    float2 vv[D];
+    bool lastf[D];
+    auto load_cols = [&](int v) { return ld_stream_i2(gdata + (size_t)v * kRtStepBytes + 8 * q); };
+    auto issue = [&](int j, int v) {  // k-step v (its columns in cc[j]) into slot j
+      const int2 c = cc[j];
+      lastf[j] = __any_sync(0xffffffffu, q == 3 && c.y < 0);
+      xa[j] = ldg4(tnp + (size_t)(uint32_t)(c.x & 0x7fffffff) * C);
+      xb[j] = ldg4(tnp + (size_t)(uint32_t)(c.y & 0x7fffffff) * C);
+      vv[j] = ld_stream_f2(gdata + (size_t)v * kRtStepBytes + 32 + 8 * lane);
+    };
+    if (lane == 0 && kPf < nk)
+      prefetch_l2_bulk(gdata + (size_t)kPf * kRtStepBytes, (uint32_t)min(8, nk - kPf) * kRtStepBytes);
+#pragma unroll
+    for (int j = 0; j < D; ++j)
+      if (j < nk) cc[j] = load_cols(j);
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      if (j < nk) {
+        issue(j, j);
+        if (j + D < nk) cc[j] = load_cols(j + D);
+      }
+    }
+    for (int u0 = 0; u0 < nk; u0 += D) {
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        const int u = u0 + j;
+        if (u >= nk) break;  // warp-uniform
+        if (start) {
+          begin_block();
+          start = false;
+        }
+        float4 fa, fb;
+        fa.x = __shfl_sync(0xffffffffu, xa[j].x, src);
+        fa.y = __shfl_sync(0xffffffffu, xa[j].y, src);
+        fa.z = __shfl_sync(0xffffffffu, xa[j].z, src);
+        fa.w = __shfl_sync(0xffffffffu, xa[j].w, src);
+        fb.x = __shfl_sync(0xffffffffu, xb[j].x, src);
+        fb.y = __shfl_sync(0xffffffffu, xb[j].y, src);
+        fb.z = __shfl_sync(0xffffffffu, xb[j].z, src);
+        fb.w = __shfl_sync(0xffffffffu, xb[j].w, src);
+        const float2 v = vv[j];
+        const bool last = lastf[j];
+        // the slot is free: k-step u + D goes into it, and the columns of u + 2D
+        if (u + D < nk) {
+          issue(j, u + D);
+          if (u + 2 * D < nk) cc[j] = load_cols(u + 2 * D);
+        }
+        if (lane == 0 && ((u + D) & 7) == 0 && u + D + kPf < nk)
+          prefetch_l2_bulk(gdata + (size_t)(u + D + kPf) * kRtStepBytes,
+                           (uint32_t)min(8, nk - (u + D + kPf)) * kRtStepBytes);
+        acc.add(fa, fb, v);
+        if (last) {
+          end_block();
+          start = true;
         }
       }
     }
   }
   flush();
+  // warps add their columns in warp order (deterministic)
   __shared__ double bsum[2 * C];
   for (int i = threadIdx.x; i < 2 * C; i += NT) bsum[i] = 0.0;
   __syncthreads();
@@ -866,27 +749,27 @@ void rt_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
   const int key = shape.rt_warps * 10 + shape.rt_depth;
   if (shape.rt_regs) {
     switch (key) {
-      case 162: return go(k_cheb_rtr<16, 2>, 16);
-      case 163: return go(k_cheb_rtr<16, 3>, 16);
-      case 164: return go(k_cheb_rtr<16, 4>, 16);
-      case 124: return go(k_cheb_rtr<12, 4>, 12);
-      case 126: return go(k_cheb_rtr<12, 6>, 12);
-      case 86: return go(k_cheb_rtr<8, 6>, 8);
+      case 162: return go(k_cheb_rt<16, 2, 0, true>, 16);
+      case 163: return go(k_cheb_rt<16, 3, 0, true>, 16);
+      case 164: return go(k_cheb_rt<16, 4, 0, true>, 16);
+      case 124: return go(k_cheb_rt<12, 4, 0, true>, 12);
+      case 126: return go(k_cheb_rt<12, 6, 0, true>, 12);
+      case 86: return go(k_cheb_rt<8, 6, 0, true>, 8);
     }
     fail(LEO2D_ERR_BAD_ARG, "8-row step in registers: warps 16 (depth 2, 3, 4), 12 (4, 6) or 8 (6)");
   }
   switch (key) {
-    case 83: return go(k_cheb_rt<8, 3, 5>, 8);
-    case 84: return go(k_cheb_rt<8, 4, 6>, 8);
-    case 86: return go(k_cheb_rt<8, 6, 8>, 8);
-    case 123: return go(k_cheb_rt<12, 3, 5>, 12);
-    case 124: return go(k_cheb_rt<12, 4, 6>, 12);
-    case 126: return go(k_cheb_rt<12, 6, 8>, 12);
-    case 163: return go(k_cheb_rt<16, 3, 5>, 16);
-    case 164: return go(k_cheb_rt<16, 4, 6>, 16);
-    case 166: return go(k_cheb_rt<16, 6, 8>, 16);
-    case 243: return go(k_cheb_rt<24, 3, 5>, 24);
-    case 244: return go(k_cheb_rt<24, 4, 6>, 24);
+    case 83: return go(k_cheb_rt<8, 3, 5, false>, 8);
+    case 84: return go(k_cheb_rt<8, 4, 6, false>, 8);
+    case 86: return go(k_cheb_rt<8, 6, 8, false>, 8);
+    case 123: return go(k_cheb_rt<12, 3, 5, false>, 12);
+    case 124: return go(k_cheb_rt<12, 4, 6, false>, 12);
+    case 126: return go(k_cheb_rt<12, 6, 8, false>, 12);
+    case 163: return go(k_cheb_rt<16, 3, 5, false>, 16);
+    case 164: return go(k_cheb_rt<16, 4, 6, false>, 16);
+    case 166: return go(k_cheb_rt<16, 6, 8, false>, 16);
+    case 243: return go(k_cheb_rt<24, 3, 5, false>, 24);
+    case 244: return go(k_cheb_rt<24, 4, 6, false>, 24);
   }
   fail(LEO2D_ERR_BAD_ARG, "8-row step: warps 8, 12, 16 (depth 3, 4, 6) or 24 (depth 3, 4)");
 }

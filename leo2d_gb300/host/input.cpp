@@ -134,7 +134,9 @@ bool parse_input(const std::string& path, JobSpec& spec, std::string& err) {
         if (v == "SQ") spec.solver_type = 1;
         else if (v == "LC") spec.solver_type = 2;
         else if (v == "FIXED_SHIFT") spec.solver_type = 6;
-        else if (v == "MLMC_VAC" || v == "VD_FILE" || v == "STRAIN")
+        else if (v == "MLMC_VAC") spec.solver_type = 3;
+        else if (v == "VD_FILE") spec.solver_type = 4;
+        else if (v == "STRAIN")
           spec.unsupported.push_back("SOLVER_TYPE = " + v);
       } else if (key == "NUM_LC_POINTS") {
         spec.num_lc_points = std::atoi(value().c_str());
@@ -195,8 +197,23 @@ bool parse_input(const std::string& path, JobSpec& spec, std::string& err) {
         spec.use_e = std::atoi(value().c_str());
       } else if (key == "E_FIELD") {
         spec.e_field = std::atof(value().c_str());
-      } else if (key == "DIAGONALIZE" ||
-                 key == "MLMC" || key == "CHIRAL_ON" || key == "BALLISTIC_TRANSPORT" ||
+      } else if (key == "MLMC") {  // main.cpp:730-775
+        spec.mlmc = std::atoi(value().c_str());
+      } else if (key == "MLMC_MAX_LEVEL") {
+        spec.mlmc_max_level = std::atoi(value().c_str());
+      } else if (key == "MLMC_LEVEL") {
+        spec.mlmc_level = std::atoi(value().c_str());
+      } else if (key == "MLMC_NUM_CLUSTERS") {
+        spec.mlmc_num_clusters = std::atoi(value().c_str());
+      } else if (key == "MLMC_CLUSTER_SIZE") {
+        spec.mlmc_cluster_size = std::atoi(value().c_str());
+      } else if (key == "MLMC_OUT_ROOT") {
+        spec.mlmc_out_root = value();
+      } else if (key == "MLMC_TEMP_ROOT") {
+        spec.mlmc_temp_root = value();
+      } else if (key == "VACANCY_FILE") {
+        spec.vacancy_file = value();
+      } else if (key == "DIAGONALIZE" || key == "CHIRAL_ON" || key == "BALLISTIC_TRANSPORT" ||
                  key == "MAT_FROM_FILE" || key == "GLOBAL_SHIFTS_ON" || key == "UNIFORM_STRAIN" ||
                  key == "COND_POLY_PAR" || key == "MAT_SOC_ON") {
         const std::string v = value();

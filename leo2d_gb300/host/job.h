@@ -18,7 +18,7 @@ namespace leo2d_host {
 struct JobSpec {
   std::string job_name = "LEO2D_JOB";
   leo2d_geom geom{};
-  int solver_type = 0;        // SOLVER_TYPE: 1 = SQ, 2 = LC, 6 = FIXED_SHIFT
+  int solver_type = 0;        // SOLVER_TYPE: 1 = SQ, 2 = LC, 3 = MLMC_VAC, 4 = VD_FILE, 6 = FIXED_SHIFT
   int num_lc_points = 0;      // NUM_LC_POINTS (LC: the polyline of shifts of the last sheet)
   std::vector<double> lc_points;  // LC_POINTS, (s1, s2) pairs
   int observable_type = 0;    // 0 = DOS, 1 = COND
@@ -48,6 +48,15 @@ struct JobSpec {
   int num_k1 = 1, num_k2 = 1; // K_GRID
   double e_field = 0.0;       // E_FIELD
   int energies = 0;           // > 0: also write a DOS on this many equispaced energies
+  // multilevel Monte Carlo over vacancy configurations (job_params.cpp:131-152)
+  int mlmc = 0;               // MLMC: 1 = the jobs' results go to the level statistics, no .cheb
+  int mlmc_level = 0;         // MLMC_LEVEL
+  int mlmc_max_level = 1;     // MLMC_MAX_LEVEL
+  int mlmc_num_clusters = 0;  // MLMC_NUM_CLUSTERS
+  int mlmc_cluster_size = 4;  // MLMC_CLUSTER_SIZE
+  std::string mlmc_out_root = "out";    // MLMC_OUT_ROOT
+  std::string mlmc_temp_root = "temp";  // MLMC_TEMP_ROOT
+  std::string vacancy_file = "vacancies.dat";  // VACANCY_FILE (MLMC_VAC jobs)
   int block = 0;
   std::vector<std::string> unsupported;  // keys that select paths outside this build
 };

@@ -84,6 +84,140 @@ void write_energies(std::ofstream& f, const std::vector<double>& E) {
   f << "\n";
 }
 
+// One job of the vacancy solvers: its vacancies (0-based) and targets, and for
+// MLMC_VAC its IDs from the vacancy file.
+struct VacJob {
+  std::vector<int64_t> vacancies;
+  std::vector<int64_t> targets;
+  int mlmc_id = -1, cluster_id = -1;
+};
+
+// Locality::getVacanciesFromFile (src/locality.cpp:536-640). MLMC_VAC: lines
+// "JOBID = j", "CLUSTERID = c" and "VAC = v1,v2,..." (1-based, no spaces in the
+// list), a job per JOBID; the IDs (j, c) are also the job's target list
+// (locality.cpp:1432-1446), and a list that is just "-1" means no vacancies.
+// VD_FILE: the file vacancies.dat, each "JOB=" line followed by a line of
+// vacancies and a line of targets (1-based, comma-separated).
+bool read_vacancy_jobs(int solver_type, const std::string& path, std::vector<VacJob>& jobs, std::string& err) {
+  std::ifstream in(path);
+  if (!in.is_open()) {
+    err = "cannot read the vacancy file " + path;
+    return false;
+  }
+  std::string line;
+  if (solver_type == 3) {
+    int job_id = -1, cluster_id = -1;
+    std::vector<int64_t> vac;
+    auto push = [&]() {
+      VacJob j;
+      j.vacancies = vac;
+      // "VAC = -1" (read as -2): the job has no vacancies (locality.cpp:1425-1430)
+      if (j.vacancies.size() == 1 && j.vacancies[0] == -2) j.vacancies.clear();
+      j.targets = {job_id, cluster_id};
+      j.mlmc_id = job_id;
+      j.cluster_id = cluster_id;
+      jobs.push_back(j);
+      vac.clear();
+    };
+    while (std::getline(in, line)) {
+      std::istringstream ls(line);
+      std::string tok;
+      while (std::getline(ls, tok, ' ')) {
+        if (tok == "JOBID") {
+          if (job_id != -1) push();
+          std::getline(ls, tok, ' ');
+          std::getline(ls, tok, ' ');
+          job_id = std::atoi(tok.c_str());
+        } else if (tok == "CLUSTERID") {
+          std::getline(ls, tok, ' ');
+          std::getline(ls, tok, ' ');
+          cluster_id = std::atoi(tok.c_str());
+        } else if (tok == "VAC") {
+          std::getline(ls, tok, ' ');
+          std::string list;
+          std::getline(ls, list, ' ');
+          std::istringstream vs(list);
+          while (std::getline(vs, tok, ',')) vac.push_back(std::atoi(tok.c_str()) - 1);
+        }
+      }
+    }
+    push();  // the last job
+  } else {
+    while (std::getline(in, line)) {
+      std::istringstream ls(line);
+      std::string tok;
+      while (std::getline(ls, tok, '=')) {
+        if (tok != "JOB") continue;
+        std::string vline, tline;
+        std::getline(in, vline);
+        std::getline(in, tline);
+        VacJob j;
+        std::istringstream vs(vline), ts(tline);
+        while (std::getline(vs, tok, ',')) j.vacancies.push_back(std::atoi(tok.c_str()) - 1);
+        while (std::getline(ts, tok, ',')) j.targets.push_back(std::atoi(tok.c_str()) - 1);
+        jobs.push_back(j);
+      }
+    }
+  }
+  if (jobs.empty()) {
+    err = "the vacancy file " + path + " holds no job";
+    return false;
+  }
+  return true;
+}
+
+// Mlmc_handler (src/mlmc/mlmc_handler.cpp) for trace-DOS jobs: running means
+// of the jobs' DOS (E) and of its square (V), and for jobs of a cluster the
+// same of the difference from the cluster's original at the next level (DE,
+// DV), with Param_tools::mlmc_average / _variance / _cluster_average /
+// _cluster_variance's update (param_tools.cpp:1213-1720): with c the
+// accumulator's sample count, x <- x (c - 1) / c + sample / c, the first sample
+// taken as is. Files as Param_tools::mlmc_save / mlmc_load (975-1211): raw FP64.
+struct MlmcStats {
+  std::vector<double> E, V, DE, DV;
+  int nE = 1, nV = 1, nDE = 1, nDV = 1;
+  std::vector<std::vector<double>> cluster_original;
+
+  static void update(std::vector<double>& tot, int& count, const std::vector<double>& samp) {
+    if (tot.empty() || count == 1) {
+      tot = samp;
+    } else {
+      const double s_t = (1.0 * count - 1) / (1.0 * count), s_s = 1.0 / (1.0 * count);
+      for (size_t i = 0; i < tot.size() && i < samp.size(); ++i) tot[i] = tot[i] * s_t + samp[i] * s_s;
+    }
+    ++count;
+  }
+  static std::vector<double> square(const std::vector<double>& x) {
+    std::vector<double> y(x.size());
+    for (size_t i = 0; i < x.size(); ++i) y[i] = std::pow(x[i], 2);
+    return y;
+  }
+  static std::vector<double> diff(const std::vector<double>& a, const std::vector<double>& b) {
+    std::vector<double> y(a.size());
+    for (size_t i = 0; i < a.size(); ++i) y[i] = a[i] - (i < b.size() ? b[i] : 0.0);
+    return y;
+  }
+  static std::vector<double> load(const std::string& file) {
+    std::ifstream f(file, std::ios::binary | std::ios::ate);
+    if (!f.is_open()) return {};
+    const std::streamsize bytes = f.tellg();
+    std::vector<double> v((size_t)std::max<std::streamsize>(bytes, 0) / sizeof(double));
+    f.seekg(0);
+    f.read(reinterpret_cast<char*>(v.data()), (std::streamsize)(v.size() * sizeof(double)));
+    return v;
+  }
+  static bool save(const std::string& file, const std::vector<double>& v) {
+    std::ofstream f(file, std::ios::binary);
+    if (!f.is_open()) return false;
+    f.write(reinterpret_cast<const char*>(v.data()), (std::streamsize)(v.size() * sizeof(double)));
+    return true;
+  }
+};
+
+std::string mlmc_name(const std::string& root, const std::string& prefix, int level, const std::string& tail) {
+  return root + "/" + prefix + "_L" + std::to_string(level) + tail;
+}
+
 }  // namespace
 
 leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device, std::string& err) {
@@ -97,8 +231,17 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     err = "poly_order = " + std::to_string(P) + " is NOT divisible 4 (needed for KPM iterative method)";
     return LEO2D_ERR_BAD_ARG;
   }
-  if (spec.solver_type != 1 && spec.solver_type != 2 && spec.solver_type != 6) {
-    err = "SOLVER_TYPE must be SQ, LC or FIXED_SHIFT (their job lists are built)";
+  if (spec.solver_type < 1 || spec.solver_type > 6 || spec.solver_type == 5) {
+    err = "SOLVER_TYPE must be SQ, LC, MLMC_VAC, VD_FILE or FIXED_SHIFT (their job lists are built)";
+    return LEO2D_ERR_UNSUPPORTED;
+  }
+  if (spec.mlmc == 1 && spec.solver_type != 3) {
+    err = "MLMC = 1 takes its jobs from SOLVER_TYPE = MLMC_VAC";
+    return LEO2D_ERR_BAD_ARG;
+  }
+  if ((spec.solver_type == 3 || spec.solver_type == 4) &&
+      (spec.geom.boundary_condition != 0 || spec.use_b == 1 || spec.k_sampling == 1 || spec.observable_type != 0)) {
+    err = "the vacancy solvers run DOS jobs on real flakes here (no periodic cell, field, k points or COND)";
     return LEO2D_ERR_UNSUPPORTED;
   }
   if (spec.solver_type == 2 && (spec.num_lc_points < 2 || spec.lc_points.size() < 2 * (size_t)spec.num_lc_points)) {
@@ -140,7 +283,18 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
   // for the last shift sheet every (i/N, j/N), i outer, j inner, and for each
   // of those the list of the remaining shift sheets
   std::vector<std::vector<double>> jobs;  // [job][2 * sheet]
-  if (spec.solver_type == 6) {
+  std::vector<VacJob> vjobs;              // the vacancy solvers' jobs (no shifts)
+  if (spec.solver_type == 3 || spec.solver_type == 4) {
+    // MLMC_VAC reads VACANCY_FILE; VD_FILE reads vacancies.dat (locality.cpp:536, 591)
+    // (relative paths: in the output directory, the reference's working directory)
+    std::string vf = spec.solver_type == 3 ? spec.vacancy_file : std::string("vacancies.dat");
+    if (!vf.empty() && vf[0] != '/') vf = join_path(out_dir, vf);
+    if (!read_vacancy_jobs(spec.solver_type, vf, vjobs, err)) return LEO2D_ERR_IO;
+    // VD_FILE jobs never set num_vacancies, so the worker removes nothing (locality.cpp:1456-1494, 2994)
+    if (spec.solver_type == 4)
+      for (auto& j : vjobs) j.vacancies.clear();
+    for (size_t i = 0; i < vjobs.size(); ++i) jobs.push_back(std::vector<double>(2 * LEO2D_MAX_SHEETS, 0.0));
+  } else if (spec.solver_type == 6) {
     // one job, every sheet but the first shifted by (1/3, 1/3) (locality.cpp:1580-1608)
     std::vector<double> sh(2 * LEO2D_MAX_SHEETS, 0.0);
     for (int s = 1; s < g0.num_sheets; ++s) sh[2 * s] = sh[2 * s + 1] = 1.0 / 3.0;
@@ -273,12 +427,29 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
   if (spec.observable_type == 1 || spec.matrix_save > 1) flags |= LEO2D_CSR_WITH_DX;
   // generateCpxH's matrix save lists every stored pair, zeros included (locality.cpp:5213-5228)
   if (cpx_run && spec.matrix_save > 0) flags |= LEO2D_CSR_KEEP_ZEROS;
-  std::ofstream cheb(join_path(out_dir, spec.job_name + ".cheb"));
-  if (!cheb.is_open()) {
-    err = "cannot write " + spec.job_name + ".cheb";
-    return LEO2D_ERR_IO;
+  // (an MLMC run writes its level statistics instead of a .cheb, locality.cpp:2773-2837)
+  std::ofstream cheb;
+  if (spec.mlmc != 1) {
+    cheb.open(join_path(out_dir, spec.job_name + ".cheb"));
+    if (!cheb.is_open()) {
+      err = "cannot write " + spec.job_name + ".cheb";
+      return LEO2D_ERR_IO;
+    }
   }
   cheb << std::fixed;
+  // Mlmc_handler::setup (mlmc_handler.cpp:29-116): below the top level, the
+  // cluster originals are the next level's saved job results
+  MlmcStats mlmc;
+  const std::string mlmc_out = spec.mlmc_out_root.empty() || spec.mlmc_out_root[0] == '/'
+                                   ? spec.mlmc_out_root : join_path(out_dir, spec.mlmc_out_root);
+  const std::string mlmc_temp = spec.mlmc_temp_root.empty() || spec.mlmc_temp_root[0] == '/'
+                                    ? spec.mlmc_temp_root : join_path(out_dir, spec.mlmc_temp_root);
+  if (spec.mlmc == 1 && spec.mlmc_level < spec.mlmc_max_level)
+    for (int i = 0; i < spec.mlmc_num_clusters; ++i)
+      mlmc.cluster_original.push_back(spec.kpm_trace == 1
+                                          ? MlmcStats::load(mlmc_name(mlmc_temp, spec.job_name, spec.mlmc_level + 1,
+                                                                      "_J" + std::to_string(i + 1) + "_dos.bin"))
+                                          : std::vector<double>());
   // one generator draws every job's trace vectors in job order (locality.cpp:2274-2305)
   std::default_random_engine generator;
   std::normal_distribution<double> distribution(0.0, 1.0);
@@ -327,7 +498,36 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     grid4.assign(4 * n, 0);
     pos.assign(3 * n, 0.0);
     CHECK(leo2d_csr_geometry(ctx.h, csr.h, grid4.data(), pos.data()));
-    if (first_job && !target_list(spec, grid4, targets, err)) return LEO2D_ERR_BAD_ARG;
+    if (vjobs.empty() && first_job && !target_list(spec, grid4, targets, err)) return LEO2D_ERR_BAD_ARG;
+    // the vacancy solvers: the job's own targets, and its matrix without its
+    // vacancies (workerChebSolve, locality.cpp:2989-3016)
+    Csr vcsr;
+    leo2d_csr* kcsr = csr.h;
+    int64_t n_kpm = n;
+    int n_vac = 0;
+    if (!vjobs.empty()) {
+      const VacJob& vj = vjobs[job];
+      n_vac = (int)vj.vacancies.size();
+      if (n_vac > 0) {
+        CHECK(leo2d_csr_remove_orbitals(ctx.h, csr.h, vj.vacancies.data(), (int64_t)n_vac, &vcsr.h));
+        int64_t z0 = 0, z1 = 0, z2 = 0;
+        CHECK(leo2d_csr_info(vcsr.h, &n_kpm, &z0, &z1, &z2));
+        kcsr = vcsr.h;
+        // the root draws trace vectors of max_index - num_vacancies entries
+        // (locality.cpp:2282-2287): a list with repeats or orbitals outside the
+        // flake would not match the worker's matrix
+        if (n - n_kpm != n_vac) {
+          err = "vacancy list of job " + std::to_string(job + 1) + " repeats orbitals or names ones outside the flake";
+          return LEO2D_ERR_BAD_ARG;
+        }
+      }
+      targets.clear();
+      for (int64_t t : vj.targets) {
+        int64_t below = 0;
+        for (int64_t v : vj.vacancies) below += v < t ? 1 : 0;
+        targets.push_back(t - below);
+      }
+    }
 
     // Chebyshev nodes of Param_tools::save (param_tools.cpp:57-62); with
     // Gershgorin bounds the axis is centre + rescale x.
@@ -376,18 +576,42 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
       cfg.num_vectors = S;
       std::vector<double> mu((size_t)S * P);
       if (spec.vectors == 0) {
-        std::vector<double> vec((size_t)S * n);
+        std::vector<double> vec((size_t)S * n_kpm);
         for (int s = 0; s < S; ++s)
-          for (int64_t i = 0; i < n; ++i) vec[(size_t)s * n + i] = distribution(generator);
+          for (int64_t i = 0; i < n_kpm; ++i) vec[(size_t)s * n_kpm + i] = distribution(generator);
         cfg.vector_kind = LEO2D_VEC_HOST;
-        CHECK(leo2d_kpm_dos(ctx.h, csr.h, &cfg, vec.data(), mu.data()));
+        CHECK(leo2d_kpm_dos(ctx.h, kcsr, &cfg, vec.data(), mu.data()));
       } else {
         cfg.vector_kind = LEO2D_VEC_PHASE;
-        CHECK(leo2d_kpm_dos(ctx.h, csr.h, &cfg, nullptr, mu.data()));
+        CHECK(leo2d_kpm_dos(ctx.h, kcsr, &cfg, nullptr, mu.data()));
       }
       std::vector<double> dos(P), Ek(P);
-      // densityTransformTrace(results, 1/num_dofs) (locality.cpp:3126-3131)
-      CHECK(leo2d_dos_transform(ctx.h, mu.data(), P, S, rescale, shift, 1.0 / (double)n, dos.data(), Ek.data()));
+      // densityTransformTrace(results, 1/num_dofs) (locality.cpp:3126-3131); a
+      // vacancy job's num_dofs takes its vacancies off the reduced size again
+      const double num_dofs = (double)(n_kpm - n_vac);
+      CHECK(leo2d_dos_transform(ctx.h, mu.data(), P, S, rescale, shift, 1.0 / num_dofs, dos.data(), Ek.data()));
+      if (spec.mlmc == 1) {  // Mlmc_handler::process (mlmc_handler.cpp:118-178)
+        const VacJob& vj = vjobs[job];
+        if (vj.cluster_id == -1) {
+          MlmcStats::update(mlmc.E, mlmc.nE, dos);
+          MlmcStats::update(mlmc.V, mlmc.nV, MlmcStats::square(dos));
+          if (spec.mlmc_level > 1 &&
+              !MlmcStats::save(mlmc_name(mlmc_temp, spec.job_name, spec.mlmc_level,
+                                         "_J" + std::to_string(vj.mlmc_id) + "_dos.bin"), dos)) {
+            err = "cannot write the MLMC job file under " + mlmc_temp;
+            return LEO2D_ERR_IO;
+          }
+        } else {
+          if (vj.cluster_id < 1 || vj.cluster_id > (int)mlmc.cluster_original.size()) {
+            err = "CLUSTERID " + std::to_string(vj.cluster_id) + " is outside MLMC_NUM_CLUSTERS";
+            return LEO2D_ERR_BAD_ARG;
+          }
+          const std::vector<double> d = MlmcStats::diff(mlmc.cluster_original[vj.cluster_id - 1], dos);
+          MlmcStats::update(mlmc.DE, mlmc.nDE, d);
+          MlmcStats::update(mlmc.DV, mlmc.nDV, MlmcStats::square(d));
+        }
+        continue;
+      }
       if (spec.verbose_save == 1) {
         if (first_job) {
           cheb << "E: ";
@@ -421,7 +645,7 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     } else if (spec.observable_type == 0) {
       const int64_t T = (int64_t)targets.size();
       std::vector<double> mu((size_t)T * P);
-      CHECK(leo2d_kpm_ldos(ctx.h, csr.h, &cfg, targets.data(), T, mu.data()));
+      CHECK(leo2d_kpm_ldos(ctx.h, kcsr, &cfg, targets.data(), T, mu.data()));
       std::vector<double> out = mu;
       if (spec.dos_transform == 1) {  // Param_tools::densityTransform
         std::vector<double> Ek(P);
@@ -472,6 +696,26 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     }
   }  // jobs
   cheb.close();
+  if (spec.mlmc == 1) {  // Mlmc_handler::save (mlmc_handler.cpp:394-481)
+    const int lvl = spec.mlmc_level;
+    bool ok = true;
+    if (spec.kpm_trace == 1) {
+      ok = ok && MlmcStats::save(mlmc_name(mlmc_out, spec.job_name, lvl, "_E_dos.bin"), mlmc.E);
+      ok = ok && MlmcStats::save(mlmc_name(mlmc_out, spec.job_name, lvl, "_V_dos.bin"), mlmc.V);
+    }
+    std::vector<double> Ef(P);
+    for (int i = 0; i < P; ++i)
+      Ef[i] = spec.geom.energy_shift + spec.geom.energy_rescale * std::cos((i * 1.0 + 0.5) * M_PI / P);
+    ok = ok && MlmcStats::save(mlmc_name(mlmc_out, spec.job_name, lvl, "_ENERGIES.bin"), Ef);
+    if (lvl < spec.mlmc_max_level && spec.kpm_trace == 1) {
+      ok = ok && MlmcStats::save(mlmc_name(mlmc_out, spec.job_name, lvl, "_DE_dos.bin"), mlmc.DE);
+      ok = ok && MlmcStats::save(mlmc_name(mlmc_out, spec.job_name, lvl, "_DV_dos.bin"), mlmc.DV);
+    }
+    if (!ok) {
+      err = "cannot write the MLMC statistics under " + mlmc_out;
+      return LEO2D_ERR_IO;
+    }
+  }
   if (!kjobs.empty()) {  // Param_tools::saveKpts (param_tools.cpp:579-602), one line per job
     std::ofstream kf(join_path(out_dir, spec.job_name + ".kpts"));
     kf << std::fixed;

@@ -9,6 +9,7 @@
  * threads of its own (no OpenMP, MKL absent); here disjoint vector sets run on
  * `threads` host threads, standing in for one MPI worker per core.
  */
+#include <algorithm>
 #include <chrono>
 #include <cstdint>
 #include <thread>
@@ -64,6 +65,56 @@ double oracle_cpu_kpm_steps(int64_t n, const int64_t* rp, const int32_t* col, co
   for (double s : sums) cs += s;
   if (checksum) *checksum = cs;
   return std::chrono::duration<double>(t1 - t0).count();
+}
+
+/* The doubling recursion of the oracle (oracle_kpm_trace_doubling: T_{k+1} =
+ * 2 H T_k - T_{k-1}, mu_{2k} = 2 <T_k|T_k> - mu_0, mu_{2k+1} = 2 <T_{k+1}|T_k> -
+ * mu_1) with each SpMV split over `threads` row ranges. Every row is summed in
+ * the same order as the serial loop and the dots are serial, so the moments
+ * equal the serial oracle's bit for bit. */
+void oracle_kpm_trace_doubling_threads(int64_t n, const int64_t* rp, const int32_t* col, const double* val,
+                                       int32_t R, const double* vectors, int32_t P, int32_t threads,
+                                       double* mu_out) {
+  if (threads < 1) threads = 1;
+  std::vector<double> Tp(n), Tj(n), Tn(n);
+  auto spmv = [&](const double* in, double* out, double alpha) {
+    std::vector<std::thread> th;
+    for (int t = 0; t < threads; ++t)
+      th.emplace_back([&, t] {
+        for (int64_t r = n * t / threads; r < n * (t + 1) / threads; ++r) {
+          double temp_sum = 0;
+          for (int64_t i = rp[r]; i < rp[r + 1]; ++i) temp_sum += in[col[i]] * val[i];
+          out[r] = alpha * temp_sum + 0 * out[r];
+        }
+      });
+    for (auto& x : th) x.join();
+  };
+  for (int t = 0; t < R; ++t) {
+    const double* v = vectors + (size_t)t * n;
+    double* mu = mu_out + (size_t)t * P;
+    for (int64_t i = 0; i < n; ++i) Tj[i] = v[i];
+    std::fill(Tp.begin(), Tp.end(), 0.0);
+    std::fill(Tn.begin(), Tn.end(), 0.0);
+    for (int k = 0; k < P / 2; ++k) {
+      spmv(Tj.data(), Tn.data(), k == 0 ? 1.0 : 2.0);
+      if (k > 0)
+        for (int64_t c = 0; c < n; ++c) Tn[c] -= Tp[c];
+      double d0 = 0, d1 = 0;
+      for (int64_t c = 0; c < n; ++c) {
+        d0 += Tj[c] * Tj[c];
+        d1 += Tn[c] * Tj[c];
+      }
+      if (k == 0) {
+        mu[0] = d0;
+        mu[1] = d1;
+      } else {
+        mu[2 * k] = 2 * d0 - mu[0];
+        mu[2 * k + 1] = 2 * d1 - mu[1];
+      }
+      Tp.swap(Tj);
+      Tj.swap(Tn);
+    }
+  }
 }
 
 }  // extern "C"

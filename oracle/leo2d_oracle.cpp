@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <random>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -701,6 +702,124 @@ int64_t oracle_targets(const oracle_h* h, const int32_t* target_sheets, int32_t 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- simple-model flakes at scale
+
+// The compact Hamiltonian of a flake of the simple model (the timed workloads)
+// without the pair lists oracle_build keeps, so that flakes of 1e7 orbitals fit
+// host memory: rows in the reference order (Sheet::setIndex per sheet, sheets
+// in order), for each row its nearest-neighbour intralayer entries (the
+// Sheet::getIntraPairs window, t = -2.7 eV on the first shell), the diagonal,
+// and the interlayer entries of the sheets below and above (the
+// Hstruct::getInterPairs window, in-plane distance < 12.5 A, kept where the
+// 3-D distance is < 8 A), each divided by `rescale` with `shift` on the
+// diagonal as generateRealH does (locality.cpp:4166-4176). Rows are built on
+// `threads` host threads. Entries whose value is zero (the diagonal excepted)
+// are not stored, as the device's compact copy. Returns the entry count; the
+// arrays are written when cap >= that count (rowptr: n + 1 entries always).
+extern "C" int64_t oracle_flake_sites(const leo2d_geom* g) {
+  if (!g || !g->prepared || g->boundary_condition != 0) return -1;
+  int64_t n = 0;
+  for (int s = 0; s < g->num_sheets; ++s) {
+    SheetGeo sh;
+    make_sheet(g, s, sh);
+    n += sh.max_index;
+  }
+  return n;
+}
+
+extern "C" int64_t oracle_simple_flake_csr(const leo2d_geom* g, double rescale, double shift, int threads,
+                                           int64_t* rowptr, int32_t* col, double* val, int64_t cap) {
+  if (!g || !g->prepared || g->boundary_condition != 0 || g->model != LEO2D_MODEL_SIMPLE) return -1;
+  const int S = g->num_sheets;
+  std::vector<SheetGeo> sheets(S);
+  std::vector<int64_t> base(S + 1, 0);
+  for (int s = 0; s < S; ++s) {
+    make_sheet(g, s, sheets[s]);
+    base[s + 1] = base[s] + sheets[s].max_index;
+  }
+  const int64_t n = base[S];
+  auto pos_of = [&](int s, int i, int j, int l, double p[3]) {
+    const SheetGeo& sh = sheets[s];
+    double lp[3];
+    sh.pos_grid(i, j, l, lp);
+    const double th = g->angles[s];
+    p[0] = lp[0] * std::cos(th) - lp[1] * std::sin(th);
+    p[1] = lp[0] * std::sin(th) + lp[1] * std::cos(th);
+    p[2] = lp[2] + g->heights[s];
+  };
+  // row r: visits (column, value) of its stored entries
+  auto row = [&](int64_t r, auto&& emit) {
+    int s = 0;
+    while (r >= base[s + 1]) ++s;
+    const SheetGeo& sh = sheets[s];
+    const int k = (int)(r - base[s]);
+    const int ih = sh.idx[3 * (size_t)k], jh = sh.idx[3 * (size_t)k + 1], l0 = sh.idx[3 * (size_t)k + 2];
+    double ph[3];
+    pos_of(s, ih, jh, l0, ph);
+    emit((int32_t)r, shift / rescale);  // the diagonal
+    double lp[3];
+    sh.pos_grid(ih, jh, l0, lp);
+    const int i0 = sh.find_nearest(lp, 0), j0 = sh.find_nearest(lp, 1);
+    for (int i = i0 - 4; i < i0 + 4; ++i)
+      for (int j = j0 - 4; j < j0 + 4; ++j)
+        for (int l = 0; l < sh.n_orb; ++l) {
+          const int k2 = sh.grid_to_index(i, j, l);
+          if (k2 < 0 || k2 == k) continue;
+          const double t = intralayer(LEO2D_MODEL_SIMPLE, l0, l, i - ih, j - jh);
+          if (t != 0) emit((int32_t)(base[s] + k2), t / rescale);
+        }
+    for (int side = 0; side < 2; ++side) {
+      const int s0 = side == 0 ? s - 1 : s + 1;
+      if (s0 < 0 || s0 >= S) continue;
+      const SheetGeo& o = sheets[s0];
+      const double th = -g->angles[s0];
+      const double xr = ph[0] * std::cos(th) - ph[1] * std::sin(th);
+      const double yr = ph[0] * std::sin(th) + ph[1] * std::cos(th);
+      const int ic = std::min(std::max(int(std::floor(o.a_inv[0][0] * xr + o.a_inv[0][1] * yr)), o.min0), o.max0) - o.min0;
+      const int jc = std::min(std::max(int(std::floor(o.a_inv[1][0] * xr + o.a_inv[1][1] * yr)), o.min1), o.max1) - o.min1;
+      for (int i = std::max(0, ic - 6); i < std::min(o.H, ic + 6); ++i)
+        for (int j = std::max(0, jc - 6); j < std::min(o.W, jc + 6); ++j)
+          for (int l = 0; l < o.n_orb; ++l) {
+            const int k2 = o.grid_to_index(i, j, l);
+            if (k2 < 0) continue;
+            double p2[3];
+            pos_of(s0, i, j, l, p2);
+            const double dx = p2[0] - ph[0], dy = p2[1] - ph[1];
+            if (dx * dx + dy * dy >= 12.5 * 12.5) continue;
+            const double t = simple_inter_t(dx, dy, p2[2] - ph[2], rescale);
+            if (t != 0) emit((int32_t)(base[s0] + k2), t);
+          }
+    }
+  };
+  if (threads < 1) threads = 1;
+  auto parallel = [&](auto&& body) {
+    std::vector<std::thread> th;
+    for (int t = 0; t < threads; ++t)
+      th.emplace_back([&, t] {
+        for (int64_t r = n * t / threads; r < n * (t + 1) / threads; ++r) body(r);
+      });
+    for (auto& x : th) x.join();
+  };
+  parallel([&](int64_t r) {
+    int64_t c = 0;
+    row(r, [&](int32_t, double) { ++c; });
+    rowptr[r + 1] = c;
+  });
+  rowptr[0] = 0;
+  for (int64_t r = 0; r < n; ++r) rowptr[r + 1] += rowptr[r];
+  const int64_t nnz = rowptr[n];
+  if (cap < nnz) return nnz;
+  parallel([&](int64_t r) {
+    int64_t e = rowptr[r];
+    row(r, [&](int32_t c, double v) {
+      col[e] = c;
+      val[e] = v;
+      ++e;
+    });
+  });
+  return nnz;
+}
 
 // ---------------------------------------------------------------- recursions
 

@@ -14,8 +14,9 @@ vectors) and cfg1_sc3132.in (the commensurate (31,32) supercell at 1.05 deg,
 on job 1 - and stores what the GPU tests compare against, small enough to
 commit: SHA-256 digests of the CSR arrays (row pointers and columns as int32,
 values as FP64 bytes), every 997th entry's column and value, the row pointers
-themselves, the moments of both vectors, the DOS at the Chebyshev nodes and a
-digest of the trace vectors (which oracle.reference_gaussian reproduces).
+themselves, each row's sum of values and of their magnitudes, the moments of
+both vectors, the DOS at the Chebyshev nodes and a digest of the trace vectors
+(which oracle.reference_gaussian reproduces).
 """
 import hashlib
 import os
@@ -49,6 +50,8 @@ def make(name):
     out = {"meta": meta, "rowptr": rowptr, "sample_idx": idx, "sample_col": col[idx], "sample_val": val[idx],
            "moments": moments.reshape(-1, P), "dos": dos, "targets": targets,
            "val_sum": np.array([val.sum(), np.abs(val).sum(), (val * val).sum()]),
+           "row_sum": np.add.reduceat(val, rowptr[:-1].astype(np.int64)),
+           "row_abs": np.add.reduceat(np.abs(val), rowptr[:-1].astype(np.int64)),
            "digests": np.array([sha(rowptr), sha(col), sha(val), sha(tv)])}
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print(f"{name}: N={n} nnz={nnz} P={P} samples={len(idx)} vectors={out['moments'].shape[0]}")

@@ -40,10 +40,19 @@ def test_geometry_matches_fixture_spec(name):
 def test_unsupported_options_are_reported(tmp_path):
     p = tmp_path / "x.in"
     p.write_text("NUM_SHEETS = 1\nSTART_SHEET 1\nMATERIAL = MoS2\nEND_SHEET 1\nDIAGONALIZE = 1\n"
-                 "STRAIN_TYPE = 2\nPOLY_ORDER = 30\nSOLVER_TYPE = MLMC_VAC\n")
+                 "STRAIN_TYPE = 2\nPOLY_ORDER = 30\nSOLVER_TYPE = STRAIN\n")
     st, g, ints, msg = _parse(p)
     assert st == 0
     assert ints[7] == 4 and "MoS2" in msg and "DIAGONALIZE" in msg and "STRAIN_TYPE" in msg
+
+
+def test_vacancy_solver_keys():
+    """SOLVER_TYPE = MLMC_VAC (3) and VD_FILE (4) with the MLMC keys parse as the
+    reference reads them (main.cpp:410-430, 730-775)."""
+    from tests._golden import GOLDEN as G
+    st, g, ints, msg = _parse(os.path.join(G, "mlmc", "mlmc_L1.in"))
+    assert st == 0 and ints[7] == 0, msg
+    assert ints[0] == 3 and ints[3] == 1 and ints[2] == 64
 
 
 @pytest.mark.parametrize("name", BFIELD_CASES)

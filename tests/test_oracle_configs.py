@@ -46,6 +46,8 @@ def test_csr_bit_exact_at_full_size(built):
     idx = gold["sample_idx"]
     np.testing.assert_array_equal(b.col[idx], gold["sample_col"])
     np.testing.assert_array_equal(b.val[idx], gold["sample_val"])
+    starts = b.rowptr[:-1].astype(np.int64)
+    np.testing.assert_array_equal(np.add.reduceat(b.val, starts), gold["row_sum"])
 
 
 def test_trace_vectors_and_first_moments(built):
