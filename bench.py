@@ -181,9 +181,8 @@ class CpuFlake:
         if a is None:  # Gershgorin bounds x 1.01 of the host-built matrix, then rescale in place
             lo, hi = oracle.gershgorin(rp, col, val)
             a, b = 1.01 * (hi - lo) / 2, (hi + lo) / 2
-            diag = np.repeat(np.arange(n, dtype=np.int64), np.diff(rp)) == col
-            val[diag] -= b
-            val /= a
+            lib.oracle_rescale_csr(ctypes.c_int64(n), oracle._p(rp), oracle._p(col), oracle._p(val),
+                                   ctypes.c_double(a), ctypes.c_double(-b))
         self.build_s = time.perf_counter() - t0
         self.n, self.nnz, self.rp, self.col, self.val, self.a, self.b = n, nnz, rp, col, val, a, b
 
@@ -221,6 +220,9 @@ def kernel_case(args):
     with L.Context(0) as ctx:
         if args.step_kernel >= 0:
             ctx.set_option("step_kernel", args.step_kernel)
+        for key in ("rt_stage", "rt_warps", "rt_depth"):
+            if getattr(args, key) is not None:
+                ctx.set_option(key, getattr(args, key))
         csr = ctx.build_csr(ctx.prepare(geom(L, radius=radius)))
         lo, hi = csr.bounds()
         csr.rescale(1.01 * (hi - lo) / 2, -(hi + lo) / 2)
@@ -877,6 +879,10 @@ def main():
     ap.add_argument("--step-kernel", type=int, default=-1, choices=[-1, 0, 1, 2, 3, 5],
                     help="force the Chebyshev step kernel: 0 tiled gathers, 1 register gathers, 2 tensor cores, "
                          "3 row blocks, 5 row blocks of 8 on the tensor cores (default: the autotuner's choice)")
+    ap.add_argument("--rt-stage", type=int, default=None, choices=[0, 1],
+                    help="8-row tensor-core step: T_n rows staged in registers (0) or shared memory (1)")
+    ap.add_argument("--rt-warps", type=int, default=None, help="8-row tensor-core step: warps per CTA")
+    ap.add_argument("--rt-depth", type=int, default=None, help="8-row tensor-core step: k-steps in flight")
     ap.add_argument("--kernel-case", type=int, default=0, metavar="COLS",
                     help="profiling case: two short DOS runs (P=16) of COLS-wide vector blocks on the flake "
                          "of --radius (1000 A: 2.4M orbitals), then exit; prints no bench line")

@@ -134,8 +134,11 @@ int64_t leo2d_ctx_launch_count(const leo2d_ctx* ctx);
  * "tile_chunk" (1..65536 consecutive row tiles per block between grid-wide
  * jumps, default 4), "rt_warps" / "rt_depth" / "rt_group" / "rt_chunk" (the
  * 8-row tensor-core step: warps per CTA 8, 12, 16 or 24; k-steps of T_n rows in
- * flight per warp 3, 4 or 6; blocks per warp run 1..16, default 2; tiles per
- * CTA between grid-wide jumps 1..64, default 2; 0 = autotuned or default),
+ * flight per warp 2, 3, 4, 6 with the rows in registers or 3, 7 in shared
+ * memory; blocks per warp run 1..16, default 2; tiles per CTA between grid-wide
+ * jumps 1..64, default 2; 0 = autotuned or default), "rt_stage" (-1 =
+ * autotuned, 0 = the T_n rows of the 8-row step staged in registers, 1 = in
+ * shared memory),
  * "alloc_cap_mb" (the largest single device allocation a call on this context
  * may make, in MiB; a larger one fails with LEO2D_ERR_OOM and a message naming
  * its size; 0 = no limit, the default),

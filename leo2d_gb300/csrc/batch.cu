@@ -148,9 +148,11 @@ int64_t tile_max_nnz(leo2d_ctx* ctx, const int64_t* rp, int64_t n, int tile_rows
   return (int64_t)h;
 }
 
-// Shape of the batched step.
+// Shape of the batched step: the tiled CSR step, or the row-block step of
+// rb_spmm.cu (32 columns, 24 warps, each flake's locality-ordered row blocks).
 struct BatchShape {
   int cols = 32, warps = 8, rows_per_item = 0;
+  bool rb = false;
 };
 
 }  // namespace
@@ -183,22 +185,33 @@ namespace {
 // of this shape does not fit in shared memory.
 bool layout(leo2d_batch* b, const BatchShape& s) {
   leo2d_ctx* ctx = b->ctx;
-  const int ns = batch_slots(s.cols, s.warps);
-  const int ri = s.rows_per_item > 0 ? s.rows_per_item : std::max(1, 32 / ns);
-  b->tile_rows = ns * ri;
-  int64_t mx = 0;
-  for (auto& f : b->fl) mx = std::max(mx, tile_max_nnz(ctx, f.rowptr, f.n, b->tile_rows));
-  auto up = [](int64_t x, int64_t a) { return (x + a - 1) / a * a; };
-  b->tile_cap = (int)up(mx + 8, 4);
-  b->rp_bytes = (int)up((int64_t)(b->tile_rows + 4) * 8, 128);
-  b->col_bytes = (int)up((int64_t)b->tile_cap * 8, 128);
-  b->stage_bytes = (int)up(b->rp_bytes + b->col_bytes, 128);
-  b->dyn_smem = (size_t)ctx->tile_stages * b->stage_bytes;
-  if (b->dyn_smem + 24 * 1024 > ctx->smem_optin) return false;
-  int occ = 0;
-  batch_dispatch(ctx, s.cols, 0, 0, nullptr, &occ, b->dyn_smem, s.warps);
   const int F = (int)b->fl.size();
-  int G = ctx->sm_count * std::max(occ, 1);
+  int G = 0;
+  std::vector<int64_t> tiles_of(F);
+  if (s.rb) {
+    std::vector<const leo2d_csr*> cs(F);
+    for (int f = 0; f < F; ++f) cs[f] = b->fl[f].csr;
+    b->dyn_smem = rb_batch_smem(ctx, cs.data(), F, s.warps);
+    G = ctx->sm_count;  // one CTA of 24 warps per SM
+    for (int f = 0; f < F; ++f) tiles_of[f] = rb_tiles(b->fl[f].csr, s.warps);
+  } else {
+    const int ns = batch_slots(s.cols, s.warps);
+    const int ri = s.rows_per_item > 0 ? s.rows_per_item : std::max(1, 32 / ns);
+    b->tile_rows = ns * ri;
+    int64_t mx = 0;
+    for (auto& f : b->fl) mx = std::max(mx, tile_max_nnz(ctx, f.rowptr, f.n, b->tile_rows));
+    auto up = [](int64_t x, int64_t a) { return (x + a - 1) / a * a; };
+    b->tile_cap = (int)up(mx + 8, 4);
+    b->rp_bytes = (int)up((int64_t)(b->tile_rows + 4) * 8, 128);
+    b->col_bytes = (int)up((int64_t)b->tile_cap * 8, 128);
+    b->stage_bytes = (int)up(b->rp_bytes + b->col_bytes, 128);
+    b->dyn_smem = (size_t)ctx->tile_stages * b->stage_bytes;
+    if (b->dyn_smem + 24 * 1024 > ctx->smem_optin) return false;
+    int occ = 0;
+    batch_dispatch(ctx, s.cols, 0, 0, nullptr, &occ, b->dyn_smem, s.warps);
+    G = ctx->sm_count * std::max(occ, 1);
+    for (int f = 0; f < F; ++f) tiles_of[f] = (b->fl[f].n + b->tile_rows - 1) / b->tile_rows;
+  }
   if (G < F) G = F;
   // blocks per flake: proportional to its bytes per step, at least one, at most
   // its number of tile chunks
@@ -208,8 +221,7 @@ bool layout(leo2d_batch* b, const BatchShape& s) {
   for (int f = 0; f < F; ++f) {
     w[f] = (double)b->fl[f].nnz * 8 + (double)b->fl[f].n * (8 + 12.0 * s.cols);
     wsum += w[f];
-    const int64_t tiles = (b->fl[f].n + b->tile_rows - 1) / b->tile_rows;
-    cap[f] = std::max<int64_t>(1, (tiles + ctx->tile_chunk - 1) / ctx->tile_chunk);
+    cap[f] = std::max<int64_t>(1, (tiles_of[f] + ctx->tile_chunk - 1) / ctx->tile_chunk);
   }
   std::vector<int> nb(F, 1);
   int left = G - F;
@@ -270,6 +282,41 @@ void fill_params(leo2d_batch* b) {
   }
 }
 
+// One batched step over all flakes: T_{k+1} from T_k (buffer parity k % 2).
+void step_launch(leo2d_batch* b, int k, double* partials, const double* prev_partials, const double* dots_pass,
+                 bool with_dots) {
+  leo2d_ctx* ctx = b->ctx;
+  const int C = b->shape.cols, F = (int)b->fl.size(), S = b->steps;
+  if (b->shape.rb) {
+    std::vector<RbBatchFlake> fl(F);
+    for (int f = 0; f < F; ++f) {
+      const FlakeView& v = b->fl[f];
+      const size_t off = (size_t)b->block_first[f] * 2 * C;
+      fl[f].csr = v.csr;
+      fl[f].tn = (k % 2 == 0 ? b->x0.p : b->x1.p) + v.row_off * C;
+      fl[f].tp = (k % 2 == 0 ? b->x1.p : b->x0.p) + v.row_off * C;
+      fl[f].first = k == 0;
+      fl[f].partials = partials + off;
+      fl[f].prev_partials = prev_partials ? prev_partials + off : nullptr;
+      fl[f].prev_dots =
+          with_dots && k > 0 ? const_cast<double*>(dots_pass) + ((size_t)f * S + (k - 1)) * 2 * C : nullptr;
+    }
+    rb_batch_launch(ctx, fl.data(), b->block_first.data(), F, b->shape.warps, b->dyn_smem);
+    return;
+  }
+  BatchParams<float>& p = b->params[k % 2];
+  for (int f = 0; f < F; ++f) {
+    StepArgs<float>& a = p.f[f].s;
+    const size_t off = (size_t)b->block_first[f] * 2 * C;
+    a.first = k == 0;
+    a.partials = partials + off;
+    a.prev_partials = prev_partials ? prev_partials + off : nullptr;
+    a.prev_dots =
+        with_dots && k > 0 ? const_cast<double*>(dots_pass) + ((size_t)f * S + (k - 1)) * 2 * C : nullptr;
+  }
+  batch_dispatch(ctx, C, b->grid, b->dyn_smem, &p, nullptr, 0, b->shape.warps);
+}
+
 // Enqueues one full run (all passes) on the context stream.
 void enqueue_run(leo2d_batch* b) {
   leo2d_ctx* ctx = b->ctx;
@@ -287,18 +334,9 @@ void enqueue_run(leo2d_batch* b) {
       });
     }
     double* dots = b->dots.p + (size_t)pass * F * S * 2 * C;
-    for (int k = 0; k < S; ++k) {
-      BatchParams<float>& p = b->params[k % 2];
-      for (int f = 0; f < F; ++f) {
-        StepArgs<float>& a = p.f[f].s;
-        const size_t off = (size_t)b->block_first[f] * 2 * C;
-        a.first = k == 0;
-        a.partials = b->partials.p + (size_t)(k % 2) * part + off;
-        a.prev_partials = k == 0 ? nullptr : b->partials.p + (size_t)((k + 1) % 2) * part + off;
-        a.prev_dots = k == 0 ? nullptr : dots + ((size_t)f * S + (k - 1)) * 2 * C;
-      }
-      batch_dispatch(ctx, C, b->grid, b->dyn_smem, &p, nullptr, 0, b->shape.warps);
-    }
+    for (int k = 0; k < S; ++k)
+      step_launch(b, k, b->partials.p + (size_t)(k % 2) * part,
+                  k == 0 ? nullptr : b->partials.p + (size_t)((k + 1) % 2) * part, dots, true);
     for (int f = 0; f < F; ++f) {
       const size_t off = (size_t)b->block_first[f] * 2 * C;
       batch_reduce(ctx, C, b->partials.p + (size_t)((S - 1) % 2) * part + off,
@@ -358,15 +396,7 @@ float time_steps(leo2d_batch* b, int reps) {
   cudaEvent_t e0 = ctx_event(ctx), e1 = ctx_event(ctx);
   for (int k = 0; k < reps + 1; ++k) {
     if (k == 1) LEO_CUDA(cudaEventRecord(e0, ctx->stream));
-    BatchParams<float>& p = b->params[k % 2];
-    for (int f = 0; f < F; ++f) {
-      StepArgs<float>& a = p.f[f].s;
-      a.first = k == 0;
-      a.partials = b->partials.p + (size_t)(k % 2) * part + (size_t)b->block_first[f] * 2 * C;
-      a.prev_partials = nullptr;
-      a.prev_dots = nullptr;
-    }
-    batch_dispatch(ctx, C, b->grid, b->dyn_smem, &p, nullptr, 0, b->shape.warps);
+    step_launch(b, k, b->partials.p + (size_t)(k % 2) * part, nullptr, nullptr, false);
   }
   LEO_CUDA(cudaEventRecord(e1, ctx->stream));
   LEO_CUDA(cudaEventSynchronize(e1));
@@ -404,17 +434,24 @@ leo2d_status leo2d_batch_create(leo2d_ctx* ctx, const leo2d_csr* const* csrs, in
     b->steps = cfg->poly_order / 2;
     b->R = cfg->num_vectors;
     int64_t off = 0;
+    bool rb_mode = (cfg->block == 0 || cfg->block == 32) && ctx->reorder != 0 && ctx->kernel_variant != 0 &&
+                   ctx->kernel_variant != 1;
+    for (int f = 0; f < num; ++f)
+      rb_mode = rb_mode && csrs[f] && csrs[f]->pos.p != nullptr && csrs[f]->nnz > 0;
     for (int f = 0; f < num; ++f) {
       const leo2d_csr* m = csrs[f];
       LEO_REQUIRE(m != nullptr && m->n > 0, "batch matrix is null or empty");
       for (int g = 0; g < f; ++g) LEO_REQUIRE(csrs[g] != m, "a matrix appears twice in the batch");
       leo2d_csr* mm = const_cast<leo2d_csr*>(m);
       LEO_REQUIRE(m->ent.p != nullptr || m->nnz == 0, "matrix has no FP32 values");
-      const bool perm = m->pos.p != nullptr && m->nnz > 0 &&
-                        (ctx->reorder == 1 || (ctx->reorder == -1 && m->n >= 100000));
-      if (perm && (!m->reordered || m->reorder_patch != reorder_patch_for(ctx, false) ||
-                   m->reorder_curve_req != ctx->reorder_curve))
-        csr_build_reordered(ctx, mm, reorder_patch_for(ctx, false), m->reorder_fp64, ctx->reorder_curve != 0);
+      // the row-block step (every flake ordered, 32 columns) unless the tiled step is asked for
+      const bool perm = rb_mode || (m->pos.p != nullptr && m->nnz > 0 &&
+                                    (ctx->reorder == 1 || (ctx->reorder == -1 && m->n >= 100000)));
+      const double patch = reorder_patch_for(ctx, rb_mode);
+      if (perm && (!m->reordered || m->reorder_patch != patch || m->reorder_curve_req != ctx->reorder_curve))
+        csr_build_reordered(ctx, mm, patch, m->reorder_fp64, ctx->reorder_curve != 0);
+      if (rb_mode && (!m->rb_built || m->rb_patch != m->reorder_patch))
+        LEO_REQUIRE(csr_build_rb(ctx, mm), "a batched flake's row blocks exceed the build limits");
       FlakeView v;
       v.csr = m;
       v.n = m->n;
@@ -434,8 +471,9 @@ leo2d_status leo2d_batch_create(leo2d_ctx* ctx, const leo2d_csr* const* csrs, in
     // shape: the caller's, or the fastest estimated run time over widths,
     // warps and rows per slot (each candidate timed on real batched steps)
     std::vector<BatchShape> cands;
+    if (rb_mode) cands.push_back(BatchShape{32, 24, 0, true});
     const int widths[5] = {8, 16, 32, 64, 128};
-    for (int w : widths) {
+    for (int w : rb_mode ? std::vector<int>() : std::vector<int>(widths, widths + 5)) {
       if (cfg->block && w != cfg->block) continue;
       if (!cfg->block && w > 2 * ((2 * b->R + 7) / 8 * 4)) continue;  // wider than the vectors need
       for (int warps : {8, 24})
@@ -444,7 +482,7 @@ leo2d_status leo2d_batch_create(leo2d_ctx* ctx, const leo2d_csr* const* csrs, in
           cands.push_back(BatchShape{w, warps, cfg->rows_per_warp ? cfg->rows_per_warp : ri});
         }
     }
-    if (cands.empty()) cands.push_back(BatchShape{cfg->block ? cfg->block : 32, 8, cfg->rows_per_warp});
+    if (cands.empty()) cands.push_back(BatchShape{cfg->block ? cfg->block : 32, 8, cfg->rows_per_warp, false});
     BatchShape best;
     double best_t = 1e300;
     if (cands.size() == 1) {

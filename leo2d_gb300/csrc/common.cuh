@@ -113,7 +113,8 @@ struct leo2d_ctx {
   int rb_unroll = 0;          // row-block step: slot batches in flight per lane: 0 autotuned, 4, 8
   int rb_window = -1;         // row-block step over shared-memory windows: -1 autotuned, 0 no, 1 yes
   int rt_warps = 0;           // 8-row tensor-core step: warps per CTA: 0 autotuned, 8, 12, 16, 24
-  int rt_depth = 0;           // 8-row tensor-core step: k-steps of T_n rows in flight per warp: 0 autotuned, 2, 3, 4, 6
+  int rt_depth = 0;           // 8-row tensor-core step: k-steps of T_n rows in flight per warp: 0 autotuned,
+                              // 2, 3, 4, 6 (rows in registers) or 3, 7 (shared memory)
   int rt_stage = -1;          // 8-row tensor-core step: T_n rows staged in -1 autotuned, 0 registers, 1 shared memory
   int rt_group = 0;           // 8-row tensor-core step: consecutive blocks per warp run: 0 default (2), 1..16
   int rt_chunk = 0;           // 8-row tensor-core step: tiles per CTA between grid-wide jumps: 0 default (2)

@@ -525,9 +525,8 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
     s.rb_warps = 24;
   }
   s.rt_warps = ctx->rt_warps > 0 ? ctx->rt_warps : (cached && it->second.rt_warps > 0 ? it->second.rt_warps : 16);
-  s.rt_regs = ctx->rt_stage >= 0 ? ctx->rt_stage == 0 : (cached && it->second.rt ? it->second.rt_regs : true);
-  s.rt_depth = ctx->rt_depth > 0 ? ctx->rt_depth
-                                 : (cached && it->second.rt_depth > 0 ? it->second.rt_depth : (s.rt_regs ? 3 : 4));
+  s.rt_regs = ctx->rt_stage >= 0 ? ctx->rt_stage == 0 : (cached && it->second.rt ? it->second.rt_regs : false);
+  s.rt_depth = ctx->rt_depth > 0 ? ctx->rt_depth : (cached && it->second.rt_depth > 0 ? it->second.rt_depth : 3);
   LEO_REQUIRE(s.rows_per_item >= 0 && s.rows_per_item <= 64, "rows_per_warp must be 0..64");
   return s;
 }
@@ -826,8 +825,8 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
       if (!fp64 && cols == 32 && !csr->complex_h && ctx->reorder != 0 &&
           (ctx->kernel_variant == -1 || ctx->kernel_variant == 5)) {
         struct RtTry { int warps, depth; bool regs; };
-        for (const RtTry t : {RtTry{16, 3, true}, RtTry{16, 2, true}, RtTry{12, 4, true}, RtTry{16, 4, false},
-                              RtTry{16, 3, false}}) {
+        for (const RtTry t : {RtTry{16, 3, false}, RtTry{16, 2, true}, RtTry{12, 7, false}, RtTry{8, 7, false},
+                              RtTry{16, 3, true}}) {
           if (ctx->rt_stage >= 0 && (ctx->rt_stage == 0) != t.regs) continue;
           StepShape sh = choose_shape(ctx, csr, fp64, cols, cols, 0);
           sh.tc = false;

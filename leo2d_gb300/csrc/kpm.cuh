@@ -21,8 +21,8 @@ struct StepShape {
   bool rb_window = false;  // row-block step over shared-memory windows (rbw_spmm.cu)
   bool rt = false;         // 8-row blocks on the tensor cores (rt_spmm.cu; FP32, 32 columns)
   int rt_warps = 16;       // 8-row step: warps per CTA (8, 12, 16, 24)
-  int rt_depth = 4;        // 8-row step: k-steps of T_n rows in flight per warp (2, 3, 4, 6)
-  bool rt_regs = true;     // 8-row step: T_n rows staged in registers (else shared memory)
+  int rt_depth = 3;        // 8-row step: k-steps of T_n rows in flight per warp (registers 2, 3, 4, 6; shared 3, 7)
+  bool rt_regs = false;    // 8-row step: T_n rows staged in registers (else shared memory)
 };
 
 // Vector block resident on the device: two buffers of n x cols (T_k, T_{k-1}).
@@ -87,6 +87,24 @@ int rt_chunk_of(const leo2d_ctx* ctx);
 void rt_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape, unsigned grid, size_t smem,
                     const float* tn, float* tp, const float* tprev, int first, float alpha, double* partials,
                     const double* prev_partials, double* prev_dots);
+
+// The row-block step over several matrices (flakes) in one launch: flake f runs
+// on CTAs [block_first[f], block_first[f+1]) with its own vectors and partials.
+constexpr int kRbBatchMax = 64;
+struct RbBatchFlake {
+  const leo2d_csr* csr = nullptr;
+  const float* tn = nullptr;
+  float* tp = nullptr;
+  double* partials = nullptr;
+  const double* prev_partials = nullptr;
+  double* prev_dots = nullptr;
+  int first = 0;
+};
+// shared memory of the widest flake's stages; the tiles of a matrix (chunk units)
+size_t rb_batch_smem(leo2d_ctx* ctx, const leo2d_csr* const* csrs, int n, int warps);
+int64_t rb_tiles(const leo2d_csr* csr, int warps);
+void rb_batch_launch(leo2d_ctx* ctx, const RbBatchFlake* fl, const int* block_first, int nflakes, int warps,
+                     size_t smem);
 
 // The windowed row-block step (rbw_spmm.cu), as above.
 int rbw_stages(leo2d_ctx* ctx, leo2d_csr* csr);

@@ -35,6 +35,7 @@
 //   CSR kernels. Every wait is bounded (two seconds or the context's poll
 //   limit) and reports a status.
 #include <algorithm>
+#include <cstring>
 #include <cmath>
 
 #include "kpm.cuh"
@@ -82,8 +83,10 @@ struct RbArgs {
   int never_wait;  // test hook: wait on a barrier that nobody completes
 };
 
+// One CTA's share of a step: CTA `bid` of `nblk` working on the matrix of `a`
+// (the whole grid for one matrix, a block group of a batched launch).
 template <int WARPS, bool PACKED, int U, bool CPX = false, bool DJ = false>
-__global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant__ RbArgs a) {
+__device__ __forceinline__ void rb_body(const RbArgs& a, const int bid, const int nblk) {
   constexpr int C = 32;
   constexpr int NT = WARPS * 32;
   constexpr int kMaxStages = 4;
@@ -92,7 +95,6 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
   __shared__ int released[kMaxStages];
   __shared__ int issued[kMaxStages];
   __shared__ __align__(8) uint64_t never;
-  const int bid = (int)blockIdx.x, nblk = (int)gridDim.x;
   if (a.prev_partials) reduce_prev<C, NT>(a.prev_partials, a.prev_dots, nblk, bid, nblk);
 
   const int nst = a.stages;
@@ -357,6 +359,28 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant
     __syncthreads();
   }
   for (int t = threadIdx.x; t < 2 * C; t += NT) a.partials[(size_t)bid * 2 * C + t] = bsum[t];
+}
+
+template <int WARPS, bool PACKED, int U, bool CPX = false, bool DJ = false>
+__global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb(const __grid_constant__ RbArgs a) {
+  rb_body<WARPS, PACKED, U, CPX, DJ>(a, (int)blockIdx.x, (int)gridDim.x);
+}
+
+// Several matrices in one launch: matrix f runs on the CTAs [block_first[f],
+// block_first[f+1]) as block group of its own (tiles, partials and the deferred
+// reduction stay within the matrix).
+struct RbBatchParams {
+  RbArgs f[kRbBatchMax];
+  int block_first[kRbBatchMax + 1];
+  int nflakes;
+};
+static_assert(sizeof(RbBatchParams) <= 32764, "batched row-block parameters exceed the parameter space");
+
+template <int WARPS, bool PACKED, int U>
+__global__ void __launch_bounds__(WARPS * 32, 1) k_cheb_rb_batch(const __grid_constant__ RbBatchParams p) {
+  int f = 0;
+  while (f + 1 < p.nflakes && (int)blockIdx.x >= p.block_first[f + 1]) ++f;
+  rb_body<WARPS, PACKED, U>(p.f[f], (int)blockIdx.x - p.block_first[f], p.block_first[f + 1] - p.block_first[f]);
 }
 
 // ---------------------------------------------------------------- format build
@@ -950,6 +974,59 @@ void rb_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
 #undef LEO2D_RB_W
 #undef LEO2D_RB_CASE
   fail(LEO2D_ERR_BAD_ARG, "row-block warps must be 16, 24 or 32 and batches 4 or 8");
+}
+
+size_t rb_batch_smem(leo2d_ctx* ctx, const leo2d_csr* const* csrs, int n, int warps) {
+  size_t m = 0;
+  for (int f = 0; f < n; ++f) {
+    leo2d_csr* c = const_cast<leo2d_csr*>(csrs[f]);
+    LEO_REQUIRE(rb_stages(ctx, c, warps) >= 2, "row blocks of a batched matrix do not fit shared memory");
+    m = std::max(m, rb_smem_bytes(ctx, c, warps));
+  }
+  return m;
+}
+
+int64_t rb_tiles(const leo2d_csr* csr, int warps) { return (csr->rb_blocks + warps - 1) / warps; }
+
+void rb_batch_launch(leo2d_ctx* ctx, const RbBatchFlake* fl, const int* block_first, int nflakes, int warps,
+                     size_t smem) {
+  LEO_REQUIRE(nflakes >= 1 && nflakes <= kRbBatchMax, "a row-block batch holds 1..64 matrices");
+  LEO_REQUIRE(warps == 24, "the batched row-block step runs 24 warps");
+  RbBatchParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.nflakes = nflakes;
+  for (int f = 0; f <= nflakes; ++f) p.block_first[f] = block_first[f];
+  for (int f = 0; f < nflakes; ++f) {
+    leo2d_csr* m = const_cast<leo2d_csr*>(fl[f].csr);
+    LEO_REQUIRE(m->rb_built && !m->complex_h, "a batched matrix lacks its row blocks");
+    RbArgs& a = p.f[f];
+    a.n = m->n;
+    a.nrb = m->rb_blocks;
+    a.off = m->rb_off.p;
+    a.data = m->rb_data.p;
+    a.tn = fl[f].tn;
+    a.tp = fl[f].tp;
+    a.tprev = nullptr;
+    a.first = fl[f].first;
+    a.alpha = 0.0f;
+    a.partials = fl[f].partials;
+    a.prev_partials = fl[f].prev_partials;
+    a.prev_dots = fl[f].prev_dots;
+    a.stages = rb_stages(ctx, m, warps);
+    LEO_REQUIRE(a.stages >= 2 && (size_t)a.stages * rb_stage_bytes(ctx, m, warps, false) <= smem,
+                "batched row-block shared memory changed since setup");
+    a.chunk = std::max(1, ctx->tile_chunk);
+    a.off_bytes = rb_off_bytes(warps);
+    a.stage_bytes = (int)rb_stage_bytes(ctx, m, warps, false);
+    a.panel_at = (int)(a.stage_bytes - rb_panel_bytes(ctx, m, warps, false));
+    a.spin_limit = ctx->spin_limit;
+    a.status = ctx->status.p;
+    a.never_wait = ctx->test_unsatisfied_wait;
+  }
+  auto kern = k_cheb_rb_batch<24, true, 8>;
+  LEO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  launch(ctx, "cheb_batch_step",
+         [&] { kern<<<(unsigned)block_first[nflakes], warps * 32, smem, ctx->stream>>>(p); });
 }
 
 }  // namespace leo2d

@@ -24,14 +24,14 @@
 //   valid column with zero values). Slots go in k-steps of 8; a k-step is
 //   288 bytes:
 //     int32 col[8]       slots in the order 0 4 1 5 2 6 3 7, so lane q of a
-//                        quarter-warp reads (slot q, slot q + 4) as one int2;
-//                        bit 31 of the last entry marks the block's last k-step
+//                        quarter-warp reads (slot q, slot q + 4) as one int2
 //     float2 v[32]       lane 4g + t holds (V[row g][slot t], V[row g][slot t+4]),
 //                        the B fragment of mma.m16n8k8 (B = V^T, k = slot, n = row)
 //   Blocks are stored in the order the kernel processes them: warp w of CTA c
 //   takes runs of G consecutive blocks (one run per tile of W runs, tiles in
 //   chunked round-robin over the CTAs), so each warp streams one contiguous
-//   range of k-steps, rt_wbeg[c W + w] .. rt_wbeg[c W + w + 1].
+//   range of k-steps, rt_wbeg[c W + w] .. rt_wbeg[c W + w + 1]; rt_kst holds
+//   each block's k-step count (the kernel's block boundaries).
 // Kernel (one CTA per SM, W warps, no CTA-wide barrier in the main loop)
 //   Each warp runs a software pipeline over its k-steps with cp.async groups:
 //   at iteration u it copies the matrix data of k-step u + D + DM (cp.async.cg,
@@ -93,6 +93,7 @@ struct RtArgs {
   int64_t nrb;  // row blocks
   const unsigned char* __restrict__ data;  // k-steps in processing order
   const int64_t* __restrict__ wbeg;        // [grid * W + 1] first k-step of each warp
+  const int64_t* __restrict__ kst;         // [blocks] k-steps of each block
   const float* __restrict__ tn;
   float* __restrict__ tp;
   const float* __restrict__ tprev;  // null: T_{n-1} is read from tp
@@ -112,9 +113,10 @@ namespace {
 // ---------------------------------------------------------------- the step kernels
 
 // FP32 products from TF32 units: x = hi + lo with hi = x with its low 13
-// mantissa bits cleared (a TF32 value) and lo = x - hi (exact) cleared the same
-// way; the product is taken as lo*hi + hi*lo + hi*hi. The dropped lo*lo term and
-// the truncation of lo leave a relative error below 2^-20 per product. The
+// mantissa bits cleared (a TF32 value) and lo = x - hi (exact); the tensor core
+// reads the TF32 bits of each operand (the top 19) and ignores the rest, so lo
+// enters truncated. The product is taken as lo*hi + hi*lo + hi*hi; the dropped
+// lo*lo term and the truncation of lo leave a relative error below 2^-20. The
 // hi*hi terms and the two cross terms go to separate FP32 accumulators (four
 // independent MMA chains per k-step), summed at the block's end.
 struct RtAcc {
@@ -131,11 +133,11 @@ struct RtAcc {
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       ah[i] = __float_as_uint(xs[i]) & m;
-      al[i] = __float_as_uint(xs[i] - __uint_as_float(ah[i])) & m;
+      al[i] = __float_as_uint(xs[i] - __uint_as_float(ah[i]));
     }
     const uint32_t bh0 = __float_as_uint(v.x) & m, bh1 = __float_as_uint(v.y) & m;
-    const uint32_t bl0 = __float_as_uint(v.x - __uint_as_float(bh0)) & m;
-    const uint32_t bl1 = __float_as_uint(v.y - __uint_as_float(bh1)) & m;
+    const uint32_t bl0 = __float_as_uint(v.x - __uint_as_float(bh0));
+    const uint32_t bl1 = __float_as_uint(v.y - __uint_as_float(bh1));
     // logical columns g, g + 8 (m-tile 0) and g + 16, g + 24 (m-tile 1)
     mma_tf32(l0, al[0], al[1], al[4], al[5], bh0, bh1);
     mma_tf32(l1, al[2], al[3], al[6], al[7], bh0, bh1);
@@ -164,7 +166,9 @@ __device__ __forceinline__ float2 ld_stream_f2(const void* p) {
 
 // One kernel, two ways of staging the gathered T_n rows:
 //  - REGS = false: cp.async copies into a per-warp shared-memory ring (see the
-//    file comment), D k-steps ahead, the matrix data DM ahead of those;
+//    file comment) D = XS - 1 k-steps ahead, the matrix data MS - 1 ahead; both
+//    rings are powers of two and the main loop is unrolled over the matrix ring,
+//    so every slot is a compile-time constant;
 //  - REGS = true: no shared memory, so the whole L1 caches T_n rows. Lane (q, p)
 //    loads 16-byte chunk p of the T_n rows of slots q and q + 4 (one 128-byte row
 //    per quarter-warp, one L1 wavefront per slot) D k-steps ahead into registers,
@@ -174,19 +178,20 @@ __device__ __forceinline__ float2 ld_stream_f2(const void* p) {
 //    k-steps ahead (they address the row loads), the values D ahead.
 // Either way the matrix stream is prefetched into L2 in bulk further ahead.
 // Each warp walks its blocks in the build's processing order: runs of G
-// consecutive blocks, run i in tile (bid + (i / chunk) grid) chunk + i % chunk.
-template <int W, int D, int DM, bool REGS>
-__global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ RtArgs a) {
+// consecutive blocks, run i in tile (bid + (i / chunk) grid) chunk + i % chunk;
+// a block ends after its k-step count (kst), read one block ahead.
+template <int W, int D, bool REGS>
+__device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const int nblk) {
   constexpr int C = 32;
   constexpr int NT = W * 32;
-  constexpr int XS = D + 1;       // shared ring of staged T_n rows (k-steps)
-  constexpr int MS = D + DM + 1;  // shared ring of matrix k-steps
+  constexpr int XS = D + 1;      // shared ring of staged T_n rows (k-steps)
+  constexpr int MS = 2 * XS;     // shared ring of matrix k-steps
+  constexpr int DM = MS - 1 - D; // matrix lookahead beyond the rows'
   constexpr int kWarpBytes = REGS ? 0 : XS * 1024 + MS * kRtStepBytes;
   constexpr int kPf = REGS ? 48 : 32;  // matrix k-steps prefetched into L2 ahead
   constexpr int kDotFlush = 16;        // blocks summed in FP32 between FP64 flushes
-  static_assert(REGS || DM >= D + 1, "the matrix lookahead must exceed the row lookahead");
+  static_assert(REGS || ((XS & (XS - 1)) == 0 && DM >= D + 1), "power-of-two rings, matrix ahead of the rows");
   extern __shared__ __align__(1024) unsigned char rt_smem[];
-  const int bid = (int)blockIdx.x, nblk = (int)gridDim.x;
   if (a.prev_partials) reduce_prev<C, NT>(a.prev_partials, a.prev_dots, nblk, bid, nblk);
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -198,18 +203,21 @@ __global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ R
   const float* tprev = a.tprev ? a.tprev : a.tp;
   float* tp = a.tp;
   const float* tnc = a.tn + 4 * cg;
-  const float* tnp = a.tn + 4 * p;
+  const unsigned char* tnb = reinterpret_cast<const unsigned char*>(a.tn + 4 * p);  // + column * 128
+  const int64_t* kst = a.kst;
   const int64_t k0 = a.wbeg[bid * W + warp];
   const int nk = (int)(a.wbeg[bid * W + warp + 1] - k0);
   const unsigned char* gdata = a.data + k0 * kRtStepBytes;
 
-  // block walk and epilogue operands
+  // block walk, block-end countdown and epilogue operands
   int jb = 0, irun = 0;
   auto run_row0 = [&](int i) -> int64_t {
     const int tile = (bid + (i / chunk) * nblk) * chunk + i % chunk;
     return ((int64_t)tile * W + warp) * group * kRtRows;
   };
   int64_t rbase = run_row0(0), row0 = 0;
+  int left = 0;                                       // k-steps of the current block still to run
+  int next_left = nk > 0 ? (int)kst[rbase / kRtRows] : 0;  // the next block's k-steps
   float4 xn0 = make_float4(0.f, 0.f, 0.f, 0.f), xn1 = xn0, xp0 = xn0, xp1 = xn0;
   // dots: FP32 over kDotFlush blocks, then FP64; lane (g, t) ends with column 4 cg + t
   double d0 = 0.0, d1 = 0.0;
@@ -239,6 +247,10 @@ __global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ R
   };
   auto begin_block = [&]() {
     row0 = rbase + (int64_t)jb * kRtRows;
+    left = next_left;
+    // the k-steps of the block after this one (its run may start elsewhere)
+    const int64_t nrow = jb + 1 < group ? row0 + kRtRows : run_row0(irun + 1);
+    if (nrow / kRtRows < a.nrb) next_left = (int)kst[nrow / kRtRows];
     const int64_t r0 = row0 + 2 * t;
     if (r0 < n) {
       xn0 = ldg4(tnc + r0 * C);
@@ -282,73 +294,70 @@ __global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ R
       flush();
     }
   };
-  bool start = true;
+  // the MMAs of one k-step, with the block walk around them
+  auto consume = [&](const float4& fa, const float4& fb, const float2& v) {
+    if (left == 0) begin_block();
+    acc.add(fa, fb, v);
+    if (--left == 0) end_block();
+  };
 
   if constexpr (!REGS) {
     unsigned char* xr = rt_smem + (size_t)warp * kWarpBytes;
     unsigned char* mr = xr + XS * 1024;
-    const unsigned char* msrc = gdata + 16 * lane;
+    const bool mlane = lane < kRtStepBytes / 16;
+    const unsigned char* msrc = gdata + 16 * lane;  // this lane's chunk of matrix k-step u + D + DM
     // per-lane offsets in a row-ring entry: writes (slot q and q + 4, chunk p) and
     // reads (slot t and t + 4, chunk cg), 16-byte chunk c of row s at c ^ s
     const int wo0 = q * 128 + 16 * (p ^ q), wo1 = 512 + q * 128 + 16 * (p ^ (q + 4));
     const int ro0 = t * 128 + 16 * (cg ^ t), ro1 = 512 + t * 128 + 16 * (cg ^ (t + 4));
-    int im = 0;                      // matrix slot of k-step u + D + DM
-    int ix = (XS - (DM % XS)) % XS;  // row slot of k-step u + D
-    for (int u = -(D + DM); u < nk; ++u) {
+    // iteration u (matrix slot sm = u mod MS): copy matrix k-step u + D + DM and the
+    // rows of k-step u + D, wait for k-step u's rows, run its MMAs
+    auto iter = [&](int u, int sm, bool checks) {
       __syncwarp();  // every lane is done with the entries these copies overwrite
       const int vm = u + D + DM, vx = u + D;
-      if (vm < nk && lane < kRtStepBytes / 16) cp_async_cg16(mr + im * kRtStepBytes + 16 * lane, msrc);
+      if (mlane && (!checks || vm < nk)) cp_async_cg16(mr + ((sm + MS - 1) & (MS - 1)) * kRtStepBytes + 16 * lane, msrc);
       msrc += kRtStepBytes;
       if (lane == 0 && (vm & 7) == 0 && vm + kPf < nk)
-        prefetch_l2_bulk(gdata + (size_t)(vm + kPf) * kRtStepBytes,
-                         (uint32_t)min(8, nk - vm - kPf) * kRtStepBytes);
-      if (vx >= 0 && vx < nk) {
-        // the columns of k-step vx landed DM iterations ago (slot im - DM)
-        const int jm = im >= DM ? im - DM : im + MS - DM;
-        const int2 cc = *reinterpret_cast<const int2*>(mr + jm * kRtStepBytes + 8 * q);
-        unsigned char* dst = xr + ix * 1024;
-        cp_async_ca16(dst + wo0, tnp + (size_t)(uint32_t)(cc.x & 0x7fffffff) * C);
-        cp_async_ca16(dst + wo1, tnp + (size_t)(uint32_t)(cc.y & 0x7fffffff) * C);
+        prefetch_l2_bulk(gdata + (size_t)(vm + kPf) * kRtStepBytes, (uint32_t)min(8, nk - vm - kPf) * kRtStepBytes);
+      if (!checks || (vx >= 0 && vx < nk)) {
+        // the columns of k-step vx landed DM iterations ago
+        const int2 cc = *reinterpret_cast<const int2*>(mr + ((sm + D) & (MS - 1)) * kRtStepBytes + 8 * q);
+        unsigned char* dst = xr + ((sm + D) & (XS - 1)) * 1024;
+        cp_async_ca16(dst + wo0, tnb + (uint64_t)(uint32_t)cc.x * (C * 4));
+        cp_async_ca16(dst + wo1, tnb + (uint64_t)(uint32_t)cc.y * (C * 4));
       }
       cp_async_commit();
       cp_async_wait<D>();  // k-step u's rows (and k-step u + D + 1's matrix data) have landed
       __syncwarp();
-      im = im == MS - 1 ? 0 : im + 1;  // now the slot of matrix k-step u
-      ix = ix == XS - 1 ? 0 : ix + 1;  // now the slot of row k-step u
-      if (u < 0) continue;
-      if (start) {
-        begin_block();
-        start = false;
-      }
-      const unsigned char* xs = xr + ix * 1024;
-      const unsigned char* ms = mr + im * kRtStepBytes;
-      const float4 fa = *reinterpret_cast<const float4*>(xs + ro0);
-      const float4 fb = *reinterpret_cast<const float4*>(xs + ro1);
-      const float2 v = *reinterpret_cast<const float2*>(ms + 32 + 8 * lane);
-      const bool last = *reinterpret_cast<const int*>(ms + 28) < 0;
-      acc.add(fa, fb, v);
-      if (last) {  // warp-uniform: the block's epilogue
-        end_block();
-        start = true;
-      }
+      if (checks && u < 0) return;
+      const unsigned char* xs = xr + (sm & (XS - 1)) * 1024;
+      const unsigned char* ms = mr + sm * kRtStepBytes;
+      consume(*reinterpret_cast<const float4*>(xs + ro0), *reinterpret_cast<const float4*>(xs + ro1),
+              *reinterpret_cast<const float2*>(ms + 32 + 8 * lane));
+    };
+    int u = -(D + DM);
+    for (; u < 0; ++u) iter(u, u & (MS - 1), true);
+    const int main_end = nk - (D + DM) > 0 ? ((nk - (D + DM)) & ~(MS - 1)) : 0;
+    for (; u < main_end; u += MS) {
+#pragma unroll
+      for (int j = 0; j < MS; ++j) iter(u + j, j, false);
     }
+    for (; u < nk; ++u) iter(u, u & (MS - 1), true);
     cp_async_wait<0>();
   } else {
     const int src = 8 * t + cg;  // the lane holding chunk cg of slots t and t + 4
-    // rings (slot j = k-step mod D): columns of k-steps u + D .. u + 2D - 1, rows,
-    // values and block-end flags of k-steps u .. u + D - 1
+    // rings (slot j = k-step mod D): columns of k-steps u + D .. u + 2D - 1, rows
+    // and values of k-steps u .. u + D - 1
     int2 cc[D];
 #pragma unroll
     for (int j = 0; j < D; ++j) cc[j] = make_int2(0, 0);
     float4 xa[D], xb[D];
     float2 vv[D];
-    bool lastf[D];
     auto load_cols = [&](int v) { return ld_stream_i2(gdata + (size_t)v * kRtStepBytes + 8 * q); };
     auto issue = [&](int j, int v) {  // k-step v (its columns in cc[j]) into slot j
       const int2 c = cc[j];
-      lastf[j] = __any_sync(0xffffffffu, q == 3 && c.y < 0);
-      xa[j] = ldg4(tnp + (size_t)(uint32_t)(c.x & 0x7fffffff) * C);
-      xb[j] = ldg4(tnp + (size_t)(uint32_t)(c.y & 0x7fffffff) * C);
+      xa[j] = ldg4(reinterpret_cast<const float*>(tnb + (uint64_t)(uint32_t)c.x * (C * 4)));
+      xb[j] = ldg4(reinterpret_cast<const float*>(tnb + (uint64_t)(uint32_t)c.y * (C * 4)));
       vv[j] = ld_stream_f2(gdata + (size_t)v * kRtStepBytes + 32 + 8 * lane);
     };
     if (lane == 0 && kPf < nk)
@@ -368,10 +377,6 @@ __global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ R
       for (int j = 0; j < D; ++j) {
         const int u = u0 + j;
         if (u >= nk) break;  // warp-uniform
-        if (start) {
-          begin_block();
-          start = false;
-        }
         float4 fa, fb;
         fa.x = __shfl_sync(0xffffffffu, xa[j].x, src);
         fa.y = __shfl_sync(0xffffffffu, xa[j].y, src);
@@ -382,7 +387,6 @@ __global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ R
         fb.z = __shfl_sync(0xffffffffu, xb[j].z, src);
         fb.w = __shfl_sync(0xffffffffu, xb[j].w, src);
         const float2 v = vv[j];
-        const bool last = lastf[j];
         // the slot is free: k-step u + D goes into it, and the columns of u + 2D
         if (u + D < nk) {
           issue(j, u + D);
@@ -391,11 +395,7 @@ __global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ R
         if (lane == 0 && ((u + D) & 7) == 0 && u + D + kPf < nk)
           prefetch_l2_bulk(gdata + (size_t)(u + D + kPf) * kRtStepBytes,
                            (uint32_t)min(8, nk - (u + D + kPf)) * kRtStepBytes);
-        acc.add(fa, fb, v);
-        if (last) {
-          end_block();
-          start = true;
-        }
+        consume(fa, fb, v);
       }
     }
   }
@@ -415,6 +415,11 @@ __global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ R
   for (int i = threadIdx.x; i < 2 * C; i += NT) a.partials[(size_t)bid * 2 * C + i] = bsum[i];
 }
 
+template <int W, int D, bool REGS>
+__global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ RtArgs a) {
+  rt_body<W, D, REGS>(a, (int)blockIdx.x, (int)gridDim.x);
+}
+
 // ---------------------------------------------------------------- format build
 
 // One warp per block of 8 rows, at most kRtMaxEnt stored entries: the keys
@@ -422,7 +427,7 @@ __global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ R
 // the distinct columns are the slots. Pass 0 writes the k-steps of each block;
 // pass 1 writes the block's k-steps at kstart[b] (data zero-filled before): the
 // columns in the interleaved order, the values in fragment order, entries of
-// one (row, column) summed in entry order, and the last k-step's flag.
+// one (row, column) summed in entry order.
 __global__ void __launch_bounds__(kRtBuildWarps * 32)
     k_rt_build(int64_t n, int64_t nrb, const int64_t* __restrict__ prow, const int32_t* __restrict__ pcol,
                const float* __restrict__ pval, int pass, int64_t* __restrict__ kst,
@@ -544,11 +549,6 @@ __global__ void __launch_bounds__(kRtBuildWarps * 32)
         vp[2 * (4 * r + (jj & 3)) + (jj >> 2)] = v;
       }
     }
-    __syncwarp();  // every column entry is written before the flag goes on
-    if (lane == 0) {
-      int32_t* lastc = reinterpret_cast<int32_t*>(base + (size_t)(KS - 1) * kRtStepBytes) + 7;
-      *lastc = (int32_t)((uint32_t)*lastc | 0x80000000u);
-    }
   }
 }
 
@@ -591,8 +591,9 @@ RtShape rt_shape(const leo2d_ctx* ctx, int64_t n, int warps, int group, int chun
   return s;
 }
 
-// Smem of one warp's rings for lookahead D (matrix lookahead D + 2).
-constexpr int rt_warp_bytes(int depth) { return (depth + 1) * 1024 + (2 * depth + 3) * kRtStepBytes; }
+// Shared memory of one warp's rings for row lookahead D (rows: D + 1 k-steps,
+// matrix: 2 (D + 1) k-steps).
+constexpr int rt_warp_bytes(int depth) { return (depth + 1) * 1024 + 2 * (depth + 1) * kRtStepBytes; }
 
 }  // namespace
 
@@ -730,6 +731,7 @@ void rt_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
   a.nrb = csr->rt_blocks;
   a.data = csr->rt_data.p;
   a.wbeg = csr->rt_wbeg.p;
+  a.kst = csr->rt_kst.p;
   a.tn = tn;
   a.tp = tp;
   a.tprev = tprev;
@@ -749,29 +751,24 @@ void rt_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
   const int key = shape.rt_warps * 10 + shape.rt_depth;
   if (shape.rt_regs) {
     switch (key) {
-      case 162: return go(k_cheb_rt<16, 2, 0, true>, 16);
-      case 163: return go(k_cheb_rt<16, 3, 0, true>, 16);
-      case 164: return go(k_cheb_rt<16, 4, 0, true>, 16);
-      case 124: return go(k_cheb_rt<12, 4, 0, true>, 12);
-      case 126: return go(k_cheb_rt<12, 6, 0, true>, 12);
-      case 86: return go(k_cheb_rt<8, 6, 0, true>, 8);
+      case 162: return go(k_cheb_rt<16, 2, true>, 16);
+      case 163: return go(k_cheb_rt<16, 3, true>, 16);
+      case 164: return go(k_cheb_rt<16, 4, true>, 16);
+      case 124: return go(k_cheb_rt<12, 4, true>, 12);
+      case 126: return go(k_cheb_rt<12, 6, true>, 12);
+      case 86: return go(k_cheb_rt<8, 6, true>, 8);
     }
     fail(LEO2D_ERR_BAD_ARG, "8-row step in registers: warps 16 (depth 2, 3, 4), 12 (4, 6) or 8 (6)");
   }
   switch (key) {
-    case 83: return go(k_cheb_rt<8, 3, 5, false>, 8);
-    case 84: return go(k_cheb_rt<8, 4, 6, false>, 8);
-    case 86: return go(k_cheb_rt<8, 6, 8, false>, 8);
-    case 123: return go(k_cheb_rt<12, 3, 5, false>, 12);
-    case 124: return go(k_cheb_rt<12, 4, 6, false>, 12);
-    case 126: return go(k_cheb_rt<12, 6, 8, false>, 12);
-    case 163: return go(k_cheb_rt<16, 3, 5, false>, 16);
-    case 164: return go(k_cheb_rt<16, 4, 6, false>, 16);
-    case 166: return go(k_cheb_rt<16, 6, 8, false>, 16);
-    case 243: return go(k_cheb_rt<24, 3, 5, false>, 24);
-    case 244: return go(k_cheb_rt<24, 4, 6, false>, 24);
+    case 83: return go(k_cheb_rt<8, 3, false>, 8);
+    case 87: return go(k_cheb_rt<8, 7, false>, 8);
+    case 123: return go(k_cheb_rt<12, 3, false>, 12);
+    case 127: return go(k_cheb_rt<12, 7, false>, 12);
+    case 163: return go(k_cheb_rt<16, 3, false>, 16);
+    case 243: return go(k_cheb_rt<24, 3, false>, 24);
   }
-  fail(LEO2D_ERR_BAD_ARG, "8-row step: warps 8, 12, 16 (depth 3, 4, 6) or 24 (depth 3, 4)");
+  fail(LEO2D_ERR_BAD_ARG, "8-row step in shared memory: warps 8 or 12 (depth 3 or 7), 16 or 24 (depth 3)");
 }
 
 }  // namespace leo2d

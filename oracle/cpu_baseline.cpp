@@ -67,6 +67,14 @@ double oracle_cpu_kpm_steps(int64_t n, const int64_t* rp, const int32_t* col, co
   return std::chrono::duration<double>(t1 - t0).count();
 }
 
+/* H~ = (H + shift I) / rescale in place (generateRealH's rescale,
+ * src/locality.cpp:4166-4176): the diagonal entries get the shift. */
+void oracle_rescale_csr(int64_t n, const int64_t* rp, const int32_t* col, double* val, double rescale,
+                        double shift) {
+  for (int64_t r = 0; r < n; ++r)
+    for (int64_t i = rp[r]; i < rp[r + 1]; ++i) val[i] = ((col[i] == r ? shift : 0.0) + val[i]) / rescale;
+}
+
 /* The doubling recursion of the oracle (oracle_kpm_trace_doubling: T_{k+1} =
  * 2 H T_k - T_{k-1}, mu_{2k} = 2 <T_k|T_k> - mu_0, mu_{2k+1} = 2 <T_{k+1}|T_k> -
  * mu_1) with each SpMV split over `threads` row ranges. Every row is summed in

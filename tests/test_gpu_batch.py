@@ -86,3 +86,30 @@ def test_batch_rejects(ctx, flakes):
         L.Batch(ctx, flakes[:1], L.kpm_cfg(16, R=1, precision=L.FP64))
     with pytest.raises(L.Leo2dError, match="random-phase"):
         L.Batch(ctx, flakes[:1], L.kpm_cfg(16, R=1, kind=L.VEC_GAUSSIAN))
+
+
+def test_batch_row_blocks(ctx, flakes):
+    """Flakes with positions at 32 columns run the row-block step in one launch
+    per step (24 warps per CTA, a block group per flake): each flake's vectors
+    are those of the single-matrix row-block step, so the moments agree with it
+    to the order of the FP64 dot sums, and with the FP64 oracle to 1e-4."""
+    P, R, seed = 64, 16, 8
+    b = L.Batch(ctx, flakes, L.kpm_cfg(P, R=R, seed=seed, block=32))
+    assert b.warps == 24 and b.block_cols == 32
+    mu = b.run()
+    np.testing.assert_array_equal(mu, b.run())
+    ctx.set_option("step_kernel", 3)
+    ctx.set_option("reorder", 1)
+    try:
+        singles = [c.kpm_dos(L.kpm_cfg(P, R=R, seed=seed, block=32)) for c in flakes]
+    finally:
+        ctx.set_option("step_kernel", -1)
+        ctx.set_option("reorder", -1)
+    for f in range(len(flakes)):
+        assert _rel(mu[f], singles[f]) < 1e-9, f
+    csr = flakes[3]
+    rp, col, val = csr.download()
+    re, im = oracle.phase_vectors(seed, 0, R, csr.n)
+    ref = oracle.kpm_trace(rp, col, val, re, P, literal=False) + oracle.kpm_trace(rp, col, val, im, P, literal=False)
+    assert _rel(mu[3], ref) < FP32_RTOL
+    b.close()

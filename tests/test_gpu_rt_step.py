@@ -79,8 +79,8 @@ def test_rt_dos_matches(ctx, size, twist, model):
 
 
 @pytest.mark.parametrize("opts", [{"rt_stage": 1, "rt_warps": 8, "rt_depth": 3},
-                                  {"rt_stage": 1, "rt_warps": 12, "rt_depth": 6},
-                                  {"rt_stage": 1, "rt_warps": 24, "rt_depth": 4},
+                                  {"rt_stage": 1, "rt_warps": 12, "rt_depth": 7},
+                                  {"rt_stage": 1, "rt_warps": 24, "rt_depth": 3},
                                   {"rt_stage": 0, "rt_warps": 16, "rt_depth": 2},
                                   {"rt_stage": 0, "rt_warps": 12, "rt_depth": 6},
                                   {"rt_stage": 0, "rt_warps": 8, "rt_depth": 6},
