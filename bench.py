@@ -554,8 +554,8 @@ def run_cv_bound(args):
         tg = np.arange(s0, min(n, s0 + blk), dtype=np.int64)
         exact += csr.kpm_ldos(L.kpm_cfg(P_cv, R=1), tg).sum(axis=0)
     t_exact = time.perf_counter() - t0
-    d_exact = dos_of(exact / n)
-    mean_exact = exact / n
+    # the site moments sum to Tr T_n, what one random-phase vector estimates
+    d_exact = dos_of(exact)
     R_max = args.cv_max_vectors
     res = []
     for sd in seeds:
@@ -568,7 +568,7 @@ def run_cv_bound(args):
                 r_plain = R
             if r_cv is None:
                 mc = mu.copy()
-                mc[:P_s] = mean_exact[:P_s]
+                mc[:P_s] = exact[:P_s]
                 if l1(dos_of(mc), d_exact) <= TARGET_L1:
                     r_cv = R
             if r_plain is not None and r_cv is not None:
@@ -879,8 +879,9 @@ def main():
     ap.add_argument("--step-kernel", type=int, default=-1, choices=[-1, 0, 1, 2, 3, 5],
                     help="force the Chebyshev step kernel: 0 tiled gathers, 1 register gathers, 2 tensor cores, "
                          "3 row blocks, 5 row blocks of 8 on the tensor cores (default: the autotuner's choice)")
-    ap.add_argument("--rt-stage", type=int, default=None, choices=[0, 1],
-                    help="8-row tensor-core step: T_n rows staged in registers (0) or shared memory (1)")
+    ap.add_argument("--rt-stage", type=int, default=None, choices=[0, 1, 2],
+                    help="8-row tensor-core step: T_n rows staged in registers (0), shared memory by cp.async (1) "
+                         "or shared memory by TMA row gathers (2)")
     ap.add_argument("--rt-warps", type=int, default=None, help="8-row tensor-core step: warps per CTA")
     ap.add_argument("--rt-depth", type=int, default=None, help="8-row tensor-core step: k-steps in flight")
     ap.add_argument("--kernel-case", type=int, default=0, metavar="COLS",
@@ -916,6 +917,9 @@ def main():
     ctx = L.Context(local)
     if args.step_kernel >= 0:
         ctx.set_option("step_kernel", args.step_kernel)
+    for key in ("rt_stage", "rt_warps", "rt_depth"):
+        if getattr(args, key) is not None:
+            ctx.set_option(key, getattr(args, key))
     g = ctx.prepare(geom(L, radius=args.radius))
     t0 = time.perf_counter()
     csr = ctx.build_csr(g)
@@ -1029,7 +1033,8 @@ def main():
     tp = os.path.join(REPO, "profiles", "cheb_step_traffic.json")
     if os.path.exists(tp):
         try:
-            t = json.load(open(tp))[{0: "tiled", 3: "row_blocks", 4: "row_blocks_windows"}[kernel_id]]
+            t = json.load(open(tp))[{0: "tiled", 3: "row_blocks", 4: "row_blocks_windows",
+                                     5: "row_blocks_8_tensor_cores"}[kernel_id]]
             traffic = int(bytes_step * t["dram_bytes_per_launch"] / t["algorithmic_bytes_per_launch"])
         except (OSError, ValueError, KeyError, ZeroDivisionError):
             traffic = None

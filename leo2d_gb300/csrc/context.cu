@@ -297,15 +297,17 @@ leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value
       LEO_REQUIRE(value >= -1 && value <= 1, "rb_window must be -1 (autotuned), 0 or 1");
       ctx->rb_window = (int)value;
     } else if (k == "rt_warps") {
-      LEO_REQUIRE(value == 0 || value == 8 || value == 12 || value == 16 || value == 24,
-                  "rt_warps must be 0 (autotuned), 8, 12, 16 or 24");
+      LEO_REQUIRE(value == 0 || value == 8 || value == 12 || value == 16 || value == 20 || value == 24,
+                  "rt_warps must be 0 (autotuned), 8, 12, 16, 20 or 24");
       ctx->rt_warps = (int)value;
     } else if (k == "rt_depth") {
       LEO_REQUIRE(value == 0 || value == 2 || value == 3 || value == 4 || value == 6 || value == 7,
                   "rt_depth must be 0 (autotuned), 2, 3, 4, 6 (rows in registers) or 3, 7 (shared memory)");
       ctx->rt_depth = (int)value;
     } else if (k == "rt_stage") {
-      LEO_REQUIRE(value >= -1 && value <= 1, "rt_stage must be -1 (autotuned), 0 (registers) or 1 (shared memory)");
+      LEO_REQUIRE(value >= -1 && value <= 2,
+                  "rt_stage must be -1 (autotuned), 0 (registers), 1 (shared memory by cp.async) or 2 (shared "
+                  "memory by TMA gathers)");
       ctx->rt_stage = (int)value;
     } else if (k == "rt_group") {
       LEO_REQUIRE(value >= 0 && value <= 16, "rt_group must be 0 (default) or 1..16");

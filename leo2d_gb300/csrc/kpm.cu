@@ -264,7 +264,7 @@ struct Tuned {
   bool rb_window = false;
   bool rt = false;  // the 8-row tensor-core step won for this block width
   int rt_warps = 0, rt_depth = 0;
-  bool rt_regs = true;
+  int rt_stage = 0;
 };
 std::map<std::pair<leo2d_ctx*, ShapeKey>, Tuned> g_shape_cache;
 // best block width per (context, matrix, precision, columns requested)
@@ -338,9 +338,9 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
   if (shape.rt) {
     // 8-row blocks of the locality-ordered copy, stored for this launch shape
     const int w = shape.rt_warps;
-    const bool fits = rt_smem_bytes(w, shape.rt_depth, shape.rt_regs) + 8 * 1024 <= ctx->smem_optin;
+    const bool fits = rt_smem_bytes(w, shape.rt_depth, shape.rt_stage) + 8 * 1024 <= ctx->smem_optin;
     if (fits && csr_build_rt(ctx, mm, w, rt_group_of(ctx), rt_chunk_of(ctx))) {
-      dyn_smem = rt_smem_bytes(w, shape.rt_depth, shape.rt_regs);
+      dyn_smem = rt_smem_bytes(w, shape.rt_depth, shape.rt_stage);
       grid = m->rt_grid;
       shape.tiled = false;
     } else {
@@ -462,7 +462,7 @@ void Recursion::step(const void* in, void* out, const void* prev, bool first, do
 void Recursion::run() {
   if (shape.fp64) enqueue_steps<double>(*this);
   else enqueue_steps<float>(*this);
-  if (shape.tiled || shape.tc || shape.rb) ctx_check_status(ctx, "Chebyshev recursion");
+  if (shape.tiled || shape.tc || shape.rb || shape.rt) ctx_check_status(ctx, "Chebyshev recursion");
 }
 
 Recursion::~Recursion() {
@@ -525,7 +525,7 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
     s.rb_warps = 24;
   }
   s.rt_warps = ctx->rt_warps > 0 ? ctx->rt_warps : (cached && it->second.rt_warps > 0 ? it->second.rt_warps : 16);
-  s.rt_regs = ctx->rt_stage >= 0 ? ctx->rt_stage == 0 : (cached && it->second.rt ? it->second.rt_regs : false);
+  s.rt_stage = ctx->rt_stage >= 0 ? ctx->rt_stage : (cached && it->second.rt ? it->second.rt_stage : 1);
   s.rt_depth = ctx->rt_depth > 0 ? ctx->rt_depth : (cached && it->second.rt_depth > 0 ? it->second.rt_depth : 3);
   LEO_REQUIRE(s.rows_per_item >= 0 && s.rows_per_item <= 64, "rows_per_warp must be 0..64");
   return s;
@@ -824,15 +824,17 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
       // the 8-row tensor-core step where it applies: a few (warps, depth) shapes
       if (!fp64 && cols == 32 && !csr->complex_h && ctx->reorder != 0 &&
           (ctx->kernel_variant == -1 || ctx->kernel_variant == 5)) {
-        struct RtTry { int warps, depth; bool regs; };
-        for (const RtTry t : {RtTry{16, 3, false}, RtTry{16, 2, true}, RtTry{12, 7, false}, RtTry{8, 7, false},
-                              RtTry{16, 3, true}}) {
-          if (ctx->rt_stage >= 0 && (ctx->rt_stage == 0) != t.regs) continue;
+        struct RtTry { int warps, depth, stage; };
+        // (the TMA form, stage 2, is timed only when asked for: 1.8x slower)
+        for (const RtTry t : {RtTry{16, 3, 1}, RtTry{16, 2, 0}, RtTry{12, 7, 1}, RtTry{8, 7, 1}, RtTry{16, 3, 0},
+                              RtTry{16, 3, 2}, RtTry{12, 7, 2}}) {
+          if (t.stage == 2 && ctx->rt_stage != 2) continue;
+          if (ctx->rt_stage >= 0 && ctx->rt_stage != t.stage) continue;
           StepShape sh = choose_shape(ctx, csr, fp64, cols, cols, 0);
           sh.tc = false;
           sh.rb = false;
           sh.rt = true;
-          sh.rt_regs = t.regs;
+          sh.rt_stage = t.stage;
           sh.rt_warps = ctx->rt_warps > 0 ? ctx->rt_warps : t.warps;
           sh.rt_depth = ctx->rt_depth > 0 ? ctx->rt_depth : t.depth;
           Recursion r;
@@ -853,7 +855,7 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
             best_t.rt = true;
             best_t.rt_warps = sh.rt_warps;
             best_t.rt_depth = sh.rt_depth;
-            best_t.rt_regs = sh.rt_regs;
+            best_t.rt_stage = sh.rt_stage;
           }
           if (ctx->rt_warps > 0 && ctx->rt_depth > 0) break;  // one shape asked for
         }

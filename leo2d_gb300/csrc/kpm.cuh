@@ -21,8 +21,10 @@ struct StepShape {
   bool rb_window = false;  // row-block step over shared-memory windows (rbw_spmm.cu)
   bool rt = false;         // 8-row blocks on the tensor cores (rt_spmm.cu; FP32, 32 columns)
   int rt_warps = 16;       // 8-row step: warps per CTA (8, 12, 16, 24)
-  int rt_depth = 3;        // 8-row step: k-steps of T_n rows in flight per warp (registers 2, 3, 4, 6; shared 3, 7)
-  bool rt_regs = false;    // 8-row step: T_n rows staged in registers (else shared memory)
+  int rt_depth = 3;        // 8-row step: k-steps of T_n rows in flight per warp (registers 2, 3, 4, 6;
+                           // cp.async 3, 7; TMA 3, 7)
+  int rt_stage = 1;        // 8-row step: T_n rows staged in 0 registers, 1 shared memory by cp.async,
+                           // 2 shared memory by TMA gathers
 };
 
 // Vector block resident on the device: two buffers of n x cols (T_k, T_{k-1}).
@@ -80,7 +82,7 @@ void rb_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
 // The 8-row tensor-core step (rt_spmm.cu): shared memory of a shape, the grid
 // its blocks are built for (csr_build_rt with rt_group_of / rt_chunk_of), and
 // one launch.
-size_t rt_smem_bytes(int warps, int depth, bool regs);
+size_t rt_smem_bytes(int warps, int depth, int stage);
 unsigned rt_grid(leo2d_ctx* ctx, const leo2d_csr* csr, int warps);
 int rt_group_of(const leo2d_ctx* ctx);
 int rt_chunk_of(const leo2d_ctx* ctx);

@@ -34,11 +34,12 @@
 //   each block's k-step count (the kernel's block boundaries).
 // Kernel (one CTA per SM, W warps, no CTA-wide barrier in the main loop)
 //   Each warp runs a software pipeline over its k-steps with cp.async groups:
-//   at iteration u it copies the matrix data of k-step u + D + DM (cp.async.cg,
-//   L2 only) and the 8 T_n rows of k-step u + D (cp.async.ca, so rows stay in
-//   L1 for the neighbouring blocks; the columns come from the matrix data that
-//   landed DM iterations earlier), then waits for k-step u's group and runs its
-//   MMAs. T_n rows land in a 1 KB ring entry with 16-byte chunk c of row s at
+//   at iteration u it copies the matrix data of k-step u + D + DM and the 8 T_n
+//   rows of k-step u + D (the columns come from the matrix data that landed DM
+//   iterations earlier), both with cp.async.cg (from L2: keeping the rows in L1
+//   for neighbouring blocks hit 46 % but cost an L1 tag wavefront per copy on
+//   the pipe that bounds the kernel; 0.68 -> 0.65 ms on a 2.4M-orbital flake),
+//   then waits for k-step u's group and runs its MMAs. T_n rows land in a 1 KB ring entry with 16-byte chunk c of row s at
 //   chunk c ^ s; lane (g, t) reads columns 4 cg .. 4 cg + 3, cg = (g >> 1) |
 //   ((g & 1) << 2), of slots t and t + 4 with no bank conflicts (memory column
 //   4 cg + i is logical column g + 8 i of the MMA). At a block's last k-step
@@ -50,6 +51,7 @@
 #include <vector>
 
 #include "kpm.cuh"
+#include "tc_gemm.cuh"
 
 using namespace leo2d;
 
@@ -63,12 +65,13 @@ constexpr int kRtRows = 8;           // rows per block
 constexpr int kRtStepBytes = 288;    // one k-step: 8 columns + 32 value pairs
 constexpr int kRtMaxEnt = 2048;      // stored entries of one block (build limit)
 constexpr int kRtBuildWarps = 4;
+// staging of the gathered T_n rows (the kernel's STAGE parameter)
+constexpr int kRtRegs = 0;     // registers, fragments exchanged by shuffles
+constexpr int kRtCpAsync = 1;  // shared-memory ring filled by cp.async (16 bytes a lane)
+constexpr int kRtTma = 2;      // shared-memory ring filled by TMA row gathers (tile::gather4)
 
 __device__ __forceinline__ void cp_async_cg16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_ca16(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
@@ -77,6 +80,29 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 __device__ __forceinline__ void prefetch_l2_bulk(const void* p, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// Four 128-byte rows y0..y3 of the [n][32] FP32 tensor of `map` into 512 bytes
+// of shared memory (rows at dst + 128 i, 16-byte chunk c of the row at address
+// bits 4..6 = c ^ (address bits 7..9): the 128-byte swizzle), completion counted
+// on `bar` in bytes.
+__device__ __forceinline__ void tma_gather4(void* dst, const CUtensorMap* map, int y0, int y1, int y2, int y3,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(y0), "r"(y1), "r"(y2), "r"(y3), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Arrival with the byte count of the copies to come, without release
+// semantics: the producer publishes nothing of its own through the barrier
+// (the copies' bytes are made visible by their completion), so the arrival
+// need not wait for this lane's earlier memory operations (its matrix copies
+// in flight).
+__device__ __forceinline__ void mbar_expect_tx_relaxed(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.relaxed.cta.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
 }
 
 __device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
@@ -89,6 +115,7 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1
 }
 
 struct RtArgs {
+  CUtensorMap tmap;  // kRtTma: T_n as [n][32] FP32, boxes of one 128-byte row, 128-byte swizzle
   int64_t n;    // rows
   int64_t nrb;  // row blocks
   const unsigned char* __restrict__ data;  // k-steps in processing order
@@ -104,6 +131,10 @@ struct RtArgs {
   double* __restrict__ prev_dots;
   int group;        // G: consecutive blocks per run
   int chunk;        // consecutive tiles per CTA between grid-wide jumps
+  // kRtTma: row waits give up after spin_limit polls or two seconds and set *status
+  uint64_t spin_limit;
+  int* status;
+  int never_wait;   // test hook: the warps first wait on a barrier nothing completes
 };
 
 }  // namespace
@@ -164,12 +195,24 @@ __device__ __forceinline__ float2 ld_stream_f2(const void* p) {
   return r;
 }
 
-// One kernel, two ways of staging the gathered T_n rows:
-//  - REGS = false: cp.async copies into a per-warp shared-memory ring (see the
-//    file comment) D = XS - 1 k-steps ahead, the matrix data MS - 1 ahead; both
-//    rings are powers of two and the main loop is unrolled over the matrix ring,
-//    so every slot is a compile-time constant;
-//  - REGS = true: no shared memory, so the whole L1 caches T_n rows. Lane (q, p)
+// One kernel, three ways of staging the gathered T_n rows:
+//  - STAGE = kRtCpAsync: cp.async copies into a per-warp shared-memory ring (see
+//    the file comment) D = XS - 1 k-steps ahead, the matrix data MS - 1 ahead;
+//    both rings are powers of two and the main loop is unrolled over the matrix
+//    ring, so every slot is a compile-time constant;
+//  - STAGE = kRtTma: the same pipeline, but lane 0 fetches the 8 rows of a
+//    k-step with two TMA row gathers (tile::gather4, 4 rows of 128 bytes each),
+//    completion counted on the entry's mbarrier. Each gather lands on a 1 KB
+//    boundary, where the 128-byte swizzle of the tensor map puts chunk c of row
+//    r at c ^ r, the layout the cp.async form writes by hand, so the fragment
+//    reads are the same. The gathers leave the load/store pipe out of the row
+//    copies, but a warp's iteration then carries an mbarrier arrive, two tensor
+//    copies and a wait (each a few hundred cycles of latency even when the data
+//    is there), and 4-row gathers top out near 4.5 TB/s per GPU at 16 warps:
+//    1.2 ms against 0.65 ms on a 2.4M-orbital flake. Kept as a tested option.
+//    Waits are bounded: after spin_limit polls or two seconds the warp records
+//    a timeout in *status, drains the gathers it issued and stops;
+//  - STAGE = kRtRegs: no shared memory, so the whole L1 caches T_n rows. Lane (q, p)
 //    loads 16-byte chunk p of the T_n rows of slots q and q + 4 (one 128-byte row
 //    per quarter-warp, one L1 wavefront per slot) D k-steps ahead into registers,
 //    and the A fragments are gathered from those registers with eight shuffles
@@ -180,18 +223,21 @@ __device__ __forceinline__ float2 ld_stream_f2(const void* p) {
 // Each warp walks its blocks in the build's processing order: runs of G
 // consecutive blocks, run i in tile (bid + (i / chunk) grid) chunk + i % chunk;
 // a block ends after its k-step count (kst), read one block ahead.
-template <int W, int D, bool REGS>
+template <int W, int D, int STAGE>
 __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const int nblk) {
+  constexpr bool REGS = STAGE == kRtRegs;
   constexpr int C = 32;
   constexpr int NT = W * 32;
   constexpr int XS = D + 1;      // shared ring of staged T_n rows (k-steps)
   constexpr int MS = 2 * XS;     // shared ring of matrix k-steps
   constexpr int DM = MS - 1 - D; // matrix lookahead beyond the rows'
-  constexpr int kWarpBytes = REGS ? 0 : XS * 1024 + MS * kRtStepBytes;
   constexpr int kPf = REGS ? 48 : 32;  // matrix k-steps prefetched into L2 ahead
   constexpr int kDotFlush = 16;        // blocks summed in FP32 between FP64 flushes
   static_assert(REGS || ((XS & (XS - 1)) == 0 && DM >= D + 1), "power-of-two rings, matrix ahead of the rows");
-  extern __shared__ __align__(1024) unsigned char rt_smem[];
+  extern __shared__ __align__(1024) unsigned char rt_smem_raw[];
+  // the 128-byte swizzle of TMA copies is a function of the address: ring
+  // entries sit on 1 KB boundaries (the launch adds 1 KB of slack)
+  unsigned char* rt_smem = rt_smem_raw + ((1024u - (smem_u32(rt_smem_raw) & 1023u)) & 1023u);
   if (a.prev_partials) reduce_prev<C, NT>(a.prev_partials, a.prev_dots, nblk, bid, nblk);
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -210,12 +256,22 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
   const unsigned char* gdata = a.data + k0 * kRtStepBytes;
 
   // block walk, block-end countdown and epilogue operands
-  int jb = 0, irun = 0;
-  auto run_row0 = [&](int i) -> int64_t {
-    const int tile = (bid + (i / chunk) * nblk) * chunk + i % chunk;
-    return ((int64_t)tile * W + warp) * group * kRtRows;
+  // run i of the warp lies in tile (bid + (i / chunk) nblk) chunk + i % chunk;
+  // the walk keeps that tile split as (tb, ic) for the run after the current
+  // one, advanced without divisions
+  int jb = 0;
+  int64_t tb = (int64_t)bid * chunk;
+  int ic = 0;
+  auto run_row = [&]() -> int64_t { return ((tb + ic) * W + warp) * group * kRtRows; };
+  auto next_run = [&]() {
+    if (++ic == chunk) {
+      ic = 0;
+      tb += (int64_t)nblk * chunk;
+    }
   };
-  int64_t rbase = run_row0(0), row0 = 0;
+  int64_t rbase = run_row(), row0 = 0;  // first row of the current run
+  next_run();
+  int64_t nbase = run_row();  // first row of the next run
   int left = 0;                                       // k-steps of the current block still to run
   int next_left = nk > 0 ? (int)kst[rbase / kRtRows] : 0;  // the next block's k-steps
   float4 xn0 = make_float4(0.f, 0.f, 0.f, 0.f), xn1 = xn0, xp0 = xn0, xp1 = xn0;
@@ -249,7 +305,7 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
     row0 = rbase + (int64_t)jb * kRtRows;
     left = next_left;
     // the k-steps of the block after this one (its run may start elsewhere)
-    const int64_t nrow = jb + 1 < group ? row0 + kRtRows : run_row0(irun + 1);
+    const int64_t nrow = jb + 1 < group ? row0 + kRtRows : nbase;
     if (nrow / kRtRows < a.nrb) next_left = (int)kst[nrow / kRtRows];
     const int64_t r0 = row0 + 2 * t;
     if (r0 < n) {
@@ -287,7 +343,9 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
     row_out(r0 + 1, h1, xp1, xn1);
     if (++jb == group) {
       jb = 0;
-      rbase = run_row0(++irun);
+      rbase = nbase;
+      next_run();
+      nbase = run_row();
     }
     if (++since_flush == kDotFlush) {
       since_flush = 0;
@@ -301,49 +359,156 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
     if (--left == 0) end_block();
   };
 
-  if constexpr (!REGS) {
+  if constexpr (STAGE == kRtCpAsync) {
+    constexpr int kWarpBytes = XS * 1024 + MS * kRtStepBytes;
+    static_assert(MS % 8 == 0, "L2 prefetch every 8 matrix k-steps at fixed slots of the unrolled loop");
     unsigned char* xr = rt_smem + (size_t)warp * kWarpBytes;
     unsigned char* mr = xr + XS * 1024;
     const bool mlane = lane < kRtStepBytes / 16;
-    const unsigned char* msrc = gdata + 16 * lane;  // this lane's chunk of matrix k-step u + D + DM
-    // per-lane offsets in a row-ring entry: writes (slot q and q + 4, chunk p) and
-    // reads (slot t and t + 4, chunk cg), 16-byte chunk c of row s at c ^ s
-    const int wo0 = q * 128 + 16 * (p ^ q), wo1 = 512 + q * 128 + 16 * (p ^ (q + 4));
+    // Lane (g, t) copies, and later reads, chunk cg of the T_n rows of slots t
+    // and t + 4 (16-byte chunk c of row s at c ^ s: no bank conflicts either
+    // way, and a quarter of the warp covers each 128-byte row). A lane reads
+    // only rows it copied itself, so its own cp.async wait orders them; the
+    // matrix k-steps (copied by lanes 0..17, read by all) are ordered by one
+    // __syncwarp per iteration.
     const int ro0 = t * 128 + 16 * (cg ^ t), ro1 = 512 + t * 128 + 16 * (cg ^ (t + 4));
-    // iteration u (matrix slot sm = u mod MS): copy matrix k-step u + D + DM and the
-    // rows of k-step u + D, wait for k-step u's rows, run its MMAs
-    auto iter = [&](int u, int sm, bool checks) {
-      __syncwarp();  // every lane is done with the entries these copies overwrite
+    // iteration u (matrix slot sm = u mod MS): wait for the copies of iteration
+    // u - D (the rows of k-step u, matrix k-step u + DM), copy matrix k-step
+    // u + D + DM and the rows of k-step u + D, run k-step u's MMAs. The matrix
+    // source of the iteration is mb + off (mb: k-step u's chunk of this lane).
+    auto iter = [&](int u, int sm, const unsigned char* mb, int off, bool checks, bool pf) {
+      cp_async_wait<D - 1>();
+      __syncwarp();  // every lane's matrix copies have landed; k-step u - 1 is read
       const int vm = u + D + DM, vx = u + D;
-      if (mlane && (!checks || vm < nk)) cp_async_cg16(mr + ((sm + MS - 1) & (MS - 1)) * kRtStepBytes + 16 * lane, msrc);
-      msrc += kRtStepBytes;
-      if (lane == 0 && (vm & 7) == 0 && vm + kPf < nk)
+      if (mlane && (!checks || vm < nk))
+        cp_async_cg16(mr + ((sm + MS - 1) & (MS - 1)) * kRtStepBytes + 16 * lane, mb + (off + (D + DM) * kRtStepBytes));
+      if (pf && lane == 0 && vm + kPf < nk)
         prefetch_l2_bulk(gdata + (size_t)(vm + kPf) * kRtStepBytes, (uint32_t)min(8, nk - vm - kPf) * kRtStepBytes);
       if (!checks || (vx >= 0 && vx < nk)) {
-        // the columns of k-step vx landed DM iterations ago
-        const int2 cc = *reinterpret_cast<const int2*>(mr + ((sm + D) & (MS - 1)) * kRtStepBytes + 8 * q);
+        // the columns of k-step vx (slots t, t + 4) landed DM iterations ago
+        const int2 cc = *reinterpret_cast<const int2*>(mr + ((sm + D) & (MS - 1)) * kRtStepBytes + 8 * t);
         unsigned char* dst = xr + ((sm + D) & (XS - 1)) * 1024;
-        cp_async_ca16(dst + wo0, tnb + (uint64_t)(uint32_t)cc.x * (C * 4));
-        cp_async_ca16(dst + wo1, tnb + (uint64_t)(uint32_t)cc.y * (C * 4));
+        cp_async_cg16(dst + ro0, tnc + (uint64_t)(uint32_t)cc.x * C);
+        cp_async_cg16(dst + ro1, tnc + (uint64_t)(uint32_t)cc.y * C);
       }
       cp_async_commit();
-      cp_async_wait<D>();  // k-step u's rows (and k-step u + D + 1's matrix data) have landed
-      __syncwarp();
       if (checks && u < 0) return;
       const unsigned char* xs = xr + (sm & (XS - 1)) * 1024;
       const unsigned char* ms = mr + sm * kRtStepBytes;
-      consume(*reinterpret_cast<const float4*>(xs + ro0), *reinterpret_cast<const float4*>(xs + ro1),
+      acc.add(*reinterpret_cast<const float4*>(xs + ro0), *reinterpret_cast<const float4*>(xs + ro1),
               *reinterpret_cast<const float2*>(ms + 32 + 8 * lane));
+      if (--left == 0) {
+        end_block();
+        if (u + 1 < nk) begin_block();
+      }
     };
+    if (nk > 0) begin_block();
+    const unsigned char* mlan = gdata + 16 * lane;  // this lane's chunk of matrix k-step 0
     int u = -(D + DM);
-    for (; u < 0; ++u) iter(u, u & (MS - 1), true);
+    for (; u < 0; ++u) iter(u, u & (MS - 1), mlan, u * kRtStepBytes, true, (((u + D + DM) & 7) == 0));
     const int main_end = nk - (D + DM) > 0 ? ((nk - (D + DM)) & ~(MS - 1)) : 0;
     for (; u < main_end; u += MS) {
+      const unsigned char* mb = mlan + (size_t)u * kRtStepBytes;
 #pragma unroll
-      for (int j = 0; j < MS; ++j) iter(u + j, j, false);
+      for (int j = 0; j < MS; ++j) iter(u + j, j, mb, j * kRtStepBytes, false, ((j + D + DM) & 7) == 0);
     }
-    for (; u < nk; ++u) iter(u, u & (MS - 1), true);
+    for (; u < nk; ++u)
+      iter(u, u & (MS - 1), mlan, u * kRtStepBytes, true, (((u + D + DM) & 7) == 0));
     cp_async_wait<0>();
+  } else if constexpr (STAGE == kRtTma) {
+    // Each warp owns XS entries of 2 KB (1 KB aligned): row entry e holds slots
+    // 0..3 of its k-step at [0, 512) and slots 4..7 at [1024, 1536), each the
+    // target of one gather on a 1 KB boundary, so the swizzle puts chunk c of
+    // row r at c ^ r (r = 0..3); matrix slot m sits in the hole after a half,
+    // at 2048 (m >> 1) + 512 + 1024 (m & 1). Then one mbarrier per row entry.
+    unsigned char* xr = rt_smem + (size_t)warp * XS * 2048;
+    unsigned char* mr = xr + 512;
+    auto mslot = [&](int m) { return mr + (m >> 1) * 2048 + (m & 1) * 1024; };
+    uint64_t* bars = reinterpret_cast<uint64_t*>(rt_smem + (size_t)W * XS * 2048) + warp * XS;
+    if (lane == 0) {
+#pragma unroll
+      for (int i = 0; i < XS; ++i) mbar_init(&bars[i], 1);
+      mbar_fence_init();
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncwarp();
+    const bool mlane = lane < kRtStepBytes / 16;
+    const unsigned char* msrc = gdata + 16 * lane;  // this lane's chunk of matrix k-step u + D + DM
+    // reads of slot t and t + 4, chunk cg, in the swizzled entry
+    const int ro0 = t * 128 + 16 * (cg ^ t), ro1 = 1024 + t * 128 + 16 * (cg ^ t);
+    constexpr int kLogXS = XS == 4 ? 2 : XS == 8 ? 3 : XS == 2 ? 1 : 4;
+    static_assert((1 << kLogXS) == XS, "row ring of 2, 4, 8 or 16 entries");
+    bool gave_up = false;
+    int stop = nk;  // first k-step not consumed
+    if (a.never_wait && !bounded_wait(&bars[0], 0u, a.spin_limit)) {
+      // test hook: nothing arrives on the entry, no copy was issued
+      if (lane == 0) atomicExch(a.status, leo2d::kStatusTimeout);
+      gave_up = true;
+      stop = 0;
+    }
+    // iteration u (matrix slot sm = u mod MS): copy matrix k-step u + D + DM,
+    // gather the rows of k-step u + D (their columns landed DM iterations ago),
+    // wait for k-step u's rows, run its MMAs. Returns false after a timeout.
+    auto iter = [&](int u, int sm, bool checks) -> bool {
+      __syncwarp();  // every lane is done with the entries these copies overwrite
+      const int vm = u + D + DM, vx = u + D;
+      if (mlane && (!checks || vm < nk)) cp_async_cg16(mslot((sm + MS - 1) & (MS - 1)) + 16 * lane, msrc);
+      msrc += kRtStepBytes;
+      if (lane == 0) {
+        if ((vm & 7) == 0 && vm + kPf < nk)
+          prefetch_l2_bulk(gdata + (size_t)(vm + kPf) * kRtStepBytes, (uint32_t)min(8, nk - vm - kPf) * kRtStepBytes);
+        if (!checks || (vx >= 0 && vx < nk)) {
+          const int4* cp = reinterpret_cast<const int4*>(mslot((sm + D) & (MS - 1)));
+          const int4 c0 = cp[0], c1 = cp[1];  // slots (0 4 1 5), (2 6 3 7)
+          const int e = (sm + D) & (XS - 1);
+          unsigned char* dst = xr + e * 2048;
+          // no proxy fence here: the entry's last reads fed the warp's mma.sync of
+          // the previous iteration, so they completed before this copy is issued
+          // (a fence would also wait for this lane's matrix copies in flight)
+          mbar_expect_tx_relaxed(&bars[e], 1024);
+          tma_gather4(dst, &a.tmap, c0.x, c0.z, c1.x, c1.z, &bars[e]);
+          tma_gather4(dst + 1024, &a.tmap, c0.y, c0.w, c1.y, c1.w, &bars[e]);
+        }
+      }
+      cp_async_commit();
+      cp_async_wait<D>();  // matrix k-step u + DM - 1 has landed (columns of the next gather, values of u)
+      __syncwarp();
+      if (checks && u < 0) return true;
+      const int e = sm & (XS - 1);
+      const bool ok = bounded_wait(&bars[e], (uint32_t)(u >> kLogXS) & 1u, a.spin_limit);
+      if (!__all_sync(0xffffffffu, ok)) {
+        if (lane == 0) atomicExch(a.status, leo2d::kStatusTimeout);
+        stop = u;
+        return false;
+      }
+      const unsigned char* xs = xr + e * 2048;
+      consume(*reinterpret_cast<const float4*>(xs + ro0), *reinterpret_cast<const float4*>(xs + ro1),
+              *reinterpret_cast<const float2*>(mslot(sm) + 32 + 8 * lane));
+      return true;
+    };
+    int u = -(D + DM);
+    if (!gave_up)
+      for (; u < 0; ++u) iter(u, u & (MS - 1), true);
+    const int main_end = nk - (D + DM) > 0 ? ((nk - (D + DM)) & ~(MS - 1)) : 0;
+    for (; !gave_up && u < main_end; u += MS) {
+#pragma unroll
+      for (int j = 0; j < MS; ++j)
+        if (!iter(u + j, j, false)) {
+          gave_up = true;
+          break;
+        }
+    }
+    for (; !gave_up && u < nk; ++u)
+      if (!iter(u, u & (MS - 1), true)) gave_up = true;
+    cp_async_wait<0>();
+    if (gave_up) {
+      // gathers issued for k-steps stop .. stop + D may still land: wait for them
+      // (bounded by time) before the shared memory is released
+      if (lane == 0)
+        for (int v = stop; v < min(stop + D + 1, nk); ++v)
+          if (v >= 0 && !a.never_wait) bounded_wait(&bars[v & (XS - 1)], (uint32_t)(v >> kLogXS) & 1u, ~0ull);
+      __syncwarp();
+    }
   } else {
     const int src = 8 * t + cg;  // the lane holding chunk cg of slots t and t + 4
     // rings (slot j = k-step mod D): columns of k-steps u + D .. u + 2D - 1, rows
@@ -415,9 +580,9 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
   for (int i = threadIdx.x; i < 2 * C; i += NT) a.partials[(size_t)bid * 2 * C + i] = bsum[i];
 }
 
-template <int W, int D, bool REGS>
+template <int W, int D, int STAGE>
 __global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ RtArgs a) {
-  rt_body<W, D, REGS>(a, (int)blockIdx.x, (int)gridDim.x);
+  rt_body<W, D, STAGE>(a, (int)blockIdx.x, (int)gridDim.x);
 }
 
 // ---------------------------------------------------------------- format build
@@ -592,8 +757,34 @@ RtShape rt_shape(const leo2d_ctx* ctx, int64_t n, int warps, int group, int chun
 }
 
 // Shared memory of one warp's rings for row lookahead D (rows: D + 1 k-steps,
-// matrix: 2 (D + 1) k-steps).
-constexpr int rt_warp_bytes(int depth) { return (depth + 1) * 1024 + 2 * (depth + 1) * kRtStepBytes; }
+// matrix: 2 (D + 1) k-steps): packed for cp.async; for TMA gathers 2 KB per row
+// entry (the matrix in its holes) and its mbarrier.
+constexpr int rt_warp_bytes(int depth, int stage) {
+  return stage == kRtTma ? (depth + 1) * (2048 + 8) : (depth + 1) * 1024 + 2 * (depth + 1) * kRtStepBytes;
+}
+
+// TMA maps of the T_n buffers a thread launched the TMA form on (three
+// buffers rotate through a recursion): encoded once per (device, base, rows).
+struct RtMapEntry {
+  int device;
+  const float* base;
+  int64_t rows;
+  CUtensorMap map;
+};
+thread_local std::vector<RtMapEntry> g_rt_maps;
+
+const CUtensorMap& rt_tmap(int device, const float* base, int64_t rows) {
+  for (const auto& e : g_rt_maps)
+    if (e.device == device && e.base == base && e.rows == rows) return e.map;
+  if (g_rt_maps.size() >= 16) g_rt_maps.erase(g_rt_maps.begin());
+  RtMapEntry e;
+  e.device = device;
+  e.base = base;
+  e.rows = rows;
+  make_tmap_f32(&e.map, base, rows, 32, 32, 1);
+  g_rt_maps.push_back(e);
+  return g_rt_maps.back().map;
+}
 
 }  // namespace
 
@@ -602,7 +793,10 @@ namespace leo2d {
 int rt_group_of(const leo2d_ctx* ctx) { return ctx->rt_group > 0 ? ctx->rt_group : 2; }
 int rt_chunk_of(const leo2d_ctx* ctx) { return ctx->rt_chunk > 0 ? ctx->rt_chunk : 2; }
 
-size_t rt_smem_bytes(int warps, int depth, bool regs) { return regs ? 0 : (size_t)warps * rt_warp_bytes(depth); }
+size_t rt_smem_bytes(int warps, int depth, int stage) {
+  // shared-memory forms: 1 KB of slack to align the rings
+  return stage == kRtRegs ? 0 : (size_t)warps * rt_warp_bytes(depth, stage) + 1024;
+}
 
 unsigned rt_grid(leo2d_ctx* ctx, const leo2d_csr* csr, int warps) {
   return rt_shape(ctx, csr->n, warps, rt_group_of(ctx), rt_chunk_of(ctx)).grid;
@@ -724,9 +918,16 @@ void rt_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
                     const double* prev_partials, double* prev_dots) {
   LEO_REQUIRE(csr->rt_built && csr->rt_warps == shape.rt_warps && csr->rt_grid == grid,
               "8-row blocks built for another launch shape");
-  LEO_REQUIRE(smem >= rt_smem_bytes(shape.rt_warps, shape.rt_depth, shape.rt_regs),
+  LEO_REQUIRE(smem >= rt_smem_bytes(shape.rt_warps, shape.rt_depth, shape.rt_stage),
               "8-row step shared memory changed since setup");
   RtArgs a{};
+  if (shape.rt_stage == kRtTma) {
+    LEO_REQUIRE(csr->n < (1ll << 31), "TMA row gathers take int32 row coordinates");
+    a.tmap = rt_tmap(ctx->device, tn, csr->n);
+  }
+  a.spin_limit = ctx->spin_limit;
+  a.status = ctx->status.p;
+  a.never_wait = ctx->test_unsatisfied_wait;
   a.n = csr->n;
   a.nrb = csr->rt_blocks;
   a.data = csr->rt_data.p;
@@ -749,26 +950,35 @@ void rt_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
     launch(ctx, "cheb_step", [&] { kern<<<grid, warps * 32, smem, ctx->stream>>>(a); });
   };
   const int key = shape.rt_warps * 10 + shape.rt_depth;
-  if (shape.rt_regs) {
+  if (shape.rt_stage == kRtRegs) {
     switch (key) {
-      case 162: return go(k_cheb_rt<16, 2, true>, 16);
-      case 163: return go(k_cheb_rt<16, 3, true>, 16);
-      case 164: return go(k_cheb_rt<16, 4, true>, 16);
-      case 124: return go(k_cheb_rt<12, 4, true>, 12);
-      case 126: return go(k_cheb_rt<12, 6, true>, 12);
-      case 86: return go(k_cheb_rt<8, 6, true>, 8);
+      case 162: return go(k_cheb_rt<16, 2, kRtRegs>, 16);
+      case 163: return go(k_cheb_rt<16, 3, kRtRegs>, 16);
+      case 164: return go(k_cheb_rt<16, 4, kRtRegs>, 16);
+      case 124: return go(k_cheb_rt<12, 4, kRtRegs>, 12);
+      case 126: return go(k_cheb_rt<12, 6, kRtRegs>, 12);
+      case 86: return go(k_cheb_rt<8, 6, kRtRegs>, 8);
     }
     fail(LEO2D_ERR_BAD_ARG, "8-row step in registers: warps 16 (depth 2, 3, 4), 12 (4, 6) or 8 (6)");
   }
-  switch (key) {
-    case 83: return go(k_cheb_rt<8, 3, false>, 8);
-    case 87: return go(k_cheb_rt<8, 7, false>, 8);
-    case 123: return go(k_cheb_rt<12, 3, false>, 12);
-    case 127: return go(k_cheb_rt<12, 7, false>, 12);
-    case 163: return go(k_cheb_rt<16, 3, false>, 16);
-    case 243: return go(k_cheb_rt<24, 3, false>, 24);
+  if (shape.rt_stage == kRtTma) {
+    switch (key) {
+      case 87: return go(k_cheb_rt<8, 7, kRtTma>, 8);
+      case 127: return go(k_cheb_rt<12, 7, kRtTma>, 12);
+      case 163: return go(k_cheb_rt<16, 3, kRtTma>, 16);
+    }
+    fail(LEO2D_ERR_BAD_ARG, "8-row step by TMA gathers: warps 8 or 12 (depth 7) or 16 (depth 3)");
   }
-  fail(LEO2D_ERR_BAD_ARG, "8-row step in shared memory: warps 8 or 12 (depth 3 or 7), 16 or 24 (depth 3)");
+  switch (key) {
+    case 83: return go(k_cheb_rt<8, 3, kRtCpAsync>, 8);
+    case 87: return go(k_cheb_rt<8, 7, kRtCpAsync>, 8);
+    case 123: return go(k_cheb_rt<12, 3, kRtCpAsync>, 12);
+    case 127: return go(k_cheb_rt<12, 7, kRtCpAsync>, 12);
+    case 163: return go(k_cheb_rt<16, 3, kRtCpAsync>, 16);
+    case 203: return go(k_cheb_rt<20, 3, kRtCpAsync>, 20);
+    case 243: return go(k_cheb_rt<24, 3, kRtCpAsync>, 24);
+  }
+  fail(LEO2D_ERR_BAD_ARG, "8-row step in shared memory: warps 8 or 12 (depth 3 or 7), 16, 20 or 24 (depth 3)");
 }
 
 }  // namespace leo2d

@@ -298,7 +298,9 @@ __device__ __forceinline__ uint64_t global_ns() {
 }
 // Waits for the phase of `bar` with the given parity; gives up after `limit`
 // polls or two seconds, whichever comes first, and returns whether it completed.
+// A phase already complete costs one poll (the timer is read only after that).
 __device__ __forceinline__ bool bounded_wait(uint64_t* bar, uint32_t parity, uint64_t limit) {
+  if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_ns();
   for (uint64_t k = 0; k < limit; ++k) {
     if (mbar_try_wait(bar, parity)) return true;

@@ -5,9 +5,9 @@ The step sums each row over its block's k-steps of 8 slots with TF32 products
 split three ways (lo*hi + hi*lo + hi*hi, about 21 significant bits), so FP32
 moments agree with the gather kernel's to rounding (2e-5 of the largest) and
 with the FP64 oracle to 1e-4 (the FP32 bar). Repeated runs are bit-identical;
-launch shapes (T_n rows staged in registers or shared memory, warps, rows in
-flight, blocks per run, tiles per CTA) change the order in which the dots are
-summed and nothing else.
+launch shapes (T_n rows staged in registers, in shared memory by cp.async or
+by TMA row gathers; warps, rows in flight, blocks per run, tiles per CTA)
+change the order in which the dots are summed and nothing else.
 """
 import numpy as np
 import pytest
@@ -84,6 +84,10 @@ def test_rt_dos_matches(ctx, size, twist, model):
                                   {"rt_stage": 0, "rt_warps": 16, "rt_depth": 2},
                                   {"rt_stage": 0, "rt_warps": 12, "rt_depth": 6},
                                   {"rt_stage": 0, "rt_warps": 8, "rt_depth": 6},
+                                  {"rt_stage": 2, "rt_warps": 16, "rt_depth": 3},
+                                  {"rt_stage": 2, "rt_warps": 12, "rt_depth": 7},
+                                  {"rt_stage": 2, "rt_warps": 8, "rt_depth": 7},
+                                  {"rt_stage": 2, "rt_group": 3, "rt_chunk": 5},
                                   {"rt_group": 1}, {"rt_group": 7},
                                   {"rt_chunk": 1}, {"rt_chunk": 5, "rt_group": 3}])
 def test_rt_launch_shapes(ctx, opts):
@@ -163,3 +167,42 @@ def test_rt_stored_zeros(ctx):
     got = _run(ctx, 5, lambda: csr.kpm_dos(cfg))
     assert _rel(got, ref) < 2e-5
     assert _rel(got, _oracle_trace(csr, 2, 16, 32)) < 1e-4
+
+
+@pytest.mark.parametrize("size,twist,model", [(23, 2.6, L.MODEL_SIMPLE), (25, 5.09, L.MODEL_REF)])
+def test_rt_tma_gathers(ctx, size, twist, model):
+    """T_n rows fetched by TMA row gathers (four 128-byte rows per copy, the
+    128-byte swizzle) give the moments of the cp.async form to rounding and of
+    the FP64 oracle to the FP32 bar; ragged last blocks included."""
+    csr = _flake(ctx, size, twist, model)
+    P, R = 80, 16
+    cfg = L.kpm_cfg(P, R=R, seed=11, block=32)
+    ref = _run(ctx, 0, lambda: csr.kpm_dos(cfg))
+    cp = _run(ctx, 5, lambda: csr.kpm_dos(cfg), rt_stage=1, rt_warps=16, rt_depth=3)
+    got = _run(ctx, 5, lambda: csr.kpm_dos(cfg), rt_stage=2, rt_warps=16, rt_depth=3)
+    assert csr.rt_info()[0] == (csr.n + 7) // 8
+    assert _rel(got, cp) < 1e-6
+    assert _rel(got, ref) < 2e-5
+    again = _run(ctx, 5, lambda: csr.kpm_dos(cfg), rt_stage=2, rt_warps=16, rt_depth=3)
+    np.testing.assert_array_equal(got, again)
+    assert _rel(got, _oracle_trace(csr, 11, R, P)) < 1e-4
+
+
+def test_rt_tma_timeout_reports(ctx):
+    """The bounded wait of the TMA form: a barrier nobody completes gives
+    LEO2D_ERR_TIMEOUT, and the context keeps working afterwards."""
+    csr = _flake(ctx, 20, 3.0)
+    cfg = L.kpm_cfg(16, R=16, seed=1, block=32)
+    ok = _run(ctx, 5, lambda: csr.kpm_dos(cfg), rt_stage=2, rt_warps=16, rt_depth=3)
+    ctx.set_spin_limit(2000)
+    ctx.set_option("test_unsatisfied_wait", 1)
+    try:
+        with pytest.raises(L.Leo2dError) as e:
+            _run(ctx, 5, lambda: csr.kpm_dos(cfg), rt_stage=2, rt_warps=16, rt_depth=3)
+        assert e.value.status == L._abi.ERR_TIMEOUT
+        assert "wait ran out" in str(e.value)
+    finally:
+        ctx.set_option("test_unsatisfied_wait", 0)
+        ctx.set_spin_limit(0)
+    again = _run(ctx, 5, lambda: csr.kpm_dos(cfg), rt_stage=2, rt_warps=16, rt_depth=3)
+    np.testing.assert_array_equal(ok, again)
