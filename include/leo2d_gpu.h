@@ -129,16 +129,17 @@ int64_t leo2d_ctx_launch_count(const leo2d_ctx* ctx);
 /* Tuning switches of a context. Keys: "step_kernel" (-1 = autotuned or the
  * default for the matrix; 0 = shared-memory tiles filled by bulk copies;
  * 1 = register streaming of the matrix; 2 = tensor-core tiles; 3 = row blocks of
- * 4 rows; 5 = row blocks of 8 rows on the tensor cores),
+ * 4 rows; 5 = row blocks of 8 or 16 rows on the tensor cores),
  * "tile_stages" (2..4 shared-memory stages of the tiled kernel, default 2),
  * "tile_chunk" (1..65536 consecutive row tiles per block between grid-wide
  * jumps, default 4), "rt_warps" / "rt_depth" / "rt_group" / "rt_chunk" (the
- * 8-row tensor-core step: warps per CTA 8, 12, 16 or 24; k-steps of T_n rows in
- * flight per warp 2, 3, 4, 6 with the rows in registers or 3, 7 in shared
- * memory; blocks per warp run 1..16, default 2; tiles per CTA between grid-wide
- * jumps 1..64, default 2; 0 = autotuned or default), "rt_stage" (-1 =
- * autotuned, 0 = the T_n rows of the 8-row step staged in registers, 1 = in
- * shared memory),
+ * tensor-core row-block step: warps per CTA 8, 12, 16, 20 or 24; k-steps of T_n
+ * rows in flight per warp 2, 3, 4, 6 with the rows in registers or 3, 7 in
+ * shared memory; blocks per warp run 1..16, default 2; tiles per CTA between
+ * grid-wide jumps 1..64, default 2; 0 = autotuned or default), "rt_stage"
+ * (-1 = autotuned, 0 = the T_n rows staged in registers, 1 = in shared memory
+ * by cp.async, 2 = in shared memory by TMA row gathers), "rt_rows" (rows per
+ * block: 0 = autotuned, 8, or 16 with rt_stage 1, warps 12 or 16, depth 3),
  * "alloc_cap_mb" (the largest single device allocation a call on this context
  * may make, in MiB; a larger one fails with LEO2D_ERR_OOM and a message naming
  * its size; 0 = no limit, the default),

@@ -117,6 +117,7 @@ struct leo2d_ctx {
                               // 2, 3, 4, 6 (rows in registers) or 3, 7 (shared memory)
   int rt_stage = -1;          // 8-row tensor-core step: T_n rows staged in -1 autotuned, 0 registers, 1 shared memory
                               // by cp.async, 2 shared memory by TMA gathers
+  int rt_rows = 0;            // tensor-core row-block step: rows per block: 0 autotuned, 8, 16
   int rt_group = 0;           // 8-row tensor-core step: consecutive blocks per warp run: 0 default (2), 1..16
   int rt_chunk = 0;           // 8-row tensor-core step: tiles per CTA between grid-wide jumps: 0 default (2)
   int reorder_curve = 1;      // locality ordering inside a patch: 1 sheet then a fine Hilbert curve, 0 reference index

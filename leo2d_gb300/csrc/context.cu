@@ -309,6 +309,9 @@ leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value
                   "rt_stage must be -1 (autotuned), 0 (registers), 1 (shared memory by cp.async) or 2 (shared "
                   "memory by TMA gathers)");
       ctx->rt_stage = (int)value;
+    } else if (k == "rt_rows") {
+      LEO_REQUIRE(value == 0 || value == 8 || value == 16, "rt_rows must be 0 (autotuned), 8 or 16");
+      ctx->rt_rows = (int)value;
     } else if (k == "rt_group") {
       LEO_REQUIRE(value >= 0 && value <= 16, "rt_group must be 0 (default) or 1..16");
       ctx->rt_group = (int)value;

@@ -80,9 +80,10 @@ struct leo2d_csr {
   bool rb_xs_built = false;           // positions for the velocity step (Kubo)
   leo2d::DevBuf<float> rb_xrel;       // [blocks][4] x of each row minus x of its block's first row
   leo2d::DevBuf<float> rb_xs;         // [slots] x of the slot's column minus the same
-  // row blocks of 8 rows for the tensor-core step (rt_spmm.cu): the union of
-  // each block's columns in k-steps of 8 slots, stored in the processing order
-  // of one launch shape (warps, group, chunk, grid)
+  // row blocks of 8 or 16 rows for the tensor-core step (rt_spmm.cu): the union
+  // of each block's columns in k-steps of 8 slots, stored in the processing
+  // order of one launch shape (warps, group, chunk, grid)
+  int rt_rows = 0;                    // rows per block of the counted / built blocks
   bool rt_counted = false;            // rt_kst holds the k-steps of every block
   bool rt_built = false;
   double rt_patch = 0.0;              // ordering the blocks were built from
@@ -95,7 +96,7 @@ struct leo2d_csr {
   unsigned rt_grid = 0;
   leo2d::DevBuf<int64_t> rt_kst;      // [blocks] k-steps of each block
   leo2d::DevBuf<int64_t> rt_wbeg;     // [grid * warps + 1] first k-step of each warp
-  leo2d::DevBuf<unsigned char> rt_data;  // 288 bytes per k-step
+  leo2d::DevBuf<unsigned char> rt_data;  // 32 + 32 rt_rows bytes per k-step
   // shared-memory windows of the row blocks (rbw_spmm.cu): per tile of 16 blocks
   // the sorted distinct columns of its slots; slots hold window positions
   bool rbw_built = false;
@@ -138,9 +139,10 @@ void csr_drop_rb(leo2d_csr* csr);
 void csr_build_rb_xs(leo2d_ctx* ctx, leo2d_csr* csr);
 // Largest data bytes of a tile of `tile` consecutive row blocks.
 int64_t rb_tile_max_bytes(leo2d_ctx* ctx, const leo2d_csr* csr, int tile);
-// Builds the 8-row blocks of the tensor-core step for one launch shape; returns
-// false (and builds nothing) when a block holds more than 2048 stored entries.
-bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chunk);
+// Builds the row blocks (8 or 16 rows) of the tensor-core step for one launch
+// shape; returns false (and builds nothing) when a block holds more than 2048
+// stored entries.
+bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chunk, int rows);
 void csr_drop_rt(leo2d_csr* csr);
 // Builds the shared-memory windows of the row blocks; returns false (and builds
 // nothing) when a tile of 16 blocks has more than 8192 slots or 2048 distinct columns.

@@ -265,6 +265,7 @@ struct Tuned {
   bool rt = false;  // the 8-row tensor-core step won for this block width
   int rt_warps = 0, rt_depth = 0;
   int rt_stage = 0;
+  int rt_rows = 8;
 };
 std::map<std::pair<leo2d_ctx*, ShapeKey>, Tuned> g_shape_cache;
 // best block width per (context, matrix, precision, columns requested)
@@ -338,9 +339,9 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
   if (shape.rt) {
     // 8-row blocks of the locality-ordered copy, stored for this launch shape
     const int w = shape.rt_warps;
-    const bool fits = rt_smem_bytes(w, shape.rt_depth, shape.rt_stage) + 8 * 1024 <= ctx->smem_optin;
-    if (fits && csr_build_rt(ctx, mm, w, rt_group_of(ctx), rt_chunk_of(ctx))) {
-      dyn_smem = rt_smem_bytes(w, shape.rt_depth, shape.rt_stage);
+    const bool fits = rt_smem_bytes(w, shape.rt_depth, shape.rt_stage, shape.rt_rows) + 8 * 1024 <= ctx->smem_optin;
+    if (fits && csr_build_rt(ctx, mm, w, rt_group_of(ctx), rt_chunk_of(ctx), shape.rt_rows)) {
+      dyn_smem = rt_smem_bytes(w, shape.rt_depth, shape.rt_stage, shape.rt_rows);
       grid = m->rt_grid;
       shape.tiled = false;
     } else {
@@ -527,6 +528,7 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
   s.rt_warps = ctx->rt_warps > 0 ? ctx->rt_warps : (cached && it->second.rt_warps > 0 ? it->second.rt_warps : 16);
   s.rt_stage = ctx->rt_stage >= 0 ? ctx->rt_stage : (cached && it->second.rt ? it->second.rt_stage : 1);
   s.rt_depth = ctx->rt_depth > 0 ? ctx->rt_depth : (cached && it->second.rt_depth > 0 ? it->second.rt_depth : 3);
+  s.rt_rows = ctx->rt_rows > 0 ? ctx->rt_rows : (cached && it->second.rt ? it->second.rt_rows : 8);
   LEO_REQUIRE(s.rows_per_item >= 0 && s.rows_per_item <= 64, "rows_per_warp must be 0..64");
   return s;
 }
@@ -824,19 +826,26 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
       // the 8-row tensor-core step where it applies: a few (warps, depth) shapes
       if (!fp64 && cols == 32 && !csr->complex_h && ctx->reorder != 0 &&
           (ctx->kernel_variant == -1 || ctx->kernel_variant == 5)) {
-        struct RtTry { int warps, depth, stage; };
+        struct RtTry { int warps, depth, stage, rows; };
         // (the TMA form, stage 2, is timed only when asked for: 1.8x slower)
-        for (const RtTry t : {RtTry{16, 3, 1}, RtTry{16, 2, 0}, RtTry{12, 7, 1}, RtTry{8, 7, 1}, RtTry{16, 3, 0},
-                              RtTry{16, 3, 2}, RtTry{12, 7, 2}}) {
+        // (16-row blocks: a third fewer k-steps on the 0.5 deg flakes but 1.7x the
+        // cost per k-step, 0.69 against 0.60 ms at 2.4M orbitals; kept as a
+        // candidate for denser matrices)
+        for (const RtTry t : {RtTry{16, 3, 1, 8}, RtTry{20, 3, 1, 8}, RtTry{12, 3, 1, 16}, RtTry{16, 2, 0, 8},
+                              RtTry{16, 3, 2, 8}, RtTry{12, 7, 2, 8}}) {
           if (t.stage == 2 && ctx->rt_stage != 2) continue;
           if (ctx->rt_stage >= 0 && ctx->rt_stage != t.stage) continue;
+          if (ctx->rt_rows > 0 && ctx->rt_rows != t.rows) continue;
           StepShape sh = choose_shape(ctx, csr, fp64, cols, cols, 0);
           sh.tc = false;
           sh.rb = false;
           sh.rt = true;
           sh.rt_stage = t.stage;
+          sh.rt_rows = t.rows;
           sh.rt_warps = ctx->rt_warps > 0 ? ctx->rt_warps : t.warps;
           sh.rt_depth = ctx->rt_depth > 0 ? ctx->rt_depth : t.depth;
+          // 16-row blocks come in two launch shapes
+          if (t.rows == 16 && !(sh.rt_depth == 3 && (sh.rt_warps == 12 || sh.rt_warps == 16))) continue;
           Recursion r;
           r.setup(ctx, csr, sh, steps);
           if (!r.shape.rt) break;
@@ -856,6 +865,7 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
             best_t.rt_warps = sh.rt_warps;
             best_t.rt_depth = sh.rt_depth;
             best_t.rt_stage = sh.rt_stage;
+            best_t.rt_rows = sh.rt_rows;
           }
           if (ctx->rt_warps > 0 && ctx->rt_depth > 0) break;  // one shape asked for
         }

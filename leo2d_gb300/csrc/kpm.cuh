@@ -25,6 +25,7 @@ struct StepShape {
                            // cp.async 3, 7; TMA 3, 7)
   int rt_stage = 1;        // 8-row step: T_n rows staged in 0 registers, 1 shared memory by cp.async,
                            // 2 shared memory by TMA gathers
+  int rt_rows = 8;         // rows per block (8; 16 with rt_stage 1)
 };
 
 // Vector block resident on the device: two buffers of n x cols (T_k, T_{k-1}).
@@ -82,8 +83,8 @@ void rb_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
 // The 8-row tensor-core step (rt_spmm.cu): shared memory of a shape, the grid
 // its blocks are built for (csr_build_rt with rt_group_of / rt_chunk_of), and
 // one launch.
-size_t rt_smem_bytes(int warps, int depth, int stage);
-unsigned rt_grid(leo2d_ctx* ctx, const leo2d_csr* csr, int warps);
+size_t rt_smem_bytes(int warps, int depth, int stage, int rows);
+unsigned rt_grid(leo2d_ctx* ctx, const leo2d_csr* csr, int warps, int rows);
 int rt_group_of(const leo2d_ctx* ctx);
 int rt_chunk_of(const leo2d_ctx* ctx);
 void rt_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape, unsigned grid, size_t smem,

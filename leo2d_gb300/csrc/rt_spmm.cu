@@ -61,8 +61,10 @@ namespace {
 
 #include "rb_common.cuh"
 
-constexpr int kRtRows = 8;           // rows per block
-constexpr int kRtStepBytes = 288;    // one k-step: 8 columns + 32 value pairs
+constexpr int kRtRows = 8;           // rows of an n-tile (and of the 8-row blocks)
+constexpr int kRtStepBytes = 288;    // one k-step of an 8-row block: 8 columns + 32 value pairs
+// one k-step of a block of R rows: 8 columns + 8 R values
+__host__ __device__ constexpr int rt_step_bytes(int R) { return 32 + 32 * R; }
 constexpr int kRtMaxEnt = 2048;      // stored entries of one block (build limit)
 constexpr int kRtBuildWarps = 4;
 // staging of the gathered T_n rows (the kernel's STAGE parameter)
@@ -150,34 +152,48 @@ namespace {
 // lo*lo term and the truncation of lo leave a relative error below 2^-20. The
 // hi*hi terms and the two cross terms go to separate FP32 accumulators (four
 // independent MMA chains per k-step), summed at the block's end.
+// The A operand of one k-step (chunk cg of the T_n rows of slots t and t + 4)
+// split into TF32 high and low parts; shared by the n-tiles of a 16-row block.
+struct RtA {
+  uint32_t ah[8], al[8];
+  __device__ __forceinline__ void split(const float4& fa, const float4& fb) {
+    constexpr uint32_t m = 0xffffe000u;
+    const float xs[8] = {fa.x, fa.y, fa.z, fa.w, fb.x, fb.y, fb.z, fb.w};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      ah[i] = __float_as_uint(xs[i]) & m;
+      al[i] = __float_as_uint(xs[i] - __uint_as_float(ah[i]));
+    }
+  }
+};
+
 struct RtAcc {
   float h0[4], h1[4], l0[4], l1[4];  // m-tiles 0 (logical columns 0..15) and 1 (16..31)
   __device__ __forceinline__ void zero() {
 #pragma unroll
     for (int i = 0; i < 4; ++i) h0[i] = h1[i] = l0[i] = l1[i] = 0.f;
   }
+  // A: the split rows; (vx, vy) = (V[g][t], V[g][t+4]) of this n-tile's rows
+  __device__ __forceinline__ void mma(const RtA& A, float vx, float vy) {
+    constexpr uint32_t m = 0xffffe000u;
+    const uint32_t bh0 = __float_as_uint(vx) & m, bh1 = __float_as_uint(vy) & m;
+    const uint32_t bl0 = __float_as_uint(vx - __uint_as_float(bh0));
+    const uint32_t bl1 = __float_as_uint(vy - __uint_as_float(bh1));
+    // logical columns g, g + 8 (m-tile 0) and g + 16, g + 24 (m-tile 1)
+    mma_tf32(l0, A.al[0], A.al[1], A.al[4], A.al[5], bh0, bh1);
+    mma_tf32(l1, A.al[2], A.al[3], A.al[6], A.al[7], bh0, bh1);
+    mma_tf32(h0, A.ah[0], A.ah[1], A.ah[4], A.ah[5], bh0, bh1);
+    mma_tf32(h1, A.ah[2], A.ah[3], A.ah[6], A.ah[7], bh0, bh1);
+    mma_tf32(l0, A.ah[0], A.ah[1], A.ah[4], A.ah[5], bl0, bl1);
+    mma_tf32(l1, A.ah[2], A.ah[3], A.ah[6], A.ah[7], bl0, bl1);
+  }
   // fa, fb: chunk cg of the T_n rows of slots t and t + 4; v: (V[g][t], V[g][t+4])
   __device__ __forceinline__ void add(const float4& fa, const float4& fb, const float2& v) {
-    constexpr uint32_t m = 0xffffe000u;
-    const float xs[8] = {fa.x, fa.y, fa.z, fa.w, fb.x, fb.y, fb.z, fb.w};
-    uint32_t ah[8], al[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      ah[i] = __float_as_uint(xs[i]) & m;
-      al[i] = __float_as_uint(xs[i] - __uint_as_float(ah[i]));
-    }
-    const uint32_t bh0 = __float_as_uint(v.x) & m, bh1 = __float_as_uint(v.y) & m;
-    const uint32_t bl0 = __float_as_uint(v.x - __uint_as_float(bh0));
-    const uint32_t bl1 = __float_as_uint(v.y - __uint_as_float(bh1));
-    // logical columns g, g + 8 (m-tile 0) and g + 16, g + 24 (m-tile 1)
-    mma_tf32(l0, al[0], al[1], al[4], al[5], bh0, bh1);
-    mma_tf32(l1, al[2], al[3], al[6], al[7], bh0, bh1);
-    mma_tf32(h0, ah[0], ah[1], ah[4], ah[5], bh0, bh1);
-    mma_tf32(h1, ah[2], ah[3], ah[6], ah[7], bh0, bh1);
-    mma_tf32(l0, ah[0], ah[1], ah[4], ah[5], bl0, bl1);
-    mma_tf32(l1, ah[2], ah[3], ah[6], ah[7], bl0, bl1);
+    RtA A;
+    A.split(fa, fb);
+    mma(A, v.x, v.y);
   }
-  // rows 2t and 2t + 1 of the block, memory columns 4 cg .. 4 cg + 3
+  // rows 2t and 2t + 1 of the n-tile, memory columns 4 cg .. 4 cg + 3
   __device__ __forceinline__ void rows(float4& r0, float4& r1) const {
     r0 = make_float4(h0[0] + l0[0], h0[2] + l0[2], h1[0] + l1[0], h1[2] + l1[2]);
     r1 = make_float4(h0[1] + l0[1], h0[3] + l0[3], h1[1] + l1[1], h1[3] + l1[3]);
@@ -223,9 +239,12 @@ __device__ __forceinline__ float2 ld_stream_f2(const void* p) {
 // Each warp walks its blocks in the build's processing order: runs of G
 // consecutive blocks, run i in tile (bid + (i / chunk) grid) chunk + i % chunk;
 // a block ends after its k-step count (kst), read one block ahead.
-template <int W, int D, int STAGE>
+template <int W, int D, int STAGE, int R>
 __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const int nblk) {
   constexpr bool REGS = STAGE == kRtRegs;
+  constexpr int NTI = R / kRtRows;       // n-tiles (8 rows each) of a block
+  constexpr int KB = rt_step_bytes(R);   // bytes of one k-step
+  static_assert((R == 8 || R == 16) && (R == 8 || STAGE == kRtCpAsync), "16-row blocks: cp.async form only");
   constexpr int C = 32;
   constexpr int NT = W * 32;
   constexpr int XS = D + 1;      // shared ring of staged T_n rows (k-steps)
@@ -253,7 +272,7 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
   const int64_t* kst = a.kst;
   const int64_t k0 = a.wbeg[bid * W + warp];
   const int nk = (int)(a.wbeg[bid * W + warp + 1] - k0);
-  const unsigned char* gdata = a.data + k0 * kRtStepBytes;
+  const unsigned char* gdata = a.data + k0 * KB;
 
   // block walk, block-end countdown and epilogue operands
   // run i of the warp lies in tile (bid + (i / chunk) nblk) chunk + i % chunk;
@@ -262,7 +281,7 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
   int jb = 0;
   int64_t tb = (int64_t)bid * chunk;
   int ic = 0;
-  auto run_row = [&]() -> int64_t { return ((tb + ic) * W + warp) * group * kRtRows; };
+  auto run_row = [&]() -> int64_t { return ((tb + ic) * W + warp) * group * R; };
   auto next_run = [&]() {
     if (++ic == chunk) {
       ic = 0;
@@ -273,8 +292,11 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
   next_run();
   int64_t nbase = run_row();  // first row of the next run
   int left = 0;                                       // k-steps of the current block still to run
-  int next_left = nk > 0 ? (int)kst[rbase / kRtRows] : 0;  // the next block's k-steps
-  float4 xn0 = make_float4(0.f, 0.f, 0.f, 0.f), xn1 = xn0, xp0 = xn0, xp1 = xn0;
+  int next_left = nk > 0 ? (int)kst[rbase / R] : 0;  // the next block's k-steps
+  // T_n and T_{n-1} of the lane's rows 8 nt + 2t and 8 nt + 2t + 1 of the block
+  float4 xn0[NTI], xn1[NTI], xp0[NTI], xp1[NTI];
+#pragma unroll
+  for (int nt = 0; nt < NTI; ++nt) xn0[nt] = xn1[nt] = xp0[nt] = xp1[nt] = make_float4(0.f, 0.f, 0.f, 0.f);
   // dots: FP32 over kDotFlush blocks, then FP64; lane (g, t) ends with column 4 cg + t
   double d0 = 0.0, d1 = 0.0;
   float e0[4], e1[4];
@@ -302,19 +324,22 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
     for (int c = 0; c < 4; ++c) e0[c] = e1[c] = 0.f;
   };
   auto begin_block = [&]() {
-    row0 = rbase + (int64_t)jb * kRtRows;
+    row0 = rbase + (int64_t)jb * R;
     left = next_left;
     // the k-steps of the block after this one (its run may start elsewhere)
-    const int64_t nrow = jb + 1 < group ? row0 + kRtRows : nbase;
-    if (nrow / kRtRows < a.nrb) next_left = (int)kst[nrow / kRtRows];
-    const int64_t r0 = row0 + 2 * t;
-    if (r0 < n) {
-      xn0 = ldg4(tnc + r0 * C);
-      if (!first) xp0 = ld_once4(tprev + r0 * C + 4 * cg);
-    }
-    if (r0 + 1 < n) {
-      xn1 = ldg4(tnc + (r0 + 1) * C);
-      if (!first) xp1 = ld_once4(tprev + (r0 + 1) * C + 4 * cg);
+    const int64_t nrow = jb + 1 < group ? row0 + R : nbase;
+    if (nrow / R < a.nrb) next_left = (int)kst[nrow / R];
+#pragma unroll
+    for (int nt = 0; nt < NTI; ++nt) {
+      const int64_t r0 = row0 + 8 * nt + 2 * t;
+      if (r0 < n) {
+        xn0[nt] = ldg4(tnc + r0 * C);
+        if (!first) xp0[nt] = ld_once4(tprev + r0 * C + 4 * cg);
+      }
+      if (r0 + 1 < n) {
+        xn1[nt] = ldg4(tnc + (r0 + 1) * C);
+        if (!first) xp1[nt] = ld_once4(tprev + (r0 + 1) * C + 4 * cg);
+      }
     }
   };
   auto row_out = [&](int64_t r, const float4& h, const float4& xp, const float4& xn) {
@@ -332,15 +357,19 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
     e1[2] += y.z * xn.z;
     e1[3] += y.w * xn.w;
   };
-  RtAcc acc;
-  acc.zero();
+  RtAcc acc[NTI];
+#pragma unroll
+  for (int nt = 0; nt < NTI; ++nt) acc[nt].zero();
   auto end_block = [&]() {
-    float4 h0, h1;
-    acc.rows(h0, h1);
-    acc.zero();
-    const int64_t r0 = row0 + 2 * t;
-    row_out(r0, h0, xp0, xn0);
-    row_out(r0 + 1, h1, xp1, xn1);
+#pragma unroll
+    for (int nt = 0; nt < NTI; ++nt) {
+      float4 h0, h1;
+      acc[nt].rows(h0, h1);
+      acc[nt].zero();
+      const int64_t r0 = row0 + 8 * nt + 2 * t;
+      row_out(r0, h0, xp0[nt], xn0[nt]);
+      row_out(r0 + 1, h1, xp1[nt], xn1[nt]);
+    }
     if (++jb == group) {
       jb = 0;
       rbase = nbase;
@@ -355,22 +384,22 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
   // the MMAs of one k-step, with the block walk around them
   auto consume = [&](const float4& fa, const float4& fb, const float2& v) {
     if (left == 0) begin_block();
-    acc.add(fa, fb, v);
+    acc[0].add(fa, fb, v);
     if (--left == 0) end_block();
   };
 
   if constexpr (STAGE == kRtCpAsync) {
-    constexpr int kWarpBytes = XS * 1024 + MS * kRtStepBytes;
+    constexpr int kWarpBytes = XS * 1024 + MS * KB;
+    constexpr int kChunks = KB / 16;  // 16-byte chunks of a matrix k-step (18 or 34)
     static_assert(MS % 8 == 0, "L2 prefetch every 8 matrix k-steps at fixed slots of the unrolled loop");
     unsigned char* xr = rt_smem + (size_t)warp * kWarpBytes;
     unsigned char* mr = xr + XS * 1024;
-    const bool mlane = lane < kRtStepBytes / 16;
     // Lane (g, t) copies, and later reads, chunk cg of the T_n rows of slots t
     // and t + 4 (16-byte chunk c of row s at c ^ s: no bank conflicts either
     // way, and a quarter of the warp covers each 128-byte row). A lane reads
     // only rows it copied itself, so its own cp.async wait orders them; the
-    // matrix k-steps (copied by lanes 0..17, read by all) are ordered by one
-    // __syncwarp per iteration.
+    // matrix k-steps (copied in 16-byte chunks by all lanes, read by all) are
+    // ordered by one __syncwarp per iteration.
     const int ro0 = t * 128 + 16 * (cg ^ t), ro1 = 512 + t * 128 + 16 * (cg ^ (t + 4));
     // iteration u (matrix slot sm = u mod MS): wait for the copies of iteration
     // u - D (the rows of k-step u, matrix k-step u + DM), copy matrix k-step
@@ -380,13 +409,17 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
       cp_async_wait<D - 1>();
       __syncwarp();  // every lane's matrix copies have landed; k-step u - 1 is read
       const int vm = u + D + DM, vx = u + D;
-      if (mlane && (!checks || vm < nk))
-        cp_async_cg16(mr + ((sm + MS - 1) & (MS - 1)) * kRtStepBytes + 16 * lane, mb + (off + (D + DM) * kRtStepBytes));
+      if (!checks || vm < nk) {
+        unsigned char* md = mr + ((sm + MS - 1) & (MS - 1)) * KB + 16 * lane;
+        const unsigned char* msrc = mb + (off + (D + DM) * KB);
+        if (lane < kChunks) cp_async_cg16(md, msrc);
+        if (kChunks > 32 && lane < kChunks - 32) cp_async_cg16(md + 512, msrc + 512);
+      }
       if (pf && lane == 0 && vm + kPf < nk)
-        prefetch_l2_bulk(gdata + (size_t)(vm + kPf) * kRtStepBytes, (uint32_t)min(8, nk - vm - kPf) * kRtStepBytes);
+        prefetch_l2_bulk(gdata + (size_t)(vm + kPf) * KB, (uint32_t)min(8, nk - vm - kPf) * KB);
       if (!checks || (vx >= 0 && vx < nk)) {
         // the columns of k-step vx (slots t, t + 4) landed DM iterations ago
-        const int2 cc = *reinterpret_cast<const int2*>(mr + ((sm + D) & (MS - 1)) * kRtStepBytes + 8 * t);
+        const int2 cc = *reinterpret_cast<const int2*>(mr + ((sm + D) & (MS - 1)) * KB + 8 * t);
         unsigned char* dst = xr + ((sm + D) & (XS - 1)) * 1024;
         cp_async_cg16(dst + ro0, tnc + (uint64_t)(uint32_t)cc.x * C);
         cp_async_cg16(dst + ro1, tnc + (uint64_t)(uint32_t)cc.y * C);
@@ -394,9 +427,18 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
       cp_async_commit();
       if (checks && u < 0) return;
       const unsigned char* xs = xr + (sm & (XS - 1)) * 1024;
-      const unsigned char* ms = mr + sm * kRtStepBytes;
-      acc.add(*reinterpret_cast<const float4*>(xs + ro0), *reinterpret_cast<const float4*>(xs + ro1),
-              *reinterpret_cast<const float2*>(ms + 32 + 8 * lane));
+      const unsigned char* ms = mr + sm * KB;
+      RtA A;
+      A.split(*reinterpret_cast<const float4*>(xs + ro0), *reinterpret_cast<const float4*>(xs + ro1));
+      if constexpr (NTI == 1) {
+        const float2 v = *reinterpret_cast<const float2*>(ms + 32 + 8 * lane);
+        acc[0].mma(A, v.x, v.y);
+      } else {
+        // (V[g][t], V[g][t+4]) of n-tile 0, then of n-tile 1
+        const float4 v = *reinterpret_cast<const float4*>(ms + 32 + 16 * lane);
+        acc[0].mma(A, v.x, v.y);
+        acc[1].mma(A, v.z, v.w);
+      }
       if (--left == 0) {
         end_block();
         if (u + 1 < nk) begin_block();
@@ -405,15 +447,15 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
     if (nk > 0) begin_block();
     const unsigned char* mlan = gdata + 16 * lane;  // this lane's chunk of matrix k-step 0
     int u = -(D + DM);
-    for (; u < 0; ++u) iter(u, u & (MS - 1), mlan, u * kRtStepBytes, true, (((u + D + DM) & 7) == 0));
+    for (; u < 0; ++u) iter(u, u & (MS - 1), mlan, u * KB, true, (((u + D + DM) & 7) == 0));
     const int main_end = nk - (D + DM) > 0 ? ((nk - (D + DM)) & ~(MS - 1)) : 0;
     for (; u < main_end; u += MS) {
-      const unsigned char* mb = mlan + (size_t)u * kRtStepBytes;
+      const unsigned char* mb = mlan + (size_t)u * KB;
 #pragma unroll
-      for (int j = 0; j < MS; ++j) iter(u + j, j, mb, j * kRtStepBytes, false, ((j + D + DM) & 7) == 0);
+      for (int j = 0; j < MS; ++j) iter(u + j, j, mb, j * KB, false, ((j + D + DM) & 7) == 0);
     }
     for (; u < nk; ++u)
-      iter(u, u & (MS - 1), mlan, u * kRtStepBytes, true, (((u + D + DM) & 7) == 0));
+      iter(u, u & (MS - 1), mlan, u * KB, true, (((u + D + DM) & 7) == 0));
     cp_async_wait<0>();
   } else if constexpr (STAGE == kRtTma) {
     // Each warp owns XS entries of 2 KB (1 KB aligned): row entry e holds slots
@@ -580,19 +622,21 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
   for (int i = threadIdx.x; i < 2 * C; i += NT) a.partials[(size_t)bid * 2 * C + i] = bsum[i];
 }
 
-template <int W, int D, int STAGE>
+template <int W, int D, int STAGE, int R = kRtRows>
 __global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ RtArgs a) {
-  rt_body<W, D, STAGE>(a, (int)blockIdx.x, (int)gridDim.x);
+  rt_body<W, D, STAGE, R>(a, (int)blockIdx.x, (int)gridDim.x);
 }
 
 // ---------------------------------------------------------------- format build
 
-// One warp per block of 8 rows, at most kRtMaxEnt stored entries: the keys
+// One warp per block of R rows, at most kRtMaxEnt stored entries: the keys
 // (column << 16 | entry index) are sorted in the warp's slice of shared memory;
 // the distinct columns are the slots. Pass 0 writes the k-steps of each block;
 // pass 1 writes the block's k-steps at kstart[b] (data zero-filled before): the
-// columns in the interleaved order, the values in fragment order, entries of
-// one (row, column) summed in entry order.
+// columns in the interleaved order, the values in fragment order (lane 4g + t
+// holds V[g][t], V[g][t+4] of each n-tile of 8 rows in turn), entries of one
+// (row, column) summed in entry order.
+template <int R>
 __global__ void __launch_bounds__(kRtBuildWarps * 32)
     k_rt_build(int64_t n, int64_t nrb, const int64_t* __restrict__ prow, const int32_t* __restrict__ pcol,
                const float* __restrict__ pval, int pass, int64_t* __restrict__ kst,
@@ -603,16 +647,16 @@ __global__ void __launch_bounds__(kRtBuildWarps * 32)
   unsigned long long* keys = rt_keys + (size_t)w * kRtMaxEnt;
   const int64_t warps = (int64_t)gridDim.x * kRtBuildWarps;
   for (int64_t b = (int64_t)blockIdx.x * kRtBuildWarps + w; b < nrb; b += warps) {
-    const int64_t r0 = b * kRtRows;
-    const int rows = (int)min((int64_t)kRtRows, n - r0);
-    const int64_t mine = lane <= kRtRows ? prow[r0 + min(lane, rows)] : 0;
-    int64_t srp[kRtRows + 1];
+    const int64_t r0 = b * R;
+    const int rows = (int)min((int64_t)R, n - r0);
+    const int64_t mine = lane <= R ? prow[r0 + min(lane, rows)] : 0;
+    int64_t srp[R + 1];
 #pragma unroll
-    for (int k = 0; k <= kRtRows; ++k) srp[k] = __shfl_sync(0xffffffffu, mine, k);
+    for (int k = 0; k <= R; ++k) srp[k] = __shfl_sync(0xffffffffu, mine, k);
     auto srp_at = [&](int k) {
       int64_t v = srp[0];
 #pragma unroll
-      for (int kk = 1; kk <= kRtRows; ++kk)
+      for (int kk = 1; kk <= R; ++kk)
         if (k == kk) v = srp[kk];
       return v;
     };
@@ -620,7 +664,7 @@ __global__ void __launch_bounds__(kRtBuildWarps * 32)
     auto row_of = [&](int e) {
       int r = 0;
 #pragma unroll
-      for (int k = 1; k < kRtRows; ++k) r += (k < rows && srp[k] - srp[0] <= e) ? 1 : 0;
+      for (int k = 1; k < R; ++k) r += (k < rows && srp[k] - srp[0] <= e) ? 1 : 0;
       return r;
     };
     const int64_t q0 = srp[0];
@@ -678,10 +722,10 @@ __global__ void __launch_bounds__(kRtBuildWarps * 32)
       }
       continue;
     }
-    unsigned char* base = data + (size_t)kstart[b] * kRtStepBytes;
+    unsigned char* base = data + (size_t)kstart[b] * rt_step_bytes(R);
     auto col_at = [&](int s) {  // column entry of slot s
       const int jj = s & 7;
-      return reinterpret_cast<int32_t*>(base + (size_t)(s >> 3) * kRtStepBytes) + (jj < 4 ? 2 * jj : 2 * (jj - 4) + 1);
+      return reinterpret_cast<int32_t*>(base + (size_t)(s >> 3) * rt_step_bytes(R)) + (jj < 4 ? 2 * jj : 2 * (jj - 4) + 1);
     };
     const int32_t pad_col = K > 0 ? (int32_t)(keys[0] >> 16) : 0;
     for (int s = K + lane; s < 8 * KS; s += 32) *col_at(s) = pad_col;
@@ -710,8 +754,8 @@ __global__ void __launch_bounds__(kRtBuildWarps * 32)
           v += pval[q0 + e2];
         }
         const int jj = s & 7;
-        float* vp = reinterpret_cast<float*>(base + (size_t)(s >> 3) * kRtStepBytes + 32);
-        vp[2 * (4 * r + (jj & 3)) + (jj >> 2)] = v;
+        float* vp = reinterpret_cast<float*>(base + (size_t)(s >> 3) * rt_step_bytes(R) + 32);
+        vp[(4 * (r & 7) + (jj & 3)) * (R / 4) + 2 * (r >> 3) + (jj >> 2)] = v;
       }
     }
   }
@@ -746,9 +790,9 @@ struct RtShape {
   unsigned grid;
 };
 
-RtShape rt_shape(const leo2d_ctx* ctx, int64_t n, int warps, int group, int chunk) {
+RtShape rt_shape(const leo2d_ctx* ctx, int64_t n, int warps, int group, int chunk, int rows) {
   RtShape s;
-  s.nrb = (n + kRtRows - 1) / kRtRows;
+  s.nrb = (n + rows - 1) / rows;
   s.nruns = (s.nrb + group - 1) / group;
   s.ntiles = (s.nruns + warps - 1) / warps;
   const int64_t chunks = (s.ntiles + chunk - 1) / chunk;
@@ -757,10 +801,10 @@ RtShape rt_shape(const leo2d_ctx* ctx, int64_t n, int warps, int group, int chun
 }
 
 // Shared memory of one warp's rings for row lookahead D (rows: D + 1 k-steps,
-// matrix: 2 (D + 1) k-steps): packed for cp.async; for TMA gathers 2 KB per row
-// entry (the matrix in its holes) and its mbarrier.
-constexpr int rt_warp_bytes(int depth, int stage) {
-  return stage == kRtTma ? (depth + 1) * (2048 + 8) : (depth + 1) * 1024 + 2 * (depth + 1) * kRtStepBytes;
+// matrix: 2 (D + 1) k-steps of blocks of `rows` rows): packed for cp.async; for
+// TMA gathers 2 KB per row entry (the matrix in its holes) and its mbarrier.
+constexpr int rt_warp_bytes(int depth, int stage, int rows) {
+  return stage == kRtTma ? (depth + 1) * (2048 + 8) : (depth + 1) * 1024 + 2 * (depth + 1) * rt_step_bytes(rows);
 }
 
 // TMA maps of the T_n buffers a thread launched the TMA form on (three
@@ -793,13 +837,13 @@ namespace leo2d {
 int rt_group_of(const leo2d_ctx* ctx) { return ctx->rt_group > 0 ? ctx->rt_group : 2; }
 int rt_chunk_of(const leo2d_ctx* ctx) { return ctx->rt_chunk > 0 ? ctx->rt_chunk : 2; }
 
-size_t rt_smem_bytes(int warps, int depth, int stage) {
+size_t rt_smem_bytes(int warps, int depth, int stage, int rows) {
   // shared-memory forms: 1 KB of slack to align the rings
-  return stage == kRtRegs ? 0 : (size_t)warps * rt_warp_bytes(depth, stage) + 1024;
+  return stage == kRtRegs ? 0 : (size_t)warps * rt_warp_bytes(depth, stage, rows) + 1024;
 }
 
-unsigned rt_grid(leo2d_ctx* ctx, const leo2d_csr* csr, int warps) {
-  return rt_shape(ctx, csr->n, warps, rt_group_of(ctx), rt_chunk_of(ctx)).grid;
+unsigned rt_grid(leo2d_ctx* ctx, const leo2d_csr* csr, int warps, int rows) {
+  return rt_shape(ctx, csr->n, warps, rt_group_of(ctx), rt_chunk_of(ctx), rows).grid;
 }
 
 void csr_drop_rt(leo2d_csr* csr) {
@@ -812,29 +856,35 @@ void csr_drop_rt(leo2d_csr* csr) {
   csr->rt_max_slots = 0;
   csr->rt_warps = csr->rt_group = csr->rt_chunk = 0;
   csr->rt_grid = 0;
+  csr->rt_rows = 0;
 }
 
-bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chunk) {
-  LEO_REQUIRE(csr->reordered && !csr->complex_h, "the 8-row tensor-core step needs the real locality-ordered copy");
+bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chunk, int rows) {
+  LEO_REQUIRE(csr->reordered && !csr->complex_h, "the tensor-core row-block step needs the real locality-ordered copy");
+  LEO_REQUIRE(rows == 8 || rows == 16, "tensor-core row blocks hold 8 or 16 rows");
   const int64_t n = csr->n;
-  const RtShape sh = rt_shape(ctx, n, warps, group, chunk);
-  if (csr->rt_built && csr->rt_patch == csr->reorder_patch && csr->rt_curve == csr->reorder_curve &&
-      csr->rt_warps == warps && csr->rt_group == group && csr->rt_chunk == chunk && csr->rt_grid == sh.grid)
+  const int KB = rt_step_bytes(rows);
+  const RtShape sh = rt_shape(ctx, n, warps, group, chunk, rows);
+  if (csr->rt_built && csr->rt_rows == rows && csr->rt_patch == csr->reorder_patch &&
+      csr->rt_curve == csr->reorder_curve && csr->rt_warps == warps && csr->rt_group == group &&
+      csr->rt_chunk == chunk && csr->rt_grid == sh.grid)
     return true;
   const size_t smem = (size_t)kRtBuildWarps * kRtMaxEnt * sizeof(unsigned long long);
-  LEO_CUDA(cudaFuncSetAttribute(k_rt_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  auto build_kernel = rows == 16 ? k_rt_build<16> : k_rt_build<8>;
+  LEO_CUDA(cudaFuncSetAttribute(build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const unsigned bgrid = grid_for(sh.nrb * 32, kRtBuildWarps * 32, (int64_t)ctx->sm_count * 8);
   DevBuf<int> err(2);
   DevBuf<unsigned long long> ssum(1);
   LEO_CUDA(cudaMemsetAsync(err.p, 0, 2 * sizeof(int), ctx->stream));
   LEO_CUDA(cudaMemsetAsync(ssum.p, 0, sizeof(unsigned long long), ctx->stream));
-  if (!(csr->rt_counted && csr->rt_patch == csr->reorder_patch && csr->rt_curve == csr->reorder_curve)) {
+  if (!(csr->rt_counted && csr->rt_rows == rows && csr->rt_patch == csr->reorder_patch &&
+        csr->rt_curve == csr->reorder_curve)) {
     csr_drop_rt(csr);
     csr->rt_kst.alloc(std::max<int64_t>(sh.nrb, 1));
     launch(ctx, "rt_build", [&] {
-      k_rt_build<<<bgrid, kRtBuildWarps * 32, smem, ctx->stream>>>(n, sh.nrb, csr->prow.p, csr->pcol.p,
-                                                                     csr->pval32.p, 0, csr->rt_kst.p, nullptr,
-                                                                     nullptr, err.p, ssum.p);
+      build_kernel<<<bgrid, kRtBuildWarps * 32, smem, ctx->stream>>>(n, sh.nrb, csr->prow.p, csr->pcol.p,
+                                                                       csr->pval32.p, 0, csr->rt_kst.p, nullptr,
+                                                                       nullptr, err.p, ssum.p);
     });
     int h[2] = {0, 0};
     unsigned long long hs = 0;
@@ -846,6 +896,7 @@ bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chun
       return false;
     }
     csr->rt_counted = true;
+    csr->rt_rows = rows;
     csr->rt_patch = csr->reorder_patch;
     csr->rt_curve = csr->reorder_curve;
     csr->rt_union = (int64_t)hs;
@@ -873,7 +924,7 @@ bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chun
       }
     }
   first[(size_t)sh.grid * warps] = (int64_t)seq.size();
-  LEO_REQUIRE((int64_t)seq.size() == sh.nrb, "8-row block order does not cover the matrix");
+  LEO_REQUIRE((int64_t)seq.size() == sh.nrb, "row-block order does not cover the matrix");
   DevBuf<int32_t> dseq(std::max<int64_t>(sh.nrb, 1));
   DevBuf<int64_t> kseq(std::max<int64_t>(sh.nrb, 1)), pos(sh.nrb + 1), dfirst(first.size());
   h2d(ctx, dseq.p, seq.data(), seq.size());
@@ -892,17 +943,17 @@ bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chun
                                                                                    csr->rt_wbeg.p);
   });
   csr->rt_data.release();
-  csr->rt_data.alloc((size_t)std::max<int64_t>(total, 1) * kRtStepBytes);
-  LEO_CUDA(cudaMemsetAsync(csr->rt_data.p, 0, (size_t)std::max<int64_t>(total, 1) * kRtStepBytes, ctx->stream));
+  csr->rt_data.alloc((size_t)std::max<int64_t>(total, 1) * KB);
+  LEO_CUDA(cudaMemsetAsync(csr->rt_data.p, 0, (size_t)std::max<int64_t>(total, 1) * KB, ctx->stream));
   launch(ctx, "rt_build", [&] {
-    k_rt_build<<<bgrid, kRtBuildWarps * 32, smem, ctx->stream>>>(n, sh.nrb, csr->prow.p, csr->pcol.p, csr->pval32.p,
-                                                                   1, nullptr, kstart.p, csr->rt_data.p, err.p,
-                                                                   ssum.p);
+    build_kernel<<<bgrid, kRtBuildWarps * 32, smem, ctx->stream>>>(n, sh.nrb, csr->prow.p, csr->pcol.p,
+                                                                     csr->pval32.p, 1, nullptr, kstart.p,
+                                                                     csr->rt_data.p, err.p, ssum.p);
   });
   int h0 = 0;
   d2h(ctx, &h0, err.p, 1);
   ctx_sync(ctx);
-  LEO_REQUIRE(h0 == 0, "8-row block build: a block exceeds the entry limit after counting");
+  LEO_REQUIRE(h0 == 0, "row-block build: a block exceeds the entry limit after counting");
   csr->rt_blocks = sh.nrb;
   csr->rt_ksteps = total;
   csr->rt_warps = warps;
@@ -916,10 +967,11 @@ bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chun
 void rt_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape, unsigned grid, size_t smem,
                     const float* tn, float* tp, const float* tprev, int first, float alpha, double* partials,
                     const double* prev_partials, double* prev_dots) {
-  LEO_REQUIRE(csr->rt_built && csr->rt_warps == shape.rt_warps && csr->rt_grid == grid,
-              "8-row blocks built for another launch shape");
-  LEO_REQUIRE(smem >= rt_smem_bytes(shape.rt_warps, shape.rt_depth, shape.rt_stage),
-              "8-row step shared memory changed since setup");
+  LEO_REQUIRE(csr->rt_built && csr->rt_warps == shape.rt_warps && csr->rt_grid == grid &&
+                  csr->rt_rows == shape.rt_rows,
+              "tensor-core row blocks built for another launch shape");
+  LEO_REQUIRE(smem >= rt_smem_bytes(shape.rt_warps, shape.rt_depth, shape.rt_stage, shape.rt_rows),
+              "tensor-core row-block step: shared memory changed since setup");
   RtArgs a{};
   if (shape.rt_stage == kRtTma) {
     LEO_REQUIRE(csr->n < (1ll << 31), "TMA row gathers take int32 row coordinates");
@@ -950,6 +1002,14 @@ void rt_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
     launch(ctx, "cheb_step", [&] { kern<<<grid, warps * 32, smem, ctx->stream>>>(a); });
   };
   const int key = shape.rt_warps * 10 + shape.rt_depth;
+  if (shape.rt_rows == 16) {
+    if (shape.rt_stage == kRtCpAsync)
+      switch (key) {
+        case 123: return go(k_cheb_rt<12, 3, kRtCpAsync, 16>, 12);
+        case 163: return go(k_cheb_rt<16, 3, kRtCpAsync, 16>, 16);
+      }
+    fail(LEO2D_ERR_BAD_ARG, "16-row blocks: shared memory by cp.async (stage 1), warps 12 or 16, depth 3");
+  }
   if (shape.rt_stage == kRtRegs) {
     switch (key) {
       case 162: return go(k_cheb_rt<16, 2, kRtRegs>, 16);

@@ -46,7 +46,7 @@ def _run(ctx, variant, fn, **opts):
     finally:
         ctx.set_option("step_kernel", -1)
         ctx.set_option("reorder", -1)
-        for k in ("rt_warps", "rt_depth", "rt_group", "rt_chunk"):
+        for k in ("rt_warps", "rt_depth", "rt_group", "rt_chunk", "rt_rows"):
             ctx.set_option(k, 0)
         ctx.set_option("rt_stage", -1)
         ctx.set_option("reorder_curve", 1)
@@ -88,6 +88,8 @@ def test_rt_dos_matches(ctx, size, twist, model):
                                   {"rt_stage": 2, "rt_warps": 12, "rt_depth": 7},
                                   {"rt_stage": 2, "rt_warps": 8, "rt_depth": 7},
                                   {"rt_stage": 2, "rt_group": 3, "rt_chunk": 5},
+                                  {"rt_rows": 16}, {"rt_rows": 16, "rt_warps": 12},
+                                  {"rt_rows": 16, "rt_group": 3, "rt_chunk": 5},
                                   {"rt_group": 1}, {"rt_group": 7},
                                   {"rt_chunk": 1}, {"rt_chunk": 5, "rt_group": 3}])
 def test_rt_launch_shapes(ctx, opts):
@@ -97,7 +99,8 @@ def test_rt_launch_shapes(ctx, opts):
     cfg = L.kpm_cfg(64, R=16, seed=5, block=32)
     base = _run(ctx, 5, lambda: csr.kpm_dos(cfg))
     got = _run(ctx, 5, lambda: csr.kpm_dos(cfg), **opts)
-    assert csr.rt_info()[0] == (csr.n + 7) // 8
+    rows = opts.get("rt_rows", 8)
+    assert csr.rt_info()[0] == (csr.n + rows - 1) // rows
     assert _rel(got, base) < 1e-6
 
 
@@ -143,16 +146,18 @@ def test_rt_ldos_and_host_vectors(ctx):
     assert _rel(got2, got) > 1e-3  # the values really changed
 
 
-def test_rt_ragged_last_block(ctx):
-    """Row counts that leave a partial last block (n not a multiple of 8 rows)."""
+@pytest.mark.parametrize("rows", [8, 16])
+def test_rt_ragged_last_block(ctx, rows):
+    """Row counts that leave a partial last block (n not a multiple of the rows
+    per block)."""
     seen = set()
     for size in (9, 10, 11, 13):
         csr = _flake(ctx, size, 4.0)
-        seen.add(csr.n % 8)
+        seen.add(csr.n % rows)
         cfg = L.kpm_cfg(32, R=16, seed=9, block=32)
         ref = _run(ctx, 0, lambda: csr.kpm_dos(cfg))
-        got = _run(ctx, 5, lambda: csr.kpm_dos(cfg))
-        assert csr.rt_info()[0] == (csr.n + 7) // 8
+        got = _run(ctx, 5, lambda: csr.kpm_dos(cfg), rt_rows=rows)
+        assert csr.rt_info()[0] == (csr.n + rows - 1) // rows
         assert _rel(got, ref) < 2e-5, (size, csr.n)
     assert seen - {0}
 
@@ -206,3 +211,41 @@ def test_rt_tma_timeout_reports(ctx):
         ctx.set_spin_limit(0)
     again = _run(ctx, 5, lambda: csr.kpm_dos(cfg), rt_stage=2, rt_warps=16, rt_depth=3)
     np.testing.assert_array_equal(ok, again)
+
+
+@pytest.mark.parametrize("size,twist,model", [(22, 3.0, L.MODEL_SIMPLE), (37, 1.2, L.MODEL_SIMPLE),
+                                             (25, 5.09, L.MODEL_REF)])
+def test_rt16_dos_matches(ctx, size, twist, model):
+    """Blocks of 16 rows (two n-tiles sharing each k-step's gathered rows): the
+    moments of the gather kernel to rounding, of the FP64 oracle to the FP32
+    bar, bit-identical on repeat; fewer union slots per row than 8-row blocks."""
+    csr = _flake(ctx, size, twist, model)
+    P, R = 96, 16
+    cfg = L.kpm_cfg(P, R=R, seed=3, block=32)
+    ref = _run(ctx, 0, lambda: csr.kpm_dos(cfg))
+    _run(ctx, 5, lambda: csr.kpm_dos(cfg), rt_rows=8)
+    union8 = csr.rt_info()[2]
+    got = _run(ctx, 5, lambda: csr.kpm_dos(cfg), rt_rows=16)
+    blocks, ksteps, union, max_slots = csr.rt_info()
+    assert blocks == (csr.n + 15) // 16
+    assert union <= 8 * ksteps < union + 8 * blocks
+    assert union < union8 and max_slots > 0
+    assert _rel(got, ref) < 2e-5
+    again = _run(ctx, 5, lambda: csr.kpm_dos(cfg), rt_rows=16)
+    np.testing.assert_array_equal(got, again)
+    assert _rel(got, _oracle_trace(csr, 3, R, P)) < 1e-4
+
+
+def test_rt16_stored_zeros_and_host_vectors(ctx):
+    """16-row blocks over a matrix with stored zeros, and host (Gaussian) start
+    vectors."""
+    csr = _flake(ctx, 24, 2.5, keep_zeros=True)
+    cfg = L.kpm_cfg(32, R=16, seed=2, block=32)
+    ref = _run(ctx, 0, lambda: csr.kpm_dos(cfg))
+    got = _run(ctx, 5, lambda: csr.kpm_dos(cfg), rt_rows=16)
+    assert _rel(got, ref) < 2e-5
+    vec = np.random.default_rng(8).normal(size=(20, csr.n))
+    cfgh = L.kpm_cfg(48, R=20, kind=L.VEC_HOST, block=32)
+    ref = _run(ctx, 0, lambda: csr.kpm_dos(cfgh, vec))
+    got = _run(ctx, 5, lambda: csr.kpm_dos(cfgh, vec), rt_rows=16)
+    assert _rel(got, ref) < 2e-5
