@@ -220,7 +220,7 @@ def kernel_case(args):
     with L.Context(0) as ctx:
         if args.step_kernel >= 0:
             ctx.set_option("step_kernel", args.step_kernel)
-        for key in ("rt_stage", "rt_warps", "rt_depth"):
+        for key in ("rt_stage", "rt_warps", "rt_depth", "rt_group", "rt_chunk", "rt_rows"):
             if getattr(args, key) is not None:
                 ctx.set_option(key, getattr(args, key))
         csr = ctx.build_csr(ctx.prepare(geom(L, radius=radius)))
@@ -515,6 +515,11 @@ def run_cfg0(args):
                         "kernel": {0: "k_cheb_tile<double>", 1: "k_cheb_step<double>"}.get(kernel_id, str(kernel_id)),
                         "bytes_per_launch": bytes_step, "launch_ms": round(launch_ms, 4), "peak_kind": peak_kind,
                         "note": "working set in L2: the fraction of HBM is a bandwidth figure, not an HBM bound"},
+           # what bounds this workload: the FP64 FMAs (2 flops per entry and column)
+           # on GB300's small FP64 unit
+           "compute": {"bound": "fp64", "achieved_gflops": round(2.0 * nnz * cols / (launch_ms / 1000.0) / 1e9, 1),
+                       "peak_gflops": 1250.0, "peak_kind": "nominal GB300 FP64 (no measured figure)",
+                       "frac": round(2.0 * nnz * cols / (launch_ms / 1000.0) / 1e9 / 1250.0, 4)},
            "clocks": clk.summary(),
            "cpu_baseline": {"value": round(t_cpu, 3), "unit": "s", "cores": min(threads, R), "kind": "port",
                             "sample": f"the whole workload: oracle FP64 recursion, {R} vectors x {Pc // 2} steps on "
@@ -734,8 +739,24 @@ def run_mlp(args):
     layer_macs = 64 * 256 + 3 * 256 * 256
     flops_step = 2 * B * layer_macs * 2 + 2 * B * 3 * 256 * 256  # forward, weight gradients, input gradients
     csr = ctx.build_csr(ctx.prepare(geom(L, radius=args.radius)))
-    mlp.site_sum(csr, TWIST_DEG)
-    t_inf, _ = _timed(stream, lambda: mlp.site_sum(csr, TWIST_DEG), args.steps, 1)
+    # the forward alone: the fused launch (default) and one GEMM per layer
+    # (mlp_fused = 0), each timed per launch on the library's stream; the
+    # whole call also computes the disregistry features of every orbital
+    fwd = {}
+    for fused in (0, 1):
+        ctx.set_option("mlp_fused", fused)
+        mlp.site_sum(csr, TWIST_DEG)
+        ctx.reset_stats()
+        ctx.set_profiling(True)
+        t_call, _ = _timed(stream, lambda: mlp.site_sum(csr, TWIST_DEG), args.steps, 1)
+        names = ("mlp_fused", "mlp_fused_sums") if fused else ("tc_gemm", "mlp_sum")
+        ms = 0.0
+        for nm in names:
+            k_n, k_ms = ctx.kernel_stats(nm)
+            ms += k_ms / max(args.steps, 1)
+        ctx.set_profiling(False)
+        fwd[fused] = (t_call, ms / 1000.0)
+    t_inf, t_fwd = fwd[1]
     flops_inf = 2 * csr.n * layer_macs
     peak = 1900.0
     try:
@@ -747,10 +768,14 @@ def run_mlp(args):
            "value": round(t_inf, 6), "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": 1,
            "higher_is_better": False, "dtype": "bf16 (fp32 accumulation)", "data": "synthetic",
            "config": {"workload": f"site sums over {csr.n} orbitals; training batch {B}", "orbitals": csr.n},
+           "forward_s": round(t_fwd, 6), "forward_tflops": round(flops_inf / t_fwd / 1e12, 1),
+           "layered_call_s": round(fwd[0][0], 6), "layered_forward_s": round(fwd[0][1], 6),
+           "layered_forward_tflops": round(flops_inf / fwd[0][1] / 1e12, 1),
            "inference_tflops": round(flops_inf / t_inf / 1e12, 1),
            "train_step_ms": round(t_step * 1000, 4), "train_tflops": round(flops_step / t_step / 1e12, 1),
-           "roofline": {"bound": "tensor", "achieved": round(flops_inf / t_inf / 1e12, 1), "peak": peak,
-                        "unit": "TFLOP/s", "frac": round(flops_inf / t_inf / 1e12 / peak, 4),
+           "roofline": {"bound": "tensor", "achieved": round(flops_inf / t_fwd / 1e12, 1), "peak": peak,
+                        "unit": "TFLOP/s", "frac": round(flops_inf / t_fwd / 1e12 / peak, 4),
+                        "kernel": "k_mlp_fused (+ k_mlp_fused_sums)", "launch_ms": round(t_fwd * 1000, 4),
                         "peak_kind": "measured (cuBLAS bf16 burst)"}}
     print(json.dumps(out))
     mlp.close()
@@ -884,6 +909,11 @@ def main():
                          "or shared memory by TMA row gathers (2)")
     ap.add_argument("--rt-warps", type=int, default=None, help="8-row tensor-core step: warps per CTA")
     ap.add_argument("--rt-depth", type=int, default=None, help="8-row tensor-core step: k-steps in flight")
+    ap.add_argument("--rt-group", type=int, default=None, help="tensor-core row-block step: blocks per warp run")
+    ap.add_argument("--rt-chunk", type=int, default=None,
+                    help="tensor-core row-block step: tiles per CTA between grid-wide jumps")
+    ap.add_argument("--rt-rows", type=int, default=None, choices=[8, 16],
+                    help="tensor-core row-block step: rows per block")
     ap.add_argument("--kernel-case", type=int, default=0, metavar="COLS",
                     help="profiling case: two short DOS runs (P=16) of COLS-wide vector blocks on the flake "
                          "of --radius (1000 A: 2.4M orbitals), then exit; prints no bench line")
@@ -917,7 +947,7 @@ def main():
     ctx = L.Context(local)
     if args.step_kernel >= 0:
         ctx.set_option("step_kernel", args.step_kernel)
-    for key in ("rt_stage", "rt_warps", "rt_depth"):
+    for key in ("rt_stage", "rt_warps", "rt_depth", "rt_group", "rt_chunk", "rt_rows"):
         if getattr(args, key) is not None:
             ctx.set_option(key, getattr(args, key))
     g = ctx.prepare(geom(L, radius=args.radius))

@@ -131,6 +131,7 @@ struct leo2d_ctx {
   size_t alloc_cap = 0;       // largest single device allocation of a call, bytes (0: no limit)
   int kubo_velocity = -1;     // Kubo trace: -1 D built in the row-block step where possible, 0 stored dxH
   int64_t kubo_chunk = 0;     // Kubo trace: B-side moments held at once (0: as many as memory allows)
+  int mlp_fused = 1;          // network forward over many sites: 1 one fused launch, 0 one GEMM per layer
   leo2d::DevBuf<int> status;  // one int, reset before kernels that may set it
 };
 

@@ -321,6 +321,9 @@ leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value
     } else if (k == "alloc_cap_mb") {
       LEO_REQUIRE(value >= 0, "alloc_cap_mb must be >= 0 (0: no limit)");
       ctx->alloc_cap = (size_t)value << 20;
+    } else if (k == "mlp_fused") {
+      LEO_REQUIRE(value == 0 || value == 1, "mlp_fused must be 0 (one GEMM per layer) or 1 (one fused launch)");
+      ctx->mlp_fused = (int)value;
     } else if (k == "reorder_curve") {
       LEO_REQUIRE(value == 0 || value == 1, "reorder_curve must be 0 or 1");
       ctx->reorder_curve = (int)value;

@@ -420,10 +420,20 @@ void upload_x(leo2d_mlp* M, const float* x, int64_t n, int F) {
   ctx_sync(ctx);
 }
 
-// Forward of `n` rows whose BF16 features sit in X (row-major [n][64]) in
-// chunks of kChunk rows: either Y [n][256] FP32, or the column sums (FP64).
+// Forward of `n` rows whose BF16 features sit in X (row-major [n][64]): either
+// Y [n][256] FP32, or the column sums (FP64). By default one fused launch keeps
+// every activation on chip (mlp_fused.cu); option mlp_fused = 0 runs one GEMM
+// per layer over chunks of kChunk rows, with the activations in HBM.
 void infer_rows(leo2d_mlp* M, const __nv_bfloat16* X, int64_t n, float* Y, double* sums_dev) {
   leo2d_ctx* ctx = M->ctx;
+  if (ctx->mlp_fused) {
+    CUtensorMap tx;
+    make_tmap_bf16(&tx, X, n, kIn, kGemmBM);
+    const float* bias[kLayers];
+    for (int l = 0; l < kLayers; ++l) bias[l] = M->p.p + M->b_off[l];
+    mlp_forward_fused(ctx, tx, M->tWt, bias, n, Y, sums_dev);
+    return;
+  }
   const int64_t chunk = std::min<int64_t>(kChunk, n);
   DevBuf<__nv_bfloat16> h0((size_t)chunk * kHid), h1((size_t)chunk * kHid);
   const int grid = tc_gemm_grid(ctx, (int)chunk, kOut);

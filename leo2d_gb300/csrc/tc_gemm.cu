@@ -14,10 +14,8 @@ constexpr int BM = kGemmBM, BK = kGemmBK, ST = kGemmStages, BN = 256;
 constexpr uint32_t kABytes = BM * BK * 2, kBBytes = BN * BK * 2, kStage = kABytes + kBBytes;
 constexpr uint32_t kIdesc = umma::idesc_bf16(BM, BN);
 
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
-__device__ __forceinline__ float gelu_grad(float z) {
-  return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * expf(-0.5f * z * z) * 0.39894228040143268f;
-}
+__device__ __forceinline__ float gelu(float z) { return mlp_gelu(z); }
+__device__ __forceinline__ float gelu_grad(float z) { return mlp_gelu_grad(z); }
 
 template <int EPI>
 __global__ void __launch_bounds__(256, 1)

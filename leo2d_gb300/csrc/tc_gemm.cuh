@@ -82,4 +82,100 @@ void tc_gemm_prepare(leo2d_ctx* ctx);
 void tc_gemm(leo2d_ctx* ctx, GemmEpi epi, const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g,
              int grid_cap = 0);
 
+// The activation of the control variate's network: GELU(z) = z Phi(z) =
+// z (1 + erf(z / sqrt 2)) / 2, with erf from Abramowitz & Stegun, Handbook of
+// Mathematical Functions (1964), formula 7.1.28: for x >= 0
+//   erf(x) = 1 - (1 + a1 x + a2 x^2 + ... + a6 x^6)^-16,  |error| <= 3e-7,
+// extended as an odd function. One reciprocal (rcp.approx) and no exponential:
+// the fused forward evaluates 3 x 256 of these per site, and this form keeps the
+// special-function unit at one operation per activation. Every product and sum
+// is an explicitly rounded operation, so the packed two-lane form
+// (mlp_gelu2, fma.rn.f32x2) and this scalar form agree bit for bit; in FP32 the
+// result is within about 1e-5 of GELU (the 16th power amplifies rounding).
+namespace mlp_act {
+constexpr float kA1 = 0.0705230784f, kA2 = 0.0422820123f, kA3 = 0.0092705272f;
+constexpr float kA4 = 0.0001520143f, kA5 = 0.0002765672f, kA6 = 0.0000430638f;
+constexpr float kRsqrt2 = 0.70710678118654752f;
+}  // namespace mlp_act
+
+__device__ __forceinline__ float mlp_rcp(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+// erf(x) for x >= 0 (A&S 7.1.28)
+__device__ __forceinline__ float mlp_erf_pos(float x) {
+  using namespace mlp_act;
+  float p = __fmaf_rn(kA6, x, kA5);
+  p = __fmaf_rn(p, x, kA4);
+  p = __fmaf_rn(p, x, kA3);
+  p = __fmaf_rn(p, x, kA2);
+  p = __fmaf_rn(p, x, kA1);
+  p = __fmaf_rn(p, x, 1.0f);
+  p = __fmul_rn(p, p);
+  p = __fmul_rn(p, p);
+  p = __fmul_rn(p, p);
+  p = __fmul_rn(p, p);
+  return __fsub_rn(1.0f, mlp_rcp(p));
+}
+__device__ __forceinline__ float mlp_gelu(float z) {
+  const float e = copysignf(mlp_erf_pos(__fmul_rn(fabsf(z), mlp_act::kRsqrt2)), z);
+  const float hz = __fmul_rn(0.5f, z);
+  return __fmaf_rn(hz, e, hz);
+}
+// d GELU / dz = Phi(z) + z phi(z), Phi from the same erf
+__device__ __forceinline__ float mlp_gelu_grad(float z) {
+  const float e = copysignf(mlp_erf_pos(__fmul_rn(fabsf(z), mlp_act::kRsqrt2)), z);
+  return 0.5f * (1.0f + e) + z * expf(-0.5f * z * z) * 0.39894228040143268f;
+}
+
+// GELU of two values at once (fma.rn.f32x2 / mul.rn.f32x2: the same roundings
+// as mlp_gelu on each lane).
+__device__ __forceinline__ void mlp_gelu2(float& a, float& b) {
+  using namespace mlp_act;
+  auto pk = [](float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+  };
+  auto mul2 = [](unsigned long long x, unsigned long long y) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(x), "l"(y));
+    return r;
+  };
+  auto fma2 = [](unsigned long long x, unsigned long long y, unsigned long long c) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(x), "l"(y), "l"(c));
+    return r;
+  };
+  const unsigned long long x = mul2(pk(fabsf(a), fabsf(b)), pk(kRsqrt2, kRsqrt2));
+  unsigned long long p = fma2(pk(kA6, kA6), x, pk(kA5, kA5));
+  p = fma2(p, x, pk(kA4, kA4));
+  p = fma2(p, x, pk(kA3, kA3));
+  p = fma2(p, x, pk(kA2, kA2));
+  p = fma2(p, x, pk(kA1, kA1));
+  p = fma2(p, x, pk(1.0f, 1.0f));
+  p = mul2(p, p);
+  p = mul2(p, p);
+  p = mul2(p, p);
+  p = mul2(p, p);
+  float p0, p1;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(p0), "=f"(p1) : "l"(p));
+  const float e0 = copysignf(__fsub_rn(1.0f, mlp_rcp(p0)), a);
+  const float e1 = copysignf(__fsub_rn(1.0f, mlp_rcp(p1)), b);
+  const unsigned long long hz = mul2(pk(a, b), pk(0.5f, 0.5f));
+  const unsigned long long g = fma2(hz, pk(e0, e1), hz);
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(g));
+}
+
+// Forward of the control variate's network (64 -> 256 -> 256 -> 256 -> 256,
+// GELU on the hidden layers) over n rows in one persistent launch with every
+// activation kept on chip (mlp_fused.cu). tx: TMA map of the BF16 features
+// [n][64] (boxes of 64 columns x 128 rows, 128-byte swizzle); tw[l]: TMA maps of
+// the BF16 weights W_l [256][in_l] (boxes of 64 x 256); bias[l]: FP32 [256].
+// Writes Y (FP32 [n][256]) or, with Y null, sums_dev[256] = the FP64 column
+// sums of the outputs over the n rows (overwritten). n < 2^31.
+void mlp_forward_fused(leo2d_ctx* ctx, const CUtensorMap& tx, const CUtensorMap* tw, const float* const* bias,
+                       int64_t n, float* Y, double* sums_dev);
+
 }  // namespace leo2d

@@ -6,8 +6,10 @@ W2, b2, W3, b3 as one FP32 vector) in float64. With exact=False it applies
 BF16 rounding (round to nearest even) where the GPU stores BF16: the input
 features, the weights, the activations, the loss gradient and the
 back-propagated gradients. The remaining differences to the GPU are then FP32
-accumulation order and rare rounding-boundary cases. With exact=True no rounding
-is applied (for finite-difference checks of this oracle).
+accumulation order, rare rounding-boundary cases and the GPU's erf (Abramowitz &
+Stegun 7.1.28 in FP32, within about 1e-5 of erf; this oracle uses the exact
+erf). With exact=True no rounding is applied (for finite-difference checks of
+this oracle).
 
 The network has no counterpart in the reference (LEO2D has no learned part);
 the site features follow Hstruct::getShiftConfigs (hstruct.cpp:672-820).
@@ -113,3 +115,22 @@ def loss_and_grad(p, x, t, w=None, exact=False):
             dZf = (dZb @ Wr[l]) * gelu_grad(Zs[l - 1])
             dZb = r(dZf)
     return loss, pack(gW, gb)
+
+
+def erf_as7128(x, dtype=np.float64):
+    """erf by Abramowitz & Stegun 7.1.28 (odd extension), the form the GPU
+    network evaluates; dtype=np.float32 rounds every operation to FP32 in the
+    GPU's order (the GPU's reciprocal is rcp.approx, within an ulp of this)."""
+    a = [0.0705230784, 0.0422820123, 0.0092705272, 0.0001520143, 0.0002765672, 0.0000430638]
+    t = dtype
+    z = np.asarray(x, t)
+    ax = np.abs(z)
+    p = t(a[5]) * ax + t(a[4])
+    for c in (a[3], a[2], a[1], a[0], 1.0):
+        p = (p * ax + t(c)).astype(t)
+    with np.errstate(over="ignore"):
+        for _ in range(4):
+            p = (p * p).astype(t)
+        e = (t(1.0) - (t(1.0) / p).astype(t)).astype(t)
+    return np.copysign(e, z)
+

@@ -137,3 +137,44 @@ def test_bad_batch_is_rejected(ctx):
     with pytest.raises(L.Leo2dError, match="multiple of 64"):
         m.grad(np.zeros((100, 16), np.float32), np.zeros((100, 256), np.float32))
     m.close()
+
+
+@pytest.mark.parametrize("n", [1, 127, 129, 1000, 40_000, 100_003])
+def test_fused_forward_matches_layered(n):
+    """The fused forward (one persistent launch, activations on chip) against
+    one GEMM per layer: same BF16 roundings and K order, so the outputs agree to
+    FP32 accumulation order (1e-5 of the largest output). The sizes cover a
+    single partial tile, a padding tile of the last pair, and several tile
+    pairs per CTA."""
+    rng = np.random.default_rng(n)
+    x = rng.uniform(-1, 1, (n, mo.N_FEAT)).astype(np.float32)
+    with L.Context(0) as c:
+        m = L.Mlp(c, seed=6)
+        c.set_option("mlp_fused", 1)
+        y_fused = m.predict(x)
+        c.set_option("mlp_fused", 0)
+        y_layer = m.predict(x)
+        m.close()
+    scale = np.max(np.abs(y_layer))
+    assert np.max(np.abs(y_fused - y_layer)) <= 1e-5 * scale
+
+
+def test_fused_site_sum_matches_layered():
+    """Site sums of the fused forward (warp transpose-reduce of the outputs, FP64
+    per-lane partials) against the layer-by-layer sums over the same flake."""
+    twist = 1.1
+    with L.Context(0) as c:
+        g = L.make_geom(model=L.MODEL_SIMPLE, size=160, angles_deg=(0.0, twist), energy_rescale=1.0)
+        csr = c.build_csr(c.prepare(g))
+        assert csr.n > 2 * 152 * 128  # several tile pairs per CTA
+        m = L.Mlp(c, seed=8)
+        c.set_option("mlp_fused", 1)
+        s_fused = m.site_sum(csr, twist)
+        c.set_option("mlp_fused", 0)
+        s_layer = m.site_sum(csr, twist)
+        c.set_option("mlp_fused", 1)
+        y = m.predict(csr.site_features(twist)).astype(np.float64)
+        m.close()
+    tol = 1e-6 * np.abs(y).sum(axis=0).max()
+    np.testing.assert_allclose(s_fused, s_layer, rtol=1e-6, atol=tol)
+    np.testing.assert_allclose(s_fused, y.sum(axis=0), rtol=1e-6, atol=tol)

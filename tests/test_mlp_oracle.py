@@ -39,3 +39,17 @@ def test_bf16_rounding():
     # 1 + 2^-8 is a tie between 1 and 1 + 2^-7: ties go to even (1.0)
     assert r[0] == 1.0 and r[1] == 1.0 and r[2] == 1.0078125
     assert np.all(np.abs(r[:4] - x[:4]) <= np.abs(x[:4]) * 2.0 ** -8)
+
+
+def test_erf_form_of_the_gpu_network():
+    """The network's erf (Abramowitz & Stegun 7.1.28) against the exact erf: the
+    published bound 3e-7 in float64; within 1e-5 with every operation rounded to
+    FP32 in the GPU's order (the 16th power amplifies the polynomial's rounding)."""
+    from scipy.special import erf
+    x = np.linspace(-6.0, 6.0, 200_001)
+    assert np.max(np.abs(mo.erf_as7128(x) - erf(x))) <= 3e-7
+    e32 = mo.erf_as7128(x.astype(np.float32), np.float32).astype(np.float64)
+    assert np.max(np.abs(e32 - erf(x.astype(np.float32).astype(np.float64)))) <= 1e-5
+    # saturation: the polynomial's 16th power overflows to inf and erf to +-1 exactly
+    assert mo.erf_as7128(np.float32(40.0), np.float32) == 1.0
+    assert mo.erf_as7128(np.float32(-40.0), np.float32) == -1.0
