@@ -25,6 +25,10 @@ struct leo2d_csr {
   leo2d::DevBuf<uint2> entd;      // nnz, (column, FP32 dxH bits)
   leo2d::DevBuf<double> dx64, dy64;
   bool complex_h = false;         // Peierls phases: entries have imaginary parts
+  // a field on a periodic supercell: the reference's Peierls phase on the
+  // images (x1 shifted by the image, locality.cpp:4718-4738, 7157-7161) breaks
+  // Hermiticity, so the moments below P/2 are taken directly (see run_trace)
+  bool nonhermitian = false;
   leo2d::DevBuf<double> val_im64; // nnz, FP64 imaginary parts (complex_h)
   leo2d::DevBuf<float> val_im32;  // nnz, FP32 copy
   leo2d::DevBuf<float> dx32;

@@ -724,8 +724,12 @@ __global__ void __launch_bounds__(256) k_periodic_rows(const __grid_constant__ G
           const double t = periodic_value(G, row, grid4, spos, inter, k2, img, x1, y1);
           if (t != 0) {
             if (G.cpx) {
-              // std::polar(t, k.(r2 - r1)) summed over the images (locality.cpp:4896-4941)
-              const double ph = G.kx * (spos[3 * k2] - x1) + G.ky * (spos[3 * k2 + 1] - y1);
+              // std::polar(t, phase) summed over the images, the phase the Peierls
+              // phase plus k.(r2 - r1) with r1 the row's orbital shifted by the
+              // image (locality.cpp:4718-4738, 4896-4941)
+              const double x2 = spos[3 * k2], y2 = spos[3 * k2 + 1];
+              double ph = peierls_phase(x1, x2, y1, y2, G.b_field);
+              ph = ph + G.kx * (x2 - x1) + G.ky * (y2 - y1);
               double sn, cs;
               sincos(ph, &sn, &cs);
               v += t * cs;
@@ -891,8 +895,6 @@ void validate_geom(const leo2d_geom* g) {
     LEO_REQUIRE(std::isfinite(g->shifts[s][0]) && std::isfinite(g->shifts[s][1]) &&
                     std::fabs(g->shifts[s][0]) <= 1.0 && std::fabs(g->shifts[s][1]) <= 1.0,
                 "sheet shifts must be finite fractions of the lattice vectors (|shift| <= 1)");
-  LEO_REQUIRE(g->b_field == 0.0 || g->boundary_condition == 0,
-              "a magnetic field is supported for flakes (BOUNDARY_CONDITION = 0)");
 }
 
 }  // namespace
@@ -1155,6 +1157,7 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     csr->n_inter = reduce_sum_i64(ctx, cnt_inter.p, n);
     csr_alloc_entries(ctx, csr, nnz, G.with_dx != 0);
     csr->complex_h = G.cpx != 0;
+    csr->nonhermitian = csr->complex_h && G.bc == 1 && G.b_field != 0.0;
     if (csr->complex_h) {
       csr->val_im64.alloc(nnz + kCsrPad);
       LEO_CUDA(cudaMemsetAsync(csr->val_im64.p, 0, (nnz + kCsrPad) * sizeof(double), ctx->stream));

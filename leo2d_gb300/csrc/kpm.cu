@@ -179,11 +179,35 @@ int occupancy(int cols, bool fp64) {
   return 1;
 }
 
+// out[c] = sum_i x[i][c] y[i][c] in FP64, one block per column, fixed order.
+__global__ void __launch_bounds__(256) k_col_dots(int64_t n, int C, const float* __restrict__ x,
+                                                  const float* __restrict__ y, double* __restrict__ out) {
+  __shared__ double red[256];
+  const int c = blockIdx.x;
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += (double)x[i * C + c] * (double)y[i * C + c];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[c] = red[0];
+}
+
 template <typename T>
 void enqueue_steps(Recursion& r) {
   leo2d_ctx* ctx = r.ctx;
   const int C = r.shape.cols;
   for (int k = 0; k < r.steps; ++k) {
+    if constexpr (std::is_same<T, float>::value) {
+      if (r.direct) {
+        const float* tk = reinterpret_cast<const float*>(r.buf(k % 2));
+        launch(ctx, "direct_dots", [&] {
+          k_col_dots<<<C, 256, 0, ctx->stream>>>(r.n, C, tk, r.start, r.direct + (size_t)k * C);
+        });
+      }
+    }
     StepArgs<T> a;
     a.n = r.n;
     a.ent = r.use_perm ? r.csr->pent.p : r.csr->ent.p;  // (Recursion::step selects dxH itself)
@@ -505,7 +529,7 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
   else if (ctx->kernel_variant == -1) s.rb = rb_ok && (cached ? it->second.rb : (ctx->reorder == 1 || csr->n >= 100000));
   const bool rt_ok = rb_ok && !csr->complex_h;
   if (ctx->kernel_variant == 5) s.rt = rt_ok;
-  else if (ctx->kernel_variant == -1) s.rt = rt_ok && cached && it->second.rt;
+  else if (ctx->kernel_variant == -1) s.rt = rt_ok && (cached ? it->second.rt : s.rb);
   if (s.rt) s.rb = false;
   if (s.rb || s.rt) s.tc = false;
   if (csr->complex_h) {
@@ -591,6 +615,26 @@ void fill_unit(leo2d_ctx* ctx, Recursion& r, const int64_t* targets, int n_t) {
   LEO_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
+// The moments of a non-Hermitian H~ in the reference's order (the complex
+// branches of computeDosKPM and computeDosTraceKPM, locality.cpp:6074-6120,
+// 6276-6330): mu_j = Re sum_i T_j[i] v[i]
+// directly for j < P/2 (complex pairs: re*re - im*im), then for j >= P/4
+// mu_2j = 2 <T_j|T_j> - mu_0 and mu_2j+1 = 2 Re <T_j+1|T_j> - mu_1.
+void direct_to_moments(const std::vector<double>& direct, const std::vector<double>& dots, int cols, int steps,
+                       int n_vec, double* mu_out, int P) {
+  for (int v = 0; v < n_vec; ++v) {
+    double* mu = mu_out + (size_t)v * P;
+    const int cr = 2 * v, ci = 2 * v + 1;
+    for (int k = 0; k < steps; ++k) mu[k] = direct[(size_t)k * cols + cr] - direct[(size_t)k * cols + ci];
+    for (int k = P / 4; k < steps; ++k) {
+      const double D0 = dots[((size_t)k * cols + cr) * 2] + dots[((size_t)k * cols + ci) * 2];
+      const double D1 = dots[((size_t)k * cols + cr) * 2 + 1] + dots[((size_t)k * cols + ci) * 2 + 1];
+      mu[2 * k] = 2 * D0 - mu[0];
+      mu[2 * k + 1] = 2 * D1 - mu[1];
+    }
+  }
+}
+
 void dots_to_moments(const std::vector<double>& dots, int cols, int steps, int group, int n_vec,
                      double* mu_out, int P) {
   for (int v = 0; v < n_vec; ++v) {
@@ -627,6 +671,35 @@ void validate_cfg(const leo2d_kpm_cfg* cfg) {
   LEO_REQUIRE(cfg->block >= 0 && cfg->rows_per_warp >= 0, "block and rows_per_warp must be >= 0");
 }
 
+// For a non-Hermitian H~ (a field on a periodic supercell): keeps a copy of
+// each block's start vectors and has the recursion record the direct dots.
+struct DirectMoments {
+  leo2d_ctx* ctx;
+  Recursion& r;
+  DevBuf<float> start;
+  DevBuf<double> direct;
+  DirectMoments(leo2d_ctx* c, const leo2d_csr* csr, Recursion& rr) : ctx(c), r(rr) {
+    if (!csr->nonhermitian) return;
+    LEO_REQUIRE(!r.shape.fp64, "a complex Hamiltonian runs in FP32");
+    start.alloc((size_t)r.n * r.shape.cols);
+    direct.alloc((size_t)r.steps * r.shape.cols);
+    r.start = start.p;
+    r.direct = direct.p;
+  }
+  bool on() const { return start.p != nullptr; }
+  void keep_start() {
+    if (on())
+      LEO_CUDA(cudaMemcpyAsync(start.p, r.x0.p, (size_t)r.n * r.shape.cols * sizeof(float),
+                               cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  void moments(const std::vector<double>& dots, int nv, double* mu, int P) {
+    std::vector<double> d((size_t)r.steps * r.shape.cols);
+    d2h(ctx, d.data(), direct.p, d.size());
+    ctx_sync(ctx);
+    direct_to_moments(d, dots, r.shape.cols, r.steps, nv, mu, P);
+  }
+};
+
 // Runs the recursion over the vector blocks of a trace estimate and writes moments.
 void run_trace(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg, const double* host_vectors,
                double* mu_out) {
@@ -642,6 +715,7 @@ void run_trace(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg, c
   Recursion r;
   r.setup(ctx, csr, shape, steps);
   std::vector<double> dots((size_t)steps * 2 * shape.cols);
+  DirectMoments dm(ctx, csr, r);
   for (int v0 = 0; v0 < cfg->num_vectors; v0 += vec_per_block) {
     const int nv = std::min(vec_per_block, cfg->num_vectors - v0);
     switch (cfg->vector_kind) {
@@ -650,10 +724,12 @@ void run_trace(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* cfg, c
       case LEO2D_VEC_HOST: fill_host(ctx, r, host_vectors, v0, nv); break;
       default: fail(LEO2D_ERR_BAD_ARG, "unknown vector_kind");
     }
+    dm.keep_start();
     r.run();
     d2h(ctx, dots.data(), r.dots.p, dots.size());
     ctx_sync(ctx);
-    dots_to_moments(dots, shape.cols, steps, group, nv, mu_out + (size_t)v0 * P, P);
+    if (dm.on()) dm.moments(dots, nv, mu_out + (size_t)v0 * P, P);
+    else dots_to_moments(dots, shape.cols, steps, group, nv, mu_out + (size_t)v0 * P, P);
   }
   for (size_t i = 0; i < (size_t)cfg->num_vectors * P; ++i)
     if (!std::isfinite(mu_out[i])) fail(LEO2D_ERR_NONFINITE, "non-finite moment (check the spectral bounds)");
@@ -692,14 +768,17 @@ leo2d_status leo2d_kpm_ldos(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kp
     Recursion r;
     r.setup(ctx, csr, shape, steps);
     std::vector<double> dots((size_t)steps * 2 * shape.cols);
+    DirectMoments dm(ctx, csr, r);
     const int per_block = shape.cols / group;
     for (int64_t t0 = 0; t0 < num_targets; t0 += per_block) {
       const int nt = (int)std::min<int64_t>(per_block, num_targets - t0);
       fill_unit(ctx, r, targets + t0, nt);
+      dm.keep_start();
       r.run();
       d2h(ctx, dots.data(), r.dots.p, dots.size());
       ctx_sync(ctx);
-      dots_to_moments(dots, shape.cols, steps, group, nt, mu_out + (size_t)t0 * P, P);
+      if (dm.on()) dm.moments(dots, nt, mu_out + (size_t)t0 * P, P);
+      else dots_to_moments(dots, shape.cols, steps, group, nt, mu_out + (size_t)t0 * P, P);
     }
   });
 }

@@ -46,6 +46,10 @@ struct Recursion {
   int graph_steps = -1;
   bool use_perm = false;  // stream the locality-ordered copy of the matrix
   bool allow_perm = true; // set false before setup() to keep the reference row order
+  // the direct moments of a non-Hermitian H~: before step k, direct[k][c] =
+  // sum_i T_k[i][c] start[i][c] (FP64), start = a copy of T_0 (FP32 only)
+  const float* start = nullptr;
+  double* direct = nullptr;
   const int32_t* perm() const { return use_perm ? csr->new2old.p : nullptr; }
   // complex H: vector v occupies columns 2v (real part) and 2v + 1 (imaginary part)
   int pairs() const { return csr->complex_h ? 1 : 0; }

@@ -9,24 +9,25 @@
 // sites in pairs (two slots), so the tensor core works on one slot while the
 // epilogue warps turn the other slot's accumulator into the next layer's
 // operand:
-//   warp 8 lane 0   TMA producer: the slot's feature tile [128][64] into the
+//   warp 16 lane 0  TMA producer: the slot's feature tile [128][64] into the
 //                   slot's activation buffer, then the weight panels of each
 //                   layer (64 K-columns x 256 rows, 32 KB) through a 3-stage ring
 //                   (the weights stay L2-resident: 416 KB for the network);
-//   warp 9 lane 0   MMA issuer: per (slot, layer) tcgen05.mma M = 128, N = 256,
+//   warp 17 lane 0  MMA issuer: per (slot, layer) tcgen05.mma M = 128, N = 256,
 //                   K = 16 over the layer's K into the slot's 256-column TMEM
 //                   accumulator (two slots: all 512 columns); tcgen05.commit
 //                   frees weight stages, hands the accumulator to the epilogue
 //                   and, after the last layer, frees the activation buffer;
-//   warps 0..7      epilogue: warp w reads TMEM lanes 32 (w & 3) .. + 31 (one
-//                   site each), columns 128 (w >> 2) .. + 127, in chunks of 32
+//   warps 0..15     epilogue: warp w reads TMEM lanes 32 (w & 3) .. + 31 (one
+//                   site each), columns 64 (w >> 2) .. + 63, in chunks of 32
 //                   (tcgen05.ld.32x32b.x32). Hidden layers: + bias, GELU, BF16,
 //                   stored into the slot's activation buffer in the K-major
 //                   128-byte-swizzled layout the next MMA reads (the layout TMA
 //                   writes). Last layer: + bias, then either the FP32 outputs
 //                   to HBM or, for the site sum, a warp transpose-reduce of
 //                   each 32 x 32 chunk (lane j ends with column j's sum over
-//                   the warp's sites) added into FP64 per-lane partials.
+//                   the warp's sites) added into per-lane partials (FP32 over
+//                   8 tile pairs, then FP64).
 // Order of work: (slot 0, layer 0), (slot 1, layer 0), (slot 0, layer 1), ...
 // for each pair of tiles; the MMA and the epilogue both walk it, so the MMA
 // of (slot s, layer l) waits only for the epilogue of (s, l - 1).
@@ -52,7 +53,10 @@ constexpr int kWStages = 3;
 constexpr uint32_t kAKBlock = kRows * kKB * 2;             // 16 KB: one K block of an activation tile
 constexpr uint32_t kABytes = kAKBlock * (kWidth / kKB);     // 64 KB: a 128 x 256 BF16 activation tile
 constexpr uint32_t kWBytes = kWidth * kKB * 2;              // 32 KB: one weight panel
-constexpr int kEpiWarps = 8, kProducerWarp = 8, kMmaWarp = 9, kThreads = 320;
+// 16 epilogue warps (four per TMEM lane quarter, 64 columns each): with 8 the
+// epilogue issued at 57 % with two warps per scheduler and bounded the launch
+constexpr int kEpiWarps = 16, kProducerWarp = 16, kMmaWarp = 17, kThreads = 32 * (kEpiWarps + 2);
+constexpr int kEpiCols = kWidth / (kEpiWarps / 4);  // columns of one epilogue warp
 constexpr uint32_t kIdesc = umma::idesc_bf16(kRows, kWidth);
 constexpr size_t kSmemBytes = 2 * (size_t)kABytes + kWStages * (size_t)kWBytes + 1024;
 
@@ -90,6 +94,16 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
   const __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);  // lo at the lower address
   return *reinterpret_cast<const uint32_t*>(&p);
+}
+
+// (a, b) += (x, y) with one add.rn.f32x2 (the roundings of two FADDs)
+__device__ __forceinline__ void add2(float& a, float& b, float x, float y) {
+  unsigned long long r;
+  asm("{\n\t.reg .b64 u, w;\n\tmov.b64 u, {%1, %2};\n\tmov.b64 w, {%3, %4};\n\t"
+      "add.rn.f32x2 %0, u, w;\n\t}"
+      : "=l"(r)
+      : "f"(a), "f"(b), "f"(x), "f"(y));
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
 }
 
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
@@ -236,10 +250,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_fused(const __grid_constant
       if (!umma::bar_wait(&drain, 0u)) give_up();
     }
   } else {
-    // epilogue: site r = 32 q + lane of the tile, columns 128 h .. 128 h + 127
+    // epilogue: site r = 32 q + lane of the tile, columns kEpiCols h .. + kEpiCols - 1
     const int q = warp & 3, h = warp >> 2, r = q * 32 + lane;
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-    double csum[4] = {0.0, 0.0, 0.0, 0.0};
+    // site sums: FP32 over 8 tile pairs, then FP64 (the FP64 pipe is narrow)
+    double csum[kEpiCols / 32];
+    float fsum[kEpiCols / 32];
+#pragma unroll
+    for (int ci = 0; ci < kEpiCols / 32; ++ci) {
+      csum[ci] = 0.0;
+      fsum[ci] = 0.f;
+    }
     // byte offset of K column k (multiple of 8) of this site in an activation buffer
     auto a_off = [&](int k) -> uint32_t {
       return (uint32_t)(k >> 6) * kAKBlock + (uint32_t)(r >> 3) * 1024u + (uint32_t)(r & 7) * 128u +
@@ -261,18 +282,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_fused(const __grid_constant
           const uint32_t tacc = tmem + (uint32_t)(s * kWidth) + lane_off;
           const float* bl = a.bias[l];
           const uint32_t ab = umma::saddr(abuf + s * kABytes);
-#pragma unroll 1
-          for (int ci = 0; ci < 4; ++ci) {
-            const int c0 = h * 128 + ci * 32;
+#pragma unroll
+          for (int ci = 0; ci < kEpiCols / 32; ++ci) {
+            const int c0 = h * kEpiCols + ci * 32;
             float v[32];
             tmem_ld32(tacc + (uint32_t)c0, v);
 #pragma unroll
             for (int i = 0; i < 32; i += 4) {
               const float4 b = __ldg(reinterpret_cast<const float4*>(bl + c0 + i));
-              v[i] += b.x;
-              v[i + 1] += b.y;
-              v[i + 2] += b.z;
-              v[i + 3] += b.w;
+              add2(v[i], v[i + 1], b.x, b.y);
+              add2(v[i + 2], v[i + 3], b.z, b.w);
             }
             if (l < 3) {
               uint32_t pk[16];
@@ -294,7 +313,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_fused(const __grid_constant
               if (!valid)
 #pragma unroll
                 for (int i = 0; i < 32; ++i) v[i] = 0.f;
-              csum[ci] += (double)warp_transpose_sum(v, lane);
+              fsum[ci] += warp_transpose_sum(v, lane);
             }
           }
           umma::fence_before_sync();
@@ -306,10 +325,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_fused(const __grid_constant
         give_up();
         break;
       }
+      if ((it & 7) == 7) {
+#pragma unroll
+        for (int ci = 0; ci < kEpiCols / 32; ++ci) {
+          csum[ci] += (double)fsum[ci];
+          fsum[ci] = 0.f;
+        }
+      }
     }
     if (!a.y) {
 #pragma unroll
-      for (int ci = 0; ci < 4; ++ci) a.part[((size_t)bid * 4 + q) * kWidth + h * 128 + ci * 32 + lane] = csum[ci];
+      for (int ci = 0; ci < kEpiCols / 32; ++ci)
+        a.part[((size_t)bid * 4 + q) * kWidth + h * kEpiCols + ci * 32 + lane] = csum[ci] + (double)fsum[ci];
     }
   }
   umma::fence_before_sync();

@@ -629,10 +629,11 @@ __global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ R
 
 // ---------------------------------------------------------------- format build
 
-// One warp per block of R rows, at most kRtMaxEnt stored entries: the keys
-// (column << 16 | entry index) are sorted in the warp's slice of shared memory;
-// the distinct columns are the slots. Pass 0 writes the k-steps of each block;
-// pass 1 writes the block's k-steps at kstart[b] (data zero-filled before): the
+// One warp per block of R rows, at most kRtMaxEnt stored entries; the distinct
+// columns are the slots. Pass 0 counts them in a hash set in the warp's slice of
+// shared memory and writes the k-steps of each block; pass 1 sorts the keys
+// (column << 16 | entry index) in that slice and writes the block's k-steps at
+// kstart[b] (data zero-filled before): the
 // columns in the interleaved order, the values in fragment order (lane 4g + t
 // holds V[g][t], V[g][t+4] of each n-tile of 8 rows in turn), entries of one
 // (row, column) summed in entry order.
@@ -677,6 +678,36 @@ __global__ void __launch_bounds__(kRtBuildWarps * 32)
       continue;
     }
     __syncwarp();  // the previous block's keys are read
+    if (pass == 0) {
+      // counting needs the distinct columns only: a hash set in the warp's slice
+      // (2 kRtMaxEnt 32-bit slots, load <= 1/2), no sort (was half the build)
+      uint32_t* set = reinterpret_cast<uint32_t*>(keys);
+      constexpr int kSet = 2 * kRtMaxEnt;
+      for (int i = lane; i < kSet; i += 32) set[i] = 0xFFFFFFFFu;
+      __syncwarp();
+      int fresh = 0;
+      for (int i = lane; i < E; i += 32) {
+        const uint32_t c = (uint32_t)pcol[q0 + i];
+        uint32_t h = (c * 2654435761u) & (kSet - 1);
+        for (int probe = 0; probe < kSet; ++probe) {  // bounded: the set never fills
+          const uint32_t prev = atomicCAS(&set[h], 0xFFFFFFFFu, c);
+          if (prev == 0xFFFFFFFFu) {
+            ++fresh;
+            break;
+          }
+          if (prev == c) break;
+          h = (h + 1) & (kSet - 1);
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) fresh += __shfl_xor_sync(0xffffffffu, fresh, o);
+      if (lane == 0) {
+        kst[b] = max(1, (fresh + 7) / 8);
+        atomicAdd(ssum, (unsigned long long)fresh);
+        atomicMax(err + 1, fresh);
+      }
+      continue;
+    }
     int P2 = 32;
     while (P2 < E) P2 <<= 1;
     for (int i = lane; i < P2; i += 32)
@@ -714,14 +745,6 @@ __global__ void __launch_bounds__(kRtBuildWarps * 32)
     }
     const int K = __shfl_sync(0xffffffffu, incl, 31);
     const int KS = max(1, (K + 7) / 8);
-    if (pass == 0) {
-      if (lane == 0) {
-        kst[b] = KS;
-        atomicAdd(ssum, (unsigned long long)K);
-        atomicMax(err + 1, K);
-      }
-      continue;
-    }
     unsigned char* base = data + (size_t)kstart[b] * rt_step_bytes(R);
     auto col_at = [&](int s) {  // column entry of slot s
       const int jj = s & 7;

@@ -267,7 +267,6 @@ bool parse_input(const std::string& path, JobSpec& spec, std::string& err) {
   }
   if (spec.use_b == 1) {
     g.b_field = spec.b_field;
-    if (g.boundary_condition != 0) spec.unsupported.push_back("USE_B_FIELD = 1 with BOUNDARY_CONDITION = 1");
     if (spec.observable_type == 1) spec.unsupported.push_back("USE_B_FIELD = 1 with OBSERVABLE_TYPE = COND");
   }
   return true;

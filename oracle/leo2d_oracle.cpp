@@ -547,7 +547,8 @@ void oracle_bloch(const oracle_h* h, double kx, double ky, double* re, double* i
     }
     const double x1 = P[3 * ki] + shx, y1 = P[3 * ki + 1] + shy;
     const double x2 = P[3 * pr.j], y2 = P[3 * pr.j + 1];
-    double phase = 0.0;  // peierlsPhase with B = 0
+    // Locality::peierlsPhase (locality.cpp:7157-7161), then k.(r2 - r1) (4896-4900)
+    double phase = 3.14e-5 * g.b_field * (x2 - x1) * (0.5) * (y1 + y2);
     phase = phase + kx * (x2 - x1) + ky * (y2 - y1);
     const std::complex<double> z = std::polar(t, phase);
     if (z != std::complex<double>(0.0)) v[cnt] += z;

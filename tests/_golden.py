@@ -53,6 +53,7 @@ def parse_in(name, folder="inputs"):
                 max_R = float(v(2))
             elif key == "BOUNDARY_CONDITION":
                 g.boundary_condition = int(v(2))
+                kv["periodic"] = g.boundary_condition == 1
             elif key == "NUM_SHEETS":
                 g.num_sheets = int(v(2))
             elif key == "SUPERCELL_M_N":

@@ -153,16 +153,17 @@ def test_rb_timeout_reports(ctx, window):
     np.testing.assert_array_equal(ok, again)
 
 
-def test_rb_is_the_default_where_ordered(ctx):
+def test_row_blocks_are_the_default_where_ordered(ctx):
     """With the locality ordering on and no kernel forced, 32-column FP32
-    recursions take the row-block step; FP64 and other widths keep the gather
-    kernels."""
+    recursions on a real matrix take the 8-row tensor-core row-block step; FP64
+    and other widths keep the gather kernels."""
     csr = _flake(ctx, 24, 2.2)
     cfg = L.kpm_cfg(32, R=16, seed=4, block=32)
     ctx.set_option("reorder", 1)
     try:
         mu = csr.kpm_dos(cfg)
-        assert csr.rb_info()[0] == (csr.n + 3) // 4
+        assert csr.rt_info()[0] == (csr.n + 7) // 8
+        assert csr.rb_info()[0] == 0
     finally:
         ctx.set_option("reorder", -1)
     ref = _run(ctx, 0, lambda: csr.kpm_dos(cfg))

@@ -121,9 +121,9 @@ def test_vacancies_in_a_field(ctx):
 
 
 def test_vacancy_flake_on_the_row_block_paths(ctx):
-    """A larger flake with 2 % vacancies: the locality ordering and the row blocks
-    take the kept orbitals' positions; DOS moments against the FP64 oracle and the
-    Kubo trace (dxH built in the step) against the stored-dxH path."""
+    """A larger flake with 2 % vacancies: the locality ordering and the 8-row
+    blocks take the kept orbitals' positions; DOS moments against the FP64 oracle
+    and the Kubo trace against the stored-dxH path."""
     g = L.make_geom(model=L.MODEL_SIMPLE, size=30, angles_deg=(0.0, 2.5), energy_rescale=1.0)
     full = ctx.build_csr(ctx.prepare(g), with_dx=True)
     rng = np.random.default_rng(5)
@@ -135,7 +135,7 @@ def test_vacancy_flake_on_the_row_block_paths(ctx):
     try:
         cfg = L.kpm_cfg(64, R=16, seed=4, block=32)
         mu = csr.kpm_dos(cfg)
-        assert csr.rb_info()[0] == (csr.n + 3) // 4
+        assert csr.rt_info()[0] == (csr.n + 7) // 8  # the 8-row tensor-core step ran
         rp, col, val, dx, dy = csr.download(dx=True)
         re, im = oracle.phase_vectors(4, 0, 16, csr.n)
         ref = (oracle.kpm_trace(rp, col, val, re, 64, literal=False) +

@@ -66,11 +66,17 @@ def test_magnetic_field_inputs(name):
 
 
 def test_magnetic_field_limits(tmp_path):
+    # a field on a periodic supercell runs (generateCpxH's Peierls phase on every image)
     p = tmp_path / "x.in"
     p.write_text("NUM_SHEETS = 1\nSTART_SHEET 1\nMATERIAL = Graphene\nEND_SHEET 1\nBOUNDARY_CONDITION = 1\n"
                  "SUPERCELL_M_N = 2 3\nUSE_B_FIELD = 1\nB_FIELD = 10\nPOLY_ORDER = 32\n")
     st, g, ints, msg = _parse(p)
-    assert st == 0 and ints[7] == 1 and "BOUNDARY_CONDITION" in msg
+    assert st == 0 and ints[7] == 0 and g.b_field == 10.0
+    # the Kubo observable in a field is refused by name
+    p.write_text("NUM_SHEETS = 1\nSTART_SHEET 1\nMATERIAL = Graphene\nEND_SHEET 1\n"
+                 "OBSERVABLE_TYPE = COND\nUSE_B_FIELD = 1\nB_FIELD = 10\nPOLY_ORDER = 32\n")
+    st, g, ints, msg = _parse(p)
+    assert st == 0 and ints[7] == 1 and "COND" in msg
 
 
 def test_missing_file():
