@@ -152,7 +152,9 @@ int64_t leo2d_ctx_launch_count(const leo2d_ctx* ctx);
  * "kubo_velocity" (trace Kubo moments: -1 = dxH built inside the row-block
  * step from the flake's positions, the default where it applies; 0 = the
  * stored dxH), "kubo_chunk" (trace Kubo moments: T_m vectors held at once,
- * a multiple of 4; 0 = as many as device memory allows). */
+ * a multiple of 4; 0 = as many as device memory allows), "mlp_fused" (the
+ * control variate's network over many sites: 1 = one persistent launch with
+ * every activation on chip, the default; 0 = one GEMM per layer). */
 leo2d_status leo2d_ctx_set_option(leo2d_ctx* ctx, const char* key, int64_t value);
 
 /* ---------------------------------------------------------------- geometry */

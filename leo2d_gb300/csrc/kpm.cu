@@ -839,8 +839,10 @@ extern "C" leo2d_status leo2d_kpm_autotune(leo2d_ctx* ctx, const leo2d_csr* csr,
           }
         }
       }
-      // the tensor-core step (one shape) where it applies
-      if (!fp64 && (cols == 32 || cols == 64) && ctx->kernel_variant != 0 && ctx->kernel_variant != 1) {
+      // the windowed tensor-core step (one shape), timed only when asked for: it
+      // lost to the gather kernels by 3x on twisted-bilayer flakes and its build
+      // took a second per 10M-orbital matrix
+      if (!fp64 && (cols == 32 || cols == 64) && ctx->kernel_variant == 2) {
         StepShape sh = choose_shape(ctx, csr, fp64, cols, cols, 0);
         sh.tc = true;
         sh.rb = false;

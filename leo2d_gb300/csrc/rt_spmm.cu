@@ -66,6 +66,9 @@ constexpr int kRtStepBytes = 288;    // one k-step of an 8-row block: 8 columns 
 // one k-step of a block of R rows: 8 columns + 8 R values
 __host__ __device__ constexpr int rt_step_bytes(int R) { return 32 + 32 * R; }
 constexpr int kRtMaxEnt = 2048;      // stored entries of one block (build limit)
+constexpr int kRtHashCols = 1024;    // distinct columns a block may have for the hashed fill
+// shared memory of one build warp: the keys (or the hash table) and the column list
+constexpr size_t kRtBuildSlice = (size_t)kRtMaxEnt * 8 + (size_t)kRtHashCols * 4;
 constexpr int kRtBuildWarps = 4;
 // staging of the gathered T_n rows (the kernel's STAGE parameter)
 constexpr int kRtRegs = 0;     // registers, fragments exchanged by shuffles
@@ -643,9 +646,10 @@ __global__ void __launch_bounds__(kRtBuildWarps * 32)
                const float* __restrict__ pval, int pass, int64_t* __restrict__ kst,
                const int64_t* __restrict__ kstart, unsigned char* __restrict__ data, int* __restrict__ err,
                unsigned long long* __restrict__ ssum) {
-  extern __shared__ unsigned long long rt_keys[];
+  extern __shared__ __align__(16) unsigned char rt_build_smem[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  unsigned long long* keys = rt_keys + (size_t)w * kRtMaxEnt;
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(rt_build_smem + (size_t)w * kRtBuildSlice);
+  uint32_t* list = reinterpret_cast<uint32_t*>(rt_build_smem + (size_t)w * kRtBuildSlice + (size_t)kRtMaxEnt * 8);
   const int64_t warps = (int64_t)gridDim.x * kRtBuildWarps;
   for (int64_t b = (int64_t)blockIdx.x * kRtBuildWarps + w; b < nrb; b += warps) {
     const int64_t r0 = b * R;
@@ -708,6 +712,106 @@ __global__ void __launch_bounds__(kRtBuildWarps * 32)
       }
       continue;
     }
+    unsigned char* base = data + (size_t)kstart[b] * rt_step_bytes(R);
+    auto col_at = [&](int s) {  // column entry of slot s
+      const int jj = s & 7;
+      return reinterpret_cast<int32_t*>(base + (size_t)(s >> 3) * rt_step_bytes(R)) + (jj < 4 ? 2 * jj : 2 * (jj - 4) + 1);
+    };
+    auto val_at = [&](int s, int r) {  // value of (row r, slot s)
+      const int jj = s & 7;
+      float* vp = reinterpret_cast<float*>(base + (size_t)(s >> 3) * rt_step_bytes(R) + 32);
+      return vp + (4 * (r & 7) + (jj & 3)) * (R / 4) + 2 * (r >> 3) + (jj >> 2);
+    };
+    const int KS = (int)kst[b];
+    if (8 * KS <= kRtHashCols) {
+      // Hashed fill: a table of (column << 32 | slot << 16 | row mask) words holds
+      // the distinct columns; only they are sorted (about 124 of the ~540 entries
+      // of an 8-row block), and each entry finds its slot in the table. A
+      // (row, column) pair stored twice falls through to the sort below, which
+      // sums the pair in entry order.
+      constexpr int kSet = kRtMaxEnt;  // 64-bit words; load <= 1/2
+      constexpr unsigned long long kEmpty = ~0ull;
+      for (int i = lane; i < kSet; i += 32) keys[i] = kEmpty;
+      __syncwarp();
+      auto find = [&](uint32_t c) {  // the table slot holding column c (present)
+        uint32_t h = (c * 2654435761u) & (kSet - 1);
+        for (int probe = 0; probe < kSet && (uint32_t)(keys[h] >> 32) != c; ++probe) h = (h + 1) & (kSet - 1);
+        return h;
+      };
+      bool dup = false;
+      for (int i = lane; i < E; i += 32) {
+        const uint32_t c = (uint32_t)pcol[q0 + i];
+        const unsigned long long bit = 1ull << row_of(i);
+        uint32_t h = (c * 2654435761u) & (kSet - 1);
+        for (int probe = 0; probe < kSet; ++probe) {  // bounded: the table never fills
+          unsigned long long cur = keys[h];
+          if (cur == kEmpty) {
+            cur = atomicCAS(&keys[h], kEmpty, ((unsigned long long)c << 32) | bit);
+            if (cur == kEmpty) break;
+          }
+          if ((uint32_t)(cur >> 32) == c) {
+            if (atomicOr(&keys[h], bit) & bit) dup = true;
+            break;
+          }
+          h = (h + 1) & (kSet - 1);
+        }
+      }
+      if (!__any_sync(0xffffffffu, dup)) {
+        __syncwarp();
+        // the distinct columns, compacted in table order, then sorted
+        constexpr int kPer = kSet / 32;
+        int cnt = 0;
+        for (int j = 0; j < kPer; ++j) cnt += keys[lane * kPer + j] != kEmpty ? 1 : 0;
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += v;
+        }
+        const int K = __shfl_sync(0xffffffffu, incl, 31);
+        int at = incl - cnt;
+        for (int j = 0; j < kPer; ++j) {
+          const unsigned long long v = keys[lane * kPer + j];
+          if (v != kEmpty) list[at++] = (uint32_t)(v >> 32);
+        }
+        int P2 = 32;
+        while (P2 < K) P2 <<= 1;
+        for (int i = K + lane; i < P2; i += 32) list[i] = 0xFFFFFFFFu;
+        __syncwarp();
+        for (int k = 2; k <= P2; k <<= 1)
+          for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = lane; i < P2; i += 32) {
+              const int ixj = i ^ j;
+              if (ixj > i) {
+                const bool up = (i & k) == 0;
+                const uint32_t x = list[i], y = list[ixj];
+                if ((x > y) == up) {
+                  list[i] = y;
+                  list[ixj] = x;
+                }
+              }
+            }
+            __syncwarp();
+          }
+        // slot s = the rank of its column; the table learns it
+        for (int s2 = lane; s2 < K; s2 += 32) {
+          const uint32_t c = list[s2];
+          *col_at(s2) = (int32_t)c;
+          const uint32_t h = find(c);
+          keys[h] |= (unsigned long long)s2 << 16;
+        }
+        const int32_t pad_col = K > 0 ? (int32_t)list[0] : 0;
+        for (int s2 = K + lane; s2 < 8 * KS; s2 += 32) *col_at(s2) = pad_col;
+        __syncwarp();
+        for (int i = lane; i < E; i += 32) {
+          const uint32_t c = (uint32_t)pcol[q0 + i];
+          const int s2 = (int)((keys[find(c)] >> 16) & 0xFFFFu);
+          *val_at(s2, row_of(i)) = pval[q0 + i];
+        }
+        continue;
+      }
+      __syncwarp();  // the table is read; the sort below reuses the slice
+    }
     int P2 = 32;
     while (P2 < E) P2 <<= 1;
     for (int i = lane; i < P2; i += 32)
@@ -744,12 +848,6 @@ __global__ void __launch_bounds__(kRtBuildWarps * 32)
       if (lane >= o) incl += v;
     }
     const int K = __shfl_sync(0xffffffffu, incl, 31);
-    const int KS = max(1, (K + 7) / 8);
-    unsigned char* base = data + (size_t)kstart[b] * rt_step_bytes(R);
-    auto col_at = [&](int s) {  // column entry of slot s
-      const int jj = s & 7;
-      return reinterpret_cast<int32_t*>(base + (size_t)(s >> 3) * rt_step_bytes(R)) + (jj < 4 ? 2 * jj : 2 * (jj - 4) + 1);
-    };
     const int32_t pad_col = K > 0 ? (int32_t)(keys[0] >> 16) : 0;
     for (int s = K + lane; s < 8 * KS; s += 32) *col_at(s) = pad_col;
     int s = incl - cnt - 1;
@@ -776,9 +874,7 @@ __global__ void __launch_bounds__(kRtBuildWarps * 32)
           if (row_of(e2) != r) break;
           v += pval[q0 + e2];
         }
-        const int jj = s & 7;
-        float* vp = reinterpret_cast<float*>(base + (size_t)(s >> 3) * rt_step_bytes(R) + 32);
-        vp[(4 * (r & 7) + (jj & 3)) * (R / 4) + 2 * (r >> 3) + (jj >> 2)] = v;
+        *val_at(s, r) = v;
       }
     }
   }
@@ -892,7 +988,7 @@ bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chun
       csr->rt_curve == csr->reorder_curve && csr->rt_warps == warps && csr->rt_group == group &&
       csr->rt_chunk == chunk && csr->rt_grid == sh.grid)
     return true;
-  const size_t smem = (size_t)kRtBuildWarps * kRtMaxEnt * sizeof(unsigned long long);
+  const size_t smem = (size_t)kRtBuildWarps * kRtBuildSlice;
   auto build_kernel = rows == 16 ? k_rt_build<16> : k_rt_build<8>;
   LEO_CUDA(cudaFuncSetAttribute(build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const unsigned bgrid = grid_for(sh.nrb * 32, kRtBuildWarps * 32, (int64_t)ctx->sm_count * 8);
@@ -969,8 +1065,9 @@ bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chun
   csr->rt_data.alloc((size_t)std::max<int64_t>(total, 1) * KB);
   LEO_CUDA(cudaMemsetAsync(csr->rt_data.p, 0, (size_t)std::max<int64_t>(total, 1) * KB, ctx->stream));
   launch(ctx, "rt_build", [&] {
+    // pass 1 reads each block's k-step count (kst) and writes nothing to it
     build_kernel<<<bgrid, kRtBuildWarps * 32, smem, ctx->stream>>>(n, sh.nrb, csr->prow.p, csr->pcol.p,
-                                                                     csr->pval32.p, 1, nullptr, kstart.p,
+                                                                     csr->pval32.p, 1, csr->rt_kst.p, kstart.p,
                                                                      csr->rt_data.p, err.p, ssum.p);
   });
   int h0 = 0;
