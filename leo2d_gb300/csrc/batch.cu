@@ -154,6 +154,7 @@ int64_t tile_max_nnz(leo2d_ctx* ctx, const int64_t* rp, int64_t n, int tile_rows
 struct BatchShape {
   int cols = 32, warps = 8, rows_per_item = 0;
   bool rb = false;
+  bool rt = false;  // every step of a pass in one cooperative launch of the 8-row step
 };
 
 }  // namespace
@@ -172,6 +173,10 @@ struct leo2d_batch {
   DevBuf<double> partials;  // [2][grid][2C]
   DevBuf<double> dots;      // [passes][F][steps][2C]
   DevBuf<uint64_t> seed_first;
+  DevBuf<unsigned> bar;  // 8-row form: per-flake step barriers
+  DevBuf<int> abort;
+  // 8-row form: what the captured graph points at, per flake (checked before a run)
+  std::vector<const unsigned char*> rt_data;
   BatchParams<float> params[2];  // step parity 0 / 1 differ in buffer roles
   cudaGraphExec_t graph = nullptr;
   int64_t launches_per_run = 0;
@@ -189,7 +194,12 @@ bool layout(leo2d_batch* b, const BatchShape& s) {
   const int F = (int)b->fl.size();
   int G = 0;
   std::vector<int64_t> tiles_of(F);
-  if (s.rb) {
+  if (s.rt) {
+    b->dyn_smem = rt_batch_smem();
+    G = ctx->sm_count;  // one CTA of 16 warps per SM, all resident at once
+    // cap[f] below: the chunks of the flake's walk (tile_chunk = 1 in these units)
+    for (int f = 0; f < F; ++f) tiles_of[f] = rt_batch_cap(ctx, b->fl[f].csr);
+  } else if (s.rb) {
     std::vector<const leo2d_csr*> cs(F);
     for (int f = 0; f < F; ++f) cs[f] = b->fl[f].csr;
     b->dyn_smem = rb_batch_smem(ctx, cs.data(), F, s.warps);
@@ -224,7 +234,8 @@ bool layout(leo2d_batch* b, const BatchShape& s) {
   std::vector<int64_t> cap(F);
   for (int f = 0; f < F; ++f) {
     w[f] = (double)b->fl[f].nnz * 8 + (double)b->fl[f].n * (8 + 12.0 * s.cols);
-    cap[f] = std::max<int64_t>(1, (tiles_of[f] + ctx->tile_chunk - 1) / ctx->tile_chunk);
+    cap[f] = s.rt ? std::max<int64_t>(1, tiles_of[f])
+                  : std::max<int64_t>(1, (tiles_of[f] + ctx->tile_chunk - 1) / ctx->tile_chunk);
   }
   std::vector<int> nb(F, 1);
   {
@@ -338,9 +349,33 @@ void enqueue_run(leo2d_batch* b) {
       });
     }
     double* dots = b->dots.p + (size_t)pass * F * S * 2 * C;
-    for (int k = 0; k < S; ++k)
-      step_launch(b, k, b->partials.p + (size_t)(k % 2) * part,
-                  k == 0 ? nullptr : b->partials.p + (size_t)((k + 1) % 2) * part, dots, true);
+    if (b->shape.rt) {
+      // the pass's S steps in one cooperative launch
+      std::vector<RtBatchFlake> fl(F);
+      for (int f = 0; f < F; ++f) {
+        const FlakeView& v = b->fl[f];
+        const leo2d_csr* m = v.csr;
+        RtBatchFlake& r = fl[f];
+        r.data = m->rt_data.p;
+        r.wbeg = m->rt_wbeg.p;
+        r.kst = m->rt_kst.p;
+        r.n = m->n;
+        r.nrb = m->rt_blocks;
+        r.group = m->rt_group;
+        r.chunk = m->rt_chunk;
+        r.x0 = b->x0.p + v.row_off * C;
+        r.x1 = b->x1.p + v.row_off * C;
+        r.partials[0] = b->partials.p + (size_t)b->block_first[f] * 2 * C;
+        r.partials[1] = b->partials.p + part + (size_t)b->block_first[f] * 2 * C;
+        r.dots = dots + (size_t)f * S * 2 * C;
+      }
+      rt_batch_launch(ctx, fl.data(), b->block_first.data(), F, S, b->bar.p, b->abort.p,
+                      ctx->test_unsatisfied_wait);
+    } else {
+      for (int k = 0; k < S; ++k)
+        step_launch(b, k, b->partials.p + (size_t)(k % 2) * part,
+                    k == 0 ? nullptr : b->partials.p + (size_t)((k + 1) % 2) * part, dots, true);
+    }
     for (int f = 0; f < F; ++f) {
       const size_t off = (size_t)b->block_first[f] * 2 * C;
       batch_reduce(ctx, C, b->partials.p + (size_t)((S - 1) % 2) * part + off,
@@ -349,8 +384,37 @@ void enqueue_run(leo2d_batch* b) {
   }
 }
 
+// The 8-row form: each flake's blocks built for the CTAs it gets (a single run on
+// the same matrix rebuilds them for one CTA per SM, so a run checks them first).
+void build_rt_formats(leo2d_batch* b) {
+  leo2d_ctx* ctx = b->ctx;
+  rt_batch_prepare(ctx, b->grid);
+  b->rt_data.assign(b->fl.size(), nullptr);
+  for (size_t f = 0; f < b->fl.size(); ++f) {
+    leo2d_csr* m = const_cast<leo2d_csr*>(b->fl[f].csr);
+    const int nb = b->block_first[f + 1] - b->block_first[f];
+    LEO_REQUIRE(csr_build_rt(ctx, m, kRtBatchWarps, rt_group_of(ctx), rt_chunk_of(ctx), 8, nb) &&
+                    m->rt_grid == (unsigned)nb,
+                "a batched flake's 8-row blocks exceed the build limits");
+    b->rt_data[f] = m->rt_data.p;
+  }
+}
+
+bool rt_formats_current(const leo2d_batch* b) {
+  for (size_t f = 0; f < b->fl.size(); ++f) {
+    const leo2d_csr* m = b->fl[f].csr;
+    const int nb = b->block_first[f + 1] - b->block_first[f];
+    if (!m->rt_built || m->rt_data.p != b->rt_data[f] || m->rt_grid != (unsigned)nb || m->rt_rows != 8 ||
+        m->rt_warps != kRtBatchWarps)
+      return false;
+  }
+  return true;
+}
+
 void allocate(leo2d_batch* b) {
   const int C = b->shape.cols, F = (int)b->fl.size();
+  b->bar.alloc((size_t)F);
+  b->abort.alloc(1);
   b->x0.alloc((size_t)b->n_total * C);
   b->x1.alloc((size_t)b->n_total * C);
   b->partials.alloc((size_t)2 * b->grid * 2 * C);
@@ -454,7 +518,7 @@ leo2d_status leo2d_batch_create(leo2d_ctx* ctx, const leo2d_csr* const* csrs, in
       const double patch = reorder_patch_for(ctx, rb_mode);
       if (perm && (!m->reordered || m->reorder_patch != patch || m->reorder_curve_req != ctx->reorder_curve))
         csr_build_reordered(ctx, mm, patch, m->reorder_fp64, ctx->reorder_curve != 0);
-      if (rb_mode && (!m->rb_built || m->rb_patch != m->reorder_patch))
+      if (rb_mode && ctx->kernel_variant == 3 && (!m->rb_built || m->rb_patch != m->reorder_patch))
         LEO_REQUIRE(csr_build_rb(ctx, mm), "a batched flake's row blocks exceed the build limits");
       FlakeView v;
       v.csr = m;
@@ -475,7 +539,11 @@ leo2d_status leo2d_batch_create(leo2d_ctx* ctx, const leo2d_csr* const* csrs, in
     // shape: the caller's, or the fastest estimated run time over widths,
     // warps and rows per slot (each candidate timed on real batched steps)
     std::vector<BatchShape> cands;
-    if (rb_mode) cands.push_back(BatchShape{32, 24, 0, true});
+    // 32-column passes over ordered flakes: every step of a pass in one launch of
+    // the 8-row tensor-core step, or (step_kernel 3) one launch per step of the
+    // 4-row step
+    if (rb_mode && ctx->kernel_variant == 3) cands.push_back(BatchShape{32, 24, 0, true, false});
+    else if (rb_mode) cands.push_back(BatchShape{32, kRtBatchWarps, 0, false, true});
     const int widths[5] = {8, 16, 32, 64, 128};
     for (int w : rb_mode ? std::vector<int>() : std::vector<int>(widths, widths + 5)) {
       if (cfg->block && w != cfg->block) continue;
@@ -509,6 +577,7 @@ leo2d_status leo2d_batch_create(leo2d_ctx* ctx, const leo2d_csr* const* csrs, in
     }
     allocate(b.get());
     fill_params(b.get());
+    if (b->shape.rt) build_rt_formats(b.get());
     capture(b.get());
     *out = b.release();
   });
@@ -519,6 +588,12 @@ leo2d_status leo2d_batch_run(leo2d_batch* b, uint64_t seed, uint64_t first_vecto
   leo2d_ctx* ctx = b->ctx;
   return guard(ctx, [&] {
     LEO_CUDA(cudaSetDevice(ctx->device));
+    if (b->shape.rt && !rt_formats_current(b)) {
+      // a single run on one of the flakes rebuilt its blocks for another grid:
+      // rebuild them for the batch and capture the run again
+      build_rt_formats(b);
+      capture(b);
+    }
     uint64_t sf[2] = {seed, first_vector};
     h2d(ctx, b->seed_first.p, sf, 2);
     LEO_CUDA(cudaGraphLaunch(b->graph, ctx->stream));

@@ -144,9 +144,10 @@ void csr_build_rb_xs(leo2d_ctx* ctx, leo2d_csr* csr);
 // Largest data bytes of a tile of `tile` consecutive row blocks.
 int64_t rb_tile_max_bytes(leo2d_ctx* ctx, const leo2d_csr* csr, int tile);
 // Builds the row blocks (8 or 16 rows) of the tensor-core step for one launch
-// shape; returns false (and builds nothing) when a block holds more than 2048
-// stored entries.
-bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chunk, int rows);
+// shape (max_grid > 0: at most that many CTAs walk them, else one per SM);
+// returns false (and builds nothing) when a block holds more than 2048 stored
+// entries.
+bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chunk, int rows, int max_grid = 0);
 void csr_drop_rt(leo2d_csr* csr);
 // Builds the shared-memory windows of the row blocks; returns false (and builds
 // nothing) when a tile of 16 blocks has more than 8192 slots or 2048 distinct columns.

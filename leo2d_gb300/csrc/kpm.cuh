@@ -95,6 +95,35 @@ void rt_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
                     const float* tn, float* tp, const float* tprev, int first, float alpha, double* partials,
                     const double* prev_partials, double* prev_dots);
 
+// Every step of one pass over several matrices (flakes) in one cooperative
+// launch of the 8-row tensor-core step (rt_spmm.cu): flake f runs on CTAs
+// [block_first[f], block_first[f+1]), whose count its blocks were built for
+// (csr_build_rt's max_grid), and its CTAs meet at a barrier between steps.
+constexpr int kRtBatchMax = 64;
+constexpr int kRtBatchWarps = 16, kRtBatchDepth = 3;  // the launch shape of every flake
+struct RtBatchFlake {
+  const unsigned char* data = nullptr;  // the flake's k-steps (csr->rt_data)
+  const int64_t* wbeg = nullptr;
+  const int64_t* kst = nullptr;
+  int64_t n = 0, nrb = 0;
+  int group = 0, chunk = 0;
+  float* x0 = nullptr;            // T_0 (step parity 0 reads x0, writes x1)
+  float* x1 = nullptr;
+  double* partials[2] = {nullptr, nullptr};  // by step parity, [CTAs of the flake][64]
+  double* dots = nullptr;         // [steps][64] of this pass
+};
+// CTAs the flake's 8-row blocks can keep busy (its walk's chunks, at most one per SM)
+unsigned rt_batch_cap(leo2d_ctx* ctx, const leo2d_csr* csr);
+size_t rt_batch_smem();
+// Sets the launch's shared-memory attribute and checks that `grid` CTAs can all
+// be resident (call outside stream capture, before the first launch).
+void rt_batch_prepare(leo2d_ctx* ctx, unsigned grid);
+// One launch of `steps` steps over every flake; bar [nflakes] and abort are zeroed
+// first (on the stream). never_arrive: the barriers wait for one arrival too many
+// (tests the bounded wait).
+void rt_batch_launch(leo2d_ctx* ctx, const RtBatchFlake* fl, const int* block_first, int nflakes, int steps,
+                     unsigned* bar, int* abort, int never_arrive);
+
 // The row-block step over several matrices (flakes) in one launch: flake f runs
 // on CTAs [block_first[f], block_first[f+1]) with its own vectors and partials.
 constexpr int kRbBatchMax = 64;

@@ -242,12 +242,27 @@ __device__ __forceinline__ float2 ld_stream_f2(const void* p) {
 // Each warp walks its blocks in the build's processing order: runs of G
 // consecutive blocks, run i in tile (bid + (i / chunk) grid) chunk + i % chunk;
 // a block ends after its k-step count (kst), read one block ahead.
-template <int W, int D, int STAGE, int R>
+// The epilogue's reads of T_n and T_{n-1} rows: through the read-only path, or,
+// in a launch that runs several steps (COH), from L2, since other CTAs of the
+// launch wrote those rows after L1 may have cached older ones.
+template <bool COH>
+__device__ __forceinline__ float4 ld_rows_tn(const float* p) {
+  if constexpr (COH) return __ldcg(reinterpret_cast<const float4*>(p));
+  else return ldg4(p);
+}
+template <bool COH>
+__device__ __forceinline__ float4 ld_rows_tprev(const float* p) {
+  if constexpr (COH) return __ldcg(reinterpret_cast<const float4*>(p));
+  else return ld_once4(p);
+}
+
+template <int W, int D, int STAGE, int R, bool COH = false>
 __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const int nblk) {
   constexpr bool REGS = STAGE == kRtRegs;
   constexpr int NTI = R / kRtRows;       // n-tiles (8 rows each) of a block
   constexpr int KB = rt_step_bytes(R);   // bytes of one k-step
   static_assert((R == 8 || R == 16) && (R == 8 || STAGE == kRtCpAsync), "16-row blocks: cp.async form only");
+  static_assert(!COH || STAGE == kRtCpAsync, "multi-step launches: the cp.async form (its gathers bypass L1)");
   constexpr int C = 32;
   constexpr int NT = W * 32;
   constexpr int XS = D + 1;      // shared ring of staged T_n rows (k-steps)
@@ -336,12 +351,12 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
     for (int nt = 0; nt < NTI; ++nt) {
       const int64_t r0 = row0 + 8 * nt + 2 * t;
       if (r0 < n) {
-        xn0[nt] = ldg4(tnc + r0 * C);
-        if (!first) xp0[nt] = ld_once4(tprev + r0 * C + 4 * cg);
+        xn0[nt] = ld_rows_tn<COH>(tnc + r0 * C);
+        if (!first) xp0[nt] = ld_rows_tprev<COH>(tprev + r0 * C + 4 * cg);
       }
       if (r0 + 1 < n) {
-        xn1[nt] = ldg4(tnc + (r0 + 1) * C);
-        if (!first) xp1[nt] = ld_once4(tprev + (r0 + 1) * C + 4 * cg);
+        xn1[nt] = ld_rows_tn<COH>(tnc + (r0 + 1) * C);
+        if (!first) xp1[nt] = ld_rows_tprev<COH>(tprev + (r0 + 1) * C + 4 * cg);
       }
     }
   };
@@ -630,6 +645,97 @@ __global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ R
   rt_body<W, D, STAGE, R>(a, (int)blockIdx.x, (int)gridDim.x);
 }
 
+// ---------------------------------------------------------------- batched flakes, one launch
+
+// Every Chebyshev step of one pass over a batch of flakes in a single
+// cooperative launch: the CTAs of flake f (block_first[f] .. block_first[f+1])
+// run the 8-row step on its blocks, then meet at the flake's barrier (a counter
+// in global memory) before the next step; flakes never wait on one another.
+// Step k reads T_k from one buffer and writes T_{k+1} over T_{k-1} in the other;
+// its prologue reduces step k-1's partials into dots[k-1], as the per-step
+// launches do. The barrier: __syncthreads, a GPU-scope fence and an atomic
+// arrival by thread 0, which then polls the counter with acquire loads. Polls
+// give up after spin_limit rounds or two seconds: the CTA records a timeout,
+// raises the abort flag (which every polling CTA also reads) and leaves; its
+// copies were all waited for at the end of its step.
+struct RtBatchParams {
+  leo2d::RtBatchFlake f[leo2d::kRtBatchMax];
+  int block_first[leo2d::kRtBatchMax + 1];
+  int nflakes, steps;
+  unsigned* bar;    // [nflakes] arrivals, zero at launch
+  int* abort;       // non-zero: some CTA gave up
+  int* status;
+  uint64_t spin_limit;
+  int never_arrive; // test hook: barrier targets one arrival more than the group makes
+};
+static_assert(sizeof(RtBatchParams) <= 32764, "batched 8-row parameters exceed the parameter space");
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ bool rt_group_barrier(const RtBatchParams& p, unsigned* bar, unsigned target) {
+  __shared__ int go;
+  __syncthreads();  // every thread of the CTA is done with the step
+  if (threadIdx.x == 0) {
+    __threadfence();  // the CTA's T_{k+1} rows and partials, at GPU scope
+    atomicAdd(bar, 1u);
+    int ok = 1;
+    const uint64_t t0 = umma::now_ns();
+    for (uint64_t k = 0;; ++k) {
+      if (ld_acquire_u32(bar) >= target) break;
+      if (*reinterpret_cast<volatile int*>(p.abort) != 0) {
+        ok = 0;
+        break;
+      }
+      if (k >= p.spin_limit || ((k & 255) == 255 && umma::now_ns() - t0 > 2000000000ull)) {
+        atomicExch(p.status, leo2d::kStatusTimeout);
+        atomicExch(p.abort, 1);
+        ok = 0;
+        break;
+      }
+    }
+    __threadfence();
+    go = ok;
+  }
+  __syncthreads();
+  return go != 0;
+}
+
+template <int W, int D>
+__global__ void __launch_bounds__(W * 32, 1) k_cheb_rt_batch(const __grid_constant__ RtBatchParams p) {
+  int f = 0;
+  while (f + 1 < p.nflakes && (int)blockIdx.x >= p.block_first[f + 1]) ++f;
+  const int bid = (int)blockIdx.x - p.block_first[f], nblk = p.block_first[f + 1] - p.block_first[f];
+  const leo2d::RtBatchFlake& F = p.f[f];
+  constexpr int C = 32;
+  for (int k = 0; k < p.steps; ++k) {
+    RtArgs a{};
+    a.n = F.n;
+    a.nrb = F.nrb;
+    a.data = F.data;
+    a.wbeg = F.wbeg;
+    a.kst = F.kst;
+    a.tn = k % 2 == 0 ? F.x0 : F.x1;
+    a.tp = k % 2 == 0 ? F.x1 : F.x0;
+    a.tprev = nullptr;
+    a.first = k == 0;
+    a.alpha = 0.f;
+    a.partials = F.partials[k % 2];
+    a.prev_partials = k == 0 ? nullptr : F.partials[(k + 1) % 2];
+    a.prev_dots = k == 0 ? nullptr : F.dots + (size_t)(k - 1) * 2 * C;
+    a.group = F.group;
+    a.chunk = F.chunk;
+    a.spin_limit = p.spin_limit;
+    a.status = p.status;
+    rt_body<W, D, kRtCpAsync, kRtRows, true>(a, bid, nblk);
+    const unsigned target = (unsigned)(k + 1) * (unsigned)nblk + (p.never_arrive ? 1u : 0u);
+    if (!rt_group_barrier(p, p.bar + f, target)) break;
+  }
+}
+
 // ---------------------------------------------------------------- format build
 
 // One warp per block of R rows, at most kRtMaxEnt stored entries; the distinct
@@ -909,13 +1015,14 @@ struct RtShape {
   unsigned grid;
 };
 
-RtShape rt_shape(const leo2d_ctx* ctx, int64_t n, int warps, int group, int chunk, int rows) {
+RtShape rt_shape(const leo2d_ctx* ctx, int64_t n, int warps, int group, int chunk, int rows, int max_grid = 0) {
   RtShape s;
   s.nrb = (n + rows - 1) / rows;
   s.nruns = (s.nrb + group - 1) / group;
   s.ntiles = (s.nruns + warps - 1) / warps;
   const int64_t chunks = (s.ntiles + chunk - 1) / chunk;
-  s.grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->sm_count, chunks));
+  const int64_t cap = max_grid > 0 ? max_grid : (int64_t)ctx->sm_count;
+  s.grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cap, chunks));
   return s;
 }
 
@@ -978,12 +1085,12 @@ void csr_drop_rt(leo2d_csr* csr) {
   csr->rt_rows = 0;
 }
 
-bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chunk, int rows) {
+bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chunk, int rows, int max_grid) {
   LEO_REQUIRE(csr->reordered && !csr->complex_h, "the tensor-core row-block step needs the real locality-ordered copy");
   LEO_REQUIRE(rows == 8 || rows == 16, "tensor-core row blocks hold 8 or 16 rows");
   const int64_t n = csr->n;
   const int KB = rt_step_bytes(rows);
-  const RtShape sh = rt_shape(ctx, n, warps, group, chunk, rows);
+  const RtShape sh = rt_shape(ctx, n, warps, group, chunk, rows, max_grid);
   if (csr->rt_built && csr->rt_rows == rows && csr->rt_patch == csr->reorder_patch &&
       csr->rt_curve == csr->reorder_curve && csr->rt_warps == warps && csr->rt_group == group &&
       csr->rt_chunk == chunk && csr->rt_grid == sh.grid)
@@ -1082,6 +1189,56 @@ bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chun
   csr->rt_grid = sh.grid;
   csr->rt_built = true;
   return true;
+}
+
+unsigned rt_batch_cap(leo2d_ctx* ctx, const leo2d_csr* csr) {
+  return rt_shape(ctx, csr->n, kRtBatchWarps, rt_group_of(ctx), rt_chunk_of(ctx), kRtRows).grid;
+}
+
+size_t rt_batch_smem() { return rt_smem_bytes(kRtBatchWarps, kRtBatchDepth, kRtCpAsync, kRtRows); }
+
+void rt_batch_prepare(leo2d_ctx* ctx, unsigned grid) {
+  auto kern = k_cheb_rt_batch<kRtBatchWarps, kRtBatchDepth>;
+  const size_t smem = rt_batch_smem();
+  LEO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 0, coop = 0;
+  LEO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kRtBatchWarps * 32, smem));
+  LEO_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
+  LEO_REQUIRE(coop != 0, "batched 8-row step: the device has no cooperative launches");
+  LEO_REQUIRE(occ >= 1 && grid <= (unsigned)(occ * ctx->sm_count),
+              "batched 8-row step: the CTAs of one launch cannot all be resident");
+}
+
+void rt_batch_launch(leo2d_ctx* ctx, const RtBatchFlake* fl, const int* block_first, int nflakes, int steps,
+                     unsigned* bar, int* abort, int never_arrive) {
+  LEO_REQUIRE(nflakes >= 1 && nflakes <= kRtBatchMax, "a batched launch holds 1..64 matrices");
+  RtBatchParams p{};
+  for (int f = 0; f < nflakes; ++f) p.f[f] = fl[f];
+  for (int f = 0; f <= nflakes; ++f) p.block_first[f] = block_first[f];
+  p.nflakes = nflakes;
+  p.steps = steps;
+  p.bar = bar;
+  p.abort = abort;
+  p.status = ctx->status.p;
+  p.spin_limit = ctx->spin_limit;
+  p.never_arrive = never_arrive;
+  const unsigned grid = (unsigned)block_first[nflakes];
+  const size_t smem = rt_batch_smem();
+  auto kern = k_cheb_rt_batch<kRtBatchWarps, kRtBatchDepth>;
+  LEO_REQUIRE(grid <= (unsigned)ctx->sm_count, "batched 8-row step: more CTAs than SMs");
+  LEO_CUDA(cudaMemsetAsync(bar, 0, sizeof(unsigned) * nflakes, ctx->stream));
+  LEO_CUDA(cudaMemsetAsync(abort, 0, sizeof(int), ctx->stream));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kRtBatchWarps * 32);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;  // every CTA resident at once: the barriers need it
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  launch(ctx, "cheb_batch_step", [&] { LEO_CUDA(cudaLaunchKernelEx(&cfg, kern, p)); });
 }
 
 void rt_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape, unsigned grid, size_t smem,
