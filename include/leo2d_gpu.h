@@ -291,21 +291,26 @@ leo2d_status leo2d_dos_reconstruct(leo2d_ctx* ctx, const double* mu, int32_t pol
 
 /* ---------------------------------------------------------------- batched flakes */
 
-/* Many matrices (flakes or twist angles of uneven size) in one launch per
- * Chebyshev step, the whole run captured once in a CUDA graph. Stands in for
- * the reference's farm of independent jobs, each running
- * Locality::computeDosTraceKPM on its own rank (src/locality.cpp:2295-2309,
- * 6138-6346). Each matrix must already be rescaled (leo2d_csr_rescale) and must
- * outlive the batch. cfg: random-phase vectors, FP32 recursion (FP64 moments);
- * block / rows_per_warp 0 = autotuned over the batch (block width, warps,
- * rows per slot timed on real batched steps). 1..64 matrices. */
+/* Many matrices (flakes or twist angles of uneven size) run together, the whole
+ * run captured once in a CUDA graph. Stands in for the reference's farm of
+ * independent jobs, each running Locality::computeDosTraceKPM on its own rank
+ * (src/locality.cpp:2295-2309, 6138-6346). With 32-column passes over matrices
+ * with positions (block 0 or 32, the locality ordering on), every step of a
+ * pass runs in one cooperative launch of the 8-row tensor-core step, each
+ * matrix on its own group of CTAs (step_kernel = 3: one launch per step of the
+ * 4-row step); otherwise one launch per step over all matrices. Each matrix
+ * must already be rescaled (leo2d_csr_rescale) and must outlive the batch.
+ * cfg: random-phase vectors, FP32 recursion (FP64 moments); block /
+ * rows_per_warp 0 = autotuned over the batch (block width, warps, rows per slot
+ * timed on real batched steps). 1..64 matrices. */
 typedef struct leo2d_batch leo2d_batch;
 leo2d_status leo2d_batch_create(leo2d_ctx* ctx, const leo2d_csr* const* csrs, int32_t num,
                                 const leo2d_kpm_cfg* cfg, leo2d_batch** out);
 /* One replay: mu_out[f][v][n], f < num, v < cfg->num_vectors, n < poly_order, for
  * Philox vectors first_vector + v under key seed (the vectors leo2d_kpm_dos draws). */
 leo2d_status leo2d_batch_run(leo2d_batch* b, uint64_t seed, uint64_t first_vector, double* mu_out);
-/* The chosen shape, the grid of each step launch and the kernel launches in one replay. */
+/* The chosen shape (warps 16: the one-launch form), the grid of each launch and
+ * the kernel launches in one replay. */
 leo2d_status leo2d_batch_info(const leo2d_batch* b, int32_t* block_cols, int32_t* warps,
                               int32_t* rows_per_item, int32_t* grid, int64_t* launches_per_run);
 leo2d_status leo2d_batch_destroy(leo2d_batch* b);
