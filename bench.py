@@ -603,6 +603,8 @@ def run_bfield(args):
     from oracle import oracle
     B = 20.0
     ctx = L.Context(0)
+    if args.step_kernel >= 0:  # 3: the 4-row complex step, 5: the 8-row one
+        ctx.set_option("step_kernel", args.step_kernel)
     g = geom(L, radius=args.radius)
     g.b_field = B
     t0 = time.perf_counter()
@@ -650,7 +652,8 @@ def run_bfield(args):
            "build_s": round(t_build, 3),
            "roofline": {"bound": "hbm", "achieved": round(bytes_step / (step_ms / 1000) / 1e9, 1), "peak": peak,
                         "unit": "GB/s", "frac": round(bytes_step / (step_ms / 1000) / 1e9 / peak, 4),
-                        "kernel": "k_cheb_rb complex", "bytes_per_launch": bytes_step,
+                        "kernel": {3: "k_cheb_rb complex", 5: "k_cheb_rt complex"}.get(
+                            csr.step_kernel(cfg)[0], str(csr.step_kernel(cfg)[0])), "bytes_per_launch": bytes_step,
                         "launch_ms": round(step_ms, 4), "peak_kind": peak_kind},
            "fp32_gpu_vs_fp64_oracle_moments_162k": float(np.abs(ms - mo).max() / np.abs(mo).max()),
            "gpu_launches": int(launches)}

@@ -189,6 +189,7 @@ bool cond_trace_rows(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* 
   leo2d_csr* m = const_cast<leo2d_csr*>(csr);
   StepShape s = choose_shape(ctx, csr, false, 32, 32, 0);
   s.rb = true;
+  s.rt = false;  // the velocity step exists in the 4-row form only
   s.tc = false;
   s.rb_window = false;
   Recursion r;
@@ -206,6 +207,15 @@ bool cond_trace_rows(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* 
   }
   if (!r.shape.rb || !r.use_perm || rb_stages(ctx, m, sv.rb_warps, true) < 2) return false;
   csr_build_rb_xs(ctx, m);
+  // the B side's plain steps: the 8-row tensor-core step where it builds (the
+  // 4-row step otherwise); its moment dots go to a scratch row nobody reads
+  StepShape sb = choose_shape(ctx, csr, false, 32, 32, 0);
+  sb.rb = false;
+  sb.tc = false;
+  sb.rt = ctx->kernel_variant == -1 || ctx->kernel_variant == 5;
+  Recursion rt;
+  if (sb.rt) rt.setup(ctx, csr, sb, 1);
+  const bool b_rt = sb.rt && rt.shape.rt && rt.use_perm && m->rb_built;
   const size_t smem_v = rb_smem_bytes(ctx, m, sv.rb_warps, true);
   const unsigned grid_v = rb_grid(ctx, csr, sv.rb_warps);
   constexpr int C = 32;
@@ -250,6 +260,10 @@ bool cond_trace_rows(leo2d_ctx* ctx, const leo2d_csr* csr, const leo2d_kpm_cfg* 
       for (int64_t mm = m0; mm < m0 + mn; ++mm) {
         if (mm == 0)
           LEO_CUDA(cudaMemcpyAsync(slot(0), X0, vec * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+        else if (b_rt)
+          rt_launch_step(ctx, csr, rt.shape, rt.grid, rt.dyn_smem, slot(mm - 1), slot(mm),
+                         mm == 1 ? nullptr : slot(mm - 2), mm == 1 ? 1 : 0, mm == 1 ? 1.f : 2.f, part.p, nullptr,
+                         nullptr);
         else if (mm == 1)
           rb_launch_step(ctx, csr, r.shape, r.grid, r.dyn_smem, slot(0), slot(1), nullptr, 1, 1.f, part.p,
                          nullptr, nullptr);

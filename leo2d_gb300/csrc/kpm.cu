@@ -310,11 +310,18 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
   leo2d_csr* mm = const_cast<leo2d_csr*>(m);
   const bool can_perm = allow_perm && m->pos.p != nullptr && m->nnz > 0;
   if (shape.tc && !can_perm) shape.tc = false;
-  if (m->complex_h)
-    LEO_REQUIRE(shape.rb && can_perm && !s.fp64 && s.cols == 32 && ctx->reorder != 0,
-                "a complex Hamiltonian needs the row-block step (FP32, 32 columns, locality ordering on)");
+  if (m->complex_h) {
+    LEO_REQUIRE((shape.rb || shape.rt) && can_perm && !s.fp64 && s.cols == 32 && ctx->reorder != 0,
+                "a complex Hamiltonian needs a row-block step (FP32, 32 columns, locality ordering on)");
+    if (shape.rt) {  // the complex 8-row step's one launch form
+      shape.rt_stage = 1;
+      shape.rt_rows = 8;
+      shape.rt_depth = 3;
+      if (shape.rt_warps != 12) shape.rt_warps = 16;
+    }
+  }
   if (shape.rb && (!can_perm || s.fp64 || s.cols != 32 || ctx->reorder == 0)) shape.rb = false;
-  if (shape.rt && (!can_perm || s.fp64 || s.cols != 32 || ctx->reorder == 0 || m->complex_h)) shape.rt = false;
+  if (shape.rt && (!can_perm || s.fp64 || s.cols != 32 || ctx->reorder == 0)) shape.rt = false;
   if (shape.rt) shape.rb = false;
   if (shape.rb || shape.rt) shape.tc = false;
   const bool want_perm = can_perm && (shape.tc || shape.rb || shape.rt || ctx->reorder == 1 ||
@@ -363,12 +370,14 @@ void Recursion::setup(leo2d_ctx* c, const leo2d_csr* m, StepShape s, int steps_)
   if (shape.rt) {
     // 8-row blocks of the locality-ordered copy, stored for this launch shape
     const int w = shape.rt_warps;
-    const bool fits = rt_smem_bytes(w, shape.rt_depth, shape.rt_stage, shape.rt_rows) + 8 * 1024 <= ctx->smem_optin;
+    const int panel = m->complex_h ? 16 : shape.rt_rows;  // complex: real and imaginary panels
+    const bool fits = rt_smem_bytes(w, shape.rt_depth, shape.rt_stage, panel) + 8 * 1024 <= ctx->smem_optin;
     if (fits && csr_build_rt(ctx, mm, w, rt_group_of(ctx), rt_chunk_of(ctx), shape.rt_rows)) {
-      dyn_smem = rt_smem_bytes(w, shape.rt_depth, shape.rt_stage, shape.rt_rows);
+      dyn_smem = rt_smem_bytes(w, shape.rt_depth, shape.rt_stage, panel);
       grid = m->rt_grid;
       shape.tiled = false;
     } else {
+      LEO_REQUIRE(!m->complex_h, "the complex 8-row blocks do not build here: step_kernel 3 runs the 4-row step");
       shape.rt = false;  // a block too heavy for the 8-row build: the gather kernels run
     }
   }
@@ -527,7 +536,7 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
   const bool cached = it != g_shape_cache.end();
   if (ctx->kernel_variant == 3) s.rb = rb_ok;
   else if (ctx->kernel_variant == -1) s.rb = rb_ok && (cached ? it->second.rb : (ctx->reorder == 1 || csr->n >= 100000));
-  const bool rt_ok = rb_ok && !csr->complex_h;
+  const bool rt_ok = rb_ok;
   if (ctx->kernel_variant == 5) s.rt = rt_ok;
   else if (ctx->kernel_variant == -1) s.rt = rt_ok && (cached ? it->second.rt : s.rb);
   if (s.rt) s.rb = false;
@@ -537,7 +546,7 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
     LEO_REQUIRE(!fp64, "a complex Hamiltonian (magnetic field) runs in FP32");
     LEO_REQUIRE(s.cols == 32 || requested_cols <= 0, "a complex Hamiltonian takes 32-column blocks");
     s.cols = 32;
-    s.rb = true;
+    s.rb = !s.rt;  // the 4-row step, or the 8-row step when asked for
     s.tc = false;
     s.tiled = true;
   }
@@ -977,7 +986,7 @@ extern "C" leo2d_status leo2d_kpm_step_kernel(leo2d_ctx* ctx, const leo2d_csr* c
     // the demotions Recursion::setup applies before any build
     const bool can_perm = csr->pos.p != nullptr && csr->nnz > 0;
     if (s.rb && (!can_perm || s.fp64 || s.cols != 32 || ctx->reorder == 0)) s.rb = false;
-    if (s.rt && (!can_perm || s.fp64 || s.cols != 32 || ctx->reorder == 0 || csr->complex_h)) s.rt = false;
+    if (s.rt && (!can_perm || s.fp64 || s.cols != 32 || ctx->reorder == 0)) s.rt = false;
     if (s.tc && !can_perm) s.tc = false;
     *kernel = s.rt ? 5 : s.rb ? (s.rb_window ? 4 : 3) : s.tc ? 2 : s.tiled ? 0 : 1;
     *block = s.cols;

@@ -256,10 +256,19 @@ __device__ __forceinline__ float4 ld_rows_tprev(const float* p) {
   else return ld_once4(p);
 }
 
-template <int W, int D, int STAGE, int R, bool COH = false>
+// CPX: a complex H~ on blocks of 8 rows, stored with the 16-row k-step layout
+// (R = 16): n-tile 0 holds the real parts of the values, n-tile 1 the imaginary
+// parts. A complex vector is a (re, im) column pair, so with X the gathered
+// rows, the products P_re = X Re(V)^T and P_im = X Im(V)^T give
+//   (H X)_re = P_re[re col] - P_im[im col],  (H X)_im = P_re[im col] + P_im[re col],
+// combined in the lane's own four columns (two pairs) at the block's end.
+template <int W, int D, int STAGE, int R, bool COH = false, bool CPX = false>
 __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const int nblk) {
   constexpr bool REGS = STAGE == kRtRegs;
-  constexpr int NTI = R / kRtRows;       // n-tiles (8 rows each) of a block
+  constexpr int NTI = R / kRtRows;       // n-tiles (8 rows each) of the k-step panel
+  constexpr int RB = CPX ? kRtRows : R;  // rows of a block
+  constexpr int NTR = RB / kRtRows;      // n-tiles of the block's rows
+  static_assert(!CPX || R == 16, "complex blocks: 8 rows in the 16-row k-step layout");
   constexpr int KB = rt_step_bytes(R);   // bytes of one k-step
   static_assert((R == 8 || R == 16) && (R == 8 || STAGE == kRtCpAsync), "16-row blocks: cp.async form only");
   static_assert(!COH || STAGE == kRtCpAsync, "multi-step launches: the cp.async form (its gathers bypass L1)");
@@ -299,7 +308,7 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
   int jb = 0;
   int64_t tb = (int64_t)bid * chunk;
   int ic = 0;
-  auto run_row = [&]() -> int64_t { return ((tb + ic) * W + warp) * group * R; };
+  auto run_row = [&]() -> int64_t { return ((tb + ic) * W + warp) * group * RB; };
   auto next_run = [&]() {
     if (++ic == chunk) {
       ic = 0;
@@ -310,7 +319,7 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
   next_run();
   int64_t nbase = run_row();  // first row of the next run
   int left = 0;                                       // k-steps of the current block still to run
-  int next_left = nk > 0 ? (int)kst[rbase / R] : 0;  // the next block's k-steps
+  int next_left = nk > 0 ? (int)kst[rbase / RB] : 0;  // the next block's k-steps
   // T_n and T_{n-1} of the lane's rows 8 nt + 2t and 8 nt + 2t + 1 of the block
   float4 xn0[NTI], xn1[NTI], xp0[NTI], xp1[NTI];
 #pragma unroll
@@ -342,13 +351,13 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
     for (int c = 0; c < 4; ++c) e0[c] = e1[c] = 0.f;
   };
   auto begin_block = [&]() {
-    row0 = rbase + (int64_t)jb * R;
+    row0 = rbase + (int64_t)jb * RB;
     left = next_left;
     // the k-steps of the block after this one (its run may start elsewhere)
-    const int64_t nrow = jb + 1 < group ? row0 + R : nbase;
-    if (nrow / R < a.nrb) next_left = (int)kst[nrow / R];
+    const int64_t nrow = jb + 1 < group ? row0 + RB : nbase;
+    if (nrow / RB < a.nrb) next_left = (int)kst[nrow / RB];
 #pragma unroll
-    for (int nt = 0; nt < NTI; ++nt) {
+    for (int nt = 0; nt < NTR; ++nt) {
       const int64_t r0 = row0 + 8 * nt + 2 * t;
       if (r0 < n) {
         xn0[nt] = ld_rows_tn<COH>(tnc + r0 * C);
@@ -379,14 +388,28 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
 #pragma unroll
   for (int nt = 0; nt < NTI; ++nt) acc[nt].zero();
   auto end_block = [&]() {
+    if constexpr (CPX) {
+      float4 a0, a1, b0, b1;  // real-part and imaginary-part products, rows 2t and 2t + 1
+      acc[0].rows(a0, a1);
+      acc[1].rows(b0, b1);
+      acc[0].zero();
+      acc[1].zero();
+      // memory columns 4 cg .. 4 cg + 3 are the pairs (4 cg, 4 cg + 1), (4 cg + 2, 4 cg + 3)
+      const float4 h0 = make_float4(a0.x - b0.y, a0.y + b0.x, a0.z - b0.w, a0.w + b0.z);
+      const float4 h1 = make_float4(a1.x - b1.y, a1.y + b1.x, a1.z - b1.w, a1.w + b1.z);
+      const int64_t r0 = row0 + 2 * t;
+      row_out(r0, h0, xp0[0], xn0[0]);
+      row_out(r0 + 1, h1, xp1[0], xn1[0]);
+    } else {
 #pragma unroll
-    for (int nt = 0; nt < NTI; ++nt) {
-      float4 h0, h1;
-      acc[nt].rows(h0, h1);
-      acc[nt].zero();
-      const int64_t r0 = row0 + 8 * nt + 2 * t;
-      row_out(r0, h0, xp0[nt], xn0[nt]);
-      row_out(r0 + 1, h1, xp1[nt], xn1[nt]);
+      for (int nt = 0; nt < NTI; ++nt) {
+        float4 h0, h1;
+        acc[nt].rows(h0, h1);
+        acc[nt].zero();
+        const int64_t r0 = row0 + 8 * nt + 2 * t;
+        row_out(r0, h0, xp0[nt], xn0[nt]);
+        row_out(r0 + 1, h1, xp1[nt], xn1[nt]);
+      }
     }
     if (++jb == group) {
       jb = 0;
@@ -640,9 +663,9 @@ __device__ __forceinline__ void rt_body(const RtArgs& a, const int bid, const in
   for (int i = threadIdx.x; i < 2 * C; i += NT) a.partials[(size_t)bid * 2 * C + i] = bsum[i];
 }
 
-template <int W, int D, int STAGE, int R = kRtRows>
+template <int W, int D, int STAGE, int R = kRtRows, bool CPX = false>
 __global__ void __launch_bounds__(W * 32, 1) k_cheb_rt(const __grid_constant__ RtArgs a) {
-  rt_body<W, D, STAGE, R>(a, (int)blockIdx.x, (int)gridDim.x);
+  rt_body<W, D, STAGE, R, false, CPX>(a, (int)blockIdx.x, (int)gridDim.x);
 }
 
 // ---------------------------------------------------------------- batched flakes, one launch
@@ -746,10 +769,10 @@ __global__ void __launch_bounds__(W * 32, 1) k_cheb_rt_batch(const __grid_consta
 // columns in the interleaved order, the values in fragment order (lane 4g + t
 // holds V[g][t], V[g][t+4] of each n-tile of 8 rows in turn), entries of one
 // (row, column) summed in entry order.
-template <int R>
+template <int R, bool CPX = false>
 __global__ void __launch_bounds__(kRtBuildWarps * 32)
     k_rt_build(int64_t n, int64_t nrb, const int64_t* __restrict__ prow, const int32_t* __restrict__ pcol,
-               const float* __restrict__ pval, int pass, int64_t* __restrict__ kst,
+               const float* __restrict__ pval, const float* __restrict__ pim, int pass, int64_t* __restrict__ kst,
                const int64_t* __restrict__ kstart, unsigned char* __restrict__ data, int* __restrict__ err,
                unsigned long long* __restrict__ ssum) {
   extern __shared__ __align__(16) unsigned char rt_build_smem[];
@@ -757,17 +780,20 @@ __global__ void __launch_bounds__(kRtBuildWarps * 32)
   unsigned long long* keys = reinterpret_cast<unsigned long long*>(rt_build_smem + (size_t)w * kRtBuildSlice);
   uint32_t* list = reinterpret_cast<uint32_t*>(rt_build_smem + (size_t)w * kRtBuildSlice + (size_t)kRtMaxEnt * 8);
   const int64_t warps = (int64_t)gridDim.x * kRtBuildWarps;
+  // rows of a block: R, or 8 for a complex H (its values and imaginary parts in
+  // n-tiles 0 and 1 of the 16-row k-step layout)
+  constexpr int RB = CPX ? 8 : R;
   for (int64_t b = (int64_t)blockIdx.x * kRtBuildWarps + w; b < nrb; b += warps) {
-    const int64_t r0 = b * R;
-    const int rows = (int)min((int64_t)R, n - r0);
-    const int64_t mine = lane <= R ? prow[r0 + min(lane, rows)] : 0;
-    int64_t srp[R + 1];
+    const int64_t r0 = b * RB;
+    const int rows = (int)min((int64_t)RB, n - r0);
+    const int64_t mine = lane <= RB ? prow[r0 + min(lane, rows)] : 0;
+    int64_t srp[RB + 1];
 #pragma unroll
-    for (int k = 0; k <= R; ++k) srp[k] = __shfl_sync(0xffffffffu, mine, k);
+    for (int k = 0; k <= RB; ++k) srp[k] = __shfl_sync(0xffffffffu, mine, k);
     auto srp_at = [&](int k) {
       int64_t v = srp[0];
 #pragma unroll
-      for (int kk = 1; kk <= R; ++kk)
+      for (int kk = 1; kk <= RB; ++kk)
         if (k == kk) v = srp[kk];
       return v;
     };
@@ -775,7 +801,7 @@ __global__ void __launch_bounds__(kRtBuildWarps * 32)
     auto row_of = [&](int e) {
       int r = 0;
 #pragma unroll
-      for (int k = 1; k < R; ++k) r += (k < rows && srp[k] - srp[0] <= e) ? 1 : 0;
+      for (int k = 1; k < RB; ++k) r += (k < rows && srp[k] - srp[0] <= e) ? 1 : 0;
       return r;
     };
     const int64_t q0 = srp[0];
@@ -912,7 +938,9 @@ __global__ void __launch_bounds__(kRtBuildWarps * 32)
         for (int i = lane; i < E; i += 32) {
           const uint32_t c = (uint32_t)pcol[q0 + i];
           const int s2 = (int)((keys[find(c)] >> 16) & 0xFFFFu);
-          *val_at(s2, row_of(i)) = pval[q0 + i];
+          const int r = row_of(i);
+          *val_at(s2, r) = pval[q0 + i];
+          if constexpr (CPX) *val_at(s2, r + 8) = pim[q0 + i];
         }
         continue;
       }
@@ -972,15 +1000,17 @@ __global__ void __launch_bounds__(kRtBuildWarps * 32)
       // the first entry of each (column, row) run sums the run in entry order
       const bool run_start = new_col || row_of((int)(keys[i - 1] & 0xFFFFu)) != r;
       if (run_start) {
-        float v = pval[q0 + e];
+        float v = pval[q0 + e], vi = CPX ? pim[q0 + e] : 0.f;
         for (int i2 = i + 1; i2 < E; ++i2) {
           const unsigned long long k2 = keys[i2];
           if ((uint32_t)(k2 >> 16) != c) break;
           const int e2 = (int)(k2 & 0xFFFFu);
           if (row_of(e2) != r) break;
           v += pval[q0 + e2];
+          if constexpr (CPX) vi += pim[q0 + e2];
         }
         *val_at(s, r) = v;
+        if constexpr (CPX) *val_at(s, r + 8) = vi;
       }
     }
   }
@@ -1086,17 +1116,19 @@ void csr_drop_rt(leo2d_csr* csr) {
 }
 
 bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chunk, int rows, int max_grid) {
-  LEO_REQUIRE(csr->reordered && !csr->complex_h, "the tensor-core row-block step needs the real locality-ordered copy");
+  LEO_REQUIRE(csr->reordered, "the tensor-core row-block step needs the locality-ordered copy");
   LEO_REQUIRE(rows == 8 || rows == 16, "tensor-core row blocks hold 8 or 16 rows");
+  const bool cpx = csr->complex_h;
+  LEO_REQUIRE(!cpx || (rows == 8 && csr->pval_im32.p), "a complex Hamiltonian takes 8-row blocks");
   const int64_t n = csr->n;
-  const int KB = rt_step_bytes(rows);
+  const int KB = rt_step_bytes(cpx ? 16 : rows);  // complex: real and imaginary panels
   const RtShape sh = rt_shape(ctx, n, warps, group, chunk, rows, max_grid);
   if (csr->rt_built && csr->rt_rows == rows && csr->rt_patch == csr->reorder_patch &&
       csr->rt_curve == csr->reorder_curve && csr->rt_warps == warps && csr->rt_group == group &&
       csr->rt_chunk == chunk && csr->rt_grid == sh.grid)
     return true;
   const size_t smem = (size_t)kRtBuildWarps * kRtBuildSlice;
-  auto build_kernel = rows == 16 ? k_rt_build<16> : k_rt_build<8>;
+  auto build_kernel = cpx ? k_rt_build<16, true> : rows == 16 ? k_rt_build<16> : k_rt_build<8>;
   LEO_CUDA(cudaFuncSetAttribute(build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const unsigned bgrid = grid_for(sh.nrb * 32, kRtBuildWarps * 32, (int64_t)ctx->sm_count * 8);
   DevBuf<int> err(2);
@@ -1109,8 +1141,8 @@ bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chun
     csr->rt_kst.alloc(std::max<int64_t>(sh.nrb, 1));
     launch(ctx, "rt_build", [&] {
       build_kernel<<<bgrid, kRtBuildWarps * 32, smem, ctx->stream>>>(n, sh.nrb, csr->prow.p, csr->pcol.p,
-                                                                       csr->pval32.p, 0, csr->rt_kst.p, nullptr,
-                                                                       nullptr, err.p, ssum.p);
+                                                                       csr->pval32.p, nullptr, 0, csr->rt_kst.p,
+                                                                       nullptr, nullptr, err.p, ssum.p);
     });
     int h[2] = {0, 0};
     unsigned long long hs = 0;
@@ -1174,8 +1206,9 @@ bool csr_build_rt(leo2d_ctx* ctx, leo2d_csr* csr, int warps, int group, int chun
   launch(ctx, "rt_build", [&] {
     // pass 1 reads each block's k-step count (kst) and writes nothing to it
     build_kernel<<<bgrid, kRtBuildWarps * 32, smem, ctx->stream>>>(n, sh.nrb, csr->prow.p, csr->pcol.p,
-                                                                     csr->pval32.p, 1, csr->rt_kst.p, kstart.p,
-                                                                     csr->rt_data.p, err.p, ssum.p);
+                                                                     csr->pval32.p, cpx ? csr->pval_im32.p : nullptr,
+                                                                     1, csr->rt_kst.p, kstart.p, csr->rt_data.p,
+                                                                     err.p, ssum.p);
   });
   int h0 = 0;
   d2h(ctx, &h0, err.p, 1);
@@ -1247,7 +1280,8 @@ void rt_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
   LEO_REQUIRE(csr->rt_built && csr->rt_warps == shape.rt_warps && csr->rt_grid == grid &&
                   csr->rt_rows == shape.rt_rows,
               "tensor-core row blocks built for another launch shape");
-  LEO_REQUIRE(smem >= rt_smem_bytes(shape.rt_warps, shape.rt_depth, shape.rt_stage, shape.rt_rows),
+  LEO_REQUIRE(smem >= rt_smem_bytes(shape.rt_warps, shape.rt_depth, shape.rt_stage,
+                                    csr->complex_h ? 16 : shape.rt_rows),
               "tensor-core row-block step: shared memory changed since setup");
   RtArgs a{};
   if (shape.rt_stage == kRtTma) {
@@ -1279,6 +1313,15 @@ void rt_launch_step(leo2d_ctx* ctx, const leo2d_csr* csr, const StepShape& shape
     launch(ctx, "cheb_step", [&] { kern<<<grid, warps * 32, smem, ctx->stream>>>(a); });
   };
   const int key = shape.rt_warps * 10 + shape.rt_depth;
+  if (csr->complex_h) {
+    if (shape.rt_stage == kRtCpAsync && shape.rt_rows == 8)
+      switch (key) {
+        case 123: return go(k_cheb_rt<12, 3, kRtCpAsync, 16, true>, 12);
+        case 163: return go(k_cheb_rt<16, 3, kRtCpAsync, 16, true>, 16);
+      }
+    fail(LEO2D_ERR_BAD_ARG,
+         "complex 8-row step: shared memory by cp.async (stage 1), warps 12 or 16, depth 3");
+  }
   if (shape.rt_rows == 16) {
     if (shape.rt_stage == kRtCpAsync)
       switch (key) {

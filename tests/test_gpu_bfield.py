@@ -181,3 +181,37 @@ def test_bloch_phase_on_a_flake_is_a_gauge(ctx):
     targets = np.array([5, 100, 333])
     cfg = L.kpm_cfg(64, precision=L.FP32)
     assert _rel(ck.kpm_ldos(cfg, targets), c0.kpm_ldos(cfg, targets)) < FP32_RTOL
+
+
+@pytest.mark.parametrize("warps", [16, 12])
+def test_complex_eight_row_step(ctx, warps):
+    """The complex 8-row tensor-core step (step_kernel 5): real and imaginary value
+    panels of each 8-row block, the complex product combined per column pair at
+    the block's end. Against the 4-row complex step to 2e-5 and the oracle's
+    complex recursion to the FP32 bar, with random-phase and host start vectors,
+    on a flake whose row count leaves a partial last block."""
+    g = L.make_geom(model=L.MODEL_SIMPLE, size=40, max_R=69.0, angles_deg=(0.0, 2.0), energy_rescale=1.0,
+                    b_field=300.0)
+    csr = ctx.build_csr(ctx.prepare(g))
+    assert csr.n % 8 != 0  # 11,438 orbitals
+    lo, hi = csr.bounds()
+    csr.rescale(1.01 * (hi - lo) / 2, -(hi + lo) / 2)
+    rp, col, val = csr.download()
+    im = csr.download_imag()
+    P, R, seed = 96, 16, 11
+    cfg = L.kpm_cfg(P, R=R, kind=L.VEC_PHASE, precision=L.FP32, seed=seed)
+    rb = csr.kpm_dos(cfg)  # the 4-row complex step (the default)
+    ctx.set_option("step_kernel", 5)
+    ctx.set_option("rt_warps", warps)
+    try:
+        mu = csr.kpm_dos(cfg)
+        assert csr.rt_info()[0] == (csr.n + 7) // 8
+        vec = np.random.default_rng(3).normal(size=(5, csr.n))
+        host = csr.kpm_dos(L.kpm_cfg(P, R=5, kind=L.VEC_HOST, precision=L.FP32), vec)
+    finally:
+        ctx.set_option("step_kernel", -1)
+        ctx.set_option("rt_warps", 0)
+    assert _rel(mu, rb) < 2e-5
+    re_v, im_v = oracle.phase_vectors(seed, 0, R, csr.n)
+    assert _rel(mu, oracle.kpm_trace_cpx_doubling(rp, col, val, im, re_v, im_v, P)) < FP32_RTOL
+    assert _rel(host, oracle.kpm_trace_cpx(rp, col, val, im, vec, P)) < FP32_RTOL

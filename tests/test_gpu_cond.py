@@ -164,3 +164,27 @@ def test_velocity_step_variants(ctx):
         ctx.set_option("rb_packed", -1)
         ctx.set_option("rb_unroll", 0)
         assert _rel(got, base) < 1e-6, (w, p, u)
+
+
+def test_velocity_in_step_on_an_ordered_flake(ctx):
+    """With the locality ordering on (what a flake of 1e5 orbitals or more gets by
+    default), the DOS default is the 8-row step; the Kubo trace must still take the
+    4-row velocity step for the A side, with the B side on the 8-row step, and
+    need no stored dxH."""
+    csr = _flake(ctx, 13, 3.0, with_dx=False)
+    ref_csr = _flake(ctx, 13, 3.0)
+    M, R, seed = 32, 16, 5
+    cfg = L.kpm_cfg(M, R=R, kind=L.VEC_PHASE, seed=seed)
+    ctx.set_option("reorder", 1)
+    try:
+        fly = csr.kpm_cond(cfg)
+        assert csr.rb_info()[0] == (csr.n + 3) // 4  # the velocity step's 4-row blocks
+        assert csr.rt_info()[0] == (csr.n + 7) // 8  # the B side's 8-row blocks
+    finally:
+        ctx.set_option("reorder", -1)
+    stored = _opts(ctx, lambda: ref_csr.kpm_cond(cfg), kubo_velocity=0)
+    assert _rel(fly, stored) < 2e-5
+    rp, col, val, dx, dy = ref_csr.download(dx=True)
+    re, im = oracle.phase_vectors(seed, 0, R, csr.n)
+    ref = (oracle.kpm_cond_trace(rp, col, val, dx, re, M) + oracle.kpm_cond_trace(rp, col, val, dx, im, M)) / R
+    assert _rel(fly, ref) < FP32_RTOL
