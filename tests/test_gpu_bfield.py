@@ -44,20 +44,29 @@ def test_complex_csr_matches_reference(ctx, name):
     np.testing.assert_allclose(im, gold["val_im"], rtol=0, atol=1e-15 * scale)
 
 
+@pytest.mark.parametrize("kernel", [-1, 5])
 @pytest.mark.parametrize("name", COMPLEX_CASES)
-def test_complex_moments_match_reference(ctx, name):
+def test_complex_moments_match_reference(ctx, name, kernel):
+    """The reference's complex moments (fields on flakes and supercells, k points),
+    with the default step and with the complex 8-row tensor-core step."""
     gold = load(name)
     g, kv = parse_in(name)
     meta = gold["meta"]
     P, trace = int(meta[5]), int(meta[6])
     csr = ctx.build_csr(ctx.prepare(g), keep_zeros=True)
-    if trace == 1:
-        R = int(meta[4])
-        vec = oracle.reference_gaussian(R, csr.n)
-        mu = csr.kpm_dos(L.kpm_cfg(P, R=R, kind=L.VEC_HOST, precision=L.FP32), vec)
-    else:
-        tg = gold["targets"].astype(np.int64)
-        mu = csr.kpm_ldos(L.kpm_cfg(P, precision=L.FP32), tg)
+    ctx.set_option("step_kernel", kernel)
+    try:
+        if trace == 1:
+            R = int(meta[4])
+            vec = oracle.reference_gaussian(R, csr.n)
+            mu = csr.kpm_dos(L.kpm_cfg(P, R=R, kind=L.VEC_HOST, precision=L.FP32), vec)
+        else:
+            tg = gold["targets"].astype(np.int64)
+            mu = csr.kpm_ldos(L.kpm_cfg(P, precision=L.FP32), tg)
+        if kernel == 5:
+            assert csr.rt_info()[0] == (csr.n + 7) // 8
+    finally:
+        ctx.set_option("step_kernel", -1)
     ref = gold["moments"].reshape(mu.shape)
     assert _rel(mu, ref) < FP32_RTOL
 
