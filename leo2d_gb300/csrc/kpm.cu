@@ -521,6 +521,13 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
       s.cols = c;
     }
   }
+  if (csr->complex_h) {
+    // a complex H runs on the row-block steps only: 16 complex vectors (32
+    // columns), FP32, also when fewer columns are needed (a few LDOS targets)
+    LEO_REQUIRE(!fp64, "a complex Hamiltonian (magnetic field) runs in FP32");
+    LEO_REQUIRE(s.cols == 32 || requested_cols <= 0, "a complex Hamiltonian takes 32-column blocks");
+    s.cols = 32;
+  }
   auto it = g_shape_cache.find({ctx, ShapeKey{csr, csr->n, csr->nnz, fp64, s.cols}});
   s.rows_per_item = requested_rows > 0 ? requested_rows : (it != g_shape_cache.end() ? it->second.rows : 0);
   if (ctx->tile_warps > 0) s.warps = ctx->tile_warps;
@@ -542,10 +549,6 @@ StepShape choose_shape(leo2d_ctx* ctx, const leo2d_csr* csr, bool fp64, int cols
   if (s.rt) s.rb = false;
   if (s.rb || s.rt) s.tc = false;
   if (csr->complex_h) {
-    // a complex H runs on the row-block step only: 16 complex vectors (32 columns), FP32
-    LEO_REQUIRE(!fp64, "a complex Hamiltonian (magnetic field) runs in FP32");
-    LEO_REQUIRE(s.cols == 32 || requested_cols <= 0, "a complex Hamiltonian takes 32-column blocks");
-    s.cols = 32;
     s.rb = !s.rt;  // the 4-row step, or the 8-row step when asked for
     s.tc = false;
     s.tiled = true;
