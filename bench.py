@@ -236,11 +236,24 @@ def kernel_case(args):
         k, ms = ctx.kernel_stats("cheb_step")
         nnz_true = csr.nnz
         gbs = step_bytes(csr.n, nnz_true, args.kernel_case) / (ms / k * 1e-3) / 1e9
+        # a second build of the same flake: the assembly kernel's CUDA-event time
+        # and the whole build's wall time
+        ctx.reset_stats()
+        ctx.set_profiling(True)
+        gp = ctx.prepare(geom(L, radius=radius))
+        t0 = time.perf_counter()
+        c2 = ctx.build_csr(gp)
+        build_ms = (time.perf_counter() - t0) * 1e3
+        ctx.set_profiling(False)
+        ka, asm_ms = ctx.kernel_stats("flake_rows_fill")
+        c2.close()
         print(json.dumps({"kernel_case": {"n": csr.n, "nnz": csr.nnz, "cols": args.kernel_case,
                                           "step_kernel": args.step_kernel, "radius_A": radius,
                                           "step_kernel_run": csr.step_kernel(cfg)[0],
                                           "rb_info": list(csr.rb_info()), "rt_info": list(csr.rt_info()),
-                                          "step_ms": round(ms / k, 4), "step_gbs": round(gbs, 1)}}))
+                                          "step_ms": round(ms / k, 4), "step_gbs": round(gbs, 1),
+                                          "assembly_kernel_ms": round(asm_ms / max(ka, 1), 3),
+                                          "build_ms": round(build_ms, 2)}}))
 
 
 # ---------------------------------------------------------------- learned control variate

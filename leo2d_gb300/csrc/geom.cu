@@ -41,6 +41,9 @@ constexpr int kMaxSheets = LEO2D_MAX_SHEETS;
 constexpr int kIntraSearch = 4;    // (int) Graphene::intra_search_radius (graphene.h:94)
 constexpr int kInterSearch = 6;    // (int) Graphene::inter_search_radius (graphene.h:95)
 constexpr double kInterCutoff = 12.5;  // hstruct.cpp:310
+constexpr int kIntraShellMax = 16;     // no intralayer hopping beyond this neighbour shell
+constexpr int kRowWarps = 8;           // k_flake_rows: warps (rows in flight) per 256-thread block
+constexpr int kInterSeg = 288;         // k_flake_rows: interlayer candidates per segment (a 12 x 12 x 2 window)
 
 struct SheetDev {
   int min0, min1, max0, max1, H, W, n_orb;
@@ -65,6 +68,12 @@ struct GeomDev {
   double e_field;     // USE_E_FIELD's E: the diagonal gains z E (Locality::onSiteE)
   double b_field;  // non-zero: complex entries t e^{i phi} (Peierls phase)
   double kx, ky;   // Bloch vector: phases k.(r_col - r_row) per periodic image
+  // the flake rows' quotients, taken once on the host (IEEE division, the same
+  // bits as per entry): intra_q[r] = t(r) / rescale for the shells r <=
+  // kIntraShellMax, diag_q = (t(0) + shift) / rescale (used without a field E)
+  double intra_q[kIntraShellMax + 1];
+  double diag_q;
+  int diag_const;  // no field E: every diagonal entry is diag_q
   int cpx;         // complex entries (a field or a Bloch vector)
   int shifted;     // some sheet is shifted: values from the shifted positions
   SheetDev sh[kMaxSheets];
@@ -118,13 +127,16 @@ __device__ __forceinline__ int find_nearest_h(const SheetDev& s, const double p[
   return min(max(int(floor(j_new)), s.min1), s.max1) - s.min1;
 }
 
-// Coupling::Intralayer::graphene (graphene.cpp:13-89) and the simple model.
-__device__ __forceinline__ double intralayer(int model, int orow, int ocol, int d0, int d1) {
+// Coupling::Intralayer::graphene (graphene.cpp:13-89) and the simple model:
+// the neighbour shell r of a grid offset, and the shell's hopping.
+__device__ __forceinline__ int intra_shell(int orow, int ocol, int d0, int d1) {
   int h0 = 2 * d0 + d1;
   const int h1 = -1 * d0 + d1;
   if (ocol == 0 && orow == 1) h0 -= 1;
   else if (ocol == 1 && orow == 0) h0 += 1;
-  const int r = h0 * (h0 + h1) + h1 * h1;
+  return h0 * (h0 + h1) + h1 * h1;
+}
+__host__ __device__ inline double intra_shell_t(int model, int r) {
   if (model == LEO2D_MODEL_SIMPLE) return r == 1 ? -2.7 : 0.0;
   switch (r) {
     case 0: return 0.3504;
@@ -138,6 +150,9 @@ __device__ __forceinline__ double intralayer(int model, int orow, int ocol, int 
     case 16: return -0.0211;
     default: return 0.;
   }
+}
+__device__ __forceinline__ double intralayer(int model, int orow, int ocol, int d0, int d1) {
+  return intra_shell_t(model, intra_shell(orow, ocol, d0, d1));
 }
 
 // Coupling::Interlayer::C_to_C (graphene.cpp:91-222). abs() at graphene.cpp:117
@@ -291,12 +306,18 @@ __device__ __forceinline__ double peierls_phase(double x1, double x2, double y1,
   return pre * B * (x2 - x1) * (0.5) * (y1 + y2);
 }
 
+// t != 0 on the integer pipe (GB300's FP64 unit is the assembly's bottleneck):
+// false for +0.0 and -0.0 only, as the FP64 comparison
+__device__ __forceinline__ bool t_nonzero(double t) {
+  return ((unsigned long long)__double_as_longlong(t) << 1) != 0ull;
+}
+
 // One stored entry: real H (value t) or, in a field, std::polar(t, phi) as
 // generateCpxH adds it (locality.cpp:4896-4941: zero couplings stay 0).
 __device__ __forceinline__ void store_value(const GeomDev& G, const RowOut& out, int64_t e, double t, double x1,
                                             double y1, double x2, double y2) {
   if (!G.cpx) {
-    out.val[e] = t != 0 ? 0.0 + t : 0.0;
+    out.val[e] = t_nonzero(t) ? t : 0.0;  // (0.0 + t of a non-zero t is t; -0.0 is stored as 0.0)
     return;
   }
   if (t == 0) {
@@ -336,13 +357,17 @@ constexpr float kPrefilterMargin = 0.05f;
 // and count in one pass, row r at r * pad_cap of padded arrays (entries past
 // pad_cap are counted, not stored, and raise `overflow`).
 template <int kMode>
-__global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ GeomDev G, int64_t n,
+__global__ void __launch_bounds__(kRowWarps * 32, 3) k_flake_rows(const __grid_constant__ GeomDev G, int64_t n,
                                                     const int32_t* __restrict__ grid4,
                                                     const double* __restrict__ pos,
                                                     const float4* __restrict__ pos32,
                                                     const double* __restrict__ spos,
                                                     const float4* __restrict__ spos32, RowOut out) {
   constexpr bool kFill = kMode != 0, kPad = kMode == 2;
+  // per warp: the interlayer segment's candidate codes, queue and hoppings
+  __shared__ int32_t s_code[kRowWarps][kInterSeg];
+  __shared__ int16_t s_queue[kRowWarps][kInterSeg];
+  __shared__ double s_hop[kRowWarps][kInterSeg];
   const unsigned lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -378,14 +403,18 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
           const int k2 = grid_to_index(sh, i, j, l);
           if (k2 != -1) {
             k2g = k2 + sh.base;
-            const double raw = intralayer(G.model, l0, l, i - ih, j - jh);
-            // (0 / rescale is 0: the FP64 division runs for nonzero entries only)
-            t = k2g == row ? diag_value(G, raw, sz1) : (raw != 0.0 ? raw / G.rescale : 0.0);
+            // the quotients by the rescale from the host's table; a field E
+            // makes the diagonal depend on the orbital's height
+            const int r = intra_shell(l0, l, i - ih, j - jh);
+            if (k2g == row)
+              t = G.diag_const ? G.diag_q : diag_value(G, intra_shell_t(G.model, r), sz1);
+            else
+              t = r <= kIntraShellMax ? G.intra_q[r] : 0.0;
           }
         }
         const bool keep = k2g >= 0;
         // without KEEP_ZEROS the diagonal stays so a later rescale can shift it
-        const bool store = keep && (G.keep_zeros || t != 0 || k2g == row);
+        const bool store = keep && (G.keep_zeros || t_nonzero(t) || k2g == row);
         const unsigned m = __ballot_sync(0xffffffffu, store);
         n_intra += __popc(__ballot_sync(0xffffffffu, keep));
         if (kFill && store && (!kPad || o + __popc(m & lt_mask) < o_end)) {
@@ -403,14 +432,25 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
       }
     }
 
-    // interlayer: sheet below, then sheet above; window +-6 clipped; d_xy < 12.5 A
+    // interlayer: sheet below, then sheet above; window +-6 clipped; d_xy < 12.5 A.
+    // Most candidates of the window have no hopping (beyond 8 A), so the FP64
+    // hoppings are not taken where the candidates fall, which would leave most
+    // lanes of GB300's small FP64 unit idle. Per segment of up to kInterSeg
+    // candidates: (1) the FP32 tests mark each candidate (outside the window;
+    // inside without a hopping to evaluate; inside with one) and queue the
+    // last kind in the warp's shared memory, in candidate order; (2) the FP64
+    // hoppings of the queue, on every lane; (3) the entries in candidate
+    // order, as a single pass would write them.
     {
       const double ph[3] = {x1, y1, z1};
-      const float x1f = (float)x1, y1f = (float)y1, z1f = (float)z1;
+      const float x1f = (float)x1, y1f = (float)y1;
       const float sx1f = (float)sx1, sy1f = (float)sy1, sz1f = (float)sz1;
       constexpr float kWinLo = (float)(kInterCutoff - kPrefilterMargin), kWinHi = (float)(kInterCutoff + kPrefilterMargin);
       // every hopping is zero from 8 A on (in-plane for the reference model, 3-D for the simple one)
       constexpr float kHopHi = 8.0f + kPrefilterMargin, kHopLo = 8.0f - kPrefilterMargin;
+      int32_t* const seg_code = s_code[threadIdx.x >> 5];
+      int16_t* const seg_queue = s_queue[threadIdx.x >> 5];
+      double* const seg_t = s_hop[threadIdx.x >> 5];
       for (int side_k = 0; side_k < 2; ++side_k) {
         const int s0 = side_k == 0 ? s - 1 : s + 1;
         if (s0 < 0 || s0 >= G.S) continue;
@@ -421,70 +461,115 @@ __global__ void __launch_bounds__(256) k_flake_rows(const __grid_constant__ Geom
         if (ihi <= ilo || jhi <= jlo) continue;
         const int wj = jhi - jlo;
         const int nc = (ihi - ilo) * wj * o0.n_orb;
-        for (int c0 = 0; c0 < nc; c0 += 32) {
-          const int c = c0 + (int)lane;
-          int64_t k2g = -1;
-          double t = 0.0;
-          if (c < nc) {
-            const int l = c % o0.n_orb;
-            const int j = jlo + (c / o0.n_orb) % wj;
-            const int i = ilo + c / (o0.n_orb * wj);
-            const int k2 = grid_to_index(o0, i, j, l);
-            if (k2 != -1) {
-              const int64_t kk = k2 + o0.base;
-              const float4 q = pos32[kk];
-              const float dxf = q.x - x1f, dyf = q.y - y1f;
-              const float d2f = dxf * dxf + dyf * dyf;
-              bool in_window;
-              if (d2f < kWinLo * kWinLo) {
-                in_window = true;
-              } else if (d2f > kWinHi * kWinHi) {
-                in_window = false;
-              } else {
-                const double x2 = pos[3 * kk], y2 = pos[3 * kk + 1];
-                in_window = (x2 - ph[0]) * (x2 - ph[0]) + (y2 - ph[1]) * (y2 - ph[1]) < kInterCutoff * kInterCutoff;
-              }
-              if (in_window) {
-                k2g = kk;
-                // the hopping cutoffs test the shifted positions
-                const float4 sq = G.shifted ? spos32[kk] : q;
-                const float hdx = sq.x - sx1f, hdy = sq.y - sy1f, hdz = sq.z - sz1f;
-                const float hd2 = hdx * hdx + hdy * hdy;
-                const float h2f = G.model == LEO2D_MODEL_SIMPLE ? hd2 + hdz * hdz : hd2;
-                if (!kFill && !G.keep_zeros && G.model == LEO2D_MODEL_SIMPLE && h2f < kHopHi * kHopHi) {
-                  // counting only needs t != 0: the simple model's hopping (and its
-                  // quotient by a finite rescale) is non-zero exactly when the FP64
-                  // distance of `interlayer` is below 8 A; FP32 decides away from 8 A
-                  bool nz = h2f < kHopLo * kHopLo;
-                  if (!nz) {
-                    const double v0 = spos[3 * kk] - sx1, v1 = spos[3 * kk + 1] - sy1, v2 = spos[3 * kk + 2] - sz1;
-                    nz = sqrt(v0 * v0 + v1 * v1 + v2 * v2) < 8.0;
-                  }
-                  t = nz ? 1.0 : 0.0;
-                } else if ((kFill || !G.keep_zeros) && h2f < kHopHi * kHopHi) {
-                  const double x2 = spos[3 * kk], y2 = spos[3 * kk + 1], z2 = spos[3 * kk + 2];
-                  t = interlayer_t(G.model, l0, l, x2 - sx1, y2 - sy1, z2 - sz1, sh.angle, o0.angle, G.rescale,
-                                   G.simple_amp);
+        for (int seg0 = 0; seg0 < nc; seg0 += kInterSeg) {
+          const int seg_n = min(kInterSeg, nc - seg0);
+          // (1) code: -1 outside the window, else the column with bit 31 set
+          // when its hopping is to be evaluated (columns are below 2^31 - 1)
+          int qn = 0;
+          for (int c0 = 0; c0 < seg_n; c0 += 32) {
+            const int slot = c0 + (int)lane;
+            bool queue = false;
+            if (slot < seg_n) {
+              const int c = seg0 + slot;
+              int32_t code = -1;
+              const int l = c % o0.n_orb;
+              const int j = jlo + (c / o0.n_orb) % wj;
+              const int i = ilo + c / (o0.n_orb * wj);
+              const int k2 = grid_to_index(o0, i, j, l);
+              if (k2 != -1) {
+                const int64_t kk = k2 + o0.base;
+                const float4 q = pos32[kk];
+                const float dxf = q.x - x1f, dyf = q.y - y1f;
+                const float d2f = dxf * dxf + dyf * dyf;
+                bool in_window;
+                if (d2f < kWinLo * kWinLo) {
+                  in_window = true;
+                } else if (d2f > kWinHi * kWinHi) {
+                  in_window = false;
+                } else {
+                  const double x2 = pos[3 * kk], y2 = pos[3 * kk + 1];
+                  in_window = (x2 - ph[0]) * (x2 - ph[0]) + (y2 - ph[1]) * (y2 - ph[1]) < kInterCutoff * kInterCutoff;
+                }
+                if (in_window) {
+                  // the hopping cutoffs test the shifted positions
+                  const float4 sq = G.shifted ? spos32[kk] : q;
+                  const float hdx = sq.x - sx1f, hdy = sq.y - sy1f, hdz = sq.z - sz1f;
+                  const float hd2 = hdx * hdx + hdy * hdy;
+                  const float h2f = G.model == LEO2D_MODEL_SIMPLE ? hd2 + hdz * hdz : hd2;
+                  queue = (kFill || !G.keep_zeros) && h2f < kHopHi * kHopHi;
+                  code = (int32_t)((uint32_t)kk | (queue ? 0x80000000u : 0u));
                 }
               }
+              seg_code[slot] = code;
+            }
+            const unsigned qm = __ballot_sync(0xffffffffu, queue);
+            if (queue) seg_queue[qn + __popc(qm & lt_mask)] = (int16_t)slot;
+            qn += __popc(qm);
+          }
+          __syncwarp();
+          // (2) the queued hoppings
+          for (int q0 = 0; q0 < qn; q0 += 32) {
+            const int qi = q0 + (int)lane;
+            if (qi < qn) {
+              const int slot = seg_queue[qi];
+              const int64_t kk = (int64_t)((uint32_t)seg_code[slot] & 0x7fffffffu);
+              double t;
+              if (!kFill && !G.keep_zeros && G.model == LEO2D_MODEL_SIMPLE) {
+                // counting only needs t != 0: the simple model's hopping (and its
+                // quotient by a finite rescale) is non-zero exactly when the FP64
+                // distance of `interlayer` is below 8 A; FP32 decides away from 8 A
+                const float4 sq = G.shifted ? spos32[kk] : pos32[kk];
+                const float hdx = sq.x - sx1f, hdy = sq.y - sy1f, hdz = sq.z - sz1f;
+                bool nz = hdx * hdx + hdy * hdy + hdz * hdz < kHopLo * kHopLo;
+                if (!nz) {
+                  const double v0 = spos[3 * kk] - sx1, v1 = spos[3 * kk + 1] - sy1, v2 = spos[3 * kk + 2] - sz1;
+                  nz = sqrt(v0 * v0 + v1 * v1 + v2 * v2) < 8.0;
+                }
+                t = nz ? 1.0 : 0.0;
+              } else {
+                const int l = (seg0 + slot) % o0.n_orb;
+                const double x2 = spos[3 * kk], y2 = spos[3 * kk + 1], z2 = spos[3 * kk + 2];
+                t = interlayer_t(G.model, l0, l, x2 - sx1, y2 - sy1, z2 - sz1, sh.angle, o0.angle, G.rescale,
+                                 G.simple_amp);
+              }
+              seg_t[qi] = t;
             }
           }
-          const bool keep = k2g >= 0;
-          const bool store = keep && (G.keep_zeros || t != 0);
-          const unsigned m = __ballot_sync(0xffffffffu, store);
-          n_inter += __popc(__ballot_sync(0xffffffffu, keep));
-          if (kFill && store && (!kPad || o + __popc(m & lt_mask) < o_end)) {
-            const int64_t e = o + __popc(m & lt_mask);
-            out.col[e] = (int32_t)k2g;
-            const double x2 = spos[3 * k2g], y2 = spos[3 * k2g + 1];
-            store_value(G, out, e, t, sx1, sy1, x2, y2);
-            if (G.with_dx) {
-              out.dx[e] = t != 0 ? 0.0 + (sx1 - x2) * t : 0.0;
-              out.dy[e] = t != 0 ? 0.0 + (sy1 - y2) * t : 0.0;
+          __syncwarp();
+          // (3) the entries, in candidate order
+          int qr = 0;
+          for (int c0 = 0; c0 < seg_n; c0 += 32) {
+            const int slot = c0 + (int)lane;
+            int64_t k2g = -1;
+            bool queued = false;
+            if (slot < seg_n) {
+              const int32_t code = seg_code[slot];
+              if (code != -1) {
+                k2g = (int64_t)((uint32_t)code & 0x7fffffffu);
+                queued = code < 0;
+              }
             }
+            const unsigned qm = __ballot_sync(0xffffffffu, queued);
+            const double t = queued ? seg_t[qr + __popc(qm & lt_mask)] : 0.0;
+            qr += __popc(qm);
+            const bool keep = k2g >= 0;
+            const bool store = keep && (G.keep_zeros || t_nonzero(t));
+            const unsigned m = __ballot_sync(0xffffffffu, store);
+            n_inter += __popc(__ballot_sync(0xffffffffu, keep));
+            if (kFill && store && (!kPad || o + __popc(m & lt_mask) < o_end)) {
+              const int64_t e = o + __popc(m & lt_mask);
+              out.col[e] = (int32_t)k2g;
+              const double x2 = spos[3 * k2g], y2 = spos[3 * k2g + 1];
+              store_value(G, out, e, t, sx1, sy1, x2, y2);
+              if (G.with_dx) {
+                out.dx[e] = t != 0 ? 0.0 + (sx1 - x2) * t : 0.0;
+                out.dy[e] = t != 0 ? 0.0 + (sy1 - y2) * t : 0.0;
+              }
+            }
+            o += __popc(m);
+            n_ent += __popc(m);
           }
-          o += __popc(m);
-          n_ent += __popc(m);
+          __syncwarp();
         }
       }
     }
@@ -993,6 +1078,12 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     G.simple_amp = 0.33 / g->energy_rescale;
     G.shift = g->energy_shift;
     G.e_field = g->e_field;
+    for (int r = 0; r <= kIntraShellMax; ++r) {
+      const double raw = intra_shell_t(G.model, r);
+      G.intra_q[r] = raw != 0.0 ? raw / G.rescale : 0.0;
+    }
+    G.diag_const = G.e_field == 0.0 ? 1 : 0;
+    G.diag_q = (intra_shell_t(G.model, 0) + G.shift) / G.rescale;
     for (int s = 0; s < G.S; ++s) fill_sheet(*g, s, G.sh[s]);
 
     // sites of every sheet
@@ -1057,7 +1148,7 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
       LEO_CUDA(cudaFuncSetAttribute(k_periodic_rows<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       LEO_CUDA(cudaFuncSetAttribute(k_periodic_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
-    const unsigned rows_grid = grid_for(n, 8, (int64_t)ctx->sm_count * 64);
+    const unsigned rows_grid = grid_for(n, kRowWarps, (int64_t)ctx->sm_count * 64);
     DevBuf<float4> pos32(G.bc == 0 ? std::max<int64_t>(n, 1) : 1);
     DevBuf<float4> spos32(G.bc == 0 && G.shifted ? std::max<int64_t>(n, 1) : 0);
     if (G.bc == 0 && n > 0)
@@ -1097,7 +1188,7 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
         rp.pad_cap = kPadCap;
         rp.overflow = overflow.p;
         launch(ctx, "flake_rows_fill", [&] {
-          k_flake_rows<2><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, spos,
+          k_flake_rows<2><<<rows_grid, kRowWarps * 32, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, spos,
                                                               spos32p, rp);
         });
         int over = 0;
@@ -1138,7 +1229,7 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     if (n > 0) {
       if (G.bc == 0)
         launch(ctx, "flake_rows_count", [&] {
-          k_flake_rows<0><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, spos,
+          k_flake_rows<0><<<rows_grid, kRowWarps * 32, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, spos,
                                                               spos32p, ro);
         });
       else
@@ -1170,7 +1261,7 @@ extern "C" leo2d_status leo2d_build_csr(leo2d_ctx* ctx, const leo2d_geom* g, uin
     if (n > 0) {
       if (G.bc == 0)
         launch(ctx, "flake_rows_fill", [&] {
-          k_flake_rows<1><<<rows_grid, 256, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, spos,
+          k_flake_rows<1><<<rows_grid, kRowWarps * 32, 0, ctx->stream>>>(G, n, csr->grid4.p, csr->pos.p, pos32.p, spos,
                                                               spos32p, ro);
         });
       else
