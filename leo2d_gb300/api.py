@@ -210,7 +210,13 @@ def k_path(geom, n, k_type=1):
     Supercell zone: K = b2 turned by -30 degrees over 2 cos 30, K' = K turned by
     -60 degrees, M = b2 / 2. Sheet 0's zone: b from its lattice turned by its angle
     (Locality::getReciprocal(int), locality.cpp:7168-7213), M = b1 / 2, K = M
-    turned by 30 degrees over cos 30. Returns [n][2]."""
+    turned by 30 degrees over cos 30. Returns [n][2].
+
+    k_type 4 (locality.cpp:1990-2159): n points on each leg of Gamma -> K -> M ->
+    Gamma in the zone of a bilayer SUPERCELL_M_N cell, walked as the driver
+    walks it (k_path_gkm). Returns [3 n][2]."""
+    if k_type == 4:
+        return k_path_gkm(geom, n)
     gm = [0.0, 0.0]
     if k_type == 1 and geom.num_sheets < 2:  # locality.cpp:1661-1663, as the driver
         raise ValueError("cannot use K_TYPE == 1 (twisted BZ) for a single layer")
@@ -237,7 +243,7 @@ def k_path(geom, n, k_type=1):
                   np.sin(-np.pi / 3) * kk[0] + np.cos(-np.pi / 3) * kk[1]]
             pts = [gm, mm, kk, k2, gm]
     else:
-        raise ValueError("k_type must be 1, 2 or 3")
+        raise ValueError("k_type must be 1, 2, 3 or 4")
     legs = len(pts) - 1
     out = []
     for i in range(n):
@@ -246,6 +252,53 @@ def k_path(geom, n, k_type=1):
         while j < legs - 1 and c > j + 1:
             j += 1
         out.append([((j + 1.0) - c) * pts[j][d] + (c - j) * pts[j + 1][d] for d in range(2)])
+    return np.array(out)
+
+
+def k_path_gkm(geom, nk):
+    """K_TYPE 4's Bloch vectors (locality.cpp:1990-2159): nk points on each leg of
+    Gamma -> K -> M -> Gamma of the zone of the (M, N) supercell of a bilayer,
+    A = [N M; -M M+N] (M > N) or [M N; -N M+N] in sheet 0's unrotated lattice
+    vectors; M = (b1 + b2) / 2 and K = b2 turned by +30 degrees over sqrt 3. Each
+    leg runs by the reference's slope and intercept, in its order of operations
+    (the second leg adds no intercept; the third runs along y from M when M's
+    coordinates are equal). Returns [3 nk][2]."""
+    import math
+    if geom.num_sheets != 2 or geom.boundary_condition != 1 or (geom.supercell_m == 0 and geom.supercell_n == 0):
+        raise ValueError("K_TYPE = 4 samples the zone of a bilayer SUPERCELL_M_N supercell")
+    M, N = geom.supercell_m, geom.supercell_n
+    A11, A12, A21, A22 = (N, M, -M, M + N) if M > N else (M, N, -N, M + N)
+    a = geom.lattice[0]
+    sc = [[A11 * a[0][0] + A12 * a[1][0], A11 * a[0][1] + A12 * a[1][1]],
+          [A21 * a[0][0] + A22 * a[1][0], A21 * a[0][1] + A22 * a[1][1]]]
+    b = _reciprocal(sc)
+    r3, al = math.sqrt(3.0), math.pi / 6
+    rot = [[math.cos(al), math.sin(al)], [-math.sin(al), math.cos(al)]]
+    gm = [0.0, 0.0]
+    m = [0.5 * (b[0][i] + b[1][i]) for i in range(2)]
+    k = [0.0, 0.0]
+    for i in range(2):
+        for j in range(2):
+            k[i] = k[i] + rot[i][j] * b[1][j] / r3
+    s1 = (k[1] - gm[1]) / (k[0] - gm[0])
+    s2 = (m[1] - k[1]) / (m[0] - k[0])
+    s3 = (gm[1] - m[1]) / (gm[0] - m[0])
+    c1 = (k[0] * gm[1] - gm[0] * k[1]) / (k[0] - gm[0])
+    c3 = (gm[0] * m[1] - m[0] * gm[1]) / (gm[0] - m[0])
+    l1, l2, l3 = k[0] - gm[0], m[0] - k[0], gm[0] - m[0]
+    out = []
+    for i in range(3 * nk):
+        if i < nk:
+            out.append([gm[0] + i * l1 / nk, gm[1] + s1 * i * l1 / nk + c1])
+        elif i < 2 * nk:
+            n2 = i - nk
+            out.append([k[0] + n2 * l2 / nk, k[1] + s2 * n2 * l2 / nk])
+        else:
+            n3 = i - 2 * nk
+            if m[0] == m[1]:
+                out.append([m[0], m[1] + n3 * (gm[1] - m[1]) / nk])
+            else:
+                out.append([m[0] + n3 * l3 / nk, m[1] + s3 * n3 * l3 / nk + c3])
     return np.array(out)
 
 

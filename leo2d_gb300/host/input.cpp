@@ -261,7 +261,7 @@ bool parse_input(const std::string& path, JobSpec& spec, std::string& err) {
   // a magnetic field: the complex Hamiltonian of generateCpxH (locality.cpp:2906-2909)
   if (spec.use_e == 1) g.e_field = spec.e_field;
   if (spec.k_sampling == 1) {
-    if (spec.k_type < 0 || spec.k_type > 3) spec.unsupported.push_back("K_TYPE = " + std::to_string(spec.k_type));
+    if (spec.k_type < 0 || spec.k_type > 4) spec.unsupported.push_back("K_TYPE = " + std::to_string(spec.k_type));
     if (g.boundary_condition != 1) spec.unsupported.push_back("K_SAMPLING = 1 with BOUNDARY_CONDITION = 0");
     if (spec.observable_type == 1) spec.unsupported.push_back("K_SAMPLING = 1 with OBSERVABLE_TYPE = COND");
   }

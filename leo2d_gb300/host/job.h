@@ -44,7 +44,7 @@ struct JobSpec {
   double b_field = 0.0;       // B_FIELD, tesla
   int use_e = 0;              // USE_E_FIELD: the on-site z E term
   int k_sampling = 0;         // K_SAMPLING: every job at each point of a k grid (complex H)
-  int k_type = 0;             // K_TYPE (0 = grid of the supercell's Brillouin zone)
+  int k_type = 0;             // K_TYPE (0 = grid of the supercell's Brillouin zone; 1-4 zone paths)
   int num_k1 = 1, num_k2 = 1; // K_GRID
   double e_field = 0.0;       // E_FIELD
   int energies = 0;           // > 0: also write a DOS on this many equispaced energies

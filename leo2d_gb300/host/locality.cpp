@@ -252,6 +252,14 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     err = "cannot use K_TYPE == 1 (twisted BZ) for a single layer";
     return LEO2D_ERR_BAD_ARG;
   }
+  if (spec.k_sampling == 1 && spec.k_type == 4 &&
+      (spec.geom.boundary_condition != 1 || spec.geom.num_sheets != 2 ||
+       (spec.geom.supercell_m == 0 && spec.geom.supercell_n == 0))) {
+    // locality.cpp:1996-2031: the zone of the (M, N) supercell; the two-sheet
+    // grouping is the one setupSupercell gives a bilayer (locality.cpp:156-160)
+    err = "K_TYPE = 4 samples the zone of a bilayer SUPERCELL_M_N supercell";
+    return LEO2D_ERR_UNSUPPORTED;
+  }
   if (spec.k_sampling == 1 && (spec.num_k1 < 1 || (spec.k_type == 0 && spec.num_k2 < 1))) {
     err = "K_GRID must name at least one k point";
     return LEO2D_ERR_BAD_ARG;
@@ -360,7 +368,63 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
     reciprocal(g0.supercell, b);
     std::vector<std::vector<double>> shift_jobs = jobs;
     jobs.clear();
-    if (spec.k_type >= 1) {
+    if (spec.k_type == 4) {
+      // K_TYPE 4 (locality.cpp:1990-2159): 3 NUM_K1 points of the bilayer (M, N)
+      // supercell's zone, Gamma -> K -> M -> Gamma. The zone is that of the
+      // cell A = [N M; -M M+N] (M > N) or [M N; -N M+N] in sheet 0's unrotated
+      // lattice vectors; M = (b1 + b2) / 2, K = b2 turned by +30 degrees over
+      // sqrt 3. Each leg is walked by the reference's slope and intercept, with
+      // its operations in its order: the second leg adds no intercept, and the
+      // third runs along y from M when M's two coordinates are equal.
+      const int Mi = g0.supercell_m, Ni = g0.supercell_n;
+      const int A11 = Mi > Ni ? Ni : Mi, A12 = Mi > Ni ? Mi : Ni;
+      const int A21 = Mi > Ni ? -Mi : -Ni, A22 = Mi + Ni;
+      const auto& a0 = g0.lattice[0];
+      const double sc4[2][2] = {{A11 * a0[0][0] + A12 * a0[1][0], A11 * a0[0][1] + A12 * a0[1][1]},
+                                {A21 * a0[0][0] + A22 * a0[1][0], A21 * a0[0][1] + A22 * a0[1][1]}};
+      double bs[2][2];
+      reciprocal(sc4, bs);
+      const double r3 = std::sqrt(3.0), alpha = M_PI / 6;
+      const double rot30[2][2] = {{std::cos(alpha), std::sin(alpha)}, {-std::sin(alpha), std::cos(alpha)}};
+      const double gm[2] = {0.0, 0.0};
+      double mm[2], kk[2];
+      for (int i = 0; i < 2; ++i) mm[i] = 0.5 * (bs[0][i] + bs[1][i]);
+      for (int i = 0; i < 2; ++i) {
+        kk[i] = 0;
+        for (int j = 0; j < 2; ++j) kk[i] = kk[i] + rot30[i][j] * bs[1][j] / r3;
+      }
+      const double s1 = (kk[1] - gm[1]) / (kk[0] - gm[0]);
+      const double s2 = (mm[1] - kk[1]) / (mm[0] - kk[0]);
+      const double s3 = (gm[1] - mm[1]) / (gm[0] - mm[0]);
+      const double c1 = (kk[0] * gm[1] - gm[0] * kk[1]) / (kk[0] - gm[0]);
+      const double c3 = (gm[0] * mm[1] - mm[0] * gm[1]) / (gm[0] - mm[0]);
+      const double l1 = kk[0] - gm[0], l2 = mm[0] - kk[0], l3 = gm[0] - mm[0];
+      const int nk = spec.num_k1;
+      for (const auto& sj : shift_jobs)
+        for (int i = 0; i < 3 * nk; ++i) {
+          double kx, ky;
+          if (i < nk) {
+            kx = gm[0] + i * l1 / nk;
+            ky = gm[1] + s1 * i * l1 / nk + c1;
+          } else if (i < 2 * nk) {
+            const int n2 = i - nk;
+            kx = kk[0] + n2 * l2 / nk;
+            ky = kk[1] + s2 * n2 * l2 / nk;
+          } else {
+            const int n3 = i - 2 * nk;
+            if (mm[0] == mm[1]) {
+              const double len = gm[1] - mm[1];
+              kx = mm[0];
+              ky = mm[1] + n3 * len / nk;
+            } else {
+              kx = mm[0] + n3 * l3 / nk;
+              ky = mm[1] + s3 * n3 * l3 / nk + c3;
+            }
+          }
+          jobs.push_back(sj);
+          kjobs.push_back({kx, ky});
+        }
+    } else if (spec.k_type >= 1) {
       // k paths (locality.cpp:1655-1990): each job at NUM_K1 points of a path through
       // the corners P_0 .. P_L; point i sits at c = L i / NUM_K1 and on leg j = the
       // first with c <= j + 1 (the last leg takes the rest), at (j+1-c) P_j + (c-j) P_j+1.

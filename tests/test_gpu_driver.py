@@ -96,8 +96,13 @@ def test_unsupported_input_is_refused(tmp_path):
         "POLY_ORDER = 64", "POLY_ORDER = 62"))
     with pytest.raises(L.Leo2dError, match="divisible 4"):
         L.run_input(p, tmp_path)
-    # the k lists of K_TYPE 4 and 5 (trilayer Dirac-point paths) are not built
+    # the k list of K_TYPE 5 (the trilayer's Dirac points) is not built
     p.write_text(open(os.path.join(GOLDEN, "inputs", "sc32_ksamp_path_ldos.in")).read().replace(
-        "K_TYPE = 1", "K_TYPE = 4"))
+        "K_TYPE = 1", "K_TYPE = 5"))
+    with pytest.raises(L.Leo2dError, match="K_TYPE = 5"):
+        L.run_input(p, tmp_path)
+    # K_TYPE 4 samples a bilayer (M, N) cell's zone
+    p.write_text(open(os.path.join(GOLDEN, "inputs", "sc32_ksamp_path_ldos.in")).read().replace(
+        "K_TYPE = 1", "K_TYPE = 4").replace("SUPERCELL_M_N = 3 2", "SUPERCELL_M_N = 0 0"))
     with pytest.raises(L.Leo2dError, match="K_TYPE = 4"):
         L.run_input(p, tmp_path)

@@ -42,13 +42,17 @@ def _kpts_text(ks):
 def test_k_lists_match_the_reference_kpts_files():
     """The k points the reference's own main() wrote for a K_TYPE = 0 grid (2 x 2),
     a K_TYPE = 1 path (6 points, every leg of K -> Gamma -> M -> K), a K_TYPE = 2
-    path (5 points of sheet 0's zone, Gamma -> M -> K -> Gamma) and a K_TYPE = 3
-    path (7 points, Gamma -> M -> K -> K' -> Gamma)."""
+    path (5 points of sheet 0's zone, Gamma -> M -> K -> Gamma), a K_TYPE = 3
+    path (7 points, Gamma -> M -> K -> K' -> Gamma) and K_TYPE = 4 paths
+    (Gamma -> K -> M -> Gamma, 3 and 2 points a leg, on (3,2) and (2,3) cells:
+    both orderings of the cell's basis)."""
     from tests._golden import e2e_text, parse_in
     for name, ks in (("sc32_ksamp_ldos", lambda g: L.k_grid(g, 2, 2)),
                      ("sc32_ksamp_path_ldos", lambda g: L.k_path(g, 6)),
                      ("sc32_ksamp_mono_ldos", lambda g: L.k_path(g, 5, k_type=2)),
-                     ("sc32_ksamp_loop_ldos", lambda g: L.k_path(g, 7, k_type=3))):
+                     ("sc32_ksamp_loop_ldos", lambda g: L.k_path(g, 7, k_type=3)),
+                     ("sc32_ksamp_gkm_ldos", lambda g: L.k_path(g, 3, k_type=4)),
+                     ("sc23_ksamp_gkm_ldos", lambda g: L.k_path(g, 2, k_type=4))):
         g, _ = parse_in(name)
         g = oracle.geom_prepare(g)
         assert _kpts_text(ks(g)) == e2e_text(name, ".kpts"), name
@@ -73,3 +77,16 @@ def test_k_path_twisted_zone_needs_two_sheets():
     with pytest.raises(ValueError, match="single layer"):
         L.k_path(g, 4, k_type=1)
     assert L.k_path(g, 4, k_type=2).shape == (4, 2)
+
+
+def test_gkm_path_needs_a_bilayer_mn_cell():
+    """K_TYPE = 4 takes the (M, N) cell of a bilayer; other cells are refused by
+    the helper as by the driver."""
+    g = oracle.geom_prepare(L.make_geom(num_sheets=1, boundary_condition=1, supercell_mn=(4, 5), size=16,
+                                        energy_rescale=13.0))
+    with pytest.raises(ValueError, match="bilayer SUPERCELL_M_N"):
+        L.k_path(g, 4, k_type=4)
+    g = oracle.geom_prepare(L.make_geom(boundary_condition=1, supercell_mn=(4, 5), size=16, energy_rescale=13.0))
+    ks = L.k_path(g, 4, k_type=4)
+    assert ks.shape == (12, 2)
+    np.testing.assert_array_equal(ks[0], [0.0, 0.0])

@@ -94,3 +94,17 @@ def test_model_and_kpm_keys(tmp_path):
     assert st == 0 and ints[7] == 0
     assert g.model == _abi.MODEL_SIMPLE and g.max_R[0] == 25.5 and g.max_R[1] == 25.5
     assert g.angles[1] == (2 * np.pi * 1.05) / 360.0 and g.heights[1] == 3.35
+
+
+def test_k_lists_outside_the_build_are_refused_on_the_host(tmp_path):
+    """K_TYPE = 5 (the trilayer's Dirac points) is refused by name, and K_TYPE = 4
+    away from a bilayer (M, N) cell too; both before any device is touched."""
+    import leo2d_gb300 as L
+    src = open(os.path.join(GOLDEN, "inputs", "sc32_ksamp_gkm_ldos.in")).read()
+    p = tmp_path / "k5.in"
+    p.write_text(src.replace("K_TYPE = 4", "K_TYPE = 5"))
+    with pytest.raises(L.Leo2dError, match="K_TYPE = 5"):
+        L.run_input(p, tmp_path)
+    p.write_text(src.replace("SUPERCELL_M_N = 3 2", "SUPERCELL_M_N = 0 0"))
+    with pytest.raises(L.Leo2dError, match="K_TYPE = 4"):
+        L.run_input(p, tmp_path)
