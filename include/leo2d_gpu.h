@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define LEO2D_ABI_VERSION 1
+#define LEO2D_ABI_VERSION 2
 #define LEO2D_MAX_SHEETS 8
 
 typedef enum {
@@ -99,6 +99,14 @@ typedef struct {
    * (H_ii + energy_shift + z_i E) / energy_rescale, the on-site term of
    * Locality::onSiteE (src/locality.cpp:7163-7166, 4166-4172). 0 = off. */
   double e_field;
+  /* TRILAYER_SUPERCELL = 1 (Job_params "supercell_type" 3, three sheets): the
+   * (M, N) cell of a helical trilayer, Locality::setupSupercell's type 3
+   * (src/locality.cpp:401-532). Sheets 0, 1, 2 at -theta, 0, theta with
+   * strides (N^2 - M^2, M^2 + 2MN; -(M^2 + 2MN), N^2 + 2MN),
+   * (0, M^2 + MN + N^2; -(M^2 + MN + N^2), M^2 + MN + N^2) and
+   * (M^2 - N^2, N^2 + 2MN; -(N^2 + 2MN), M^2 + 2MN); the job's cell is sheet
+   * 0's. 0 = the bilayer rule of SUPERCELL_M_N (type 1). */
+  int32_t trilayer_supercell;
 } leo2d_geom;
 
 typedef struct leo2d_ctx leo2d_ctx;

@@ -37,7 +37,7 @@ class Geom(ctypes.Structure):
         ("lattice", c_dbl * 2 * 2 * MAX_SHEETS), ("sheet_supercell", c_dbl * 2 * 2 * MAX_SHEETS),
         ("sheet_sc_stride", c_i32 * 2 * 2 * MAX_SHEETS), ("supercell", c_dbl * 2 * 2),
         ("prepared", c_i32), ("b_field", c_dbl), ("k_vec", c_dbl * 2),
-        ("shifts", c_dbl * 2 * MAX_SHEETS), ("e_field", c_dbl),
+        ("shifts", c_dbl * 2 * MAX_SHEETS), ("e_field", c_dbl), ("trilayer_supercell", c_i32),
     ]
 
 
@@ -53,7 +53,7 @@ class KpmCfg(ctypes.Structure):
 def make_geom(num_sheets=2, model=MODEL_REF, boundary_condition=0, size=50, max_R=None,
               heights=(0.0, 3.35), angles_deg=(0.0, 0.0), energy_rescale=20.0,
               energy_shift=0.0, supercell_mn=None, sc_search_size=1, b_field=0.0, k_vec=None,
-              shifts=None, e_field=0.0):
+              shifts=None, e_field=0.0, trilayer_supercell=0):
     """A Geom filled the way main.cpp fills Sdata for MAXSIZE=size, MINSIZE=-size.
 
     Angles are given in degrees and converted as main.cpp:345-351 does.
@@ -80,6 +80,7 @@ def make_geom(num_sheets=2, model=MODEL_REF, boundary_condition=0, size=50, max_
     if k_vec is not None:
         g.k_vec[0], g.k_vec[1] = float(k_vec[0]), float(k_vec[1])
     g.e_field = float(e_field)
+    g.trilayer_supercell = int(trilayer_supercell)
     if shifts is not None:  # {sheet: (s1, s2)}: fractions of the sheet's lattice vectors
         for s, (a, b) in dict(shifts).items():
             g.shifts[s][0], g.shifts[s][1] = float(a), float(b)

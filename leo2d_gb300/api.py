@@ -213,10 +213,14 @@ def k_path(geom, n, k_type=1):
     turned by 30 degrees over cos 30. Returns [n][2].
 
     k_type 4 (locality.cpp:1990-2159): n points on each leg of Gamma -> K -> M ->
-    Gamma in the zone of a bilayer SUPERCELL_M_N cell, walked as the driver
-    walks it (k_path_gkm). Returns [3 n][2]."""
+    Gamma in the zone of a bilayer (M, N) cell, walked as the driver walks it
+    (k_path_gkm). Returns [3 n][2].
+    k_type 5 (locality.cpp:2161-2250): the trilayer's K points joined
+    (k_path_dirac). Returns [2 n + 1][2]."""
     if k_type == 4:
         return k_path_gkm(geom, n)
+    if k_type == 5:
+        return k_path_dirac(geom, n)
     gm = [0.0, 0.0]
     if k_type == 1 and geom.num_sheets < 2:  # locality.cpp:1661-1663, as the driver
         raise ValueError("cannot use K_TYPE == 1 (twisted BZ) for a single layer")
@@ -243,7 +247,7 @@ def k_path(geom, n, k_type=1):
                   np.sin(-np.pi / 3) * kk[0] + np.cos(-np.pi / 3) * kk[1]]
             pts = [gm, mm, kk, k2, gm]
     else:
-        raise ValueError("k_type must be 1, 2, 3 or 4")
+        raise ValueError("k_type must be 1 to 5")
     legs = len(pts) - 1
     out = []
     for i in range(n):
@@ -255,6 +259,16 @@ def k_path(geom, n, k_type=1):
     return np.array(out)
 
 
+def _sheet_reciprocal(geom, s):
+    """b1, b2 of sheet s's lattice turned by its angle (Locality::getReciprocal(int),
+    locality.cpp:7168-7213)."""
+    import math
+    th = geom.angles[s]
+    lat = geom.lattice[s]
+    return _reciprocal([[lat[i][0] * math.cos(th) - lat[i][1] * math.sin(th),
+                         lat[i][0] * math.sin(th) + lat[i][1] * math.cos(th)] for i in range(2)])
+
+
 def k_path_gkm(geom, nk):
     """K_TYPE 4's Bloch vectors (locality.cpp:1990-2159): nk points on each leg of
     Gamma -> K -> M -> Gamma of the zone of the (M, N) supercell of a bilayer,
@@ -262,8 +276,12 @@ def k_path_gkm(geom, nk):
     vectors; M = (b1 + b2) / 2 and K = b2 turned by +30 degrees over sqrt 3. Each
     leg runs by the reference's slope and intercept, in its order of operations
     (the second leg adds no intercept; the third runs along y from M when M's
-    coordinates are equal). Returns [3 nk][2]."""
+    coordinates are equal). The trilayer's cell [0 q; -q q] puts M on the y axis,
+    where the reference's third leg divides by zero (NaN k points): refused.
+    Returns [3 nk][2]."""
     import math
+    if geom.num_sheets == 3:
+        raise ValueError("K_TYPE = 4 on a trilayer: the reference's M -> Gamma leg divides by zero there")
     if geom.num_sheets != 2 or geom.boundary_condition != 1 or (geom.supercell_m == 0 and geom.supercell_n == 0):
         raise ValueError("K_TYPE = 4 samples the zone of a bilayer SUPERCELL_M_N supercell")
     M, N = geom.supercell_m, geom.supercell_n
@@ -299,6 +317,35 @@ def k_path_gkm(geom, nk):
                 out.append([m[0], m[1] + n3 * (gm[1] - m[1]) / nk])
             else:
                 out.append([m[0] + n3 * l3 / nk, m[1] + s3 * n3 * l3 / nk + c3])
+    return np.array(out)
+
+
+def k_path_dirac(geom, nk):
+    """K_TYPE 5's Bloch vectors (locality.cpp:2161-2250): the K points of the three
+    sheets of a trilayer supercell, K_s = (2 b_s1 + b_s2) / 3 of sheet s's turned
+    lattice, joined: nk points from K_0 towards K_1, nk from K_1 towards K_2, each
+    on its line's slope and intercept, then K_2. Returns [2 nk + 1][2]."""
+    if geom.num_sheets != 3 or geom.boundary_condition != 1:
+        raise ValueError("K_TYPE = 5 joins the K points of a trilayer supercell's three sheets")
+    kl = []
+    for s in range(3):
+        b = _sheet_reciprocal(geom, s)
+        kl.append([1.0 / 3.0 * (2.0 * b[0][i] + b[1][i]) for i in range(2)])
+    s1 = (kl[1][1] - kl[0][1]) / (kl[1][0] - kl[0][0])
+    s2 = (kl[2][1] - kl[1][1]) / (kl[2][0] - kl[1][0])
+    m1 = kl[1][1] - s1 * kl[1][0]
+    m2 = kl[2][1] - s2 * kl[2][0]
+    l1, l2 = kl[1][0] - kl[0][0], kl[2][0] - kl[1][0]
+    out = []
+    for i in range(2 * nk + 1):
+        if i < nk:
+            kx = kl[0][0] + i * l1 / nk
+            out.append([kx, s1 * kx + m1])
+        elif i < 2 * nk:
+            kx = kl[1][0] + (i - nk) * l2 / nk
+            out.append([kx, s2 * kx + m2])
+        else:
+            out.append([kl[2][0], kl[2][1]])
     return np.array(out)
 
 

@@ -4,8 +4,10 @@
 // periodic jobs, Locality::setupSupercell type 1 (src/locality.cpp:153-293):
 // twist theta = acos((N^2 + 4NM + M^2) / (2 (N^2 + NM + M^2))) (negated when
 // M < N), sheet 0 at angle 0 with supercell strides (N, M; -M, M+N), sheet 1 at
-// theta with (M, N; -N, M+N), supercell vectors = strides x lattice. Compiled
-// with -ffp-contract=off so every value equals the reference's.
+// theta with (M, N; -N, M+N), supercell vectors = strides x lattice; or type 3
+// for a helical trilayer (src/locality.cpp:401-532): sheets at -theta, 0, theta
+// with the strides of leo2d_geom.trilayer_supercell. Compiled with
+// -ffp-contract=off so every value equals the reference's.
 #include <cmath>
 #include <cstring>
 
@@ -31,13 +33,27 @@ extern "C" leo2d_status leo2d_geom_prepare(leo2d_geom* g) {
   if (g->boundary_condition == 1) {
     const int M = g->supercell_m, N = g->supercell_n;
     if (M < 0 || N < 0 || (M == 0 && N == 0)) return LEO2D_ERR_BAD_ARG;
+    const bool tri = g->trilayer_supercell != 0;
+    if (tri && g->num_sheets != 3) return LEO2D_ERR_BAD_ARG;
     double theta = std::acos((N * N + 4 * N * M + M * M) / (2.0 * (N * N + N * M + M * M)));
     if (M < N) theta = -theta;
     const double h_fac = 1.0;
     for (int i = 0; i < g->num_sheets; ++i) {
-      const int group = i == 0 ? 0 : 1;
+      const int group = tri ? i : (i == 0 ? 0 : 1);
       int A1_a1, A1_a2, A2_a1, A2_a2;
-      if (group == 0) {
+      if (tri) {
+        const int q = M * M + M * N + N * N;
+        if (group == 0) {
+          g->angles[i] = -theta;
+          A1_a1 = N * N - M * M; A1_a2 = M * M + 2 * M * N; A2_a1 = -(M * M + 2 * M * N); A2_a2 = N * N + 2 * M * N;
+        } else if (group == 1) {
+          g->angles[i] = 0;
+          A1_a1 = 0; A1_a2 = q; A2_a1 = -q; A2_a2 = q;
+        } else {
+          g->angles[i] = theta;
+          A1_a1 = M * M - N * N; A1_a2 = N * N + 2 * M * N; A2_a1 = -(N * N + 2 * M * N); A2_a2 = M * M + 2 * M * N;
+        }
+      } else if (group == 0) {
         g->angles[i] = 0;
         A1_a1 = N; A1_a2 = M; A2_a1 = -M; A2_a2 = (M + N);
       } else {

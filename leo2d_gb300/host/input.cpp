@@ -43,6 +43,7 @@ bool parse_input(const std::string& path, JobSpec& spec, std::string& err) {
   std::vector<int> mn, mx;  // main.cpp pushes three entries per MINSIZE / MAXSIZE
   double max_R = 0.0;
   int num_sheets = 0, current_sheet = -1;
+  std::vector<int> sc_groups;  // SUPERCELL_GROUPS, 0-based group of each sheet (empty: not given)
   double height = 0.0, angle = 0.0;
   std::vector<double> heights, angles;
   std::vector<int> sheet_min0, sheet_max0;
@@ -82,10 +83,23 @@ bool parse_input(const std::string& path, JobSpec& spec, std::string& err) {
         sheet_max0.assign(num_sheets, 0);
         sheet_R.assign(num_sheets, 0.0);
         sheet_set.assign(num_sheets, false);
-      } else if (key == "SUPERCELL_M_N") {
+      } else if (key == "SUPERCELL_M_N") {  // main.cpp:267-277: also selects supercell type 1
         next();
         g.supercell_m = std::atoi(next().c_str());
         g.supercell_n = std::atoi(next().c_str());
+        g.trilayer_supercell = 0;
+      } else if (key == "SUPERCELL_GROUPS") {
+        // main.cpp:131-155: two groups of sheet numbers, each closed by "/"
+        next();
+        sc_groups.assign(num_sheets, 0);
+        int placed = 0;
+        for (int gc = 0; gc < 2; ++gc)
+          for (std::string t = next(); !t.empty() && t != "/" && placed < num_sheets; t = next(), ++placed) {
+            const int sheet = std::atoi(t.c_str()) - 1;
+            if (sheet >= 0 && sheet < num_sheets) sc_groups[sheet] = gc;
+          }
+      } else if (key == "TRILAYER_SUPERCELL") {  // main.cpp:295-303: 1 selects supercell type 3
+        if (std::atoi(value().c_str()) == 1) g.trilayer_supercell = 1;
       } else if (key == "SUPERCELL_SEARCH_SIZE") {
         g.sc_search_size = std::atoi(value().c_str());
       } else if (key == "START_SHEET") {
@@ -260,8 +274,17 @@ bool parse_input(const std::string& path, JobSpec& spec, std::string& err) {
   if (spec.target_sheets.empty()) spec.target_sheets.push_back(0);
   // a magnetic field: the complex Hamiltonian of generateCpxH (locality.cpp:2906-2909)
   if (spec.use_e == 1) g.e_field = spec.e_field;
+  if (g.boundary_condition == 1 && g.trilayer_supercell && num_sheets != 3)
+    spec.unsupported.push_back("TRILAYER_SUPERCELL = 1 with NUM_SHEETS = " + std::to_string(num_sheets));
+  if (g.boundary_condition == 1 && !g.trilayer_supercell && num_sheets >= 3 && !sc_groups.empty()) {
+    // the (M, N) cell here puts sheet 1 in group 1 and the others in group 2
+    // (setupSupercell reads the groups for three or more sheets, locality.cpp:161-170)
+    bool dflt = sc_groups[0] == 0;
+    for (int s = 1; s < num_sheets; ++s) dflt = dflt && sc_groups[s] == 1;
+    if (!dflt) spec.unsupported.push_back("SUPERCELL_GROUPS other than 1 / 2 .. NUM_SHEETS /");
+  }
   if (spec.k_sampling == 1) {
-    if (spec.k_type < 0 || spec.k_type > 4) spec.unsupported.push_back("K_TYPE = " + std::to_string(spec.k_type));
+    if (spec.k_type < 0 || spec.k_type > 5) spec.unsupported.push_back("K_TYPE = " + std::to_string(spec.k_type));
     if (g.boundary_condition != 1) spec.unsupported.push_back("K_SAMPLING = 1 with BOUNDARY_CONDITION = 0");
     if (spec.observable_type == 1) spec.unsupported.push_back("K_SAMPLING = 1 with OBSERVABLE_TYPE = COND");
   }

@@ -255,9 +255,18 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
   if (spec.k_sampling == 1 && spec.k_type == 4 &&
       (spec.geom.boundary_condition != 1 || spec.geom.num_sheets != 2 ||
        (spec.geom.supercell_m == 0 && spec.geom.supercell_n == 0))) {
-    // locality.cpp:1996-2031: the zone of the (M, N) supercell; the two-sheet
-    // grouping is the one setupSupercell gives a bilayer (locality.cpp:156-160)
-    err = "K_TYPE = 4 samples the zone of a bilayer SUPERCELL_M_N supercell";
+    // locality.cpp:1996-2039: the zone of the bilayer (M, N) supercell. The
+    // trilayer's cell [0 q; -q q] puts M on the y axis, where the reference's
+    // M -> Gamma leg divides by zero: its k points there are NaN.
+    err = spec.geom.num_sheets == 3
+              ? "K_TYPE = 4 on a trilayer: the reference's M -> Gamma leg divides by zero there (NaN k points)"
+              : "K_TYPE = 4 samples the zone of a bilayer SUPERCELL_M_N supercell";
+    return LEO2D_ERR_UNSUPPORTED;
+  }
+  if (spec.k_sampling == 1 && spec.k_type == 5 &&
+      (spec.geom.boundary_condition != 1 || spec.geom.num_sheets != 3)) {
+    // locality.cpp:2161-2182: the K points of the three layers
+    err = "K_TYPE = 5 joins the K points of a trilayer supercell's three sheets";
     return LEO2D_ERR_UNSUPPORTED;
   }
   if (spec.k_sampling == 1 && (spec.num_k1 < 1 || (spec.k_type == 0 && spec.num_k2 < 1))) {
@@ -364,6 +373,17 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
         b[1][k] = 2 * M_PI * cross(a[2], a[0], k) / den2;
       }
     };
+    // Locality::getReciprocal(int) (locality.cpp:7168-7213): sheet s's lattice
+    // turned by its angle
+    auto sheet_reciprocal = [&](int s, double (&bs)[2][2]) {
+      double as[2][2];
+      const double th = g0.angles[s];
+      for (int i = 0; i < 2; ++i) {
+        as[i][0] = g0.lattice[s][i][0] * std::cos(th) - g0.lattice[s][i][1] * std::sin(th);
+        as[i][1] = g0.lattice[s][i][0] * std::sin(th) + g0.lattice[s][i][1] * std::cos(th);
+      }
+      reciprocal(as, bs);
+    };
     double b[2][2];
     reciprocal(g0.supercell, b);
     std::vector<std::vector<double>> shift_jobs = jobs;
@@ -424,6 +444,40 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
           jobs.push_back(sj);
           kjobs.push_back({kx, ky});
         }
+    } else if (spec.k_type == 5) {
+      // K_TYPE 5 (locality.cpp:2161-2250): the path through the K points of the
+      // three layers, K_s = (2 b_s1 + b_s2) / 3 with b_s the reciprocal vectors
+      // of sheet s's lattice turned by its angle: NUM_K1 points from K_0 to K_1,
+      // NUM_K1 from K_1 to K_2 (each on its line's slope and intercept), then K_2.
+      double kl[3][2];
+      for (int s3 = 0; s3 < 3; ++s3) {
+        double bs[2][2];
+        sheet_reciprocal(s3, bs);
+        for (int i = 0; i < 2; ++i) kl[s3][i] = 1.0 / 3.0 * (2.0 * bs[0][i] + bs[1][i]);
+      }
+      const double s1 = (kl[1][1] - kl[0][1]) / (kl[1][0] - kl[0][0]);
+      const double s2 = (kl[2][1] - kl[1][1]) / (kl[2][0] - kl[1][0]);
+      const double m1 = kl[1][1] - s1 * kl[1][0];
+      const double m2 = kl[2][1] - s2 * kl[2][0];
+      const double l1 = kl[1][0] - kl[0][0], l2 = kl[2][0] - kl[1][0];
+      const int nk = spec.num_k1, last = 2 * nk;
+      for (const auto& sj : shift_jobs)
+        for (int i = 0; i < last + 1; ++i) {
+          double kx, ky;
+          if (i < nk) {
+            kx = kl[0][0] + i * l1 / nk;
+            ky = s1 * kx + m1;
+          } else if (i < last) {
+            const int n2 = i - nk;
+            kx = kl[1][0] + n2 * l2 / nk;
+            ky = s2 * kx + m2;
+          } else {
+            kx = kl[2][0];
+            ky = kl[2][1];
+          }
+          jobs.push_back(sj);
+          kjobs.push_back({kx, ky});
+        }
     } else if (spec.k_type >= 1) {
       // k paths (locality.cpp:1655-1990): each job at NUM_K1 points of a path through
       // the corners P_0 .. P_L; point i sits at c = L i / NUM_K1 and on leg j = the
@@ -439,13 +493,8 @@ leo2d_status run_job(const JobSpec& spec, const std::string& out_dir, int device
       const Pt gm = {0.0, 0.0};
       std::vector<Pt> pts;
       if (spec.k_type == 2) {
-        double a0[2][2], b1[2][2];
-        const double th = g0.angles[0];
-        for (int i = 0; i < 2; ++i) {
-          a0[i][0] = g0.lattice[0][i][0] * std::cos(th) - g0.lattice[0][i][1] * std::sin(th);
-          a0[i][1] = g0.lattice[0][i][0] * std::sin(th) + g0.lattice[0][i][1] * std::cos(th);
-        }
-        reciprocal(a0, b1);
+        double b1[2][2];
+        sheet_reciprocal(0, b1);
         const double h = (M_PI / 3.0) / 2.0;
         const Pt mm = {b1[0][0] / 2.0, b1[0][1] / 2.0};
         const Pt kk = {(mm[0] * std::cos(h) - mm[1] * std::sin(h)) / std::cos(h),

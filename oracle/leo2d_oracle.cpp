@@ -248,7 +248,8 @@ struct oracle_h {
 
 extern "C" {
 
-// Locality::setupSupercell, type 1 (locality.cpp:153-293) + lattices.
+// Locality::setupSupercell, type 1 (locality.cpp:153-293) and type 3, the
+// helical trilayer (locality.cpp:401-532), + lattices.
 int oracle_geom_prepare(leo2d_geom* g) {
   if (!g || g->num_sheets < 1 || g->num_sheets > LEO2D_MAX_SHEETS) return 1;
   for (int s = 0; s < g->num_sheets; ++s) {
@@ -260,10 +261,34 @@ int oracle_geom_prepare(leo2d_geom* g) {
     double theta = std::acos((N * N + 4 * N * M + M * M) / (2.0 * (N * N + N * M + M * M)));
     if (M < N) theta = -theta;
     double h_fac = 1.0;
+    const int type = g->trilayer_supercell ? 3 : 1;
+    if (type == 3 && g->num_sheets != 3) return 1;
     for (int i = 0; i < g->num_sheets; ++i) {
-      const int group = i < 2 ? i : 1;  // sc_groups defaults to {0, 1} (locality.cpp:172-177)
+      // sc_groups: {0, 1} for a bilayer (locality.cpp:156-160), {0, 1, 2} for
+      // the trilayer (locality.cpp:404-409)
+      const int group = type == 3 ? i : (i < 2 ? i : 1);
       int A1_a1, A1_a2, A2_a1, A2_a2;
-      if (group == 0) {
+      if (type == 3) {
+        if (group == 0) {
+          g->angles[i] = -theta;
+          A1_a1 = std::pow(N, 2) - std::pow(M, 2);
+          A1_a2 = std::pow(M, 2) + 2 * M * N;
+          A2_a1 = -(std::pow(M, 2) + 2 * M * N);
+          A2_a2 = std::pow(N, 2) + 2 * M * N;
+        } else if (group == 1) {
+          g->angles[i] = 0;
+          A1_a1 = 0;
+          A1_a2 = std::pow(M, 2) + (M * N) + std::pow(N, 2);
+          A2_a1 = -(std::pow(N, 2) + (M * N) + std::pow(M, 2));
+          A2_a2 = std::pow(N, 2) + M * N + std::pow(M, 2);
+        } else {
+          g->angles[i] = theta;
+          A1_a1 = std::pow(M, 2) - std::pow(N, 2);
+          A1_a2 = std::pow(N, 2) + 2 * M * N;
+          A2_a1 = -(std::pow(N, 2) + (2 * M * N));
+          A2_a2 = std::pow(M, 2) + (2 * M * N);
+        }
+      } else if (group == 0) {
         g->angles[i] = 0;
         A1_a1 = N; A1_a2 = M; A2_a1 = -M; A2_a2 = (M + N);
       } else {

@@ -136,6 +136,10 @@ static int dump_main(int argc, char** argv) {
         int one = 1;
         opts.setParam("supercell_type", one);
       }
+      if (key == "TRILAYER_SUPERCELL" && std::atoi(val(2).c_str()) == 1) {  // main.cpp:295-303
+        int three = 3;
+        opts.setParam("supercell_type", three);
+      }
       if (key == "START_SHEET") current_sheet = std::atoi(val(1).c_str()) - 1;
       if (key == "END_SHEET") {
         if (current_sheet == std::atoi(val(1).c_str()) - 1) {

@@ -58,6 +58,10 @@ def parse_in(name, folder="inputs"):
                 g.num_sheets = int(v(2))
             elif key == "SUPERCELL_M_N":
                 g.supercell_m, g.supercell_n = int(v(2)), int(v(3))
+                g.trilayer_supercell = 0
+            elif key == "TRILAYER_SUPERCELL":
+                if int(v(2)) == 1:
+                    g.trilayer_supercell = 1
             elif key == "START_SHEET":
                 cur = int(v(1)) - 1
             elif key == "END_SHEET":

@@ -37,7 +37,7 @@ def test_exports_are_c_symbols():
 
 def test_abi_version_and_status_strings(lib):
     L = _abi.load()
-    assert L.leo2d_abi_version() == 1
+    assert L.leo2d_abi_version() == 2
     assert L.leo2d_status_string(0) == b"ok"
     assert b"argument" in L.leo2d_status_string(1)
 

@@ -45,14 +45,16 @@ def test_k_lists_match_the_reference_kpts_files():
     path (5 points of sheet 0's zone, Gamma -> M -> K -> Gamma), a K_TYPE = 3
     path (7 points, Gamma -> M -> K -> K' -> Gamma) and K_TYPE = 4 paths
     (Gamma -> K -> M -> Gamma, 3 and 2 points a leg, on (3,2) and (2,3) cells:
-    both orderings of the cell's basis)."""
+    both orderings of the cell's basis) and a K_TYPE = 5 path (the (2,1) helical
+    trilayer's three K points joined, 2 points a leg)."""
     from tests._golden import e2e_text, parse_in
     for name, ks in (("sc32_ksamp_ldos", lambda g: L.k_grid(g, 2, 2)),
                      ("sc32_ksamp_path_ldos", lambda g: L.k_path(g, 6)),
                      ("sc32_ksamp_mono_ldos", lambda g: L.k_path(g, 5, k_type=2)),
                      ("sc32_ksamp_loop_ldos", lambda g: L.k_path(g, 7, k_type=3)),
                      ("sc32_ksamp_gkm_ldos", lambda g: L.k_path(g, 3, k_type=4)),
-                     ("sc23_ksamp_gkm_ldos", lambda g: L.k_path(g, 2, k_type=4))):
+                     ("sc23_ksamp_gkm_ldos", lambda g: L.k_path(g, 2, k_type=4)),
+                     ("tri21_ksamp_dirac_ldos", lambda g: L.k_path(g, 2, k_type=5))):
         g, _ = parse_in(name)
         g = oracle.geom_prepare(g)
         assert _kpts_text(ks(g)) == e2e_text(name, ".kpts"), name
@@ -80,12 +82,22 @@ def test_k_path_twisted_zone_needs_two_sheets():
 
 
 def test_gkm_path_needs_a_bilayer_mn_cell():
-    """K_TYPE = 4 takes the (M, N) cell of a bilayer; other cells are refused by
-    the helper as by the driver."""
+    """K_TYPE = 4 takes the (M, N) cell of a bilayer, K_TYPE = 5 a trilayer; other
+    cells are refused by the helper as by the driver. On the trilayer's cell the
+    reference's K_TYPE = 4 list ends in NaN points (its M -> Gamma leg divides by
+    zero: M lies on the y axis), which the helper refuses by name."""
     g = oracle.geom_prepare(L.make_geom(num_sheets=1, boundary_condition=1, supercell_mn=(4, 5), size=16,
                                         energy_rescale=13.0))
     with pytest.raises(ValueError, match="bilayer SUPERCELL_M_N"):
         L.k_path(g, 4, k_type=4)
+    with pytest.raises(ValueError, match="trilayer supercell"):
+        L.k_path(g, 4, k_type=5)
+    g = oracle.geom_prepare(L.make_geom(num_sheets=3, boundary_condition=1, supercell_mn=(2, 1), size=20,
+                                        heights=(0.0, 3.35, 6.7), angles_deg=(0, 0, 0), energy_rescale=13.0,
+                                        trilayer_supercell=1))
+    with pytest.raises(ValueError, match="divides by zero"):
+        L.k_path(g, 2, k_type=4)
+    assert L.k_path(g, 2, k_type=5).shape == (5, 2)
     g = oracle.geom_prepare(L.make_geom(boundary_condition=1, supercell_mn=(4, 5), size=16, energy_rescale=13.0))
     ks = L.k_path(g, 4, k_type=4)
     assert ks.shape == (12, 2)

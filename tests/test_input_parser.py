@@ -108,3 +108,16 @@ def test_k_lists_outside_the_build_are_refused_on_the_host(tmp_path):
     p.write_text(src.replace("SUPERCELL_M_N = 3 2", "SUPERCELL_M_N = 0 0"))
     with pytest.raises(L.Leo2dError, match="K_TYPE = 4"):
         L.run_input(p, tmp_path)
+
+
+@pytest.mark.parametrize("name", CASES + BFIELD_CASES)
+def test_prepared_geometry_matches_the_oracle(name):
+    """leo2d_geom_prepare (the library's host code: lattices, supercell strides and
+    angles, the helical trilayer's cell included) gives the oracle's prepared
+    geometry byte for byte on every golden input."""
+    import copy
+    from oracle import oracle
+    g, _ = parse_in(name)
+    ours = copy.copy(g)
+    assert _abi.load().leo2d_geom_prepare(ctypes.byref(ours)) == 0
+    assert bytes(ours) == bytes(oracle.geom_prepare(g))
