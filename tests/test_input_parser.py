@@ -121,3 +121,29 @@ def test_prepared_geometry_matches_the_oracle(name):
     ours = copy.copy(g)
     assert _abi.load().leo2d_geom_prepare(ctypes.byref(ours)) == 0
     assert bytes(ours) == bytes(oracle.geom_prepare(g))
+
+
+def test_trilayer_cell_and_supercell_groups(tmp_path):
+    """TRILAYER_SUPERCELL = 1 selects the helical trilayer cell on three sheets (a
+    later SUPERCELL_M_N selects the bilayer rule again, as main.cpp's order of
+    keys does); elsewhere it is refused by name. SUPERCELL_GROUPS that put sheet
+    1 alone against the rest are the cell built here; other groupings are
+    refused by name."""
+    sheets = "".join(f"START_SHEET {s}\nMATERIAL = Graphene\nHEIGHT = {3.35 * (s - 1)}\nEND_SHEET {s}\n"
+                     for s in (1, 2, 3))
+    head = "MAXSIZE = 20\nMINSIZE = -20\nBOUNDARY_CONDITION = 1\nNUM_SHEETS = 3\n"
+    p = tmp_path / "t.in"
+    p.write_text(head + "SUPERCELL_M_N = 2 1\nTRILAYER_SUPERCELL = 1\n" + sheets + "POLY_ORDER = 32\n")
+    st, g, ints, msg = _parse(p)
+    assert st == 0 and ints[7] == 0 and g.trilayer_supercell == 1, msg
+    p.write_text(head + "TRILAYER_SUPERCELL = 1\nSUPERCELL_M_N = 2 1\n" + sheets + "POLY_ORDER = 32\n")
+    st, g, ints, msg = _parse(p)
+    assert st == 0 and g.trilayer_supercell == 0
+    p.write_text(head.replace("NUM_SHEETS = 3", "NUM_SHEETS = 2") + "SUPERCELL_M_N = 2 1\nTRILAYER_SUPERCELL = 1\n"
+                 + sheets.split("START_SHEET 3")[0] + "POLY_ORDER = 32\n")
+    st, g, ints, msg = _parse(p)
+    assert ints[7] == 1 and "TRILAYER_SUPERCELL" in msg
+    for groups, ok in (("1 / 2 3 /", True), ("1 2 / 3 /", False), ("2 / 1 3 /", False)):
+        p.write_text(head + "SUPERCELL_M_N = 2 1\n" + f"SUPERCELL_GROUPS = {groups}\n" + sheets + "POLY_ORDER = 32\n")
+        st, g, ints, msg = _parse(p)
+        assert st == 0 and (ints[7] == 0) == ok and (ok or "SUPERCELL_GROUPS" in msg), (groups, msg)
