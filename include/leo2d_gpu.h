@@ -81,7 +81,9 @@ typedef struct {
    * Hamiltonian is complex, each entry t e^{i phi} with the Peierls phase
    * phi = 3.14e-5 B (x_col - x_row)(y_row + y_col)/2 of Locality::peierlsPhase
    * (src/locality.cpp:7157-7161), as generateCpxH builds it
-   * (src/locality.cpp:4485-5310). Flakes only (BOUNDARY_CONDITION = 0). */
+   * (src/locality.cpp:4485-5310). On a periodic supercell every image takes the
+   * phase with the row's orbital shifted into that image, as generateCpxH does
+   * (src/locality.cpp:4718-4738); that H~ is not Hermitian in this gauge. */
   double b_field;
   /* Bloch vector (1/A) of a k-sampled job (K_SAMPLING = 1, Job_params "k_vec",
    * locality.cpp:1615-1650): when non-zero the Hamiltonian is complex, each
